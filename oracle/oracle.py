@@ -1,0 +1,164 @@
+"""ctypes front end of the CPU oracle (oracle/tc_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's
+cpu_baseline / --impl reference legs, as the checker.  The product (treecorr_gb300) never
+imports this module.
+
+The oracle restates the reference TreeCorr algorithm for the 2-point hot path; its parity
+with the reference C++ is pinned by the fixtures in tests/golden/.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_ROOT = os.path.dirname(_HERE)
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+
+DTYPES = {"N": 0, "K": 1, "G": 2}
+COORDS = {"flat": 1, "3d": 2, "spherical": 3}
+METRICS = {"Euclidean": 1, "Arc": 4}
+SPLITS = {"middle": 0, "median": 1, "mean": 2}
+
+_lib = None
+
+
+def build():
+    """Compile the oracle with its Makefile (seconds)."""
+    subprocess.check_call(["make", "-s", "-f", os.path.join("oracle", "Makefile")], cwd=_ROOT)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            build()
+        L = ctypes.CDLL(_LIB_PATH)
+        dp = ctypes.POINTER(ctypes.c_double)
+        L.orc_field_build.restype = ctypes.c_void_p
+        L.orc_field_build.argtypes = [ctypes.c_int, ctypes.c_int] + [dp] * 7 + [
+            ctypes.c_long, ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+            ctypes.c_int, ctypes.c_int]
+        L.orc_field_free.argtypes = [ctypes.c_void_p]
+        L.orc_field_ntop.restype = ctypes.c_long
+        L.orc_field_ntop.argtypes = [ctypes.c_void_p]
+        L.orc_field_center.argtypes = [ctypes.c_void_p, dp]
+        L.orc_field_dump.restype = ctypes.c_long
+        L.orc_field_dump.argtypes = [ctypes.c_void_p, dp, ctypes.POINTER(ctypes.c_float),
+                                     ctypes.POINTER(ctypes.c_long),
+                                     ctypes.POINTER(ctypes.c_int), ctypes.c_long]
+        L.orc_field_order.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_long)]
+        L.orc_corr2_process.restype = ctypes.c_int
+        L.orc_corr2_process.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int] + [dp] * 8
+        L.orc_corr2_process_rows.restype = ctypes.c_int
+        L.orc_corr2_process_rows.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                             ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                             ctypes.c_void_p, ctypes.c_long, ctypes.c_long,
+                                             ctypes.c_int] + [dp] * 8
+        L.orc_max_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class OracleField:
+    """A field built by the oracle; mirrors the arguments of _treecorr.{N,K,G}Field*."""
+
+    def __init__(self, dtype, coords, x, y, z=None, d1=None, d2=None, w=None, wpos=None,
+                 min_size=0.0, max_size=np.inf, split_method="mean", brute=False,
+                 min_top=3, max_top=10):
+        L = lib()
+        self._keep = [np.ascontiguousarray(a, dtype=float) if a is not None else None
+                      for a in (x, y, z, d1, d2, w, wpos)]
+        x, y, z, d1, d2, w, wpos = self._keep
+        self.n = len(x)
+        self.coords = coords
+        self.h = L.orc_field_build(DTYPES[dtype], COORDS[coords], _p(x), _p(y), _p(z),
+                                   _p(d1), _p(d2), _p(w), _p(wpos), self.n,
+                                   float(min_size), float(max_size), SPLITS[split_method],
+                                   int(bool(brute)), int(min_top), int(max_top))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_field_free(self.h)
+            self.h = None
+
+    def ntop(self):
+        return lib().orc_field_ntop(self.h)
+
+    def center(self):
+        out = np.zeros(4)
+        lib().orc_field_center(self.h, _p(out))
+        return out
+
+    def dump(self):
+        """Canonical depth-first dump: dict of arrays (x,y,z,size,w,d1,d2,n,start,depth)."""
+        L = lib()
+        cap = 2 * self.n + 2
+        xyz = np.zeros((cap, 3))
+        swd = np.zeros((cap, 4), dtype=np.float32)
+        ns = np.zeros((cap, 2), dtype=np.int64)
+        depth = np.zeros(cap, dtype=np.int32)
+        cnt = L.orc_field_dump(self.h, _p(xyz), swd.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                               ns.ctypes.data_as(ctypes.POINTER(ctypes.c_long)),
+                               depth.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), cap)
+        return dict(x=xyz[:cnt, 0], y=xyz[:cnt, 1], z=xyz[:cnt, 2], size=swd[:cnt, 0],
+                    w=swd[:cnt, 1], d1=swd[:cnt, 2], d2=swd[:cnt, 3], n=ns[:cnt, 0],
+                    start=ns[:cnt, 1], depth=depth[:cnt])
+
+    def order(self):
+        out = np.zeros(self.n, dtype=np.int64)
+        lib().orc_field_order(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_long)))
+        return out
+
+
+def bin_setup(min_sep, max_sep, nbins, bin_slop=None, angle_slop=0.1):
+    """Log binning + slop as the reference's Python layer derives them
+    (treecorr/corr2base.py:420-443, 519-523)."""
+    bin_size = np.log(max_sep / min_sep) / nbins
+    max_good_slop = 0.1 / bin_size
+    if bin_slop is None or bin_slop < 0:
+        bin_slop = min(max_good_slop, 1.0)
+    b = bin_size * bin_slop
+    return dict(min_sep=float(min_sep), max_sep=float(max_sep), nbins=int(nbins),
+                bin_size=float(bin_size), b=float(b), a=float(angle_slop))
+
+
+def minmax_size(metric, bins):
+    """Corr2._get_minmax_size for Log binning (treecorr/corr2base.py:1595-1625)."""
+    if metric == "Euclidean":
+        b1 = min(bins["a"], bins["b"])
+        return bins["min_sep"] * b1 / (2. + 3. * b1), bins["max_sep"] * b1
+    return 0.0, 0.0
+
+
+def process(dtype, metric, bins, f1, f2=None, quick=False, nthreads=0, rows=None):
+    """Run the oracle's 2-point process; returns a dict of the 8 accumulated arrays."""
+    nb = bins["nbins"]
+    out = {k: np.zeros(nb) for k in ("xi0", "xi1", "xi2", "xi3", "meanr", "meanlogr",
+                                      "weight", "npairs")}
+    args = [DTYPES[dtype], METRICS[metric], int(bool(quick)), bins["min_sep"], bins["max_sep"],
+            nb, bins["bin_size"], bins["b"], bins["a"]]
+    ptrs = [_p(out[k]) for k in ("xi0", "xi1", "xi2", "xi3", "meanr", "meanlogr", "weight",
+                                 "npairs")]
+    L = lib()
+    if rows is None:
+        L.orc_corr2_process(*args, f1.h, f2.h if f2 is not None else None, int(nthreads), *ptrs)
+    else:
+        L.orc_corr2_process_rows(*args, f1.h, int(rows[0]), int(rows[1]), int(nthreads), *ptrs)
+    return out
+
+
+def max_threads():
+    return lib().orc_max_threads()

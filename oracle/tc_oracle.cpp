@@ -1,0 +1,705 @@
+// tc_oracle.cpp -- CPU oracle for the TreeCorr 2-point hot path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file restates, in plain C++ with OpenMP, the reference
+// algorithm of TreeCorr (rmjarvis/TreeCorr) for:
+//   * the ball-tree build (Field / Cell),
+//   * the dual-tree 2-point traversal with the bin_slop accept/split rule,
+//   * the per-pair accumulation for NN, KK and GG with Log binning,
+// on Flat, ThreeD and Sphere coordinates with the Euclidean and Arc metrics.
+// It is the checker for the CUDA path (tests/, __graft_entry__.smoke, bench.py's
+// cpu_baseline and --impl reference arm), never part of the product.
+//
+// Each function cites the reference file:line it follows.  The restatement keeps the
+// reference's precision choices (double positions and bin sums; float cell weight,
+// size and payload), its summation order inside a cell, and std::partition /
+// std::nth_element for the split so that cell membership and order match.
+//
+// Parity pin: tests/golden/ holds outputs of the reference C++ itself, built from its own
+// sources by oracle/Makefile.ref and driven by tests/golden/make_golden.py; the CPU
+// tests compare this oracle to those fixtures.
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+enum { FLAT = 1, THREED = 2, SPHERE = 3 };             // include/Position.h:24
+enum { EUCLIDEAN = 1, ARC = 4 };                       // include/Metric.h:29
+enum { MIDDLE = 0, MEDIAN = 1, MEAN = 2, RANDOM = 3 }; // include/Cell.h:26
+enum { DN = 0, DK = 1, DG = 2 };                       // N, K, G payloads
+
+typedef std::complex<double> cd;
+
+struct Pt {
+    double x, y, z;   // position (Sphere: normalised, include/Position.h:235-257)
+    double wpos;      // position weight (src/Field.cpp:146-152)
+    float w;          // weight (include/Cell.h:93)
+    float d1, d2;     // payload: wk (Cell.h:154) or wz (Cell.h:190), w-weighted
+    long index;
+};
+
+struct Node {
+    double x = 0., y = 0., z = 0.;
+    float size = 0.f;  // include/Cell.h:346 (float)
+    float w = 0.f;
+    long n = 0;
+    float d1 = 0.f, d2 = 0.f;
+    int left = -1, right = -1;  // -1 for leaves
+    long start = 0, end = 0;
+};
+
+struct Field {
+    int dtype, coords;
+    double minsize, maxsize;
+    int sm, brute, mintop, maxtop;
+    std::vector<Pt> pts;
+    std::vector<Node> nodes;
+    std::vector<int> tops;
+    double cx, cy, cz, sizesq;   // overall centre and size (src/Field.cpp:198-203)
+    bool built;
+};
+
+inline double sqr(double x) { return x * x; }
+
+// Position<Sphere>::normalize, include/Position.h:258-263.
+inline void normalize3(double& x, double& y, double& z)
+{
+    double n = std::sqrt(x * x + y * y + z * z);
+    if (n == 0.) { x = 1.; y = 0.; z = 0.; }
+    else { x /= n; y /= n; z /= n; }
+}
+
+inline double coord_of(const Pt& p, int split)
+{ return split == 2 ? p.z : split == 1 ? p.y : p.x; }
+
+// BuildCellData, src/Cell.cpp:170-200: wpos-weighted centroid, sum of w.
+void build_cell_data(const Field& f, long start, long end, Node& nd)
+{
+    const std::vector<Pt>& v = f.pts;
+    double wp = v[start].wpos;
+    double px = v[start].x * wp, py = v[start].y * wp, pz = v[start].z * wp;
+    double ww = v[start].w;
+    double sumwp = wp;
+    for (long i = start + 1; i != end; ++i) {
+        wp = v[i].wpos;
+        px += v[i].x * wp; py += v[i].y * wp; pz += v[i].z * wp;
+        sumwp += wp;
+        ww += v[i].w;
+    }
+    nd.w = float(ww);
+    if (sumwp != 0.) {
+        px /= sumwp; py /= sumwp; pz /= sumwp;
+        if (f.coords == SPHERE) normalize3(px, py, pz);
+    } else {
+        px = v[start].x; py = v[start].y; pz = v[start].z;
+    }
+    nd.x = px; nd.y = py; nd.z = pz;
+    nd.n = end - start;
+}
+
+// calculate_expmsialpha<2>, include/ProjectHelper.h:45-47 (safe_norm 25-31).
+inline cd expmsialpha2(const cd& r)
+{
+    double n = std::norm(r);
+    if (!(n > 0.)) n = 1.;
+    return std::conj(r * r) / n;
+}
+
+// finishAverages: SimpleSum (src/Cell.cpp:221-234) for Flat, ParallelTransportSum
+// (src/Cell.cpp:276-321) for ThreeD/Sphere; K is a plain double sum (src/Cell.cpp:208-218).
+void finish_averages(const Field& f, long start, long end, Node& nd)
+{
+    const std::vector<Pt>& v = f.pts;
+    if (f.dtype == DK) {
+        double s = 0.;
+        for (long i = start; i < end; ++i) s += v[i].d1;
+        nd.d1 = float(s); nd.d2 = 0.f;
+    } else if (f.dtype == DG) {
+        cd sum(0.);
+        if (f.coords == FLAT) {
+            for (long i = start; i < end; ++i) sum += cd(v[i].d1, v[i].d2);
+        } else {
+            // Position<Sphere> cen(center): normalises for ThreeD, copies for Sphere.
+            double cx = nd.x, cy = nd.y, cz = nd.z;
+            if (f.coords == THREED) normalize3(cx, cy, cz);
+            double z1 = nd.z;   // center.getZ() on the un-normalised centre
+            for (long i = start; i < end; ++i) {
+                double px = v[i].x, py = v[i].y, pz = v[i].z;
+                if (f.coords == THREED) normalize3(px, py, pz);
+                double z2 = pz;
+                double dsq = sqr(cx - px) + sqr(cy - py) + sqr(cz - pz);
+                cd wz(v[i].d1, v[i].d2);
+                if (dsq < 1.e-12) {
+                    sum += wz;
+                } else {
+                    double cosA = (z1 - z2) + 0.5 * z2 * dsq;
+                    double sinA = cy * px - cx * py;
+                    double cosB = (z2 - z1) + 0.5 * z1 * dsq;
+                    double sinB = sinA;
+                    double cosbeta = -cosA * cosB + sinA * sinB;
+                    double sinbeta = sinA * cosB + cosA * sinB;
+                    sum += wz * expmsialpha2(cd(cosbeta, sinbeta));
+                }
+            }
+        }
+        nd.d1 = float(sum.real()); nd.d2 = float(sum.imag());
+    } else {
+        nd.d1 = nd.d2 = 0.f;
+    }
+}
+
+// CalculateSizeSq, src/Cell.cpp:89-100.
+double calc_sizesq(const Field& f, const Node& nd, long start, long end)
+{
+    double s = 0.;
+    for (long i = start; i < end; ++i) {
+        const Pt& p = f.pts[i];
+        double d = sqr(nd.x - p.x) + sqr(nd.y - p.y);
+        if (f.coords != FLAT) d += sqr(nd.z - p.z);
+        if (d > s) s = d;
+    }
+    return s;
+}
+
+// SplitData + SplitDataCore<Middle/Median/Mean>, src/Cell.cpp:426-554, with
+// Bounds::getSplit (include/Bounds.h:65-66, 133-141).
+long split_data(Field& f, long start, long end, const Node& nd, int sm)
+{
+    std::vector<Pt>& v = f.pts;
+    double xmin = v[start].x, xmax = xmin, ymin = v[start].y, ymax = ymin;
+    double zmin = v[start].z, zmax = zmin;
+    for (long i = start + 1; i < end; ++i) {
+        xmin = std::min(xmin, v[i].x); xmax = std::max(xmax, v[i].x);
+        ymin = std::min(ymin, v[i].y); ymax = std::max(ymax, v[i].y);
+        zmin = std::min(zmin, v[i].z); zmax = std::max(zmax, v[i].z);
+    }
+    int split;
+    if (f.coords == FLAT) {
+        split = (ymax - ymin) > (xmax - xmin) ? 1 : 0;
+    } else {
+        double xr = xmax - xmin, yr = ymax - ymin, zr = zmax - zmin;
+        split = yr > xr ? (zr > yr ? 2 : 1) : (zr > xr ? 2 : 0);
+    }
+    long mid;
+    if (sm == MEDIAN) {
+        mid = (start + end) / 2;
+        std::nth_element(v.begin() + start, v.begin() + mid, v.begin() + end,
+                         [split](const Pt& a, const Pt& b)
+                         { return coord_of(a, split) < coord_of(b, split); });
+        return mid;
+    }
+    double splitvalue;
+    if (sm == MIDDLE) {
+        splitvalue = split == 2 ? (zmax + zmin) / 2. : split == 1 ? (ymax + ymin) / 2.
+                                                                 : (xmax + xmin) / 2.;
+    } else {
+        splitvalue = split == 2 ? nd.z : split == 1 ? nd.y : nd.x;
+    }
+    auto it = std::partition(v.begin() + start, v.begin() + end,
+                             [split, splitvalue](const Pt& p)
+                             { return coord_of(p, split) < splitvalue; });
+    mid = it - v.begin();
+    if (mid == start || mid == end) return split_data(f, start, end, nd, MEDIAN);
+    return mid;
+}
+
+// BuildCell, src/Cell.cpp:556-615.  Nodes are stored depth first from `next`.
+int build_cell(Field& f, double minsizesq, long start, long end, const Node* data,
+               double sizesq, int& next)
+{
+    int id = next++;
+    Node nd;
+    if (end - start == 1) {
+        const Pt& p = f.pts[start];
+        nd.x = p.x; nd.y = p.y; nd.z = p.z; nd.w = p.w; nd.n = 1;
+        nd.d1 = p.d1; nd.d2 = p.d2;
+        nd.size = 0.f; nd.left = nd.right = -1; nd.start = start; nd.end = end;
+        f.nodes[id] = nd;
+        return id;
+    }
+    if (data) {
+        nd = *data;
+    } else {
+        build_cell_data(f, start, end, nd);
+        finish_averages(f, start, end, nd);
+        sizesq = calc_sizesq(f, nd, start, end);
+    }
+    nd.start = start; nd.end = end;
+    if (sizesq > minsizesq) {
+        double size = f.brute ? std::numeric_limits<double>::max() : std::sqrt(sizesq);
+        nd.size = float(size);
+        long mid = split_data(f, start, end, nd, f.sm);
+        nd.left = build_cell(f, minsizesq, start, mid, nullptr, 0., next);
+        nd.right = build_cell(f, minsizesq, mid, end, nullptr, 0., next);
+    } else {
+        nd.size = 0.f;
+        nd.left = nd.right = -1;
+    }
+    f.nodes[id] = nd;
+    return id;
+}
+
+struct TopInfo { Node data; double sizesq; long start, end; };
+
+// SetupTopLevelCells, src/Field.cpp:27-81.
+void setup_top(Field& f, double maxsizesq, long start, long end, int mintop, int maxtop,
+               std::vector<TopInfo>& tops)
+{
+    Node nd;
+    double sizesq;
+    if (end - start == 1) {
+        const Pt& p = f.pts[start];
+        nd.x = p.x; nd.y = p.y; nd.z = p.z; nd.w = p.w; nd.n = 1;
+        nd.d1 = p.d1; nd.d2 = p.d2;
+        sizesq = 0.;
+    } else {
+        build_cell_data(f, start, end, nd);
+        sizesq = calc_sizesq(f, nd, start, end);
+    }
+    if (sizesq == 0 || (sizesq <= maxsizesq && mintop <= 0) || maxtop <= 0) {
+        if (end - start > 1) finish_averages(f, start, end, nd);
+        tops.push_back(TopInfo{nd, sizesq, start, end});
+    } else {
+        long mid = split_data(f, start, end, nd, f.sm);
+        setup_top(f, maxsizesq, start, mid, mintop - 1, maxtop - 1, tops);
+        setup_top(f, maxsizesq, mid, end, mintop - 1, maxtop - 1, tops);
+    }
+}
+
+// Field::DoBuildCells, src/Field.cpp:230-277.
+void build_cells(Field& f)
+{
+    if (f.built) return;
+    f.built = true;
+    long n = (long)f.pts.size();
+    if (n == 0) return;
+    double minsizesq = f.minsize * f.minsize;
+    double maxsizesq = f.maxsize * f.maxsize;
+    std::vector<TopInfo> tops;
+    setup_top(f, maxsizesq, 0, n, f.mintop, f.maxtop, tops);
+    f.nodes.assign(2 * n, Node());
+    f.tops.resize(tops.size());
+    long ntop = (long)tops.size();
+#pragma omp parallel for schedule(dynamic)
+    for (long i = 0; i < ntop; ++i) {
+        int next = int(2 * tops[i].start);
+        f.tops[i] = build_cell(f, minsizesq, tops[i].start, tops[i].end,
+                               (tops[i].end - tops[i].start > 1) ? &tops[i].data : nullptr,
+                               tops[i].sizesq, next);
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// 2-point traversal (src/Corr2.cpp:146-566, include/BinType.h:40-156, include/Split.h:82-101)
+
+struct Accum {
+    int nbins;
+    std::vector<double> xi0, xi1, xi2, xi3, meanr, meanlogr, weight, npairs;
+    explicit Accum(int nb) : nbins(nb), xi0(nb), xi1(nb), xi2(nb), xi3(nb), meanr(nb),
+                             meanlogr(nb), weight(nb), npairs(nb) {}
+};
+
+struct Params {
+    int dtype, coords, metric, quick, nbins;
+    double minsep, maxsep, binsize, b, a;
+    double logminsep, halfminsep, minsepsq, maxsepsq, bsq, asq;
+};
+
+// MetricHelper<Euclidean>::DistSq (include/Metric.h:143-147, 202-207) and
+// MetricHelper<Arc>::DistSq for Sphere (include/Metric.h:668-682).
+inline double dist_sq(const Params& P, const Node& c1, const Node& c2)
+{
+    double dx = c1.x - c2.x, dy = c1.y - c2.y;
+    if (P.coords == FLAT) return dx * dx + dy * dy;
+    double dz = c1.z - c2.z;
+    double dsq = dx * dx + dy * dy + dz * dz;
+    if (P.metric == ARC) {
+        double L = std::sqrt(dsq);
+        double theta = 2. * std::asin(L / 2.);
+        return theta * theta;
+    }
+    return dsq;
+}
+
+// ProjectHelper<Sphere>::calculate_direction, include/ProjectHelper.h:272-345.
+inline cd calc_direction(double x1, double y1, double z1, double x2, double y2, double z2)
+{
+    double dsq = sqr(x1 - x2) + sqr(y1 - y2) + sqr(z1 - z2);
+    double cosA = (z1 - z2) + 0.5 * z2 * dsq;
+    double sinA = y1 * x2 - x1 * y2;
+    return cd(sinA, -cosA);
+}
+
+// Corr2::finishProcess + DirectHelper<0,1,3>, src/Corr2.cpp:394-566.
+void finish_process(const Params& P, const Node& c1, const Node& c2, double r, double logr,
+                    int k, Accum& A)
+{
+    double ww = double(c1.w) * double(c2.w);
+    A.weight[k] += ww;
+    if (!P.quick) {
+        A.npairs[k] += double(c1.n) * double(c2.n);
+        A.meanr[k] += ww * r;
+        A.meanlogr[k] += ww * logr;
+    }
+    if (P.dtype == DK) {
+        A.xi0[k] += double(c1.d1) * double(c2.d1);
+    } else if (P.dtype == DG) {
+        cd g1(c1.d1, c1.d2), g2(c2.d1, c2.d2);
+        if (P.coords == FLAT) {
+            // ProjectHelper<Flat>::Project, include/ProjectHelper.h:126-136.
+            cd r12(c2.x - c1.x, c2.y - c1.y);
+            cd e = expmsialpha2(r12);
+            g1 *= e; g2 *= e;
+        } else {
+            // ProjectHelper<Sphere>::Project(c1,c2,z1,z2), include/ProjectHelper.h:370-388;
+            // ThreeD first normalises both positions (include/ProjectHelper.h:570-584).
+            double x1 = c1.x, y1 = c1.y, z1 = c1.z, x2 = c2.x, y2 = c2.y, z2 = c2.z;
+            if (P.coords == THREED) { normalize3(x1, y1, z1); normalize3(x2, y2, z2); }
+            g2 *= expmsialpha2(calc_direction(x1, y1, z1, x2, y2, z2));
+            g1 *= expmsialpha2(calc_direction(x2, y2, z2, x1, y1, z1));
+        }
+        // both_complex_prod(g2, g1), include/ProjectHelper.h:84-101.
+        double z1rz2r = g2.real() * g1.real();
+        double z1rz2i = g2.real() * g1.imag();
+        double z1iz2r = g2.imag() * g1.real();
+        double z1iz2i = g2.imag() * g1.imag();
+        A.xi2[k] += z1rz2r - z1iz2i;   // xim = g1 g2
+        A.xi3[k] += z1rz2i + z1iz2r;
+        A.xi0[k] += z1rz2r + z1iz2i;   // xip = g1 conj(g2)
+        A.xi1[k] += z1rz2i - z1iz2r;
+    }
+}
+
+// BaseCorr2::directProcess11, src/Corr2.cpp:476-525.
+inline void direct_process(const Params& P, const Node& c1, const Node& c2, double rsq, int k,
+                           double r, double logr, Accum& A)
+{
+    if (k < 0) {
+        r = std::sqrt(rsq);
+        logr = std::log(r);
+        k = int((logr - P.logminsep) / P.binsize);
+    }
+    if (k == P.nbins) --k;
+    if (k < 0 || k >= P.nbins) return;   // Assert() in the reference; never true in range
+    finish_process(P, c1, c2, r, logr, k, A);
+}
+
+// BinTypeHelper<Log>::singleBin, include/BinType.h:93-151.
+inline bool single_bin(const Params& P, double rsq, double s1ps2, int& ik, double& r,
+                       double& logr)
+{
+    if (s1ps2 == 0.) return true;
+    double s1ps2sq = s1ps2 * s1ps2;
+    if (s1ps2sq > P.asq * rsq) return false;
+    if (s1ps2sq <= P.bsq * rsq) return true;
+    if (s1ps2sq > 0.25 * sqr(P.binsize + P.b) * rsq) return false;
+    logr = 0.5 * std::log(rsq);
+    double kk = (logr - P.logminsep) / P.binsize;
+    ik = int(kk);
+    double frackk = kk - ik;
+    double f = std::min(frackk, 1. - frackk);
+    if (s1ps2sq > sqr(f * P.binsize + P.b) * rsq) return false;
+    if (s1ps2sq > sqr(frackk * P.binsize + P.b - s1ps2sq / rsq) * rsq) return false;
+    r = std::sqrt(rsq);
+    return true;
+}
+
+// CalcSplitSq, include/Split.h:82-101.
+inline void calc_split_sq(bool& split1, bool& split2, double s1, double s2, double bsq)
+{
+    const double splitfactorsq = 0.3422;
+    if (s2 > s1) {
+        calc_split_sq(split2, split1, s2, s1, bsq);
+    } else if (s1 > 2. * s2) {
+        split1 = true;
+    } else {
+        split1 = true;
+        split2 = s2 * s2 > splitfactorsq * bsq;
+    }
+}
+
+// BaseCorr2::process11, src/Corr2.cpp:308-389 (Log binning, Euclidean/Arc: no rpar).
+void process11(const Params& P, const Field& f1, const Field& f2, int i1, int i2, Accum& A)
+{
+    const Node& c1 = f1.nodes[i1];
+    const Node& c2 = f2.nodes[i2];
+    if (c1.w == 0.f || c2.w == 0.f) return;
+    double s1 = c1.size, s2 = c2.size;
+    const double rsq = dist_sq(P, c1, c2);
+    const double s1ps2 = s1 + s2;
+    // tooSmallDist / tooLargeDist, include/BinType.h:70-82.
+    if (rsq < P.minsepsq && s1ps2 < P.minsep && rsq < sqr(P.minsep - s1ps2)) return;
+    if (rsq >= P.maxsepsq && rsq >= sqr(P.maxsep + s1ps2)) return;
+    int k = -1;
+    double r = 0., logr = 0.;
+    if (single_bin(P, rsq, s1ps2, k, r, logr)) {
+        if (rsq >= P.minsepsq && rsq < P.maxsepsq)
+            direct_process(P, c1, c2, rsq, k, r, logr, A);
+    } else {
+        bool split1 = false, split2 = false;
+        double bsq_eff = rsq * std::min(P.bsq, P.asq);
+        calc_split_sq(split1, split2, s1, s2, bsq_eff);
+        if (split1 && split2) {
+            process11(P, f1, f2, c1.left, c2.left, A);
+            process11(P, f1, f2, c1.left, c2.right, A);
+            process11(P, f1, f2, c1.right, c2.left, A);
+            process11(P, f1, f2, c1.right, c2.right, A);
+        } else if (split1) {
+            process11(P, f1, f2, c1.left, i2, A);
+            process11(P, f1, f2, c1.right, i2, A);
+        } else {
+            process11(P, f1, f2, i1, c2.left, A);
+            process11(P, f1, f2, i1, c2.right, A);
+        }
+    }
+}
+
+// BaseCorr2::process2, src/Corr2.cpp:290-306.
+void process2(const Params& P, const Field& f, int i, Accum& A)
+{
+    const Node& c = f.nodes[i];
+    if (c.w == 0.f) return;
+    if (c.size <= P.halfminsep) return;
+    process2(P, f, c.left, A);
+    process2(P, f, c.right, A);
+    process11(P, f, f, c.left, c.right, A);
+}
+
+void add_into(const Accum& A, double* xi0, double* xi1, double* xi2, double* xi3,
+              double* meanr, double* meanlogr, double* weight, double* npairs)
+{
+    for (int k = 0; k < A.nbins; ++k) {
+        if (xi0) xi0[k] += A.xi0[k];
+        if (xi1) xi1[k] += A.xi1[k];
+        if (xi2) xi2[k] += A.xi2[k];
+        if (xi3) xi3[k] += A.xi3[k];
+        meanr[k] += A.meanr[k];
+        meanlogr[k] += A.meanlogr[k];
+        weight[k] += A.weight[k];
+        npairs[k] += A.npairs[k];
+    }
+}
+
+Params make_params(int dtype, int coords, int metric, int quick, double minsep, double maxsep,
+                   int nbins, double binsize, double b, double a)
+{
+    Params P;
+    P.dtype = dtype; P.coords = coords; P.metric = metric; P.quick = quick; P.nbins = nbins;
+    P.minsep = minsep; P.maxsep = maxsep; P.binsize = binsize; P.b = b; P.a = a;
+    // BaseCorr2 constructor, src/Corr2.cpp:55-80.
+    P.logminsep = std::log(minsep);
+    P.halfminsep = 0.5 * minsep;
+    P.minsepsq = minsep * minsep;
+    P.maxsepsq = maxsep * maxsep;
+    P.bsq = b * b;
+    P.asq = a * a;
+    return P;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Field::Field, src/Field.cpp:163-204 (copies the inputs; cells are built lazily).
+void* orc_field_build(int dtype, int coords, const double* x, const double* y, const double* z,
+                      const double* d1, const double* d2, const double* w, const double* wpos,
+                      long n, double minsize, double maxsize, int sm, int brute, int mintop,
+                      int maxtop)
+{
+    Field* f = new Field();
+    f->dtype = dtype; f->coords = coords; f->minsize = minsize; f->maxsize = maxsize;
+    f->sm = sm; f->brute = brute; f->mintop = mintop; f->maxtop = maxtop; f->built = false;
+    f->pts.resize(n);
+    for (long i = 0; i < n; ++i) {
+        Pt& p = f->pts[i];
+        p.x = x[i]; p.y = y[i]; p.z = (z && coords != FLAT) ? z[i] : 0.;
+        if (coords == SPHERE) normalize3(p.x, p.y, p.z);
+        p.wpos = wpos ? wpos[i] : w[i];
+        p.w = float(w[i]);
+        p.index = i;
+        if (dtype == DK) { p.d1 = float(w[i] * d1[i]); p.d2 = 0.f; }
+        else if (dtype == DG) { p.d1 = float(w[i] * d1[i]); p.d2 = float(w[i] * d2[i]); }
+        else { p.d1 = p.d2 = 0.f; }
+    }
+    f->cx = f->cy = f->cz = 0.; f->sizesq = 0.;
+    if (n > 0) {
+        Node nd;
+        build_cell_data(*f, 0, n, nd);
+        f->cx = nd.x; f->cy = nd.y; f->cz = nd.z;
+        f->sizesq = calc_sizesq(*f, nd, 0, n);
+    }
+    return f;
+}
+
+void orc_field_free(void* h) { delete static_cast<Field*>(h); }
+
+long orc_field_ntop(void* h)
+{
+    Field* f = static_cast<Field*>(h);
+    build_cells(*f);
+    return (long)f->tops.size();
+}
+
+void orc_field_center(void* h, double* out4)
+{
+    Field* f = static_cast<Field*>(h);
+    out4[0] = f->cx; out4[1] = f->cy; out4[2] = f->cz; out4[3] = std::sqrt(f->sizesq);
+}
+
+// Canonical depth-first dump of the tree (tops in order, then left before right), used to
+// compare cell membership and cell data with the CUDA tree build.
+long orc_field_dump(void* h, double* xyz, float* size_w_d, long* n_start, int* depth,
+                    long cap)
+{
+    Field* f = static_cast<Field*>(h);
+    build_cells(*f);
+    long cnt = 0;
+    std::vector<std::pair<int, int>> stack;
+    for (long t = (long)f->tops.size() - 1; t >= 0; --t) stack.push_back({f->tops[t], 0});
+    while (!stack.empty()) {
+        auto [id, d] = stack.back();
+        stack.pop_back();
+        const Node& nd = f->nodes[id];
+        if (cnt < cap) {
+            xyz[3 * cnt] = nd.x; xyz[3 * cnt + 1] = nd.y; xyz[3 * cnt + 2] = nd.z;
+            size_w_d[4 * cnt] = nd.size; size_w_d[4 * cnt + 1] = nd.w;
+            size_w_d[4 * cnt + 2] = nd.d1; size_w_d[4 * cnt + 3] = nd.d2;
+            n_start[2 * cnt] = nd.n; n_start[2 * cnt + 1] = nd.start;
+            depth[cnt] = d;
+        }
+        ++cnt;
+        if (nd.left >= 0) {
+            stack.push_back({nd.right, d + 1});
+            stack.push_back({nd.left, d + 1});
+        }
+    }
+    return cnt;
+}
+
+// Original indices of the points in final tree order (list-leaf membership checks).
+void orc_field_order(void* h, long* out)
+{
+    Field* f = static_cast<Field*>(h);
+    build_cells(*f);
+    for (size_t i = 0; i < f->pts.size(); ++i) out[i] = f->pts[i].index;
+}
+
+// BaseCorr2::process (auto, src/Corr2.cpp:146-205; cross, 207-288) for Log binning.
+// Outputs are caller-owned and accumulated into (+=), like the reference.
+int orc_corr2_process(int dtype, int metric, int quick, double minsep, double maxsep, int nbins,
+                      double binsize, double b, double a, void* h1, void* h2, int nthreads,
+                      double* xi0, double* xi1, double* xi2, double* xi3, double* meanr,
+                      double* meanlogr, double* weight, double* npairs)
+{
+    Field* f1 = static_cast<Field*>(h1);
+    Field* f2 = h2 ? static_cast<Field*>(h2) : nullptr;
+    Params P = make_params(dtype, f1->coords, metric, quick, minsep, maxsep, nbins, binsize,
+                           b, a);
+    if (f1->pts.empty() || (f2 && f2->pts.empty())) return 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    if (f2) {
+        // Early exit when the fields cannot overlap, src/Corr2.cpp:213-231.
+        Node a1, a2;
+        a1.x = f1->cx; a1.y = f1->cy; a1.z = f1->cz;
+        a2.x = f2->cx; a2.y = f2->cy; a2.z = f2->cz;
+        double rsq = dist_sq(P, a1, a2);
+        double s1ps2 = std::sqrt(f1->sizesq) + std::sqrt(f2->sizesq);
+        if ((rsq < P.minsepsq && s1ps2 < P.minsep && rsq < sqr(P.minsep - s1ps2)) ||
+            (rsq >= P.maxsepsq && rsq >= sqr(P.maxsep + s1ps2)))
+            return 0;
+    }
+    build_cells(*f1);
+    if (f2) build_cells(*f2);
+    const long n1 = (long)f1->tops.size();
+    const long n2 = f2 ? (long)f2->tops.size() : 0;
+    Accum total(nbins);
+#pragma omp parallel
+    {
+        Accum A(nbins);
+#pragma omp for schedule(dynamic)
+        for (long i = 0; i < n1; ++i) {
+            if (!f2) {
+                process2(P, *f1, f1->tops[i], A);
+                for (long j = i + 1; j < n1; ++j) process11(P, *f1, *f1, f1->tops[i], f1->tops[j], A);
+            } else {
+                for (long j = 0; j < n2; ++j) process11(P, *f1, *f2, f1->tops[i], f2->tops[j], A);
+            }
+        }
+#pragma omp critical
+        {
+            for (int k = 0; k < nbins; ++k) {
+                total.xi0[k] += A.xi0[k]; total.xi1[k] += A.xi1[k];
+                total.xi2[k] += A.xi2[k]; total.xi3[k] += A.xi3[k];
+                total.meanr[k] += A.meanr[k]; total.meanlogr[k] += A.meanlogr[k];
+                total.weight[k] += A.weight[k]; total.npairs[k] += A.npairs[k];
+            }
+        }
+    }
+    add_into(total, xi0, xi1, xi2, xi3, meanr, meanlogr, weight, npairs);
+    return 0;
+}
+
+// Only a bounded share of the top-level work: top rows [row0, row1) of the auto loop.
+// bench.py times this on a stated sample and scales by the sampled share of point pairs.
+int orc_corr2_process_rows(int dtype, int metric, int quick, double minsep, double maxsep,
+                           int nbins, double binsize, double b, double a, void* h1, long row0,
+                           long row1, int nthreads, double* xi0, double* xi1, double* xi2,
+                           double* xi3, double* meanr, double* meanlogr, double* weight,
+                           double* npairs)
+{
+    Field* f1 = static_cast<Field*>(h1);
+    Params P = make_params(dtype, f1->coords, metric, quick, minsep, maxsep, nbins, binsize,
+                           b, a);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    build_cells(*f1);
+    const long n1 = (long)f1->tops.size();
+    if (row1 > n1) row1 = n1;
+    Accum total(nbins);
+#pragma omp parallel
+    {
+        Accum A(nbins);
+#pragma omp for schedule(dynamic)
+        for (long i = row0; i < row1; ++i) {
+            process2(P, *f1, f1->tops[i], A);
+            for (long j = i + 1; j < n1; ++j) process11(P, *f1, *f1, f1->tops[i], f1->tops[j], A);
+        }
+#pragma omp critical
+        {
+            for (int k = 0; k < nbins; ++k) {
+                total.xi0[k] += A.xi0[k]; total.xi1[k] += A.xi1[k];
+                total.xi2[k] += A.xi2[k]; total.xi3[k] += A.xi3[k];
+                total.meanr[k] += A.meanr[k]; total.meanlogr[k] += A.meanlogr[k];
+                total.weight[k] += A.weight[k]; total.npairs[k] += A.npairs[k];
+            }
+        }
+    }
+    add_into(total, xi0, xi1, xi2, xi3, meanr, meanlogr, weight, npairs);
+    return 0;
+}
+
+int orc_max_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+}  // extern "C"

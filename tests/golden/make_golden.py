@@ -1,0 +1,103 @@
+"""Generate the golden fixtures in tests/golden/*.npz from the reference TreeCorr C++.
+
+Run in a container that has the reference sources (it does not run on the GPU machine):
+
+    make -f oracle/Makefile.ref -j8 REF=/root/reference   # builds oracle/_ref/_treecorr*.so
+    python tests/golden/make_golden.py
+
+For every case in tests/golden/cases.py it builds the reference's own native Field and
+Corr objects (the module `_treecorr`, exactly as treecorr/field.py and
+treecorr/corr2base.py drive it) and stores the inputs next to the accumulated outputs.
+The reference is run with one OpenMP thread so its summation order is fixed.
+"""
+import glob
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, HERE)
+from cases import CASES, make_inputs, spec_dict  # noqa: E402
+
+so = glob.glob(os.path.join(ROOT, "oracle", "_ref", "_treecorr*.so"))
+if not so:
+    sys.exit("reference module not built: make -f oracle/Makefile.ref -j8")
+sys.path.insert(0, os.path.dirname(so[0]))
+import _treecorr  # noqa: E402  (the reference's own module)
+
+SPLIT = {"mean": _treecorr.Mean, "median": _treecorr.Median, "middle": _treecorr.Middle}
+METRIC = {"Euclidean": _treecorr.Euclidean, "Arc": _treecorr.Arc}
+COORDS = {"flat": "Flat", "spherical": "Sphere", "3d": "ThreeD"}
+
+
+def build_field(dtype, coords, cat, min_size, max_size, split, brute, min_top, max_top):
+    empty = np.array([])
+    z = cat["z"] if cat["z"] is not None else empty
+    cls = getattr(_treecorr, dtype + "Field" + COORDS[coords])
+    args = [cat["x"], cat["y"], z]
+    if dtype == "K":
+        args += [cat["k"]]
+    elif dtype == "G":
+        args += [cat["g1"], cat["g2"]]
+    args += [cat["w"], empty, min_size, max_size, SPLIT[split], 0, brute, min_top, max_top]
+    return cls(*args)
+
+
+def run_case(name):
+    s = spec_dict(name)
+    cat1, cat2 = make_inputs(name)
+    bin_size = np.log(s["max_sep"] / s["min_sep"]) / s["nbins"]
+    b = bin_size * s["bin_slop"]
+    a = s["angle_slop"]
+    if s["metric"] == "Euclidean":
+        b1 = min(a, b)
+        min_size, max_size = s["min_sep"] * b1 / (2 + 3 * b1), s["max_sep"] * b1
+    else:
+        min_size, max_size = 0.0, 0.0
+    if s["brute"]:
+        min_size = 0.0
+    max_size = max_size if max_size > 0 else 0.0
+    nb = s["nbins"]
+    out = {k: np.zeros(nb) for k in ("xi0", "xi1", "xi2", "xi3", "meanr", "meanlogr",
+                                      "weight", "npairs")}
+    e = np.array([])
+    xi = [out["xi0"], out["xi1"], out["xi2"], out["xi3"]]
+    if s["dtype"] == "N":
+        xi = [e, e, e, e]
+    elif s["dtype"] == "K":
+        xi = [out["xi0"], e, e, e]
+    corr = getattr(_treecorr, s["dtype"] * 2 + "Corr")(
+        _treecorr.Log, s["min_sep"], s["max_sep"], nb, bin_size, b, a,
+        -sys.float_info.max, sys.float_info.max, 0., 0., 0.,
+        xi[0], xi[1], xi[2], xi[3], out["meanr"], out["meanlogr"], out["weight"], out["npairs"])
+    f1 = build_field(s["dtype"], s["coords"], cat1, min_size, max_size, s["split"], s["brute"],
+                     s["min_top"], s["max_top"])
+    if cat2 is None:
+        corr.processAuto(f1, False, False, METRIC[s["metric"]])
+    else:
+        f2 = build_field(s["dtype"], s["coords"], cat2, min_size, max_size, s["split"],
+                         s["brute"], s["min_top"], s["max_top"])
+        corr.processCross(f1, f2, False, False, METRIC[s["metric"]])
+    save = dict(min_size=min_size, max_size=max_size, bin_size=bin_size, b=b, a=a,
+                ntop=f1.getNTopLevel())
+    for k, v in cat1.items():
+        if v is not None:
+            save["c1_" + k] = v
+    if cat2 is not None:
+        for k, v in cat2.items():
+            if v is not None:
+                save["c2_" + k] = v
+    for k, v in out.items():
+        save["ref_" + k] = v
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **save)
+    return out
+
+
+if __name__ == "__main__":
+    _treecorr.SetOMPThreads(1)
+    names = sys.argv[1:] or list(CASES)
+    for name in names:
+        out = run_case(name)
+        print(f"{name:24s} npairs={out['npairs'].sum():.0f} weight={out['weight'].sum():.6g}")
