@@ -1,0 +1,429 @@
+#!/usr/bin/env python
+"""Benchmark of the 2-point hot path: GG on a 10M-point curved-sky catalog.
+
+Workload (the curved-sky precision configuration): N = 10,000,000 points uniform on a
+1000 deg^2 spherical cap; shear = an E-mode Gaussian random field with
+xi+(theta) = 1e-4 (theta/1')^-0.8 drawn on a 4096^2 grid, plus N(0, 0.25) shape noise;
+w ~ U[0.5, 1.5]; GG auto-correlation, Arc metric, 30 Log bins from 1 to 300 arcmin,
+bin_slop 0.1, angle_slop 0.1 (the reference's defaults), split 'mean', min_top 3,
+max_top 10.  The catalog is synthetic (seeded); no public dataset is involved.
+
+One step = one pass of the hot path over the catalog: field construction from the
+catalog columns (normalisation, float payloads), ball-tree build, dual-tree traversal,
+accumulation and the final reduction into the caller's 8 output arrays.
+
+metric: pair evaluations per second -- accepted cell pairs (directProcess11 calls in the
+reference, src/Corr2.cpp:476-525) per second of the whole step.  The GPU path takes the
+reference's accept/split decisions, so its count equals the reference's.
+
+value: inputs resident in HBM (device columns), timed with CUDA events on the library's
+stream.  e2e: the same step through the C ABI with host columns (pinned), host->device
+copies and the device->host read of the results inside the timed region.
+
+The inputs (10M x 6 float64 columns = 480 MB, plus a tree of ~1.3 GB) are larger than L2,
+so no L2 flush is needed between steps.
+
+--impl reference times the reference algorithm's CPU implementation (the oracle port of
+TreeCorr's C++, OpenMP on all host cores) on a bounded sample of the same workload: each
+step processes a fixed set of top-level rows of the auto-correlation loop; value = pair
+evaluations in the sample / time of the sample (the tree build is excluded, which favours
+the CPU).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ARCMIN = np.pi / 180.0 / 60.0
+METRIC = "GG pair-evals/s at N=10M (curved sky, Arc, 30 Log bins 1-300', bin_slop 0.1)"
+UNIT = "pair-evals/s"
+
+
+# ----------------------------------------------------------------------------------------
+# Synthetic catalog
+
+def grf_shear(ngrid, pix_arcmin, rng, amp=1e-4, alpha=0.8):
+    """E-mode shear field on a periodic ngrid^2 grid whose xi+ is amp*(theta/1')^-alpha.
+
+    The 2D Fourier transform of theta^-alpha is 2^(2-alpha) pi Gamma(1-alpha/2) /
+    Gamma(alpha/2) k^(alpha-2), which is the convergence power spectrum P(k) (k in 1/arcmin);
+    gamma(k) = exp(2 i phi_k) kappa(k)."""
+    from math import gamma, pi
+    try:
+        import scipy.fft as sfft
+        fft2 = lambda a: sfft.fft2(a, workers=-1)       # noqa: E731
+        ifft2 = lambda a: sfft.ifft2(a, workers=-1)     # noqa: E731
+    except Exception:                                    # pragma: no cover
+        fft2, ifft2 = np.fft.fft2, np.fft.ifft2
+    k1 = 2 * np.pi * np.fft.fftfreq(ngrid, d=pix_arcmin)
+    kx, ky = np.meshgrid(k1, k1, indexing="xy")
+    ksq = kx * kx + ky * ky
+    ksq[0, 0] = 1.0
+    pk = amp * 2 ** (2 - alpha) * pi * gamma(1 - alpha / 2) / gamma(alpha / 2) * ksq ** ((alpha - 2) / 2)
+    pk[0, 0] = 0.0
+    noise = rng.standard_normal((ngrid, ngrid))
+    w = fft2(noise)
+    w *= np.sqrt(pk) * ((kx * kx - ky * ky) + 2j * kx * ky) / ksq
+    g = ifft2(w) / pix_arcmin
+    return g.real.astype(np.float64), g.imag.astype(np.float64)
+
+
+def curved_sky_catalog(n, seed=20261203, area_deg2=1000.0, ngrid=4096):
+    rng = np.random.default_rng(seed)
+    r = np.arccos(1 - area_deg2 * (np.pi / 180) ** 2 / (2 * np.pi))   # cap radius (rad)
+    u = rng.uniform(np.cos(r), 1.0, n)
+    phi = rng.uniform(0, 2 * np.pi, n)
+    th = np.arccos(u)
+    # Cap around the pole, rotated to (ra, dec) = (180, -30) deg.
+    s = np.sin(th)
+    v = np.stack([s * np.cos(phi), s * np.sin(phi), u])
+    dec0, ra0 = np.radians(-30.0), np.radians(180.0)
+    a = np.pi / 2 - dec0
+    Ry = np.array([[np.cos(a), 0, np.sin(a)], [0, 1, 0], [-np.sin(a), 0, np.cos(a)]])
+    Rz = np.array([[np.cos(ra0), -np.sin(ra0), 0], [np.sin(ra0), np.cos(ra0), 0], [0, 0, 1]])
+    v = Rz @ Ry @ v
+    # Shear: GRF on the azimuthal-equidistant plane of the cap, plus shape noise.
+    half = r / ARCMIN
+    pix = 2 * half / ngrid
+    g1f, g2f = grf_shear(ngrid, pix, rng)
+    px = np.clip(((th / ARCMIN) * np.cos(phi) + half) / pix, 0, ngrid - 1).astype(np.int64)
+    py = np.clip(((th / ARCMIN) * np.sin(phi) + half) / pix, 0, ngrid - 1).astype(np.int64)
+    g1 = g1f[py, px] + rng.normal(0, 0.25, n)
+    g2 = g2f[py, px] + rng.normal(0, 0.25, n)
+    w = rng.uniform(0.5, 1.5, n)
+    return dict(x=np.ascontiguousarray(v[0]), y=np.ascontiguousarray(v[1]),
+                z=np.ascontiguousarray(v[2]), g1=g1, g2=g2, w=w)
+
+
+def binning(bin_slop):
+    min_sep, max_sep, nbins = 1.0 * ARCMIN, 300.0 * ARCMIN, 30
+    bin_size = np.log(max_sep / min_sep) / nbins
+    return dict(min_sep=min_sep, max_sep=max_sep, nbins=nbins, bin_size=bin_size,
+                b=bin_slop * bin_size, a=0.1)
+
+
+# ----------------------------------------------------------------------------------------
+# Clock sampling during the timed region
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                p = [t.strip() for t in line.split(",")]
+                if len(p) >= 9:
+                    rows.append(p)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for nm, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ----------------------------------------------------------------------------------------
+# GPU arm
+
+def run_gpu(args, rank, world):
+    import torch
+    from treecorr_gb300 import _treecorr as T
+    dev = torch.device("cuda", rank % max(torch.cuda.device_count(), 1))
+    torch.cuda.set_device(dev)
+    cat = curved_sky_catalog(args.n, seed=args.seed + rank)
+    bins = binning(args.bin_slop)
+    nb = bins["nbins"]
+    cols = ["x", "y", "z", "g1", "g2", "w"]
+    dcols = {k: torch.from_numpy(cat[k]).to(dev) for k in cols}
+    hcols = {k: torch.from_numpy(cat[k]).pin_memory() for k in cols}
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(T.stream_handle(), device=dev)
+
+    def outputs():
+        return {k: np.zeros(nb) for k in ("xi0", "xi1", "xi2", "xi3", "meanr", "meanlogr",
+                                          "weight", "npairs")}
+
+    def corr_for(out):
+        return T.GGCorr(T.Log, bins["min_sep"], bins["max_sep"], nb, bins["bin_size"],
+                        bins["b"], bins["a"], -sys.float_info.max, sys.float_info.max, 0., 0.,
+                        0., out["xi0"], out["xi1"], out["xi2"], out["xi3"], out["meanr"],
+                        out["meanlogr"], out["weight"], out["npairs"])
+
+    def step_device():
+        out = outputs()
+        f = T.DeviceField(2, T.Sphere, args.n, dcols["x"].data_ptr(), dcols["y"].data_ptr(),
+                          dcols["z"].data_ptr(), dcols["g1"].data_ptr(), dcols["g2"].data_ptr(),
+                          dcols["w"].data_ptr(), 0, 0.0, 0.0, T.Mean, 0, False, 3, 10)
+        c = corr_for(out)
+        c.processAuto(f, False, False, T.Arc)
+        st = c.stats()
+        del f, c
+        return out, st
+
+    def step_host():
+        out = outputs()
+        e = np.array([])
+        f = T.GFieldSphere(hcols["x"].numpy(), hcols["y"].numpy(), hcols["z"].numpy(),
+                           hcols["g1"].numpy(), hcols["g2"].numpy(), hcols["w"].numpy(), e,
+                           0.0, 0.0, T.Mean, 0, False, 3, 10)
+        c = corr_for(out)
+        c.processAuto(f, False, False, T.Arc)
+        st = c.stats()
+        del f, c
+        return out, st
+
+    def timed(fn, k):
+        """k steps bracketed by barrier + synchronize; CUDA events on the library stream."""
+        res = []
+        launches0 = T.launch_count()
+        barrier(world)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            res.append(fn())
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        ms = e0.elapsed_time(e1)
+        return ms, res, T.launch_count() - launches0
+
+    for _ in range(args.warmup):
+        step_device()
+    with ClockSampler(dev.index) as clk:
+        ms, res, launches = timed(step_device, args.steps)
+    clocks = clk.summary()
+    ms = allreduce_max(ms, world)
+    acc_per_step = res[-1][1]["accepted"]
+    value = world * acc_per_step * args.steps / (ms / 1e3)
+    # e2e: host columns through the C ABI.
+    for _ in range(max(1, args.warmup // 2)):
+        step_host()
+    ms_e2e, res_e2e, _ = timed(step_host, args.steps)
+    ms_e2e = allreduce_max(ms_e2e, world)
+    e2e = world * res_e2e[-1][1]["accepted"] * args.steps / (ms_e2e / 1e3)
+    out, st = res[-1]
+    # Roofline of the dominant kernel (the traversal): algorithmic bytes per launch =
+    # cell pairs evaluated x (two 64-byte cell records + the 8-byte work item) / launches,
+    # over the device time of the traversal launches measured by the library with events.
+    tr_ms = st["traverse_ms"]
+    bytes_per_launch = st["cell_pairs"] * (2 * 64 + 8) / max(st["launches"], 1)
+    per_launch_ms = tr_ms / max(st["launches"], 1)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+                "frac": round(achieved / hbm, 4), "traffic": args.traffic,
+                "kernel": "k_traverse",
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
+    h2d = sum(cat[k].nbytes for k in cols)
+    d2h = 8 * nb * 8
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded curved-sky GRF catalog)",
+        "config": {"workload": "GG auto, 10M-point 1000 deg^2 cap, Arc, 30 Log bins 1-300', "
+                               f"bin_slop {args.bin_slop}, angle_slop 0.1",
+                   "n": args.n, "nbins": nb, "bin_slop": args.bin_slop,
+                   "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2 (480 MB columns + 1.3 GB tree); no flush"},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e / args.steps},
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "clocks": clocks,
+        "detail": {"accepted_per_step": acc_per_step, "cell_pairs_per_step": st["cell_pairs"],
+                   "escalated_per_step": st["escalated"],
+                   "traverse_launches_per_step": st["launches"], "build_ms": st["build_ms"],
+                   "traverse_ms": tr_ms, "npairs_total": float(out["npairs"].sum()),
+                   "xip_bin10": float(out["xi0"][10] / out["weight"][10])},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_sample(cat, bins, args, budget_s=args.cpu_budget)
+    return line
+
+
+def cpu_sample(cat, bins, args, budget_s=15.0):
+    """The oracle port of the reference algorithm on the host cores, over top-level rows of
+    the auto loop until about budget_s seconds of traversal have been timed."""
+    from oracle import oracle as O
+    nthreads = os.cpu_count() or 1
+    f = O.OracleField("G", "spherical", cat["x"], cat["y"], cat["z"], cat["g1"], cat["g2"],
+                      cat["w"], None, 0.0, 0.0, "mean", False, 3, 10)
+    t0 = time.perf_counter()
+    ntop = f.ntop()
+    build_s = time.perf_counter() - t0
+    acc, spent, row = 0, 0.0, 0
+    chunk = 1
+    while spent < budget_s and row < ntop:
+        r1 = min(ntop, row + chunk)
+        t0 = time.perf_counter()
+        out = O.process("G", "Arc", bins, f, rows=(row, r1), nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        acc += out["_accepted"]
+        spent += dt
+        row = r1
+        chunk = min(chunk * 2, 64)
+    return {"value": acc / spent if spent > 0 else None, "unit": UNIT, "cores": nthreads,
+            "kind": "port",
+            "sample": f"top-level rows 0..{row} of {ntop} of the same catalog "
+                      f"({acc} pair evaluations, {spent:.1f} s traversal; "
+                      f"tree build {build_s:.1f} s excluded)"}
+
+
+def run_reference(args, rank, world):
+    """The reference algorithm's CPU implementation (oracle port) on a bounded sample."""
+    from oracle import oracle as O
+    if rank != 0:
+        return None
+    cat = curved_sky_catalog(args.n, seed=args.seed)
+    bins = binning(args.bin_slop)
+    nthreads = os.cpu_count() or 1
+    f = O.OracleField("G", "spherical", cat["x"], cat["y"], cat["z"], cat["g1"], cat["g2"],
+                      cat["w"], None, 0.0, 0.0, "mean", False, 3, 10)
+    ntop = f.ntop()
+    # Size the per-step sample: rows until ~args.cpu_budget/steps seconds.
+    target = max(2.0, args.cpu_budget / max(args.steps, 1))
+    t0 = time.perf_counter()
+    rows = 0
+    while rows < ntop and time.perf_counter() - t0 < target:
+        O.process("G", "Arc", bins, f, rows=(rows, rows + 1), nthreads=nthreads)
+        rows += 1
+    rows = max(rows, 1)
+    sample = (0, rows)
+    for _ in range(args.warmup):
+        O.process("G", "Arc", bins, f, rows=sample, nthreads=nthreads)
+    acc, t = 0, 0.0
+    for _ in range(args.steps):
+        t1 = time.perf_counter()
+        out = O.process("G", "Arc", bins, f, rows=sample, nthreads=nthreads)
+        t += time.perf_counter() - t1
+        acc += out["_accepted"]
+    value = acc / t
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded curved-sky GRF catalog)", "impl": "reference",
+            "config": {"workload": "GG auto, 10M-point 1000 deg^2 cap, Arc, 30 Log bins "
+                                   f"1-300', bin_slop {args.bin_slop}, angle_slop 0.1",
+                       "n": args.n, "nbins": 30, "bin_slop": args.bin_slop},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                             "sample": f"top-level rows 0..{rows} of {ntop} per step "
+                                       "(tree build excluded)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+# ----------------------------------------------------------------------------------------
+# Multi-process plumbing (replicas: one independent full workload per GPU)
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(v, world):
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v)])
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    p.add_argument("--n", type=int, default=10_000_000)
+    p.add_argument("--bin-slop", type=float, default=0.1)
+    p.add_argument("--seed", type=int, default=20261203)
+    p.add_argument("--cpu-budget", type=float, default=15.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--traffic", type=float, default=None,
+                   help="DRAM bytes per traversal launch from an ncu capture, if known")
+    args = p.parse_args()
+    rank, world = dist_init()
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    else:
+        line = run_gpu(args, rank, world)
+    if rank == 0 and line is not None:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

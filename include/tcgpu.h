@@ -1,0 +1,178 @@
+/* tcgpu.h -- C ABI of the GB300 (sm_103a) engine for TreeCorr's 2-point correlation
+ * hot path: ball-tree build, dual-tree traversal with the bin_slop accept/split rule, and
+ * the per-pair NN / KK / GG accumulation with Log binning on Flat, ThreeD and Sphere
+ * coordinates (Euclidean and Arc metrics).
+ *
+ * Each entry point replaces one call of the reference's native module `_treecorr`
+ * (TreeCorr's pybind11 layer); the reference file:line is given beside it.  Arguments keep
+ * the reference's names, order and meaning.  Differences at the boundary:
+ *   - plain pointers and sizes instead of numpy buffers; an absent optional array
+ *     (z, wpos, an unused xi) is NULL instead of an empty array;
+ *   - every call returns a status code (TC_OK == 0) instead of printing an Assert and
+ *     continuing; tc_last_error() gives the message of the calling thread's last failure.
+ *
+ * Ownership: a field owns its device copy of the catalog and its tree (tc_field_free).
+ * A corr object aliases the caller's output arrays, exactly like BuildCorr2
+ * (src/Corr2.cpp:842-864): they must outlive it, and every process call only ADDS into
+ * them (clearing them is the caller's job, as in treecorr/corr2base.py:1296-1306).
+ *
+ * All work runs on the current CUDA device, on the library's own stream; calls return
+ * after the results are in the caller's arrays.  One corr object must not be used from
+ * two threads at once (its outputs are aliased), as in the reference.
+ */
+#ifndef TCGPU_H
+#define TCGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define TC_OK               0
+#define TC_ERR_ARG          1   /* invalid argument (sizes, enums, NULL where required) */
+#define TC_ERR_CUDA         2   /* a CUDA runtime call failed */
+#define TC_ERR_UNSUPPORTED  3   /* combination outside the GPU path (e.g. Rperp metric) */
+#define TC_ERR_DEVICE       4   /* a kernel reported an error through its status word */
+#define TC_ERR_NOMEM        5   /* device allocation failed */
+
+/* Enumerations: same numeric values as the reference's enums. */
+/* Coord, include/Position.h:24 */
+#define TC_FLAT    1
+#define TC_THREED  2
+#define TC_SPHERE  3
+/* Metric, include/Metric.h:29 */
+#define TC_EUCLIDEAN 1
+#define TC_RPERP     2
+#define TC_RLENS     3
+#define TC_ARC       4
+#define TC_OLDRPERP  5
+#define TC_PERIODIC  6
+/* SplitMethod, include/Cell.h:26 */
+#define TC_MIDDLE 0
+#define TC_MEDIAN 1
+#define TC_MEAN   2
+#define TC_RANDOM 3
+/* BinType, include/BinType.h:36 */
+#define TC_LOG          0
+#define TC_LINEAR       1
+#define TC_TWOD         2
+#define TC_LOGRUV       3
+#define TC_LOGSAS       4
+#define TC_LOGMULTIPOLE 5
+/* Data kinds of a field (NData, KData, GData in include/Cell.h:37). */
+#define TC_NDATA 0
+#define TC_KDATA 1
+#define TC_GDATA 2
+
+typedef struct tc_field tc_field;
+typedef struct tc_corr2 tc_corr2;
+
+/* Counters of the last process call (no reference counterpart; the reference has none). */
+typedef struct tc_stats {
+    int64_t cell_pairs;      /* cell pairs evaluated by the traversal */
+    int64_t accepted;        /* cell pairs accumulated (directProcess11 calls) */
+    int64_t escalated;       /* decisions re-done in FP64 near a threshold */
+    int64_t launches;        /* traversal kernel launches */
+    double  build_ms;        /* device time of the tree builds done by this call */
+    double  traverse_ms;     /* device time of the traversal + reduction */
+} tc_stats;
+
+/* Field construction: replaces BuildNField / BuildKField / BuildGField for
+ * C = Flat, Sphere, ThreeD (src/Field.cpp:430-546, pybind11 constructors at 686-691),
+ * i.e. Field<D,C>::Field (src/Field.cpp:163-204).  Host arrays of length n:
+ *   x, y: positions; z: NULL for Flat; d1 = k (KData) or g1 (GData), d2 = g2 (GData);
+ *   w: weights; wpos: NULL means "use w" (src/Field.cpp:146-152).
+ * The data are copied to the device here; the tree is built on the first call that needs
+ * it (tc_field_ntop or a process call), like the reference's lazy BuildCells. */
+int tc_field_create(int dkind, int coords,
+                    const double* x, const double* y, const double* z,
+                    const double* d1, const double* d2,
+                    const double* w, const double* wpos, int64_t n,
+                    double min_size, double max_size, int split_method, int64_t seed,
+                    int brute, int min_top, int max_top, tc_field** out);
+
+/* Same as tc_field_create, but the arrays are DEVICE pointers already resident on the
+ * current device (no counterpart in the reference: it is the device-resident form of the
+ * same constructor, for callers whose catalog already lives in HBM). */
+int tc_field_create_device(int dkind, int coords,
+                           const double* x, const double* y, const double* z,
+                           const double* d1, const double* d2,
+                           const double* w, const double* wpos, int64_t n,
+                           double min_size, double max_size, int split_method, int64_t seed,
+                           int brute, int min_top, int max_top, tc_field** out);
+
+/* ~BaseField, src/Field.cpp:279-285. */
+void tc_field_free(tc_field* f);
+
+/* BaseField::getNObj, include/Field.h:52. */
+int64_t tc_field_nobj(const tc_field* f);
+/* BaseField::getSize, include/Field.h:55 (sqrt of the overall size^2). */
+double tc_field_size(const tc_field* f);
+/* BaseField::getNTopLevel, include/Field.h:56: builds the tree if needed; < 0 on error. */
+int64_t tc_field_ntop(tc_field* f);
+/* Overall centre (x,y,z) as in Field::Field, src/Field.cpp:198-203. */
+int tc_field_center(const tc_field* f, double* xyz3);
+
+/* Canonical depth-first dump of the tree (tops in order, left child before right) for
+ * parity tests against the oracle: per cell its centre (xyz, 3 doubles), size, w, and
+ * payload (4 floats), count and first point index in tree order (2 int64), and depth.
+ * Returns the number of cells (writes at most cap of them), < 0 on error.  No reference
+ * counterpart (BaseCell::WriteTree, src/Cell.cpp:703-710, is the closest). */
+int64_t tc_field_dump(tc_field* f, double* xyz, float* size_w_d, int64_t* n_start,
+                      int32_t* depth, int64_t cap);
+
+/* Corr construction: replaces BuildCorr2 (src/Corr2.cpp:842-864) for the NN, KK and GG
+ * classes (pybind11 at src/Corr2.cpp:1177-1199).  d1, d2: TC_NDATA/TC_KDATA/TC_GDATA with
+ * d1 == d2.  xi0..xi3 may be NULL when unused (NN: all; KK: xi1..xi3).  Only
+ * bin_type == TC_LOG is on the GPU path; minrpar/maxrpar/xp/yp/zp are accepted and
+ * must be the defaults (no r_parallel cut, no period). */
+int tc_corr2_create(int d1, int d2, int bin_type, double minsep, double maxsep, int nbins,
+                    double binsize, double b, double a,
+                    double minrpar, double maxrpar, double xp, double yp, double zp,
+                    double* xi0, double* xi1, double* xi2, double* xi3,
+                    double* meanr, double* meanlogr, double* weight, double* npairs,
+                    tc_corr2** out);
+
+void tc_corr2_free(tc_corr2* c);
+
+/* BaseCorr2.processAuto -> ProcessAuto (src/Corr2.cpp:913-929) ->
+ * BaseCorr2::process(field) (src/Corr2.cpp:146-205).  quick == corr_only. */
+int tc_corr2_process_auto(tc_corr2* c, tc_field* f, int dots, int quick, int metric);
+
+/* BaseCorr2.processCross -> ProcessCross (src/Corr2.cpp:978-993) ->
+ * BaseCorr2::process(field1, field2) (src/Corr2.cpp:207-288). */
+int tc_corr2_process_cross(tc_corr2* c, tc_field* f1, tc_field* f2, int dots, int quick,
+                           int metric);
+
+/* BaseCorr2.triviallyZero -> TriviallyZero (src/Corr2.cpp:1107-1128): 1 if no pair of
+ * the two patches (centre + size) can fall in range.  Result in *out. */
+int tc_corr2_trivially_zero(tc_corr2* c, int metric, int coords,
+                            double x1, double y1, double z1, double s1,
+                            double x2, double y2, double z2, double s2, int* out);
+
+/* Counters of the last process call on c. */
+int tc_corr2_stats(const tc_corr2* c, tc_stats* out);
+
+/* SetOMPThreads / GetOMPThreads (src/Corr2.cpp:995-1011).  The GPU path has no host
+ * threads to set: both return 1, which the Python layer accepts. */
+int tc_set_omp_threads(int num_threads);
+int tc_get_omp_threads(void);
+
+/* Message of the last failure on the calling thread ("" if none). */
+const char* tc_last_error(void);
+
+/* Number of CUDA kernels the library has launched since it was loaded (no reference
+ * counterpart; used by benchmarks to report the device work behind a measurement). */
+long long tc_launch_count(void);
+
+/* The CUDA stream (cudaStream_t) on which the library launches its work, created on first
+ * use; callers may record events on it to time the device work (no reference counterpart). */
+void* tc_stream(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TCGPU_H */

@@ -61,6 +61,8 @@ def lib():
                                              ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                              ctypes.c_void_p, ctypes.c_long, ctypes.c_long,
                                              ctypes.c_int] + [dp] * 8
+        L.orc_last_accepted.restype = ctypes.c_longlong
+        L.orc_last_accepted.argtypes = []
         L.orc_max_threads.restype = ctypes.c_int
         _lib = L
     return _lib
@@ -157,6 +159,7 @@ def process(dtype, metric, bins, f1, f2=None, quick=False, nthreads=0, rows=None
         L.orc_corr2_process(*args, f1.h, f2.h if f2 is not None else None, int(nthreads), *ptrs)
     else:
         L.orc_corr2_process_rows(*args, f1.h, int(rows[0]), int(rows[1]), int(nthreads), *ptrs)
+    out["_accepted"] = int(L.orc_last_accepted())
     return out
 
 

@@ -302,6 +302,7 @@ void build_cells(Field& f)
 
 struct Accum {
     int nbins;
+    long long accepted = 0;
     std::vector<double> xi0, xi1, xi2, xi3, meanr, meanlogr, weight, npairs;
     explicit Accum(int nb) : nbins(nb), xi0(nb), xi1(nb), xi2(nb), xi3(nb), meanr(nb),
                              meanlogr(nb), weight(nb), npairs(nb) {}
@@ -389,6 +390,7 @@ inline void direct_process(const Params& P, const Node& c1, const Node& c2, doub
     }
     if (k == P.nbins) --k;
     if (k < 0 || k >= P.nbins) return;   // Assert() in the reference; never true in range
+    ++A.accepted;
     finish_process(P, c1, c2, r, logr, k, A);
 }
 
@@ -504,9 +506,13 @@ Params make_params(int dtype, int coords, int metric, int quick, double minsep, 
     return P;
 }
 
+long long g_last_accepted = 0;   // directProcess11 calls of the last process call
+
 }  // namespace
 
 extern "C" {
+
+long long orc_last_accepted(void) { return g_last_accepted; }
 
 // Field::Field, src/Field.cpp:163-204 (copies the inputs; cells are built lazily).
 void* orc_field_build(int dtype, int coords, const double* x, const double* y, const double* z,
@@ -645,8 +651,10 @@ int orc_corr2_process(int dtype, int metric, int quick, double minsep, double ma
                 total.meanr[k] += A.meanr[k]; total.meanlogr[k] += A.meanlogr[k];
                 total.weight[k] += A.weight[k]; total.npairs[k] += A.npairs[k];
             }
+            total.accepted += A.accepted;
         }
     }
+    g_last_accepted = total.accepted;
     add_into(total, xi0, xi1, xi2, xi3, meanr, meanlogr, weight, npairs);
     return 0;
 }
@@ -687,8 +695,10 @@ int orc_corr2_process_rows(int dtype, int metric, int quick, double minsep, doub
                 total.meanr[k] += A.meanr[k]; total.meanlogr[k] += A.meanlogr[k];
                 total.weight[k] += A.weight[k]; total.npairs[k] += A.npairs[k];
             }
+            total.accepted += A.accepted;
         }
     }
+    g_last_accepted = total.accepted;
     add_into(total, xi0, xi1, xi2, xi3, meanr, meanlogr, weight, npairs);
     return 0;
 }

@@ -1,0 +1,53 @@
+"""CPU tests: the oracle against the reference's golden outputs (the parity pin)."""
+import numpy as np
+import pytest
+
+import helpers as H
+from cases import CASES
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_oracle_matches_reference(name):
+    s, c1, c2, bins, min_size, max_size, ref = H.load_case(name)
+    f1 = H.oracle_field(s["dtype"], s["coords"], c1, min_size, max_size, s["split"], s["brute"],
+                        s["min_top"], s["max_top"])
+    f2 = None
+    if c2 is not None:
+        f2 = H.oracle_field(s["dtype"], s["coords"], c2, min_size, max_size, s["split"],
+                            s["brute"], s["min_top"], s["max_top"])
+    out = H.oracle_process(s["dtype"], s["metric"], bins, f1, f2, nthreads=1)
+    assert np.array_equal(out["npairs"], ref["npairs"])
+    for k in H.OUT_KEYS:
+        r = ref[k]
+        scale = max(np.abs(r).max(), 1e-300)
+        assert np.abs(out[k] - r).max() <= 1e-12 * scale, k
+
+
+def test_oracle_brute_force_flat():
+    """Independent FP64 brute force (the math of tests/test_gg.py:58-77 of the reference):
+    with bin_slop=0 and angle_slop=0 the tree result equals the all-pairs sum."""
+    from cases import flat_catalog
+    rng = np.random.default_rng(5)
+    cat = flat_catalog(rng, 600)
+    nb, lo, hi = 8, 2.0, 30.0
+    bins = dict(min_sep=lo, max_sep=hi, nbins=nb, bin_size=np.log(hi / lo) / nb, b=0.0, a=0.0)
+    f = H.oracle_field("G", "flat", cat, 0.0, 0.0)
+    out = H.oracle_process("G", "Euclidean", bins, f, nthreads=1)
+    x, y, w = cat["x"], cat["y"], cat["w"]
+    g = (cat["g1"] + 1j * cat["g2"]) * w
+    i, j = np.triu_indices(len(x), 1)
+    dx, dy = x[j] - x[i], y[j] - y[i]
+    r = np.hypot(dx, dy)
+    ok = (r >= lo) & (r < hi)
+    i, j, dx, dy, r = i[ok], j[ok], dx[ok], dy[ok], r[ok]
+    k = np.floor(np.log(r / lo) / bins["bin_size"]).astype(int)
+    e = ((dx - 1j * dy) / r) ** 2      # exp(-2i alpha), alpha = angle of p2 - p1
+    g1, g2 = g[i] * e, g[j] * e
+    np_ = np.bincount(k, minlength=nb)
+    xip = np.bincount(k, (g1 * np.conj(g2)).real, minlength=nb)
+    xim = np.bincount(k, (g1 * g2).real, minlength=nb)
+    ww = np.bincount(k, w[i] * w[j], minlength=nb)
+    assert np.array_equal(out["npairs"], np_.astype(float))
+    np.testing.assert_allclose(out["weight"], ww, rtol=1e-6)
+    np.testing.assert_allclose(out["xi0"], xip, rtol=1e-5, atol=1e-6 * ww.max())
+    np.testing.assert_allclose(out["xi2"], xim, rtol=1e-5, atol=1e-6 * ww.max())

@@ -1,0 +1,407 @@
+"""Drop-in for TreeCorr's native module ``_treecorr`` on the 2-point hot path.
+
+Same class names, constructor signatures, methods and enum values as the reference's
+pybind11 module (src/module.cpp:21-26; fields src/Field.cpp:610-703; correlations
+src/Corr2.cpp:1132-1235), implemented over the C ABI of libtcgpu.so (include/tcgpu.h),
+whose kernels run on the GPU.  TreeCorr's own Python layer can use it unchanged:
+
+    import treecorr
+    from treecorr_gb300 import _treecorr as gpu
+    treecorr._treecorr = gpu            # or sys.modules['treecorr._treecorr'] = gpu
+
+What is on the GPU path: N/K/G fields on Flat, Sphere and ThreeD coordinates, NN/KK/GG
+correlations with Log binning, Euclidean (any coords) and Arc (spherical) metrics, split
+methods Mean, Middle and Median.  Every other combination raises NotImplementedError --
+there is no CPU fallback.  Errors from the library raise RuntimeError / ValueError (the
+reference prints an Assert and continues).
+"""
+import ctypes
+import enum
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_lib", "libtcgpu.so")
+
+TC_OK, TC_ERR_ARG, TC_ERR_CUDA, TC_ERR_UNSUPPORTED, TC_ERR_DEVICE, TC_ERR_NOMEM = range(6)
+
+
+class tc_stats(ctypes.Structure):
+    _fields_ = [("cell_pairs", ctypes.c_int64), ("accepted", ctypes.c_int64),
+                ("escalated", ctypes.c_int64), ("launches", ctypes.c_int64),
+                ("build_ms", ctypes.c_double), ("traverse_ms", ctypes.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libtcgpu.so (built by treecorr_gb300.build); raises if it is missing."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            raise ImportError("libtcgpu.so is not built: run `python -m treecorr_gb300.build` "
+                              "(the GPU path has no CPU fallback)")
+        L = ctypes.CDLL(_LIB_PATH)
+        dp = ctypes.POINTER(ctypes.c_double)
+        vp = ctypes.c_void_p
+        i64 = ctypes.c_int64
+        L.tc_field_create.restype = ctypes.c_int
+        L.tc_field_create.argtypes = [ctypes.c_int, ctypes.c_int] + [dp] * 7 + [
+            i64, ctypes.c_double, ctypes.c_double, ctypes.c_int, i64, ctypes.c_int,
+            ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]
+        L.tc_field_create_device.restype = ctypes.c_int
+        L.tc_field_create_device.argtypes = [ctypes.c_int, ctypes.c_int] + [vp] * 7 + [
+            i64, ctypes.c_double, ctypes.c_double, ctypes.c_int, i64, ctypes.c_int,
+            ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp)]
+        L.tc_field_free.restype = None
+        L.tc_field_free.argtypes = [vp]
+        L.tc_field_nobj.restype = i64
+        L.tc_field_nobj.argtypes = [vp]
+        L.tc_field_size.restype = ctypes.c_double
+        L.tc_field_size.argtypes = [vp]
+        L.tc_field_ntop.restype = i64
+        L.tc_field_ntop.argtypes = [vp]
+        L.tc_field_center.restype = ctypes.c_int
+        L.tc_field_center.argtypes = [vp, dp]
+        L.tc_field_dump.restype = i64
+        L.tc_field_dump.argtypes = [vp, dp, ctypes.POINTER(ctypes.c_float),
+                                    ctypes.POINTER(i64), ctypes.POINTER(ctypes.c_int32), i64]
+        L.tc_corr2_create.restype = ctypes.c_int
+        L.tc_corr2_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_double, ctypes.c_double, ctypes.c_int] + \
+            [ctypes.c_double] * 8 + [dp] * 8 + [ctypes.POINTER(vp)]
+        L.tc_corr2_free.restype = None
+        L.tc_corr2_free.argtypes = [vp]
+        L.tc_corr2_process_auto.restype = ctypes.c_int
+        L.tc_corr2_process_auto.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.tc_corr2_process_cross.restype = ctypes.c_int
+        L.tc_corr2_process_cross.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_int,
+                                             ctypes.c_int]
+        L.tc_corr2_trivially_zero.restype = ctypes.c_int
+        L.tc_corr2_trivially_zero.argtypes = [vp, ctypes.c_int, ctypes.c_int] + \
+            [ctypes.c_double] * 8 + [ctypes.POINTER(ctypes.c_int)]
+        L.tc_corr2_stats.restype = ctypes.c_int
+        L.tc_corr2_stats.argtypes = [vp, ctypes.POINTER(tc_stats)]
+        L.tc_set_omp_threads.restype = ctypes.c_int
+        L.tc_set_omp_threads.argtypes = [ctypes.c_int]
+        L.tc_get_omp_threads.restype = ctypes.c_int
+        L.tc_get_omp_threads.argtypes = []
+        L.tc_last_error.restype = ctypes.c_char_p
+        L.tc_last_error.argtypes = []
+        L.tc_launch_count.restype = ctypes.c_longlong
+        L.tc_launch_count.argtypes = []
+        L.tc_stream.restype = ctypes.c_void_p
+        L.tc_stream.argtypes = []
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc == TC_OK:
+        return
+    msg = lib().tc_last_error().decode(errors="replace")
+    if rc == TC_ERR_UNSUPPORTED:
+        raise NotImplementedError(msg)
+    if rc == TC_ERR_ARG:
+        raise ValueError(msg)
+    raise RuntimeError(f"tcgpu error {rc}: {msg}")
+
+
+# ----------------------------------------------------------------------------------------
+# Enums (values as in include/BinType.h:36, Position.h:24, Metric.h:29, Cell.h:26), exported
+# at module level like pybind11's export_values (src/Corr2.cpp:1204-1234).
+
+class BinType(enum.IntEnum):
+    Log = 0
+    Linear = 1
+    TwoD = 2
+    LogRUV = 3
+    LogSAS = 4
+    LogMultipole = 5
+
+
+class Coord(enum.IntEnum):
+    Flat = 1
+    ThreeD = 2
+    Sphere = 3
+
+
+class Metric(enum.IntEnum):
+    Euclidean = 1
+    Rperp = 2
+    Rlens = 3
+    Arc = 4
+    OldRperp = 5
+    Periodic = 6
+
+
+class SplitMethod(enum.IntEnum):
+    Middle = 0
+    Median = 1
+    Mean = 2
+    Random = 3
+
+
+for _e in (BinType, Coord, Metric, SplitMethod):
+    for _m in _e:
+        globals()[_m.name] = _m
+del _e, _m
+
+
+def SetOMPThreads(num_threads):
+    """SetOMPThreads (src/Corr2.cpp:995-1003): the GPU path has no host threads; returns 1."""
+    return lib().tc_set_omp_threads(int(num_threads))
+
+
+def GetOMPThreads():
+    """GetOMPThreads (src/Corr2.cpp:1005-1011); returns 1."""
+    return lib().tc_get_omp_threads()
+
+
+def _arr(a, n=None, name="array"):
+    """Contiguous float64 copy/view, or None for an absent (empty) array."""
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if a.size == 0:
+        return None
+    if n is not None and a.size != n:
+        raise ValueError(f"{name} has size {a.size}, expected {n}")
+    return a
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+# ----------------------------------------------------------------------------------------
+# Fields
+
+class _FieldBase:
+    _dkind = 0
+    _coords = 1
+
+    def _build(self, x, y, z, d1, d2, w, wpos, minsize, maxsize, sm, seed, brute, mintop,
+               maxtop):
+        x = _arr(x, name="x")
+        n = 0 if x is None else x.size
+        y = _arr(y, n, "y")
+        z = _arr(z, n, "z")
+        w = _arr(w, n, "w")
+        wpos = _arr(wpos, n, "wpos")
+        d1 = _arr(d1, n, "d1")
+        d2 = _arr(d2, n, "d2")
+        if self._coords == Coord.Flat:
+            z = None
+        self._keep = (x, y, z, d1, d2, w, wpos)
+        h = ctypes.c_void_p()
+        _check(lib().tc_field_create(self._dkind, int(self._coords), _ptr(x), _ptr(y), _ptr(z),
+                                     _ptr(d1), _ptr(d2), _ptr(w), _ptr(wpos), n,
+                                     float(minsize), float(maxsize), int(sm), int(seed),
+                                     int(bool(brute)), int(mintop), int(maxtop),
+                                     ctypes.byref(h)))
+        self._h = h
+        self._keep = None   # the library copied the data (src/Field.cpp:180-196)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _lib is not None:
+            _lib.tc_field_free(h)
+            self._h = None
+
+    # BaseField methods (src/Field.cpp:624-634)
+    def getNObj(self):
+        return int(lib().tc_field_nobj(self._h))
+
+    def getSize(self):
+        return float(lib().tc_field_size(self._h))
+
+    def getNTopLevel(self):
+        r = lib().tc_field_ntop(self._h)
+        if r < 0:
+            _check(int(-r))
+        return int(r)
+
+    def countNear(self, *args):
+        raise NotImplementedError("countNear is not on the GPU path")
+
+    def getNear(self, *args):
+        raise NotImplementedError("getNear is not on the GPU path")
+
+    def KMeansInitTree(self, *args):
+        raise NotImplementedError("k-means patches are not on the GPU path")
+
+    KMeansInitRand = KMeansInitKMPP = KMeansRun = KMeansAssign = KMeansInitTree
+
+    def _dump(self):
+        """Canonical depth-first dump of the tree (tests only)."""
+        cap = 2 * max(self.getNObj(), 1) + 2
+        xyz = np.zeros((cap, 3))
+        swd = np.zeros((cap, 4), dtype=np.float32)
+        ns = np.zeros((cap, 2), dtype=np.int64)
+        depth = np.zeros(cap, dtype=np.int32)
+        cnt = lib().tc_field_dump(self._h, _ptr(xyz),
+                                  swd.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                  ns.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)),
+                                  depth.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), cap)
+        if cnt < 0:
+            _check(int(-cnt))
+        return dict(x=xyz[:cnt, 0], y=xyz[:cnt, 1], z=xyz[:cnt, 2], size=swd[:cnt, 0],
+                    w=swd[:cnt, 1], d1=swd[:cnt, 2], d2=swd[:cnt, 3], n=ns[:cnt, 0],
+                    start=ns[:cnt, 1], depth=depth[:cnt])
+
+
+def _field_class(name, dkind, coords):
+    if dkind == 0:
+        def __init__(self, x, y, z, w, wpos, minsize, maxsize, sm, seed, brute, mintop, maxtop):
+            self._build(x, y, z, None, None, w, wpos, minsize, maxsize, sm, seed, brute,
+                        mintop, maxtop)
+    elif dkind == 1:
+        def __init__(self, x, y, z, k, w, wpos, minsize, maxsize, sm, seed, brute, mintop,
+                     maxtop):
+            self._build(x, y, z, k, None, w, wpos, minsize, maxsize, sm, seed, brute, mintop,
+                        maxtop)
+    else:
+        def __init__(self, x, y, z, g1, g2, w, wpos, minsize, maxsize, sm, seed, brute,
+                     mintop, maxtop):
+            self._build(x, y, z, g1, g2, w, wpos, minsize, maxsize, sm, seed, brute, mintop,
+                        maxtop)
+    return type(name, (_FieldBase,), {"__init__": __init__, "_dkind": dkind,
+                                       "_coords": coords, "__module__": __name__})
+
+
+# BuildNField / BuildKField / BuildGField (src/Field.cpp:430-546)
+NFieldFlat = _field_class("NFieldFlat", 0, Coord.Flat)
+NFieldSphere = _field_class("NFieldSphere", 0, Coord.Sphere)
+NFieldThreeD = _field_class("NFieldThreeD", 0, Coord.ThreeD)
+KFieldFlat = _field_class("KFieldFlat", 1, Coord.Flat)
+KFieldSphere = _field_class("KFieldSphere", 1, Coord.Sphere)
+KFieldThreeD = _field_class("KFieldThreeD", 1, Coord.ThreeD)
+GFieldFlat = _field_class("GFieldFlat", 2, Coord.Flat)
+GFieldSphere = _field_class("GFieldSphere", 2, Coord.Sphere)
+GFieldThreeD = _field_class("GFieldThreeD", 2, Coord.ThreeD)
+
+
+class DeviceField(_FieldBase):
+    """A field built from catalog columns already resident on the GPU (no reference
+    counterpart: the device-resident form of the N/K/G field constructors).  The columns are
+    float64 device arrays given as integer pointers (e.g. torch.Tensor.data_ptr()) or
+    0 for an absent column; they must stay alive until the constructor returns."""
+
+    def __init__(self, dkind, coords, n, x, y, z, d1, d2, w, wpos, minsize, maxsize, sm, seed,
+                 brute, mintop, maxtop):
+        self._dkind = int(dkind)
+        self._coords = int(coords)
+        vp = ctypes.c_void_p
+        h = vp()
+        _check(lib().tc_field_create_device(self._dkind, self._coords, vp(x or None),
+                                            vp(y or None), vp(z or None), vp(d1 or None),
+                                            vp(d2 or None), vp(w or None), vp(wpos or None),
+                                            int(n), float(minsize), float(maxsize), int(sm),
+                                            int(seed), int(bool(brute)), int(mintop),
+                                            int(maxtop), ctypes.byref(h)))
+        self._h = h
+
+
+def launch_count():
+    """Kernels launched by libtcgpu.so since it was loaded."""
+    return int(lib().tc_launch_count())
+
+
+def stream_handle():
+    """The cudaStream_t (as an int) on which libtcgpu.so launches its work."""
+    return int(lib().tc_stream() or 0)
+
+
+# ----------------------------------------------------------------------------------------
+# Correlations
+
+class BaseCorr2:
+    """BaseCorr2 (src/Corr2.cpp:1168-1175): processAuto, processCross, triviallyZero."""
+    _dkind = 0
+
+    def __init__(self, bin_type, minsep, maxsep, nbins, binsize, b, a, minrpar, maxrpar, xp,
+                 yp, zp, xi0, xi1, xi2, xi3, meanr, meanlogr, weight, npairs):
+        # The outputs are aliased, never copied (BuildCorr2, src/Corr2.cpp:842-864).
+        outs = []
+        for name, arr in (("xi0", xi0), ("xi1", xi1), ("xi2", xi2), ("xi3", xi3),
+                          ("meanr", meanr), ("meanlogr", meanlogr), ("weight", weight),
+                          ("npairs", npairs)):
+            if arr is None or arr.size == 0:
+                outs.append(None)
+                continue
+            if arr.dtype != np.float64 or not arr.flags["C_CONTIGUOUS"] or \
+                    not arr.flags["WRITEABLE"]:
+                raise ValueError(f"{name} must be a writeable contiguous float64 array")
+            if arr.size != int(nbins):
+                raise ValueError(f"{name} has size {arr.size}, expected nbins={nbins}")
+            outs.append(arr)
+        self._outs = outs
+        h = ctypes.c_void_p()
+        _check(lib().tc_corr2_create(self._dkind, self._dkind, int(bin_type), float(minsep),
+                                     float(maxsep), int(nbins), float(binsize), float(b),
+                                     float(a), float(minrpar), float(maxrpar), float(xp),
+                                     float(yp), float(zp), *[_ptr(o) for o in outs],
+                                     ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _lib is not None:
+            _lib.tc_corr2_free(h)
+            self._h = None
+
+    def processAuto(self, field, dots, quick, metric):
+        _check(lib().tc_corr2_process_auto(self._h, field._h, int(bool(dots)), int(bool(quick)),
+                                           int(metric)))
+
+    def processCross(self, field1, field2, dots, quick, metric):
+        _check(lib().tc_corr2_process_cross(self._h, field1._h, field2._h, int(bool(dots)),
+                                            int(bool(quick)), int(metric)))
+
+    def triviallyZero(self, metric, coords, x1, y1, z1, s1, x2, y2, z2, s2):
+        out = ctypes.c_int(0)
+        _check(lib().tc_corr2_trivially_zero(self._h, int(metric), int(coords), float(x1),
+                                             float(y1), float(z1), float(s1), float(x2),
+                                             float(y2), float(z2), float(s2), ctypes.byref(out)))
+        return int(out.value)
+
+    def samplePairs(self, *args):
+        raise NotImplementedError("samplePairs is not on the GPU path")
+
+    def stats(self):
+        """Counters of the last process call (no reference counterpart)."""
+        s = tc_stats()
+        _check(lib().tc_corr2_stats(self._h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in tc_stats._fields_}
+
+
+class NNCorr(BaseCorr2):
+    _dkind = 0
+
+
+class KKCorr(BaseCorr2):
+    _dkind = 1
+
+
+class GGCorr(BaseCorr2):
+    _dkind = 2
+
+
+def _not_on_path(name):
+    def f(*args, **kwargs):
+        raise NotImplementedError(f"{name} is not on the GPU path")
+    f.__name__ = name
+    return f
+
+
+# Correlation classes of the reference that are outside this hot path.
+for _n in ("NKCorr", "NZCorr", "KZCorr", "ZZCorr", "NVCorr", "KVCorr", "VVCorr", "NGCorr",
+           "KGCorr", "NTCorr", "KTCorr", "TTCorr", "NQCorr", "KQCorr", "QQCorr"):
+    globals()[_n] = _not_on_path(_n)
+QuickAssign = _not_on_path("QuickAssign")
+SelectPatch = _not_on_path("SelectPatch")
+GenerateXYZ = _not_on_path("GenerateXYZ")
+del _n

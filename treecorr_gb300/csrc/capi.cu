@@ -1,0 +1,695 @@
+// capi.cu -- the C ABI (include/tcgpu.h): fields, corr objects, process calls.
+//
+// Objects mirror the reference's native classes: a tc_field is Field<D,C>
+// (include/Field.h:88-106) holding its catalog on the device and building its tree lazily;
+// a tc_corr2 is Corr2<D1,D2> (include/Corr2.h:139-223) aliasing caller-owned output arrays
+// and adding into them.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "../../include/tcgpu.h"
+#include "tc_internal.cuh"
+#include "tc_host.hpp"
+#include "traverse2pt.hpp"
+
+namespace tc {
+
+static thread_local std::string g_last_error;
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+static std::atomic<long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+static cudaStream_t g_stream = nullptr;
+static int stream_get(cudaStream_t* s)
+{
+    if (!g_stream) TC_CU(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking));
+    *s = g_stream;
+    return 0;
+}
+
+static const char* dev_err_msg(int code)
+{
+    switch (code) {
+      case DEV_STACK_OVERFLOW: return "traversal stack overflow";
+      case DEV_SPILL_OVERFLOW: return "traversal spill list overflow";
+      case DEV_DEGENERATE_SPLIT:
+          return "mean split put every point of a large cell on one side although the points "
+                 "differ along the split axis (degenerate weights)";
+      case DEV_BAD_CHILD: return "traversal asked to split a leaf cell (inconsistent tree)";
+      case DEV_TASK_OVERFLOW: return "tree build task stack overflow";
+      default: return "unknown device error";
+    }
+}
+
+}  // namespace tc
+
+using namespace tc;
+
+struct tc_field {
+    int dkind = 0, coords = 0, split = 0, brute = 0, mintop = 0, maxtop = 0;
+    int64_t n = 0;
+    double minsize = 0., maxsize = 0.;
+    bool built = false;
+    Points buf[2] = {};
+    Cells cells = {};
+    TCell* tcells = nullptr;
+    int* d_tops_raw = nullptr;   // (start, id) pairs written by the build
+    int* d_ntop = nullptr;
+    int* d_tops = nullptr;       // ordered top ids
+    std::vector<int> tops;
+    double center[4] = {0., 0., 0., 0.};   // x, y, z, size^2
+    BuildScratch S;
+    int* d_err = nullptr;
+    float build_ms = 0.f;
+};
+
+struct tc_corr2 {
+    int d1 = 0, d2 = 0, bin_type = 0, nbins = 0;
+    double minsep = 0., maxsep = 0., binsize = 0., b = 0., a = 0.;
+    double *xi0 = nullptr, *xi1 = nullptr, *xi2 = nullptr, *xi3 = nullptr;
+    double *meanr = nullptr, *meanlogr = nullptr, *weight = nullptr, *npairs = nullptr;
+    tc_stats stats = {};
+    // Traversal scratch, grown on demand.
+    int2* stacks = nullptr;
+    int2* spill[2] = {nullptr, nullptr};
+    long long spill_cap = 0;
+    int stack_cap = 0, nwarps_alloc = 0, nq_alloc = 0;
+    double* wacc = nullptr;
+    unsigned long long* wnp = nullptr;
+    double* tot = nullptr;
+    unsigned long long* totnp = nullptr;
+    unsigned long long* ctl = nullptr;   // root_next, nout, counters[3]
+    int* idle = nullptr;
+    int* d_err = nullptr;
+};
+
+namespace {
+
+void free_points(Points& P)
+{
+    dfree(P.x); dfree(P.y); dfree(P.z); dfree(P.wp); dfree(P.w); dfree(P.d1); dfree(P.d2);
+    dfree(P.idx);
+}
+
+int alloc_points(Points& P, int64_t n)
+{
+    TC_TRY(dalloc(&P.x, n)); TC_TRY(dalloc(&P.y, n)); TC_TRY(dalloc(&P.z, n));
+    TC_TRY(dalloc(&P.wp, n)); TC_TRY(dalloc(&P.w, n)); TC_TRY(dalloc(&P.d1, n));
+    TC_TRY(dalloc(&P.d2, n)); TC_TRY(dalloc(&P.idx, n));
+    return 0;
+}
+
+void free_cells(Cells& C)
+{
+    dfree(C.x); dfree(C.y); dfree(C.z); dfree(C.size); dfree(C.w); dfree(C.d1); dfree(C.d2);
+    dfree(C.n); dfree(C.start); dfree(C.left); dfree(C.right);
+}
+
+int alloc_cells(Cells& C, int64_t m)
+{
+    TC_TRY(dalloc(&C.x, m)); TC_TRY(dalloc(&C.y, m)); TC_TRY(dalloc(&C.z, m));
+    TC_TRY(dalloc(&C.size, m)); TC_TRY(dalloc(&C.w, m)); TC_TRY(dalloc(&C.d1, m));
+    TC_TRY(dalloc(&C.d2, m)); TC_TRY(dalloc(&C.n, m)); TC_TRY(dalloc(&C.start, m));
+    TC_TRY(dalloc(&C.left, m)); TC_TRY(dalloc(&C.right, m));
+    return 0;
+}
+
+void free_scratch(BuildScratch& S)
+{
+    dfree(S.tasks); dfree(S.chunk0); dfree(S.chunks); dfree(S.part1); dfree(S.part2);
+    dfree(S.stats); dfree(S.big_next); dfree(S.small); dfree(S.counters); dfree(S.wstack);
+    S.cap_tasks = S.cap_chunks = 0;
+}
+
+void field_release(tc_field* f)
+{
+    free_points(f->buf[0]); free_points(f->buf[1]); free_cells(f->cells);
+    dfree(f->tcells); dfree(f->d_tops_raw); dfree(f->d_ntop); dfree(f->d_tops);
+    free_scratch(f->S); dfree(f->d_err);
+}
+
+int check_dev_err(int* d_err, cudaStream_t st)
+{
+    int e = 0;
+    TC_CU(cudaMemcpyAsync(&e, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TC_CU(cudaStreamSynchronize(st));
+    if (e) {
+        set_last_error(std::string("device error: ") + dev_err_msg(e));
+        TC_CU(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+        return TC_ERR_DEVICE;
+    }
+    return 0;
+}
+
+// BaseField::BuildCells (src/Field.cpp:206-277) on the device.
+int field_build(tc_field* f)
+{
+    if (f->built) return 0;
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    const int64_t n = f->n;
+    if (n == 0) { f->built = true; return 0; }
+    const int64_t ncap = 2 * n - 1;
+    TC_TRY(alloc_cells(f->cells, ncap));
+    TC_TRY(dalloc(&f->tcells, ncap));
+    TC_TRY(dalloc(&f->d_tops_raw, 2 * n));
+    TC_TRY(dalloc(&f->d_ntop, 1));
+    TC_TRY(dalloc(&f->S.small, n));
+    TC_TRY(dalloc(&f->S.wstack, n));
+    TC_TRY(dalloc(&f->S.counters, 2));
+    TC_TRY(alloc_points(f->buf[1], n));
+    // Unused ids (inside list leaves) keep harmless contents.
+    TC_CU(cudaMemsetAsync(f->cells.left, 0xff, ncap * sizeof(int), st));
+    TC_CU(cudaMemsetAsync(f->cells.right, 0xff, ncap * sizeof(int), st));
+    cudaEvent_t e0, e1;
+    TC_CU(cudaEventCreate(&e0));
+    TC_CU(cudaEventCreate(&e1));
+    TC_CU(cudaEventRecord(e0, st));
+    BuildParams BP;
+    BP.coords = f->coords; BP.dkind = f->dkind; BP.split = f->split; BP.brute = f->brute;
+    BP.minsizesq = f->minsize * f->minsize;
+    BP.maxsizesq = f->maxsize * f->maxsize;
+    BP.n = (int)n;
+    TC_TRY(build_tree(BP, f->buf, f->cells, f->d_tops_raw, f->d_ntop, f->S, st, f->tops, f->d_err,
+                      f->mintop, f->maxtop));
+    launch_pack_cells((int)ncap, f->cells, f->tcells, st);
+    TC_CU(cudaGetLastError());
+    TC_TRY(dalloc(&f->d_tops, f->tops.size()));
+    TC_CU(cudaMemcpyAsync(f->d_tops, f->tops.data(), f->tops.size() * sizeof(int),
+                          cudaMemcpyHostToDevice, st));
+    launch_validate_tree((int)ncap, f->cells, f->d_tops, (int)f->tops.size(), f->d_err, st);
+    TC_CU(cudaGetLastError());
+    TC_CU(cudaEventRecord(e1, st));
+    TC_CU(cudaEventSynchronize(e1));
+    TC_CU(cudaEventElapsedTime(&f->build_ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    TC_TRY(check_dev_err(f->d_err, st));
+    // The second point buffer and the build scratch are no longer needed.
+    free_points(f->buf[1]);
+    free_scratch(f->S);
+    f->built = true;
+    return 0;
+}
+
+int field_create_impl(int dkind, int coords, const double* x, const double* y, const double* z,
+                      const double* d1, const double* d2, const double* w, const double* wpos,
+                      int64_t n, double min_size, double max_size, int split_method, int brute,
+                      int min_top, int max_top, bool on_device, tc_field** out)
+{
+    if (!out) { set_last_error("out is NULL"); return TC_ERR_ARG; }
+    *out = nullptr;
+    if (n < 0 || n > (int64_t)std::numeric_limits<int>::max() / 2) {
+        set_last_error("n out of range for the GPU path (0 <= n < 2^30)");
+        return TC_ERR_ARG;
+    }
+    if (dkind < TC_NDATA || dkind > TC_GDATA) { set_last_error("bad data kind"); return TC_ERR_ARG; }
+    if (coords != TC_FLAT && coords != TC_THREED && coords != TC_SPHERE) {
+        set_last_error("bad coords"); return TC_ERR_ARG;
+    }
+    if (split_method == TC_RANDOM) {
+        set_last_error("split_method='random' is not on the GPU path");
+        return TC_ERR_UNSUPPORTED;
+    }
+    if (split_method < TC_MIDDLE || split_method > TC_RANDOM) {
+        set_last_error("bad split_method"); return TC_ERR_ARG;
+    }
+    if (n > 0 && (!x || !y || !w || (coords != TC_FLAT && !z) || (dkind >= TC_KDATA && !d1) ||
+                  (dkind == TC_GDATA && !d2))) {
+        set_last_error("missing input array"); return TC_ERR_ARG;
+    }
+    tc_field* f = new tc_field();
+    f->dkind = dkind; f->coords = coords; f->split = split_method; f->brute = brute ? 1 : 0;
+    f->mintop = min_top; f->maxtop = max_top; f->n = n;
+    f->minsize = min_size; f->maxsize = max_size;
+    cudaStream_t st;
+    int rc = stream_get(&st);
+    if (rc) { delete f; return rc; }
+    auto fail = [&](int code) { field_release(f); delete f; return code; };
+    if ((rc = dalloc(&f->d_err, 1))) return fail(rc);
+    if (cudaMemsetAsync(f->d_err, 0, sizeof(int), st) != cudaSuccess) {
+        set_last_error("cudaMemsetAsync failed"); return fail(TC_ERR_CUDA);
+    }
+    if (n > 0) {
+        if ((rc = alloc_points(f->buf[0], n))) return fail(rc);
+        const double* src[7] = {x, y, (coords != TC_FLAT) ? z : nullptr, d1, d2, w, wpos};
+        const double* dsrc[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+        double* staging = nullptr;
+        if (!on_device) {
+            int cnt = 0;
+            for (int k = 0; k < 7; ++k) if (src[k]) ++cnt;
+            if ((rc = dalloc(&staging, (size_t)cnt * n))) return fail(rc);
+            int slot = 0;
+            for (int k = 0; k < 7; ++k) {
+                if (!src[k]) continue;
+                double* dst = staging + (size_t)slot * n;
+                if (cudaMemcpyAsync(dst, src[k], n * sizeof(double), cudaMemcpyHostToDevice, st) !=
+                    cudaSuccess) {
+                    dfree(staging);
+                    set_last_error("host to device copy failed");
+                    return fail(TC_ERR_CUDA);
+                }
+                dsrc[k] = dst;
+                ++slot;
+            }
+        } else {
+            for (int k = 0; k < 7; ++k) dsrc[k] = src[k];
+        }
+        launch_prepare((int)n, coords, dkind, dsrc[0], dsrc[1], dsrc[2], dsrc[3], dsrc[4], dsrc[5],
+                       dsrc[6], f->buf[0], st);
+        BuildParams BP;
+        BP.coords = coords; BP.dkind = dkind; BP.split = split_method; BP.brute = f->brute;
+        BP.minsizesq = 0.; BP.maxsizesq = 0.; BP.n = (int)n;
+        rc = field_center(BP, f->buf[0], f->S, st, f->center);
+        if (staging) { cudaStreamSynchronize(st); dfree(staging); }
+        if (rc) return fail(rc);
+        if (cudaGetLastError() != cudaSuccess) {
+            set_last_error("field preparation kernel failed");
+            return fail(TC_ERR_CUDA);
+        }
+    }
+    *out = f;
+    return TC_OK;
+}
+
+// Per-call traversal scratch.
+int corr_scratch(tc_corr2* c, int nwarps, int nq)
+{
+    const int stack_cap = c->stack_cap > 0 ? c->stack_cap : 8192;
+    if (nwarps > c->nwarps_alloc || stack_cap != c->stack_cap || nq > c->nq_alloc || !c->ctl) {
+        dfree(c->stacks); dfree(c->spill[0]); dfree(c->spill[1]); dfree(c->wacc); dfree(c->wnp);
+        dfree(c->tot); dfree(c->totnp); dfree(c->ctl); dfree(c->idle); dfree(c->d_err);
+        long long cap = (long long)nwarps * stack_cap;
+        if (c->spill_cap < cap) c->spill_cap = cap;
+        TC_TRY(dalloc(&c->stacks, (size_t)nwarps * stack_cap));
+        TC_TRY(dalloc(&c->spill[0], (size_t)c->spill_cap));
+        TC_TRY(dalloc(&c->spill[1], (size_t)c->spill_cap));
+        TC_TRY(dalloc(&c->wacc, (size_t)nwarps * nq * c->nbins));
+        TC_TRY(dalloc(&c->wnp, (size_t)nwarps * c->nbins));
+        TC_TRY(dalloc(&c->tot, (size_t)nq * c->nbins));
+        TC_TRY(dalloc(&c->totnp, (size_t)c->nbins));
+        TC_TRY(dalloc(&c->ctl, 8));
+        TC_TRY(dalloc(&c->idle, 1));
+        TC_TRY(dalloc(&c->d_err, 1));
+        c->nwarps_alloc = nwarps;
+        c->stack_cap = stack_cap;
+        c->nq_alloc = nq;
+    }
+    return 0;
+}
+
+double sqr(double x) { return x * x; }
+
+// MetricHelper<M>::DistSq on two host positions (include/Metric.h:143-147, 202-207, 668-682).
+double host_dist_sq(int coords, int metric, const double* p1, const double* p2)
+{
+    double dx = p1[0] - p2[0], dy = p1[1] - p2[1];
+    if (coords == TC_FLAT) return dx * dx + dy * dy;
+    double dz = p1[2] - p2[2];
+    double dsq = dx * dx + dy * dy + dz * dz;
+    if (metric == TC_ARC) {
+        double th = 2. * std::asin(std::sqrt(dsq) / 2.);
+        return th * th;
+    }
+    return dsq;
+}
+
+int check_metric(int coords, int metric)
+{
+    if (metric == TC_EUCLIDEAN) return 0;
+    if (metric == TC_ARC && coords == TC_SPHERE) return 0;
+    set_last_error("metric/coords combination is not on the GPU path (Euclidean on any "
+                   "coords, Arc on spherical coords)");
+    return TC_ERR_UNSUPPORTED;
+}
+
+// BaseCorr2::process for one or two fields.
+int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
+{
+    if (!c || !f1) { set_last_error("NULL argument"); return TC_ERR_ARG; }
+    if (c->d1 != f1->dkind || (f2 && c->d2 != f2->dkind)) {
+        set_last_error("field data kind does not match the correlation"); return TC_ERR_ARG;
+    }
+    if (f2 && f2->coords != f1->coords) {
+        set_last_error("fields have different coords"); return TC_ERR_ARG;
+    }
+    TC_TRY(check_metric(f1->coords, metric));
+    c->stats = tc_stats();
+    if (f1->n == 0 || (f2 && f2->n == 0)) return TC_OK;
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    if (f2) {
+        // Early exit when the fields cannot overlap, src/Corr2.cpp:213-231.
+        double rsq = host_dist_sq(f1->coords, metric, f1->center, f2->center);
+        double s1ps2 = std::sqrt(f1->center[3]) + std::sqrt(f2->center[3]);
+        double minsepsq = c->minsep * c->minsep, maxsepsq = c->maxsep * c->maxsep;
+        if ((rsq < minsepsq && s1ps2 < c->minsep && rsq < sqr(c->minsep - s1ps2)) ||
+            (rsq >= maxsepsq && rsq >= sqr(c->maxsep + s1ps2)))
+            return TC_OK;
+    }
+    TC_TRY(field_build(f1));
+    if (f2) TC_TRY(field_build(f2));
+    c->stats.build_ms = f1->build_ms + (f2 ? f2->build_ms : 0.f);
+
+    const int nb = c->nbins;
+    const int nq = c->d1 == TC_GDATA ? 7 : (c->d1 == TC_KDATA ? 4 : 3);
+    TravParams T;
+    std::memset(&T, 0, sizeof(T));
+    T.coords = f1->coords; T.metric = metric; T.dkind = c->d1; T.quick = quick ? 1 : 0;
+    T.nbins = nb; T.autoc = f2 ? 0 : 1; T.nqf = nq;
+    T.minsep = c->minsep; T.maxsep = c->maxsep; T.binsize = c->binsize; T.b = c->b; T.a = c->a;
+    T.logminsep = std::log(c->minsep); T.halfminsep = 0.5 * c->minsep;
+    T.minsepsq = c->minsep * c->minsep; T.maxsepsq = c->maxsep * c->maxsep;
+    T.bsq = c->b * c->b; T.asq = c->a * c->a;
+    T.fminsep = (float)T.minsep; T.fmaxsep = (float)T.maxsep; T.fbinsize = (float)T.binsize;
+    T.fb = (float)T.b; T.fminsepsq = (float)T.minsepsq; T.fmaxsepsq = (float)T.maxsepsq;
+    T.fbsq = (float)T.bsq; T.fasq = (float)std::min(T.asq, 1e30);
+    T.fbb = (float)(0.25 * sqr(T.binsize + T.b));
+    T.fmineff = (float)std::min(T.bsq, T.asq);
+    T.finvminsepsq = (float)(1. / T.minsepsq);
+    T.finvbinsize = (float)(1. / T.binsize);
+    T.flogminsep = (float)T.logminsep;
+    tc_field* g = f2 ? f2 : f1;
+    T.c1 = f1->tcells; T.c2 = g->tcells;
+    T.x1 = f1->cells.x; T.y1 = f1->cells.y; T.z1 = f1->cells.z;
+    T.x2 = g->cells.x; T.y2 = g->cells.y; T.z2 = g->cells.z;
+    T.tops1 = f1->d_tops; T.tops2 = g->d_tops;
+    T.ntop1 = (long long)f1->tops.size(); T.ntop2 = (long long)g->tops.size();
+    T.ngen = f2 ? T.ntop1 * T.ntop2 : T.ntop1 * (T.ntop1 + 1) / 2;
+    if (T.minsep <= 0. || T.binsize <= 0. || nb <= 0) {
+        set_last_error("Log binning needs min_sep > 0, bin_size > 0, nbins > 0");
+        return TC_ERR_ARG;
+    }
+
+    int blocks = 0, nwarps = 0;
+    TC_TRY(traverse_grid(nq, nb, &blocks, &nwarps));
+    cudaEvent_t e0, e1;
+    TC_CU(cudaEventCreate(&e0));
+    TC_CU(cudaEventCreate(&e1));
+    for (int attempt = 0; attempt < 4; ++attempt) {
+        TC_TRY(corr_scratch(c, nwarps, nq));
+        T.stacks = c->stacks; T.stack_cap = c->stack_cap; T.nwarps = nwarps;
+        T.wacc = c->wacc; T.wnp = c->wnp; T.idle = c->idle; T.err = c->d_err;
+        T.root_next = c->ctl; T.nout = c->ctl + 1; T.counters = c->ctl + 2;
+        T.out_cap = c->spill_cap;
+        TC_CU(cudaMemsetAsync(c->wacc, 0, sizeof(double) * (size_t)nwarps * nq * nb, st));
+        TC_CU(cudaMemsetAsync(c->wnp, 0, sizeof(unsigned long long) * (size_t)nwarps * nb, st));
+        TC_CU(cudaMemsetAsync(c->ctl, 0, 8 * sizeof(unsigned long long), st));
+        TC_CU(cudaMemsetAsync(c->d_err, 0, sizeof(int), st));
+        TC_CU(cudaEventRecord(e0, st));
+        int cur = 0;
+        long long nin = 0;
+        T.in_tasks = nullptr;
+        int launches = 0;
+        int derr = 0;
+        while (true) {
+            T.nin = nin;
+            T.out_tasks = c->spill[cur ^ 1];
+            TC_CU(cudaMemsetAsync(c->ctl, 0, 2 * sizeof(unsigned long long), st));
+            TC_CU(cudaMemsetAsync(c->idle, 0, sizeof(int), st));
+            TC_TRY(launch_traverse(T, blocks, st));
+            ++launches;
+            unsigned long long nout = 0;
+            TC_CU(cudaMemcpyAsync(&nout, c->ctl + 1, sizeof(nout), cudaMemcpyDeviceToHost, st));
+            TC_CU(cudaMemcpyAsync(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+            TC_CU(cudaStreamSynchronize(st));
+            if (derr) break;
+            if (nout == 0) break;
+            if (launches >= 100000) {
+                set_last_error("traversal did not finish within 100000 relaunches");
+                cudaEventDestroy(e0); cudaEventDestroy(e1);
+                return TC_ERR_DEVICE;
+            }
+            // The spilled items become the roots of the next launch.
+            T.ngen = 0;
+            T.in_tasks = c->spill[cur ^ 1];
+            nin = (long long)nout;
+            cur ^= 1;
+        }
+        if (derr == DEV_SPILL_OVERFLOW || derr == DEV_STACK_OVERFLOW) {
+            // Retry with larger stacks and spill lists.
+            c->stack_cap *= 2;
+            c->spill_cap *= 4;
+            T.ngen = f2 ? T.ntop1 * T.ntop2 : T.ntop1 * (T.ntop1 + 1) / 2;
+            continue;
+        }
+        if (derr) {
+            set_last_error(std::string("device error: ") + dev_err_msg(derr));
+            cudaEventDestroy(e0); cudaEventDestroy(e1);
+            return TC_ERR_DEVICE;
+        }
+        TC_TRY(launch_reduce(nwarps, nq, nb, c->wacc, c->wnp, c->tot, c->totnp, st));
+        TC_CU(cudaEventRecord(e1, st));
+        std::vector<double> tot((size_t)nq * nb);
+        std::vector<unsigned long long> totnp(nb);
+        unsigned long long cnt[3];
+        TC_CU(cudaMemcpyAsync(tot.data(), c->tot, tot.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+        TC_CU(cudaMemcpyAsync(totnp.data(), c->totnp, nb * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        TC_CU(cudaMemcpyAsync(cnt, c->ctl + 2, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        TC_CU(cudaStreamSynchronize(st));
+        float ms = 0.f;
+        TC_CU(cudaEventElapsedTime(&ms, e0, e1));
+        cudaEventDestroy(e0); cudaEventDestroy(e1);
+        c->stats.cell_pairs = (int64_t)cnt[0];
+        c->stats.accepted = (int64_t)cnt[1];
+        c->stats.escalated = (int64_t)cnt[2];
+        c->stats.launches = launches;
+        c->stats.traverse_ms = ms;
+        // Corr2::finishProcess adds into the caller's arrays (src/Corr2.cpp:527-566).
+        for (int k = 0; k < nb; ++k) {
+            c->weight[k] += tot[k];
+            if (!quick) {
+                c->meanr[k] += tot[nb + k];
+                c->meanlogr[k] += tot[2 * nb + k];
+                c->npairs[k] += (double)totnp[k];
+            }
+            if (c->d1 == TC_KDATA) {
+                if (c->xi0) c->xi0[k] += tot[3 * nb + k];
+            } else if (c->d1 == TC_GDATA) {
+                if (c->xi0) c->xi0[k] += tot[3 * nb + k];
+                if (c->xi1) c->xi1[k] += tot[4 * nb + k];
+                if (c->xi2) c->xi2[k] += tot[5 * nb + k];
+                if (c->xi3) c->xi3[k] += tot[6 * nb + k];
+            }
+        }
+        return TC_OK;
+    }
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    set_last_error("traversal scratch still too small after retries");
+    return TC_ERR_DEVICE;
+}
+
+// Canonical depth-first dump of the tree (host walk over device-copied cells).
+int64_t field_dump(tc_field* f, double* xyz, float* swd, int64_t* ns, int32_t* depth, int64_t cap)
+{
+    int rc = field_build(f);
+    if (rc) return -rc;
+    if (f->n == 0) return 0;
+    const int64_t m = 2 * f->n - 1;
+    std::vector<double> X(m), Y(m), Z(m);
+    std::vector<float> S(m), W(m), D1(m), D2(m);
+    std::vector<int> N(m), ST(m), L(m), R(m);
+    auto cp = [&](void* dst, const void* src, size_t bytes) {
+        return cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost) == cudaSuccess;
+    };
+    bool ok = cp(X.data(), f->cells.x, m * 8) && cp(Y.data(), f->cells.y, m * 8) &&
+              cp(Z.data(), f->cells.z, m * 8) && cp(S.data(), f->cells.size, m * 4) &&
+              cp(W.data(), f->cells.w, m * 4) && cp(D1.data(), f->cells.d1, m * 4) &&
+              cp(D2.data(), f->cells.d2, m * 4) && cp(N.data(), f->cells.n, m * 4) &&
+              cp(ST.data(), f->cells.start, m * 4) && cp(L.data(), f->cells.left, m * 4) &&
+              cp(R.data(), f->cells.right, m * 4);
+    if (!ok) { set_last_error("device to host copy failed"); return -TC_ERR_CUDA; }
+    int64_t cnt = 0;
+    std::vector<std::pair<int, int>> stack;
+    for (int t = (int)f->tops.size() - 1; t >= 0; --t) stack.push_back({f->tops[t], 0});
+    while (!stack.empty()) {
+        auto [id, d] = stack.back();
+        stack.pop_back();
+        if (cnt < cap) {
+            xyz[3 * cnt] = X[id]; xyz[3 * cnt + 1] = Y[id]; xyz[3 * cnt + 2] = Z[id];
+            swd[4 * cnt] = S[id]; swd[4 * cnt + 1] = W[id];
+            swd[4 * cnt + 2] = D1[id]; swd[4 * cnt + 3] = D2[id];
+            ns[2 * cnt] = N[id]; ns[2 * cnt + 1] = ST[id];
+            depth[cnt] = d;
+        }
+        ++cnt;
+        if (L[id] >= 0) {
+            stack.push_back({R[id], d + 1});
+            stack.push_back({L[id], d + 1});
+        }
+    }
+    return cnt;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tc_field_create(int dkind, int coords, const double* x, const double* y, const double* z,
+                    const double* d1, const double* d2, const double* w, const double* wpos,
+                    int64_t n, double min_size, double max_size, int split_method, int64_t seed,
+                    int brute, int min_top, int max_top, tc_field** out)
+{
+    (void)seed;
+    return field_create_impl(dkind, coords, x, y, z, d1, d2, w, wpos, n, min_size, max_size,
+                             split_method, brute, min_top, max_top, false, out);
+}
+
+int tc_field_create_device(int dkind, int coords, const double* x, const double* y,
+                           const double* z, const double* d1, const double* d2, const double* w,
+                           const double* wpos, int64_t n, double min_size, double max_size,
+                           int split_method, int64_t seed, int brute, int min_top, int max_top,
+                           tc_field** out)
+{
+    (void)seed;
+    return field_create_impl(dkind, coords, x, y, z, d1, d2, w, wpos, n, min_size, max_size,
+                             split_method, brute, min_top, max_top, true, out);
+}
+
+void tc_field_free(tc_field* f)
+{
+    if (!f) return;
+    field_release(f);
+    delete f;
+}
+
+int64_t tc_field_nobj(const tc_field* f) { return f ? f->n : 0; }
+
+double tc_field_size(const tc_field* f) { return f ? std::sqrt(f->center[3]) : 0.; }
+
+int64_t tc_field_ntop(tc_field* f)
+{
+    if (!f) { set_last_error("NULL field"); return -TC_ERR_ARG; }
+    int rc = field_build(f);
+    if (rc) return -rc;
+    return (int64_t)f->tops.size();
+}
+
+int tc_field_center(const tc_field* f, double* xyz3)
+{
+    if (!f || !xyz3) { set_last_error("NULL argument"); return TC_ERR_ARG; }
+    xyz3[0] = f->center[0]; xyz3[1] = f->center[1]; xyz3[2] = f->center[2];
+    return TC_OK;
+}
+
+int64_t tc_field_dump(tc_field* f, double* xyz, float* size_w_d, int64_t* n_start,
+                      int32_t* depth, int64_t cap)
+{
+    if (!f) { set_last_error("NULL field"); return -TC_ERR_ARG; }
+    return field_dump(f, xyz, size_w_d, n_start, depth, cap);
+}
+
+int tc_corr2_create(int d1, int d2, int bin_type, double minsep, double maxsep, int nbins,
+                    double binsize, double b, double a, double minrpar, double maxrpar,
+                    double xp, double yp, double zp, double* xi0, double* xi1, double* xi2,
+                    double* xi3, double* meanr, double* meanlogr, double* weight,
+                    double* npairs, tc_corr2** out)
+{
+    if (!out) { set_last_error("out is NULL"); return TC_ERR_ARG; }
+    *out = nullptr;
+    if (d1 != d2 || d1 < TC_NDATA || d1 > TC_GDATA) {
+        set_last_error("only NN, KK and GG are on the GPU path");
+        return TC_ERR_UNSUPPORTED;
+    }
+    if (bin_type != TC_LOG) {
+        set_last_error("only Log binning is on the GPU path");
+        return TC_ERR_UNSUPPORTED;
+    }
+    const double big = std::numeric_limits<double>::max();
+    if (!(minrpar <= -big) || !(maxrpar >= big) || xp != 0. || yp != 0. || zp != 0.) {
+        set_last_error("min_rpar/max_rpar/period are not on the GPU path");
+        return TC_ERR_UNSUPPORTED;
+    }
+    if (nbins <= 0 || !(minsep > 0.) || !(maxsep > minsep) || !(binsize > 0.) || b < 0. || a < 0.) {
+        set_last_error("invalid binning");
+        return TC_ERR_ARG;
+    }
+    if (!meanr || !meanlogr || !weight || !npairs || (d1 == TC_KDATA && !xi0) ||
+        (d1 == TC_GDATA && (!xi0 || !xi1 || !xi2 || !xi3))) {
+        set_last_error("missing output array");
+        return TC_ERR_ARG;
+    }
+    tc_corr2* c = new tc_corr2();
+    c->d1 = d1; c->d2 = d2; c->bin_type = bin_type; c->nbins = nbins;
+    c->minsep = minsep; c->maxsep = maxsep; c->binsize = binsize; c->b = b; c->a = a;
+    c->xi0 = xi0; c->xi1 = xi1; c->xi2 = xi2; c->xi3 = xi3;
+    c->meanr = meanr; c->meanlogr = meanlogr; c->weight = weight; c->npairs = npairs;
+    *out = c;
+    return TC_OK;
+}
+
+void tc_corr2_free(tc_corr2* c)
+{
+    if (!c) return;
+    dfree(c->stacks); dfree(c->spill[0]); dfree(c->spill[1]); dfree(c->wacc); dfree(c->wnp);
+    dfree(c->tot); dfree(c->totnp); dfree(c->ctl); dfree(c->idle); dfree(c->d_err);
+    delete c;
+}
+
+int tc_corr2_process_auto(tc_corr2* c, tc_field* f, int dots, int quick, int metric)
+{
+    (void)dots;
+    if (!f) { set_last_error("NULL field"); return TC_ERR_ARG; }
+    return corr_process(c, f, nullptr, quick, metric);
+}
+
+int tc_corr2_process_cross(tc_corr2* c, tc_field* f1, tc_field* f2, int dots, int quick,
+                           int metric)
+{
+    (void)dots;
+    if (!f1 || !f2) { set_last_error("NULL field"); return TC_ERR_ARG; }
+    return corr_process(c, f1, f2, quick, metric);
+}
+
+int tc_corr2_trivially_zero(tc_corr2* c, int metric, int coords, double x1, double y1,
+                            double z1, double s1, double x2, double y2, double z2, double s2,
+                            int* out)
+{
+    if (!c || !out) { set_last_error("NULL argument"); return TC_ERR_ARG; }
+    TC_TRY(check_metric(coords, metric));
+    // BaseCorr2::triviallyZero, src/Corr2.cpp:590-601; Position<Sphere> normalises.
+    double p1[3] = {x1, y1, coords == TC_FLAT ? 0. : z1};
+    double p2[3] = {x2, y2, coords == TC_FLAT ? 0. : z2};
+    if (coords == TC_SPHERE) {
+        for (double* p : {p1, p2}) {
+            double nn = std::sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+            if (nn == 0.) { p[0] = 1.; p[1] = 0.; p[2] = 0.; }
+            else { p[0] /= nn; p[1] /= nn; p[2] /= nn; }
+        }
+    }
+    double rsq = host_dist_sq(coords, metric, p1, p2);
+    double s1ps2 = s1 + s2;
+    double maxsepsq = c->maxsep * c->maxsep;
+    *out = (rsq >= maxsepsq && rsq >= sqr(c->maxsep + s1ps2)) ? 1 : 0;
+    return TC_OK;
+}
+
+int tc_corr2_stats(const tc_corr2* c, tc_stats* out)
+{
+    if (!c || !out) { set_last_error("NULL argument"); return TC_ERR_ARG; }
+    *out = c->stats;
+    return TC_OK;
+}
+
+int tc_set_omp_threads(int num_threads) { (void)num_threads; return 1; }
+int tc_get_omp_threads(void) { return 1; }
+
+const char* tc_last_error(void) { return g_last_error.c_str(); }
+
+long long tc_launch_count(void) { return g_launches.load(); }
+
+void* tc_stream(void)
+{
+    cudaStream_t s = nullptr;
+    if (stream_get(&s)) return nullptr;
+    return (void*)s;
+}
+
+}  // extern "C"

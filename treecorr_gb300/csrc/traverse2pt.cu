@@ -1,0 +1,656 @@
+// traverse2pt.cu -- dual-tree 2-point traversal and per-pair accumulation on sm_103a.
+//
+// Semantics follow the reference exactly:
+//   BaseCorr2::process (auto src/Corr2.cpp:146-205, cross 207-288), process2 (290-306),
+//   process11 (308-389), directProcess11 (476-525), finishProcess + DirectHelper (394-566),
+//   BinTypeHelper<Log> (include/BinType.h:40-156), CalcSplitSq (include/Split.h:82-101),
+//   MetricHelper<Euclidean> / <Arc> (include/Metric.h:119-258, 658-700) and the spin-2
+//   projections (include/ProjectHelper.h:45-47, 84-136, 272-388).
+//
+// GB300 design:
+//   * Work items are cell pairs (plus "self" items for process2).  A persistent grid of
+//     warps takes 32 items at a time; each lane evaluates one item and pushes 0, 2, 3 or 4
+//     children onto its warp's stack (LIFO, so the warp walks depth first and the stack
+//     stays shallow).  Roots are the top-level pairs, generated on the fly from a counter.
+//   * Decisions are taken in FP32 on cells stored as float hi/lo positions (differences of
+//     nearby cells keep ~48 bits).  Every comparison carries an error bound; when a value
+//     falls inside it, the whole decision for that pair is redone in FP64 from the FP64
+//     centres with the reference's formulas.  So accept/split/bin choices are the
+//     reference's, while almost all work runs at FP32 rate (GB300's FP64 rate is ~1/64).
+//   * Accepted pairs are accumulated into per-warp FP32 shared-memory bins that are flushed
+//     every few iterations into per-warp FP64 totals; npairs is an exact 64-bit integer.
+//   * When the roots run out and many warps are idle, warps with deep stacks spill them to
+//     a global list that the next launch redistributes (no inter-warp waiting anywhere).
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+#include <vector>
+
+#include "tc_internal.cuh"
+#include "tc_host.hpp"
+#include "traverse2pt.hpp"
+
+namespace tc {
+
+static constexpr int TB = 256;        // threads per traversal block
+static constexpr int WPB = TB / 32;   // warps per block
+static constexpr int FLUSH = 8;       // iterations between FP32 -> FP64 flushes
+
+// ---------------------------------------------------------------------------------------
+// Packing of the traversal records.
+
+__global__ void k_pack_cells(int ncap, Cells C, TCell* out)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ncap) return;
+    double x = C.x[i], y = C.y[i], z = C.z[i];
+    float xh = float(x), yh = float(y), zh = float(z);
+    TCell t;
+    t.a = make_float4(xh, yh, zh, C.size[i]);
+    t.b = make_float4(float(x - double(xh)), float(y - double(yh)), float(z - double(zh)), C.w[i]);
+    t.c = make_float4(C.d1[i], C.d2[i], __int_as_float(C.n[i]), __int_as_float(C.left[i]));
+    t.d = make_float4(__int_as_float(C.right[i]), 0.f, 0.f, 0.f);
+    out[i] = t;
+}
+
+void launch_pack_cells(int ncap, const Cells& C, TCell* out, cudaStream_t st)
+{
+    if (ncap <= 0) return;
+    count_launch(); k_pack_cells<<<(ncap + 255) / 256, 256, 0, st>>>(ncap, C, out);
+}
+
+// ---------------------------------------------------------------------------------------
+// Tri-state comparisons.  A value v known up to [lo, hi].
+
+enum : int { NO = 0, YES = 1, UNSURE = 2 };
+
+// Is a > b, given a in [alo, ahi] and b in [blo, bhi]?
+__device__ __forceinline__ int gt3(float alo, float ahi, float blo, float bhi)
+{ return alo > bhi ? YES : (ahi <= blo ? NO : UNSURE); }
+
+// Square of an interval.
+__device__ __forceinline__ void sq_iv(float lo, float hi, float& slo, float& shi)
+{
+    if (lo >= 0.f) { slo = lo * lo; shi = hi * hi; }
+    else if (hi <= 0.f) { slo = hi * hi; shi = lo * lo; }
+    else { slo = 0.f; shi = fmaxf(lo * lo, hi * hi); }
+}
+
+// Slack added to every bound to cover the FP32 rounding of the bound itself.
+__device__ __forceinline__ float LOW(float v) { return v - fabsf(v) * 2e-6f - 1e-30f; }
+__device__ __forceinline__ float HIGH(float v) { return v + fabsf(v) * 2e-6f + 1e-30f; }
+
+struct Decision {
+    int act;         // ACT_*
+    int k;           // bin (accept)
+    float r, logr;   // separation and its log (accept)
+};
+enum : int { ACT_DROP = 0, ACT_ACCEPT = 1, ACT_SPLIT1 = 2, ACT_SPLIT2 = 3, ACT_SPLIT12 = 4,
+             ACT_UNSURE = 5 };
+
+// FP32 decision of process11 for one cell pair; ACT_UNSURE when any comparison is within
+// its error bound.
+__device__ __forceinline__ Decision decide32(const TravParams& T, float rsq, float s1, float s2,
+                                             bool arc)
+{
+    Decision D;
+    D.act = ACT_UNSURE; D.k = -1; D.r = 0.f; D.logr = 0.f;
+    // Error bounds: rsq (relative), s1+s2 (relative).
+    const float ER = arc ? 2e-5f : 1e-5f;
+    const float ES = 1e-6f;
+    const float Rlo = rsq * (1.f - ER), Rhi = rsq * (1.f + ER);
+    const float s1ps2 = s1 + s2;
+    const float Slo = s1ps2 * (1.f - ES), Shi = s1ps2 * (1.f + ES);
+
+    // tooSmallDist, include/BinType.h:70-76.
+    {
+        int c1 = gt3(T.fminsepsq * (1.f - 1e-7f), T.fminsepsq * (1.f + 1e-7f), Rlo, Rhi);  // rsq < minsepsq
+        int c2 = gt3(T.fminsep, T.fminsep, Slo, Shi);                                    // s1ps2 < minsep
+        float xlo = T.fminsep - Shi, xhi = T.fminsep - Slo, x2lo, x2hi;
+        sq_iv(xlo, xhi, x2lo, x2hi);
+        int c3 = gt3(LOW(x2lo), HIGH(x2hi), Rlo, Rhi);                                  // rsq < (minsep-s)^2
+        if (c1 == YES && c2 == YES && c3 == YES) { D.act = ACT_DROP; return D; }
+        if (!(c1 == NO || c2 == NO || c3 == NO)) return D;
+    }
+    // tooLargeDist, include/BinType.h:77-82.
+    {
+        int c1b = gt3(T.fmaxsepsq * (1.f - 1e-7f), T.fmaxsepsq * (1.f + 1e-7f), Rlo, Rhi);
+        // rsq >= maxsepsq  <=>  !(maxsepsq > rsq)
+        int ge1 = c1b == YES ? NO : (c1b == NO ? YES : UNSURE);
+        float ylo = T.fmaxsep + Slo, yhi = T.fmaxsep + Shi;
+        float y2lo = LOW(ylo * ylo), y2hi = HIGH(yhi * yhi);
+        int lt2 = gt3(y2lo, y2hi, Rlo, Rhi);   // (maxsep+s)^2 > rsq
+        int ge2 = lt2 == YES ? NO : (lt2 == NO ? YES : UNSURE);
+        if (ge1 == YES && ge2 == YES) { D.act = ACT_DROP; return D; }
+        if (!(ge1 == NO || ge2 == NO)) return D;
+    }
+    // singleBin, include/BinType.h:93-151.
+    int sb = UNSURE;
+    int k = -1;
+    if (s1ps2 == 0.f) {
+        sb = YES;
+    } else {
+        const float S2lo = LOW(Slo * Slo), S2hi = HIGH(Shi * Shi);
+        int t1 = gt3(S2lo, S2hi, LOW(T.fasq * Rlo), HIGH(T.fasq * Rhi));
+        if (t1 == UNSURE) return D;
+        if (t1 == YES) sb = NO;
+        else {
+            int t2 = gt3(S2lo, S2hi, LOW(T.fbsq * Rlo), HIGH(T.fbsq * Rhi));   // > bsq*rsq
+            if (t2 == UNSURE) return D;
+            if (t2 == NO) sb = YES;
+            else {
+                int t3 = gt3(S2lo, S2hi, LOW(T.fbb * Rlo), HIGH(T.fbb * Rhi));
+                if (t3 == UNSURE) return D;
+                if (t3 == YES) sb = NO;
+                else {
+                    float lr = 0.5f * logf(rsq * T.finvminsepsq);
+                    float kk = lr * T.finvbinsize;
+                    float ek = (0.5f * ER + 1e-6f * (1.f + fabsf(lr))) * T.finvbinsize + 1e-6f;
+                    float klo = kk - ek, khi = kk + ek;
+                    // int(kk) truncates toward zero, as in the reference (kk < 0 is possible).
+                    float ik = truncf(kk);
+                    if (truncf(klo) != ik || truncf(khi) != ik) return D;
+                    float flo = klo - ik, fhi = khi - ik;
+                    float mlo = fminf(flo, 1.f - fhi), mhi = fminf(fhi, 1.f - flo);
+                    float alo = mlo * T.fbinsize + T.fb, ahi = mhi * T.fbinsize + T.fb;
+                    float a2lo, a2hi;
+                    sq_iv(alo, ahi, a2lo, a2hi);
+                    int t4 = gt3(S2lo, S2hi, LOW(a2lo * Rlo), HIGH(a2hi * Rhi));
+                    if (t4 == UNSURE) return D;
+                    if (t4 == YES) sb = NO;
+                    else {
+                        float zlo = flo * T.fbinsize + T.fb - S2hi / Rlo;
+                        float zhi = fhi * T.fbinsize + T.fb - S2lo / Rhi;
+                        float z2lo, z2hi;
+                        sq_iv(LOW(zlo) - 1e-7f, HIGH(zhi) + 1e-7f, z2lo, z2hi);
+                        int t5 = gt3(S2lo, S2hi, LOW(z2lo * Rlo), HIGH(z2hi * Rhi));
+                        if (t5 == UNSURE) return D;
+                        if (t5 == YES) sb = NO;
+                        else { sb = YES; k = int(ik); }
+                    }
+                }
+            }
+        }
+    }
+    if (sb == YES) {
+        // isRSqInRange, include/BinType.h:61-66: minsepsq <= rsq < maxsepsq.
+        int below = gt3(T.fminsepsq * (1.f - 1e-7f), T.fminsepsq * (1.f + 1e-7f), Rlo, Rhi);
+        int above = gt3(T.fmaxsepsq * (1.f - 1e-7f), T.fmaxsepsq * (1.f + 1e-7f), Rlo, Rhi);
+        if (below == UNSURE || above == UNSURE) return D;
+        if (below == YES || above == NO) { D.act = ACT_DROP; return D; }
+        float r = arc ? 0.f : sqrtf(rsq);
+        float lr = 0.5f * logf(rsq * T.finvminsepsq);
+        if (k < 0) {
+            // directProcess11, src/Corr2.cpp:492-514.
+            float kk = lr * T.finvbinsize;
+            float ek = (0.5f * ER + 1e-6f * (1.f + fabsf(lr))) * T.finvbinsize + 1e-6f;
+            float ik = truncf(kk);
+            if (truncf(kk - ek) != ik || truncf(kk + ek) != ik) return D;
+            k = int(ik);
+        }
+        if (k == T.nbins) k = T.nbins - 1;
+        if (k < 0 || k >= T.nbins) return D;
+        D.act = ACT_ACCEPT;
+        D.k = k;
+        D.r = r;
+        D.logr = lr + T.flogminsep;
+        return D;
+    }
+    // CalcSplitSq with bsq_eff = rsq*min(bsq,asq), include/Split.h:82-101 and
+    // getEffectiveBSq, include/BinType.h:50-51.
+    bool sw = s2 > s1;
+    float big = sw ? s2 : s1, sml = sw ? s1 : s2;
+    int which;
+    if (big > 2.f * sml) {
+        which = 1;
+    } else {
+        float m2lo = LOW(sml * sml), m2hi = HIGH(sml * sml);
+        int t = gt3(m2lo, m2hi, LOW(0.3422f * T.fmineff * Rlo), HIGH(0.3422f * T.fmineff * Rhi));
+        if (t == UNSURE) return D;
+        which = (t == YES) ? 2 : 1;
+    }
+    D.act = which == 2 ? ACT_SPLIT12 : (sw ? ACT_SPLIT2 : ACT_SPLIT1);
+    return D;
+}
+
+// FP64 decision of process11, the reference's arithmetic on the FP64 centres.
+__device__ Decision decide64(const TravParams& T, double dsq, double s1, double s2)
+{
+    Decision D;
+    D.act = ACT_DROP; D.k = -1; D.r = 0.f; D.logr = 0.f;
+    double rsq = dsq;
+    if (T.metric == ARC) {
+        double L = sqrt(dsq);
+        double th = 2. * asin(L / 2.);
+        rsq = th * th;
+    }
+    const double s1ps2 = s1 + s2;
+    if (rsq < T.minsepsq && s1ps2 < T.minsep && rsq < (T.minsep - s1ps2) * (T.minsep - s1ps2))
+        return D;
+    if (rsq >= T.maxsepsq && rsq >= (T.maxsep + s1ps2) * (T.maxsep + s1ps2)) return D;
+    int k = -1;
+    double r = 0., logr = 0.;
+    bool single = false;
+    if (s1ps2 == 0.) {
+        single = true;
+    } else {
+        double s1ps2sq = s1ps2 * s1ps2;
+        if (s1ps2sq > T.asq * rsq) single = false;
+        else if (s1ps2sq <= T.bsq * rsq) single = true;
+        else if (s1ps2sq > 0.25 * (T.binsize + T.b) * (T.binsize + T.b) * rsq) single = false;
+        else {
+            logr = 0.5 * log(rsq);
+            double kk = (logr - T.logminsep) / T.binsize;
+            int ik = int(kk);
+            double frackk = kk - ik;
+            double f = fmin(frackk, 1. - frackk);
+            double t4 = f * T.binsize + T.b;
+            double t5 = frackk * T.binsize + T.b - s1ps2sq / rsq;
+            if (s1ps2sq > t4 * t4 * rsq) single = false;
+            else if (s1ps2sq > t5 * t5 * rsq) single = false;
+            else { single = true; k = ik; r = sqrt(rsq); }
+        }
+    }
+    if (single) {
+        if (!(rsq >= T.minsepsq && rsq < T.maxsepsq)) return D;
+        if (k < 0) {
+            r = sqrt(rsq);
+            logr = log(r);
+            k = int((logr - T.logminsep) / T.binsize);
+        }
+        if (k == T.nbins) --k;
+        if (k < 0 || k >= T.nbins) return D;
+        D.act = ACT_ACCEPT; D.k = k; D.r = float(r); D.logr = float(logr);
+        return D;
+    }
+    double bsq_eff = rsq * fmin(T.bsq, T.asq);
+    bool sw = s2 > s1;
+    double big = sw ? s2 : s1, sml = sw ? s1 : s2;
+    bool both = !(big > 2. * sml) && (sml * sml > 0.3422 * bsq_eff);
+    D.act = both ? ACT_SPLIT12 : (sw ? ACT_SPLIT2 : ACT_SPLIT1);
+    return D;
+}
+
+// spin-2 rotation conj(r^2)/|r|^2 (calculate_expmsialpha<2>, include/ProjectHelper.h:45-47).
+__device__ __forceinline__ void expm2i(float rx, float ry, float& er, float& ei)
+{
+    float n = rx * rx + ry * ry;
+    float inv = n > 0.f ? 1.f / n : 1.f;
+    er = (rx * rx - ry * ry) * inv;
+    ei = -2.f * rx * ry * inv;
+}
+
+__device__ __forceinline__ void cmul(float ar, float ai, float br, float bi, float& cr, float& ci)
+{
+    cr = ar * br - ai * bi;
+    ci = ar * bi + ai * br;
+}
+
+// GG projection for ThreeD coordinates in FP64 (positions normalised first,
+// include/ProjectHelper.h:570-584).
+__device__ void project3d64(const TravParams& T, int i, int j, float& g1r, float& g1i,
+                            float& g2r, float& g2i)
+{
+    double x1 = T.x1[i], y1 = T.y1[i], z1 = T.z1[i];
+    double x2 = T.x2[j], y2 = T.y2[j], z2 = T.z2[j];
+    double n1 = sqrt(x1 * x1 + y1 * y1 + z1 * z1), n2 = sqrt(x2 * x2 + y2 * y2 + z2 * z2);
+    if (n1 == 0.) { x1 = 1.; y1 = 0.; z1 = 0.; } else { x1 /= n1; y1 /= n1; z1 /= n1; }
+    if (n2 == 0.) { x2 = 1.; y2 = 0.; z2 = 0.; } else { x2 /= n2; y2 /= n2; z2 /= n2; }
+    double dsq = (x1 - x2) * (x1 - x2) + (y1 - y2) * (y1 - y2) + (z1 - z2) * (z1 - z2);
+    double ca = (z1 - z2) + 0.5 * z2 * dsq, sa = y1 * x2 - x1 * y2;   // direction at p2
+    double cb = (z2 - z1) + 0.5 * z1 * dsq, sb = y2 * x1 - x2 * y1;   // direction at p1
+    double ax = sa, ay = -ca, bx = sb, by = -cb;
+    double na = ax * ax + ay * ay, nb = bx * bx + by * by;
+    if (!(na > 0.)) na = 1.;
+    if (!(nb > 0.)) nb = 1.;
+    double e2r = (ax * ax - ay * ay) / na, e2i = -2. * ax * ay / na;
+    double e1r = (bx * bx - by * by) / nb, e1i = -2. * bx * by / nb;
+    double a = g2r, b = g2i;
+    g2r = float(a * e2r - b * e2i); g2i = float(a * e2i + b * e2r);
+    a = g1r; b = g1i;
+    g1r = float(a * e1r - b * e1i); g1i = float(a * e1i + b * e1r);
+}
+
+// ---------------------------------------------------------------------------------------
+// Root generation.
+
+__device__ __forceinline__ int2 make_root(const TravParams& T, long long g)
+{
+    if (g >= T.ngen) return T.in_tasks[g - T.ngen];
+    if (T.autoc) {
+        // Row i of the upper triangle (self + pairs j>i) starts at i*n - i*(i-1)/2.
+        long long n = T.ntop1;
+        double b = 2.0 * n + 1.0;
+        long long i = (long long)((b - sqrt(b * b - 8.0 * (double)g)) * 0.5);
+        if (i < 0) i = 0;
+        if (i > n - 1) i = n - 1;
+        while (i > 0 && i * n - i * (i - 1) / 2 > g) --i;
+        while (i + 1 < n && (i + 1) * n - (i + 1) * i / 2 <= g) ++i;
+        long long j = g - (i * n - i * (i - 1) / 2) + i;
+        if (j == i) return make_int2(T.tops1[i], -1);
+        return make_int2(T.tops1[i], T.tops1[j]);
+    }
+    long long i = g / T.ntop2, j = g - i * T.ntop2;
+    return make_int2(T.tops1[i], T.tops2[j]);
+}
+
+// ---------------------------------------------------------------------------------------
+// The traversal kernel.
+
+__device__ __forceinline__ void flush_bins(const TravParams& T, float* fb,
+                                           unsigned long long* np, int gw, int lane)
+{
+    const int nq = T.nqf, nb = T.nbins;
+    double* wa = T.wacc + (size_t)gw * nq * nb;
+    for (int q = lane; q < nq * nb; q += 32) {
+        float v = fb[q];
+        if (v != 0.f) { wa[q] += (double)v; fb[q] = 0.f; }
+    }
+    if (!T.quick) {
+        unsigned long long* wn = T.wnp + (size_t)gw * nb;
+        for (int q = lane; q < nb; q += 32) {
+            unsigned long long v = np[q];
+            if (v) { wn[q] += v; np[q] = 0ull; }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(TB) k_traverse(TravParams T)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int gw = blockIdx.x * WPB + wib;
+    const int nq = T.nqf, nb = T.nbins;
+    // Per-warp bins: nb npairs (u64), then nq*nb floats.
+    const size_t wbytes = (size_t)nb * 8 + (size_t)nq * nb * 4;
+    unsigned long long* np = (unsigned long long*)(smem + wib * ((wbytes + 15) & ~(size_t)15));
+    float* fb = (float*)(np + nb);
+    for (int q = lane; q < nb; q += 32) np[q] = 0ull;
+    for (int q = lane; q < nq * nb; q += 32) fb[q] = 0.f;
+    __syncwarp();
+
+    int2* stk = T.stacks + (size_t)gw * T.stack_cap;
+    int sp = 0;
+    bool roots_done = false;
+    int iter = 0;
+    long long n_eval = 0, n_acc = 0, n_esc = 0;
+    const long long total_roots = T.ngen + T.nin;
+    const bool arc = (T.metric == ARC);
+    const bool flat = (T.coords == FLAT);
+
+    while (true) {
+        if (sp < 32 && !roots_done) {
+            unsigned long long base = 0;
+            if (lane == 0) base = atomicAdd(T.root_next, 32ull);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if ((long long)base >= total_roots) {
+                roots_done = true;
+            } else {
+                long long g = (long long)base + lane;
+                bool ok = g < total_roots;
+                int2 t = ok ? make_root(T, g) : make_int2(0, 0);
+                unsigned m = __ballot_sync(0xffffffffu, ok);
+                if (ok) stk[sp + __popc(m & ((1u << lane) - 1u))] = t;
+                sp += __popc(m);
+                __syncwarp();
+            }
+        }
+        if (sp == 0) {
+            if (roots_done) break;
+            continue;
+        }
+        if (roots_done && (iter & 7) == 0 && sp > 64) {
+            // Spill when many warps are idle, so the next launch can spread this stack.
+            int idle = 0;
+            if (lane == 0) idle = *(volatile int*)T.idle;
+            idle = __shfl_sync(0xffffffffu, idle, 0);
+            if (idle * 4 > T.nwarps) {
+                unsigned long long o = 0;
+                if (lane == 0) o = atomicAdd(T.nout, (unsigned long long)sp);
+                o = __shfl_sync(0xffffffffu, o, 0);
+                if ((long long)(o + sp) > T.out_cap) {
+                    if (lane == 0) atomicCAS(T.err, 0, DEV_SPILL_OVERFLOW);
+                } else {
+                    for (int q = lane; q < sp; q += 32) T.out_tasks[o + q] = stk[q];
+                }
+                sp = 0;
+                break;
+            }
+        }
+        // Keep room for the children of 32 items: spill the bottom of a full stack.
+        if (sp + 160 > T.stack_cap) {
+            const int keep = 256;
+            int mv = sp - keep;
+            unsigned long long o = 0;
+            if (lane == 0) o = atomicAdd(T.nout, (unsigned long long)mv);
+            o = __shfl_sync(0xffffffffu, o, 0);
+            if ((long long)(o + mv) > T.out_cap) {
+                if (lane == 0) atomicCAS(T.err, 0, DEV_SPILL_OVERFLOW);
+                break;
+            }
+            for (int q = lane; q < mv; q += 32) T.out_tasks[o + q] = stk[q];
+            __syncwarp();
+            for (int q = lane; q < keep; q += 32) {
+                int2 v = stk[mv + q];
+                __syncwarp();
+                stk[q] = v;
+            }
+            sp = keep;
+            __syncwarp();
+        }
+        if (iter >= (1 << 30)) {   // last-resort bound; a valid tree never gets here
+            if (lane == 0) atomicCAS(T.err, 0, DEV_STACK_OVERFLOW);
+            break;
+        }
+        const int nt = sp < 32 ? sp : 32;
+        sp -= nt;
+        int2 task = make_int2(0, 0);
+        const bool has = lane < nt;
+        if (has) task = stk[sp + lane];
+        __syncwarp();
+        ++iter;
+
+        int nch = 0;
+        int2 ch[4];
+        if (has) {
+            ++n_eval;
+            const int i = task.x;
+            if (task.y < 0) {
+                // process2, src/Corr2.cpp:290-306.
+                const TCell A = T.c1[i];
+                const float w = A.b.w, s = A.a.w;
+                if (w != 0.f && !((double)s <= T.halfminsep)) {
+                    int L = __float_as_int(A.c.w), R = __float_as_int(A.d.x);
+                    if (L < 0 || R < 0) {
+                        atomicCAS(T.err, 0, DEV_BAD_CHILD);
+                    } else {
+                        ch[0] = make_int2(L, -1); ch[1] = make_int2(R, -1); ch[2] = make_int2(L, R);
+                        nch = 3;
+                    }
+                }
+            } else {
+                const int j = task.y;
+                const TCell A = T.c1[i];
+                const TCell B = T.c2[j];
+                if (A.b.w != 0.f && B.b.w != 0.f) {
+                    const float dx = (A.a.x - B.a.x) + (A.b.x - B.b.x);
+                    const float dy = (A.a.y - B.a.y) + (A.b.y - B.b.y);
+                    const float dz = flat ? 0.f : (A.a.z - B.a.z) + (A.b.z - B.b.z);
+                    const float dsq = dx * dx + dy * dy + dz * dz;
+                    float rsq = dsq, theta = 0.f;
+                    if (arc) {
+                        theta = 2.f * asinf(0.5f * sqrtf(dsq));
+                        rsq = theta * theta;
+                    }
+                    const float s1 = A.a.w, s2 = B.a.w;
+                    Decision D = decide32(T, rsq, s1, s2, arc);
+                    if (D.act == ACT_UNSURE) {
+                        ++n_esc;
+                        double ddx = T.x1[i] - T.x2[j], ddy = T.y1[i] - T.y2[j];
+                        double ddsq = ddx * ddx + ddy * ddy;
+                        if (!flat) { double ddz = T.z1[i] - T.z2[j]; ddsq += ddz * ddz; }
+                        D = decide64(T, ddsq, (double)s1, (double)s2);
+                        if (D.act == ACT_ACCEPT && arc) theta = D.r;
+                    } else if (D.act == ACT_ACCEPT && arc) {
+                        D.r = theta;
+                    }
+                    if (D.act == ACT_ACCEPT) {
+                        ++n_acc;
+                        const int k = D.k;
+                        const float ww = A.b.w * B.b.w;
+                        atomicAdd(&fb[k], ww);
+                        if (!T.quick) {
+                            unsigned long long nn = (unsigned long long)__float_as_int(A.c.z) *
+                                                    (unsigned long long)__float_as_int(B.c.z);
+                            atomicAdd(&np[k], nn);
+                            atomicAdd(&fb[nb + k], ww * D.r);
+                            atomicAdd(&fb[2 * nb + k], ww * D.logr);
+                        }
+                        if (T.dkind == DK) {
+                            atomicAdd(&fb[3 * nb + k], A.c.x * B.c.x);
+                        } else if (T.dkind == DG) {
+                            float g1r = A.c.x, g1i = A.c.y, g2r = B.c.x, g2i = B.c.y;
+                            if (flat) {
+                                // ProjectHelper<Flat>::Project: r = p2 - p1 (ProjectHelper.h:126-136)
+                                float er, ei;
+                                expm2i(-dx, -dy, er, ei);
+                                cmul(g1r, g1i, er, ei, g1r, g1i);
+                                cmul(g2r, g2i, er, ei, g2r, g2i);
+                            } else if (T.coords == SPHERE) {
+                                // ProjectHelper<Sphere>::Project(c1,c2,z1,z2), ProjectHelper.h:370-388,
+                                // with the direction terms written on accurate differences:
+                                // y1*x2 - x1*y2 = x1*dy - y1*dx,  d = p1 - p2.
+                                const float x1 = A.a.x, y1 = A.a.y, z1 = A.a.z, z2 = B.a.z;
+                                const float sinA = x1 * dy - y1 * dx;
+                                const float cosA = dz + 0.5f * z2 * dsq;
+                                const float cosB = -dz + 0.5f * z1 * dsq;
+                                float e2r, e2i, e1r, e1i;
+                                expm2i(sinA, -cosA, e2r, e2i);
+                                expm2i(-sinA, -cosB, e1r, e1i);
+                                cmul(g2r, g2i, e2r, e2i, g2r, g2i);
+                                cmul(g1r, g1i, e1r, e1i, g1r, g1i);
+                            } else {
+                                project3d64(T, i, j, g1r, g1i, g2r, g2i);
+                            }
+                            // both_complex_prod(g2, g1), ProjectHelper.h:84-101.
+                            const float rr = g2r * g1r, ri = g2r * g1i, ir = g2i * g1r, ii = g2i * g1i;
+                            atomicAdd(&fb[3 * nb + k], rr + ii);   // xip
+                            atomicAdd(&fb[4 * nb + k], ri - ir);
+                            atomicAdd(&fb[5 * nb + k], rr - ii);   // xim
+                            atomicAdd(&fb[6 * nb + k], ri + ir);
+                        }
+                    } else if (D.act != ACT_DROP) {
+                        const int L1 = __float_as_int(A.c.w), R1 = __float_as_int(A.d.x);
+                        const int L2 = __float_as_int(B.c.w), R2 = __float_as_int(B.d.x);
+                        if (D.act == ACT_SPLIT12) {
+                            if (L1 < 0 || L2 < 0) atomicCAS(T.err, 0, DEV_BAD_CHILD);
+                            else {
+                                ch[0] = make_int2(L1, L2); ch[1] = make_int2(L1, R2);
+                                ch[2] = make_int2(R1, L2); ch[3] = make_int2(R1, R2);
+                                nch = 4;
+                            }
+                        } else if (D.act == ACT_SPLIT1) {
+                            if (L1 < 0) atomicCAS(T.err, 0, DEV_BAD_CHILD);
+                            else { ch[0] = make_int2(L1, j); ch[1] = make_int2(R1, j); nch = 2; }
+                        } else {
+                            if (L2 < 0) atomicCAS(T.err, 0, DEV_BAD_CHILD);
+                            else { ch[0] = make_int2(i, L2); ch[1] = make_int2(i, R2); nch = 2; }
+                        }
+                    }
+                }
+            }
+        }
+        // Push the children: exclusive warp scan of the counts.
+        int off = nch;
+        for (int o = 1; o < 32; o <<= 1) {
+            int v = __shfl_up_sync(0xffffffffu, off, o);
+            if (lane >= o) off += v;
+        }
+        const int tot = __shfl_sync(0xffffffffu, off, 31);
+        off -= nch;
+        for (int c = 0; c < nch; ++c) stk[sp + off + c] = ch[c];
+        sp += tot;
+        __syncwarp();
+        if ((iter % FLUSH) == 0) {
+            flush_bins(T, fb, np, gw, lane);
+            __syncwarp();
+        }
+    }
+    __syncwarp();
+    flush_bins(T, fb, np, gw, lane);
+    // Counters.
+    for (int o = 16; o > 0; o >>= 1) {
+        n_eval += __shfl_xor_sync(0xffffffffu, n_eval, o);
+        n_acc += __shfl_xor_sync(0xffffffffu, n_acc, o);
+        n_esc += __shfl_xor_sync(0xffffffffu, n_esc, o);
+    }
+    if (lane == 0) {
+        atomicAdd(&T.counters[0], (unsigned long long)n_eval);
+        atomicAdd(&T.counters[1], (unsigned long long)n_acc);
+        atomicAdd(&T.counters[2], (unsigned long long)n_esc);
+        atomicAdd(T.idle, 1);
+    }
+}
+
+// Sum of the per-warp totals in a fixed order: out[q*nb+k] (double), outnp[k] (u64).
+__global__ void k_reduce_acc(int nwarps, int nq, int nb, const double* wacc,
+                             const unsigned long long* wnp, double* out,
+                             unsigned long long* outnp)
+{
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < nq * nb) {
+        double s = 0.;
+        for (int w = 0; w < nwarps; ++w) s += wacc[(size_t)w * nq * nb + q];
+        out[q] = s;
+    }
+    if (q < nb) {
+        unsigned long long s = 0;
+        for (int w = 0; w < nwarps; ++w) s += wnp[(size_t)w * nb + q];
+        outnp[q] = s;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Host side.
+
+size_t traverse_smem_bytes(int nq, int nb)
+{
+    size_t wbytes = (size_t)nb * 8 + (size_t)nq * nb * 4;
+    wbytes = (wbytes + 15) & ~(size_t)15;
+    return wbytes * WPB;
+}
+
+int traverse_grid(int nq, int nb, int* blocks, int* nwarps)
+{
+    int dev = 0, nsm = 0, per = 0;
+    TC_CU(cudaGetDevice(&dev));
+    TC_CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    size_t sm = traverse_smem_bytes(nq, nb);
+    if (sm > 48 * 1024)
+        TC_CU(cudaFuncSetAttribute(k_traverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    TC_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_traverse, TB, sm));
+    if (per < 1) per = 1;
+    *blocks = nsm * per;
+    *nwarps = *blocks * WPB;
+    return 0;
+}
+
+int launch_traverse(const TravParams& T, int blocks, cudaStream_t st)
+{
+    size_t sm = traverse_smem_bytes(T.nqf, T.nbins);
+    count_launch(); k_traverse<<<blocks, TB, sm, st>>>(T);
+    TC_CU(cudaGetLastError());
+    return 0;
+}
+
+int launch_reduce(int nwarps, int nq, int nb, const double* wacc, const unsigned long long* wnp,
+                  double* out, unsigned long long* outnp, cudaStream_t st)
+{
+    int n = nq * nb > nb ? nq * nb : nb;
+    count_launch(); k_reduce_acc<<<(n + 127) / 128, 128, 0, st>>>(nwarps, nq, nb, wacc, wnp, out, outnp);
+    TC_CU(cudaGetLastError());
+    return 0;
+}
+
+}  // namespace tc
