@@ -61,6 +61,12 @@ def lib():
                                              ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                              ctypes.c_void_p, ctypes.c_long, ctypes.c_long,
                                              ctypes.c_int] + [dp] * 8
+        L.orc_corr3_multipole_auto.restype = ctypes.c_int
+        L.orc_corr3_multipole_auto.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                               ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                               ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                               ctypes.c_void_p, ctypes.c_int,
+                                               ctypes.POINTER(dp)] + [dp] * 7
         L.orc_last_accepted.restype = ctypes.c_longlong
         L.orc_last_accepted.argtypes = []
         L.orc_max_threads.restype = ctypes.c_int
@@ -165,3 +171,23 @@ def process(dtype, metric, bins, f1, f2=None, quick=False, nthreads=0, rows=None
 
 def max_threads():
     return lib().orc_max_threads()
+
+
+MP_KEYS = ("gam0r", "gam0i", "gam1r", "gam1i", "gam2r", "gam2i", "gam3r", "gam3i",
+           "meand2", "meanlogd2", "meand3", "meanlogd3", "weight", "weight_im", "ntri")
+
+
+def multipole(metric, bins, max_n, f, quick=False, nthreads=0):
+    """The oracle's GGG LogMultipole auto-correlation; dict of (nbins, nbins, 2*max_n+1)
+    arrays (zeta0..7 as gam0r..gam3i, meand2/3, meanlogd2/3, weight, weight_im, ntri)."""
+    nb = bins["nbins"]
+    shape = (nb, nb, 2 * max_n + 1)
+    out = {k: np.zeros(shape) for k in MP_KEYS}
+    gam = (ctypes.POINTER(ctypes.c_double) * 8)(*[_p(out[k]) for k in MP_KEYS[:8]])
+    rc = lib().orc_corr3_multipole_auto(METRICS[metric], int(bool(quick)), bins["min_sep"],
+                                        bins["max_sep"], nb, bins["bin_size"], bins["b"],
+                                        bins["a"], int(max_n), f.h, int(nthreads), gam,
+                                        *[_p(out[k]) for k in MP_KEYS[8:]])
+    if rc:
+        raise ValueError("multipole needs a G field")
+    return out

@@ -54,6 +54,11 @@ struct Node {
     float d1 = 0.f, d2 = 0.f;
     int left = -1, right = -1;  // -1 for leaves
     long start = 0, end = 0;
+    // Sums over the cell's leaves used by the multipole ww corrections:
+    // calculateSumWSq / calculateSumWZSq / calculateSumAbsWZSq (src/Cell.cpp:138-168).
+    double sumwsq = 0.;
+    std::complex<double> sumwzsq = 0.;
+    double sumabswzsq = 0.;
 };
 
 struct Field {
@@ -247,6 +252,28 @@ int build_cell(Field& f, double minsizesq, long start, long end, const Node* dat
     return id;
 }
 
+// The leaf sums of a subtree, bottom up: a leaf (size 0 or one point) contributes
+// w^2, wz^2, |wz|^2; a parent is left + right, as the reference's recursion adds them.
+void leaf_sums(Field& f, int id)
+{
+    Node& nd = f.nodes[id];
+    if (nd.size == 0.f || nd.n == 1 || nd.left < 0) {
+        double w = nd.w;
+        std::complex<double> wz(nd.d1, nd.d2);
+        nd.sumwsq = w * w;
+        nd.sumwzsq = wz * wz;
+        nd.sumabswzsq = std::norm(wz);
+        return;
+    }
+    leaf_sums(f, nd.left);
+    leaf_sums(f, nd.right);
+    const Node& L = f.nodes[nd.left];
+    const Node& R = f.nodes[nd.right];
+    nd.sumwsq = L.sumwsq + R.sumwsq;
+    nd.sumwzsq = L.sumwzsq + R.sumwzsq;
+    nd.sumabswzsq = L.sumabswzsq + R.sumabswzsq;
+}
+
 struct TopInfo { Node data; double sizesq; long start, end; };
 
 // SetupTopLevelCells, src/Field.cpp:27-81.
@@ -294,6 +321,7 @@ void build_cells(Field& f)
         f.tops[i] = build_cell(f, minsizesq, tops[i].start, tops[i].end,
                                (tops[i].end - tops[i].start > 1) ? &tops[i].data : nullptr,
                                tops[i].sizesq, next);
+        leaf_sums(f, f.tops[i]);
     }
 }
 
@@ -506,6 +534,295 @@ Params make_params(int dtype, int coords, int metric, int quick, double minsep, 
     return P;
 }
 
+
+// ---------------------------------------------------------------------------------------
+// 3-point multipole algorithm for GGG, LogMultipole auto-correlation
+// (BaseCorr3::multipole, src/Corr3.cpp:1124-1175, and the functions it calls).
+
+struct Out3 {
+    int nbins, maxn, size;
+    std::vector<double> gam[8];          // gam0r, gam0i, gam1r, gam1i, gam2r, gam2i, gam3r, gam3i
+    std::vector<double> meand2, meanlogd2, meand3, meanlogd3, weight, weight_im, ntri;
+    Out3(int nb, int mn) : nbins(nb), maxn(mn), size(nb * nb * (2 * mn + 1))
+    {
+        for (auto& g : gam) g.assign(size, 0.);
+        meand2.assign(size, 0.); meanlogd2.assign(size, 0.); meand3.assign(size, 0.);
+        meanlogd3.assign(size, 0.); weight.assign(size, 0.); weight_im.assign(size, 0.);
+        ntri.assign(size, 0.);
+    }
+    void add(const Out3& o)
+    {
+        for (int q = 0; q < 8; ++q) for (int i = 0; i < size; ++i) gam[q][i] += o.gam[q][i];
+        for (int i = 0; i < size; ++i) {
+            meand2[i] += o.meand2[i]; meanlogd2[i] += o.meanlogd2[i];
+            meand3[i] += o.meand3[i]; meanlogd3[i] += o.meanlogd3[i];
+            weight[i] += o.weight[i]; weight_im[i] += o.weight_im[i]; ntri[i] += o.ntri[i];
+        }
+    }
+};
+
+// MultipoleScratch<GData> with ww = true, buffer = 1 (include/MultipoleScratch.h:36-125,
+// 296-383; Corr3::getMP2, src/Corr3.cpp:1307-1313).
+struct MPS {
+    int nbins, maxn;
+    std::vector<cd> Wn, Gn, gg0, gg1, gg2;
+    std::vector<double> npairs, sumw, sumwr, sumwlogr, sumww, sumwwr, sumwwlogr;
+    MPS(int nb, int mn) : nbins(nb), maxn(mn) { clear(); }
+    void clear()
+    {
+        Wn.assign(nbins * (maxn + 1), 0.);
+        Gn.assign(nbins * (2 * (maxn + 1) + 1), 0.);
+        gg0.assign(nbins, 0.); gg1.assign(nbins, 0.); gg2.assign(nbins, 0.);
+        npairs.assign(nbins, 0.); sumw.assign(nbins, 0.); sumwr.assign(nbins, 0.);
+        sumwlogr.assign(nbins, 0.); sumww.assign(nbins, 0.); sumwwr.assign(nbins, 0.);
+        sumwwlogr.assign(nbins, 0.);
+    }
+    int widx(int k) const { return k * (maxn + 1); }
+    int gidx(int k) const { return (2 * k + 1) * (maxn + 1) + k; }   // index of n = 0
+    cd G(int k, int n) const { return Gn[gidx(k) + n]; }
+};
+
+// ExpIPhi: Flat (p2-p1)/r (include/ProjectHelper.h:264-266); Sphere: the normalised
+// direction of p2 seen from p1 (526-535); ThreeD normalises the positions first (688-697).
+inline cd exp_i_phi(const Params& P, const Node& c1, const Node& c2, double r)
+{
+    if (P.coords == FLAT) return cd(c2.x - c1.x, c2.y - c1.y) / r;
+    double x1 = c1.x, y1 = c1.y, z1 = c1.z, x2 = c2.x, y2 = c2.y, z2 = c2.z;
+    if (P.coords == THREED) { normalize3(x1, y1, z1); normalize3(x2, y2, z2); }
+    cd z = calc_direction(x2, y2, z2, x1, y1, z1);
+    double n = std::norm(z);
+    if (!(n > 0.)) n = 1.;
+    return z / std::sqrt(n);
+}
+
+// The spin-2 projection of c2's shear onto the c1-c2 line (ProjectWithSq).
+inline cd project2(const Params& P, const Node& c1, const Node& c2)
+{
+    if (P.coords == FLAT) return expmsialpha2(cd(c2.x - c1.x, c2.y - c1.y));
+    double x1 = c1.x, y1 = c1.y, z1 = c1.z, x2 = c2.x, y2 = c2.y, z2 = c2.z;
+    if (P.coords == THREED) { normalize3(x1, y1, z1); normalize3(x2, y2, z2); }
+    return expmsialpha2(calc_direction(x1, y1, z1, x2, y2, z2));
+}
+
+// Corr3::calculateGn + MultipoleScratch<GData>::calculateGn, src/Corr3.cpp:1681-1704,
+// 1767-1828.
+void calculate_gn(const Params& P, const Node& c1, const Node& c2, double r, double logr,
+                  int k, MPS& mp)
+{
+    double n = double(c2.n), w = c2.w;
+    mp.npairs[k] += n;
+    mp.sumw[k] += w;
+    mp.sumwr[k] += w * r;
+    mp.sumwlogr[k] += w * logr;
+    double wsq = c2.sumwsq;
+    mp.sumww[k] += wsq;
+    mp.sumwwr[k] += wsq * r;
+    mp.sumwwlogr[k] += wsq * logr;
+    cd wg(c2.d1, c2.d2);
+    cd z = exp_i_phi(P, c1, c2, r);
+    cd e = project2(P, c1, c2);
+    cd wgsq = c2.sumwzsq;
+    wg *= e;
+    wgsq *= e * e;
+    cd abswgsq = c2.sumabswzsq;
+    cd zsq = z * z;
+    mp.gg0[k] += wgsq * std::conj(zsq);
+    mp.gg1[k] += wgsq * zsq;
+    mp.gg2[k] += abswgsq * std::conj(zsq);
+    int iw = mp.widx(k);
+    mp.Wn[iw] += w;
+    cd t = w;
+    for (int m = 1; m <= mp.maxn; ++m) { t *= z; mp.Wn[iw + m] += t; }
+    int ig = mp.gidx(k);
+    mp.Gn[ig] += wg;
+    t = wg;
+    for (int m = 1; m <= mp.maxn + 1; ++m) { t *= z; mp.Gn[ig + m] += t; }
+    t = wg;
+    cd zc = std::conj(z);
+    for (int m = 1; m <= mp.maxn + 1; ++m) { t *= zc; mp.Gn[ig - m] += t; }
+}
+
+// Corr3::calculateZeta (src/Corr3.cpp:1861-1974) with MultipoleHelper<5>::CalculateZeta
+// (src/Corr3.cpp:2585-2843) for the rows k2 in [kstart, mink_zeta).  Every written entry
+// (a, b, n) with min(a,b) in that range equals the direct Porth et al. product, which is
+// what the reference's unrolled loops compute; the k2 = k3 entries subtract the
+// self-pair sums.
+void calculate_zeta(const Params& P, const Node& c1, const MPS& mp, int kstart, int mink_zeta,
+                    Out3& O)
+{
+    const int nb = mp.nbins, maxn = mp.maxn, nn = 2 * maxn + 1;
+    const double w1 = c1.w;
+    const cd wg1(c1.d1, c1.d2);
+    auto idx = [&](int a, int b, int n) { return (a * nb + b) * nn + maxn + n; };
+    if (!P.quick) {
+        double n1 = double(c1.n);
+        for (int k2 = kstart; k2 < mink_zeta; ++k2) {
+            int i22 = idx(k2, k2, 0);
+            O.ntri[i22] += n1 * mp.npairs[k2] * (mp.npairs[k2] - 1);
+            O.meand2[i22] += w1 * (mp.sumw[k2] * mp.sumwr[k2] - mp.sumwwr[k2]);
+            O.meanlogd2[i22] += w1 * (mp.sumw[k2] * mp.sumwlogr[k2] - mp.sumwwlogr[k2]);
+            O.meand3[i22] += w1 * (mp.sumw[k2] * mp.sumwr[k2] - mp.sumwwr[k2]);
+            O.meanlogd3[i22] += w1 * (mp.sumw[k2] * mp.sumwlogr[k2] - mp.sumwwlogr[k2]);
+            for (int k3 = k2 + 1; k3 < nb; ++k3) {
+                int i23 = idx(k2, k3, 0), i32 = idx(k3, k2, 0);
+                double nnn = n1 * mp.npairs[k2] * mp.npairs[k3];
+                O.ntri[i23] += nnn; O.ntri[i32] += nnn;
+                double ww12 = w1 * mp.sumw[k2], ww13 = w1 * mp.sumw[k3];
+                O.meand2[i23] += ww13 * mp.sumwr[k2]; O.meand3[i32] += ww13 * mp.sumwr[k2];
+                O.meanlogd2[i23] += ww13 * mp.sumwlogr[k2]; O.meanlogd3[i32] += ww13 * mp.sumwlogr[k2];
+                O.meand3[i23] += ww12 * mp.sumwr[k3]; O.meand2[i32] += ww12 * mp.sumwr[k3];
+                O.meanlogd3[i23] += ww12 * mp.sumwlogr[k3]; O.meanlogd2[i32] += ww12 * mp.sumwlogr[k3];
+            }
+        }
+    }
+    // weight (Porth et al. eq. 27): W[a,b,n] = w1 Wn[a,n] conj(Wn[b,n]), Wn[-n] = conj(Wn[n]).
+    auto Wn = [&](int k, int n) { return n >= 0 ? mp.Wn[mp.widx(k) + n] : std::conj(mp.Wn[mp.widx(k) - n]); };
+    for (int k2 = kstart; k2 < mink_zeta; ++k2) {
+        for (int n = -maxn; n <= maxn; ++n)
+            O.weight[idx(k2, k2, n)] += w1 * (std::norm(Wn(k2, n)) - mp.sumww[k2]);
+        for (int k3 = k2 + 1; k3 < nb; ++k3) {
+            for (int n = -maxn; n <= maxn; ++n) {
+                cd a = w1 * Wn(k2, n) * std::conj(Wn(k3, n));
+                O.weight[idx(k2, k3, n)] += a.real(); O.weight_im[idx(k2, k3, n)] += a.imag();
+                cd b = w1 * Wn(k3, n) * std::conj(Wn(k2, n));
+                O.weight[idx(k3, k2, n)] += b.real(); O.weight_im[idx(k3, k2, n)] += b.imag();
+            }
+        }
+    }
+    // gam0..3 (Porth et al. eqs. 21, 23-25 with the projection already applied to G).
+    auto add_gam = [&](int a, int b, bool diag) {
+        for (int n = -maxn; n <= maxn; ++n) {
+            cd g0 = wg1 * mp.G(a, n - 1) * mp.G(b, -n - 1);
+            cd g1 = std::conj(wg1) * mp.G(a, n + 1) * mp.G(b, -n + 1);
+            cd g2 = wg1 * mp.G(a, n - 1) * std::conj(mp.G(b, n + 1));
+            cd g3 = wg1 * std::conj(mp.G(a, -n + 1)) * mp.G(b, -n - 1);
+            if (diag) {
+                g0 -= wg1 * mp.gg0[a];
+                g1 -= std::conj(wg1) * mp.gg1[a];
+                g2 -= wg1 * mp.gg2[a];
+                g3 -= wg1 * mp.gg2[a];
+            }
+            int i = idx(a, b, n);
+            O.gam[0][i] += g0.real(); O.gam[1][i] += g0.imag();
+            O.gam[2][i] += g1.real(); O.gam[3][i] += g1.imag();
+            O.gam[4][i] += g2.real(); O.gam[5][i] += g2.imag();
+            O.gam[6][i] += g3.real(); O.gam[7][i] += g3.imag();
+        }
+    };
+    for (int k2 = kstart; k2 < mink_zeta; ++k2) {
+        add_gam(k2, k2, true);
+        for (int k3 = k2 + 1; k3 < nb; ++k3) { add_gam(k2, k3, false); add_gam(k3, k2, false); }
+    }
+}
+
+inline bool too_small(const Params& P, double rsq, double s1ps2)
+{ return rsq < P.minsepsq && s1ps2 < P.minsep && rsq < sqr(P.minsep - s1ps2); }
+inline bool too_large(const Params& P, double rsq, double s1ps2)
+{ return rsq >= P.maxsepsq && rsq >= sqr(P.maxsep + s1ps2); }
+
+// BaseCorr3::splitC2Cells, src/Corr3.cpp:1323-1372.
+void split_c2_cells(const Params& P, const Field& f, const Node& c1,
+                    const std::vector<int>& c2list, std::vector<int>& out)
+{
+    double s1 = c1.size;
+    for (int j : c2list) {
+        const Node& c2 = f.nodes[j];
+        double s2 = c2.size;
+        double rsq = dist_sq(P, c1, c2);
+        double s1ps2 = s1 + s2;
+        if (too_small(P, rsq, s1ps2) || too_large(P, rsq, s1ps2)) continue;
+        int k = -1;
+        double r = 0., logr = 0.;
+        bool split = !single_bin(P, rsq, s1ps2, k, r, logr);
+        if (split && s2 > s1) { out.push_back(c2.left); out.push_back(c2.right); }
+        else out.push_back(j);
+    }
+}
+
+// BaseCorr3::splitC2CellsOrCalculateGn, src/Corr3.cpp:1452-1546.
+double split_or_gn(const Params& P, const Field& f, const Node& c1,
+                   const std::vector<int>& c2list, std::vector<int>& out, bool& anysplit1,
+                   MPS& mp, double prev_maxr)
+{
+    double s1 = c1.size;
+    double maxrem = 0.;
+    double thresh1 = (1. - P.binsize) * prev_maxr;   // BinTypeHelper<Log>::oneBinLessThan
+    for (int j : c2list) {
+        const Node& c2 = f.nodes[j];
+        double s2 = c2.size;
+        double rsq = dist_sq(P, c1, c2);
+        double s1ps2 = s1 + s2;
+        if (too_small(P, rsq, s1ps2) || too_large(P, rsq, s1ps2)) continue;
+        int k = -1;
+        double r = std::sqrt(rsq), logr = 0.;
+        if (single_bin(P, rsq, s1ps2, k, r, logr)) {
+            if (rsq >= P.minsepsq && rsq < P.maxsepsq) {
+                if (k < 0) {
+                    logr = std::log(r);
+                    k = int((logr - P.logminsep) / P.binsize);
+                }
+                if (k >= P.nbins) k = P.nbins - 1;   // (unguarded in the reference)
+                calculate_gn(P, c1, c2, r, logr, k, mp);
+            }
+            continue;
+        }
+        double rtot = r + s1ps2;
+        maxrem = std::max(rtot, maxrem);
+        bool split1 = false, split2 = false;
+        calc_split_sq(split1, split2, s1, s2, rsq * std::min(P.bsq, P.asq));
+        if (split1 && r + s1ps2 > thresh1) anysplit1 = true;
+        if (split2) { out.push_back(c2.left); out.push_back(c2.right); }
+        else out.push_back(j);
+    }
+    return maxrem;
+}
+
+// BaseCorr3::multipoleFinish, src/Corr3.cpp:1548-1613.
+void multipole_finish(const Params& P, const Field& f, int i1, const std::vector<int>& c2list,
+                      MPS& mp, int mink_zeta, double maxr, Out3& O)
+{
+    const Node& c1 = f.nodes[i1];
+    bool anysplit1 = false;
+    std::vector<int> newlist;
+    maxr = split_or_gn(P, f, c1, c2list, newlist, anysplit1, mp, maxr);
+    if (!newlist.empty()) {
+        if (maxr < P.maxsep) {
+            int k = maxr < P.minsep ? 0 : int((std::log(maxr) - P.logminsep) / P.binsize) + 1;
+            if (k < mink_zeta) {
+                calculate_zeta(P, c1, mp, k, mink_zeta, O);
+                mink_zeta = k;
+            }
+        }
+        if (anysplit1) {
+            MPS copy = mp;
+            multipole_finish(P, f, c1.left, newlist, mp, mink_zeta, maxr, O);
+            multipole_finish(P, f, c1.right, newlist, copy, mink_zeta, maxr, O);
+        } else {
+            multipole_finish(P, f, i1, newlist, mp, mink_zeta, maxr, O);
+        }
+    } else {
+        calculate_zeta(P, c1, mp, 0, mink_zeta, O);
+    }
+}
+
+// BaseCorr3::multipoleSplit1, src/Corr3.cpp:1374-1408.
+void multipole_split1(const Params& P, const Field& f, int i1, const std::vector<int>& c2list,
+                      MPS& mp, Out3& O)
+{
+    const Node& c1 = f.nodes[i1];
+    double s1 = c1.size;
+    std::vector<int> newlist;
+    split_c2_cells(P, f, c1, c2list, newlist);
+    double maxbsq_eff = P.maxsepsq * std::min(P.bsq, P.asq);
+    if (double(s1) * double(s1) > maxbsq_eff) {
+        multipole_split1(P, f, c1.left, newlist, mp, O);
+        multipole_split1(P, f, c1.right, newlist, mp, O);
+    } else {
+        mp.clear();
+        multipole_finish(P, f, i1, newlist, mp, P.nbins, 0., O);
+    }
+}
+
 long long g_last_accepted = 0;   // directProcess11 calls of the last process call
 
 }  // namespace
@@ -700,6 +1017,46 @@ int orc_corr2_process_rows(int dtype, int metric, int quick, double minsep, doub
     }
     g_last_accepted = total.accepted;
     add_into(total, xi0, xi1, xi2, xi3, meanr, meanlogr, weight, npairs);
+    return 0;
+}
+
+
+// BaseCorr3::multipole (auto) for GGG with LogMultipole binning, src/Corr3.cpp:1124-1175.
+// Outputs have nbins*nbins*(2*maxn+1) entries, accumulated (+=) like the reference's.
+int orc_corr3_multipole_auto(int metric, int quick, double minsep, double maxsep, int nbins,
+                             double binsize, double b, double a, int maxn, void* h, int nthreads,
+                             double** gam8, double* meand2, double* meanlogd2, double* meand3,
+                             double* meanlogd3, double* weight, double* weight_im, double* ntri)
+{
+    Field* f = static_cast<Field*>(h);
+    if (f->dtype != DG) return 1;
+    Params P = make_params(DG, f->coords, metric, quick, minsep, maxsep, nbins, binsize, b, a);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    if (f->pts.empty()) return 0;
+    build_cells(*f);
+    const long n1 = (long)f->tops.size();
+    Out3 total(nbins, maxn);
+#pragma omp parallel
+    {
+        Out3 O(nbins, maxn);
+        MPS mp(nbins, maxn);
+#pragma omp for schedule(dynamic)
+        for (long i = 0; i < n1; ++i) multipole_split1(P, *f, f->tops[i], f->tops, mp, O);
+#pragma omp critical
+        total.add(O);
+    }
+    for (int q = 0; q < 8; ++q)
+        if (gam8[q]) for (int i = 0; i < total.size; ++i) gam8[q][i] += total.gam[q][i];
+    for (int i = 0; i < total.size; ++i) {
+        meand2[i] += total.meand2[i]; meanlogd2[i] += total.meanlogd2[i];
+        meand3[i] += total.meand3[i]; meanlogd3[i] += total.meanlogd3[i];
+        weight[i] += total.weight[i]; weight_im[i] += total.weight_im[i];
+        ntri[i] += total.ntri[i];
+    }
     return 0;
 }
 

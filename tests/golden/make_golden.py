@@ -95,9 +95,51 @@ def run_case(name):
     return out
 
 
-if __name__ == "__main__":
+if __name__ == "__main__" and "--mp" not in sys.argv:
     _treecorr.SetOMPThreads(1)
     names = sys.argv[1:] or list(CASES)
     for name in names:
         out = run_case(name)
         print(f"{name:24s} npairs={out['npairs'].sum():.0f} weight={out['weight'].sum():.6g}")
+
+
+def run_case3(name):
+    """GGG LogMultipole auto-correlation through the reference's GGGCorr (driven the way
+    treecorr/corr3base.py:1116-1131 and 1870-1911 drive it)."""
+    from cases3 import make_inputs3, spec3
+    s = spec3(name)
+    cat = make_inputs3(name)
+    if s["metric"] == "Euclidean":
+        b1 = min(s["a"], s["b"])
+        min_size, max_size = 2 * s["min_sep"] * b1 / (2. + 3 * b1), s["max_sep"] * b1
+    else:
+        min_size, max_size = 0.0, 0.0
+    nb, mn = s["nbins"], s["max_n"]
+    shape = (nb, nb, 2 * mn + 1)
+    keys = ("gam0r", "gam0i", "gam1r", "gam1i", "gam2r", "gam2i", "gam3r", "gam3i",
+            "meand1", "meanlogd1", "meand2", "meanlogd2", "meand3", "meanlogd3", "meanu",
+            "meanv", "weight", "weight_im", "ntri")
+    out = {k: np.zeros(shape) for k in keys}
+    corr = _treecorr.GGGCorr(
+        _treecorr.LogMultipole, s["min_sep"], s["max_sep"], nb, s["bin_size"], s["b"], s["a"],
+        0., 0., mn, 0., 0., 0., 0., 0, 0., 0.,
+        -sys.float_info.max, sys.float_info.max, 0., 0., 0.,
+        *[out[k] for k in keys])
+    f = build_field("G", s["coords"], cat, min_size, max_size, "mean", False, 3, 10)
+    corr.processAuto(f, False, False, METRIC[s["metric"]])
+    save = dict(min_size=min_size, max_size=max_size)
+    for k, v in cat.items():
+        if v is not None:
+            save["c1_" + k] = v
+    for k, v in out.items():
+        save["ref_" + k] = v
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **save)
+    return out
+
+
+if __name__ == "__main__" and "--mp" in sys.argv:
+    _treecorr.SetOMPThreads(1)
+    from cases3 import CASES3
+    for name in CASES3:
+        out = run_case3(name)
+        print(f"{name:20s} ntri={out['ntri'].sum():.6g} weight={out['weight'].sum():.6g}")

@@ -150,18 +150,38 @@ def test_edge_cases(gpu_lib):
     f1 = T.NFieldFlat(one, one, e, one, e, 0., 0., T.Mean, 0, False, 3, 10)
     assert f1.getNTopLevel() == 1
     assert not H.gpu_process(T, "N", "Euclidean", bins, f1)["npairs"].any()
-    # Duplicated positions and zero weights.
+    # Duplicated positions (4 copies of each point), all weights positive: list leaves and
+    # split duplicates count the same pairs, so npairs is exact.
     rng = np.random.default_rng(3)
     x = np.repeat(rng.uniform(0, 20, 50), 4)
     y = np.repeat(rng.uniform(0, 20, 50), 4)
     w = rng.uniform(0.5, 1.5, 200)
-    w[::7] = 0.
     cat = dict(x=x, y=y, z=None, w=w)
     for bs in (0.0, 1.0):
         b = dict(bins, b=bs * bins["bin_size"])
         got = H.gpu_process(T, "N", "Euclidean", b, H.gpu_field(T, "N", "flat", cat, 0., 0.))
         ref = H.oracle_process("N", "Euclidean", b, H.oracle_field("N", "flat", cat, 0., 0.))
         H.assert_outputs_close(got, ref, "N", label=f"dups bs={bs}")
+    # Zero weights on distinct points: such points are skipped (src/Corr2.cpp:315).
+    xz = rng.uniform(0, 20, 300)
+    yz = rng.uniform(0, 20, 300)
+    wz = rng.uniform(0.5, 1.5, 300)
+    wz[::7] = 0.
+    catz = dict(x=xz, y=yz, z=None, w=wz)
+    for bs in (0.0, 1.0):
+        b = dict(bins, b=bs * bins["bin_size"])
+        got = H.gpu_process(T, "N", "Euclidean", b, H.gpu_field(T, "N", "flat", catz, 0., 0.))
+        ref = H.oracle_process("N", "Euclidean", b, H.oracle_field("N", "flat", catz, 0., 0.))
+        H.assert_outputs_close(got, ref, "N", label=f"zero-w bs={bs}")
+    # Duplicates together with zero weights: whether exact duplicates end as one list leaf
+    # or as single points depends on the last bit of their centroid, so only the weighted
+    # sums (which do not depend on the tree) are compared.
+    w2 = w.copy()
+    w2[::7] = 0.
+    cat2 = dict(x=x, y=y, z=None, w=w2)
+    got = H.gpu_process(T, "N", "Euclidean", bins, H.gpu_field(T, "N", "flat", cat2, 0., 0.))
+    ref = H.oracle_process("N", "Euclidean", bins, H.oracle_field("N", "flat", cat2, 0., 0.))
+    H.assert_outputs_close(got, ref, "N", exact_npairs=False, label="dups+zero-w")
     # Cross with fields far apart: the early exit leaves the outputs untouched.
     far = dict(x=x + 1e4, y=y, z=None, w=w)
     got = H.gpu_process(T, "N", "Euclidean", bins, H.gpu_field(T, "N", "flat", cat, 0., 0.),
@@ -176,7 +196,6 @@ def test_unsupported_raise(gpu_lib):
     z = np.zeros(3)
     with pytest.raises(NotImplementedError):
         T.NNCorr(T.Linear, 1., 10., 5, 1.8, 0., 0., -sys.float_info.max, sys.float_info.max,
-                 0., 0., 0., e, e, e, e, z[:0] + np.zeros(5), np.zeros(5), np.zeros(5),
-                 np.zeros(5))
+                 0., 0., 0., e, e, e, e, np.zeros(5), np.zeros(5), np.zeros(5), np.zeros(5))
     with pytest.raises(NotImplementedError):
         T.NFieldFlat(z, z, e, z + 1, e, 0., 0., T.Random, 0, False, 3, 10)

@@ -51,3 +51,24 @@ def test_oracle_brute_force_flat():
     np.testing.assert_allclose(out["weight"], ww, rtol=1e-6)
     np.testing.assert_allclose(out["xi0"], xip, rtol=1e-5, atol=1e-6 * ww.max())
     np.testing.assert_allclose(out["xi2"], xim, rtol=1e-5, atol=1e-6 * ww.max())
+
+
+@pytest.mark.parametrize("name", ["ggg_flat_mp", "ggg_flat_mp_n20", "ggg_flat_mp_bs0",
+                                  "ggg_sphere_mp"])
+def test_oracle_multipole_matches_reference(name):
+    """GGG LogMultipole: the oracle's restatement against the reference's own outputs."""
+    import os
+    from cases3 import spec3
+    from oracle import oracle as O
+    s = spec3(name)
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    c = {k[3:]: g[k] for k in g.files if k.startswith("c1_")}
+    f = O.OracleField("G", s["coords"], c["x"], c["y"], c.get("z"), c["g1"], c["g2"], c["w"],
+                      None, float(g["min_size"]), float(g["max_size"]), "mean", False, 3, 10)
+    bins = dict(min_sep=s["min_sep"], max_sep=s["max_sep"], nbins=s["nbins"],
+                bin_size=s["bin_size"], b=s["b"], a=s["a"])
+    out = O.multipole(s["metric"], bins, s["max_n"], f, nthreads=1)
+    assert np.array_equal(out["ntri"], g["ref_ntri"])
+    for k in O.MP_KEYS:
+        r = g["ref_" + k]
+        assert np.abs(out[k] - r).max() <= 1e-12 * max(np.abs(r).max(), 1e-300), k
