@@ -32,7 +32,7 @@
 
 namespace tc {
 
-static constexpr int TB = 256;        // threads per traversal block
+static constexpr int TB = 128;        // threads per traversal block
 static constexpr int WPB = TB / 32;   // warps per block
 static constexpr int FLUSH = 8;       // iterations between FP32 -> FP64 flushes
 
@@ -96,37 +96,35 @@ __device__ __forceinline__ Decision decide32(const TravParams& T, float rsq, flo
     Decision D;
     D.act = ACT_UNSURE; D.k = -1; D.r = 0.f; D.logr = 0.f;
     // Error bounds: rsq (relative), s1+s2 (relative).
-    const float ER = arc ? 2e-5f : 1e-5f;
+    const float ER = arc ? 5e-6f : 2e-6f;
     const float ES = 1e-6f;
     const float Rlo = rsq * (1.f - ER), Rhi = rsq * (1.f + ER);
     const float s1ps2 = s1 + s2;
     const float Slo = s1ps2 * (1.f - ES), Shi = s1ps2 * (1.f + ES);
 
-    // tooSmallDist, include/BinType.h:70-76.
-    {
-        int c1 = gt3(T.fminsepsq * (1.f - 1e-7f), T.fminsepsq * (1.f + 1e-7f), Rlo, Rhi);  // rsq < minsepsq
+    // tooSmallDist, include/BinType.h:70-76 (the first clause decides most pairs).
+    const int below = gt3(T.fminsepsq * (1.f - 1e-7f), T.fminsepsq * (1.f + 1e-7f), Rlo, Rhi);
+    if (below != NO) {
         int c2 = gt3(T.fminsep, T.fminsep, Slo, Shi);                                    // s1ps2 < minsep
         float xlo = T.fminsep - Shi, xhi = T.fminsep - Slo, x2lo, x2hi;
         sq_iv(xlo, xhi, x2lo, x2hi);
         int c3 = gt3(LOW(x2lo), HIGH(x2hi), Rlo, Rhi);                                  // rsq < (minsep-s)^2
-        if (c1 == YES && c2 == YES && c3 == YES) { D.act = ACT_DROP; return D; }
-        if (!(c1 == NO || c2 == NO || c3 == NO)) return D;
+        if (below == YES && c2 == YES && c3 == YES) { D.act = ACT_DROP; return D; }
+        if (!(c2 == NO || c3 == NO)) return D;
     }
-    // tooLargeDist, include/BinType.h:77-82.
-    {
-        int c1b = gt3(T.fmaxsepsq * (1.f - 1e-7f), T.fmaxsepsq * (1.f + 1e-7f), Rlo, Rhi);
-        // rsq >= maxsepsq  <=>  !(maxsepsq > rsq)
-        int ge1 = c1b == YES ? NO : (c1b == NO ? YES : UNSURE);
+    // tooLargeDist, include/BinType.h:77-82: rsq >= maxsepsq  <=>  !(maxsepsq > rsq).
+    const int inside = gt3(T.fmaxsepsq * (1.f - 1e-7f), T.fmaxsepsq * (1.f + 1e-7f), Rlo, Rhi);
+    if (inside != YES) {
         float ylo = T.fmaxsep + Slo, yhi = T.fmaxsep + Shi;
         float y2lo = LOW(ylo * ylo), y2hi = HIGH(yhi * yhi);
         int lt2 = gt3(y2lo, y2hi, Rlo, Rhi);   // (maxsep+s)^2 > rsq
-        int ge2 = lt2 == YES ? NO : (lt2 == NO ? YES : UNSURE);
-        if (ge1 == YES && ge2 == YES) { D.act = ACT_DROP; return D; }
-        if (!(ge1 == NO || ge2 == NO)) return D;
+        if (inside == NO && lt2 == NO) { D.act = ACT_DROP; return D; }
+        if (lt2 != YES) return D;
     }
     // singleBin, include/BinType.h:93-151.
     int sb = UNSURE;
     int k = -1;
+    float lr = 0.f;   // log(r/minsep), set once it is needed
     if (s1ps2 == 0.f) {
         sb = YES;
     } else {
@@ -143,9 +141,9 @@ __device__ __forceinline__ Decision decide32(const TravParams& T, float rsq, flo
                 if (t3 == UNSURE) return D;
                 if (t3 == YES) sb = NO;
                 else {
-                    float lr = 0.5f * logf(rsq * T.finvminsepsq);
+                    lr = 0.5f * logf(rsq * T.finvminsepsq);
                     float kk = lr * T.finvbinsize;
-                    float ek = (0.5f * ER + 1e-6f * (1.f + fabsf(lr))) * T.finvbinsize + 1e-6f;
+                    float ek = (0.5f * ER + 3e-7f * (1.f + fabsf(lr))) * T.finvbinsize + 1e-6f;
                     float klo = kk - ek, khi = kk + ek;
                     // int(kk) truncates toward zero, as in the reference (kk < 0 is possible).
                     float ik = truncf(kk);
@@ -174,16 +172,14 @@ __device__ __forceinline__ Decision decide32(const TravParams& T, float rsq, flo
     }
     if (sb == YES) {
         // isRSqInRange, include/BinType.h:61-66: minsepsq <= rsq < maxsepsq.
-        int below = gt3(T.fminsepsq * (1.f - 1e-7f), T.fminsepsq * (1.f + 1e-7f), Rlo, Rhi);
-        int above = gt3(T.fmaxsepsq * (1.f - 1e-7f), T.fmaxsepsq * (1.f + 1e-7f), Rlo, Rhi);
-        if (below == UNSURE || above == UNSURE) return D;
-        if (below == YES || above == NO) { D.act = ACT_DROP; return D; }
+        if (below == UNSURE || inside == UNSURE) return D;
+        if (below == YES || inside == NO) { D.act = ACT_DROP; return D; }
         float r = arc ? 0.f : sqrtf(rsq);
-        float lr = 0.5f * logf(rsq * T.finvminsepsq);
+        if (k < 0) lr = 0.5f * logf(rsq * T.finvminsepsq);
         if (k < 0) {
             // directProcess11, src/Corr2.cpp:492-514.
             float kk = lr * T.finvbinsize;
-            float ek = (0.5f * ER + 1e-6f * (1.f + fabsf(lr))) * T.finvbinsize + 1e-6f;
+            float ek = (0.5f * ER + 3e-7f * (1.f + fabsf(lr))) * T.finvbinsize + 1e-6f;
             float ik = truncf(kk);
             if (truncf(kk - ek) != ik || truncf(kk + ek) != ik) return D;
             k = int(ik);
@@ -337,22 +333,76 @@ __device__ __forceinline__ int2 make_root(const TravParams& T, long long g)
 // ---------------------------------------------------------------------------------------
 // The traversal kernel.
 
-__device__ __forceinline__ void flush_bins(const TravParams& T, float* fb,
-                                           unsigned long long* np, int gw, int lane)
+// FP32 bins (4 segment copies) -> the warp's FP64 bins, all in shared memory.
+__device__ __forceinline__ void flush_bins(int nqnb, float* fb, double* fd, int lane)
 {
-    const int nq = T.nqf, nb = T.nbins;
-    double* wa = T.wacc + (size_t)gw * nq * nb;
-    for (int q = lane; q < nq * nb; q += 32) {
-        float v = fb[q];
-        if (v != 0.f) { wa[q] += (double)v; fb[q] = 0.f; }
-    }
-    if (!T.quick) {
-        unsigned long long* wn = T.wnp + (size_t)gw * nb;
-        for (int q = lane; q < nb; q += 32) {
-            unsigned long long v = np[q];
-            if (v) { wn[q] += v; np[q] = 0ull; }
+    for (int q = lane; q < nqnb; q += 32) {
+        float a = fb[q], b = fb[nqnb + q], c = fb[2 * nqnb + q], d = fb[3 * nqnb + q];
+        if (a != 0.f || b != 0.f || c != 0.f || d != 0.f) {
+            fd[q] += ((double)a + (double)b) + ((double)c + (double)d);
+            fb[q] = 0.f; fb[nqnb + q] = 0.f; fb[2 * nqnb + q] = 0.f; fb[3 * nqnb + q] = 0.f;
         }
     }
+}
+
+// Adds the accepted pairs of this iteration to the warp's bins without atomics.  Each lane
+// stages (k, 7 values, npairs) in shared memory; then the warp works as 4 segments of 8
+// lanes: lane q of a segment owns quantity q (q = 7: npairs) and walks the segment's 8
+// staged entries in order, summing runs of equal bins in a register and adding each run
+// to its segment's copy of the bins.  The order is fixed, so the sums are deterministic.
+static constexpr int STG = 11;   // staged words per lane (odd stride: no bank conflicts)
+
+__host__ __device__ inline size_t traverse_warp_bytes(int nq, int nb)
+{
+    size_t b = (size_t)nq * nb * 8 + (size_t)4 * nb * 8 + (size_t)4 * nq * nb * 4 +
+               (size_t)32 * STG * 4;
+    return (b + 15) & ~(size_t)15;
+}
+
+__device__ __forceinline__ void stage_accumulate(int k, const float (&v)[7],
+                                                 unsigned long long nn, int nq, bool quick,
+                                                 float* stage, float* fb, unsigned long long* np,
+                                                 int nb, int lane)
+{
+    float* my = stage + lane * STG;
+#pragma unroll
+    for (int q = 0; q < 7; ++q) my[q] = v[q];
+    my[7] = __int_as_float(k);
+    my[8] = __uint_as_float((unsigned)(nn & 0xffffffffull));
+    my[9] = __uint_as_float((unsigned)(nn >> 32));
+    __syncwarp();
+    const int seg = lane >> 3, q = lane & 7;
+    const bool isn = (q == 7);
+    if (q < nq || (isn && !quick)) {
+        float* fbs = fb + seg * nq * nb + q * nb;
+        unsigned long long* nps = np + seg * nb;
+        int curk = -1;
+        float acc = 0.f;
+        unsigned long long acc64 = 0ull;
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const float* e = stage + (seg * 8 + t) * STG;
+            const int kj = __float_as_int(e[7]);
+            if (kj < 0) continue;
+            if (kj != curk) {
+                if (curk >= 0) {
+                    if (isn) nps[curk] += acc64;
+                    else fbs[curk] += acc;
+                }
+                curk = kj;
+                acc = 0.f;
+                acc64 = 0ull;
+            }
+            if (isn) acc64 += (unsigned long long)__float_as_uint(e[8]) |
+                              ((unsigned long long)__float_as_uint(e[9]) << 32);
+            else acc += e[q];
+        }
+        if (curk >= 0) {
+            if (isn) nps[curk] += acc64;
+            else fbs[curk] += acc;
+        }
+    }
+    __syncwarp();
 }
 
 __global__ void __launch_bounds__(TB) k_traverse(TravParams T)
@@ -362,12 +412,16 @@ __global__ void __launch_bounds__(TB) k_traverse(TravParams T)
     const int wib = threadIdx.x >> 5;
     const int gw = blockIdx.x * WPB + wib;
     const int nq = T.nqf, nb = T.nbins;
-    // Per-warp bins: nb npairs (u64), then nq*nb floats.
-    const size_t wbytes = (size_t)nb * 8 + (size_t)nq * nb * 4;
-    unsigned long long* np = (unsigned long long*)(smem + wib * ((wbytes + 15) & ~(size_t)15));
-    float* fb = (float*)(np + nb);
-    for (int q = lane; q < nb; q += 32) np[q] = 0ull;
-    for (int q = lane; q < nq * nb; q += 32) fb[q] = 0.f;
+    // Per-warp bins: nq*nb FP64 totals, 4 segment copies of the npairs (u64) and of the
+    // nq*nb FP32 partials, and the 32-lane staging area.
+    const size_t wbytes = traverse_warp_bytes(nq, nb);
+    double* fd = (double*)(smem + wib * wbytes);
+    unsigned long long* np = (unsigned long long*)(fd + nq * nb);
+    float* fb = (float*)(np + 4 * nb);
+    float* stage = fb + 4 * nq * nb;
+    for (int q = lane; q < nq * nb; q += 32) fd[q] = 0.;
+    for (int q = lane; q < 4 * nb; q += 32) np[q] = 0ull;
+    for (int q = lane; q < 4 * nq * nb; q += 32) fb[q] = 0.f;
     __syncwarp();
 
     int2* stk = T.stacks + (size_t)gw * T.stack_cap;
@@ -381,14 +435,23 @@ __global__ void __launch_bounds__(TB) k_traverse(TravParams T)
 
     while (true) {
         if (sp < 32 && !roots_done) {
+            // Take up to 32 roots; fewer when the pool is small, so that the last items of
+            // a launch are spread over many warps.
             unsigned long long base = 0;
-            if (lane == 0) base = atomicAdd(T.root_next, 32ull);
+            int want = 32;
+            if (lane == 0) {
+                long long cur = (long long)*(volatile unsigned long long*)T.root_next;
+                long long per = (total_roots - cur) / T.nwarps;
+                want = per >= 32 ? 32 : (per < 1 ? 1 : (int)per);
+                base = atomicAdd(T.root_next, (unsigned long long)want);
+            }
             base = __shfl_sync(0xffffffffu, base, 0);
+            want = __shfl_sync(0xffffffffu, want, 0);
             if ((long long)base >= total_roots) {
                 roots_done = true;
             } else {
                 long long g = (long long)base + lane;
-                bool ok = g < total_roots;
+                bool ok = lane < want && g < total_roots;
                 int2 t = ok ? make_root(T, g) : make_int2(0, 0);
                 unsigned m = __ballot_sync(0xffffffffu, ok);
                 if (ok) stk[sp + __popc(m & ((1u << lane) - 1u))] = t;
@@ -400,7 +463,7 @@ __global__ void __launch_bounds__(TB) k_traverse(TravParams T)
             if (roots_done) break;
             continue;
         }
-        if (roots_done && (iter & 7) == 0 && sp > 64) {
+        if (roots_done && (iter & 3) == 0) {
             // Spill when many warps are idle, so the next launch can spread this stack.
             int idle = 0;
             if (lane == 0) idle = *(volatile int*)T.idle;
@@ -453,6 +516,9 @@ __global__ void __launch_bounds__(TB) k_traverse(TravParams T)
 
         int nch = 0;
         int2 ch[4];
+        int acc_k = -1;
+        float av[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        unsigned long long acc_nn = 0ull;
         if (has) {
             ++n_eval;
             const int i = task.x;
@@ -497,18 +563,15 @@ __global__ void __launch_bounds__(TB) k_traverse(TravParams T)
                     }
                     if (D.act == ACT_ACCEPT) {
                         ++n_acc;
-                        const int k = D.k;
+                        acc_k = D.k;
                         const float ww = A.b.w * B.b.w;
-                        atomicAdd(&fb[k], ww);
-                        if (!T.quick) {
-                            unsigned long long nn = (unsigned long long)__float_as_int(A.c.z) *
-                                                    (unsigned long long)__float_as_int(B.c.z);
-                            atomicAdd(&np[k], nn);
-                            atomicAdd(&fb[nb + k], ww * D.r);
-                            atomicAdd(&fb[2 * nb + k], ww * D.logr);
-                        }
+                        av[0] = ww;
+                        av[1] = ww * D.r;
+                        av[2] = ww * D.logr;
+                        acc_nn = (unsigned long long)__float_as_int(A.c.z) *
+                                 (unsigned long long)__float_as_int(B.c.z);
                         if (T.dkind == DK) {
-                            atomicAdd(&fb[3 * nb + k], A.c.x * B.c.x);
+                            av[3] = A.c.x * B.c.x;
                         } else if (T.dkind == DG) {
                             float g1r = A.c.x, g1i = A.c.y, g2r = B.c.x, g2i = B.c.y;
                             if (flat) {
@@ -535,10 +598,10 @@ __global__ void __launch_bounds__(TB) k_traverse(TravParams T)
                             }
                             // both_complex_prod(g2, g1), ProjectHelper.h:84-101.
                             const float rr = g2r * g1r, ri = g2r * g1i, ir = g2i * g1r, ii = g2i * g1i;
-                            atomicAdd(&fb[3 * nb + k], rr + ii);   // xip
-                            atomicAdd(&fb[4 * nb + k], ri - ir);
-                            atomicAdd(&fb[5 * nb + k], rr - ii);   // xim
-                            atomicAdd(&fb[6 * nb + k], ri + ir);
+                            av[3] = rr + ii;   // xip
+                            av[4] = ri - ir;
+                            av[5] = rr - ii;   // xim
+                            av[6] = ri + ir;
                         }
                     } else if (D.act != ACT_DROP) {
                         const int L1 = __float_as_int(A.c.w), R1 = __float_as_int(A.d.x);
@@ -561,6 +624,9 @@ __global__ void __launch_bounds__(TB) k_traverse(TravParams T)
                 }
             }
         }
+        // Accumulate this iteration's accepted pairs (warp-converged here).
+        if (__any_sync(0xffffffffu, acc_k >= 0))
+            stage_accumulate(acc_k, av, acc_nn, nq, T.quick, stage, fb, np, nb, lane);
         // Push the children: exclusive warp scan of the counts.
         int off = nch;
         for (int o = 1; o < 32; o <<= 1) {
@@ -573,12 +639,21 @@ __global__ void __launch_bounds__(TB) k_traverse(TravParams T)
         sp += tot;
         __syncwarp();
         if ((iter % FLUSH) == 0) {
-            flush_bins(T, fb, np, gw, lane);
+            __syncwarp();
+            flush_bins(nq * nb, fb, fd, lane);
             __syncwarp();
         }
     }
     __syncwarp();
-    flush_bins(T, fb, np, gw, lane);
+    flush_bins(nq * nb, fb, fd, lane);
+    __syncwarp();
+    {
+        // The warp's totals: added to its global slot (kept across relaunches).
+        double* wa = T.wacc + (size_t)gw * nq * nb;
+        for (int q = lane; q < nq * nb; q += 32) wa[q] += fd[q];
+        unsigned long long* wn = T.wnp + (size_t)gw * nb;
+        for (int q = lane; q < nb; q += 32) wn[q] += (np[q] + np[nb + q]) + (np[2 * nb + q] + np[3 * nb + q]);
+    }
     // Counters.
     for (int o = 16; o > 0; o >>= 1) {
         n_eval += __shfl_xor_sync(0xffffffffu, n_eval, o);
@@ -616,9 +691,7 @@ __global__ void k_reduce_acc(int nwarps, int nq, int nb, const double* wacc,
 
 size_t traverse_smem_bytes(int nq, int nb)
 {
-    size_t wbytes = (size_t)nb * 8 + (size_t)nq * nb * 4;
-    wbytes = (wbytes + 15) & ~(size_t)15;
-    return wbytes * WPB;
+    return traverse_warp_bytes(nq, nb) * WPB;
 }
 
 int traverse_grid(int nq, int nb, int* blocks, int* nwarps)
