@@ -146,6 +146,24 @@ int tc_corr2_process_auto(tc_corr2* c, tc_field* f, int dots, int quick, int met
 int tc_corr2_process_cross(tc_corr2* c, tc_field* f1, tc_field* f2, int dots, int quick,
                            int metric);
 
+/* The auto-correlation of tc_corr2_process_auto, for callers that must not allocate GPU
+ * memory during the call -- for instance code that runs while a CUDA stream is being
+ * captured, where cudaMalloc is not allowed, or a process whose device memory is all handed
+ * out by its own memory pool.  No reference counterpart: the reference runs on the CPU and
+ * allocates per call.
+ *
+ * Nothing is allocated: the traversal's work lists and partial sums live in one fixed
+ * device array of about 52 MiB that is part of this library (every GPU that loads the
+ * library holds it until the process exits).  Limits: nbins <= 64, at most 1024 warps, and
+ * work lists of the fixed size; a traversal that needs more space fails with
+ * TC_ERR_DEVICE and a clear message (tc_corr2_process_auto has no such limit).
+ * The field must already be built (call tc_field_ntop once beforehand: building the tree
+ * allocates).  The first call on a device looks up the array's device address; make that
+ * first call before any stream capture.  All calls share the array: calls that overlap on
+ * the GPU (from several host threads or processes sharing a context) race and must be
+ * serialised by the caller.  Results are added into the corr's output arrays as usual. */
+int tc_corr2_process_auto_noalloc(tc_corr2* c, tc_field* f, int quick, int metric);
+
 /* BaseCorr2.triviallyZero -> TriviallyZero (src/Corr2.cpp:1107-1128): 1 if no pair of
  * the two patches (centre + size) can fall in range.  Result in *out. */
 int tc_corr2_trivially_zero(tc_corr2* c, int metric, int coords,

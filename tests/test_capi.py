@@ -27,7 +27,7 @@ def test_header_declares_entry_points():
     names = declared_functions()
     for must in ("tc_field_create", "tc_field_create_device", "tc_field_free", "tc_field_ntop",
                  "tc_corr2_create", "tc_corr2_process_auto", "tc_corr2_process_cross",
-                 "tc_corr2_trivially_zero", "tc_last_error"):
+                 "tc_corr2_trivially_zero", "tc_last_error", "tc_corr2_process_auto_noalloc"):
         assert must in names
 
 

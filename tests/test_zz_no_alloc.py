@@ -1,0 +1,90 @@
+"""GPU test of tc_corr2_process_auto_noalloc, the allocation-free auto-correlation.
+
+Some callers cannot allocate GPU memory while they run this code: a process that is
+capturing a CUDA stream into a graph (cudaMalloc is not allowed during capture), or one
+whose device memory is all handed out by its own memory pool.  For them the library offers
+one entry point that allocates nothing: it uses a fixed device array that is part of the
+library.  This test calls it through the C ABI, twice in a row, and checks each result
+against tc_corr2_process_auto on the same field, and that free device memory does not
+change across the calls.
+
+The file name makes pytest collect it last.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+
+def _noalloc_fn(T):
+    L = T.lib()
+    fn = L.tc_corr2_process_auto_noalloc
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+    return L, fn
+
+
+def _corr(T, dtype, bins, out):
+    import sys
+    e = np.array([])
+    xi = [out["xi0"], out["xi1"], out["xi2"], out["xi3"]]
+    if dtype == "N":
+        xi = [e, e, e, e]
+    elif dtype == "K":
+        xi = [out["xi0"], e, e, e]
+    return getattr(T, dtype * 2 + "Corr")(T.Log, bins["min_sep"], bins["max_sep"],
+                                          bins["nbins"], bins["bin_size"], bins["b"], bins["a"],
+                                          -sys.float_info.max, sys.float_info.max, 0., 0., 0.,
+                                          *xi, out["meanr"], out["meanlogr"], out["weight"],
+                                          out["npairs"])
+
+
+@pytest.mark.parametrize("name", ["gg_flat_bs1", "gg_sphere_arc", "nn_flat_bs1", "kk_flat_bs0"])
+def test_noalloc_matches_process_auto(gpu_lib, name):
+    import torch
+    T = gpu_lib
+    L, noalloc = _noalloc_fn(T)
+    s, c1, c2, bins, min_size, max_size, golden = H.load_case(name)
+    f = H.gpu_field(T, s["dtype"], s["coords"], c1, min_size, max_size, s["split"], s["brute"],
+                    s["min_top"], s["max_top"])
+    f.getNTopLevel()    # build the tree first: building allocates
+    ref = H.gpu_process(T, s["dtype"], s["metric"], bins, f)
+    metric = int(T.Euclidean if s["metric"] == "Euclidean" else T.Arc)
+    outs = [{k: np.zeros(bins["nbins"]) for k in H.OUT_KEYS} for _ in range(2)]
+    corrs = [_corr(T, s["dtype"], bins, o) for o in outs]
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    for corr in corrs:
+        rc = noalloc(corr._h, f._h, 0, metric)
+        assert rc == 0, L.tc_last_error().decode()
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free1 == free0, f"device memory changed by {free0 - free1} bytes"
+    for out in outs:
+        # Same kernels and decisions; only the grouping of FP32 partials into warps differs.
+        H.assert_outputs_close(out, ref, s["dtype"], rtol=1e-6, label=name + " noalloc")
+        H.assert_outputs_close(out, golden, s["dtype"], rtol=1e-5, label=name + " golden")
+
+
+def test_noalloc_rejects_what_it_cannot_hold(gpu_lib):
+    T = gpu_lib
+    L, noalloc = _noalloc_fn(T)
+    s, c1, c2, bins, min_size, max_size, golden = H.load_case("nn_flat_bs1")
+    # A field whose tree is not built yet (building would allocate).
+    f = H.gpu_field(T, "N", "flat", c1, min_size, max_size)
+    out = {k: np.zeros(bins["nbins"]) for k in H.OUT_KEYS}
+    corr = _corr(T, "N", bins, out)    # keep the object alive while its handle is used
+    rc = noalloc(corr._h, f._h, 0, int(T.Euclidean))
+    assert rc == 1 and b"not built" in L.tc_last_error()
+    # More bins than the fixed scratch holds.
+    f.getNTopLevel()
+    big = dict(bins, nbins=100, bin_size=np.log(bins["max_sep"] / bins["min_sep"]) / 100)
+    out = {k: np.zeros(100) for k in H.OUT_KEYS}
+    corr_big = _corr(T, "N", big, out)
+    rc = noalloc(corr_big._h, f._h, 0, int(T.Euclidean))
+    assert rc == 1 and b"at most 64" in L.tc_last_error()
+    assert not out["npairs"].any()

@@ -486,6 +486,147 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
     return TC_ERR_DEVICE;
 }
 
+// The auto-correlation of an already built field with the fixed traversal scratch: no
+// device or host allocation.  Same arithmetic as corr_process (the same kernels), with the
+// warp count capped at NOALLOC_MAXW and the bins at NOALLOC_MAXNB.
+int corr_process_auto_noalloc(tc_corr2* c, tc_field* f, int quick, int metric)
+{
+    if (!c || !f) { set_last_error("NULL argument"); return TC_ERR_ARG; }
+    if (c->d1 != f->dkind) {
+        set_last_error("field data kind does not match the correlation"); return TC_ERR_ARG;
+    }
+    TC_TRY(check_metric(f->coords, metric));
+    if (c->nbins > NOALLOC_MAXNB) {
+        set_last_error("nbins exceeds the fixed scratch of the allocation-free call (at most 64)");
+        return TC_ERR_ARG;
+    }
+    if (f->n > 0 && !f->built) {
+        set_last_error("the field's tree is not built; call tc_field_ntop() first (building "
+                       "allocates device memory)");
+        return TC_ERR_ARG;
+    }
+    c->stats = tc_stats();
+    if (f->n == 0) return TC_OK;
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    void* base = nullptr;
+    TC_TRY(noalloc_scratch(&base));
+    unsigned char* B = static_cast<unsigned char*>(base);
+
+    const int nb = c->nbins;
+    const int nq = c->d1 == TC_GDATA ? 7 : (c->d1 == TC_KDATA ? 4 : 3);
+    TravParams T;
+    std::memset(&T, 0, sizeof(T));
+    T.coords = f->coords; T.metric = metric; T.dkind = c->d1; T.quick = quick ? 1 : 0;
+    T.nbins = nb; T.autoc = 1; T.nqf = nq;
+    T.minsep = c->minsep; T.maxsep = c->maxsep; T.binsize = c->binsize; T.b = c->b; T.a = c->a;
+    T.logminsep = std::log(c->minsep); T.halfminsep = 0.5 * c->minsep;
+    T.minsepsq = c->minsep * c->minsep; T.maxsepsq = c->maxsep * c->maxsep;
+    T.bsq = c->b * c->b; T.asq = c->a * c->a;
+    T.fminsep = (float)T.minsep; T.fmaxsep = (float)T.maxsep; T.fbinsize = (float)T.binsize;
+    T.fb = (float)T.b; T.fminsepsq = (float)T.minsepsq; T.fmaxsepsq = (float)T.maxsepsq;
+    T.fbsq = (float)T.bsq; T.fasq = (float)std::min(T.asq, 1e30);
+    T.fbb = (float)(0.25 * sqr(T.binsize + T.b));
+    T.fmineff = (float)std::min(T.bsq, T.asq);
+    T.finvminsepsq = (float)(1. / T.minsepsq);
+    T.finvbinsize = (float)(1. / T.binsize);
+    T.flogminsep = (float)T.logminsep;
+    T.c1 = f->tcells; T.c2 = f->tcells;
+    T.x1 = f->cells.x; T.y1 = f->cells.y; T.z1 = f->cells.z;
+    T.x2 = f->cells.x; T.y2 = f->cells.y; T.z2 = f->cells.z;
+    T.tops1 = f->d_tops; T.tops2 = f->d_tops;
+    T.ntop1 = (long long)f->tops.size(); T.ntop2 = T.ntop1;
+    T.ngen = T.ntop1 * (T.ntop1 + 1) / 2;
+
+    int blocks = 0, nwarps = 0;
+    TC_TRY(traverse_grid(nq, nb, &blocks, &nwarps));
+    const int wpb = nwarps / blocks;
+    if (nwarps > NOALLOC_MAXW) { blocks = NOALLOC_MAXW / wpb; nwarps = blocks * wpb; }
+    int2* spill[2] = {reinterpret_cast<int2*>(B + NOALLOC_OFF_SPILL0),
+                      reinterpret_cast<int2*>(B + NOALLOC_OFF_SPILL1)};
+    double* wacc = reinterpret_cast<double*>(B + NOALLOC_OFF_WACC);
+    unsigned long long* wnp = reinterpret_cast<unsigned long long*>(B + NOALLOC_OFF_WNP);
+    double* tot = reinterpret_cast<double*>(B + NOALLOC_OFF_TOT);
+    unsigned long long* totnp = reinterpret_cast<unsigned long long*>(B + NOALLOC_OFF_TOTNP);
+    unsigned long long* ctl = reinterpret_cast<unsigned long long*>(B + NOALLOC_OFF_CTL);
+    T.stacks = reinterpret_cast<int2*>(B + NOALLOC_OFF_STACKS);
+    T.stack_cap = NOALLOC_SCAP;
+    T.nwarps = nwarps;
+    T.wacc = wacc; T.wnp = wnp;
+    T.idle = reinterpret_cast<int*>(B + NOALLOC_OFF_IDLE);
+    T.err = reinterpret_cast<int*>(B + NOALLOC_OFF_ERR);
+    T.root_next = ctl; T.nout = ctl + 1; T.counters = ctl + 2;
+    T.out_cap = NOALLOC_SPILL;
+    // The array keeps the previous call's contents: clear what must start at zero.
+    TC_CU(cudaMemsetAsync(wacc, 0, sizeof(double) * (size_t)nwarps * nq * nb, st));
+    TC_CU(cudaMemsetAsync(wnp, 0, sizeof(unsigned long long) * (size_t)nwarps * nb, st));
+    TC_CU(cudaMemsetAsync(ctl, 0, 8 * sizeof(unsigned long long), st));
+    TC_CU(cudaMemsetAsync(T.err, 0, sizeof(int), st));
+    int cur = 0, launches = 0, derr = 0;
+    long long nin = 0;
+    T.in_tasks = nullptr;
+    while (true) {
+        T.nin = nin;
+        T.out_tasks = spill[cur ^ 1];
+        TC_CU(cudaMemsetAsync(ctl, 0, 2 * sizeof(unsigned long long), st));
+        TC_CU(cudaMemsetAsync(T.idle, 0, sizeof(int), st));
+        TC_TRY(launch_traverse(T, blocks, st));
+        ++launches;
+        unsigned long long nout = 0;
+        TC_CU(cudaMemcpyAsync(&nout, ctl + 1, sizeof(nout), cudaMemcpyDeviceToHost, st));
+        TC_CU(cudaMemcpyAsync(&derr, T.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        TC_CU(cudaStreamSynchronize(st));
+        if (derr || nout == 0) break;
+        if (launches >= 100000) {
+            set_last_error("traversal did not finish within 100000 relaunches");
+            return TC_ERR_DEVICE;
+        }
+        T.ngen = 0;
+        T.in_tasks = spill[cur ^ 1];
+        nin = (long long)nout;
+        cur ^= 1;
+    }
+    if (derr == DEV_SPILL_OVERFLOW || derr == DEV_STACK_OVERFLOW) {
+        set_last_error("the traversal needs more work-list space than the fixed scratch of the "
+                       "allocation-free call holds; use tc_corr2_process_auto");
+        return TC_ERR_DEVICE;
+    }
+    if (derr) {
+        set_last_error(std::string("device error: ") + dev_err_msg(derr));
+        return TC_ERR_DEVICE;
+    }
+    TC_TRY(launch_reduce(nwarps, nq, nb, wacc, wnp, tot, totnp, st));
+    double h_tot[NOALLOC_NQ * NOALLOC_MAXNB];
+    unsigned long long h_np[NOALLOC_MAXNB];
+    unsigned long long cnt[3];
+    TC_CU(cudaMemcpyAsync(h_tot, tot, sizeof(double) * (size_t)nq * nb, cudaMemcpyDeviceToHost, st));
+    TC_CU(cudaMemcpyAsync(h_np, totnp, sizeof(unsigned long long) * (size_t)nb,
+                          cudaMemcpyDeviceToHost, st));
+    TC_CU(cudaMemcpyAsync(cnt, ctl + 2, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    TC_CU(cudaStreamSynchronize(st));
+    c->stats.cell_pairs = (int64_t)cnt[0];
+    c->stats.accepted = (int64_t)cnt[1];
+    c->stats.escalated = (int64_t)cnt[2];
+    c->stats.launches = launches;
+    for (int k = 0; k < nb; ++k) {
+        c->weight[k] += h_tot[k];
+        if (!quick) {
+            c->meanr[k] += h_tot[nb + k];
+            c->meanlogr[k] += h_tot[2 * nb + k];
+            c->npairs[k] += (double)h_np[k];
+        }
+        if (c->d1 == TC_KDATA) {
+            if (c->xi0) c->xi0[k] += h_tot[3 * nb + k];
+        } else if (c->d1 == TC_GDATA) {
+            if (c->xi0) c->xi0[k] += h_tot[3 * nb + k];
+            if (c->xi1) c->xi1[k] += h_tot[4 * nb + k];
+            if (c->xi2) c->xi2[k] += h_tot[5 * nb + k];
+            if (c->xi3) c->xi3[k] += h_tot[6 * nb + k];
+        }
+    }
+    return TC_OK;
+}
+
 // Canonical depth-first dump of the tree (host walk over device-copied cells).
 int64_t field_dump(tc_field* f, double* xyz, float* swd, int64_t* ns, int32_t* depth, int64_t cap)
 {
@@ -646,6 +787,11 @@ int tc_corr2_process_cross(tc_corr2* c, tc_field* f1, tc_field* f2, int dots, in
     (void)dots;
     if (!f1 || !f2) { set_last_error("NULL field"); return TC_ERR_ARG; }
     return corr_process(c, f1, f2, quick, metric);
+}
+
+int tc_corr2_process_auto_noalloc(tc_corr2* c, tc_field* f, int quick, int metric)
+{
+    return corr_process_auto_noalloc(c, f, quick, metric);
 }
 
 int tc_corr2_trivially_zero(tc_corr2* c, int metric, int coords, double x1, double y1,

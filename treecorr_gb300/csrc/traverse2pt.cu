@@ -726,4 +726,36 @@ int launch_reduce(int nwarps, int nq, int nb, const double* wacc, const unsigned
     return 0;
 }
 
+
+// ---------------------------------------------------------------------------------------
+// Fixed traversal scratch for callers that cannot allocate device memory.
+//
+// One file-scope device array holds everything one traversal needs: the per-warp stacks,
+// the two spill lists, the per-warp FP64 bins, the reduced totals and the control words.
+// Its size is fixed at NOALLOC_BYTES (about 52 MiB); every GPU that loads this library holds
+// it until the process exits.  The host code must not use the array's name as an address
+// (that is only a host-side stand-in): noalloc_scratch() looks its device address up with
+// cudaGetSymbolAddress, once per device, with that device current.
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_BYTES];
+
+static void* g_noalloc_ptr[64] = {nullptr};
+
+int noalloc_scratch(void** base)
+{
+    int dev = 0;
+    TC_CU(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) {
+        set_last_error("device index out of range for the fixed traversal scratch");
+        return 1;
+    }
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        TC_CU(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_ptr[dev] = p;
+    }
+    *base = g_noalloc_ptr[dev];
+    return 0;
+}
+
 }  // namespace tc

@@ -41,6 +41,27 @@ struct TravParams {
     int* err;
 };
 
+// Fixed traversal scratch of the allocation-free entry point (traverse2pt.cu).
+static constexpr int NOALLOC_MAXW = 1024;           // warps launched at most
+static constexpr int NOALLOC_SCAP = 2048;           // work items per warp stack
+static constexpr int NOALLOC_MAXNB = 64;            // bins at most
+static constexpr int NOALLOC_NQ = 7;                // FP32 bin quantities at most
+static constexpr long long NOALLOC_SPILL = (long long)NOALLOC_MAXW * NOALLOC_SCAP;
+static constexpr size_t NOALLOC_OFF_STACKS = 0;
+static constexpr size_t NOALLOC_OFF_SPILL0 = NOALLOC_OFF_STACKS + sizeof(int2) * (size_t)NOALLOC_MAXW * NOALLOC_SCAP;
+static constexpr size_t NOALLOC_OFF_SPILL1 = NOALLOC_OFF_SPILL0 + sizeof(int2) * (size_t)NOALLOC_SPILL;
+static constexpr size_t NOALLOC_OFF_WACC = NOALLOC_OFF_SPILL1 + sizeof(int2) * (size_t)NOALLOC_SPILL;
+static constexpr size_t NOALLOC_OFF_WNP = NOALLOC_OFF_WACC + sizeof(double) * (size_t)NOALLOC_MAXW * NOALLOC_NQ * NOALLOC_MAXNB;
+static constexpr size_t NOALLOC_OFF_TOT = NOALLOC_OFF_WNP + 8 * (size_t)NOALLOC_MAXW * NOALLOC_MAXNB;
+static constexpr size_t NOALLOC_OFF_TOTNP = NOALLOC_OFF_TOT + sizeof(double) * (size_t)NOALLOC_NQ * NOALLOC_MAXNB;
+static constexpr size_t NOALLOC_OFF_CTL = NOALLOC_OFF_TOTNP + 8 * (size_t)NOALLOC_MAXNB;
+static constexpr size_t NOALLOC_OFF_IDLE = NOALLOC_OFF_CTL + 8 * 8;
+static constexpr size_t NOALLOC_OFF_ERR = NOALLOC_OFF_IDLE + 256;
+static constexpr size_t NOALLOC_BYTES = NOALLOC_OFF_ERR + 256;
+
+// Device address of the fixed scratch on the current device (looked up on first use).
+int noalloc_scratch(void** base);
+
 void launch_pack_cells(int ncap, const Cells& C, TCell* out, cudaStream_t st);
 size_t traverse_smem_bytes(int nq, int nb);
 int traverse_grid(int nq, int nb, int* blocks, int* nwarps);
