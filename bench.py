@@ -338,14 +338,17 @@ def run_reference(args, rank, world):
     f = O.OracleField("G", "spherical", cat["x"], cat["y"], cat["z"], cat["g1"], cat["g2"],
                       cat["w"], None, 0.0, 0.0, "mean", False, 3, 10)
     ntop = f.ntop()
-    # Size the per-step sample: rows until ~args.cpu_budget/steps seconds.
+    # Size the per-step sample: a range of top-level rows with at least 4 rows per thread
+    # (so that every core has work), grown until it takes ~cpu_budget/steps seconds.
     target = max(2.0, args.cpu_budget / max(args.steps, 1))
-    t0 = time.perf_counter()
-    rows = 0
-    while rows < ntop and time.perf_counter() - t0 < target:
-        O.process("G", "Arc", bins, f, rows=(rows, rows + 1), nthreads=nthreads)
-        rows += 1
-    rows = max(rows, 1)
+    rows = min(ntop, 4 * nthreads)
+    while True:
+        t0 = time.perf_counter()
+        O.process("G", "Arc", bins, f, rows=(0, rows), nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        if dt >= 0.5 * target or rows >= ntop:
+            break
+        rows = min(ntop, int(rows * max(1.5, min(4.0, target / max(dt, 1e-3)))))
     sample = (0, rows)
     for _ in range(args.warmup):
         O.process("G", "Arc", bins, f, rows=sample, nthreads=nthreads)

@@ -68,6 +68,7 @@ extern "C" {
 
 typedef struct tc_field tc_field;
 typedef struct tc_corr2 tc_corr2;
+typedef struct tc_corr3 tc_corr3;
 
 /* Counters of the last process call (no reference counterpart; the reference has none). */
 typedef struct tc_stats {
@@ -172,6 +173,32 @@ int tc_corr2_trivially_zero(tc_corr2* c, int metric, int coords,
 
 /* Counters of the last process call on c. */
 int tc_corr2_stats(const tc_corr2* c, tc_stats* out);
+
+/* 3-point correlation, GGG with LogMultipole binning: replaces BuildCorr3
+ * (src/Corr3.cpp:3599-3645) for the GGG class (pybind11 at src/Corr3.cpp:4207-4225).
+ * Arguments as the reference's (nubins = max_n; the u/v arguments are unused by
+ * LogMultipole).  Every output has nbins*nbins*(2*max_n+1) entries; zeta0..zeta7 are
+ * gam0r, gam0i, gam1r, gam1i, gam2r, gam2i, gam3r, gam3i.  meand1, meanlogd1, meanu and meanv
+ * are accepted and left untouched, as the reference's multipole code leaves them. */
+int tc_corr3_create(int d1, int d2, int d3, int bin_type, double minsep, double maxsep,
+                    int nbins, double binsize, double b, double a, double minu, double maxu,
+                    int nubins, double ubinsize, double bu, double minv, double maxv,
+                    int nvbins, double vbinsize, double bv, double minrpar, double maxrpar,
+                    double xp, double yp, double zp, double* zeta0, double* zeta1,
+                    double* zeta2, double* zeta3, double* zeta4, double* zeta5, double* zeta6,
+                    double* zeta7, double* meand1, double* meanlogd1, double* meand2,
+                    double* meanlogd2, double* meand3, double* meanlogd3, double* meanu,
+                    double* meanv, double* weight, double* weight_im, double* ntri,
+                    tc_corr3** out);
+
+void tc_corr3_free(tc_corr3* c);
+
+/* BaseCorr3.processAuto -> ProcessAutoc -> BaseCorr3::multipole (src/Corr3.cpp:3654-3669,
+ * 1124-1175): the G_n / Gamma_n multipole accumulation over one G field. */
+int tc_corr3_process_auto(tc_corr3* c, tc_field* f, int dots, int quick, int metric);
+
+/* Device time of the last tc_corr3_process_auto call in ms (no reference counterpart). */
+double tc_corr3_last_ms(const tc_corr3* c);
 
 /* SetOMPThreads / GetOMPThreads (src/Corr2.cpp:995-1011).  The GPU path has no host
  * threads to set: both return 1, which the Python layer accepts. */

@@ -90,6 +90,17 @@ def lib():
         L.tc_get_omp_threads.argtypes = []
         L.tc_last_error.restype = ctypes.c_char_p
         L.tc_last_error.argtypes = []
+        L.tc_corr3_create.restype = ctypes.c_int
+        cd_, ci_ = ctypes.c_double, ctypes.c_int
+        L.tc_corr3_create.argtypes = [ci_] * 4 + [cd_, cd_, ci_, cd_, cd_, cd_] + \
+            [cd_, cd_, ci_, cd_, cd_] + [cd_, cd_, ci_, cd_, cd_] + [cd_] * 5 + [dp] * 19 + \
+            [ctypes.POINTER(vp)]
+        L.tc_corr3_free.restype = None
+        L.tc_corr3_free.argtypes = [vp]
+        L.tc_corr3_process_auto.restype = ctypes.c_int
+        L.tc_corr3_process_auto.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.tc_corr3_last_ms.restype = ctypes.c_double
+        L.tc_corr3_last_ms.argtypes = [vp]
         L.tc_launch_count.restype = ctypes.c_longlong
         L.tc_launch_count.argtypes = []
         L.tc_stream.restype = ctypes.c_void_p
@@ -388,6 +399,61 @@ class KKCorr(BaseCorr2):
 
 class GGCorr(BaseCorr2):
     _dkind = 2
+
+
+class BaseCorr3:
+    """BaseCorr3 (src/Corr3.cpp:4228-4235): processAuto for GGG with LogMultipole binning."""
+
+    def processAuto(self, field, dots, quick, metric):
+        _check(lib().tc_corr3_process_auto(self._h, field._h, int(bool(dots)), int(bool(quick)),
+                                           int(metric)))
+
+    def processCross12(self, *args):
+        raise NotImplementedError("3-point cross correlations are not on the GPU path")
+
+    processCross21 = processCross = processCross12
+
+    def triviallyZero(self, *args):
+        raise NotImplementedError("triviallyZero for 3-point is not on the GPU path")
+
+    def last_ms(self):
+        """Device time of the last processAuto in ms (no reference counterpart)."""
+        return float(lib().tc_corr3_last_ms(self._h))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value and _lib is not None:
+            _lib.tc_corr3_free(h)
+            self._h = None
+
+
+class GGGCorr(BaseCorr3):
+    """GGGCorr (BuildCorr3, src/Corr3.cpp:3599-3645): outputs aliased, accumulated."""
+
+    def __init__(self, bin_type, minsep, maxsep, nbins, binsize, b, a, minu, maxu, nubins,
+                 ubinsize, bu, minv, maxv, nvbins, vbinsize, bv, minrpar, maxrpar, xp, yp, zp,
+                 zeta0, zeta1, zeta2, zeta3, zeta4, zeta5, zeta6, zeta7, meand1, meanlogd1,
+                 meand2, meanlogd2, meand3, meanlogd3, meanu, meanv, weight, weight_im, ntri):
+        arrs = [zeta0, zeta1, zeta2, zeta3, zeta4, zeta5, zeta6, zeta7, meand1, meanlogd1,
+                meand2, meanlogd2, meand3, meanlogd3, meanu, meanv, weight, weight_im, ntri]
+        size = int(nbins) * int(nbins) * (2 * int(nubins) + 1)
+        for a_ in arrs:
+            if a_ is None or a_.size == 0:
+                continue
+            if a_.dtype != np.float64 or not a_.flags["C_CONTIGUOUS"] or a_.size != size:
+                raise ValueError("3-point outputs must be contiguous float64 arrays of "
+                                 "nbins*nbins*(2*max_n+1) entries")
+        self._outs = arrs
+        h = ctypes.c_void_p()
+        _check(lib().tc_corr3_create(2, 2, 2, int(bin_type), float(minsep), float(maxsep),
+                                     int(nbins), float(binsize), float(b), float(a), float(minu),
+                                     float(maxu), int(nubins), float(ubinsize), float(bu),
+                                     float(minv), float(maxv), int(nvbins), float(vbinsize),
+                                     float(bv), float(minrpar), float(maxrpar), float(xp),
+                                     float(yp), float(zp),
+                                     *[_ptr(a_ if a_ is not None and a_.size else None)
+                                       for a_ in arrs], ctypes.byref(h)))
+        self._h = h
 
 
 def _not_on_path(name):

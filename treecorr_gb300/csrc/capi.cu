@@ -17,6 +17,7 @@
 #include "tc_internal.cuh"
 #include "tc_host.hpp"
 #include "traverse2pt.hpp"
+#include "multipole.hpp"
 
 namespace tc {
 
@@ -68,6 +69,17 @@ struct tc_field {
     BuildScratch S;
     int* d_err = nullptr;
     float build_ms = 0.f;
+    double* leafsums = nullptr;  // 4 per cell, built on first multipole use
+};
+
+struct tc_corr3 {
+    int bin_type = 0, nbins = 0, maxn = 0;
+    double minsep = 0., maxsep = 0., binsize = 0., b = 0., a = 0.;
+    double* zeta[8] = {nullptr};
+    double *meand2 = nullptr, *meanlogd2 = nullptr, *meand3 = nullptr, *meanlogd3 = nullptr;
+    double *weight = nullptr, *weight_im = nullptr, *ntri = nullptr;
+    MPScratch X;
+    double ms = 0.;
 };
 
 struct tc_corr2 {
@@ -88,6 +100,9 @@ struct tc_corr2 {
     unsigned long long* ctl = nullptr;   // root_next, nout, counters[3]
     int* idle = nullptr;
     int* d_err = nullptr;
+    std::vector<int2*> lev;              // per-level item buffers of the expansion
+    std::vector<long long> levcap;
+    ExpandSched* sched = nullptr;        // device-side schedule of the expansion
 };
 
 namespace {
@@ -109,7 +124,7 @@ int alloc_points(Points& P, int64_t n)
 void free_cells(Cells& C)
 {
     dfree(C.x); dfree(C.y); dfree(C.z); dfree(C.size); dfree(C.w); dfree(C.d1); dfree(C.d2);
-    dfree(C.n); dfree(C.start); dfree(C.left); dfree(C.right);
+    dfree(C.n); dfree(C.start); dfree(C.left); dfree(C.right); dfree(C.parent);
 }
 
 int alloc_cells(Cells& C, int64_t m)
@@ -117,7 +132,7 @@ int alloc_cells(Cells& C, int64_t m)
     TC_TRY(dalloc(&C.x, m)); TC_TRY(dalloc(&C.y, m)); TC_TRY(dalloc(&C.z, m));
     TC_TRY(dalloc(&C.size, m)); TC_TRY(dalloc(&C.w, m)); TC_TRY(dalloc(&C.d1, m));
     TC_TRY(dalloc(&C.d2, m)); TC_TRY(dalloc(&C.n, m)); TC_TRY(dalloc(&C.start, m));
-    TC_TRY(dalloc(&C.left, m)); TC_TRY(dalloc(&C.right, m));
+    TC_TRY(dalloc(&C.left, m)); TC_TRY(dalloc(&C.right, m)); TC_TRY(dalloc(&C.parent, m));
     return 0;
 }
 
@@ -132,7 +147,7 @@ void field_release(tc_field* f)
 {
     free_points(f->buf[0]); free_points(f->buf[1]); free_cells(f->cells);
     dfree(f->tcells); dfree(f->d_tops_raw); dfree(f->d_ntop); dfree(f->d_tops);
-    free_scratch(f->S); dfree(f->d_err);
+    free_scratch(f->S); dfree(f->d_err); dfree(f->leafsums);
 }
 
 int check_dev_err(int* d_err, cudaStream_t st)
@@ -165,9 +180,13 @@ int field_build(tc_field* f)
     TC_TRY(dalloc(&f->S.wstack, n));
     TC_TRY(dalloc(&f->S.counters, 2));
     TC_TRY(alloc_points(f->buf[1], n));
-    // Unused ids (inside list leaves) keep harmless contents.
+    // Unused ids (inside list leaves) keep harmless contents: no children, no points.
     TC_CU(cudaMemsetAsync(f->cells.left, 0xff, ncap * sizeof(int), st));
     TC_CU(cudaMemsetAsync(f->cells.right, 0xff, ncap * sizeof(int), st));
+    TC_CU(cudaMemsetAsync(f->cells.parent, 0xff, ncap * sizeof(int), st));
+    TC_CU(cudaMemsetAsync(f->cells.n, 0, ncap * sizeof(int), st));
+    TC_CU(cudaMemsetAsync(f->cells.w, 0, ncap * sizeof(float), st));
+    TC_CU(cudaMemsetAsync(f->cells.size, 0, ncap * sizeof(float), st));
     cudaEvent_t e0, e1;
     TC_CU(cudaEventCreate(&e0));
     TC_CU(cudaEventCreate(&e1));
@@ -307,6 +326,43 @@ int corr_scratch(tc_corr2* c, int nwarps, int nq)
 
 double sqr(double x) { return x * x; }
 
+// Accumulators of the level-by-level expansion (per-warp FP64 bins, totals, control words).
+int expand_scratch(tc_corr2* c, int nwarps, int nq)
+{
+    if (nwarps > c->nwarps_alloc || nq > c->nq_alloc || !c->ctl) {
+        dfree(c->wacc); dfree(c->wnp); dfree(c->tot); dfree(c->totnp); dfree(c->ctl);
+        dfree(c->d_err);
+        TC_TRY(dalloc(&c->wacc, (size_t)nwarps * nq * c->nbins));
+        TC_TRY(dalloc(&c->wnp, (size_t)nwarps * c->nbins));
+        TC_TRY(dalloc(&c->tot, (size_t)nq * c->nbins));
+        TC_TRY(dalloc(&c->totnp, (size_t)c->nbins));
+        TC_TRY(dalloc(&c->ctl, 8));
+        TC_TRY(dalloc(&c->d_err, 1));
+        c->nwarps_alloc = nwarps;
+        c->nq_alloc = nq;
+    }
+    return 0;
+}
+
+// Makes level L's item buffer hold at least `need` items, keeping its first `keep` items.
+int level_reserve(tc_corr2* c, int L, long long keep, long long need, cudaStream_t st)
+{
+    while ((int)c->lev.size() <= L) { c->lev.push_back(nullptr); c->levcap.push_back(0); }
+    if (c->levcap[L] >= need) return 0;
+    long long cap = std::max(need, 2 * c->levcap[L]);
+    int2* p = nullptr;
+    TC_TRY(dalloc(&p, (size_t)cap));
+    if (keep > 0)
+        TC_CU(cudaMemcpyAsync(p, c->lev[L], sizeof(int2) * (size_t)keep, cudaMemcpyDeviceToDevice, st));
+    TC_CU(cudaStreamSynchronize(st));
+    dfree(c->lev[L]);
+    c->lev[L] = p;
+    c->levcap[L] = cap;
+    return 0;
+}
+
+
+
 // MetricHelper<M>::DistSq on two host positions (include/Metric.h:143-147, 202-207, 668-682).
 double host_dist_sq(int coords, int metric, const double* p1, const double* p2)
 {
@@ -388,102 +444,122 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
         return TC_ERR_ARG;
     }
 
+    // Breadth-first expansion by levels: each launch takes a chunk of the deepest non-empty
+    // level (level 0 = the top-level pairs, generated on the fly) and appends the children to
+    // the next level, so memory stays bounded by (depth x 4 chunk) items.
     int blocks = 0, nwarps = 0;
-    TC_TRY(traverse_grid(nq, nb, &blocks, &nwarps));
+    TC_TRY(expand_grid(nq, nb, &blocks, &nwarps));
+    TC_TRY(expand_scratch(c, nwarps, nq));
+    T.nwarps = nwarps;
+    T.wacc = c->wacc; T.wnp = c->wnp; T.err = c->d_err;
+    T.counters = c->ctl + 2;
+    T.in_tasks = nullptr; T.nin = 0;
+    TC_CU(cudaMemsetAsync(c->wacc, 0, sizeof(double) * (size_t)nwarps * nq * nb, st));
+    TC_CU(cudaMemsetAsync(c->wnp, 0, sizeof(unsigned long long) * (size_t)nwarps * nb, st));
+    TC_CU(cudaMemsetAsync(c->ctl, 0, 8 * sizeof(unsigned long long), st));
+    TC_CU(cudaMemsetAsync(c->d_err, 0, sizeof(int), st));
     cudaEvent_t e0, e1;
     TC_CU(cudaEventCreate(&e0));
     TC_CU(cudaEventCreate(&e1));
-    for (int attempt = 0; attempt < 4; ++attempt) {
-        TC_TRY(corr_scratch(c, nwarps, nq));
-        T.stacks = c->stacks; T.stack_cap = c->stack_cap; T.nwarps = nwarps;
-        T.wacc = c->wacc; T.wnp = c->wnp; T.idle = c->idle; T.err = c->d_err;
-        T.root_next = c->ctl; T.nout = c->ctl + 1; T.counters = c->ctl + 2;
-        T.out_cap = c->spill_cap;
-        TC_CU(cudaMemsetAsync(c->wacc, 0, sizeof(double) * (size_t)nwarps * nq * nb, st));
-        TC_CU(cudaMemsetAsync(c->wnp, 0, sizeof(unsigned long long) * (size_t)nwarps * nb, st));
-        TC_CU(cudaMemsetAsync(c->ctl, 0, 8 * sizeof(unsigned long long), st));
-        TC_CU(cudaMemsetAsync(c->d_err, 0, sizeof(int), st));
-        TC_CU(cudaEventRecord(e0, st));
-        int cur = 0;
-        long long nin = 0;
-        T.in_tasks = nullptr;
-        int launches = 0;
-        int derr = 0;
-        while (true) {
-            T.nin = nin;
-            T.out_tasks = c->spill[cur ^ 1];
-            TC_CU(cudaMemsetAsync(c->ctl, 0, 2 * sizeof(unsigned long long), st));
-            TC_CU(cudaMemsetAsync(c->idle, 0, sizeof(int), st));
-            TC_TRY(launch_traverse(T, blocks, st));
-            ++launches;
-            unsigned long long nout = 0;
-            TC_CU(cudaMemcpyAsync(&nout, c->ctl + 1, sizeof(nout), cudaMemcpyDeviceToHost, st));
-            TC_CU(cudaMemcpyAsync(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
-            TC_CU(cudaStreamSynchronize(st));
-            if (derr) break;
-            if (nout == 0) break;
-            if (launches >= 100000) {
-                set_last_error("traversal did not finish within 100000 relaunches");
+    TC_CU(cudaEventRecord(e0, st));
+    // The schedule lives on the device: batches of (schedule, expand) launches run without
+    // host round trips; the host only adds level buffers when the expansion gets deeper.
+    // Chunk size: up to 4M items per launch, less for small catalogs (level buffers hold
+    // 4 chunks each).
+    long long CH = 1LL << 16;
+    while (CH < (1LL << 22) && CH < 2 * (f1->n + (f2 ? f2->n : 0))) CH <<= 1;
+    if (!c->sched) TC_TRY(dalloc(&c->sched, 1));
+    ExpandSched hs;
+    std::memset(&hs, 0, sizeof(hs));
+    hs.cnt[0] = T.ngen;
+    hs.cap = 4 * CH;
+    hs.chunk_max = CH;
+    hs.out_level = -1;
+    int nlev = 32;
+    for (int l = 1; l < nlev; ++l) {
+        TC_TRY(level_reserve(c, l, 0, hs.cap, st));
+        hs.lev[l] = c->lev[l];
+    }
+    hs.nlev = nlev;
+    TC_CU(cudaMemcpyAsync(c->sched, &hs, sizeof(hs), cudaMemcpyHostToDevice, st));
+    int derr = 0;
+    long long launches = 0;
+    for (int batch = 0;; ++batch) {
+        TC_TRY(launch_expand_batch(T, blocks, c->sched, 64, st));
+        int flags[3];
+        TC_CU(cudaMemcpyAsync(flags, &c->sched->done, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
+        TC_CU(cudaMemcpyAsync(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        TC_CU(cudaStreamSynchronize(st));
+        if (derr) break;
+        if (flags[1]) {   // need_levels: the expansion reached the last allocated level
+            if (nlev >= EXP_MAXLEV) {
+                set_last_error("the dual-tree expansion is deeper than 512 levels");
                 cudaEventDestroy(e0); cudaEventDestroy(e1);
                 return TC_ERR_DEVICE;
             }
-            // The spilled items become the roots of the next launch.
-            T.ngen = 0;
-            T.in_tasks = c->spill[cur ^ 1];
-            nin = (long long)nout;
-            cur ^= 1;
-        }
-        if (derr == DEV_SPILL_OVERFLOW || derr == DEV_STACK_OVERFLOW) {
-            // Retry with larger stacks and spill lists.
-            c->stack_cap *= 2;
-            c->spill_cap *= 4;
-            T.ngen = f2 ? T.ntop1 * T.ntop2 : T.ntop1 * (T.ntop1 + 1) / 2;
+            int nl2 = std::min(EXP_MAXLEV, 2 * nlev);
+            for (int l = nlev; l < nl2; ++l) {
+                TC_TRY(level_reserve(c, l, 0, hs.cap, st));
+                hs.lev[l] = c->lev[l];
+            }
+            TC_CU(cudaMemcpyAsync(&c->sched->lev[nlev], &hs.lev[nlev],
+                                  sizeof(int2*) * (nl2 - nlev), cudaMemcpyHostToDevice, st));
+            const int zero = 0;
+            TC_CU(cudaMemcpyAsync(&c->sched->nlev, &nl2, sizeof(int), cudaMemcpyHostToDevice, st));
+            TC_CU(cudaMemcpyAsync(&c->sched->need_levels, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
+            nlev = nl2;
             continue;
         }
-        if (derr) {
-            set_last_error(std::string("device error: ") + dev_err_msg(derr));
+        if (flags[0]) break;
+        if (batch > 1000000) {
+            set_last_error("traversal did not finish within 10^6 batches");
             cudaEventDestroy(e0); cudaEventDestroy(e1);
             return TC_ERR_DEVICE;
         }
-        TC_TRY(launch_reduce(nwarps, nq, nb, c->wacc, c->wnp, c->tot, c->totnp, st));
-        TC_CU(cudaEventRecord(e1, st));
-        std::vector<double> tot((size_t)nq * nb);
-        std::vector<unsigned long long> totnp(nb);
-        unsigned long long cnt[3];
-        TC_CU(cudaMemcpyAsync(tot.data(), c->tot, tot.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-        TC_CU(cudaMemcpyAsync(totnp.data(), c->totnp, nb * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-        TC_CU(cudaMemcpyAsync(cnt, c->ctl + 2, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-        TC_CU(cudaStreamSynchronize(st));
-        float ms = 0.f;
-        TC_CU(cudaEventElapsedTime(&ms, e0, e1));
-        cudaEventDestroy(e0); cudaEventDestroy(e1);
-        c->stats.cell_pairs = (int64_t)cnt[0];
-        c->stats.accepted = (int64_t)cnt[1];
-        c->stats.escalated = (int64_t)cnt[2];
-        c->stats.launches = launches;
-        c->stats.traverse_ms = ms;
-        // Corr2::finishProcess adds into the caller's arrays (src/Corr2.cpp:527-566).
-        for (int k = 0; k < nb; ++k) {
-            c->weight[k] += tot[k];
-            if (!quick) {
-                c->meanr[k] += tot[nb + k];
-                c->meanlogr[k] += tot[2 * nb + k];
-                c->npairs[k] += (double)totnp[k];
-            }
-            if (c->d1 == TC_KDATA) {
-                if (c->xi0) c->xi0[k] += tot[3 * nb + k];
-            } else if (c->d1 == TC_GDATA) {
-                if (c->xi0) c->xi0[k] += tot[3 * nb + k];
-                if (c->xi1) c->xi1[k] += tot[4 * nb + k];
-                if (c->xi2) c->xi2[k] += tot[5 * nb + k];
-                if (c->xi3) c->xi3[k] += tot[6 * nb + k];
-            }
-        }
-        return TC_OK;
     }
+    TC_CU(cudaMemcpyAsync(&launches, &c->sched->launches, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    TC_CU(cudaStreamSynchronize(st));
+    const long long launches_done = launches;
+    if (derr) {
+        set_last_error(std::string("device error: ") + dev_err_msg(derr));
+        cudaEventDestroy(e0); cudaEventDestroy(e1);
+        return TC_ERR_DEVICE;
+    }
+    TC_TRY(launch_reduce(nwarps, nq, nb, c->wacc, c->wnp, c->tot, c->totnp, st));
+    TC_CU(cudaEventRecord(e1, st));
+    std::vector<double> tot((size_t)nq * nb);
+    std::vector<unsigned long long> totnp(nb);
+    unsigned long long cntr[3];
+    TC_CU(cudaMemcpyAsync(tot.data(), c->tot, tot.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    TC_CU(cudaMemcpyAsync(totnp.data(), c->totnp, nb * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    TC_CU(cudaMemcpyAsync(cntr, c->ctl + 2, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    TC_CU(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    TC_CU(cudaEventElapsedTime(&ms, e0, e1));
     cudaEventDestroy(e0); cudaEventDestroy(e1);
-    set_last_error("traversal scratch still too small after retries");
-    return TC_ERR_DEVICE;
+    c->stats.cell_pairs = (int64_t)cntr[0];
+    c->stats.accepted = (int64_t)cntr[1];
+    c->stats.escalated = (int64_t)cntr[2];
+    c->stats.launches = launches_done;
+    c->stats.traverse_ms = ms;
+    // Corr2::finishProcess adds into the caller's arrays (src/Corr2.cpp:527-566).
+    for (int k = 0; k < nb; ++k) {
+        c->weight[k] += tot[k];
+        if (!quick) {
+            c->meanr[k] += tot[nb + k];
+            c->meanlogr[k] += tot[2 * nb + k];
+            c->npairs[k] += (double)totnp[k];
+        }
+        if (c->d1 == TC_KDATA) {
+            if (c->xi0) c->xi0[k] += tot[3 * nb + k];
+        } else if (c->d1 == TC_GDATA) {
+            if (c->xi0) c->xi0[k] += tot[3 * nb + k];
+            if (c->xi1) c->xi1[k] += tot[4 * nb + k];
+            if (c->xi2) c->xi2[k] += tot[5 * nb + k];
+            if (c->xi3) c->xi3[k] += tot[6 * nb + k];
+        }
+    }
+    return TC_OK;
 }
 
 // The auto-correlation of an already built field with the fixed traversal scratch: no
@@ -623,6 +699,62 @@ int corr_process_auto_noalloc(tc_corr2* c, tc_field* f, int quick, int metric)
             if (c->xi2) c->xi2[k] += h_tot[5 * nb + k];
             if (c->xi3) c->xi3[k] += h_tot[6 * nb + k];
         }
+    }
+    return TC_OK;
+}
+
+// BaseCorr3::multipole (auto) for GGG / LogMultipole, src/Corr3.cpp:1124-1175.
+int corr3_process_auto(tc_corr3* c, tc_field* f, int quick, int metric)
+{
+    if (!c || !f) { set_last_error("NULL argument"); return TC_ERR_ARG; }
+    if (f->dkind != TC_GDATA) { set_last_error("GGG needs a G field"); return TC_ERR_ARG; }
+    TC_TRY(check_metric(f->coords, metric));
+    if (f->n == 0) return TC_OK;
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    TC_TRY(field_build(f));
+    const int64_t ncap = 2 * f->n - 1;
+    if (!f->leafsums) {
+        TC_TRY(dalloc(&f->leafsums, 4 * (size_t)ncap));
+        TC_TRY(launch_leaf_sums((int)ncap, f->cells, f->leafsums, st));
+    }
+    MPParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.coords = f->coords; P.metric = metric; P.quick = quick ? 1 : 0;
+    P.nbins = c->nbins; P.maxn = c->maxn;
+    P.minsep = c->minsep; P.maxsep = c->maxsep; P.binsize = c->binsize; P.b = c->b; P.a = c->a;
+    // BaseCorr3 constructor, src/Corr3.cpp:107-115.
+    P.logminsep = std::log(c->minsep);
+    P.minsepsq = c->minsep * c->minsep; P.maxsepsq = c->maxsep * c->maxsep;
+    P.bsq = c->b * c->b; P.asq = c->a * c->a;
+    P.maxbsq_eff = P.maxsepsq * std::min(P.bsq, P.asq);
+    P.x = f->cells.x; P.y = f->cells.y; P.z = f->cells.z;
+    P.size = f->cells.size; P.w = f->cells.w; P.d1 = f->cells.d1; P.d2 = f->cells.d2;
+    P.n = f->cells.n; P.left = f->cells.left; P.right = f->cells.right;
+    P.ls = f->leafsums;
+    P.tops = f->d_tops; P.ntop = (int)f->tops.size();
+    const size_t Z = (size_t)c->nbins * c->nbins * (2 * c->maxn + 1);
+    std::vector<double> h(15 * Z);
+    cudaEvent_t e0, e1;
+    TC_CU(cudaEventCreate(&e0));
+    TC_CU(cudaEventCreate(&e1));
+    TC_CU(cudaEventRecord(e0, st));
+    int rc = run_multipole(P, c->X, P.ntop, st, h.data());
+    TC_CU(cudaEventRecord(e1, st));
+    TC_CU(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    c->ms = ms;
+    if (rc) return rc == 3 ? TC_ERR_UNSUPPORTED : (rc == 5 ? TC_ERR_NOMEM : TC_ERR_DEVICE);
+    // Corr3 adds into the caller's arrays (calculateZeta, src/Corr3.cpp:1861-1974).
+    for (int q = 0; q < 8; ++q)
+        if (c->zeta[q]) for (size_t i = 0; i < Z; ++i) c->zeta[q][i] += h[q * Z + i];
+    double* dst[7] = {c->meand2, c->meanlogd2, c->meand3, c->meanlogd3, c->weight, c->weight_im,
+                      c->ntri};
+    for (int q = 0; q < 7; ++q) {
+        if (quick && (q < 4 || q == 6)) continue;
+        if (dst[q]) for (size_t i = 0; i < Z; ++i) dst[q][i] += h[(8 + q) * Z + i];
     }
     return TC_OK;
 }
@@ -771,6 +903,8 @@ void tc_corr2_free(tc_corr2* c)
     if (!c) return;
     dfree(c->stacks); dfree(c->spill[0]); dfree(c->spill[1]); dfree(c->wacc); dfree(c->wnp);
     dfree(c->tot); dfree(c->totnp); dfree(c->ctl); dfree(c->idle); dfree(c->d_err);
+    for (auto& p : c->lev) dfree(p);
+    dfree(c->sched);
     delete c;
 }
 
@@ -823,6 +957,69 @@ int tc_corr2_stats(const tc_corr2* c, tc_stats* out)
     *out = c->stats;
     return TC_OK;
 }
+
+int tc_corr3_create(int d1, int d2, int d3, int bin_type, double minsep, double maxsep,
+                    int nbins, double binsize, double b, double a, double minu, double maxu,
+                    int nubins, double ubinsize, double bu, double minv, double maxv,
+                    int nvbins, double vbinsize, double bv, double minrpar, double maxrpar,
+                    double xp, double yp, double zp, double* zeta0, double* zeta1,
+                    double* zeta2, double* zeta3, double* zeta4, double* zeta5, double* zeta6,
+                    double* zeta7, double* meand1, double* meanlogd1, double* meand2,
+                    double* meanlogd2, double* meand3, double* meanlogd3, double* meanu,
+                    double* meanv, double* weight, double* weight_im, double* ntri,
+                    tc_corr3** out)
+{
+    (void)minu; (void)maxu; (void)ubinsize; (void)bu; (void)minv; (void)maxv; (void)nvbins;
+    (void)vbinsize; (void)bv; (void)meand1; (void)meanlogd1; (void)meanu; (void)meanv;
+    if (!out) { set_last_error("out is NULL"); return TC_ERR_ARG; }
+    *out = nullptr;
+    if (d1 != TC_GDATA || d2 != TC_GDATA || d3 != TC_GDATA) {
+        set_last_error("only GGG is on the GPU 3-point path");
+        return TC_ERR_UNSUPPORTED;
+    }
+    if (bin_type != TC_LOGMULTIPOLE) {
+        set_last_error("only LogMultipole binning is on the GPU 3-point path");
+        return TC_ERR_UNSUPPORTED;
+    }
+    const double big = std::numeric_limits<double>::max();
+    if (!(minrpar <= -big) || !(maxrpar >= big) || xp != 0. || yp != 0. || zp != 0.) {
+        set_last_error("min_rpar/max_rpar/period are not on the GPU path");
+        return TC_ERR_UNSUPPORTED;
+    }
+    if (nbins <= 0 || nubins < 0 || !(minsep > 0.) || !(maxsep > minsep) || !(binsize > 0.)) {
+        set_last_error("invalid binning");
+        return TC_ERR_ARG;
+    }
+    if (!zeta0 || !zeta1 || !zeta2 || !zeta3 || !zeta4 || !zeta5 || !zeta6 || !zeta7 ||
+        !meand2 || !meanlogd2 || !meand3 || !meanlogd3 || !weight || !weight_im || !ntri) {
+        set_last_error("missing output array");
+        return TC_ERR_ARG;
+    }
+    tc_corr3* c = new tc_corr3();
+    c->bin_type = bin_type; c->nbins = nbins; c->maxn = nubins;
+    c->minsep = minsep; c->maxsep = maxsep; c->binsize = binsize; c->b = b; c->a = a;
+    double* z[8] = {zeta0, zeta1, zeta2, zeta3, zeta4, zeta5, zeta6, zeta7};
+    for (int q = 0; q < 8; ++q) c->zeta[q] = z[q];
+    c->meand2 = meand2; c->meanlogd2 = meanlogd2; c->meand3 = meand3; c->meanlogd3 = meanlogd3;
+    c->weight = weight; c->weight_im = weight_im; c->ntri = ntri;
+    *out = c;
+    return TC_OK;
+}
+
+void tc_corr3_free(tc_corr3* c)
+{
+    if (!c) return;
+    free_mp_scratch(c->X);
+    delete c;
+}
+
+int tc_corr3_process_auto(tc_corr3* c, tc_field* f, int dots, int quick, int metric)
+{
+    (void)dots;
+    return corr3_process_auto(c, f, quick, metric);
+}
+
+double tc_corr3_last_ms(const tc_corr3* c) { return c ? c->ms : 0.; }
 
 int tc_set_omp_threads(int num_threads) { (void)num_threads; return 1; }
 int tc_get_omp_threads(void) { return 1; }

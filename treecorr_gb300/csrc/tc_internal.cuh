@@ -47,6 +47,7 @@ struct Cells {
     int* start;
     int* left;    // -1 for a leaf
     int* right;
+    int* parent;  // -1 for a top-level cell's root
 };
 
 // Traversal record of one cell, 64 bytes, read with four 16-byte loads.

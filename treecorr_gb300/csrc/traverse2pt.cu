@@ -405,6 +405,122 @@ __device__ __forceinline__ void stage_accumulate(int k, const float (&v)[7],
     __syncwarp();
 }
 
+// One work item: process2 for a self item (task.y < 0), else process11 for a cell pair.
+// Writes the children to ch (nch of them) and, for an accepted pair, its bin and values.
+__device__ __forceinline__ void eval_task(const TravParams& T, bool has, int2 task,
+                                          int2 (&ch)[4], int& nch, int& acc_k, float (&av)[7],
+                                          unsigned long long& acc_nn, long long& n_eval,
+                                          long long& n_acc, long long& n_esc)
+{
+    const bool arc = (T.metric == ARC);
+    const bool flat = (T.coords == FLAT);
+    if (has) {
+        ++n_eval;
+        const int i = task.x;
+        if (task.y < 0) {
+            // process2, src/Corr2.cpp:290-306.
+            const TCell A = T.c1[i];
+            const float w = A.b.w, s = A.a.w;
+            if (w != 0.f && !((double)s <= T.halfminsep)) {
+                int L = __float_as_int(A.c.w), R = __float_as_int(A.d.x);
+                if (L < 0 || R < 0) {
+                    atomicCAS(T.err, 0, DEV_BAD_CHILD);
+                } else {
+                    ch[0] = make_int2(L, -1); ch[1] = make_int2(R, -1); ch[2] = make_int2(L, R);
+                    nch = 3;
+                }
+            }
+        } else {
+            const int j = task.y;
+            const TCell A = T.c1[i];
+            const TCell B = T.c2[j];
+            if (A.b.w != 0.f && B.b.w != 0.f) {
+                const float dx = (A.a.x - B.a.x) + (A.b.x - B.b.x);
+                const float dy = (A.a.y - B.a.y) + (A.b.y - B.b.y);
+                const float dz = flat ? 0.f : (A.a.z - B.a.z) + (A.b.z - B.b.z);
+                const float dsq = dx * dx + dy * dy + dz * dz;
+                float rsq = dsq, theta = 0.f;
+                if (arc) {
+                    theta = 2.f * asinf(0.5f * sqrtf(dsq));
+                    rsq = theta * theta;
+                }
+                const float s1 = A.a.w, s2 = B.a.w;
+                Decision D = decide32(T, rsq, s1, s2, arc);
+                if (D.act == ACT_UNSURE) {
+                    ++n_esc;
+                    double ddx = T.x1[i] - T.x2[j], ddy = T.y1[i] - T.y2[j];
+                    double ddsq = ddx * ddx + ddy * ddy;
+                    if (!flat) { double ddz = T.z1[i] - T.z2[j]; ddsq += ddz * ddz; }
+                    D = decide64(T, ddsq, (double)s1, (double)s2);
+                    if (D.act == ACT_ACCEPT && arc) theta = D.r;
+                } else if (D.act == ACT_ACCEPT && arc) {
+                    D.r = theta;
+                }
+                if (D.act == ACT_ACCEPT) {
+                    ++n_acc;
+                    acc_k = D.k;
+                    const float ww = A.b.w * B.b.w;
+                    av[0] = ww;
+                    av[1] = ww * D.r;
+                    av[2] = ww * D.logr;
+                    acc_nn = (unsigned long long)__float_as_int(A.c.z) *
+                             (unsigned long long)__float_as_int(B.c.z);
+                    if (T.dkind == DK) {
+                        av[3] = A.c.x * B.c.x;
+                    } else if (T.dkind == DG) {
+                        float g1r = A.c.x, g1i = A.c.y, g2r = B.c.x, g2i = B.c.y;
+                        if (flat) {
+                            // ProjectHelper<Flat>::Project: r = p2 - p1 (ProjectHelper.h:126-136)
+                            float er, ei;
+                            expm2i(-dx, -dy, er, ei);
+                            cmul(g1r, g1i, er, ei, g1r, g1i);
+                            cmul(g2r, g2i, er, ei, g2r, g2i);
+                        } else if (T.coords == SPHERE) {
+                            // ProjectHelper<Sphere>::Project(c1,c2,z1,z2), ProjectHelper.h:370-388,
+                            // with the direction terms written on accurate differences:
+                            // y1*x2 - x1*y2 = x1*dy - y1*dx,  d = p1 - p2.
+                            const float x1 = A.a.x, y1 = A.a.y, z1 = A.a.z, z2 = B.a.z;
+                            const float sinA = x1 * dy - y1 * dx;
+                            const float cosA = dz + 0.5f * z2 * dsq;
+                            const float cosB = -dz + 0.5f * z1 * dsq;
+                            float e2r, e2i, e1r, e1i;
+                            expm2i(sinA, -cosA, e2r, e2i);
+                            expm2i(-sinA, -cosB, e1r, e1i);
+                            cmul(g2r, g2i, e2r, e2i, g2r, g2i);
+                            cmul(g1r, g1i, e1r, e1i, g1r, g1i);
+                        } else {
+                            project3d64(T, i, j, g1r, g1i, g2r, g2i);
+                        }
+                        // both_complex_prod(g2, g1), ProjectHelper.h:84-101.
+                        const float rr = g2r * g1r, ri = g2r * g1i, ir = g2i * g1r, ii = g2i * g1i;
+                        av[3] = rr + ii;   // xip
+                        av[4] = ri - ir;
+                        av[5] = rr - ii;   // xim
+                        av[6] = ri + ir;
+                    }
+                } else if (D.act != ACT_DROP) {
+                    const int L1 = __float_as_int(A.c.w), R1 = __float_as_int(A.d.x);
+                    const int L2 = __float_as_int(B.c.w), R2 = __float_as_int(B.d.x);
+                    if (D.act == ACT_SPLIT12) {
+                        if (L1 < 0 || L2 < 0) atomicCAS(T.err, 0, DEV_BAD_CHILD);
+                        else {
+                            ch[0] = make_int2(L1, L2); ch[1] = make_int2(L1, R2);
+                            ch[2] = make_int2(R1, L2); ch[3] = make_int2(R1, R2);
+                            nch = 4;
+                        }
+                    } else if (D.act == ACT_SPLIT1) {
+                        if (L1 < 0) atomicCAS(T.err, 0, DEV_BAD_CHILD);
+                        else { ch[0] = make_int2(L1, j); ch[1] = make_int2(R1, j); nch = 2; }
+                    } else {
+                        if (L2 < 0) atomicCAS(T.err, 0, DEV_BAD_CHILD);
+                        else { ch[0] = make_int2(i, L2); ch[1] = make_int2(i, R2); nch = 2; }
+                    }
+                }
+            }
+        }
+    }
+}
+
 __global__ void __launch_bounds__(TB) k_traverse(TravParams T)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -519,111 +635,7 @@ __global__ void __launch_bounds__(TB) k_traverse(TravParams T)
         int acc_k = -1;
         float av[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         unsigned long long acc_nn = 0ull;
-        if (has) {
-            ++n_eval;
-            const int i = task.x;
-            if (task.y < 0) {
-                // process2, src/Corr2.cpp:290-306.
-                const TCell A = T.c1[i];
-                const float w = A.b.w, s = A.a.w;
-                if (w != 0.f && !((double)s <= T.halfminsep)) {
-                    int L = __float_as_int(A.c.w), R = __float_as_int(A.d.x);
-                    if (L < 0 || R < 0) {
-                        atomicCAS(T.err, 0, DEV_BAD_CHILD);
-                    } else {
-                        ch[0] = make_int2(L, -1); ch[1] = make_int2(R, -1); ch[2] = make_int2(L, R);
-                        nch = 3;
-                    }
-                }
-            } else {
-                const int j = task.y;
-                const TCell A = T.c1[i];
-                const TCell B = T.c2[j];
-                if (A.b.w != 0.f && B.b.w != 0.f) {
-                    const float dx = (A.a.x - B.a.x) + (A.b.x - B.b.x);
-                    const float dy = (A.a.y - B.a.y) + (A.b.y - B.b.y);
-                    const float dz = flat ? 0.f : (A.a.z - B.a.z) + (A.b.z - B.b.z);
-                    const float dsq = dx * dx + dy * dy + dz * dz;
-                    float rsq = dsq, theta = 0.f;
-                    if (arc) {
-                        theta = 2.f * asinf(0.5f * sqrtf(dsq));
-                        rsq = theta * theta;
-                    }
-                    const float s1 = A.a.w, s2 = B.a.w;
-                    Decision D = decide32(T, rsq, s1, s2, arc);
-                    if (D.act == ACT_UNSURE) {
-                        ++n_esc;
-                        double ddx = T.x1[i] - T.x2[j], ddy = T.y1[i] - T.y2[j];
-                        double ddsq = ddx * ddx + ddy * ddy;
-                        if (!flat) { double ddz = T.z1[i] - T.z2[j]; ddsq += ddz * ddz; }
-                        D = decide64(T, ddsq, (double)s1, (double)s2);
-                        if (D.act == ACT_ACCEPT && arc) theta = D.r;
-                    } else if (D.act == ACT_ACCEPT && arc) {
-                        D.r = theta;
-                    }
-                    if (D.act == ACT_ACCEPT) {
-                        ++n_acc;
-                        acc_k = D.k;
-                        const float ww = A.b.w * B.b.w;
-                        av[0] = ww;
-                        av[1] = ww * D.r;
-                        av[2] = ww * D.logr;
-                        acc_nn = (unsigned long long)__float_as_int(A.c.z) *
-                                 (unsigned long long)__float_as_int(B.c.z);
-                        if (T.dkind == DK) {
-                            av[3] = A.c.x * B.c.x;
-                        } else if (T.dkind == DG) {
-                            float g1r = A.c.x, g1i = A.c.y, g2r = B.c.x, g2i = B.c.y;
-                            if (flat) {
-                                // ProjectHelper<Flat>::Project: r = p2 - p1 (ProjectHelper.h:126-136)
-                                float er, ei;
-                                expm2i(-dx, -dy, er, ei);
-                                cmul(g1r, g1i, er, ei, g1r, g1i);
-                                cmul(g2r, g2i, er, ei, g2r, g2i);
-                            } else if (T.coords == SPHERE) {
-                                // ProjectHelper<Sphere>::Project(c1,c2,z1,z2), ProjectHelper.h:370-388,
-                                // with the direction terms written on accurate differences:
-                                // y1*x2 - x1*y2 = x1*dy - y1*dx,  d = p1 - p2.
-                                const float x1 = A.a.x, y1 = A.a.y, z1 = A.a.z, z2 = B.a.z;
-                                const float sinA = x1 * dy - y1 * dx;
-                                const float cosA = dz + 0.5f * z2 * dsq;
-                                const float cosB = -dz + 0.5f * z1 * dsq;
-                                float e2r, e2i, e1r, e1i;
-                                expm2i(sinA, -cosA, e2r, e2i);
-                                expm2i(-sinA, -cosB, e1r, e1i);
-                                cmul(g2r, g2i, e2r, e2i, g2r, g2i);
-                                cmul(g1r, g1i, e1r, e1i, g1r, g1i);
-                            } else {
-                                project3d64(T, i, j, g1r, g1i, g2r, g2i);
-                            }
-                            // both_complex_prod(g2, g1), ProjectHelper.h:84-101.
-                            const float rr = g2r * g1r, ri = g2r * g1i, ir = g2i * g1r, ii = g2i * g1i;
-                            av[3] = rr + ii;   // xip
-                            av[4] = ri - ir;
-                            av[5] = rr - ii;   // xim
-                            av[6] = ri + ir;
-                        }
-                    } else if (D.act != ACT_DROP) {
-                        const int L1 = __float_as_int(A.c.w), R1 = __float_as_int(A.d.x);
-                        const int L2 = __float_as_int(B.c.w), R2 = __float_as_int(B.d.x);
-                        if (D.act == ACT_SPLIT12) {
-                            if (L1 < 0 || L2 < 0) atomicCAS(T.err, 0, DEV_BAD_CHILD);
-                            else {
-                                ch[0] = make_int2(L1, L2); ch[1] = make_int2(L1, R2);
-                                ch[2] = make_int2(R1, L2); ch[3] = make_int2(R1, R2);
-                                nch = 4;
-                            }
-                        } else if (D.act == ACT_SPLIT1) {
-                            if (L1 < 0) atomicCAS(T.err, 0, DEV_BAD_CHILD);
-                            else { ch[0] = make_int2(L1, j); ch[1] = make_int2(R1, j); nch = 2; }
-                        } else {
-                            if (L2 < 0) atomicCAS(T.err, 0, DEV_BAD_CHILD);
-                            else { ch[0] = make_int2(i, L2); ch[1] = make_int2(i, R2); nch = 2; }
-                        }
-                    }
-                }
-            }
-        }
+        eval_task(T, has, task, ch, nch, acc_k, av, acc_nn, n_eval, n_acc, n_esc);
         // Accumulate this iteration's accepted pairs (warp-converged here).
         if (__any_sync(0xffffffffu, acc_k >= 0))
             stage_accumulate(acc_k, av, acc_nn, nq, T.quick, stage, fb, np, nb, lane);
@@ -668,6 +680,124 @@ __global__ void __launch_bounds__(TB) k_traverse(TravParams T)
     }
 }
 
+// One level of the breadth-first expansion: every thread takes one work item of the input
+// array (or a generated root when in == nullptr), and the children of the whole launch are
+// appended to out.  The grid is fixed; warps stride over the input, so all lanes stay busy
+// and the launch is balanced.  Bins live in shared memory for the whole launch and are added
+// to the warp's global FP64 slot at the end (the slots persist across launches).
+__global__ void __launch_bounds__(TB, 5) k_expand(TravParams T, const int2* in, long long n_in,
+                                               long long gen0, int2* out,
+                                               unsigned long long* nout, long long out_cap,
+                                               const ExpandSched* S)
+{
+    if (S) {   // scheduled launch: the chunk comes from the device-side schedule
+        in = S->in; n_in = S->n_in; gen0 = S->gen0; out = S->out; out_cap = S->out_cap;
+        nout = const_cast<unsigned long long*>(&S->nout);
+        if (n_in <= 0) return;
+    }
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int gw = blockIdx.x * WPB + wib;
+    const int nq = T.nqf, nb = T.nbins;
+    const size_t wbytes = traverse_warp_bytes(nq, nb);
+    double* fd = (double*)(smem + wib * wbytes);
+    unsigned long long* np = (unsigned long long*)(fd + nq * nb);
+    float* fb = (float*)(np + 4 * nb);
+    float* stage = fb + 4 * nq * nb;
+    for (int q = lane; q < nq * nb; q += 32) fd[q] = 0.;
+    for (int q = lane; q < 4 * nb; q += 32) np[q] = 0ull;
+    for (int q = lane; q < 4 * nq * nb; q += 32) fb[q] = 0.f;
+    __syncwarp();
+    long long n_eval = 0, n_acc = 0, n_esc = 0;
+    const long long stride = (long long)gridDim.x * TB;
+    int iter = 0;
+    for (long long base = (long long)gw * 32; base < n_in; base += stride) {
+        const long long idx = base + lane;
+        const bool has = idx < n_in;
+        int2 task = make_int2(0, 0);
+        if (has) task = in ? in[idx] : make_root(T, gen0 + idx);
+        int nch = 0;
+        int2 ch[4];
+        int acc_k = -1;
+        float av[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        unsigned long long acc_nn = 0ull;
+        eval_task(T, has, task, ch, nch, acc_k, av, acc_nn, n_eval, n_acc, n_esc);
+        if (__any_sync(0xffffffffu, acc_k >= 0))
+            stage_accumulate(acc_k, av, acc_nn, nq, T.quick, stage, fb, np, nb, lane);
+        // Append the children: warp scan, one atomic per warp.
+        int off = nch;
+        for (int o = 1; o < 32; o <<= 1) {
+            int v = __shfl_up_sync(0xffffffffu, off, o);
+            if (lane >= o) off += v;
+        }
+        const int tot = __shfl_sync(0xffffffffu, off, 31);
+        off -= nch;
+        if (tot > 0) {
+            unsigned long long o0 = 0;
+            if (lane == 0) o0 = atomicAdd(nout, (unsigned long long)tot);
+            o0 = __shfl_sync(0xffffffffu, o0, 0);
+            if ((long long)(o0 + tot) > out_cap) {
+                if (lane == 0) atomicCAS(T.err, 0, DEV_SPILL_OVERFLOW);
+            } else {
+                for (int c = 0; c < nch; ++c) out[o0 + off + c] = ch[c];
+            }
+        }
+        if ((++iter % FLUSH) == 0) {
+            __syncwarp();
+            flush_bins(nq * nb, fb, fd, lane);
+            __syncwarp();
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        n_eval += __shfl_xor_sync(0xffffffffu, n_eval, o);
+        n_acc += __shfl_xor_sync(0xffffffffu, n_acc, o);
+        n_esc += __shfl_xor_sync(0xffffffffu, n_esc, o);
+    }
+    if (n_acc == 0) {   // nothing accumulated by this warp in this launch
+        if (lane == 0 && n_eval) atomicAdd(&T.counters[0], (unsigned long long)n_eval);
+        return;
+    }
+    __syncwarp();
+    flush_bins(nq * nb, fb, fd, lane);
+    __syncwarp();
+    double* wa = T.wacc + (size_t)gw * nq * nb;
+    for (int q = lane; q < nq * nb; q += 32) wa[q] += fd[q];
+    unsigned long long* wn = T.wnp + (size_t)gw * nb;
+    for (int q = lane; q < nb; q += 32) wn[q] += (np[q] + np[nb + q]) + (np[2 * nb + q] + np[3 * nb + q]);
+    if (lane == 0) {
+        atomicAdd(&T.counters[0], (unsigned long long)n_eval);
+        atomicAdd(&T.counters[1], (unsigned long long)n_acc);
+        atomicAdd(&T.counters[2], (unsigned long long)n_esc);
+    }
+}
+
+// The schedule step: commits the previous launch's children and picks the next chunk.
+__global__ void k_expand_sched(ExpandSched* S)
+{
+    if (S->out_level >= 0) {
+        S->cnt[S->out_level] += (long long)S->nout;
+        S->out_level = -1;
+    }
+    S->nout = 0;
+    S->n_in = 0;
+    if (S->done || S->need_levels) return;
+    int L = S->nlev - 1;
+    while (L >= 0 && S->cnt[L] == 0) --L;
+    if (L < 0) { S->done = 1; return; }
+    if (L + 1 >= S->nlev) { S->need_levels = 1; return; }
+    const long long chunk = S->cnt[L] < S->chunk_max ? S->cnt[L] : S->chunk_max;
+    const long long start = S->cnt[L] - chunk;
+    S->cnt[L] = start;
+    S->in = (L == 0) ? nullptr : S->lev[L] + start;
+    S->n_in = chunk;
+    S->gen0 = start;
+    S->out = S->lev[L + 1] + S->cnt[L + 1];
+    S->out_cap = S->cap - S->cnt[L + 1];
+    S->out_level = L + 1;
+    S->launches += 1;
+}
+
 // Sum of the per-warp totals in a fixed order: out[q*nb+k] (double), outnp[k] (u64).
 __global__ void k_reduce_acc(int nwarps, int nq, int nb, const double* wacc,
                              const unsigned long long* wnp, double* out,
@@ -703,6 +833,52 @@ int traverse_grid(int nq, int nb, int* blocks, int* nwarps)
     if (sm > 48 * 1024)
         TC_CU(cudaFuncSetAttribute(k_traverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     TC_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_traverse, TB, sm));
+    if (per < 1) per = 1;
+    *blocks = nsm * per;
+    *nwarps = *blocks * WPB;
+    return 0;
+}
+
+int launch_expand(const TravParams& T, int blocks, const int2* in, long long n_in,
+                  long long gen0, int2* out, unsigned long long* nout, long long out_cap,
+                  cudaStream_t st)
+{
+    size_t sm = traverse_smem_bytes(T.nqf, T.nbins);
+    static bool attr_set = false;
+    if (!attr_set && sm > 48 * 1024) {
+        TC_CU(cudaFuncSetAttribute(k_expand, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)traverse_smem_bytes(7, 256)));
+        attr_set = true;
+    }
+    count_launch();
+    k_expand<<<blocks, TB, sm, st>>>(T, in, n_in, gen0, out, nout, out_cap, nullptr);
+    TC_CU(cudaGetLastError());
+    return 0;
+}
+
+int launch_expand_batch(const TravParams& T, int blocks, ExpandSched* dS, int iters,
+                        cudaStream_t st)
+{
+    size_t sm = traverse_smem_bytes(T.nqf, T.nbins);
+    for (int it = 0; it < iters; ++it) {
+        count_launch();
+        k_expand_sched<<<1, 1, 0, st>>>(dS);
+        count_launch();
+        k_expand<<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
+    }
+    TC_CU(cudaGetLastError());
+    return 0;
+}
+
+int expand_grid(int nq, int nb, int* blocks, int* nwarps)
+{
+    int dev = 0, nsm = 0, per = 0;
+    TC_CU(cudaGetDevice(&dev));
+    TC_CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    size_t sm = traverse_smem_bytes(nq, nb);
+    if (sm > 48 * 1024)
+        TC_CU(cudaFuncSetAttribute(k_expand, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    TC_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_expand, TB, sm));
     if (per < 1) per = 1;
     *blocks = nsm * per;
     *nwarps = *blocks * WPB;

@@ -62,10 +62,34 @@ static constexpr size_t NOALLOC_BYTES = NOALLOC_OFF_ERR + 256;
 // Device address of the fixed scratch on the current device (looked up on first use).
 int noalloc_scratch(void** base);
 
+// Device-side schedule of the level-by-level expansion: a one-thread kernel picks the next
+// chunk (the deepest non-empty level first) so that launches need no host round trip.
+static constexpr int EXP_MAXLEV = 512;
+struct ExpandSched {
+    long long cnt[EXP_MAXLEV];     // items waiting per level (level 0: generated roots)
+    int2* lev[EXP_MAXLEV];         // item buffers (level 0 has none)
+    long long cap;                 // items per level buffer
+    long long chunk_max;
+    int nlev;                      // levels with a buffer
+    int done, need_levels, out_level;
+    const int2* in;                // current launch
+    long long n_in, gen0, out_cap;
+    int2* out;
+    unsigned long long nout;
+    long long launches;
+};
+
 void launch_pack_cells(int ncap, const Cells& C, TCell* out, cudaStream_t st);
 size_t traverse_smem_bytes(int nq, int nb);
 int traverse_grid(int nq, int nb, int* blocks, int* nwarps);
 int launch_traverse(const TravParams& T, int blocks, cudaStream_t st);
+int expand_grid(int nq, int nb, int* blocks, int* nwarps);
+// Enqueues `iters` (schedule, expand) pairs on st without synchronising.
+int launch_expand_batch(const TravParams& T, int blocks, ExpandSched* dS, int iters,
+                        cudaStream_t st);
+int launch_expand(const TravParams& T, int blocks, const int2* in, long long n_in,
+                  long long gen0, int2* out, unsigned long long* nout, long long out_cap,
+                  cudaStream_t st);
 int launch_reduce(int nwarps, int nq, int nb, const double* wacc, const unsigned long long* wnp,
                   double* out, unsigned long long* outnp, cudaStream_t st);
 

@@ -86,6 +86,7 @@ __device__ __forceinline__ void write_cell(const Cells& C, int id, double x, dou
     C.size[id] = size; C.w[id] = w; C.d1[id] = d1; C.d2[id] = d2;
     C.n[id] = n; C.start[id] = s;
     C.left[id] = -1; C.right[id] = -1;
+    C.parent[id] = parent;
     if (parent >= 0) {
         if (side == 0) C.left[parent] = id;
         else C.right[parent] = id;
