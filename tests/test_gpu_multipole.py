@@ -29,6 +29,16 @@ def gpu_multipole(T, s, cat, min_size, max_size):
     return out
 
 
+# G_n / W_n terms, their sums within a warp's run of records, and the products of the
+# contraction are FP32; every running sum is FP64.  Bound on max|gpu - ref| / max|ref| per
+# output array (the reference's own multipole test uses rtol 1e-4 on gam).
+TOL = 1e-5
+
+
+def max_rel_err(out, ref):
+    return {k: np.abs(out[k] - ref[k]).max() / max(np.abs(ref[k]).max(), 1e-300) for k in ref}
+
+
 @pytest.mark.parametrize("name", ["ggg_flat_mp", "ggg_flat_mp_n20", "ggg_flat_mp_bs0",
                                   "ggg_sphere_mp"])
 def test_multipole_golden(gpu_lib, name):
@@ -38,9 +48,24 @@ def test_multipole_golden(gpu_lib, name):
     cat = {k[3:]: g[k] for k in g.files if k.startswith("c1_")}
     out = gpu_multipole(gpu_lib, s, cat, float(g["min_size"]), float(g["max_size"]))
     assert np.array_equal(out["ntri"], g["ref_ntri"]), name
-    for k in MP_OUT:
-        r = g["ref_" + k]
-        scale = max(np.abs(r).max(), 1e-300)
-        err = np.abs(out[k] - r).max() / scale
-        # FP64 throughout; only the order of some sums differs from the reference.
-        assert err <= 1e-10, f"{name} {k}: {err:.3e}"
+    err = max_rel_err(out, {k: g["ref_" + k] for k in MP_OUT})
+    print(name, " ".join(f"{k}={v:.1e}" for k, v in err.items() if v > 0))
+    for k, v in err.items():
+        assert v <= TOL, f"{name} {k}: {v:.3e}"
+
+
+def test_multipole_record_waves(gpu_lib, monkeypatch):
+    """A record buffer of a few vertices forces many finish/contract waves and the in-place
+    FP64 contraction of records that do not fit; the result must not change."""
+    from cases3 import spec3
+    name = "ggg_flat_mp"
+    s = spec3(name)
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    cat = {k[3:]: g[k] for k in g.files if k.startswith("c1_")}
+    base = gpu_multipole(gpu_lib, s, cat, float(g["min_size"]), float(g["max_size"]))
+    monkeypatch.setenv("TCGPU_MP_RECORD_BYTES", str(40 * 16 * 1024))
+    small = gpu_multipole(gpu_lib, s, cat, float(g["min_size"]), float(g["max_size"]))
+    assert np.array_equal(small["ntri"], base["ntri"])
+    err = max_rel_err(small, {k: g["ref_" + k] for k in MP_OUT})
+    for k, v in err.items():
+        assert v <= TOL, f"{k}: {v:.3e}"

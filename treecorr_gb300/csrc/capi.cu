@@ -733,6 +733,7 @@ int corr3_process_auto(tc_corr3* c, tc_field* f, int quick, int metric)
     P.n = f->cells.n; P.left = f->cells.left; P.right = f->cells.right;
     P.ls = f->leafsums;
     P.tops = f->d_tops; P.ntop = (int)f->tops.size();
+    P.ncells = (int)ncap;
     const size_t Z = (size_t)c->nbins * c->nbins * (2 * c->maxn + 1);
     std::vector<double> h(15 * Z);
     cudaEvent_t e0, e1;

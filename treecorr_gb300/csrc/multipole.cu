@@ -12,18 +12,24 @@
 //     the c2 list with block-parallel decisions and a stable block scan, and emits one job
 //     (c1, c2 list) per cell that is small enough to start multipoleFinish.
 //   * Phase 2: persistent blocks take jobs from a counter.  A job runs multipoleFinish as a
-//     depth-first loop: each pass over the c2 list is block-parallel; the accepted c2 cells
-//     are added to the G_n / W_n scratch by warps that own disjoint bins (so no atomics, and
-//     each bin keeps the list order), with the powers z^n of a pair computed by one warp-wide
-//     multiplicative scan.  When c1 must split, the scratch is copied into a free slot and
-//     the right child is pushed, as the reference's mp.duplicate() does.  Rows of Zeta that
-//     are final are contracted into the block's private copy of the outputs.
-//   * A last kernel sums the private copies in block order.
-// All arithmetic is FP64 (the reference's precision); the cell payloads are the tree's
-// float values.
+//     depth-first loop: each pass over the c2 list is block-parallel; every accepted pair
+//     becomes a record of its FP64-computed terms stored as FP32 (phase z, projected shear,
+//     scalar sums).  The records are ranked stably by bin and split evenly over the warps;
+//     a warp forms z^n for n = 1..max_n+1 with one multiplicative warp scan per record, sums
+//     the G_n / W_n terms in FP32 and flushes them to the FP64 scratch.  When c1 must split,
+//     the scratch is copied into a free slot and the right child is pushed, as the
+//     reference's mp.duplicate() does.
+//   * Rows of Zeta that are final become vertex records (FP32 copies of G_n and W_n).  The
+//     contraction over vertices is a sum of outer products per n; k_mp_zeta runs it in
+//     batches (waves) between runs of the finish kernel, FP32 products with FP64 sums.
+//   * A last kernel sums the per-block outputs, the contraction partials and the diagonal
+//     self-pair corrections in a fixed order.
+// Geometry and the split/accept decisions are FP64 (the reference's arithmetic); the cell
+// payloads are the tree's float values.
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <vector>
 
 #include "tc_internal.cuh"
@@ -184,6 +190,16 @@ __device__ __forceinline__ int block_excl_scan(int v, int* sh, int& total)
 
 __device__ __forceinline__ void set_mp_err(int* err, int code) { atomicCAS(err, 0, code); }
 
+// A consistency check that failed: record the site, the caller skips the item.
+__device__ __forceinline__ void mp_check_fail(int* err, int site)
+{
+    atomicCAS(err, 0, MP_ERR_CHECK);
+    atomicCAS(err + 1, 0, site);
+}
+
+__device__ __forceinline__ bool mp_valid_cell(const MPParams& P, int c)
+{ return c >= 0 && c < P.ncells && P.n[c] > 0; }
+
 // ---------------------------------------------------------------------------------------
 // Phase 1: multipoleSplit1 + splitC2Cells, one block per top-level cell.
 
@@ -192,7 +208,7 @@ struct P1Entry { int c1, off, len, pad; };
 __global__ void __launch_bounds__(MB) k_mp_split1(MPParams P)
 {
     __shared__ P1Entry stk[MSTACK];
-    __shared__ int sp, top_rel, scan_sh[MW];
+    __shared__ int sp, top_rel, scan_sh[MW], have_sh;
     __shared__ P1Entry cur;
     const int b = blockIdx.x;
     int* arena = P.arena1 + (size_t)b * P.arena1_cap;
@@ -206,14 +222,19 @@ __global__ void __launch_bounds__(MB) k_mp_split1(MPParams P)
     __syncthreads();
     int guard = 0;
     while (true) {
+        // Thread 0 pops; everyone learns the outcome from a flag written before the barrier
+        // (reading sp directly would race with the pop).
         __syncthreads();
-        if (sp == 0) break;
+        if (tid == 0) {
+            have_sh = sp > 0;
+            if (have_sh) cur = stk[--sp];
+        }
+        __syncthreads();
+        if (!have_sh) break;
         if (++guard > (1 << 24)) {
             if (tid == 0) set_mp_err(P.err, MP_ERR_STACK);
             break;
         }
-        if (tid == 0) cur = stk[--sp];
-        __syncthreads();
         const int c1 = cur.c1;
         const double s1 = P.size[c1];
         const int base = top_rel;
@@ -221,8 +242,9 @@ __global__ void __launch_bounds__(MB) k_mp_split1(MPParams P)
         for (int j0 = 0; j0 < cur.len; j0 += MB) {
             const int j = j0 + tid;
             int cnt = 0, ca = -1, cb = -1;
-            if (j < cur.len) {
-                const int c2 = arena[cur.off + j];
+            const int c2 = j < cur.len ? __ldcg(arena + cur.off + j) : 0;
+            if (j < cur.len && !mp_valid_cell(P, c2)) mp_check_fail(P.err, 1);
+            else if (j < cur.len) {
                 const double s2 = P.size[c2];
                 const double rsq = mp_dist_sq(P, c1, c2);
                 const double s = s1 + s2;
@@ -274,27 +296,230 @@ struct P2Entry { int c1, len, slot, mink; long long goff; double maxr; long long
 __device__ __forceinline__ double* slot_ptr(const MPParams& P, int blk, int s)
 { return P.slots + ((size_t)blk * P.nslots + s) * P.slot_doubles; }
 
-// The Zeta contraction for rows k2 in [ks, mk) of vertex c1 (calculateZeta).
-__device__ void zeta_rows(const MPParams& P, int c1, const double* S, int ks, int mk, double* out,
-                          double* shG, double* shW)
+// Accepted-pair record (MP_REC floats): z (2), wg = g2 * e (2), w2, n2 (int), k (int), pad,
+// then the 14 scalar terms of calculateGn: w2, w2 r, w2 logr, sum w^2, (sum w^2) r,
+// (sum w^2) logr, sumwwgg0 (2), sumwwgg1 (2), sumwwgg2 (2), wg (2).
+static constexpr int REC_K = 6, REC_N = 5, REC_S = 8, NSCAL = 14;
+
+// Bin-ordered G_n / W_n accumulation of the records [0, nrec) of this block into slot S.
+// The records are ranked stably by bin (list order within a bin), then warp w takes the
+// w-th contiguous share of the ranked records.  A warp walks its share one record at a time:
+// lane l forms z^(l+1) (and z^(l+33)) by a multiplicative warp scan and adds the record's
+// W_n, G_{+n}, G_{-n} terms in FP32; lanes 0..13 add the scalar terms, lane 14 counts n2.
+// The FP32 partials go to FP64 registers every 32 records and to the slot (FP64 atomics,
+// since two warps can share a bin) when the bin changes.
+__device__ void mp_accumulate(const MPParams& P, const float* rec, int* perm, int nrec,
+                              double* S, int* bh, int (*bw)[MP_MAXNB])
+{
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int nb = P.nbins, M = P.maxn, gst = 2 * M + 3;
+    // Stable ranking by bin: bh holds the per-bin counts on entry.
+    if (tid == 0) {
+        int s = 0;
+        for (int k = 0; k < nb; ++k) { const int c = bh[k]; bh[k] = s; s += c; }
+        if (s != nrec) mp_check_fail(P.err, 8);   // counts and records disagree
+    }
+    for (int q = tid; q < MW * MP_MAXNB; q += MB) bw[q / MP_MAXNB][q % MP_MAXNB] = 0;
+    for (int a = tid; a < nrec; a += MB) perm[a] = -1;
+    __syncthreads();
+    for (int c0 = 0; c0 < nrec; c0 += MB) {
+        const int a = c0 + tid;
+        const int k = a < nrec ? __float_as_int(__ldcg(rec + (size_t)a * MP_REC + REC_K)) : nb;
+        const unsigned peers = __match_any_sync(0xffffffffu, k);
+        const int rank = __popc(peers & ((1u << lane) - 1u));
+        if (a < nrec && rank == 0) bw[wid][k] = __popc(peers);
+        __syncthreads();
+        if (a < nrec) {
+            int pos = bh[k] + rank;
+            for (int w = 0; w < wid; ++w) pos += bw[w][k];
+            perm[pos] = a;
+        }
+        __syncthreads();
+        if (tid < nb) {
+            int t = 0;
+            for (int w = 0; w < MW; ++w) { t += bw[w][tid]; bw[w][tid] = 0; }
+            bh[tid] += t;
+        }
+        __syncthreads();
+    }
+    for (int k = tid; k < nb; k += MB) bh[k] = 0;   // counts of the next batch
+    double* W = S;
+    double* G = S + 2 * (size_t)nb * (M + 1);
+    double* GG = G + 2 * (size_t)nb * gst;
+    double* SC = GG + 6 * (size_t)nb;
+    const int per = (nrec + MW - 1) / MW;
+    const int p0 = wid * per, p1 = min(nrec, p0 + per);
+    float F[12], fs = 0.f;
+    double D[12], ds = 0.;
+    unsigned long long npr = 0ull;
+#pragma unroll
+    for (int q = 0; q < 12; ++q) { F[q] = 0.f; D[q] = 0.; }
+    int curk = -1, cnt = 0;
+    auto flush = [&](int k) {
+#pragma unroll
+        for (int q = 0; q < 12; ++q) { D[q] += F[q]; F[q] = 0.f; }
+        ds += fs; fs = 0.f;
+        if (lane < 6) atomicAdd(&SC[(size_t)(lane + 1) * nb + k], ds);
+        else if (lane < 12) atomicAdd(&GG[(size_t)((lane - 6) >> 1) * 2 * nb + 2 * k + ((lane - 6) & 1)], ds);
+        else if (lane < 14) atomicAdd(&G[2 * ((size_t)k * gst + (M + 1)) + (lane - 12)], ds);
+        else if (lane == 14) atomicAdd(&SC[k], (double)npr);
+        if (lane == 0) atomicAdd(&W[2 * (size_t)k * (M + 1)], ds);
+        const int n = lane + 1, n1 = lane + 33;
+        if (n <= M) {
+            double* wp = W + 2 * ((size_t)k * (M + 1) + n);
+            atomicAdd(wp, D[0]); atomicAdd(wp + 1, D[1]);
+        }
+        if (n <= M + 1) {
+            double* gpp = G + 2 * ((size_t)k * gst + (M + 1) + n);
+            double* gmp = G + 2 * ((size_t)k * gst + (M + 1) - n);
+            atomicAdd(gpp, D[2]); atomicAdd(gpp + 1, D[3]);
+            atomicAdd(gmp, D[4]); atomicAdd(gmp + 1, D[5]);
+        }
+        if (n1 <= M) {
+            double* wp = W + 2 * ((size_t)k * (M + 1) + n1);
+            atomicAdd(wp, D[6]); atomicAdd(wp + 1, D[7]);
+        }
+        if (n1 <= M + 1) {
+            double* gpp = G + 2 * ((size_t)k * gst + (M + 1) + n1);
+            double* gmp = G + 2 * ((size_t)k * gst + (M + 1) - n1);
+            atomicAdd(gpp, D[8]); atomicAdd(gpp + 1, D[9]);
+            atomicAdd(gmp, D[10]); atomicAdd(gmp + 1, D[11]);
+        }
+#pragma unroll
+        for (int q = 0; q < 12; ++q) D[q] = 0.;
+        ds = 0.; npr = 0ull;
+    };
+    for (int p = p0; p < p1; ++p) {
+        const int pi = __ldcg(perm + p);
+        if (pi < 0 || pi >= nrec) {              // every rank is filled exactly once
+            if (lane == 0 && atomicCAS(P.err + 1, 0, 4) == 0) {
+                atomicCAS(P.err, 0, MP_ERR_CHECK);
+                P.dbg[0] = nrec; P.dbg[1] = p; P.dbg[2] = pi; P.dbg[3] = wid;
+                for (int q = 0; q < 16 && q < nrec; ++q) P.dbg[4 + q] = __ldcg(perm + q);
+            }
+            continue;
+        }
+        const float* r = rec + (size_t)pi * MP_REC;
+        const float4 h0 = __ldcg(reinterpret_cast<const float4*>(r));
+        const int k = __float_as_int(__ldcg(r + REC_K));
+        if (k < 0 || k >= nb) {
+            if (lane == 0) mp_check_fail(P.err, 5);
+            continue;
+        }
+        if (k != curk) {
+            if (curk >= 0) flush(curk);
+            curk = k; cnt = 0;
+        }
+        if (lane < NSCAL) fs += __ldcg(r + REC_S + lane);
+        else if (lane == NSCAL) npr += (unsigned long long)__float_as_int(__ldcg(r + REC_N));
+        const float zr = h0.x, zi = h0.y, wgr = h0.z, wgi = h0.w, w2 = __ldcg(r + 4);
+        float pre = zr, pim = zi;   // z^(lane+1)
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const float qr = __shfl_up_sync(0xffffffffu, pre, o);
+            const float qi = __shfl_up_sync(0xffffffffu, pim, o);
+            if (lane >= o) { const float t = qr * pre - qi * pim; pim = qr * pim + qi * pre; pre = t; }
+        }
+        F[0] += w2 * pre; F[1] += w2 * pim;
+        F[2] += wgr * pre - wgi * pim; F[3] += wgr * pim + wgi * pre;
+        F[4] += wgr * pre + wgi * pim; F[5] += wgi * pre - wgr * pim;
+        if (M + 1 > 32) {
+            const float z32r = __shfl_sync(0xffffffffu, pre, 31);
+            const float z32i = __shfl_sync(0xffffffffu, pim, 31);
+            const float qr = z32r * pre - z32i * pim, qi = z32r * pim + z32i * pre;
+            F[6] += w2 * qr; F[7] += w2 * qi;
+            F[8] += wgr * qr - wgi * qi; F[9] += wgr * qi + wgi * qr;
+            F[10] += wgr * qr + wgi * qi; F[11] += wgi * qr - wgr * qi;
+        }
+        if (++cnt == 32) {
+            cnt = 0;
+#pragma unroll
+            for (int q = 0; q < 12; ++q) { D[q] += F[q]; F[q] = 0.f; }
+            ds += fs; fs = 0.f;
+        }
+    }
+    if (curk >= 0) flush(curk);
+    __syncthreads();
+}
+
+// The n = 0 scalar outputs of calculateZeta for rows k2 in [ks, mk): ntri, meand2/3,
+// meanlogd2/3 (FP64, into the block's outputs).
+__device__ void zeta_scalars(const MPParams& P, int c1, const double* S, int ks, int mk,
+                             double* out)
 {
     const int nb = P.nbins, M = P.maxn, nn = 2 * M + 1;
-    const int gst = 2 * M + 3;          // complex entries per bin in Gn
+    const int gst = 2 * M + 3;
+    const size_t Z = (size_t)nb * nb * nn;
+    const double* SC = S + 2 * (size_t)nb * (M + 1) + 2 * (size_t)nb * gst + 6 * (size_t)nb;
+    // The slot was just updated by atomics: read it from L2.
+    auto npairs = [&](int k) { return __ldcg(SC + k); };
+    auto sumw = [&](int k) { return __ldcg(SC + nb + k); };
+    auto sumwr = [&](int k) { return __ldcg(SC + 2 * nb + k); };
+    auto sumwlogr = [&](int k) { return __ldcg(SC + 3 * nb + k); };
+    auto sumwwr = [&](int k) { return __ldcg(SC + 5 * nb + k); };
+    auto sumwwlogr = [&](int k) { return __ldcg(SC + 6 * nb + k); };
+    const double w1 = P.w[c1];
+    const double n1 = P.n[c1];
+    const int rows = mk - ks;
+    for (int t = threadIdx.x; t < rows * nb; t += MB) {
+        const int k2 = ks + t / nb, k3 = t % nb;
+        if (k3 < k2) continue;
+        const int i23 = (k2 * nb + k3) * nn + M;
+        if (k3 == k2) {
+            out[14 * Z + i23] += n1 * npairs(k2) * (npairs(k2) - 1);
+            double md = w1 * (sumw(k2) * sumwr(k2) - sumwwr(k2));
+            double ml = w1 * (sumw(k2) * sumwlogr(k2) - sumwwlogr(k2));
+            out[8 * Z + i23] += md; out[9 * Z + i23] += ml;
+            out[10 * Z + i23] += md; out[11 * Z + i23] += ml;
+        } else {
+            const int i32 = (k3 * nb + k2) * nn + M;
+            double nnn = n1 * npairs(k2) * npairs(k3);
+            out[14 * Z + i23] += nnn; out[14 * Z + i32] += nnn;
+            double ww12 = w1 * sumw(k2), ww13 = w1 * sumw(k3);
+            out[8 * Z + i23] += ww13 * sumwr(k2);  out[10 * Z + i32] += ww13 * sumwr(k2);
+            out[9 * Z + i23] += ww13 * sumwlogr(k2); out[11 * Z + i32] += ww13 * sumwlogr(k2);
+            out[10 * Z + i23] += ww12 * sumwr(k3); out[8 * Z + i32] += ww12 * sumwr(k3);
+            out[11 * Z + i23] += ww12 * sumwlogr(k3); out[9 * Z + i32] += ww12 * sumwlogr(k3);
+        }
+    }
+}
+
+// The self-pair corrections of the diagonal entries k2 == k3 (the same for every n), rows
+// [ks, mk): gam0 -= wg1 sumwwgg0, gam1 -= conj(wg1) sumwwgg1, gam2, gam3 -= wg1 sumwwgg2,
+// weight -= w1 sumww.  Stored positive in the block's diag array and subtracted at the end.
+__device__ void zeta_diag(const MPParams& P, int c1, const double* S, int ks, int mk,
+                          double* diag)
+{
+    const int nb = P.nbins, M = P.maxn, gst = 2 * M + 3;
+    const double* GG = S + 2 * (size_t)nb * (M + 1) + 2 * (size_t)nb * gst;
+    const double* sumww = GG + 6 * (size_t)nb + 4 * (size_t)nb;
+    const double w1 = P.w[c1];
+    const C2 wg1 = {(double)P.d1[c1], (double)P.d2[c1]};
+    for (int a = ks + threadIdx.x; a < mk; a += MB) {
+        const C2 t0 = cmul(wg1, {__ldcg(GG + 2 * a), __ldcg(GG + 2 * a + 1)});
+        const C2 t1 = cmul(conj2(wg1), {__ldcg(GG + 2 * nb + 2 * a), __ldcg(GG + 2 * nb + 2 * a + 1)});
+        const C2 t2 = cmul(wg1, {__ldcg(GG + 4 * nb + 2 * a), __ldcg(GG + 4 * nb + 2 * a + 1)});
+        diag[0 * nb + a] += t0.re; diag[1 * nb + a] += t0.im;
+        diag[2 * nb + a] += t1.re; diag[3 * nb + a] += t1.im;
+        diag[4 * nb + a] += t2.re; diag[5 * nb + a] += t2.im;
+        diag[6 * nb + a] += t2.re; diag[7 * nb + a] += t2.im;
+        diag[8 * nb + a] += w1 * __ldcg(sumww + a);
+    }
+}
+
+// The product terms of calculateZeta for the entries (a, b, n) with min(a, b) in [ks, mk),
+// in FP64 directly into the block's outputs: the path for a vertex record that does not fit
+// the record buffer.
+__device__ void zeta_products(const MPParams& P, int c1, const double* S, int ks, int mk,
+                              double* out, double* shG, double* shW)
+{
+    const int nb = P.nbins, M = P.maxn, nn = 2 * M + 1;
+    const int gst = 2 * M + 3;
     const size_t Z = (size_t)nb * nb * nn;
     const double* W = S;
     const double* G = S + 2 * (size_t)nb * (M + 1);
-    const double* GG = G + 2 * (size_t)nb * gst;
-    const double* SC = GG + 6 * (size_t)nb;
-    const double* npairs = SC;
-    const double* sumw = SC + nb;
-    const double* sumwr = SC + 2 * nb;
-    const double* sumwlogr = SC + 3 * nb;
-    const double* sumww = SC + 4 * nb;
-    const double* sumwwr = SC + 5 * nb;
-    const double* sumwwlogr = SC + 6 * nb;
-    // Stage G and W in shared memory.
-    for (int q = threadIdx.x; q < 2 * nb * gst; q += MB) shG[q] = G[q];
-    for (int q = threadIdx.x; q < 2 * nb * (M + 1); q += MB) shW[q] = W[q];
+    for (int q = threadIdx.x; q < 2 * nb * gst; q += MB) shG[q] = __ldcg(G + q);
+    for (int q = threadIdx.x; q < 2 * nb * (M + 1); q += MB) shW[q] = __ldcg(W + q);
     __syncthreads();
     const double w1 = P.w[c1];
     const C2 wg1 = {(double)P.d1[c1], (double)P.d2[c1]};
@@ -307,32 +532,6 @@ __device__ void zeta_rows(const MPParams& P, int c1, const double* S, int ks, in
         const double* p = shW + 2 * ((size_t)k * (M + 1) + (n >= 0 ? n : -n));
         return n >= 0 ? C2{p[0], p[1]} : C2{p[0], -p[1]};
     };
-    if (!P.quick) {
-        const double n1 = P.n[c1];
-        const int rows = mk - ks;
-        for (int t = threadIdx.x; t < rows * nb; t += MB) {
-            const int k2 = ks + t / nb, k3 = t % nb;
-            if (k3 < k2) continue;
-            const int i23 = (k2 * nb + k3) * nn + M;
-            if (k3 == k2) {
-                out[14 * Z + i23] += n1 * npairs[k2] * (npairs[k2] - 1);
-                double md = w1 * (sumw[k2] * sumwr[k2] - sumwwr[k2]);
-                double ml = w1 * (sumw[k2] * sumwlogr[k2] - sumwwlogr[k2]);
-                out[8 * Z + i23] += md; out[9 * Z + i23] += ml;
-                out[10 * Z + i23] += md; out[11 * Z + i23] += ml;
-            } else {
-                const int i32 = (k3 * nb + k2) * nn + M;
-                double nnn = n1 * npairs[k2] * npairs[k3];
-                out[14 * Z + i23] += nnn; out[14 * Z + i32] += nnn;
-                double ww12 = w1 * sumw[k2], ww13 = w1 * sumw[k3];
-                out[8 * Z + i23] += ww13 * sumwr[k2];  out[10 * Z + i32] += ww13 * sumwr[k2];
-                out[9 * Z + i23] += ww13 * sumwlogr[k2]; out[11 * Z + i32] += ww13 * sumwlogr[k2];
-                out[10 * Z + i23] += ww12 * sumwr[k3]; out[8 * Z + i32] += ww12 * sumwr[k3];
-                out[11 * Z + i23] += ww12 * sumwlogr[k3]; out[9 * Z + i32] += ww12 * sumwlogr[k3];
-            }
-        }
-    }
-    // Entries (a, b, n) with min(a, b) in [ks, mk).
     const int na = mk - ks;
     const long long cnt = (long long)na * nb * 2 * nn;   // pairs (a in rows, b >= a) and mirror
     for (long long t = threadIdx.x; t < cnt; t += MB) {
@@ -346,11 +545,10 @@ __device__ void zeta_rows(const MPParams& P, int c1, const double* S, int ks, in
         if (bb == aa && mirror) continue;
         const int a = mirror ? bb : aa, b = mirror ? aa : bb;
         const size_t i = (size_t)(a * nb + b) * nn + M + n;
-        const bool diag = (a == b);
         // weight (Porth et al. eq. 27)
-        if (diag) {
+        if (a == b) {
             C2 wv = Wv(a, n);
-            out[12 * Z + i] += w1 * ((wv.re * wv.re + wv.im * wv.im) - sumww[a]);
+            out[12 * Z + i] += w1 * (wv.re * wv.re + wv.im * wv.im);
         } else {
             C2 p = cmul(Wv(a, n), conj2(Wv(b, n)));
             out[12 * Z + i] += w1 * p.re;
@@ -361,20 +559,50 @@ __device__ void zeta_rows(const MPParams& P, int c1, const double* S, int ks, in
         C2 g1 = cmul(cmul(wg1c, Gv(a, n + 1)), Gv(b, -n + 1));
         C2 g2 = cmul(cmul(wg1, Gv(a, n - 1)), conj2(Gv(b, n + 1)));
         C2 g3 = cmul(cmul(wg1, conj2(Gv(a, -n + 1))), Gv(b, -n - 1));
-        if (diag) {
-            C2 c0 = {GG[2 * a], GG[2 * a + 1]};
-            C2 c1v = {GG[2 * nb + 2 * a], GG[2 * nb + 2 * a + 1]};
-            C2 c2v = {GG[4 * nb + 2 * a], GG[4 * nb + 2 * a + 1]};
-            C2 t0 = cmul(wg1, c0), t1 = cmul(wg1c, c1v), t2 = cmul(wg1, c2v);
-            g0.re -= t0.re; g0.im -= t0.im;
-            g1.re -= t1.re; g1.im -= t1.im;
-            g2.re -= t2.re; g2.im -= t2.im;
-            g3.re -= t2.re; g3.im -= t2.im;
-        }
         out[0 * Z + i] += g0.re; out[1 * Z + i] += g0.im;
         out[2 * Z + i] += g1.re; out[3 * Z + i] += g1.im;
         out[4 * Z + i] += g2.re; out[5 * Z + i] += g2.im;
         out[6 * Z + i] += g3.re; out[7 * Z + i] += g3.im;
+    }
+    __syncthreads();
+}
+
+// calculateZeta for vertex c1, rows [ks, mk): the scalar and diagonal parts now, and the
+// product terms as one vertex record for the batched contraction (k_mp_zeta).  Record:
+// header (c1, ks, mk, w1, wg1, pad x2), then G_n [n = -(M+1) .. M+1][bin] and W_n
+// [n = 0 .. M][bin], complex FP32.
+__device__ void zeta_emit(const MPParams& P, int c1, const double* S, int ks, int mk,
+                          double* out, double* diag, double* shG, double* shW,
+                          unsigned long long* zidx_sh)
+{
+    const int nb = P.nbins, M = P.maxn, gst = 2 * M + 3;
+    if (!P.quick) zeta_scalars(P, c1, S, ks, mk, out);
+    zeta_diag(P, c1, S, ks, mk, diag);
+    if (threadIdx.x == 0) *zidx_sh = atomicAdd(P.zcount, 1ull);
+    __syncthreads();
+    const unsigned long long zi = *zidx_sh;
+    if ((long long)zi < P.zcap) {
+        float* R = P.zrec + (size_t)zi * P.zrec_floats;
+        if (threadIdx.x == 0) {
+            R[0] = __int_as_float(c1); R[1] = __int_as_float(ks); R[2] = __int_as_float(mk);
+            R[3] = P.w[c1]; R[4] = P.d1[c1]; R[5] = P.d2[c1]; R[6] = 0.f; R[7] = 0.f;
+        }
+        const double* W = S;
+        const double* G = S + 2 * (size_t)nb * (M + 1);
+        float2* RG = reinterpret_cast<float2*>(R + 8);
+        float2* RW = RG + (size_t)gst * nb;
+        for (int q = threadIdx.x; q < gst * nb; q += MB) {
+            const int m = q / nb, a = q % nb;
+            const double* g = G + 2 * ((size_t)a * gst + m);
+            RG[q] = make_float2((float)__ldcg(g), (float)__ldcg(g + 1));
+        }
+        for (int q = threadIdx.x; q < (M + 1) * nb; q += MB) {
+            const int m = q / nb, a = q % nb;
+            const double* w = W + 2 * ((size_t)a * (M + 1) + m);
+            RW[q] = make_float2((float)__ldcg(w), (float)__ldcg(w + 1));
+        }
+    } else {
+        zeta_products(P, c1, S, ks, mk, out, shG, shW);
     }
     __syncthreads();
 }
@@ -385,10 +613,12 @@ __global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
     __shared__ P2Entry stk[MSTACK];
     __shared__ int sp, free_cnt, free_list[64], scan_sh[MW];
     __shared__ P2Entry cur;
-    __shared__ unsigned long long job_sh;
-    __shared__ int acc_n, new_n, anysplit, alloc_ok;
+    __shared__ unsigned long long job_sh, zidx_sh;
+    __shared__ int acc_n, new_n, anysplit, alloc_ok, have_sh;
     __shared__ double maxr_sh[MW];
     __shared__ long long arena_top;
+    __shared__ int bh[MP_MAXNB];
+    __shared__ int bw[MW][MP_MAXNB];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const int blk = blockIdx.x;
     const int nb = P.nbins, M = P.maxn;
@@ -396,22 +626,32 @@ __global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
     double* shG = mp_sh;
     double* shW = mp_sh + 2 * (size_t)nb * gst;
     int* arena = P.arena2 + (size_t)blk * P.arena2_cap;
-    // Accepted records of the current pass: c2, k (ints) and r, logr (doubles).
-    int* acc_c2 = P.acc_i + (size_t)blk * 2 * P.acc_cap;
-    double* acc_r = P.acc_d + (size_t)blk * 2 * P.acc_cap;
+    float* acc = P.acc + (size_t)blk * P.acc_cap * MP_REC;
+    int* perm = P.perm + (size_t)blk * P.acc_cap;
     double* out = P.out + (size_t)blk * P.out_stride;
+    double* diag = P.diag + (size_t)blk * 9 * nb;
     const int* arena1 = P.arena1;
+    for (int k = tid; k < MP_MAXNB; k += MB) bh[k] = 0;
 
     while (true) {
         if (tid == 0) {
-            job_sh = atomicAdd(P.job_next, 1ull);
             // After an error the results are discarded and the call is retried: stop early.
-            if (*(volatile int*)P.err) job_sh = (unsigned long long)P.njobs_val;
+            // With the vertex-record buffer nearly full, stop taking jobs until it is drained.
+            if (*(volatile int*)P.err ||
+                (long long)*(volatile unsigned long long*)P.zcount >= P.zstop)
+                job_sh = (unsigned long long)P.njobs_val;
+            else
+                job_sh = atomicAdd(P.job_next, 1ull);
         }
         __syncthreads();
         const unsigned long long job = job_sh;
         if ((long long)job >= P.njobs_val) break;
         const int4 J = P.jobs[job];
+        if (!mp_valid_cell(P, J.x) || J.y < 0 || J.y >= P.ntop || J.z < 0 || J.w < 0 ||
+            (long long)J.z + J.w > P.arena1_cap) {
+            if (tid == 0) mp_check_fail(P.err, 3);
+            break;
+        }
         if (tid == 0) {
             free_cnt = P.nslots;
             for (int s = 0; s < P.nslots; ++s) free_list[s] = P.nslots - 1 - s;
@@ -425,25 +665,47 @@ __global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
             stk[sp++] = e;
         }
         __syncthreads();
-        int guard = 0;
+        int guard = 0, stall = 0, stall_c1 = -1;
         {
             double* S0 = slot_ptr(P, blk, stk[0].slot);
             for (int q = tid; q < P.slot_doubles; q += MB) S0[q] = 0.;
         }
         __syncthreads();
         while (true) {
+            // Thread 0 pops (see k_mp_split1 for why the outcome goes through a flag).
             __syncthreads();
-            if (sp == 0) break;
             if (tid == 0) {
-                cur = stk[--sp];
-                arena_top = cur.mark;   // the finished left subtree's lists are dead
+                have_sh = sp > 0;
+                if (have_sh) {
+                    cur = stk[--sp];
+                    arena_top = cur.mark;   // the finished left subtree's lists are dead
+                }
             }
             __syncthreads();
+            if (!have_sh) break;
             // multipoleFinish loop on cur (c1 changes to its left child, the list to the new
             // list, the slot stays).
             while (true) {
                 if (++guard > (1 << 24)) {   // last-resort bound; the recursion is finite
-                    if (tid == 0) set_mp_err(P.err, MP_ERR_STACK);
+                    if (tid == 0) mp_check_fail(P.err, 6);
+                    break;
+                }
+                // Passes at one c1 refine its c2 list; their number is bounded by the depth
+                // of the c2 trees.
+                if (cur.c1 != stall_c1) { stall_c1 = cur.c1; stall = 0; }
+                if (++stall > 4096) {
+                    if (tid == 0 && atomicCAS(P.err + 1, 0, 7) == 0) {
+                        atomicCAS(P.err, 0, MP_ERR_CHECK);
+                        const int* l = (cur.goff >= 0) ? (arena1 + cur.goff) : (arena + (-cur.goff - 1));
+                        double* d = P.dbg;
+                        d[0] = cur.c1; d[1] = cur.len; d[2] = cur.maxr; d[3] = P.size[cur.c1];
+                        d[4] = P.left[cur.c1]; d[5] = cur.goff; d[6] = arena_top; d[7] = sp;
+                        d[8] = blk; d[9] = cur.mink;
+                        for (int q = 0; q < 8 && q < cur.len; ++q) {
+                            d[10 + 2 * q] = l[q];
+                            d[11 + 2 * q] = sqrt(mp_dist_sq(P, cur.c1, l[q])) + P.size[l[q]];
+                        }
+                    }
                     break;
                 }
                 const int c1 = cur.c1;
@@ -452,16 +714,18 @@ __global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
                 const int* list = (cur.goff >= 0) ? (arena1 + cur.goff) : nullptr;
                 const int* list2 = (cur.goff < 0) ? (arena + (-cur.goff - 1)) : nullptr;
                 const long long nbase = arena_top;
+                double* S = slot_ptr(P, blk, cur.slot);
                 if (tid == 0) { acc_n = 0; new_n = 0; anysplit = 0; }
                 double mymax = 0.;
                 int myany = 0;
                 __syncthreads();
                 for (int j0 = 0; j0 < cur.len; j0 += MB) {
                     const int j = j0 + tid;
-                    int cnt = 0, ca = -1, cb = -1, acc = 0, kacc = -1;
+                    int cnt = 0, ca = -1, cb = -1, acc_ok = 0, kacc = -1;
                     double racc = 0., lracc = 0.;
-                    if (j < cur.len) {
-                        const int c2 = list ? list[j] : list2[j];
+                    const int c2 = j < cur.len ? __ldcg(list ? list + j : list2 + j) : 0;
+                    if (j < cur.len && !mp_valid_cell(P, c2)) mp_check_fail(P.err, 2);
+                    else if (j < cur.len) {
                         const double s2 = P.size[c2];
                         const double rsq = mp_dist_sq(P, c1, c2);
                         const double s = s1 + s2;
@@ -475,7 +739,7 @@ __global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
                                         k = int((lr - P.logminsep) / P.binsize);
                                     }
                                     if (k >= nb) k = nb - 1;
-                                    acc = 1; kacc = k; racc = r; lracc = lr;
+                                    acc_ok = 1; kacc = k; racc = r; lracc = lr;
                                     ca = c2;
                                 }
                             } else {
@@ -498,30 +762,55 @@ __global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
                     }
                     int tot_new, tot_acc;
                     int pos = block_excl_scan(cnt, scan_sh, tot_new);
-                    int apos = block_excl_scan(acc, scan_sh, tot_acc);
+                    int apos = block_excl_scan(acc_ok, scan_sh, tot_acc);
                     const long long wbase = nbase + new_n;
                     if (wbase + tot_new > P.arena2_cap || acc_n + tot_acc > P.acc_cap) {
                         if (tid == 0) set_mp_err(P.err, MP_ERR_ARENA);
                     } else {
                         if (cnt >= 1) arena[wbase + pos] = ca;
                         if (cnt == 2) arena[wbase + pos + 1] = cb;
-                        if (acc) {
-                            const int a = acc_n + apos;
-                            acc_c2[2 * a] = ca;
-                            acc_c2[2 * a + 1] = kacc;
-                            acc_r[2 * a] = racc;
-                            acc_r[2 * a + 1] = lracc;
+                        if (acc_ok) {
+                            // calculateGn's per-pair terms (FP64, stored as FP32): ExpIPhi z,
+                            // the projected shear wg, and the scalar sums.
+                            C2 z, e;
+                            phases(P, c1, ca, racc, z, e);
+                            const double w2 = P.w[ca];
+                            const double* ls = P.ls + 4 * (size_t)ca;
+                            const C2 wg = cmul({(double)P.d1[ca], (double)P.d2[ca]}, e);
+                            const C2 wgsq = cmul({ls[1], ls[2]}, cmul(e, e));
+                            const C2 zsq = cmul(z, z);
+                            const C2 a0 = cmul(wgsq, conj2(zsq)), a1 = cmul(wgsq, zsq);
+                            float* R = acc + (size_t)(acc_n + apos) * MP_REC;
+                            *reinterpret_cast<float4*>(R) =
+                                make_float4((float)z.re, (float)z.im, (float)wg.re, (float)wg.im);
+                            *reinterpret_cast<float4*>(R + 4) =
+                                make_float4((float)w2, __int_as_float(P.n[ca]), __int_as_float(kacc), 0.f);
+                            *reinterpret_cast<float4*>(R + 8) =
+                                make_float4((float)w2, (float)(w2 * racc), (float)(w2 * lracc), (float)ls[0]);
+                            *reinterpret_cast<float4*>(R + 12) =
+                                make_float4((float)(ls[0] * racc), (float)(ls[0] * lracc), (float)a0.re, (float)a0.im);
+                            *reinterpret_cast<float4*>(R + 16) =
+                                make_float4((float)a1.re, (float)a1.im, (float)(ls[3] * zsq.re), (float)(-ls[3] * zsq.im));
+                            *reinterpret_cast<float4*>(R + 20) =
+                                make_float4((float)wg.re, (float)wg.im, 0.f, 0.f);
+                            atomicAdd(&bh[kacc], 1);
                         }
                     }
                     __syncthreads();
                     if (tid == 0) { new_n += tot_new; acc_n += tot_acc; }
                     __syncthreads();
+                    if (acc_n > P.acc_cap - MB) {      // record buffer full: accumulate now
+                        mp_accumulate(P, acc, perm, acc_n, S, bh, bw);
+                        if (tid == 0) acc_n = 0;
+                        __syncthreads();
+                    }
                 }
                 // An overflow of the arenas leaves the lists incomplete: stop this job (the
                 // call is retried with larger arenas).
                 if (tid == 0) alloc_ok = (*(volatile int*)P.err) ? 0 : 1;
                 __syncthreads();
                 if (!alloc_ok) break;
+                if (acc_n > 0) mp_accumulate(P, acc, perm, acc_n, S, bh, bw);
                 // Block max of the remaining separations and OR of anysplit1.
                 for (int o = 16; o > 0; o >>= 1) {
                     mymax = fmax(mymax, __shfl_xor_sync(0xffffffffu, mymax, o));
@@ -531,82 +820,17 @@ __global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
                 __syncthreads();
                 double maxrem = 0.;
                 for (int k = 0; k < MW; ++k) maxrem = fmax(maxrem, maxr_sh[k]);
-                const int n_acc = acc_n < P.acc_cap ? acc_n : P.acc_cap;
                 const int n_new = new_n;
-                // G_n / W_n accumulation: warp w owns the bins k with k % MW == w.
-                double* S = slot_ptr(P, blk, cur.slot);
-                {
-                    double* W = S;
-                    double* G = S + 2 * (size_t)nb * (M + 1);
-                    double* GG = G + 2 * (size_t)nb * gst;
-                    double* SC = GG + 6 * (size_t)nb;
-                    for (int a = 0; a < n_acc; ++a) {
-                        const int k = acc_c2[2 * a + 1];
-                        if (k % MW != wid) continue;
-                        const int c2 = acc_c2[2 * a];
-                        const double r = acc_r[2 * a], lr = acc_r[2 * a + 1];
-                        const double w2 = P.w[c2];
-                        C2 z, e;
-                        phases(P, c1, c2, r, z, e);
-                        const C2 wz = {(double)P.d1[c2], (double)P.d2[c2]};
-                        const C2 wg = cmul(wz, e);
-                        if (lane == 0) {
-                            const double* ls = P.ls + 4 * (size_t)c2;
-                            SC[k] += (double)P.n[c2];
-                            SC[nb + k] += w2;
-                            SC[2 * nb + k] += w2 * r;
-                            SC[3 * nb + k] += w2 * lr;
-                            SC[4 * nb + k] += ls[0];
-                            SC[5 * nb + k] += ls[0] * r;
-                            SC[6 * nb + k] += ls[0] * lr;
-                            const C2 wgsq = cmul({ls[1], ls[2]}, cmul(e, e));
-                            const C2 zsq = cmul(z, z);
-                            const C2 a0 = cmul(wgsq, conj2(zsq)), a1 = cmul(wgsq, zsq);
-                            const C2 a2 = {ls[3] * zsq.re, -ls[3] * zsq.im};
-                            GG[2 * k] += a0.re; GG[2 * k + 1] += a0.im;
-                            GG[2 * nb + 2 * k] += a1.re; GG[2 * nb + 2 * k + 1] += a1.im;
-                            GG[4 * nb + 2 * k] += a2.re; GG[4 * nb + 2 * k + 1] += a2.im;
-                            W[2 * (size_t)k * (M + 1)] += w2;
-                            double* g0 = G + 2 * ((size_t)k * gst + (M + 1));
-                            g0[0] += wg.re; g0[1] += wg.im;
-                        }
-                        // z^(lane+1) by a multiplicative warp scan; chunks of 32 powers.
-                        C2 p = z;
-                        for (int o = 1; o < 32; o <<= 1) {
-                            C2 q = {__shfl_up_sync(0xffffffffu, p.re, o), __shfl_up_sync(0xffffffffu, p.im, o)};
-                            if (lane >= o) p = cmul(q, p);
-                        }
-                        const C2 z32 = {__shfl_sync(0xffffffffu, p.re, 31), __shfl_sync(0xffffffffu, p.im, 31)};
-                        C2 base_pow = {1., 0.};
-                        for (int c = 0; 32 * c < M + 1; ++c) {
-                            const C2 pw = cmul(base_pow, p);     // z^(32c + lane + 1)
-                            const int n = 32 * c + lane + 1;
-                            if (n <= M) {
-                                double* wp = W + 2 * ((size_t)k * (M + 1) + n);
-                                wp[0] += w2 * pw.re; wp[1] += w2 * pw.im;
-                            }
-                            if (n <= M + 1) {
-                                const C2 gp = cmul(wg, pw), gm = cmul(wg, conj2(pw));
-                                double* gpp = G + 2 * ((size_t)k * gst + (M + 1) + n);
-                                double* gmp = G + 2 * ((size_t)k * gst + (M + 1) - n);
-                                gpp[0] += gp.re; gpp[1] += gp.im;
-                                gmp[0] += gm.re; gmp[1] += gm.im;
-                            }
-                            base_pow = cmul(base_pow, z32);
-                        }
-                    }
-                }
-                __syncthreads();
                 int mink = cur.mink;
                 if (n_new == 0) {
-                    zeta_rows(P, c1, S, 0, mink, out, shG, shW);
+                    zeta_emit(P, c1, S, 0, mink, out, diag, shG, shW, &zidx_sh);
                     break;
                 }
                 if (maxrem < P.maxsep) {
                     int k = maxrem < P.minsep ? 0
                           : int((log(maxrem) - P.logminsep) / P.binsize) + 1;
                     if (k < mink) {
-                        zeta_rows(P, c1, S, k, mink, out, shG, shW);
+                        zeta_emit(P, c1, S, k, mink, out, diag, shG, shW, &zidx_sh);
                         mink = k;
                     }
                 }
@@ -632,9 +856,9 @@ __global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
                 if (!alloc_ok) break;
                 if (split1) {
                     // The right child gets a copy of the scratch (mp.duplicate()).
-                    const double* src = slot_ptr(P, blk, cur.slot);
+                    const double* src = S;
                     double* dst = slot_ptr(P, blk, stk[sp - 1].slot);
-                    for (int q = tid; q < P.slot_doubles; q += MB) dst[q] = src[q];
+                    for (int q = tid; q < P.slot_doubles; q += MB) dst[q] = __ldcg(src + q);
                 }
                 __syncthreads();
                 // Without a split, the old list is dead unless a pushed entry still uses it:
@@ -647,7 +871,7 @@ __global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
                     for (long long i0 = 0; i0 < n_new; i0 += MB) {
                         const long long i = i0 + tid;
                         int v = 0;
-                        if (i < n_new) v = arena[nbase + i];
+                        if (i < n_new) v = __ldcg(arena + nbase + i);
                         __syncthreads();
                         if (i < n_new) arena[oo + i] = v;
                         __syncthreads();
@@ -672,14 +896,136 @@ __global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
     }
 }
 
-// Sum of the per-block output copies, in block order.
-__global__ void k_mp_reduce(int nblk, long long stride, long long total, const double* in,
-                            double* out)
+// ---------------------------------------------------------------------------------------
+// Batched Zeta contraction over vertex records.  For one n and a group of records the
+// block computes, for every entry (a, b) of the nbins x nbins tile,
+//   gam0 += (wg1 G_a[n-1]) G_b[-n-1]        gam1 += (conj(wg1) G_a[n+1]) G_b[-n+1]
+//   gam2 += (wg1 G_a[n-1]) conj(G_b[n+1])   gam3 += (wg1 conj(G_a[-n+1])) G_b[-n-1]
+//   weight += (w1 W_a[n]) conj(W_b[n])
+// over the records whose row range [ks, mk) holds min(a, b) -- a sum of outer products over
+// vertices.  Operands are staged in shared memory per chunk of records; products and chunk
+// sums are FP32, the running sums FP64; each group adds its sums to its own partial array.
+
+struct ZParams {
+    const float* rec;
+    long long nrec;
+    int rec_floats, nbins, maxn, chunk, ngroups;
+    double* part;          // [group][10][Z]
+    long long Z;
+};
+
+static constexpr int ZB = 256;   // threads per contraction block
+static constexpr int ZE = 2;     // entries per thread
+
+__global__ void __launch_bounds__(ZB) k_mp_zeta(ZParams Q)
 {
-    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= total) return;
+    extern __shared__ float4 zsh[];    // [chunk][nb][4]: (A0, A1), (A3, AW), (B0, B1), (B2, BW)
+    __shared__ int2 rows_sh[64];
+    const int nb = Q.nbins, M = Q.maxn, nn = 2 * M + 1, gst = 2 * M + 3;
+    const int n = (int)blockIdx.x - M;
+    const int g = blockIdx.y;
+    const int tid = threadIdx.x;
+    int ea[ZE], eb[ZE];
+    bool ev[ZE];
+#pragma unroll
+    for (int j = 0; j < ZE; ++j) {
+        const int e = ((int)blockIdx.z * ZE + j) * ZB + tid;
+        ev[j] = e < nb * nb;
+        ea[j] = ev[j] ? e / nb : 0;
+        eb[j] = ev[j] ? e % nb : 0;
+    }
+    double D[ZE][10];
+#pragma unroll
+    for (int j = 0; j < ZE; ++j)
+#pragma unroll
+        for (int q = 0; q < 10; ++q) D[j][q] = 0.;
+    const long long r0 = Q.nrec * g / Q.ngroups, r1 = Q.nrec * (g + 1) / Q.ngroups;
+    const int nw = (n >= 0) ? n : -n;
+    for (long long c0 = r0; c0 < r1; c0 += Q.chunk) {
+        const int nv = (int)min((long long)Q.chunk, r1 - c0);
+        __syncthreads();
+        for (int idx = tid; idx < nv * nb; idx += ZB) {
+            const int v = idx / nb, a = idx % nb;
+            const float* R = Q.rec + (size_t)(c0 + v) * Q.rec_floats;
+            const float2* RG = reinterpret_cast<const float2*>(R + 8);
+            const float2* RW = RG + (size_t)gst * nb;
+            const float w1 = R[3], wr = R[4], wi = R[5];
+            const float2 gm1 = RG[(n - 1 + M + 1) * nb + a];     // G[n-1]
+            const float2 gmm1 = RG[(-n - 1 + M + 1) * nb + a];   // G[-n-1]
+            const float2 gp1 = RG[(n + 1 + M + 1) * nb + a];     // G[n+1]
+            const float2 gmp1 = RG[(-n + 1 + M + 1) * nb + a];   // G[-n+1]
+            float2 w = RW[nw * nb + a];
+            if (n < 0) w.y = -w.y;
+            float4 o0, o1, o2, o3;
+            o0.x = wr * gm1.x - wi * gm1.y;  o0.y = wr * gm1.y + wi * gm1.x;     // A0
+            o0.z = wr * gp1.x + wi * gp1.y;  o0.w = wr * gp1.y - wi * gp1.x;     // A1
+            o1.x = wr * gmp1.x + wi * gmp1.y; o1.y = wi * gmp1.x - wr * gmp1.y;  // A3
+            o1.z = w1 * w.x;                 o1.w = w1 * w.y;                    // AW
+            o2 = make_float4(gmm1.x, gmm1.y, gmp1.x, gmp1.y);                   // B0, B1
+            o3 = make_float4(gp1.x, -gp1.y, w.x, -w.y);                         // B2, BW
+            float4* d = zsh + ((size_t)v * nb + a) * 4;
+            d[0] = o0; d[1] = o1; d[2] = o2; d[3] = o3;
+            if (a == 0) rows_sh[v] = make_int2(__float_as_int(R[1]), __float_as_int(R[2]));
+        }
+        __syncthreads();
+        float F[ZE][10];
+#pragma unroll
+        for (int j = 0; j < ZE; ++j)
+#pragma unroll
+            for (int q = 0; q < 10; ++q) F[j][q] = 0.f;
+        for (int v = 0; v < nv; ++v) {
+            const int2 rw = rows_sh[v];
+#pragma unroll
+            for (int j = 0; j < ZE; ++j) {
+                const int m = min(ea[j], eb[j]);
+                if (!ev[j] || m < rw.x || m >= rw.y) continue;
+                const float4* pa = zsh + ((size_t)v * nb + ea[j]) * 4;
+                const float4* pb = zsh + ((size_t)v * nb + eb[j]) * 4;
+                const float4 a01 = pa[0], a3w = pa[1], b01 = pb[2], b2w = pb[3];
+                F[j][0] += a01.x * b01.x - a01.y * b01.y;  F[j][1] += a01.x * b01.y + a01.y * b01.x;
+                F[j][2] += a01.z * b01.z - a01.w * b01.w;  F[j][3] += a01.z * b01.w + a01.w * b01.z;
+                F[j][4] += a01.x * b2w.x - a01.y * b2w.y;  F[j][5] += a01.x * b2w.y + a01.y * b2w.x;
+                F[j][6] += a3w.x * b01.x - a3w.y * b01.y;  F[j][7] += a3w.x * b01.y + a3w.y * b01.x;
+                F[j][8] += a3w.z * b2w.z - a3w.w * b2w.w;  F[j][9] += a3w.z * b2w.w + a3w.w * b2w.z;
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < ZE; ++j)
+#pragma unroll
+            for (int q = 0; q < 10; ++q) D[j][q] += F[j][q];
+    }
+#pragma unroll
+    for (int j = 0; j < ZE; ++j) {
+        if (!ev[j]) continue;
+        const size_t i = (size_t)(ea[j] * nb + eb[j]) * nn + M + n;
+        double* p = Q.part + (size_t)g * 10 * Q.Z + i;
+        if (ea[j] == eb[j]) D[j][9] = 0.;   // W_a conj(W_a) is real
+#pragma unroll
+        for (int q = 0; q < 10; ++q) p[(size_t)q * Q.Z] += D[j][q];
+    }
+}
+
+// Final sums, in a fixed order: the per-block outputs, the contraction groups' partials and
+// the diagonal corrections.
+__global__ void k_mp_reduce(int nblk, long long stride, long long Z, int nb, int nn,
+                            const double* in, const double* diag, long long diag_stride,
+                            int ngroups, const double* part, double* out)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 15 * Z) return;
+    const int q = (int)(i / Z);
+    const long long r = i % Z;
     double s = 0.;
     for (int b = 0; b < nblk; ++b) s += in[(size_t)b * stride + i];
+    const int qp = q < 8 ? q : (q == 12 ? 8 : (q == 13 ? 9 : -1));
+    if (qp >= 0)
+        for (int g = 0; g < ngroups; ++g) s += part[((size_t)g * 10 + qp) * Z + r];
+    const long long ab = r / nn;
+    const int a = (int)(ab / nb), b = (int)(ab % nb);
+    if (a == b && (q < 8 || q == 12)) {
+        const int d = q < 8 ? q : 8;
+        for (int bl = 0; bl < nblk; ++bl) s -= diag[(size_t)bl * diag_stride + (size_t)d * nb + a];
+    }
     out[i] = s;
 }
 
@@ -689,16 +1035,20 @@ __global__ void k_mp_reduce(int nblk, long long stride, long long total, const d
 size_t mp_slot_doubles(int nb, int M)
 { return 2 * (size_t)nb * (M + 1) + 2 * (size_t)nb * (2 * M + 3) + 13 * (size_t)nb; }
 
+static int mp_rec_floats(int nb, int M)
+{ return (8 + 2 * nb * (2 * M + 3) + 2 * nb * (M + 1) + 3) & ~3; }
+
 int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* h_out)
 {
-    const int nb = P.nbins, M = P.maxn;
-    const long long Z = (long long)nb * nb * (2 * M + 1);
+    const int nb = P.nbins, M = P.maxn, nn = 2 * M + 1;
+    const long long Z = (long long)nb * nb * nn;
     int dev = 0, nsm = 0;
     TC_CU(cudaGetDevice(&dev));
     TC_CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     const size_t shbytes = sizeof(double) * (2 * (size_t)nb * (2 * M + 3) + 2 * (size_t)nb * (M + 1));
-    if (shbytes > 200 * 1024) {
-        set_last_error("nbins * max_n too large for the multipole shared-memory staging");
+    if (shbytes > 160 * 1024 || M + 1 > 64 || nb > MP_MAXNB) {
+        set_last_error("the GPU multipole path needs max_n <= 63, nbins <= 128 and "
+                       "nbins * max_n within its shared-memory staging");
         return 3;
     }
     TC_CU(cudaFuncSetAttribute(k_mp_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shbytes));
@@ -708,10 +1058,17 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
     const int nblk = nsm * std::min(per, 2);
     P.slot_doubles = (long long)mp_slot_doubles(nb, M);
     P.out_stride = 15 * Z;
+    // Contraction geometry: records per shared-memory chunk, entry tiles, record groups.
+    const int chunk = (int)std::max<long long>(1, std::min<long long>(64, (96 * 1024) / (64LL * nb)));
+    const size_t zsh = (size_t)chunk * nb * 64;
+    TC_CU(cudaFuncSetAttribute(k_mp_zeta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zsh));
+    const int etiles = (nb * nb + ZE * ZB - 1) / (ZE * ZB);
+    const int ngroups = std::max(1, (4 * nsm + nn * etiles - 1) / (nn * etiles));
+    const int recf = mp_rec_floats(nb, M);
+    const long long acc_cap = 4096;
     X.want_a1 = std::max<long long>(X.want_a1, 4LL * ntop + (1 << 16));
     X.want_jobs = std::max<long long>(X.want_jobs, 1 << 18);
     X.want_a2 = std::max<long long>(X.want_a2, 1 << 20);
-    X.want_acc = std::max<long long>(X.want_acc, 1 << 16);
     X.want_slots = std::max(X.want_slots, 32);
     for (int attempt = 0; attempt < 4; ++attempt) {
         // Allocate what is requested (the requests grow after an overflow).
@@ -734,12 +1091,12 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
             TC_TRY(dalloc(&X.arena2, (size_t)X.want_a2 * nblk));
             X.arena2_cap = X.want_a2;
         }
-        if (X.acc_cap < X.want_acc || grow_blk) {
-            dfree(X.acc_i); dfree(X.acc_d);
+        if (X.acc_cap < acc_cap || grow_blk) {
+            dfree(X.acc); dfree(X.perm);
             X.acc_cap = 0;
-            TC_TRY(dalloc(&X.acc_i, (size_t)2 * X.want_acc * nblk));
-            TC_TRY(dalloc(&X.acc_d, (size_t)2 * X.want_acc * nblk));
-            X.acc_cap = X.want_acc;
+            TC_TRY(dalloc(&X.acc, (size_t)MP_REC * acc_cap * nblk));
+            TC_TRY(dalloc(&X.perm, (size_t)acc_cap * nblk));
+            X.acc_cap = acc_cap;
         }
         if (X.nslots < X.want_slots || grow_blk || P.slot_doubles != X.slot_doubles) {
             dfree(X.slots);
@@ -747,27 +1104,59 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
             TC_TRY(dalloc(&X.slots, (size_t)X.want_slots * P.slot_doubles * nblk));
             X.nslots = X.want_slots; X.slot_doubles = P.slot_doubles;
         }
-        if (grow_blk || P.out_stride > X.out_stride) {
-            dfree(X.out); dfree(X.total);
-            X.out_stride = 0;
+        if (grow_blk || P.out_stride > X.out_stride || 9LL * nb > X.diag_stride) {
+            dfree(X.out); dfree(X.total); dfree(X.diag);
+            X.out_stride = 0; X.diag_stride = 0;
             TC_TRY(dalloc(&X.out, (size_t)P.out_stride * nblk));
             TC_TRY(dalloc(&X.total, (size_t)P.out_stride));
-            X.out_stride = P.out_stride;
+            TC_TRY(dalloc(&X.diag, (size_t)9 * nb * nblk));
+            X.out_stride = P.out_stride; X.diag_stride = 9LL * nb;
+        }
+        {
+            // The vertex-record buffer: up to 4 GiB and a quarter of the free memory, or the
+            // byte count in TCGPU_MP_RECORD_BYTES (at least 16 records).
+            size_t budget = (size_t)4 << 30;
+            if (const char* ev = std::getenv("TCGPU_MP_RECORD_BYTES"))
+                budget = (size_t)std::max(0LL, std::atoll(ev));
+            const long long cap = std::max<long long>(16, (long long)(budget / (4ULL * recf)));
+            if (!X.zrec || X.zrec_floats != recf || X.zcap != cap) {
+                dfree(X.zrec);
+                X.zcap = 0;
+                size_t fr = 0, tot = 0;
+                TC_CU(cudaMemGetInfo(&fr, &tot));
+                const long long fit = std::max<long long>(16, (long long)(fr / 4 / (4ULL * recf)));
+                const long long c2 = std::min(cap, fit);
+                TC_TRY(dalloc(&X.zrec, (size_t)c2 * recf));
+                X.zcap = c2; X.zrec_floats = recf;
+            }
+        }
+        if (X.ngroups < ngroups || X.part_stride < 10 * Z) {
+            dfree(X.part);
+            X.ngroups = 0;
+            TC_TRY(dalloc(&X.part, (size_t)ngroups * 10 * Z));
+            X.ngroups = ngroups; X.part_stride = 10 * Z;
         }
         if (!X.ctl) TC_TRY(dalloc(&X.ctl, 4));
-        if (!X.err) TC_TRY(dalloc(&X.err, 1));
+        if (!X.err) TC_TRY(dalloc(&X.err, 2));
+        if (!X.dbg) TC_TRY(dalloc(&X.dbg, 32));
         X.nblk = std::max(X.nblk, nblk);
         P.arena1 = X.arena1; P.arena1_cap = X.arena1_cap;
         P.jobs = X.jobs; P.jobs_cap = X.jobs_cap;
-        P.njobs = X.ctl; P.job_next = X.ctl + 1;
+        P.njobs = X.ctl; P.job_next = X.ctl + 1; P.zcount = X.ctl + 2;
         P.arena2 = X.arena2; P.arena2_cap = X.arena2_cap;
-        P.acc_i = X.acc_i; P.acc_d = X.acc_d; P.acc_cap = (int)X.acc_cap;
+        P.acc = X.acc; P.perm = X.perm; P.acc_cap = (int)X.acc_cap;
         P.slots = X.slots; P.nslots = X.nslots;
         P.out = X.out;
+        P.diag = X.diag;
+        P.zrec = X.zrec; P.zcap = X.zcap; P.zrec_floats = recf;
+        P.zstop = X.zcap - std::min<long long>(X.zcap / 2, 64LL * nblk);
         P.err = X.err;
+        P.dbg = X.dbg;
         TC_CU(cudaMemsetAsync(X.ctl, 0, 4 * sizeof(unsigned long long), st));
-        TC_CU(cudaMemsetAsync(X.err, 0, sizeof(int), st));
+        TC_CU(cudaMemsetAsync(X.err, 0, 2 * sizeof(int), st));
         TC_CU(cudaMemsetAsync(X.out, 0, sizeof(double) * (size_t)P.out_stride * nblk, st));
+        TC_CU(cudaMemsetAsync(X.diag, 0, sizeof(double) * (size_t)9 * nb * nblk, st));
+        TC_CU(cudaMemsetAsync(X.part, 0, sizeof(double) * (size_t)ngroups * 10 * Z, st));
         count_launch();
         k_mp_split1<<<ntop, MB, 0, st>>>(P);
         TC_CU(cudaGetLastError());
@@ -776,19 +1165,51 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
         TC_CU(cudaMemcpyAsync(&nj, X.ctl, sizeof(nj), cudaMemcpyDeviceToHost, st));
         TC_CU(cudaMemcpyAsync(&e, X.err, sizeof(int), cudaMemcpyDeviceToHost, st));
         TC_CU(cudaStreamSynchronize(st));
-        if (e == 0) {
-            P.njobs_val = (long long)nj;
+        P.njobs_val = (long long)nj;
+        // Waves: the finish kernel runs jobs until the record buffer is nearly full, then the
+        // records are contracted and the buffer is reused.
+        for (int wave = 0; e == 0; ++wave) {
+            TC_CU(cudaMemsetAsync(X.ctl + 2, 0, sizeof(unsigned long long), st));
             count_launch();
             k_mp_finish<<<nblk, MB, shbytes, st>>>(P);
             TC_CU(cudaGetLastError());
+            unsigned long long c[3] = {0, 0, 0};
+            TC_CU(cudaMemcpyAsync(c, X.ctl, sizeof(c), cudaMemcpyDeviceToHost, st));
             TC_CU(cudaMemcpyAsync(&e, X.err, sizeof(int), cudaMemcpyDeviceToHost, st));
             TC_CU(cudaStreamSynchronize(st));
+            if (e) break;
+            ZParams Q;
+            Q.rec = X.zrec; Q.nrec = std::min<long long>((long long)c[2], X.zcap);
+            Q.rec_floats = recf; Q.nbins = nb; Q.maxn = M; Q.chunk = chunk;
+            Q.ngroups = ngroups; Q.part = X.part; Q.Z = Z;
+            if (Q.nrec > 0) {
+                count_launch();
+                k_mp_zeta<<<dim3(nn, ngroups, etiles), ZB, zsh, st>>>(Q);
+                TC_CU(cudaGetLastError());
+            }
+            if ((long long)c[1] >= P.njobs_val) break;
+            if (wave > (1 << 24)) { e = MP_ERR_STACK; break; }
         }
         if (e == MP_ERR_ARENA || e == MP_ERR_JOBS || e == MP_ERR_SLOTS) {
             X.want_a1 = X.arena1_cap * 4; X.want_jobs = X.jobs_cap * 4;
-            X.want_a2 = X.arena2_cap * 4; X.want_acc = X.acc_cap * 4;
+            X.want_a2 = X.arena2_cap * 4;
             X.want_slots = std::min(X.nslots * 2, 64);
             continue;
+        }
+        if (e == MP_ERR_CHECK) {
+            int site = 0;
+            double d[32];
+            TC_CU(cudaMemcpy(&site, X.err + 1, sizeof(int), cudaMemcpyDeviceToHost));
+            TC_CU(cudaMemcpy(d, X.dbg, sizeof(d), cudaMemcpyDeviceToHost));
+            std::string msg = "multipole: internal consistency check failed at site " +
+                              std::to_string(site);
+            if (site == 4 || site == 7) {
+                msg += " [";
+                for (int q = 0; q < 26; ++q) msg += std::to_string(d[q]) + " ";
+                msg += "]";
+            }
+            set_last_error(msg);
+            return 4;
         }
         if (e) {
             set_last_error("multipole: device stack overflow (tree too deep)");
@@ -796,7 +1217,7 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
         }
         count_launch();
         k_mp_reduce<<<(unsigned)((P.out_stride + 255) / 256), 256, 0, st>>>(
-            nblk, P.out_stride, P.out_stride, X.out, X.total);
+            nblk, P.out_stride, Z, nb, nn, X.out, X.diag, 9LL * nb, ngroups, X.part, X.total);
         TC_CU(cudaGetLastError());
         TC_CU(cudaMemcpyAsync(h_out, X.total, sizeof(double) * (size_t)P.out_stride,
                               cudaMemcpyDeviceToHost, st));
@@ -809,8 +1230,9 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
 
 void free_mp_scratch(MPScratch& X)
 {
-    dfree(X.arena1); dfree(X.jobs); dfree(X.arena2); dfree(X.acc_i); dfree(X.acc_d);
-    dfree(X.slots); dfree(X.out); dfree(X.total); dfree(X.ctl); dfree(X.err);
+    dfree(X.arena1); dfree(X.jobs); dfree(X.arena2); dfree(X.acc); dfree(X.perm);
+    dfree(X.slots); dfree(X.out); dfree(X.diag); dfree(X.total); dfree(X.zrec); dfree(X.part);
+    dfree(X.ctl); dfree(X.err); dfree(X.dbg);
     X = MPScratch();
 }
 

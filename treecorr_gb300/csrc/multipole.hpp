@@ -8,11 +8,17 @@
 
 namespace tc {
 
+// Floats per accepted-pair record of the G_n accumulation.
+constexpr int MP_REC = 24;
+// Largest nbins of the GPU multipole path (shared-memory bin counters).
+constexpr int MP_MAXNB = 128;
+
 enum MPErr : int {
     MP_ERR_ARENA = 11,   // a c2-list arena is full
     MP_ERR_JOBS = 12,    // the job list is full
     MP_ERR_SLOTS = 13,   // no free scratch slot for a c1 split
     MP_ERR_STACK = 14,   // a block-local stack is full
+    MP_ERR_CHECK = 15,   // a consistency check failed (err[1] names the site)
 };
 
 struct MPParams {
@@ -26,6 +32,7 @@ struct MPParams {
     const double* ls;
     const int* tops;
     int ntop;
+    int ncells;          // cell ids are 0 .. ncells-1
     // Phase 1: per-block list arenas and the job list.
     int* arena1;
     long long arena1_cap;
@@ -33,19 +40,27 @@ struct MPParams {
     long long jobs_cap;
     unsigned long long* njobs;
     long long njobs_val;
-    // Phase 2: job counter, per-block arenas, accepted-pair buffers, scratch slots, outputs.
+    // Phase 2: job counter, per-block arenas, accepted-pair records, scratch slots, outputs.
     unsigned long long* job_next;
     int* arena2;
     long long arena2_cap;
-    int* acc_i;
-    double* acc_d;
+    float* acc;          // per block: acc_cap records of MP_REC floats
+    int* perm;           // per block: acc_cap ints (records in bin order)
     int acc_cap;
     double* slots;
     int nslots;
     long long slot_doubles;
-    double* out;
+    double* out;         // per block: 15 arrays of nbins^2 (2 maxn + 1) doubles
     long long out_stride;
+    double* diag;        // per block: 9 x nbins self-pair corrections of the diagonal k2 == k3
+    // Vertex records for the batched contraction: zcount counts them; records at index
+    // >= zcap are contracted in place instead; jobs are not started once zcount >= zstop.
+    float* zrec;
+    long long zcap, zstop;
+    int zrec_floats;
+    unsigned long long* zcount;
     int* err;
+    double* dbg;         // 32 doubles describing the first failed check
 };
 
 // Device scratch of the multipole path, grown on demand and kept by the corr object.
@@ -57,20 +72,29 @@ struct MPScratch {
     long long jobs_cap = 0;
     int* arena2 = nullptr;
     long long arena2_cap = 0;
-    int* acc_i = nullptr;
-    double* acc_d = nullptr;
+    float* acc = nullptr;
+    int* perm = nullptr;
     long long acc_cap = 0;
     double* slots = nullptr;
     int nslots = 0;
     long long slot_doubles = 0;
     double* out = nullptr;
+    double* diag = nullptr;
     double* total = nullptr;
     long long out_stride = 0;
+    long long diag_stride = 0;
+    float* zrec = nullptr;
+    long long zcap = 0;
+    int zrec_floats = 0;
+    double* part = nullptr;     // per contraction group: 10 arrays of nbins^2 (2 maxn + 1)
+    long long part_stride = 0;
+    int ngroups = 0;
     int nblk = 0;
     unsigned long long* ctl = nullptr;
     int* err = nullptr;
+    double* dbg = nullptr;
     // Requested minimum capacities, raised after an overflow.
-    long long want_a1 = 0, want_jobs = 0, want_a2 = 0, want_acc = 0;
+    long long want_a1 = 0, want_jobs = 0, want_a2 = 0;
     int want_slots = 0;
 };
 
