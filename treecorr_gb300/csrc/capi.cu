@@ -70,6 +70,7 @@ struct tc_field {
     int* d_err = nullptr;
     float build_ms = 0.f;
     double* leafsums = nullptr;  // 4 per cell, built on first multipole use
+    float4* leafsums_f = nullptr;  // the same as floats
 };
 
 struct tc_corr3 {
@@ -147,7 +148,7 @@ void field_release(tc_field* f)
 {
     free_points(f->buf[0]); free_points(f->buf[1]); free_cells(f->cells);
     dfree(f->tcells); dfree(f->d_tops_raw); dfree(f->d_ntop); dfree(f->d_tops);
-    free_scratch(f->S); dfree(f->d_err); dfree(f->leafsums);
+    free_scratch(f->S); dfree(f->d_err); dfree(f->leafsums); dfree(f->leafsums_f);
 }
 
 int check_dev_err(int* d_err, cudaStream_t st)
@@ -716,7 +717,8 @@ int corr3_process_auto(tc_corr3* c, tc_field* f, int quick, int metric)
     const int64_t ncap = 2 * f->n - 1;
     if (!f->leafsums) {
         TC_TRY(dalloc(&f->leafsums, 4 * (size_t)ncap));
-        TC_TRY(launch_leaf_sums((int)ncap, f->cells, f->leafsums, st));
+        TC_TRY(dalloc(&f->leafsums_f, (size_t)ncap));
+        TC_TRY(launch_leaf_sums((int)ncap, f->cells, f->leafsums, f->leafsums_f, st));
     }
     MPParams P;
     std::memset(&P, 0, sizeof(P));
@@ -728,10 +730,17 @@ int corr3_process_auto(tc_corr3* c, tc_field* f, int quick, int metric)
     P.minsepsq = c->minsep * c->minsep; P.maxsepsq = c->maxsep * c->maxsep;
     P.bsq = c->b * c->b; P.asq = c->a * c->a;
     P.maxbsq_eff = P.maxsepsq * std::min(P.bsq, P.asq);
+    P.f_minsepsq = (float)P.minsepsq; P.f_maxsepsq = (float)P.maxsepsq; P.f_maxsep = (float)P.maxsep;
+    P.f_asq = (float)P.asq; P.f_bsq = (float)P.bsq;
+    P.f_q25 = (float)(0.25 * (P.binsize + P.b) * (P.binsize + P.b));
+    P.f_logminsep = (float)P.logminsep; P.f_binsize = (float)P.binsize; P.f_b = (float)P.b;
+    P.f_minba = (float)std::min(P.bsq, P.asq);
     P.x = f->cells.x; P.y = f->cells.y; P.z = f->cells.z;
     P.size = f->cells.size; P.w = f->cells.w; P.d1 = f->cells.d1; P.d2 = f->cells.d2;
     P.n = f->cells.n; P.left = f->cells.left; P.right = f->cells.right;
     P.ls = f->leafsums;
+    P.lsf = f->leafsums_f;
+    P.tc = f->tcells;
     P.tops = f->d_tops; P.ntop = (int)f->tops.size();
     P.ncells = (int)ncap;
     const size_t Z = (size_t)c->nbins * c->nbins * (2 * c->maxn + 1);

@@ -69,11 +69,22 @@ __global__ void k_leaf_sums(int ncap, Cells C, double* ls)
     }
 }
 
-int launch_leaf_sums(int ncap, const Cells& C, double* ls, cudaStream_t st)
+__global__ void k_leaf_sums_f(int ncap, const double* ls, float4* lsf)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ncap) return;
+    const double* p = ls + 4 * (size_t)i;
+    lsf[i] = make_float4((float)p[0], (float)p[1], (float)p[2], (float)p[3]);
+}
+
+int launch_leaf_sums(int ncap, const Cells& C, double* ls, float4* lsf, cudaStream_t st)
 {
     TC_CU(cudaMemsetAsync(ls, 0, 4 * sizeof(double) * (size_t)ncap, st));
     count_launch();
     k_leaf_sums<<<(ncap + 255) / 256, 256, 0, st>>>(ncap, C, ls);
+    TC_CU(cudaGetLastError());
+    count_launch();
+    k_leaf_sums_f<<<(ncap + 255) / 256, 256, 0, st>>>(ncap, ls, lsf);
     TC_CU(cudaGetLastError());
     return 0;
 }
@@ -128,6 +139,125 @@ __device__ __forceinline__ bool mp_too_small(const MPParams& P, double rsq, doub
 { return rsq < P.minsepsq && s < P.minsep && rsq < (P.minsep - s) * (P.minsep - s); }
 __device__ __forceinline__ bool mp_too_large(const MPParams& P, double rsq, double s)
 { return rsq >= P.maxsepsq && rsq >= (P.maxsep + s) * (P.maxsep + s); }
+
+// FP32 decisions.  Each comparison a < b is made with a relative margin: inside the margin
+// the entry is left to the FP64 code above, so every decision taken here equals the FP64
+// one.  Margins: 1e-5 for plain comparisons (FP32 rounding of rsq, s and the constants is
+// below 1e-6), 2e-4 where the fractional bin position enters (its FP32 error is below 1e-5).
+__device__ __forceinline__ int lt3(float a, float b, float m)
+{
+    const float d = m * (fabsf(a) + fabsf(b));
+    if (a < b - d) return 1;
+    if (a > b + d) return 0;
+    return -1;
+}
+
+// One (c1, c2) entry of a multipoleFinish pass in FP32.  Returns -1 (undecided: use FP64),
+// 0 (dropped: too small, too large, or accepted outside [min_sep, max_sep)), 1 (accepted
+// into bin k; r and logr returned) or 2 (not accepted: split flags, any = split1 and
+// r + s > thresh1, r returned).
+__device__ __forceinline__ int mp_decide32(const MPParams& P, float rsq, float s1, float s2,
+                                           float thresh1, int& k, float& r, float& logr,
+                                           bool& split1, bool& split2, bool& any)
+{
+    constexpr float M5 = 1e-5f, ML = 2e-4f;
+    const float s = s1 + s2;
+    // tooSmallDist: left to FP64 unless rsq is clearly >= min_sep^2.
+    if (lt3(rsq, P.f_minsepsq, M5) != 0) return -1;
+    const int below_max = lt3(rsq, P.f_maxsepsq, M5);
+    if (below_max < 0) return -1;
+    if (below_max == 0) {                       // tooLargeDist
+        const float ms = P.f_maxsep + s;
+        const int c = lt3(rsq, ms * ms, M5);
+        if (c < 0) return -1;
+        if (c == 0) return 0;
+    }
+    // BinTypeHelper<Log>::singleBin
+    bool sb;
+    int ik = -1;
+    float lr = 0.f;
+    if (s == 0.f) {
+        sb = true;
+    } else {
+        const float s2q = s * s;
+        int c = lt3(P.f_asq * rsq, s2q, M5);
+        if (c < 0) return -1;
+        if (c == 1) {
+            sb = false;
+        } else {
+            c = lt3(P.f_bsq * rsq, s2q, M5);
+            if (c < 0) return -1;
+            if (c == 0) {
+                sb = true;
+            } else {
+                c = lt3(P.f_q25 * rsq, s2q, M5);
+                if (c < 0) return -1;
+                if (c == 1) {
+                    sb = false;
+                } else {
+                    lr = 0.5f * logf(rsq);
+                    const float kk = (lr - P.f_logminsep) / P.f_binsize;
+                    ik = (int)kk;
+                    const float frac = kk - (float)ik;
+                    if (frac < ML || frac > 1.f - ML) return -1;
+                    const float f = fminf(frac, 1.f - frac);
+                    const float t4 = f * P.f_binsize + P.f_b;
+                    c = lt3(t4 * t4 * rsq, s2q, ML);
+                    if (c < 0) return -1;
+                    if (c == 1) {
+                        sb = false;
+                    } else {
+                        const float t5 = frac * P.f_binsize + P.f_b - s2q / rsq;
+                        c = lt3(t5 * t5 * rsq, s2q, ML);
+                        if (c < 0) return -1;
+                        sb = (c != 1);
+                    }
+                }
+            }
+        }
+    }
+    r = sqrtf(rsq);
+    if (sb) {
+        if (below_max == 0) return 0;           // isRSqInRange fails
+        if (ik < 0) {
+            lr = logf(r);
+            const float kk = (lr - P.f_logminsep) / P.f_binsize;
+            ik = (int)kk;
+            const float frac = kk - (float)ik;
+            if (frac < ML || frac > 1.f - ML) return -1;
+        }
+        k = ik < P.nbins ? ik : P.nbins - 1;
+        logr = lr;
+        return 1;
+    }
+    // CalcSplitSq (include/Split.h:82-101); s1, s2 are the cells' float sizes, so the size
+    // comparisons are exact.
+    const float bsq_eff = rsq * P.f_minba;
+    if (s2 > s1) {
+        split2 = true;
+        if (s2 > 2.f * s1) split1 = false;
+        else {
+            const int c = lt3(0.3422f * bsq_eff, s1 * s1, M5);
+            if (c < 0) return -1;
+            split1 = (c == 1);
+        }
+    } else {
+        split1 = true;
+        if (s1 > 2.f * s2) split2 = false;
+        else {
+            const int c = lt3(0.3422f * bsq_eff, s2 * s2, M5);
+            if (c < 0) return -1;
+            split2 = (c == 1);
+        }
+    }
+    any = false;
+    if (split1) {
+        const int c = lt3(thresh1, r + s, M5);
+        if (c < 0) return -1;
+        any = (c == 1);
+    }
+    return 2;
+}
 
 // calculate_direction(p1, p2) of include/ProjectHelper.h:272-345 (unnormalised).
 __device__ __forceinline__ C2 direction(double x1, double y1, double z1, double x2, double y2,
@@ -290,16 +420,19 @@ __global__ void __launch_bounds__(MB) k_mp_split1(MPParams P)
 
 struct P2Entry { int c1, len, slot, mink; long long goff; double maxr; long long mark; };
 
-// Scratch slot layout (doubles): Wn [nb][M+1] complex, Gn [nb][2M+3] complex (n = -(M+1) ..
-// M+1), gg0/gg1/gg2 [nb] complex, then npairs, sumw, sumwr, sumwlogr, sumww, sumwwr,
-// sumwwlogr [nb].
+// Scratch slot layout (doubles): W_n [n = 0 .. M][bin] complex, G_n [n + M + 1 = 0 .. 2M+2]
+// [bin] complex, gg0/gg1/gg2 [bin] complex, then npairs, sumw, sumwr, sumwlogr, sumww,
+// sumwwr, sumwwlogr [bin].  The [n][bin] order is the vertex record's order.
+__device__ __forceinline__ size_t sW(int nb, int n, int k) { return 2 * ((size_t)n * nb + k); }
+__device__ __forceinline__ size_t sG(int nb, int M, int n, int k)
+{ return 2 * ((size_t)(n + M + 1) * nb + k); }
 __device__ __forceinline__ double* slot_ptr(const MPParams& P, int blk, int s)
 { return P.slots + ((size_t)blk * P.nslots + s) * P.slot_doubles; }
 
 // Accepted-pair record (MP_REC floats): z (2), wg = g2 * e (2), w2, n2 (int), k (int), pad,
 // then the 14 scalar terms of calculateGn: w2, w2 r, w2 logr, sum w^2, (sum w^2) r,
 // (sum w^2) logr, sumwwgg0 (2), sumwwgg1 (2), sumwwgg2 (2), wg (2).
-static constexpr int REC_K = 6, REC_N = 5, REC_S = 8, NSCAL = 14;
+static constexpr int REC_K = 6, REC_S = 8, NSCAL = 14;
 
 // Bin-ordered G_n / W_n accumulation of the records [0, nrec) of this block into slot S.
 // The records are ranked stably by bin (list order within a bin), then warp w takes the
@@ -349,96 +482,126 @@ __device__ void mp_accumulate(const MPParams& P, const float* rec, int* perm, in
     double* SC = GG + 6 * (size_t)nb;
     const int per = (nrec + MW - 1) / MW;
     const int p0 = wid * per, p1 = min(nrec, p0 + per);
-    float F[12], fs = 0.f;
-    double D[12], ds = 0.;
-    unsigned long long npr = 0ull;
+    constexpr int KNONE = 0x7fffffff;
+    __shared__ float4 bz[MW][32];
+    __shared__ float2 bk[MW][32];
+    float F[12];
+    double D[12];
 #pragma unroll
     for (int q = 0; q < 12; ++q) { F[q] = 0.f; D[q] = 0.; }
-    int curk = -1, cnt = 0;
-    auto flush = [&](int k) {
+    int curk = -1;
+    // Power sums of lane n = lane+1 (and lane+33) to the slot.
+    auto flushp = [&](int k) {
 #pragma unroll
         for (int q = 0; q < 12; ++q) { D[q] += F[q]; F[q] = 0.f; }
-        ds += fs; fs = 0.f;
-        if (lane < 6) atomicAdd(&SC[(size_t)(lane + 1) * nb + k], ds);
-        else if (lane < 12) atomicAdd(&GG[(size_t)((lane - 6) >> 1) * 2 * nb + 2 * k + ((lane - 6) & 1)], ds);
-        else if (lane < 14) atomicAdd(&G[2 * ((size_t)k * gst + (M + 1)) + (lane - 12)], ds);
-        else if (lane == 14) atomicAdd(&SC[k], (double)npr);
-        if (lane == 0) atomicAdd(&W[2 * (size_t)k * (M + 1)], ds);
         const int n = lane + 1, n1 = lane + 33;
-        if (n <= M) {
-            double* wp = W + 2 * ((size_t)k * (M + 1) + n);
-            atomicAdd(wp, D[0]); atomicAdd(wp + 1, D[1]);
-        }
+        if (n <= M) { double* wp = W + sW(nb, n, k); atomicAdd(wp, D[0]); atomicAdd(wp + 1, D[1]); }
         if (n <= M + 1) {
-            double* gpp = G + 2 * ((size_t)k * gst + (M + 1) + n);
-            double* gmp = G + 2 * ((size_t)k * gst + (M + 1) - n);
+            double* gpp = G + sG(nb, M, n, k);
+            double* gmp = G + sG(nb, M, -n, k);
             atomicAdd(gpp, D[2]); atomicAdd(gpp + 1, D[3]);
             atomicAdd(gmp, D[4]); atomicAdd(gmp + 1, D[5]);
         }
-        if (n1 <= M) {
-            double* wp = W + 2 * ((size_t)k * (M + 1) + n1);
-            atomicAdd(wp, D[6]); atomicAdd(wp + 1, D[7]);
-        }
+        if (n1 <= M) { double* wp = W + sW(nb, n1, k); atomicAdd(wp, D[6]); atomicAdd(wp + 1, D[7]); }
         if (n1 <= M + 1) {
-            double* gpp = G + 2 * ((size_t)k * gst + (M + 1) + n1);
-            double* gmp = G + 2 * ((size_t)k * gst + (M + 1) - n1);
+            double* gpp = G + sG(nb, M, n1, k);
+            double* gmp = G + sG(nb, M, -n1, k);
             atomicAdd(gpp, D[8]); atomicAdd(gpp + 1, D[9]);
             atomicAdd(gmp, D[10]); atomicAdd(gmp + 1, D[11]);
         }
 #pragma unroll
         for (int q = 0; q < 12; ++q) D[q] = 0.;
-        ds = 0.; npr = 0ull;
     };
-    for (int p = p0; p < p1; ++p) {
-        const int pi = __ldcg(perm + p);
-        if (pi < 0 || pi >= nrec) {              // every rank is filled exactly once
-            if (lane == 0 && atomicCAS(P.err + 1, 0, 4) == 0) {
-                atomicCAS(P.err, 0, MP_ERR_CHECK);
-                P.dbg[0] = nrec; P.dbg[1] = p; P.dbg[2] = pi; P.dbg[3] = wid;
-                for (int q = 0; q < 16 && q < nrec; ++q) P.dbg[4 + q] = __ldcg(perm + q);
-            }
-            continue;
+    // Batches of 32 ranked records: lane l loads record base+l.  The scalar terms are summed
+    // by a segmented warp scan over the lanes of equal bin (the bins ascend along the lanes);
+    // the last lane of each run adds its run to the slot.  The powers walk the batch one
+    // record at a time with the record's values taken from its lane.
+    for (int base = p0; base < p1; base += 32) {
+        const int p = base + lane;
+        bool ok = p < p1;
+        const int pi = ok ? __ldcg(perm + p) : 0;
+        if (ok && (pi < 0 || pi >= nrec)) {          // every rank is filled exactly once
+            mp_check_fail(P.err, 4);
+            ok = false;
         }
-        const float* r = rec + (size_t)pi * MP_REC;
-        const float4 h0 = __ldcg(reinterpret_cast<const float4*>(r));
-        const int k = __float_as_int(__ldcg(r + REC_K));
-        if (k < 0 || k >= nb) {
-            if (lane == 0) mp_check_fail(P.err, 5);
-            continue;
+        const float4* r4 = reinterpret_cast<const float4*>(rec + (size_t)(ok ? pi : 0) * MP_REC);
+        const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 h0 = ok ? __ldcg(r4) : zero4, h1 = ok ? __ldcg(r4 + 1) : zero4;
+        const float4 q0 = ok ? __ldcg(r4 + 2) : zero4, q1 = ok ? __ldcg(r4 + 3) : zero4;
+        const float4 q2 = ok ? __ldcg(r4 + 4) : zero4, q3 = ok ? __ldcg(r4 + 5) : zero4;
+        int k = ok ? __float_as_int(h1.z) : KNONE;
+        if (ok && (k < 0 || k >= nb)) { mp_check_fail(P.err, 5); k = KNONE; ok = false; }
+        float sv[NSCAL] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w,
+                           q2.x, q2.y, q2.z, q2.w, q3.x, q3.y};
+        long long n2 = ok ? (long long)__float_as_int(h1.y) : 0;
+        if (!ok) {
+#pragma unroll
+            for (int q = 0; q < NSCAL; ++q) sv[q] = 0.f;
         }
-        if (k != curk) {
-            if (curk >= 0) flush(curk);
-            curk = k; cnt = 0;
-        }
-        if (lane < NSCAL) fs += __ldcg(r + REC_S + lane);
-        else if (lane == NSCAL) npr += (unsigned long long)__float_as_int(__ldcg(r + REC_N));
-        const float zr = h0.x, zi = h0.y, wgr = h0.z, wgi = h0.w, w2 = __ldcg(r + 4);
-        float pre = zr, pim = zi;   // z^(lane+1)
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const float qr = __shfl_up_sync(0xffffffffu, pre, o);
-            const float qi = __shfl_up_sync(0xffffffffu, pim, o);
-            if (lane >= o) { const float t = qr * pre - qi * pim; pim = qr * pim + qi * pre; pre = t; }
-        }
-        F[0] += w2 * pre; F[1] += w2 * pim;
-        F[2] += wgr * pre - wgi * pim; F[3] += wgr * pim + wgi * pre;
-        F[4] += wgr * pre + wgi * pim; F[5] += wgi * pre - wgr * pim;
-        if (M + 1 > 32) {
-            const float z32r = __shfl_sync(0xffffffffu, pre, 31);
-            const float z32i = __shfl_sync(0xffffffffu, pim, 31);
-            const float qr = z32r * pre - z32i * pim, qi = z32r * pim + z32i * pre;
-            F[6] += w2 * qr; F[7] += w2 * qi;
-            F[8] += wgr * qr - wgi * qi; F[9] += wgr * qi + wgi * qr;
-            F[10] += wgr * qr + wgi * qi; F[11] += wgi * qr - wgr * qi;
-        }
-        if (++cnt == 32) {
-            cnt = 0;
+            const int kk = __shfl_up_sync(0xffffffffu, k, o);
+            const bool same = lane >= o && kk == k;
 #pragma unroll
-            for (int q = 0; q < 12; ++q) { D[q] += F[q]; F[q] = 0.f; }
-            ds += fs; fs = 0.f;
+            for (int q = 0; q < NSCAL; ++q) {
+                const float t = __shfl_up_sync(0xffffffffu, sv[q], o);
+                if (same) sv[q] += t;
+            }
+            const long long tn = __shfl_up_sync(0xffffffffu, n2, o);
+            if (same) n2 += tn;
         }
+        const int kn = __shfl_down_sync(0xffffffffu, k, 1);
+        if (ok && (lane == 31 || kn != k)) {
+#pragma unroll
+            for (int q = 0; q < 6; ++q) atomicAdd(&SC[(size_t)(q + 1) * nb + k], (double)sv[q]);
+#pragma unroll
+            for (int q = 0; q < 6; ++q) atomicAdd(&GG[(size_t)(q >> 1) * 2 * nb + 2 * k + (q & 1)], (double)sv[6 + q]);
+            atomicAdd(&G[sG(nb, M, 0, k)], (double)sv[12]);
+            atomicAdd(&G[sG(nb, M, 0, k) + 1], (double)sv[13]);
+            atomicAdd(&W[sW(nb, 0, k)], (double)sv[0]);
+            atomicAdd(&SC[k], (double)n2);
+        }
+        const int nv = min(32, p1 - base);
+        // The batch's (z, wg) and (w2, k) go through shared memory: lane j's record is read
+        // by the whole warp with broadcast loads.
+        bz[wid][lane] = h0;
+        bk[wid][lane] = make_float2(h1.x, __int_as_float(k));
+        __syncwarp();
+        const int m = lane + 1;
+        for (int j = 0; j < nv; ++j) {
+            const float4 hz = bz[wid][j];
+            const float2 hk = bk[wid][j];
+            const int kj = __float_as_int(hk.y);
+            const float zr = hz.x, zi = hz.y, wgr = hz.z, wgi = hz.w, w2 = hk.x;
+            if (kj == KNONE) continue;
+            if (kj != curk) {
+                if (curk >= 0) flushp(curk);
+                curk = kj;
+            }
+            // z^(lane+1) by binary powering: every lane squares z up to z^32 and multiplies
+            // the powers of the bits of lane+1.
+            float pre = 1.f, pim = 0.f, br = zr, bi = zi;
+#pragma unroll
+            for (int t = 0; t < 6; ++t) {
+                if (m & (1 << t)) { const float u = pre * br - pim * bi; pim = pre * bi + pim * br; pre = u; }
+                if (t < 5) { const float u = br * br - bi * bi; bi = 2.f * br * bi; br = u; }
+            }
+            F[0] += w2 * pre; F[1] += w2 * pim;
+            F[2] += wgr * pre - wgi * pim; F[3] += wgr * pim + wgi * pre;
+            F[4] += wgr * pre + wgi * pim; F[5] += wgi * pre - wgr * pim;
+            if (M + 1 > 32) {
+                const float z32r = br, z32i = bi;     // z^32
+                const float qr = z32r * pre - z32i * pim, qi = z32r * pim + z32i * pre;
+                F[6] += w2 * qr; F[7] += w2 * qi;
+                F[8] += wgr * qr - wgi * qi; F[9] += wgr * qi + wgi * qr;
+                F[10] += wgr * qr + wgi * qi; F[11] += wgi * qr - wgr * qi;
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 12; ++q) { D[q] += F[q]; F[q] = 0.f; }
+        __syncwarp();
     }
-    if (curk >= 0) flush(curk);
+    if (curk >= 0) flushp(curk);
     __syncthreads();
 }
 
@@ -525,11 +688,11 @@ __device__ void zeta_products(const MPParams& P, int c1, const double* S, int ks
     const C2 wg1 = {(double)P.d1[c1], (double)P.d2[c1]};
     const C2 wg1c = conj2(wg1);
     auto Gv = [&](int k, int n) -> C2 {
-        const double* p = shG + 2 * ((size_t)k * gst + (M + 1) + n);
+        const double* p = shG + sG(nb, M, n, k);
         return {p[0], p[1]};
     };
     auto Wv = [&](int k, int n) -> C2 {
-        const double* p = shW + 2 * ((size_t)k * (M + 1) + (n >= 0 ? n : -n));
+        const double* p = shW + sW(nb, n >= 0 ? n : -n, k);
         return n >= 0 ? C2{p[0], p[1]} : C2{p[0], -p[1]};
     };
     const int na = mk - ks;
@@ -567,16 +730,16 @@ __device__ void zeta_products(const MPParams& P, int c1, const double* S, int ks
     __syncthreads();
 }
 
-// calculateZeta for vertex c1, rows [ks, mk): the scalar and diagonal parts now, and the
-// product terms as one vertex record for the batched contraction (k_mp_zeta).  Record:
-// header (c1, ks, mk, w1, wg1, pad x2), then G_n [n = -(M+1) .. M+1][bin] and W_n
-// [n = 0 .. M][bin], complex FP32.
+// calculateZeta for vertex c1, rows [ks, mk): the diagonal self-pair corrections now, the
+// rest as one vertex record for the batched contraction kernels (k_mp_zeta, k_mp_zscal).
+// Record (floats): header (c1, ks, mk, w1, Re/Im wg1, n1, pad), then G_n [n = -(M+1) ..
+// M+1][bin] and W_n [n = 0 .. M][bin] complex, then npairs (int), sumw, sumwr, sumwlogr,
+// sumwwr, sumwwlogr [bin].  A record that does not fit the buffer is contracted in place.
 __device__ void zeta_emit(const MPParams& P, int c1, const double* S, int ks, int mk,
                           double* out, double* diag, double* shG, double* shW,
                           unsigned long long* zidx_sh)
 {
     const int nb = P.nbins, M = P.maxn, gst = 2 * M + 3;
-    if (!P.quick) zeta_scalars(P, c1, S, ks, mk, out);
     zeta_diag(P, c1, S, ks, mk, diag);
     if (threadIdx.x == 0) *zidx_sh = atomicAdd(P.zcount, 1ull);
     __syncthreads();
@@ -585,23 +748,28 @@ __device__ void zeta_emit(const MPParams& P, int c1, const double* S, int ks, in
         float* R = P.zrec + (size_t)zi * P.zrec_floats;
         if (threadIdx.x == 0) {
             R[0] = __int_as_float(c1); R[1] = __int_as_float(ks); R[2] = __int_as_float(mk);
-            R[3] = P.w[c1]; R[4] = P.d1[c1]; R[5] = P.d2[c1]; R[6] = 0.f; R[7] = 0.f;
+            R[3] = P.w[c1]; R[4] = P.d1[c1]; R[5] = P.d2[c1];
+            R[6] = __int_as_float(P.n[c1]); R[7] = 0.f;
         }
+        // G then W: the slot's first 2 nb (M+1) + 2 nb gst doubles, reordered G-first.
         const double* W = S;
         const double* G = S + 2 * (size_t)nb * (M + 1);
-        float2* RG = reinterpret_cast<float2*>(R + 8);
-        float2* RW = RG + (size_t)gst * nb;
-        for (int q = threadIdx.x; q < gst * nb; q += MB) {
-            const int m = q / nb, a = q % nb;
-            const double* g = G + 2 * ((size_t)a * gst + m);
-            RG[q] = make_float2((float)__ldcg(g), (float)__ldcg(g + 1));
-        }
-        for (int q = threadIdx.x; q < (M + 1) * nb; q += MB) {
-            const int m = q / nb, a = q % nb;
-            const double* w = W + 2 * ((size_t)a * (M + 1) + m);
-            RW[q] = make_float2((float)__ldcg(w), (float)__ldcg(w + 1));
+        float* RG = R + 8;
+        float* RW = RG + 2 * (size_t)gst * nb;
+        for (int q = threadIdx.x; q < 2 * gst * nb; q += MB) RG[q] = (float)__ldcg(G + q);
+        for (int q = threadIdx.x; q < 2 * (M + 1) * nb; q += MB) RW[q] = (float)__ldcg(W + q);
+        const double* SC = G + 2 * (size_t)nb * gst + 6 * (size_t)nb;
+        float* RS = RW + 2 * (size_t)(M + 1) * nb;
+        for (int q = threadIdx.x; q < nb; q += MB) {
+            RS[q] = __int_as_float((int)__ldcg(SC + q));                // npairs
+            RS[nb + q] = (float)__ldcg(SC + nb + q);                    // sumw
+            RS[2 * nb + q] = (float)__ldcg(SC + 2 * nb + q);            // sumwr
+            RS[3 * nb + q] = (float)__ldcg(SC + 3 * nb + q);            // sumwlogr
+            RS[4 * nb + q] = (float)__ldcg(SC + 5 * nb + q);            // sumwwr
+            RS[5 * nb + q] = (float)__ldcg(SC + 6 * nb + q);            // sumwwlogr
         }
     } else {
+        if (!P.quick) zeta_scalars(P, c1, S, ks, mk, out);
         zeta_products(P, c1, S, ks, mk, out, shG, shW);
     }
     __syncthreads();
@@ -717,15 +885,67 @@ __global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
                 double* S = slot_ptr(P, blk, cur.slot);
                 if (tid == 0) { acc_n = 0; new_n = 0; anysplit = 0; }
                 double mymax = 0.;
+                float run32 = 0.f;
                 int myany = 0;
+                const float4 c1a = __ldg(reinterpret_cast<const float4*>(P.tc + c1));
+                const float4 c1b = __ldg(reinterpret_cast<const float4*>(P.tc + c1) + 1);
+                const float s1f = c1a.w;
+                const float thresh1f = (float)thresh1;
                 __syncthreads();
                 for (int j0 = 0; j0 < cur.len; j0 += MB) {
                     const int j = j0 + tid;
                     int cnt = 0, ca = -1, cb = -1, acc_ok = 0, kacc = -1;
                     double racc = 0., lracc = 0.;
                     const int c2 = j < cur.len ? __ldcg(list ? list + j : list2 + j) : 0;
-                    if (j < cur.len && !mp_valid_cell(P, c2)) mp_check_fail(P.err, 2);
+                    bool dec32 = false;          // decided (and recorded) in FP32
+                    float r32 = 0.f, lr32 = 0.f, dxf = 0.f, dyf = 0.f;
+                    float4 ta, tb, tq, td;       // the packed cell c2
+                    const bool inlist = j < cur.len && c2 >= 0 && c2 < P.ncells;
+                    if (inlist) {
+                        const float4* t4 = reinterpret_cast<const float4*>(P.tc + c2);
+                        ta = __ldg(t4); tb = __ldg(t4 + 1); tq = __ldg(t4 + 2); td = __ldg(t4 + 3);
+                    }
+                    const bool valid = inlist && __float_as_int(tq.z) > 0;
+                    if (j < cur.len && !valid) mp_check_fail(P.err, 2);
                     else if (j < cur.len) {
+                        // Geometry from the hi/lo float positions, decisions in FP32.
+                        const float s2f = ta.w;
+                        dxf = (ta.x - c1a.x) + (tb.x - c1b.x);
+                        dyf = (ta.y - c1a.y) + (tb.y - c1b.y);
+                        float dsq = dxf * dxf + dyf * dyf;
+                        if (P.coords != FLAT) {
+                            const float dzf = (ta.z - c1a.z) + (tb.z - c1b.z);
+                            dsq += dzf * dzf;
+                        }
+                        float rsqf = dsq;
+                        if (P.metric == ARC) {
+                            const float th = 2.f * asinf(0.5f * sqrtf(dsq));
+                            rsqf = th * th;
+                        }
+                        int k32 = -1;
+                        bool sp1 = false, sp2 = false, any32 = false;
+                        const int kind = mp_decide32(P, rsqf, s1f, s2f, thresh1f, k32, r32, lr32,
+                                                     sp1, sp2, any32);
+                        if (kind >= 0) {
+                            dec32 = true;
+                            if (kind == 1) {
+                                acc_ok = 1; kacc = k32; ca = c2;
+                            } else if (kind == 2) {
+                                // The running maximum of r + s is kept exact: entries within
+                                // the FP32 error of the thread's FP32 maximum get their FP64 value.
+                                const float rs32 = r32 + (s1f + s2f);
+                                if (rs32 > run32 * (1.f - 8e-6f)) {
+                                    const double rs64 = sqrt(mp_dist_sq(P, c1, c2)) + (s1 + (double)s2f);
+                                    mymax = fmax(mymax, rs64);
+                                    run32 = fmaxf(run32, rs32);
+                                }
+                                if (any32) myany = 1;
+                                if (sp2) { ca = __float_as_int(tq.w); cb = __float_as_int(td.x); cnt = 2; }
+                                else { ca = c2; cnt = 1; }
+                            }
+                        }
+                    }
+                    if (j < cur.len && !dec32 && valid) {
                         const double s2 = P.size[c2];
                         const double rsq = mp_dist_sq(P, c1, c2);
                         const double s = s1 + s2;
@@ -769,9 +989,37 @@ __global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
                     } else {
                         if (cnt >= 1) arena[wbase + pos] = ca;
                         if (cnt == 2) arena[wbase + pos + 1] = cb;
-                        if (acc_ok) {
-                            // calculateGn's per-pair terms (FP64, stored as FP32): ExpIPhi z,
-                            // the projected shear wg, and the scalar sums.
+                        if (acc_ok && dec32 && P.coords == FLAT) {
+                            // calculateGn's per-pair terms in FP32: ExpIPhi z = d / r, the
+                            // spin-2 factor e = conj(d^2) / |d|^2, the projected shear wg and
+                            // the scalar sums.
+                            const float rr = r32 > 0.f ? r32 : 1.f;
+                            const float zr = dxf / rr, zi = dyf / rr;
+                            float nn2 = dxf * dxf + dyf * dyf;
+                            if (!(nn2 > 0.f)) nn2 = 1.f;
+                            const float er = (dxf * dxf - dyf * dyf) / nn2, ei = -(2.f * dxf * dyf) / nn2;
+                            const float w2 = tb.w;
+                            const float4 lf = __ldg(P.lsf + ca);
+                            const float l0 = lf.x, l1 = lf.y, l2 = lf.z, l3 = lf.w;
+                            const float g1 = tq.x, g2 = tq.y;
+                            const float wgr = g1 * er - g2 * ei, wgi = g1 * ei + g2 * er;
+                            const float e2r = er * er - ei * ei, e2i = 2.f * er * ei;
+                            const float wsr = l1 * e2r - l2 * e2i, wsi = l1 * e2i + l2 * e2r;
+                            const float zsr = zr * zr - zi * zi, zsi = 2.f * zr * zi;
+                            const float a0r = wsr * zsr + wsi * zsi, a0i = wsi * zsr - wsr * zsi;
+                            const float a1r = wsr * zsr - wsi * zsi, a1i = wsr * zsi + wsi * zsr;
+                            float* R = acc + (size_t)(acc_n + apos) * MP_REC;
+                            *reinterpret_cast<float4*>(R) = make_float4(zr, zi, wgr, wgi);
+                            *reinterpret_cast<float4*>(R + 4) =
+                                make_float4(w2, tq.z, __int_as_float(kacc), 0.f);
+                            *reinterpret_cast<float4*>(R + 8) = make_float4(w2, w2 * r32, w2 * lr32, l0);
+                            *reinterpret_cast<float4*>(R + 12) = make_float4(l0 * r32, l0 * lr32, a0r, a0i);
+                            *reinterpret_cast<float4*>(R + 16) = make_float4(a1r, a1i, l3 * zsr, -l3 * zsi);
+                            *reinterpret_cast<float4*>(R + 20) = make_float4(wgr, wgi, 0.f, 0.f);
+                            atomicAdd(&bh[kacc], 1);
+                        } else if (acc_ok) {
+                            // The same terms from FP64 (non-flat geometry, or decided in FP64).
+                            if (dec32) { racc = r32; lracc = lr32; }
                             C2 z, e;
                             phases(P, c1, ca, racc, z, e);
                             const double w2 = P.w[ca];
@@ -1005,11 +1253,99 @@ __global__ void __launch_bounds__(ZB) k_mp_zeta(ZParams Q)
     }
 }
 
+// The n = 0 scalar outputs of calculateZeta over vertex records (ntri, meand2/3,
+// meanlogd2/3): for every entry (a, b) whose min(a, b) lies in the record's rows,
+//   a != b: ntri += n1 np_a np_b, meand2 += w1 sumw_b sumwr_a, meand3 += w1 sumw_a sumwr_b
+//   a == b: ntri += n1 np_a (np_a - 1), meand2 = meand3 += w1 (sumw_a sumwr_a - sumwwr_a)
+// (meanlogd likewise with sumwlogr).  ntri is an exact 64-bit integer sum; the means are FP32
+// products with FP64 sums.  Block (g, tile) adds its sums to group g's partial arrays.
+__global__ void __launch_bounds__(ZB) k_mp_zscal(ZParams Q, double* spart,
+                                                 unsigned long long* ntp)
+{
+    extern __shared__ float4 zsh[];    // [chunk][nb][2]
+    __shared__ int4 hdr_sh[64];
+    const int nb = Q.nbins, M = Q.maxn, gst = 2 * M + 3;
+    const int nb2 = nb * nb;
+    const int g = blockIdx.x, tid = threadIdx.x;
+    int ea[ZE], eb[ZE];
+    bool ev[ZE];
+#pragma unroll
+    for (int j = 0; j < ZE; ++j) {
+        const int e = ((int)blockIdx.y * ZE + j) * ZB + tid;
+        ev[j] = e < nb2;
+        ea[j] = ev[j] ? e / nb : 0;
+        eb[j] = ev[j] ? e % nb : 0;
+    }
+    double D[ZE][4];
+    unsigned long long C[ZE];
+#pragma unroll
+    for (int j = 0; j < ZE; ++j) { C[j] = 0ull; for (int q = 0; q < 4; ++q) D[j][q] = 0.; }
+    const long long r0 = Q.nrec * g / gridDim.x, r1 = Q.nrec * (g + 1) / gridDim.x;
+    for (long long c0 = r0; c0 < r1; c0 += Q.chunk) {
+        const int nv = (int)min((long long)Q.chunk, r1 - c0);
+        __syncthreads();
+        for (int idx = tid; idx < nv * nb; idx += ZB) {
+            const int v = idx / nb, a = idx % nb;
+            const float* R = Q.rec + (size_t)(c0 + v) * Q.rec_floats;
+            const float* RS = R + 8 + 2 * (size_t)gst * nb + 2 * (size_t)(M + 1) * nb;
+            float4* d = zsh + ((size_t)v * nb + a) * 2;
+            d[0] = make_float4(RS[a], RS[nb + a], RS[2 * nb + a], RS[3 * nb + a]);
+            d[1] = make_float4(RS[4 * nb + a], RS[5 * nb + a], 0.f, 0.f);
+            if (a == 0)
+                hdr_sh[v] = make_int4(__float_as_int(R[1]), __float_as_int(R[2]),
+                                      __float_as_int(R[6]), __float_as_int(R[3]));
+        }
+        __syncthreads();
+        float F[ZE][4];
+#pragma unroll
+        for (int j = 0; j < ZE; ++j)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) F[j][q] = 0.f;
+        for (int v = 0; v < nv; ++v) {
+            const int4 h = hdr_sh[v];
+            const float w1 = __int_as_float(h.w);
+            const unsigned long long n1 = (unsigned long long)h.z;
+#pragma unroll
+            for (int j = 0; j < ZE; ++j) {
+                const int m = min(ea[j], eb[j]);
+                if (!ev[j] || m < h.x || m >= h.y) continue;
+                const float4 pa = zsh[((size_t)v * nb + ea[j]) * 2];
+                const unsigned long long npa = (unsigned)__float_as_int(pa.x);
+                if (ea[j] == eb[j]) {
+                    const float4 pa2 = zsh[((size_t)v * nb + ea[j]) * 2 + 1];
+                    C[j] += n1 * npa * (npa > 0 ? npa - 1 : 0);
+                    const float md = w1 * (pa.y * pa.z - pa2.x);
+                    const float ml = w1 * (pa.y * pa.w - pa2.y);
+                    F[j][0] += md; F[j][1] += ml; F[j][2] += md; F[j][3] += ml;
+                } else {
+                    const float4 pb = zsh[((size_t)v * nb + eb[j]) * 2];
+                    C[j] += n1 * npa * (unsigned long long)(unsigned)__float_as_int(pb.x);
+                    F[j][0] += w1 * pb.y * pa.z; F[j][1] += w1 * pb.y * pa.w;
+                    F[j][2] += w1 * pa.y * pb.z; F[j][3] += w1 * pa.y * pb.w;
+                }
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < ZE; ++j)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) D[j][q] += F[j][q];
+    }
+#pragma unroll
+    for (int j = 0; j < ZE; ++j) {
+        if (!ev[j]) continue;
+        const int e = ea[j] * nb + eb[j];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) spart[((size_t)g * 4 + q) * nb2 + e] += D[j][q];
+        ntp[(size_t)g * nb2 + e] += C[j];
+    }
+}
+
 // Final sums, in a fixed order: the per-block outputs, the contraction groups' partials and
 // the diagonal corrections.
 __global__ void k_mp_reduce(int nblk, long long stride, long long Z, int nb, int nn,
                             const double* in, const double* diag, long long diag_stride,
-                            int ngroups, const double* part, double* out)
+                            int ngroups, const double* part, int nsg, const double* spart,
+                            const unsigned long long* ntp, double* out)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= 15 * Z) return;
@@ -1022,6 +1358,16 @@ __global__ void k_mp_reduce(int nblk, long long stride, long long Z, int nb, int
         for (int g = 0; g < ngroups; ++g) s += part[((size_t)g * 10 + qp) * Z + r];
     const long long ab = r / nn;
     const int a = (int)(ab / nb), b = (int)(ab % nb);
+    if (r % nn == nn / 2 && ((q >= 8 && q <= 11) || q == 14)) {
+        const size_t nb2 = (size_t)nb * nb;
+        if (q == 14) {
+            unsigned long long c = 0ull;
+            for (int g = 0; g < nsg; ++g) c += ntp[(size_t)g * nb2 + ab];
+            s += (double)c;
+        } else {
+            for (int g = 0; g < nsg; ++g) s += spart[((size_t)g * 4 + (q - 8)) * nb2 + ab];
+        }
+    }
     if (a == b && (q < 8 || q == 12)) {
         const int d = q < 8 ? q : 8;
         for (int bl = 0; bl < nblk; ++bl) s -= diag[(size_t)bl * diag_stride + (size_t)d * nb + a];
@@ -1036,7 +1382,7 @@ size_t mp_slot_doubles(int nb, int M)
 { return 2 * (size_t)nb * (M + 1) + 2 * (size_t)nb * (2 * M + 3) + 13 * (size_t)nb; }
 
 static int mp_rec_floats(int nb, int M)
-{ return (8 + 2 * nb * (2 * M + 3) + 2 * nb * (M + 1) + 3) & ~3; }
+{ return (8 + 2 * nb * (2 * M + 3) + 2 * nb * (M + 1) + 6 * nb + 3) & ~3; }
 
 int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* h_out)
 {
@@ -1064,6 +1410,10 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
     TC_CU(cudaFuncSetAttribute(k_mp_zeta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zsh));
     const int etiles = (nb * nb + ZE * ZB - 1) / (ZE * ZB);
     const int ngroups = std::max(1, (4 * nsm + nn * etiles - 1) / (nn * etiles));
+    // Scalar outputs: records per chunk and record groups.
+    const int chunk2 = (int)std::max<long long>(1, std::min<long long>(64, (48 * 1024) / (32LL * nb)));
+    const size_t zsh2 = (size_t)chunk2 * nb * 32;
+    const int nsg = std::max(1, 2 * nsm / etiles);
     const int recf = mp_rec_floats(nb, M);
     const long long acc_cap = 4096;
     X.want_a1 = std::max<long long>(X.want_a1, 4LL * ntop + (1 << 16));
@@ -1130,6 +1480,13 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
                 X.zcap = c2; X.zrec_floats = recf;
             }
         }
+        if (X.nsg < nsg || X.spart_nb2 < (long long)nb * nb) {
+            dfree(X.spart); dfree(X.ntp);
+            X.nsg = 0;
+            TC_TRY(dalloc(&X.spart, (size_t)nsg * 4 * nb * nb));
+            TC_TRY(dalloc(&X.ntp, (size_t)nsg * nb * nb));
+            X.nsg = nsg; X.spart_nb2 = (long long)nb * nb;
+        }
         if (X.ngroups < ngroups || X.part_stride < 10 * Z) {
             dfree(X.part);
             X.ngroups = 0;
@@ -1157,6 +1514,8 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
         TC_CU(cudaMemsetAsync(X.out, 0, sizeof(double) * (size_t)P.out_stride * nblk, st));
         TC_CU(cudaMemsetAsync(X.diag, 0, sizeof(double) * (size_t)9 * nb * nblk, st));
         TC_CU(cudaMemsetAsync(X.part, 0, sizeof(double) * (size_t)ngroups * 10 * Z, st));
+        TC_CU(cudaMemsetAsync(X.spart, 0, sizeof(double) * (size_t)nsg * 4 * nb * nb, st));
+        TC_CU(cudaMemsetAsync(X.ntp, 0, sizeof(unsigned long long) * (size_t)nsg * nb * nb, st));
         count_launch();
         k_mp_split1<<<ntop, MB, 0, st>>>(P);
         TC_CU(cudaGetLastError());
@@ -1186,6 +1545,13 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
                 count_launch();
                 k_mp_zeta<<<dim3(nn, ngroups, etiles), ZB, zsh, st>>>(Q);
                 TC_CU(cudaGetLastError());
+                if (!P.quick) {
+                    ZParams Q2 = Q;
+                    Q2.chunk = chunk2;
+                    count_launch();
+                    k_mp_zscal<<<dim3(nsg, etiles), ZB, zsh2, st>>>(Q2, X.spart, X.ntp);
+                    TC_CU(cudaGetLastError());
+                }
             }
             if ((long long)c[1] >= P.njobs_val) break;
             if (wave > (1 << 24)) { e = MP_ERR_STACK; break; }
@@ -1217,7 +1583,8 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
         }
         count_launch();
         k_mp_reduce<<<(unsigned)((P.out_stride + 255) / 256), 256, 0, st>>>(
-            nblk, P.out_stride, Z, nb, nn, X.out, X.diag, 9LL * nb, ngroups, X.part, X.total);
+            nblk, P.out_stride, Z, nb, nn, X.out, X.diag, 9LL * nb, ngroups, X.part,
+            P.quick ? 0 : nsg, X.spart, X.ntp, X.total);
         TC_CU(cudaGetLastError());
         TC_CU(cudaMemcpyAsync(h_out, X.total, sizeof(double) * (size_t)P.out_stride,
                               cudaMemcpyDeviceToHost, st));
@@ -1232,6 +1599,7 @@ void free_mp_scratch(MPScratch& X)
 {
     dfree(X.arena1); dfree(X.jobs); dfree(X.arena2); dfree(X.acc); dfree(X.perm);
     dfree(X.slots); dfree(X.out); dfree(X.diag); dfree(X.total); dfree(X.zrec); dfree(X.part);
+    dfree(X.spart); dfree(X.ntp);
     dfree(X.ctl); dfree(X.err); dfree(X.dbg);
     X = MPScratch();
 }

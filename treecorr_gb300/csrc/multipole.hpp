@@ -24,12 +24,17 @@ enum MPErr : int {
 struct MPParams {
     int coords, metric, quick, nbins, maxn;
     double minsep, maxsep, binsize, b, a, logminsep, minsepsq, maxsepsq, bsq, asq, maxbsq_eff;
+    // FP32 copies for the FP32 decisions (the FP64 values decide whenever FP32 is too close).
+    float f_minsepsq, f_maxsepsq, f_maxsep, f_asq, f_bsq, f_q25, f_logminsep, f_binsize, f_b,
+        f_minba;
     // Cells (FP64 centres, float payloads) and their leaf sums (4 doubles per cell:
     // sum w^2, Re/Im sum (wz)^2, sum |wz|^2).
     const double *x, *y, *z;
     const float *size, *w, *d1, *d2;
     const int *n, *left, *right;
     const double* ls;
+    const float4* lsf;   // the leaf sums as floats
+    const TCell* tc;     // packed cells (float hi/lo positions and payload)
     const int* tops;
     int ntop;
     int ncells;          // cell ids are 0 .. ncells-1
@@ -89,6 +94,10 @@ struct MPScratch {
     double* part = nullptr;     // per contraction group: 10 arrays of nbins^2 (2 maxn + 1)
     long long part_stride = 0;
     int ngroups = 0;
+    double* spart = nullptr;    // per scalar group: 4 arrays of nbins^2 (meand2/3, meanlogd2/3)
+    unsigned long long* ntp = nullptr;   // per scalar group: nbins^2 triangle counts
+    long long spart_nb2 = 0;
+    int nsg = 0;
     int nblk = 0;
     unsigned long long* ctl = nullptr;
     int* err = nullptr;
@@ -98,7 +107,7 @@ struct MPScratch {
     int want_slots = 0;
 };
 
-int launch_leaf_sums(int ncap, const Cells& C, double* ls, cudaStream_t st);
+int launch_leaf_sums(int ncap, const Cells& C, double* ls, float4* lsf, cudaStream_t st);
 // Runs both phases and the reduction; h_out receives 15 arrays of nbins*nbins*(2*maxn+1)
 // doubles: gam0r, gam0i, gam1r, gam1i, gam2r, gam2i, gam3r, gam3i, meand2, meanlogd2,
 // meand3, meanlogd3, weight, weight_im, ntri.
