@@ -254,9 +254,10 @@ def run_gpu(args, rank, world):
     ms_e2e = allreduce_max(ms_e2e, world)
     e2e = world * res_e2e[-1][1]["accepted"] * args.steps / (ms_e2e / 1e3)
     out, st = res[-1]
-    # Roofline of the dominant kernel (the traversal): algorithmic bytes per launch =
-    # cell pairs evaluated x (two 64-byte cell records + the 8-byte work item) / launches,
-    # over the device time of the traversal launches measured by the library with events.
+    # Roofline of the dominant kernel (k_expand, the breadth-first traversal): algorithmic
+    # bytes = cell pairs evaluated x (two 64-byte cell records + the 8-byte work item read),
+    # over the traversal's device time measured by the library with CUDA events on its
+    # stream (per launch: both divided by the number of expansion launches).
     tr_ms = st["traverse_ms"]
     bytes_per_launch = st["cell_pairs"] * (2 * 64 + 8) / max(st["launches"], 1)
     per_launch_ms = tr_ms / max(st["launches"], 1)
@@ -269,7 +270,7 @@ def run_gpu(args, rank, world):
     achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "traffic": args.traffic,
-                "kernel": "k_traverse",
+                "kernel": "k_expand",
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
     h2d = sum(cat[k].nbytes for k in cols)
     d2h = 8 * nb * 8
@@ -296,6 +297,109 @@ def run_gpu(args, rank, world):
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(cat, bins, args, budget_s=args.cpu_budget)
+    return line
+
+
+def ggg_catalog(n, seed, side=600.0):
+    """The multipole configuration's catalog: x, y ~ U[0, side] arcmin, g1, g2 ~ N(0, 0.25),
+    w ~ U[0.5, 1.5] (flat sky)."""
+    rng = np.random.default_rng(seed)
+    return {"x": rng.uniform(0, side, n), "y": rng.uniform(0, side, n),
+            "g1": rng.normal(0, 0.25, n), "g2": rng.normal(0, 0.25, n),
+            "w": rng.uniform(0.5, 1.5, n)}
+
+
+def ggg_bins():
+    lo, hi, nb, max_n = 1.0, 50.0, 20, 30
+    bs = np.log(hi / lo) / nb
+    b = min(bs, 0.1)                      # bin_slop default 0.1/bin_size (bin_size > 0.1)
+    a = np.pi / (2 * max_n + 1)           # angle_slop default
+    b1 = min(a, b)
+    return dict(min_sep=lo, max_sep=hi, nbins=nb, bin_size=bs, b=b, a=a, max_n=max_n,
+                min_size=2 * lo * b1 / (2 + 3 * b1), max_size=hi * b1)
+
+
+def run_gpu_ggg(args, rank, world):
+    """GGG LogMultipole (2M flat-sky points, 20 Log bins 1-50', max_n 30): triangles
+    accumulated per second (sum of ntri over all outputs per step time)."""
+    import torch
+    from treecorr_gb300 import _treecorr as T
+    dev = torch.device("cuda", rank % max(torch.cuda.device_count(), 1))
+    torch.cuda.set_device(dev)
+    n = args.n if args.n != 10_000_000 else 2_000_000
+    cat = ggg_catalog(n, args.seed + rank, side=600.0 * np.sqrt(n / 2e6))
+    B = ggg_bins()
+    nb, mn = B["nbins"], B["max_n"]
+    shape = (nb, nb, 2 * mn + 1)
+    keys = ("gam0r", "gam0i", "gam1r", "gam1i", "gam2r", "gam2i", "gam3r", "gam3i", "meand1",
+            "meanlogd1", "meand2", "meanlogd2", "meand3", "meanlogd3", "meanu", "meanv",
+            "weight", "weight_im", "ntri")
+    hcols = {k: torch.from_numpy(cat[k]).pin_memory() for k in ("x", "y", "g1", "g2", "w")}
+    stream = torch.cuda.ExternalStream(T.stream_handle(), device=dev)
+    e = np.array([])
+
+    def step():
+        out = {k: np.zeros(shape) for k in keys}
+        c = T.GGGCorr(T.LogMultipole, B["min_sep"], B["max_sep"], nb, B["bin_size"], B["b"],
+                      B["a"], 0., 0., mn, 0., 0., 0., 0., 0, 0., 0., -sys.float_info.max,
+                      sys.float_info.max, 0., 0., 0., *[out[k] for k in keys])
+        f = T.GFieldFlat(hcols["x"].numpy(), hcols["y"].numpy(), e, hcols["g1"].numpy(),
+                         hcols["g2"].numpy(), hcols["w"].numpy(), e, B["min_size"],
+                         B["max_size"], T.Mean, 0, False, 3, 10)
+        c.processAuto(f, False, False, T.Euclidean)
+        del c, f
+        return out
+
+    for _ in range(args.warmup):
+        step()
+    launches0 = T.launch_count()
+    barrier(world)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        e0.record(stream)
+        outs = [step() for _ in range(args.steps)]
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = allreduce_max(e0.elapsed_time(e1), world)
+    ntri = float(outs[-1]["ntri"].sum())
+    value = world * ntri * args.steps / (ms / 1e3)
+    unit = "triangles/s"
+    line = {
+        "metric": "GGG multipole triangles/s at N=2M (flat, 20 Log bins 1-50', max_n 30)",
+        "value": value, "unit": unit, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded uniform flat catalog)",
+        "config": {"workload": f"GGG LogMultipole auto, {n} points U[0,{600*np.sqrt(n/2e6):.0f}']^2, "
+                               "20 Log bins 1-50', max_n 30, bin_slop 0.1/bin_size",
+                   "n": n, "parallelism": f"replicas{world}",
+                   "l2": "tree, c2 lists and vertex records larger than L2; no flush"},
+        "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 5 * 8 * n,
+                "d2h_bytes_per_step": 15 * 8 * nb * nb * (2 * mn + 1)},
+        "gpu_launches": T.launch_count() - launches0,
+        "clocks": clk.summary(),
+        "detail": {"ntri_per_step": ntri, "gam0r_sum": float(outs[-1]["gam0r"].sum())},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        # The oracle port on a smaller catalog of the same density (the triangle rate per
+        # second is what is compared).
+        from oracle import oracle as O
+        nthreads = os.cpu_count() or 1
+        ns = 100_000
+        cs = ggg_catalog(ns, args.seed, side=600.0 * np.sqrt(ns / 2e6))
+        f = O.OracleField("G", "flat", cs["x"], cs["y"], None, cs["g1"], cs["g2"], cs["w"],
+                          None, B["min_size"], B["max_size"], "mean", False, 3, 10)
+        f.ntop()
+        t0 = time.perf_counter()
+        o = O.multipole("Euclidean", B, mn, f, nthreads=nthreads)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": float(o["ntri"].sum()) / dt, "unit": unit,
+                                "cores": nthreads, "kind": "port",
+                                "sample": f"{ns}-point catalog of the same density "
+                                          f"({dt:.1f} s, tree build excluded)"}
     return line
 
 
@@ -408,6 +512,8 @@ def main():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    p.add_argument("--workload", default="gg", choices=["gg", "ggg"],
+                   help="gg: the 2-point headline; ggg: the multipole 3-point configuration")
     p.add_argument("--n", type=int, default=10_000_000)
     p.add_argument("--bin-slop", type=float, default=0.1)
     p.add_argument("--seed", type=int, default=20261203)
@@ -419,6 +525,8 @@ def main():
     rank, world = dist_init()
     if args.impl == "reference":
         line = run_reference(args, rank, world)
+    elif args.workload == "ggg":
+        line = run_gpu_ggg(args, rank, world)
     else:
         line = run_gpu(args, rank, world)
     if rank == 0 and line is not None:

@@ -200,6 +200,11 @@ int tc_corr3_process_auto(tc_corr3* c, tc_field* f, int dots, int quick, int met
 /* Device time of the last tc_corr3_process_auto call in ms (no reference counterpart). */
 double tc_corr3_last_ms(const tc_corr3* c);
 
+/* Counters of the last tc_corr3_process_auto call (no reference counterpart):
+ * out[0] vertex records contracted in batches, out[1] records contracted in place because
+ * the record buffer was full, out[2] finish/contract waves.  Returns TC_OK. */
+int tc_corr3_stats(const tc_corr3* c, int64_t out[3]);
+
 /* SetOMPThreads / GetOMPThreads (src/Corr2.cpp:995-1011).  The GPU path has no host
  * threads to set: both return 1, which the Python layer accepts. */
 int tc_set_omp_threads(int num_threads);

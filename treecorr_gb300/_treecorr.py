@@ -101,6 +101,8 @@ def lib():
         L.tc_corr3_process_auto.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.tc_corr3_last_ms.restype = ctypes.c_double
         L.tc_corr3_last_ms.argtypes = [vp]
+        L.tc_corr3_stats.restype = ctypes.c_int
+        L.tc_corr3_stats.argtypes = [vp, ctypes.POINTER(i64)]
         L.tc_launch_count.restype = ctypes.c_longlong
         L.tc_launch_count.argtypes = []
         L.tc_stream.restype = ctypes.c_void_p
@@ -419,6 +421,13 @@ class BaseCorr3:
     def last_ms(self):
         """Device time of the last processAuto in ms (no reference counterpart)."""
         return float(lib().tc_corr3_last_ms(self._h))
+
+    def stats(self):
+        """Counters of the last process call (no reference counterpart): vertex records
+        contracted in batches, records contracted in place, finish/contract waves."""
+        out = (ctypes.c_int64 * 3)()
+        _check(lib().tc_corr3_stats(self._h, out))
+        return {"records": int(out[0]), "in_place": int(out[1]), "waves": int(out[2])}
 
     def __del__(self):
         h = getattr(self, "_h", None)

@@ -1031,6 +1031,15 @@ int tc_corr3_process_auto(tc_corr3* c, tc_field* f, int dots, int quick, int met
 
 double tc_corr3_last_ms(const tc_corr3* c) { return c ? c->ms : 0.; }
 
+int tc_corr3_stats(const tc_corr3* c, int64_t out[3])
+{
+    if (!c || !out) { set_last_error("NULL argument"); return TC_ERR_ARG; }
+    out[0] = c->X.records - c->X.overflow;
+    out[1] = c->X.overflow;
+    out[2] = c->X.waves;
+    return TC_OK;
+}
+
 int tc_set_omp_threads(int num_threads) { (void)num_threads; return 1; }
 int tc_get_omp_threads(void) { return 1; }
 

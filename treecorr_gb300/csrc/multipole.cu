@@ -737,11 +737,14 @@ __device__ void zeta_products(const MPParams& P, int c1, const double* S, int ks
 // sumwwr, sumwwlogr [bin].  A record that does not fit the buffer is contracted in place.
 __device__ void zeta_emit(const MPParams& P, int c1, const double* S, int ks, int mk,
                           double* out, double* diag, double* shG, double* shW,
-                          unsigned long long* zidx_sh)
+                          unsigned long long* zidx_sh, int* emits_sh)
 {
     const int nb = P.nbins, M = P.maxn, gst = 2 * M + 3;
     zeta_diag(P, c1, S, ks, mk, diag);
-    if (threadIdx.x == 0) *zidx_sh = atomicAdd(P.zcount, 1ull);
+    if (threadIdx.x == 0) {
+        *zidx_sh = atomicAdd(P.zcount, 1ull);
+        ++*emits_sh;
+    }
     __syncthreads();
     const unsigned long long zi = *zidx_sh;
     if ((long long)zi < P.zcap) {
@@ -782,7 +785,7 @@ __global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
     __shared__ int sp, free_cnt, free_list[64], scan_sh[MW];
     __shared__ P2Entry cur;
     __shared__ unsigned long long job_sh, zidx_sh;
-    __shared__ int acc_n, new_n, anysplit, alloc_ok, have_sh;
+    __shared__ int acc_n, new_n, anysplit, alloc_ok, have_sh, job_emits;
     __shared__ double maxr_sh[MW];
     __shared__ long long arena_top;
     __shared__ int bh[MP_MAXNB];
@@ -825,6 +828,7 @@ __global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
             for (int s = 0; s < P.nslots; ++s) free_list[s] = P.nslots - 1 - s;
             arena_top = 0;
             sp = 0;
+            job_emits = 0;
             int s0 = free_list[--free_cnt];
             P2Entry e;
             e.c1 = J.x; e.len = J.w; e.slot = s0; e.mink = nb;
@@ -1071,14 +1075,14 @@ __global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
                 const int n_new = new_n;
                 int mink = cur.mink;
                 if (n_new == 0) {
-                    zeta_emit(P, c1, S, 0, mink, out, diag, shG, shW, &zidx_sh);
+                    zeta_emit(P, c1, S, 0, mink, out, diag, shG, shW, &zidx_sh, &job_emits);
                     break;
                 }
                 if (maxrem < P.maxsep) {
                     int k = maxrem < P.minsep ? 0
                           : int((log(maxrem) - P.logminsep) / P.binsize) + 1;
                     if (k < mink) {
-                        zeta_emit(P, c1, S, k, mink, out, diag, shG, shW, &zidx_sh);
+                        zeta_emit(P, c1, S, k, mink, out, diag, shG, shW, &zidx_sh, &job_emits);
                         mink = k;
                     }
                 }
@@ -1141,6 +1145,8 @@ __global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
             if (tid == 0) free_list[free_cnt++] = cur.slot;
             __syncthreads();
         }
+        // The largest record count of one job sizes the stop margin of later waves.
+        if (tid == 0) atomicMax(P.zmaxjob, (unsigned long long)job_emits);
     }
 }
 
@@ -1463,9 +1469,9 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
             X.out_stride = P.out_stride; X.diag_stride = 9LL * nb;
         }
         {
-            // The vertex-record buffer: up to 4 GiB and a quarter of the free memory, or the
+            // The vertex-record buffer: up to 16 GiB and a quarter of the free memory, or the
             // byte count in TCGPU_MP_RECORD_BYTES (at least 16 records).
-            size_t budget = (size_t)4 << 30;
+            size_t budget = (size_t)16 << 30;
             if (const char* ev = std::getenv("TCGPU_MP_RECORD_BYTES"))
                 budget = (size_t)std::max(0LL, std::atoll(ev));
             const long long cap = std::max<long long>(16, (long long)(budget / (4ULL * recf)));
@@ -1499,17 +1505,24 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
         X.nblk = std::max(X.nblk, nblk);
         P.arena1 = X.arena1; P.arena1_cap = X.arena1_cap;
         P.jobs = X.jobs; P.jobs_cap = X.jobs_cap;
-        P.njobs = X.ctl; P.job_next = X.ctl + 1; P.zcount = X.ctl + 2;
+        P.njobs = X.ctl; P.job_next = X.ctl + 1; P.zcount = X.ctl + 2; P.zmaxjob = X.ctl + 3;
         P.arena2 = X.arena2; P.arena2_cap = X.arena2_cap;
         P.acc = X.acc; P.perm = X.perm; P.acc_cap = (int)X.acc_cap;
         P.slots = X.slots; P.nslots = X.nslots;
         P.out = X.out;
         P.diag = X.diag;
         P.zrec = X.zrec; P.zcap = X.zcap; P.zrec_floats = recf;
-        P.zstop = X.zcap - std::min<long long>(X.zcap / 2, 64LL * nblk);
+        // Jobs are not started once the buffer holds zstop records; the blocks' jobs in
+        // flight then fill at most nblk x (the largest job so far) more.
+        auto set_zstop = [&](long long maxjob) {
+            const long long margin = (long long)nblk * std::max<long long>(64, 2 * maxjob);
+            P.zstop = std::max<long long>(X.zcap / 4, X.zcap - margin);
+        };
+        set_zstop(512);
         P.err = X.err;
         P.dbg = X.dbg;
         TC_CU(cudaMemsetAsync(X.ctl, 0, 4 * sizeof(unsigned long long), st));
+        X.overflow = 0; X.records = 0; X.waves = 0;
         TC_CU(cudaMemsetAsync(X.err, 0, 2 * sizeof(int), st));
         TC_CU(cudaMemsetAsync(X.out, 0, sizeof(double) * (size_t)P.out_stride * nblk, st));
         TC_CU(cudaMemsetAsync(X.diag, 0, sizeof(double) * (size_t)9 * nb * nblk, st));
@@ -1532,7 +1545,7 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
             count_launch();
             k_mp_finish<<<nblk, MB, shbytes, st>>>(P);
             TC_CU(cudaGetLastError());
-            unsigned long long c[3] = {0, 0, 0};
+            unsigned long long c[4] = {0, 0, 0, 0};
             TC_CU(cudaMemcpyAsync(c, X.ctl, sizeof(c), cudaMemcpyDeviceToHost, st));
             TC_CU(cudaMemcpyAsync(&e, X.err, sizeof(int), cudaMemcpyDeviceToHost, st));
             TC_CU(cudaStreamSynchronize(st));
@@ -1553,6 +1566,10 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
                     TC_CU(cudaGetLastError());
                 }
             }
+            X.overflow += std::max<long long>(0, (long long)c[2] - X.zcap);
+            X.records += (long long)c[2];
+            ++X.waves;
+            set_zstop((long long)c[3]);
             if ((long long)c[1] >= P.njobs_val) break;
             if (wave > (1 << 24)) { e = MP_ERR_STACK; break; }
         }

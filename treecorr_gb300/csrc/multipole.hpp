@@ -64,6 +64,7 @@ struct MPParams {
     long long zcap, zstop;
     int zrec_floats;
     unsigned long long* zcount;
+    unsigned long long* zmaxjob;   // largest number of records of one job
     int* err;
     double* dbg;         // 32 doubles describing the first failed check
 };
@@ -98,6 +99,8 @@ struct MPScratch {
     unsigned long long* ntp = nullptr;   // per scalar group: nbins^2 triangle counts
     long long spart_nb2 = 0;
     int nsg = 0;
+    // Counters of the last run: vertex records, those contracted in place, waves.
+    long long records = 0, overflow = 0, waves = 0;
     int nblk = 0;
     unsigned long long* ctl = nullptr;
     int* err = nullptr;
