@@ -730,7 +730,7 @@ int corr3_process_auto(tc_corr3* c, tc_field* f, int quick, int metric)
     P.minsepsq = c->minsep * c->minsep; P.maxsepsq = c->maxsep * c->maxsep;
     P.bsq = c->b * c->b; P.asq = c->a * c->a;
     P.maxbsq_eff = P.maxsepsq * std::min(P.bsq, P.asq);
-    P.f_minsepsq = (float)P.minsepsq; P.f_maxsepsq = (float)P.maxsepsq; P.f_maxsep = (float)P.maxsep;
+    P.f_minsepsq = (float)P.minsepsq; P.f_minsep = (float)P.minsep; P.f_maxsepsq = (float)P.maxsepsq; P.f_maxsep = (float)P.maxsep;
     P.f_asq = (float)P.asq; P.f_bsq = (float)P.bsq;
     P.f_q25 = (float)(0.25 * (P.binsize + P.b) * (P.binsize + P.b));
     P.f_logminsep = (float)P.logminsep; P.f_binsize = (float)P.binsize; P.f_b = (float)P.b;

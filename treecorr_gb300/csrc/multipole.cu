@@ -162,8 +162,21 @@ __device__ __forceinline__ int mp_decide32(const MPParams& P, float rsq, float s
 {
     constexpr float M5 = 1e-5f, ML = 2e-4f;
     const float s = s1 + s2;
-    // tooSmallDist: left to FP64 unless rsq is clearly >= min_sep^2.
-    if (lt3(rsq, P.f_minsepsq, M5) != 0) return -1;
+    // tooSmallDist: rsq < min_sep^2 && s < min_sep && rsq < (min_sep - s)^2.  min_sep - s
+    // loses relative accuracy when s is close to min_sep: those go to FP64.
+    const int below_min = lt3(rsq, P.f_minsepsq, M5);
+    if (below_min < 0) return -1;
+    if (below_min == 1) {
+        const int c2 = lt3(s, P.f_minsep, M5);
+        if (c2 < 0) return -1;
+        if (c2 == 1) {
+            const float d = P.f_minsep - s;
+            if (d < 0.01f * P.f_minsep) return -1;
+            const int c3 = lt3(rsq, d * d, ML);
+            if (c3 < 0) return -1;
+            if (c3 == 1) return 0;
+        }
+    }
     const int below_max = lt3(rsq, P.f_maxsepsq, M5);
     if (below_max < 0) return -1;
     if (below_max == 0) {                       // tooLargeDist
@@ -199,7 +212,8 @@ __device__ __forceinline__ int mp_decide32(const MPParams& P, float rsq, float s
                     const float kk = (lr - P.f_logminsep) / P.f_binsize;
                     ik = (int)kk;
                     const float frac = kk - (float)ik;
-                    if (frac < ML || frac > 1.f - ML) return -1;
+                    const float af = fabsf(frac);      // kk < 0 below min_sep: frac <= 0
+                    if (af < ML || af > 1.f - ML) return -1;
                     const float f = fminf(frac, 1.f - frac);
                     const float t4 = f * P.f_binsize + P.f_b;
                     c = lt3(t4 * t4 * rsq, s2q, ML);
@@ -218,7 +232,7 @@ __device__ __forceinline__ int mp_decide32(const MPParams& P, float rsq, float s
     }
     r = sqrtf(rsq);
     if (sb) {
-        if (below_max == 0) return 0;           // isRSqInRange fails
+        if (below_max == 0 || below_min == 1) return 0;   // isRSqInRange fails
         if (ik < 0) {
             lr = logf(r);
             const float kk = (lr - P.f_logminsep) / P.f_binsize;
@@ -485,15 +499,18 @@ __device__ void mp_accumulate(const MPParams& P, const float* rec, int* perm, in
     constexpr int KNONE = 0x7fffffff;
     __shared__ float4 bz[MW][32];
     __shared__ float2 bk[MW][32];
-    float F[12];
+    // FP32 sums of the current bin: F over one batch, F2 over up to 32 batches; they reach
+    // FP64 (D, then the slot) only every 32 batches and when the bin changes.
+    float F[12], F2[12];
     double D[12];
 #pragma unroll
-    for (int q = 0; q < 12; ++q) { F[q] = 0.f; D[q] = 0.; }
-    int curk = -1;
+    for (int q = 0; q < 12; ++q) { F[q] = 0.f; F2[q] = 0.f; D[q] = 0.; }
+    int curk = -1, nbatch = 0;
     // Power sums of lane n = lane+1 (and lane+33) to the slot.
     auto flushp = [&](int k) {
 #pragma unroll
-        for (int q = 0; q < 12; ++q) { D[q] += F[q]; F[q] = 0.f; }
+        for (int q = 0; q < 12; ++q) { D[q] += (double)(F2[q] + F[q]); F[q] = 0.f; F2[q] = 0.f; }
+        nbatch = 0;
         const int n = lane + 1, n1 = lane + 33;
         if (n <= M) { double* wp = W + sW(nb, n, k); atomicAdd(wp, D[0]); atomicAdd(wp + 1, D[1]); }
         if (n <= M + 1) {
@@ -516,6 +533,22 @@ __device__ void mp_accumulate(const MPParams& P, const float* rec, int* perm, in
     // by a segmented warp scan over the lanes of equal bin (the bins ascend along the lanes);
     // the last lane of each run adds its run to the slot.  The powers walk the batch one
     // record at a time with the record's values taken from its lane.
+    // Scalar sums of one run of bin kb to the slot.
+    auto flush_scal = [&](int kb, const float* v, long long cnt) {
+#pragma unroll
+        for (int q = 0; q < 6; ++q) atomicAdd(&SC[(size_t)(q + 1) * nb + kb], (double)v[q]);
+#pragma unroll
+        for (int q = 0; q < 6; ++q) atomicAdd(&GG[(size_t)(q >> 1) * 2 * nb + 2 * kb + (q & 1)], (double)v[6 + q]);
+        atomicAdd(&G[sG(nb, M, 0, kb)], (double)v[12]);
+        atomicAdd(&G[sG(nb, M, 0, kb) + 1], (double)v[13]);
+        atomicAdd(&W[sW(nb, 0, kb)], (double)v[0]);
+        atomicAdd(&SC[kb], (double)cnt);
+    };
+    float cs[NSCAL];                  // carried run: FP32 scalar sums, count, bin, batches
+    long long cn = 0;
+    int ck = -1, cnum = 0;
+#pragma unroll
+    for (int q = 0; q < NSCAL; ++q) cs[q] = 0.f;
     for (int base = p0; base < p1; base += 32) {
         const int p = base + lane;
         bool ok = p < p1;
@@ -538,6 +571,17 @@ __device__ void mp_accumulate(const MPParams& P, const float* rec, int* perm, in
 #pragma unroll
             for (int q = 0; q < NSCAL; ++q) sv[q] = 0.f;
         }
+        // The run carried from the previous batch joins lane 0 when the bin continues, and
+        // goes to the slot when it does not.
+        if (lane == 0 && ck >= 0) {
+            if (k == ck) {
+#pragma unroll
+                for (int q = 0; q < NSCAL; ++q) sv[q] += cs[q];
+                n2 += cn;
+            } else {
+                flush_scal(ck, cs, cn);
+            }
+        }
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const int kk = __shfl_up_sync(0xffffffffu, k, o);
@@ -551,15 +595,20 @@ __device__ void mp_accumulate(const MPParams& P, const float* rec, int* perm, in
             if (same) n2 += tn;
         }
         const int kn = __shfl_down_sync(0xffffffffu, k, 1);
-        if (ok && (lane == 31 || kn != k)) {
+        // The last run of the batch is carried on while it stays short; runs that end inside
+        // the batch, or at the end of the warp's range, go to the slot.
+        const bool last_batch = base + 32 >= p1;
+        const bool run_end = ok && (lane == 31 || kn != k);
+        const bool carry = run_end && lane == 31 && !last_batch && cnum < 32;
+        if (run_end && !carry) flush_scal(k, sv, n2);
+        {
+            const bool c31 = __shfl_sync(0xffffffffu, carry, 31);
+            const int k31 = __shfl_sync(0xffffffffu, k, 31);
 #pragma unroll
-            for (int q = 0; q < 6; ++q) atomicAdd(&SC[(size_t)(q + 1) * nb + k], (double)sv[q]);
-#pragma unroll
-            for (int q = 0; q < 6; ++q) atomicAdd(&GG[(size_t)(q >> 1) * 2 * nb + 2 * k + (q & 1)], (double)sv[6 + q]);
-            atomicAdd(&G[sG(nb, M, 0, k)], (double)sv[12]);
-            atomicAdd(&G[sG(nb, M, 0, k) + 1], (double)sv[13]);
-            atomicAdd(&W[sW(nb, 0, k)], (double)sv[0]);
-            atomicAdd(&SC[k], (double)n2);
+            for (int q = 0; q < NSCAL; ++q) cs[q] = __shfl_sync(0xffffffffu, sv[q], 31);
+            cn = __shfl_sync(0xffffffffu, n2, 31);
+            ck = c31 ? k31 : -1;
+            cnum = c31 ? cnum + 1 : 0;
         }
         const int nv = min(32, p1 - base);
         // The batch's (z, wg) and (w2, k) go through shared memory: lane j's record is read
@@ -598,7 +647,12 @@ __device__ void mp_accumulate(const MPParams& P, const float* rec, int* perm, in
             }
         }
 #pragma unroll
-        for (int q = 0; q < 12; ++q) { D[q] += F[q]; F[q] = 0.f; }
+        for (int q = 0; q < 12; ++q) { F2[q] += F[q]; F[q] = 0.f; }
+        if (++nbatch == 32) {
+#pragma unroll
+            for (int q = 0; q < 12; ++q) { D[q] += (double)F2[q]; F2[q] = 0.f; }
+            nbatch = 0;
+        }
         __syncwarp();
     }
     if (curk >= 0) flushp(curk);
@@ -778,7 +832,7 @@ __device__ void zeta_emit(const MPParams& P, int c1, const double* S, int ks, in
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
+__global__ void __launch_bounds__(MB, 2) k_mp_finish(MPParams P)
 {
     extern __shared__ __align__(16) double mp_sh[];
     __shared__ P2Entry stk[MSTACK];
@@ -902,6 +956,7 @@ __global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
                     double racc = 0., lracc = 0.;
                     const int c2 = j < cur.len ? __ldcg(list ? list + j : list2 + j) : 0;
                     bool dec32 = false;          // decided (and recorded) in FP32
+                    float rs32 = 0.f;            // r + s of an FP32-decided unaccepted entry
                     float r32 = 0.f, lr32 = 0.f, dxf = 0.f, dyf = 0.f;
                     float4 ta, tb, tq, td;       // the packed cell c2
                     const bool inlist = j < cur.len && c2 >= 0 && c2 < P.ncells;
@@ -935,14 +990,7 @@ __global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
                             if (kind == 1) {
                                 acc_ok = 1; kacc = k32; ca = c2;
                             } else if (kind == 2) {
-                                // The running maximum of r + s is kept exact: entries within
-                                // the FP32 error of the thread's FP32 maximum get their FP64 value.
-                                const float rs32 = r32 + (s1f + s2f);
-                                if (rs32 > run32 * (1.f - 8e-6f)) {
-                                    const double rs64 = sqrt(mp_dist_sq(P, c1, c2)) + (s1 + (double)s2f);
-                                    mymax = fmax(mymax, rs64);
-                                    run32 = fmaxf(run32, rs32);
-                                }
+                                rs32 = r32 + (s1f + s2f);
                                 if (any32) myany = 1;
                                 if (sp2) { ca = __float_as_int(tq.w); cb = __float_as_int(td.x); cnt = 2; }
                                 else { ca = c2; cnt = 1; }
@@ -982,6 +1030,21 @@ __global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
                                 if (split2) { ca = P.left[c2]; cb = P.right[c2]; cnt = 2; }
                                 else { ca = c2; cnt = 1; }
                             }
+                        }
+                    }
+                    // The maximum of r + s over the unaccepted entries is kept exact (it sets
+                    // the next pass's thresholds): the warp's FP32 maximum is compared with its
+                    // running FP32 maximum, and the entries within the FP32 error of the larger
+                    // one get their FP64 value; all other entries are below an evaluated one.
+                    {
+                        float wm = rs32;
+                        for (int o = 16; o > 0; o >>= 1) wm = fmaxf(wm, __shfl_xor_sync(0xffffffffu, wm, o));
+                        if (wm > run32 * (1.f - 8e-6f)) {
+                            if (rs32 > 0.f && rs32 > wm * (1.f - 8e-6f)) {
+                                const double rs64 = sqrt(mp_dist_sq(P, c1, c2)) + (s1 + (double)ta.w);
+                                mymax = fmax(mymax, rs64);
+                            }
+                            run32 = fmaxf(run32, wm);
                         }
                     }
                     int tot_new, tot_acc;
@@ -1079,8 +1142,10 @@ __global__ void __launch_bounds__(MB) k_mp_finish(MPParams P)
                     break;
                 }
                 if (maxrem < P.maxsep) {
-                    int k = maxrem < P.minsep ? 0
-                          : int((log(maxrem) - P.logminsep) / P.binsize) + 1;
+                    int k = 0;
+                    if (lane == 0 && !(maxrem < P.minsep))
+                        k = int((log(maxrem) - P.logminsep) / P.binsize) + 1;
+                    k = __shfl_sync(0xffffffffu, k, 0);
                     if (k < mink) {
                         zeta_emit(P, c1, S, k, mink, out, diag, shG, shW, &zidx_sh, &job_emits);
                         mink = k;
@@ -1188,11 +1253,15 @@ __global__ void __launch_bounds__(ZB) k_mp_zeta(ZParams Q)
         ea[j] = ev[j] ? e / nb : 0;
         eb[j] = ev[j] ? e % nb : 0;
     }
+    // Sums: FP32 per chunk (F), FP32 over up to 16 chunks (F2), then FP64 (D) -- FP64 work is
+    // kept rare (GB300 runs FP64 at 1/64 of the FP32 rate).
     double D[ZE][10];
+    float F2[ZE][10];
 #pragma unroll
     for (int j = 0; j < ZE; ++j)
 #pragma unroll
-        for (int q = 0; q < 10; ++q) D[j][q] = 0.;
+        for (int q = 0; q < 10; ++q) { D[j][q] = 0.; F2[j][q] = 0.f; }
+    int nchunk = 0;
     const long long r0 = Q.nrec * g / Q.ngroups, r1 = Q.nrec * (g + 1) / Q.ngroups;
     const int nw = (n >= 0) ? n : -n;
     for (long long c0 = r0; c0 < r1; c0 += Q.chunk) {
@@ -1246,8 +1315,19 @@ __global__ void __launch_bounds__(ZB) k_mp_zeta(ZParams Q)
 #pragma unroll
         for (int j = 0; j < ZE; ++j)
 #pragma unroll
-            for (int q = 0; q < 10; ++q) D[j][q] += F[j][q];
+            for (int q = 0; q < 10; ++q) F2[j][q] += F[j][q];
+        if (++nchunk == 16) {
+            nchunk = 0;
+#pragma unroll
+            for (int j = 0; j < ZE; ++j)
+#pragma unroll
+                for (int q = 0; q < 10; ++q) { D[j][q] += (double)F2[j][q]; F2[j][q] = 0.f; }
+        }
     }
+#pragma unroll
+    for (int j = 0; j < ZE; ++j)
+#pragma unroll
+        for (int q = 0; q < 10; ++q) D[j][q] += (double)F2[j][q];
 #pragma unroll
     for (int j = 0; j < ZE; ++j) {
         if (!ev[j]) continue;

@@ -25,7 +25,7 @@ struct MPParams {
     int coords, metric, quick, nbins, maxn;
     double minsep, maxsep, binsize, b, a, logminsep, minsepsq, maxsepsq, bsq, asq, maxbsq_eff;
     // FP32 copies for the FP32 decisions (the FP64 values decide whenever FP32 is too close).
-    float f_minsepsq, f_maxsepsq, f_maxsep, f_asq, f_bsq, f_q25, f_logminsep, f_binsize, f_b,
+    float f_minsepsq, f_minsep, f_maxsepsq, f_maxsep, f_asq, f_bsq, f_q25, f_logminsep, f_binsize, f_b,
         f_minba;
     // Cells (FP64 centres, float payloads) and their leaf sums (4 doubles per cell:
     // sum w^2, Re/Im sum (wz)^2, sum |wz|^2).
