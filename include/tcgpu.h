@@ -78,6 +78,7 @@ typedef struct tc_stats {
     int64_t launches;        /* traversal kernel launches */
     double  build_ms;        /* device time of the tree builds done by this call */
     double  traverse_ms;     /* device time of the traversal + reduction */
+    int64_t learned;         /* cell pairs accepted by the learned criterion (of accepted) */
 } tc_stats;
 
 /* Field construction: replaces BuildNField / BuildKField / BuildGField for
@@ -204,6 +205,43 @@ double tc_corr3_last_ms(const tc_corr3* c);
  * out[0] vertex records contracted in batches, out[1] records contracted in place because
  * the record buffer was full, out[2] finish/contract waves.  Returns TC_OK. */
 int tc_corr3_stats(const tc_corr3* c, int64_t out[3]);
+
+/* ---- Learned opening criterion (no reference counterpart) ----------------------------
+ * A 5-64-64-1 ReLU network (FP32 master parameters, tc_mlp_nparam() floats: W1[64][5],
+ * b1[64], W2[64][64], b2[64], w3[64], b3) revisits the cell pairs the bin_slop rule
+ * (include/BinType.h:93-151) would split, when (s1+s2)^2 <= a^2 r^2 and
+ * (s1+s2)^2 <= (cand_factor * b)^2 r^2 with min_sep <= r < max_sep: it accepts such a pair
+ * into the bin of its separation when its output (a predicted log10 of the weight fraction
+ * that would land in another bin) is <= threshold.  Inference runs in the traversal with
+ * FP16 weights and FP32 accumulation.  Features: the larger and smaller cell size over
+ * r * bin_size, the distance of log r to the nearest bin edge (in bin sizes), the position
+ * of log r in the binned range, bin_size. */
+int tc_mlp_nparam(void);
+
+/* Enable (params != NULL) or disable the criterion for the following process calls. */
+int tc_corr2_set_learned(tc_corr2* corr, const float* params, double threshold,
+                         double cand_factor);
+
+/* Training pairs: runs processAuto with the bin_slop rule (adding into the corr outputs as
+ * usual) and samples about 1 in sample_mod of the candidate pairs; each sample gets the
+ * features and the target log10(leak + 1e-5) from a point-by-point recount (pairs with
+ * more than max_point_pairs point pairs get target NaN).  feat_out: max_samples x 5,
+ * target_out: max_samples; *n_out = samples written. */
+int tc_learn_collect(tc_corr2* corr, tc_field* field, int metric, int sample_mod,
+                     int64_t max_samples, int64_t max_point_pairs, float* feat_out,
+                     float* target_out, int64_t* n_out);
+
+/* Mean-squared-error gradient of the network over n samples (FP32, on the device). */
+int tc_mlp_grad(const float* params, const float* x, const float* y, int64_t n, float* grad,
+                float* loss);
+
+/* The traversal's network evaluation (FP16 mma) over n feature rows. */
+int tc_mlp_infer(const float* params, const float* x, int64_t n, float* y);
+
+/* Adam training on the device: steps mini-batches of `batch` samples; params in/out;
+ * loss_out (may be NULL) receives the loss of every step. */
+int tc_mlp_train(float* params, const float* x, const float* y, int64_t n, int steps,
+                 int batch, float lr, unsigned seed, float* loss_out);
 
 /* SetOMPThreads / GetOMPThreads (src/Corr2.cpp:995-1011).  The GPU path has no host
  * threads to set: both return 1, which the Python layer accepts. */

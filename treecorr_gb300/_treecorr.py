@@ -30,7 +30,8 @@ TC_OK, TC_ERR_ARG, TC_ERR_CUDA, TC_ERR_UNSUPPORTED, TC_ERR_DEVICE, TC_ERR_NOMEM 
 class tc_stats(ctypes.Structure):
     _fields_ = [("cell_pairs", ctypes.c_int64), ("accepted", ctypes.c_int64),
                 ("escalated", ctypes.c_int64), ("launches", ctypes.c_int64),
-                ("build_ms", ctypes.c_double), ("traverse_ms", ctypes.c_double)]
+                ("build_ms", ctypes.c_double), ("traverse_ms", ctypes.c_double),
+                ("learned", ctypes.c_int64)]
 
 
 _lib = None
@@ -84,6 +85,21 @@ def lib():
             [ctypes.c_double] * 8 + [ctypes.POINTER(ctypes.c_int)]
         L.tc_corr2_stats.restype = ctypes.c_int
         L.tc_corr2_stats.argtypes = [vp, ctypes.POINTER(tc_stats)]
+        fp = ctypes.POINTER(ctypes.c_float)
+        L.tc_mlp_nparam.restype = ctypes.c_int
+        L.tc_mlp_nparam.argtypes = []
+        L.tc_corr2_set_learned.restype = ctypes.c_int
+        L.tc_corr2_set_learned.argtypes = [vp, fp, ctypes.c_double, ctypes.c_double]
+        L.tc_learn_collect.restype = ctypes.c_int
+        L.tc_learn_collect.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, i64, i64, fp, fp,
+                                       ctypes.POINTER(i64)]
+        L.tc_mlp_grad.restype = ctypes.c_int
+        L.tc_mlp_grad.argtypes = [fp, fp, fp, i64, fp, fp]
+        L.tc_mlp_infer.restype = ctypes.c_int
+        L.tc_mlp_infer.argtypes = [fp, fp, i64, fp]
+        L.tc_mlp_train.restype = ctypes.c_int
+        L.tc_mlp_train.argtypes = [fp, fp, fp, i64, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                   ctypes.c_uint, fp]
         L.tc_set_omp_threads.restype = ctypes.c_int
         L.tc_set_omp_threads.argtypes = [ctypes.c_int]
         L.tc_get_omp_threads.restype = ctypes.c_int
@@ -323,6 +339,48 @@ def launch_count():
     return int(lib().tc_launch_count())
 
 
+# ----------------------------------------------------------------------------------------
+# Learned opening criterion (no reference counterpart; see include/tcgpu.h).
+
+def _fptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def mlp_nparam():
+    return int(lib().tc_mlp_nparam())
+
+
+def mlp_grad(params, x, y):
+    """Gradient and loss of the mean squared error of the network over (x, y), on the GPU."""
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    g = np.zeros(mlp_nparam(), dtype=np.float32)
+    loss = np.zeros(1, dtype=np.float32)
+    _check(lib().tc_mlp_grad(_fptr(params), _fptr(x), _fptr(y), len(y), _fptr(g), _fptr(loss)))
+    return g, float(loss[0])
+
+
+def mlp_infer(params, x):
+    """The traversal's FP16 tensor-core evaluation of the network over feature rows x."""
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.zeros(len(x), dtype=np.float32)
+    _check(lib().tc_mlp_infer(_fptr(params), _fptr(x), len(x), _fptr(y)))
+    return y
+
+
+def mlp_train(params, x, y, steps, batch=4096, lr=1e-3, seed=0):
+    """Adam training on the GPU; returns (trained parameters, per-step loss)."""
+    p = np.array(params, dtype=np.float32, copy=True)
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.ascontiguousarray(y, dtype=np.float32)
+    loss = np.zeros(max(steps, 1), dtype=np.float32)
+    _check(lib().tc_mlp_train(_fptr(p), _fptr(x), _fptr(y), len(y), int(steps), int(batch),
+                              float(lr), int(seed), _fptr(loss)))
+    return p, loss[:steps]
+
+
 def stream_handle():
     """The cudaStream_t (as an int) on which libtcgpu.so launches its work."""
     return int(lib().tc_stream() or 0)
@@ -383,6 +441,29 @@ class BaseCorr2:
 
     def samplePairs(self, *args):
         raise NotImplementedError("samplePairs is not on the GPU path")
+
+    def setLearned(self, params=None, threshold=-2.0, cand_factor=4.0):
+        """Use the learned opening criterion (params: tc_mlp_nparam() floats) in the following
+        process calls, or the bin_slop rule alone (params=None).  No reference counterpart."""
+        if params is None:
+            _check(lib().tc_corr2_set_learned(self._h, None, 0.0, 0.0))
+            self._mlp = None
+            return
+        self._mlp = np.ascontiguousarray(params, dtype=np.float32)
+        _check(lib().tc_corr2_set_learned(self._h, _fptr(self._mlp), float(threshold),
+                                          float(cand_factor)))
+
+    def learnCollect(self, field, metric, sample_mod=16, max_samples=1 << 20,
+                     max_point_pairs=1 << 16):
+        """processAuto with the bin_slop rule, sampling training pairs for the learned
+        criterion; returns (features [n, 5], targets [n]) (NaN targets: too many points)."""
+        f = np.zeros((max_samples, 5), dtype=np.float32)
+        t = np.zeros(max_samples, dtype=np.float32)
+        n = ctypes.c_int64(0)
+        _check(lib().tc_learn_collect(self._h, field._h, int(metric), int(sample_mod),
+                                      int(max_samples), int(max_point_pairs), _fptr(f), _fptr(t),
+                                      ctypes.byref(n)))
+        return f[:n.value].copy(), t[:n.value].copy()
 
     def stats(self):
         """Counters of the last process call (no reference counterpart)."""

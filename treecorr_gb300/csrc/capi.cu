@@ -18,6 +18,7 @@
 #include "tc_host.hpp"
 #include "traverse2pt.hpp"
 #include "multipole.hpp"
+#include "learned.hpp"
 
 namespace tc {
 
@@ -104,6 +105,13 @@ struct tc_corr2 {
     std::vector<int2*> lev;              // per-level item buffers of the expansion
     std::vector<long long> levcap;
     ExpandSched* sched = nullptr;        // device-side schedule of the expansion
+    // Learned opening criterion (mode 2) or sampling of its training pairs (mode 1).
+    int mode = 0;
+    MLPPacked* mlp = nullptr;
+    float mlp_thr = 0.f, cand_factor = 4.f;
+    int2* samples = nullptr;
+    long long sample_cap = 0;
+    unsigned sample_mod = 1;
 };
 
 namespace {
@@ -448,9 +456,20 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
     // Breadth-first expansion by levels: each launch takes a chunk of the deepest non-empty
     // level (level 0 = the top-level pairs, generated on the fly) and appends the children to
     // the next level, so memory stays bounded by (depth x 4 chunk) items.
+    T.mode = c->mode;
+    T.cand_f2 = (float)(sqr(c->cand_factor * c->b));
+    T.mlp_thr = c->mlp_thr;
+    T.finvlogrange = (float)(1. / std::log(c->maxsep / c->minsep));
+    T.mlp = c->mlp;
+    T.samples = c->samples; T.sample_cap = c->sample_cap; T.sample_mod = c->sample_mod;
     int blocks = 0, nwarps = 0;
-    TC_TRY(expand_grid(nq, nb, &blocks, &nwarps));
+    TC_TRY(expand_grid(nq, nb, &blocks, &nwarps, c->mode));
     TC_TRY(expand_scratch(c, nwarps, nq));
+    T.nsamples = c->ctl + 6;   // ctl exists from here on
+    if ((c->mode == 1 && (!c->samples || c->sample_cap <= 0)) || (c->mode == 2 && !c->mlp)) {
+        set_last_error("learned-criterion buffers missing");
+        return TC_ERR_ARG;
+    }
     T.nwarps = nwarps;
     T.wacc = c->wacc; T.wnp = c->wnp; T.err = c->d_err;
     T.counters = c->ctl + 2;
@@ -530,10 +549,10 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
     TC_CU(cudaEventRecord(e1, st));
     std::vector<double> tot((size_t)nq * nb);
     std::vector<unsigned long long> totnp(nb);
-    unsigned long long cntr[3];
+    unsigned long long cntr[4];
     TC_CU(cudaMemcpyAsync(tot.data(), c->tot, tot.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
     TC_CU(cudaMemcpyAsync(totnp.data(), c->totnp, nb * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-    TC_CU(cudaMemcpyAsync(cntr, c->ctl + 2, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    TC_CU(cudaMemcpyAsync(cntr, c->ctl + 2, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     TC_CU(cudaStreamSynchronize(st));
     float ms = 0.f;
     TC_CU(cudaEventElapsedTime(&ms, e0, e1));
@@ -541,6 +560,7 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
     c->stats.cell_pairs = (int64_t)cntr[0];
     c->stats.accepted = (int64_t)cntr[1];
     c->stats.escalated = (int64_t)cntr[2];
+    c->stats.learned = (int64_t)cntr[3];
     c->stats.launches = launches_done;
     c->stats.traverse_ms = ms;
     // Corr2::finishProcess adds into the caller's arrays (src/Corr2.cpp:527-566).
@@ -915,7 +935,105 @@ void tc_corr2_free(tc_corr2* c)
     dfree(c->tot); dfree(c->totnp); dfree(c->ctl); dfree(c->idle); dfree(c->d_err);
     for (auto& p : c->lev) dfree(p);
     dfree(c->sched);
+    dfree(c->mlp); dfree(c->samples);
     delete c;
+}
+
+int tc_mlp_nparam(void) { return MLP_NPARAM; }
+
+int tc_corr2_set_learned(tc_corr2* c, const float* params, double threshold, double cand_factor)
+{
+    if (!c) { set_last_error("NULL corr"); return TC_ERR_ARG; }
+    if (!params) { c->mode = 0; return TC_OK; }
+    if (!(cand_factor >= 1.)) { set_last_error("cand_factor must be >= 1"); return TC_ERR_ARG; }
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    TC_TRY(mlp_pack(params, &c->mlp, st));
+    c->mlp_thr = (float)threshold;
+    c->cand_factor = (float)cand_factor;
+    c->mode = 2;
+    return TC_OK;
+}
+
+int tc_learn_collect(tc_corr2* c, tc_field* f, int metric, int sample_mod, int64_t max_samples,
+                     int64_t max_point_pairs, float* feat_out, float* target_out, int64_t* n_out)
+{
+    if (!c || !f || !feat_out || !target_out || !n_out) { set_last_error("NULL argument"); return TC_ERR_ARG; }
+    if (sample_mod < 1 || max_samples < 1) { set_last_error("sample_mod and max_samples must be >= 1"); return TC_ERR_ARG; }
+    *n_out = 0;
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    if (c->sample_cap < max_samples) {
+        dfree(c->samples);
+        c->sample_cap = 0;
+        TC_TRY(dalloc(&c->samples, (size_t)max_samples));
+        c->sample_cap = max_samples;
+    }
+    const int old_mode = c->mode;
+    c->mode = 1;
+    c->sample_mod = (unsigned)sample_mod;
+    const long long cap_keep = c->sample_cap;
+    c->sample_cap = max_samples;
+    int rc = corr_process(c, f, nullptr, 0, metric);
+    c->sample_cap = cap_keep;
+    c->mode = old_mode;
+    if (rc) return rc;
+    unsigned long long ns = 0;
+    TC_CU(cudaMemcpy(&ns, c->ctl + 6, sizeof(ns), cudaMemcpyDeviceToHost));
+    const long long n = std::min<long long>((long long)ns, max_samples);
+    if (n == 0) return TC_OK;
+    float *dfeat = nullptr, *dtar = nullptr;
+    TC_TRY(dalloc(&dfeat, (size_t)n * MLP_IN));
+    if (dalloc(&dtar, (size_t)n)) { dfree(dfeat); return TC_ERR_NOMEM; }
+    LabelParams L;
+    std::memset(&L, 0, sizeof(L));
+    L.coords = f->coords; L.metric = metric; L.nbins = c->nbins;
+    L.minsepsq = c->minsep * c->minsep; L.maxsepsq = c->maxsep * c->maxsep;
+    L.logminsep = std::log(c->minsep); L.binsize = c->binsize;
+    L.finvminsepsq = (float)(1. / L.minsepsq); L.finvbinsize = (float)(1. / c->binsize);
+    L.finvlogrange = (float)(1. / std::log(c->maxsep / c->minsep)); L.fbinsize = (float)c->binsize;
+    L.max_point_pairs = max_point_pairs;
+    L.c1 = f->tcells; L.c2 = f->tcells;
+    L.start1 = f->cells.start; L.start2 = f->cells.start;
+    L.x1 = f->buf[0].x; L.y1 = f->buf[0].y; L.z1 = f->buf[0].z;
+    L.x2 = f->buf[0].x; L.y2 = f->buf[0].y; L.z2 = f->buf[0].z;
+    L.w1 = f->buf[0].w; L.w2 = f->buf[0].w;
+    rc = launch_label(L, c->samples, n, dfeat, dtar, st);
+    if (!rc) {
+        cudaMemcpyAsync(feat_out, dfeat, sizeof(float) * n * MLP_IN, cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(target_out, dtar, sizeof(float) * n, cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) { set_last_error("labelling failed"); rc = TC_ERR_CUDA; }
+    }
+    dfree(dfeat); dfree(dtar);
+    if (rc) return rc == 5 ? TC_ERR_NOMEM : (rc == 2 ? TC_ERR_CUDA : rc);
+    *n_out = n;
+    return TC_OK;
+}
+
+int tc_mlp_grad(const float* params, const float* x, const float* y, int64_t n, float* grad,
+                float* loss)
+{
+    if (!params || !x || !y || !grad || !loss || n < 1) { set_last_error("bad argument"); return TC_ERR_ARG; }
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    return mlp_grad_host(params, x, y, n, grad, loss, st) ? TC_ERR_CUDA : TC_OK;
+}
+
+int tc_mlp_infer(const float* params, const float* x, int64_t n, float* y)
+{
+    if (!params || !x || !y || n < 1) { set_last_error("bad argument"); return TC_ERR_ARG; }
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    return mlp_infer_host(params, x, n, y, st) ? TC_ERR_CUDA : TC_OK;
+}
+
+int tc_mlp_train(float* params, const float* x, const float* y, int64_t n, int steps, int batch,
+                 float lr, unsigned seed, float* loss_out)
+{
+    if (!params || !x || !y || n < 1 || steps < 0 || batch < 1) { set_last_error("bad argument"); return TC_ERR_ARG; }
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    return mlp_train_host(params, x, y, n, steps, batch, lr, seed, loss_out, st) ? TC_ERR_CUDA : TC_OK;
 }
 
 int tc_corr2_process_auto(tc_corr2* c, tc_field* f, int dots, int quick, int metric)

@@ -29,6 +29,7 @@
 #include "tc_internal.cuh"
 #include "tc_host.hpp"
 #include "traverse2pt.hpp"
+#include "learned.cuh"
 
 namespace tc {
 
@@ -405,12 +406,65 @@ __device__ __forceinline__ void stage_accumulate(int k, const float (&v)[7],
     __syncwarp();
 }
 
+// The values an accepted pair adds (finishProcess and DirectHelper, src/Corr2.cpp:394-566):
+// w1 w2, w1 w2 r, w1 w2 logr, n1 n2 and the correlation products.
+__device__ __forceinline__ void accept_values(const TravParams& T, const TCell& A, const TCell& B,
+                                              int i, int j, float dx, float dy, float dz,
+                                              float dsq, float r, float logr, float (&av)[7],
+                                              unsigned long long& acc_nn)
+{
+    const bool flat = (T.coords == FLAT);
+    const float ww = A.b.w * B.b.w;
+    av[0] = ww;
+    av[1] = ww * r;
+    av[2] = ww * logr;
+    acc_nn = (unsigned long long)__float_as_int(A.c.z) * (unsigned long long)__float_as_int(B.c.z);
+    if (T.dkind == DK) {
+        av[3] = A.c.x * B.c.x;
+    } else if (T.dkind == DG) {
+        float g1r = A.c.x, g1i = A.c.y, g2r = B.c.x, g2i = B.c.y;
+        if (flat) {
+            // ProjectHelper<Flat>::Project: r = p2 - p1 (ProjectHelper.h:126-136)
+            float er, ei;
+            expm2i(-dx, -dy, er, ei);
+            cmul(g1r, g1i, er, ei, g1r, g1i);
+            cmul(g2r, g2i, er, ei, g2r, g2i);
+        } else if (T.coords == SPHERE) {
+            // ProjectHelper<Sphere>::Project(c1,c2,z1,z2), ProjectHelper.h:370-388,
+            // with the direction terms written on accurate differences:
+            // y1*x2 - x1*y2 = x1*dy - y1*dx,  d = p1 - p2.
+            const float x1 = A.a.x, y1 = A.a.y, z1 = A.a.z, z2 = B.a.z;
+            const float sinA = x1 * dy - y1 * dx;
+            const float cosA = dz + 0.5f * z2 * dsq;
+            const float cosB = -dz + 0.5f * z1 * dsq;
+            float e2r, e2i, e1r, e1i;
+            expm2i(sinA, -cosA, e2r, e2i);
+            expm2i(-sinA, -cosB, e1r, e1i);
+            cmul(g2r, g2i, e2r, e2i, g2r, g2i);
+            cmul(g1r, g1i, e1r, e1i, g1r, g1i);
+        } else {
+            project3d64(T, i, j, g1r, g1i, g2r, g2i);
+        }
+        // both_complex_prod(g2, g1), ProjectHelper.h:84-101.
+        const float rr = g2r * g1r, ri = g2r * g1i, ir = g2i * g1r, ii = g2i * g1i;
+        av[3] = rr + ii;   // xip
+        av[4] = ri - ir;
+        av[5] = rr - ii;   // xim
+        av[6] = ri + ir;
+    }
+}
+
 // One work item: process2 for a self item (task.y < 0), else process11 for a cell pair.
 // Writes the children to ch (nch of them) and, for an accepted pair, its bin and values.
+// MODE 1 samples the candidate pairs of the learned criterion; MODE 2 marks them (cand),
+// returns their features and prepares both outcomes: the children and, in acc_k / av, the
+// values of accepting the pair into the bin of its separation.
+template <int MODE>
 __device__ __forceinline__ void eval_task(const TravParams& T, bool has, int2 task,
                                           int2 (&ch)[4], int& nch, int& acc_k, float (&av)[7],
                                           unsigned long long& acc_nn, long long& n_eval,
-                                          long long& n_acc, long long& n_esc)
+                                          long long& n_acc, long long& n_esc, bool& cand,
+                                          float (&feat)[MLP_IN])
 {
     const bool arc = (T.metric == ARC);
     const bool flat = (T.coords == FLAT);
@@ -459,45 +513,7 @@ __device__ __forceinline__ void eval_task(const TravParams& T, bool has, int2 ta
                 if (D.act == ACT_ACCEPT) {
                     ++n_acc;
                     acc_k = D.k;
-                    const float ww = A.b.w * B.b.w;
-                    av[0] = ww;
-                    av[1] = ww * D.r;
-                    av[2] = ww * D.logr;
-                    acc_nn = (unsigned long long)__float_as_int(A.c.z) *
-                             (unsigned long long)__float_as_int(B.c.z);
-                    if (T.dkind == DK) {
-                        av[3] = A.c.x * B.c.x;
-                    } else if (T.dkind == DG) {
-                        float g1r = A.c.x, g1i = A.c.y, g2r = B.c.x, g2i = B.c.y;
-                        if (flat) {
-                            // ProjectHelper<Flat>::Project: r = p2 - p1 (ProjectHelper.h:126-136)
-                            float er, ei;
-                            expm2i(-dx, -dy, er, ei);
-                            cmul(g1r, g1i, er, ei, g1r, g1i);
-                            cmul(g2r, g2i, er, ei, g2r, g2i);
-                        } else if (T.coords == SPHERE) {
-                            // ProjectHelper<Sphere>::Project(c1,c2,z1,z2), ProjectHelper.h:370-388,
-                            // with the direction terms written on accurate differences:
-                            // y1*x2 - x1*y2 = x1*dy - y1*dx,  d = p1 - p2.
-                            const float x1 = A.a.x, y1 = A.a.y, z1 = A.a.z, z2 = B.a.z;
-                            const float sinA = x1 * dy - y1 * dx;
-                            const float cosA = dz + 0.5f * z2 * dsq;
-                            const float cosB = -dz + 0.5f * z1 * dsq;
-                            float e2r, e2i, e1r, e1i;
-                            expm2i(sinA, -cosA, e2r, e2i);
-                            expm2i(-sinA, -cosB, e1r, e1i);
-                            cmul(g2r, g2i, e2r, e2i, g2r, g2i);
-                            cmul(g1r, g1i, e1r, e1i, g1r, g1i);
-                        } else {
-                            project3d64(T, i, j, g1r, g1i, g2r, g2i);
-                        }
-                        // both_complex_prod(g2, g1), ProjectHelper.h:84-101.
-                        const float rr = g2r * g1r, ri = g2r * g1i, ir = g2i * g1r, ii = g2i * g1i;
-                        av[3] = rr + ii;   // xip
-                        av[4] = ri - ir;
-                        av[5] = rr - ii;   // xim
-                        av[6] = ri + ir;
-                    }
+                    accept_values(T, A, B, i, j, dx, dy, dz, dsq, D.r, D.logr, av, acc_nn);
                 } else if (D.act != ACT_DROP) {
                     const int L1 = __float_as_int(A.c.w), R1 = __float_as_int(A.d.x);
                     const int L2 = __float_as_int(B.c.w), R2 = __float_as_int(B.d.x);
@@ -514,6 +530,34 @@ __device__ __forceinline__ void eval_task(const TravParams& T, bool has, int2 ta
                     } else {
                         if (L2 < 0) atomicCAS(T.err, 0, DEV_BAD_CHILD);
                         else { ch[0] = make_int2(i, L2); ch[1] = make_int2(i, R2); nch = 2; }
+                    }
+                    if constexpr (MODE != 0) {
+                        const float S = s1 + s2, S2 = S * S;
+                        if (nch > 0 && rsq >= T.fminsepsq && rsq < T.fmaxsepsq &&
+                            S2 <= T.fasq * rsq && S2 <= T.cand_f2 * rsq) {
+                            const float lr = 0.5f * logf(rsq * T.finvminsepsq);
+                            int k = (int)(lr * T.finvbinsize);
+                            if (k >= T.nbins) k = T.nbins - 1;
+                            if (k >= 0) {
+                                cand = true;
+                                if constexpr (MODE == 1) {
+                                    // A fixed hash of the pair picks ~1/sample_mod of the candidates.
+                                    unsigned h = (unsigned)i * 0x9E3779B1u ^ ((unsigned)j * 0x85EBCA77u);
+                                    h ^= h >> 15; h *= 0x2C1B3C6Du; h ^= h >> 12;
+                                    if (h % T.sample_mod == 0) {
+                                        const unsigned long long o = atomicAdd(T.nsamples, 1ull);
+                                        if ((long long)o < T.sample_cap) T.samples[o] = make_int2(i, j);
+                                    }
+                                } else {
+                                    const float r = arc ? theta : sqrtf(rsq);
+                                    mlp_features(s1, s2, r, lr, T.finvbinsize, T.finvlogrange,
+                                                 T.fbinsize, feat);
+                                    acc_k = k;
+                                    accept_values(T, A, B, i, j, dx, dy, dz, dsq, r,
+                                                  lr + T.flogminsep, av, acc_nn);
+                                }
+                            }
+                        }
                     }
                 }
             }
@@ -635,7 +679,9 @@ __global__ void __launch_bounds__(TB) k_traverse(TravParams T)
         int acc_k = -1;
         float av[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         unsigned long long acc_nn = 0ull;
-        eval_task(T, has, task, ch, nch, acc_k, av, acc_nn, n_eval, n_acc, n_esc);
+        bool cand = false;
+        float feat[MLP_IN];
+        eval_task<0>(T, has, task, ch, nch, acc_k, av, acc_nn, n_eval, n_acc, n_esc, cand, feat);
         // Accumulate this iteration's accepted pairs (warp-converged here).
         if (__any_sync(0xffffffffu, acc_k >= 0))
             stage_accumulate(acc_k, av, acc_nn, nq, T.quick, stage, fb, np, nb, lane);
@@ -685,6 +731,7 @@ __global__ void __launch_bounds__(TB) k_traverse(TravParams T)
 // appended to out.  The grid is fixed; warps stride over the input, so all lanes stay busy
 // and the launch is balanced.  Bins live in shared memory for the whole launch and are added
 // to the warp's global FP64 slot at the end (the slots persist across launches).
+template <int MODE>
 __global__ void __launch_bounds__(TB, 5) k_expand(TravParams T, const int2* in, long long n_in,
                                                long long gen0, int2* out,
                                                unsigned long long* nout, long long out_cap,
@@ -708,8 +755,21 @@ __global__ void __launch_bounds__(TB, 5) k_expand(TravParams T, const int2* in, 
     for (int q = lane; q < nq * nb; q += 32) fd[q] = 0.;
     for (int q = lane; q < 4 * nb; q += 32) np[q] = 0ull;
     for (int q = lane; q < 4 * nq * nb; q += 32) fb[q] = 0.f;
+    // MODE 2: the network in shared memory after the bins, then per-warp staging.
+    MLPPacked* mlpW = nullptr;
+    __half* msx = nullptr;
+    float* msy = nullptr;
+    if constexpr (MODE == 2) {
+        unsigned char* mb = smem + ((WPB * wbytes + 15) & ~(size_t)15);
+        mlpW = reinterpret_cast<MLPPacked*>(mb);
+        msx = reinterpret_cast<__half*>(mb + sizeof(MLPPacked)) + wib * 32 * 8;
+        msy = reinterpret_cast<float*>(mb + sizeof(MLPPacked) + WPB * 32 * 8 * sizeof(__half)) + wib * 32;
+        for (int q = threadIdx.x; q < (int)(sizeof(MLPPacked) / 4); q += TB)
+            reinterpret_cast<uint32_t*>(mlpW)[q] = reinterpret_cast<const uint32_t*>(T.mlp)[q];
+        __syncthreads();
+    }
     __syncwarp();
-    long long n_eval = 0, n_acc = 0, n_esc = 0;
+    long long n_eval = 0, n_acc = 0, n_esc = 0, n_learn = 0;
     const long long stride = (long long)gridDim.x * TB;
     int iter = 0;
     for (long long base = (long long)gw * 32; base < n_in; base += stride) {
@@ -722,7 +782,24 @@ __global__ void __launch_bounds__(TB, 5) k_expand(TravParams T, const int2* in, 
         int acc_k = -1;
         float av[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         unsigned long long acc_nn = 0ull;
-        eval_task(T, has, task, ch, nch, acc_k, av, acc_nn, n_eval, n_acc, n_esc);
+        bool cand = false;
+        float feat[MLP_IN];
+        eval_task<MODE>(T, has, task, ch, nch, acc_k, av, acc_nn, n_eval, n_acc, n_esc, cand, feat);
+        if constexpr (MODE == 2) {
+            // The learned criterion for the warp's candidate pairs: accept (drop the
+            // children) or split (drop the prepared accept values).
+            if (__any_sync(0xffffffffu, cand)) {
+                if (!cand) {
+#pragma unroll
+                    for (int q = 0; q < MLP_IN; ++q) feat[q] = 0.f;
+                }
+                const float y = mlp_warp_eval(*mlpW, feat, msx, msy);
+                if (cand) {
+                    if (y <= T.mlp_thr) { nch = 0; ++n_acc; ++n_learn; }
+                    else acc_k = -1;
+                }
+            }
+        }
         if (__any_sync(0xffffffffu, acc_k >= 0))
             stage_accumulate(acc_k, av, acc_nn, nq, T.quick, stage, fb, np, nb, lane);
         // Append the children: warp scan, one atomic per warp.
@@ -753,6 +830,7 @@ __global__ void __launch_bounds__(TB, 5) k_expand(TravParams T, const int2* in, 
         n_eval += __shfl_xor_sync(0xffffffffu, n_eval, o);
         n_acc += __shfl_xor_sync(0xffffffffu, n_acc, o);
         n_esc += __shfl_xor_sync(0xffffffffu, n_esc, o);
+        if constexpr (MODE == 2) n_learn += __shfl_xor_sync(0xffffffffu, n_learn, o);
     }
     if (n_acc == 0) {   // nothing accumulated by this warp in this launch
         if (lane == 0 && n_eval) atomicAdd(&T.counters[0], (unsigned long long)n_eval);
@@ -769,6 +847,7 @@ __global__ void __launch_bounds__(TB, 5) k_expand(TravParams T, const int2* in, 
         atomicAdd(&T.counters[0], (unsigned long long)n_eval);
         atomicAdd(&T.counters[1], (unsigned long long)n_acc);
         atomicAdd(&T.counters[2], (unsigned long long)n_esc);
+        if (MODE == 2 && n_learn) atomicAdd(&T.counters[3], (unsigned long long)n_learn);
     }
 }
 
@@ -839,46 +918,57 @@ int traverse_grid(int nq, int nb, int* blocks, int* nwarps)
     return 0;
 }
 
-int launch_expand(const TravParams& T, int blocks, const int2* in, long long n_in,
-                  long long gen0, int2* out, unsigned long long* nout, long long out_cap,
-                  cudaStream_t st)
+// Shared memory of k_expand<mode>: the warps' bins, and for mode 2 the network and the
+// warps' staging areas.
+static size_t expand_smem_bytes(int nq, int nb, int mode)
 {
-    size_t sm = traverse_smem_bytes(T.nqf, T.nbins);
-    static bool attr_set = false;
-    if (!attr_set && sm > 48 * 1024) {
-        TC_CU(cudaFuncSetAttribute(k_expand, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)traverse_smem_bytes(7, 256)));
-        attr_set = true;
-    }
-    count_launch();
-    k_expand<<<blocks, TB, sm, st>>>(T, in, n_in, gen0, out, nout, out_cap, nullptr);
-    TC_CU(cudaGetLastError());
+    size_t sm = traverse_smem_bytes(nq, nb);
+    if (mode == 2)
+        sm = ((sm + 15) & ~(size_t)15) + sizeof(MLPPacked) +
+             WPB * 32 * (8 * sizeof(__half) + sizeof(float));
+    return sm;
+}
+
+template <int MODE>
+static int set_expand_attr(size_t sm)
+{
+    if (sm > 48 * 1024)
+        TC_CU(cudaFuncSetAttribute(k_expand<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     return 0;
 }
 
 int launch_expand_batch(const TravParams& T, int blocks, ExpandSched* dS, int iters,
                         cudaStream_t st)
 {
-    size_t sm = traverse_smem_bytes(T.nqf, T.nbins);
+    const size_t sm = expand_smem_bytes(T.nqf, T.nbins, T.mode);
     for (int it = 0; it < iters; ++it) {
         count_launch();
         k_expand_sched<<<1, 1, 0, st>>>(dS);
         count_launch();
-        k_expand<<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
+        if (T.mode == 2) k_expand<2><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
+        else if (T.mode == 1) k_expand<1><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
+        else k_expand<0><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
     }
     TC_CU(cudaGetLastError());
     return 0;
 }
 
-int expand_grid(int nq, int nb, int* blocks, int* nwarps)
+int expand_grid(int nq, int nb, int* blocks, int* nwarps, int mode)
 {
     int dev = 0, nsm = 0, per = 0;
     TC_CU(cudaGetDevice(&dev));
     TC_CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    size_t sm = traverse_smem_bytes(nq, nb);
-    if (sm > 48 * 1024)
-        TC_CU(cudaFuncSetAttribute(k_expand, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    TC_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_expand, TB, sm));
+    const size_t sm = expand_smem_bytes(nq, nb, mode);
+    if (mode == 2) {
+        TC_TRY(set_expand_attr<2>(sm));
+        TC_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_expand<2>, TB, sm));
+    } else if (mode == 1) {
+        TC_TRY(set_expand_attr<1>(sm));
+        TC_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_expand<1>, TB, sm));
+    } else {
+        TC_TRY(set_expand_attr<0>(sm));
+        TC_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_expand<0>, TB, sm));
+    }
     if (per < 1) per = 1;
     *blocks = nsm * per;
     *nwarps = *blocks * WPB;

@@ -37,8 +37,20 @@ struct TravParams {
     int* idle;
     double* wacc;
     unsigned long long* wnp;
-    unsigned long long* counters;   // [0] evaluated, [1] accepted, [2] escalated
+    unsigned long long* counters;   // [0] evaluated, [1] accepted, [2] escalated,
+                                    // [3] accepted by the learned criterion
     int* err;
+    // Learned opening criterion.  mode 0: the bin_slop rule; 1: the rule, and candidate pairs
+    // are sampled into `samples`; 2: candidates go through the network.  A candidate is a
+    // pair the rule splits with min_sep^2 <= rsq < max_sep^2, (s1+s2)^2 <= a^2 rsq and
+    // (s1+s2)^2 <= cand_f2 rsq; the network accepts it when its output is <= mlp_thr.
+    int mode;
+    float cand_f2, mlp_thr, finvlogrange;
+    const struct MLPPacked* mlp;
+    int2* samples;
+    unsigned long long* nsamples;
+    long long sample_cap;
+    unsigned sample_mod;
 };
 
 // Fixed traversal scratch of the allocation-free entry point (traverse2pt.cu).
@@ -83,13 +95,10 @@ void launch_pack_cells(int ncap, const Cells& C, TCell* out, cudaStream_t st);
 size_t traverse_smem_bytes(int nq, int nb);
 int traverse_grid(int nq, int nb, int* blocks, int* nwarps);
 int launch_traverse(const TravParams& T, int blocks, cudaStream_t st);
-int expand_grid(int nq, int nb, int* blocks, int* nwarps);
+int expand_grid(int nq, int nb, int* blocks, int* nwarps, int mode = 0);
 // Enqueues `iters` (schedule, expand) pairs on st without synchronising.
 int launch_expand_batch(const TravParams& T, int blocks, ExpandSched* dS, int iters,
                         cudaStream_t st);
-int launch_expand(const TravParams& T, int blocks, const int2* in, long long n_in,
-                  long long gen0, int2* out, unsigned long long* nout, long long out_cap,
-                  cudaStream_t st);
 int launch_reduce(int nwarps, int nq, int nb, const double* wacc, const unsigned long long* wnp,
                   double* out, unsigned long long* outnp, cudaStream_t st);
 
