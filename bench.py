@@ -411,6 +411,88 @@ def run_gpu_ggg(args, rank, world):
     return line
 
 
+def run_learned(args, rank, world):
+    """Learned vs plain split on the curved-sky GG workload: the network is trained on a
+    1M-point catalog (a different seed), then the plain bin_slop 0.1 rule, the rule at
+    bin_slop 0.2 and the learned criterion (base bin_slop 0.1, candidates up to 4 b r,
+    accept when the predicted log10 leak <= threshold) process the evaluation catalog; each
+    is compared with bin_slop 0 / angle_slop 0.02 on the same catalog."""
+    import torch
+    from treecorr_gb300 import _treecorr as T, learned
+    dev = torch.device("cuda", rank % max(torch.cuda.device_count(), 1))
+    torch.cuda.set_device(dev)
+    e = np.array([])
+
+    def field(cat):
+        f = T.GFieldSphere(cat["x"], cat["y"], cat["z"], cat["g1"], cat["g2"], cat["w"], e,
+                           0.0, 0.0, T.Mean, 0, False, 3, 10)
+        f.getNTopLevel()
+        return f
+
+    def corr(slop, a=0.1):
+        B = binning(slop)
+        out = {k: np.zeros(B["nbins"]) for k in ("xi0", "xi1", "xi2", "xi3", "meanr",
+                                                  "meanlogr", "weight", "npairs")}
+        c = T.GGCorr(T.Log, B["min_sep"], B["max_sep"], B["nbins"], B["bin_size"], B["b"], a,
+                     -sys.float_info.max, sys.float_info.max, 0., 0., 0., out["xi0"],
+                     out["xi1"], out["xi2"], out["xi3"], out["meanr"], out["meanlogr"],
+                     out["weight"], out["npairs"])
+        return c, out
+
+    t0 = time.perf_counter()
+    ftrain = field(curved_sky_catalog(1_000_000, seed=args.seed + 1000))
+    c, _ = corr(0.1)
+    x, y = learned.collect(c, ftrain, T.Arc, sample_mod=4, max_samples=4 << 20)
+    params, loss = learned.train(x, y, steps=4000, batch=8192, lr=2e-3, seed=0)
+    t_train = time.perf_counter() - t0
+    del ftrain
+    f = field(curved_sky_catalog(args.n, seed=args.seed + rank))
+
+    def run(c, out, reps):
+        c.processAuto(f, False, False, T.Arc)
+        ts = []
+        for _ in range(reps):
+            for k in out:
+                out[k][:] = 0.
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            c.processAuto(f, False, False, T.Arc)
+            ts.append(time.perf_counter() - t1)
+        st = c.stats()
+        return {"wall_s": float(np.median(ts)), "cell_pairs": st["cell_pairs"],
+                "accepted": st["accepted"], "learned": st["learned"],
+                "xip": out["xi0"] / out["weight"], "xim": out["xi2"] / out["weight"]}
+
+    ce, oe = corr(0.0, a=0.02)
+    ex = run(ce, oe, 1)
+    res = {}
+    for name, slop in (("plain_bs0.1", 0.1), ("plain_bs0.2", 0.2)):
+        cp, op = corr(slop)
+        res[name] = run(cp, op, args.steps)
+    cl, ol = corr(0.1)
+    cl.setLearned(params, threshold=args.learned_threshold, cand_factor=4.0)
+    res["learned"] = run(cl, ol, args.steps)
+    mx = float(np.abs(ex["xip"]).max())
+    for r in res.values():
+        r["dxip_rel"] = float(np.abs(r["xip"] - ex["xip"]).max() / mx)
+        r["dxim_rel"] = float(np.abs(r["xim"] - ex["xim"]).max() / mx)
+        del r["xip"], r["xim"]
+    speed = res["plain_bs0.1"]["wall_s"] / res["learned"]["wall_s"]
+    return {"metric": "GG wall-s, learned vs plain split (ratio plain/learned)",
+            "value": speed, "unit": "x", "n_gpus": world, "steps": args.steps,
+            "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f16 network", "data": "synthetic (seeded curved-sky GRF catalog)",
+            "config": {"workload": f"GG auto, {args.n}-point curved sky, Arc, 30 Log bins "
+                                   "1-300'; network trained on a 1M-point catalog",
+                       "threshold": args.learned_threshold, "cand_factor": 4.0},
+            "reference_result": "bin_slop 0, angle_slop 0.02 on the same catalog "
+                                f"({ex['wall_s']:.2f} s); errors are max over bins of "
+                                "|xi - xi_ref| / max|xi+_ref|",
+            "train": {"samples": int(len(y)), "seconds": t_train,
+                      "loss_first": float(loss[0]), "loss_last": float(loss[-20:].mean())},
+            "results": res}
+
+
 def cpu_sample(cat, bins, args, budget_s=15.0):
     """The oracle port of the reference algorithm on the host cores, over top-level rows of
     the auto loop until about budget_s seconds of traversal have been timed."""
@@ -520,8 +602,10 @@ def main():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    p.add_argument("--workload", default="gg", choices=["gg", "ggg"],
-                   help="gg: the 2-point headline; ggg: the multipole 3-point configuration")
+    p.add_argument("--workload", default="gg", choices=["gg", "ggg", "learned"],
+                   help="gg: the 2-point headline; ggg: the multipole 3-point configuration; "
+                        "learned: the learned opening criterion against the plain rule")
+    p.add_argument("--learned-threshold", type=float, default=-3.0)
     p.add_argument("--n", type=int, default=10_000_000)
     p.add_argument("--bin-slop", type=float, default=0.1)
     p.add_argument("--seed", type=int, default=20261203)
@@ -535,6 +619,8 @@ def main():
         line = run_reference(args, rank, world)
     elif args.workload == "ggg":
         line = run_gpu_ggg(args, rank, world)
+    elif args.workload == "learned":
+        line = run_learned(args, rank, world)
     else:
         line = run_gpu(args, rank, world)
     if rank == 0 and line is not None:
