@@ -731,6 +731,24 @@ __global__ void __launch_bounds__(TB) k_traverse(TravParams T)
 // appended to out.  The grid is fixed; warps stride over the input, so all lanes stay busy
 // and the launch is balanced.  Bins live in shared memory for the whole launch and are added
 // to the warp's global FP64 slot at the end (the slots persist across launches).
+__device__ void sched_step(ExpandSched* S);
+
+// The last warp of a scheduled launch to finish runs the schedule step for the next one.
+__device__ __forceinline__ void expand_warp_done(const ExpandSched* S, int lane)
+{
+    if (!S) return;
+    if (lane == 0) {
+        ExpandSched* W = const_cast<ExpandSched*>(S);
+        __threadfence();
+        const unsigned total = gridDim.x * (blockDim.x >> 5);
+        if (atomicAdd(&W->warps_done, 1u) == total - 1) {
+            __threadfence();
+            W->warps_done = 0;
+            sched_step(W);
+        }
+    }
+}
+
 template <int MODE>
 __global__ void __launch_bounds__(TB, 5) k_expand(TravParams T, const int2* in, long long n_in,
                                                long long gen0, int2* out,
@@ -834,6 +852,7 @@ __global__ void __launch_bounds__(TB, 5) k_expand(TravParams T, const int2* in, 
     }
     if (n_acc == 0) {   // nothing accumulated by this warp in this launch
         if (lane == 0 && n_eval) atomicAdd(&T.counters[0], (unsigned long long)n_eval);
+        expand_warp_done(S, lane);
         return;
     }
     __syncwarp();
@@ -849,10 +868,11 @@ __global__ void __launch_bounds__(TB, 5) k_expand(TravParams T, const int2* in, 
         atomicAdd(&T.counters[2], (unsigned long long)n_esc);
         if (MODE == 2 && n_learn) atomicAdd(&T.counters[3], (unsigned long long)n_learn);
     }
+    expand_warp_done(S, lane);
 }
 
 // The schedule step: commits the previous launch's children and picks the next chunk.
-__global__ void k_expand_sched(ExpandSched* S)
+__device__ void sched_step(ExpandSched* S)
 {
     if (S->out_level >= 0) {
         S->cnt[S->out_level] += (long long)S->nout;
@@ -860,6 +880,7 @@ __global__ void k_expand_sched(ExpandSched* S)
     }
     S->nout = 0;
     S->n_in = 0;
+    S->pending = 0;
     if (S->done || S->need_levels) return;
     int L = S->nlev - 1;
     while (L >= 0 && S->cnt[L] == 0) --L;
@@ -875,6 +896,14 @@ __global__ void k_expand_sched(ExpandSched* S)
     S->out_cap = S->cap - S->cnt[L + 1];
     S->out_level = L + 1;
     S->launches += 1;
+    S->pending = 1;
+}
+
+// Start of a batch: a step only if no picked chunk is waiting (the last warp of the
+// previous batch's final launch may already have picked one).
+__global__ void k_expand_sched(ExpandSched* S)
+{
+    if (!S->pending) sched_step(S);
 }
 
 // Sum of the per-warp totals in a fixed order: out[q*nb+k] (double), outnp[k] (u64).
@@ -941,9 +970,11 @@ int launch_expand_batch(const TravParams& T, int blocks, ExpandSched* dS, int it
                         cudaStream_t st)
 {
     const size_t sm = expand_smem_bytes(T.nqf, T.nbins, T.mode);
+    // One schedule step starts the batch (the host may have changed the schedule); every
+    // expand launch ends with the next step, run by its last warp.
+    count_launch();
+    k_expand_sched<<<1, 1, 0, st>>>(dS);
     for (int it = 0; it < iters; ++it) {
-        count_launch();
-        k_expand_sched<<<1, 1, 0, st>>>(dS);
         count_launch();
         if (T.mode == 2) k_expand<2><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
         else if (T.mode == 1) k_expand<1><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);

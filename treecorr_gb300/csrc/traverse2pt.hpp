@@ -89,6 +89,8 @@ struct ExpandSched {
     int2* out;
     unsigned long long nout;
     long long launches;
+    unsigned int warps_done;       // warps of the current expand launch that have finished
+    int pending;                   // a picked chunk waits for its expand launch
 };
 
 void launch_pack_cells(int ncap, const Cells& C, TCell* out, cudaStream_t st);
