@@ -206,6 +206,36 @@ double tc_corr3_last_ms(const tc_corr3* c);
  * the record buffer was full, out[2] finish/contract waves.  Returns TC_OK. */
 int tc_corr3_stats(const tc_corr3* c, int64_t out[3]);
 
+/* Patches: every patch-pair correlation of npatch patch fields in one expansion (replaces
+ * the Python loop over patch pairs, treecorr/corr2base.py:929-950, and its processAuto /
+ * processCross calls).  Pairs (i, j), i <= j, whose fields can overlap (triviallyZero,
+ * src/Corr2.cpp:1107-1128) are processed; pair_i / pair_j receive them and results receives
+ * per pair 8 arrays of nbins doubles: weight, meanr, meanlogr, xi0, xi1, xi2, xi3, npairs
+ * (raw sums, as in the reference's results[(i, j)] before _finalize).  The corr's own
+ * output arrays are not touched. */
+int tc_corr2_process_patches(tc_corr2* corr, tc_field* const* fields, int npatch, int metric,
+                             int quick, int max_pairs, int32_t* pair_i, int32_t* pair_j,
+                             double* results, int* npairs_out);
+
+/* Jackknife design matrix and covariance on the device from per-pair results (layout of
+ * tc_corr2_process_patches): row l sums the pairs with the reference's weights
+ * (JackknifePairIterator, corr2base.py:1787-1817; cross_patch_weight 0 simple, 1 mean,
+ * 2 match), divides by the weight (_finalize) and takes the statistic (GG: xip, xim;
+ * KK: xi); cov = (1 - 1/npatch) sum_l (v_l - mean)(v_l - mean)^T (_cov_jackknife,
+ * corr2base.py:2432-2445).  v_out: npatch x nstat*nbins, cov_out: (nstat*nbins)^2. */
+int tc_jackknife_cov(const double* results, const int32_t* pair_i, const int32_t* pair_j,
+                     int npair, int npatch, int nbins, int dkind, int cross_patch_weight,
+                     double* v_out, double* cov_out);
+
+/* GenerateXYZ (src/KMeans.cpp:1013-1050, pybind11 at src/Field.cpp:700-702; caller
+ * treecorr/catalog.py:1609-1622): x = cos(dec) cos(ra), y = cos(dec) sin(ra), z = sin(dec),
+ * each times r[i] when r is not NULL.  Host arrays of length n (copied to the device and
+ * back), or device arrays for tc_generate_xyz_device. */
+int tc_generate_xyz(double* x, double* y, double* z, const double* ra, const double* dec,
+                    const double* r, int64_t n);
+int tc_generate_xyz_device(double* x, double* y, double* z, const double* ra,
+                           const double* dec, const double* r, int64_t n);
+
 /* ---- Learned opening criterion (no reference counterpart) ----------------------------
  * A 5-64-64-1 ReLU network (FP32 master parameters, tc_mlp_nparam() floats: W1[64][5],
  * b1[64], W2[64][64], b2[64], w3[64], b3) revisits the cell pairs the bin_slop rule

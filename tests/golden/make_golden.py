@@ -95,7 +95,7 @@ def run_case(name):
     return out
 
 
-if __name__ == "__main__" and "--mp" not in sys.argv:
+if __name__ == "__main__" and "--mp" not in sys.argv and "--xyz" not in sys.argv:
     _treecorr.SetOMPThreads(1)
     names = sys.argv[1:] or list(CASES)
     for name in names:
@@ -143,3 +143,19 @@ if __name__ == "__main__" and "--mp" in sys.argv:
     for name in CASES3:
         out = run_case3(name)
         print(f"{name:20s} ntri={out['ntri'].sum():.6g} weight={out['weight'].sum():.6g}")
+
+
+# GenerateXYZ (src/KMeans.cpp:1013-1050): ra/dec (radians), with and without a distance.
+if __name__ == "__main__" and "--xyz" in sys.argv:
+    rng = np.random.default_rng(20240613)
+    n = 4000
+    ra = rng.uniform(0, 2 * np.pi, n)
+    dec = np.arcsin(rng.uniform(-1, 1, n))
+    r = rng.uniform(10., 3000., n)
+    out = {"ra": ra, "dec": dec, "r": r}
+    for tag, rr in (("", np.array([])), ("_r", r)):
+        x, y, z = np.zeros(n), np.zeros(n), np.zeros(n)
+        _treecorr.GenerateXYZ(x, y, z, ra, dec, rr)
+        out["x" + tag], out["y" + tag], out["z" + tag] = x, y, z
+    np.savez(os.path.join(HERE, "generate_xyz.npz"), **out)
+    print("generate_xyz.npz")

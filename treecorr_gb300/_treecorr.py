@@ -85,6 +85,18 @@ def lib():
             [ctypes.c_double] * 8 + [ctypes.POINTER(ctypes.c_int)]
         L.tc_corr2_stats.restype = ctypes.c_int
         L.tc_corr2_stats.argtypes = [vp, ctypes.POINTER(tc_stats)]
+        i32p = ctypes.POINTER(ctypes.c_int32)
+        L.tc_corr2_process_patches.restype = ctypes.c_int
+        L.tc_corr2_process_patches.argtypes = [vp, ctypes.POINTER(vp), ctypes.c_int, ctypes.c_int,
+                                               ctypes.c_int, ctypes.c_int, i32p, i32p, dp,
+                                               ctypes.POINTER(ctypes.c_int)]
+        L.tc_jackknife_cov.restype = ctypes.c_int
+        L.tc_jackknife_cov.argtypes = [dp, i32p, i32p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_int, dp, dp]
+        L.tc_generate_xyz.restype = ctypes.c_int
+        L.tc_generate_xyz.argtypes = [dp, dp, dp, dp, dp, dp, i64]
+        L.tc_generate_xyz_device.restype = ctypes.c_int
+        L.tc_generate_xyz_device.argtypes = [vp, vp, vp, vp, vp, vp, i64]
         fp = ctypes.POINTER(ctypes.c_float)
         L.tc_mlp_nparam.restype = ctypes.c_int
         L.tc_mlp_nparam.argtypes = []
@@ -339,6 +351,43 @@ def launch_count():
     return int(lib().tc_launch_count())
 
 
+vp_t = ctypes.c_void_p
+
+_CPW = {"simple": 0, "mean": 1, "match": 2}
+
+
+def jackknife_cov(results, pairs, npatch, dkind, cross_patch_weight="simple"):
+    """Jackknife design matrix and covariance on the GPU from processPatches results
+    (_cov_jackknife, corr2base.py:2432-2445).  dkind: 1 (KK) or 2 (GG).  Returns (v, cov)."""
+    results = np.ascontiguousarray(results, dtype=float)
+    npair, _, nb = results.shape
+    pi = np.ascontiguousarray([p[0] for p in pairs], dtype=np.int32)
+    pj = np.ascontiguousarray([p[1] for p in pairs], dtype=np.int32)
+    nstat = 2 if dkind == 2 else 1
+    v = np.zeros((npatch, nstat * nb))
+    cov = np.zeros((nstat * nb, nstat * nb))
+    _check(lib().tc_jackknife_cov(_ptr(results), pi.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                  pj.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), npair, npatch,
+                                  nb, int(dkind), _CPW[cross_patch_weight], _ptr(v), _ptr(cov)))
+    return v, cov
+
+
+def GenerateXYZ(x, y, z, ra, dec, r):
+    """_treecorr.GenerateXYZ (src/KMeans.cpp:1013-1050): fills x, y, z in place from ra, dec
+    (radians) and, unless r is empty, the distance r; computed on the GPU."""
+    n = len(ra)
+    for a in (x, y, z):
+        if len(a) != n or a.dtype != np.float64 or not a.flags.c_contiguous:
+            raise ValueError("x, y, z must be contiguous float64 arrays of len(ra)")
+    ra = np.ascontiguousarray(ra, dtype=float)
+    dec = np.ascontiguousarray(dec, dtype=float)
+    if len(dec) != n or (len(r) not in (0, n)):
+        raise ValueError("ra, dec and r must have the same length")
+    rr = np.ascontiguousarray(r, dtype=float) if len(r) else None
+    _check(lib().tc_generate_xyz(_ptr(x), _ptr(y), _ptr(z), _ptr(ra), _ptr(dec),
+                                 _ptr(rr) if rr is not None else None, n))
+
+
 # ----------------------------------------------------------------------------------------
 # Learned opening criterion (no reference counterpart; see include/tcgpu.h).
 
@@ -410,6 +459,7 @@ class BaseCorr2:
                 raise ValueError(f"{name} has size {arr.size}, expected nbins={nbins}")
             outs.append(arr)
         self._outs = outs
+        self._nbins = int(nbins)
         h = ctypes.c_void_p()
         _check(lib().tc_corr2_create(self._dkind, self._dkind, int(bin_type), float(minsep),
                                      float(maxsep), int(nbins), float(binsize), float(b),
@@ -441,6 +491,26 @@ class BaseCorr2:
 
     def samplePairs(self, *args):
         raise NotImplementedError("samplePairs is not on the GPU path")
+
+    def processPatches(self, fields, metric, quick=False):
+        """Every patch-pair correlation of the patch fields in one GPU expansion (the Python
+        loop of corr2base.py:929-950).  Returns (pairs, results): pairs [(i, j)], i <= j, and
+        results [npair, 8, nbins] = weight, meanr, meanlogr, xi0..xi3, npairs for each pair
+        (raw sums).  No reference counterpart in the native module."""
+        n = len(fields)
+        arr = (vp_t * n)(*[f._h for f in fields])
+        maxp = n * (n + 1) // 2
+        nb = self._nbins
+        pi = np.zeros(maxp, dtype=np.int32)
+        pj = np.zeros(maxp, dtype=np.int32)
+        res = np.zeros((maxp, 8, nb))
+        npair = ctypes.c_int(0)
+        _check(lib().tc_corr2_process_patches(
+            self._h, arr, n, int(metric), int(bool(quick)), maxp,
+            pi.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+            pj.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _ptr(res), ctypes.byref(npair)))
+        k = npair.value
+        return list(zip(pi[:k].tolist(), pj[:k].tolist())), res[:k].copy()
 
     def setLearned(self, params=None, threshold=-2.0, cand_factor=4.0):
         """Use the learned opening criterion (params: tc_mlp_nparam() floats) in the following
@@ -559,5 +629,4 @@ for _n in ("NKCorr", "NZCorr", "KZCorr", "ZZCorr", "NVCorr", "KVCorr", "VVCorr",
     globals()[_n] = _not_on_path(_n)
 QuickAssign = _not_on_path("QuickAssign")
 SelectPatch = _not_on_path("SelectPatch")
-GenerateXYZ = _not_on_path("GenerateXYZ")
 del _n

@@ -115,6 +115,65 @@ struct tc_corr2 {
 };
 
 namespace {
+// Patches: the combined cell records of all patch fields (children ids rebased, patch id in
+// d.y) with their FP64 centres.
+__global__ void k_rebase_cells(TCell* t, long long n, int base, int patch)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    TCell c = t[i];
+    const int L = __float_as_int(c.c.w), R = __float_as_int(c.d.x);
+    c.c.w = __int_as_float(L >= 0 ? L + base : L);
+    c.d.x = __int_as_float(R >= 0 ? R + base : R);
+    c.d.y = __int_as_float(patch);
+    t[i] = c;
+}
+
+// Jackknife rows (corr2base.py:1787-1823 pair weights, 1333-1352 _sum, 1274-1294 _finalize):
+// row l sums the patch pairs' arrays with weight w(l, i, j) and divides by the weight.
+// res: [npair][8][nb] (weight, meanr, meanlogr, xi0..xi3, npairs); stat: the xi indices
+// that make the data vector (GG: xi0, xi2 = xip, xim; KK: xi0).
+__global__ void k_jackknife_rows(const double* res, const int* pi, const int* pj, int npair,
+                                 int nb, int cpw, double wmatch, int nstat, int s0, int s1,
+                                 double* v, double* wrow)
+{
+    const int l = blockIdx.x;
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+        double wsum = 0., x0 = 0., x1 = 0.;
+        for (int p = 0; p < npair; ++p) {
+            const int i = pi[p], j = pj[p];
+            double w;
+            if (cpw == 0) w = (i != l && j != l) ? 1. : 0.;                  // simple
+            else if (i == l && j == l) w = 0.;
+            else if (i == l || j == l) w = cpw == 1 ? 0.5 : wmatch;        // mean / match
+            else w = 1.;
+            if (w == 0.) continue;
+            const double* r = res + (size_t)p * 8 * nb;
+            wsum += w * r[t];
+            x0 += w * r[(3 + s0) * nb + t];
+            if (nstat > 1) x1 += w * r[(3 + s1) * nb + t];
+        }
+        v[(size_t)l * nstat * nb + t] = wsum != 0. ? x0 / wsum : 0.;
+        if (nstat > 1) v[(size_t)l * nstat * nb + nb + t] = wsum != 0. ? x1 / wsum : 0.;
+        if (t == 0) wrow[l] = 0.;
+    }
+}
+
+// C = (1 - 1/n) sum_l (v_l - mean)(v_l - mean)^T (_cov_jackknife, corr2base.py:2432-2445).
+__global__ void k_jackknife_cov(const double* v, int nrow, int nv, double* cov)
+{
+    const int a = blockIdx.x, b = threadIdx.x + blockIdx.y * blockDim.x;
+    if (b >= nv) return;
+    double ma = 0., mb = 0.;
+    for (int l = 0; l < nrow; ++l) { ma += v[(size_t)l * nv + a]; mb += v[(size_t)l * nv + b]; }
+    ma /= nrow; mb /= nrow;
+    double c = 0.;
+    for (int l = 0; l < nrow; ++l) c += (v[(size_t)l * nv + a] - ma) * (v[(size_t)l * nv + b] - mb);
+    cov[(size_t)a * nv + b] = (1. - 1. / nrow) * c;
+}
+}  // namespace
+
+namespace {
 
 void free_points(Points& P)
 {
@@ -395,6 +454,92 @@ int check_metric(int coords, int metric)
     return TC_ERR_UNSUPPORTED;
 }
 
+// The binning constants of a traversal (BaseCorr2 constructor, src/Corr2.cpp:55-80), in
+// FP64 and FP32.
+void trav_setup(const tc_corr2* c, TravParams& T, int coords, int metric, int quick, int nq)
+{
+    std::memset(&T, 0, sizeof(T));
+    T.coords = coords; T.metric = metric; T.dkind = c->d1; T.quick = quick ? 1 : 0;
+    T.nbins = c->nbins; T.nqf = nq;
+    T.minsep = c->minsep; T.maxsep = c->maxsep; T.binsize = c->binsize; T.b = c->b; T.a = c->a;
+    T.logminsep = std::log(c->minsep); T.halfminsep = 0.5 * c->minsep;
+    T.minsepsq = c->minsep * c->minsep; T.maxsepsq = c->maxsep * c->maxsep;
+    T.bsq = c->b * c->b; T.asq = c->a * c->a;
+    T.fminsep = (float)T.minsep; T.fmaxsep = (float)T.maxsep; T.fbinsize = (float)T.binsize;
+    T.fb = (float)T.b; T.fminsepsq = (float)T.minsepsq; T.fmaxsepsq = (float)T.maxsepsq;
+    T.fbsq = (float)T.bsq; T.fasq = (float)std::min(T.asq, 1e30);
+    T.fbb = (float)(0.25 * sqr(T.binsize + T.b));
+    T.fmineff = (float)std::min(T.bsq, T.asq);
+    T.finvminsepsq = (float)(1. / T.minsepsq);
+    T.finvbinsize = (float)(1. / T.binsize);
+    T.flogminsep = (float)T.logminsep;
+}
+
+// Runs the breadth-first expansion of T to completion (device-side schedule, batches of
+// launches, more level buffers on demand).  *derr: the device error word afterwards.
+int expand_run(tc_corr2* c, const TravParams& T, int blocks, long long npoints, cudaStream_t st,
+               int* derr_out, long long* launches_out)
+{
+    // The schedule lives on the device: batches of (schedule, expand) launches run without
+    // host round trips; the host only adds level buffers when the expansion gets deeper.
+    // Chunk size: up to 4M items per launch, less for small catalogs (level buffers hold
+    // 4 chunks each).
+    long long CH = 1LL << 16;
+    while (CH < (1LL << 22) && CH < 2 * npoints) CH <<= 1;
+    if (!c->sched) TC_TRY(dalloc(&c->sched, 1));
+    ExpandSched hs;
+    std::memset(&hs, 0, sizeof(hs));
+    hs.cnt[0] = T.ngen + T.nin;
+    hs.cap = 4 * CH;
+    hs.chunk_max = CH;
+    hs.out_level = -1;
+    int nlev = 32;
+    for (int l = 1; l < nlev; ++l) {
+        TC_TRY(level_reserve(c, l, 0, hs.cap, st));
+        hs.lev[l] = c->lev[l];
+    }
+    hs.nlev = nlev;
+    TC_CU(cudaMemcpyAsync(c->sched, &hs, sizeof(hs), cudaMemcpyHostToDevice, st));
+    int derr = 0;
+    long long launches = 0;
+    for (int batch = 0;; ++batch) {
+        TC_TRY(launch_expand_batch(T, blocks, c->sched, 64, st));
+        int flags[3];
+        TC_CU(cudaMemcpyAsync(flags, &c->sched->done, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
+        TC_CU(cudaMemcpyAsync(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        TC_CU(cudaStreamSynchronize(st));
+        if (derr) break;
+        if (flags[1]) {   // need_levels: the expansion reached the last allocated level
+            if (nlev >= EXP_MAXLEV) {
+                set_last_error("the dual-tree expansion is deeper than 512 levels");
+                return TC_ERR_DEVICE;
+            }
+            int nl2 = std::min(EXP_MAXLEV, 2 * nlev);
+            for (int l = nlev; l < nl2; ++l) {
+                TC_TRY(level_reserve(c, l, 0, hs.cap, st));
+                hs.lev[l] = c->lev[l];
+            }
+            TC_CU(cudaMemcpyAsync(&c->sched->lev[nlev], &hs.lev[nlev],
+                                  sizeof(int2*) * (nl2 - nlev), cudaMemcpyHostToDevice, st));
+            const int zero = 0;
+            TC_CU(cudaMemcpyAsync(&c->sched->nlev, &nl2, sizeof(int), cudaMemcpyHostToDevice, st));
+            TC_CU(cudaMemcpyAsync(&c->sched->need_levels, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
+            nlev = nl2;
+            continue;
+        }
+        if (flags[0]) break;
+        if (batch > 1000000) {
+            set_last_error("traversal did not finish within 10^6 batches");
+            return TC_ERR_DEVICE;
+        }
+    }
+    TC_CU(cudaMemcpyAsync(&launches, &c->sched->launches, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    TC_CU(cudaStreamSynchronize(st));
+    *derr_out = derr;
+    *launches_out = launches;
+    return TC_OK;
+}
+
 // BaseCorr2::process for one or two fields.
 int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
 {
@@ -426,21 +571,8 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
     const int nb = c->nbins;
     const int nq = c->d1 == TC_GDATA ? 7 : (c->d1 == TC_KDATA ? 4 : 3);
     TravParams T;
-    std::memset(&T, 0, sizeof(T));
-    T.coords = f1->coords; T.metric = metric; T.dkind = c->d1; T.quick = quick ? 1 : 0;
-    T.nbins = nb; T.autoc = f2 ? 0 : 1; T.nqf = nq;
-    T.minsep = c->minsep; T.maxsep = c->maxsep; T.binsize = c->binsize; T.b = c->b; T.a = c->a;
-    T.logminsep = std::log(c->minsep); T.halfminsep = 0.5 * c->minsep;
-    T.minsepsq = c->minsep * c->minsep; T.maxsepsq = c->maxsep * c->maxsep;
-    T.bsq = c->b * c->b; T.asq = c->a * c->a;
-    T.fminsep = (float)T.minsep; T.fmaxsep = (float)T.maxsep; T.fbinsize = (float)T.binsize;
-    T.fb = (float)T.b; T.fminsepsq = (float)T.minsepsq; T.fmaxsepsq = (float)T.maxsepsq;
-    T.fbsq = (float)T.bsq; T.fasq = (float)std::min(T.asq, 1e30);
-    T.fbb = (float)(0.25 * sqr(T.binsize + T.b));
-    T.fmineff = (float)std::min(T.bsq, T.asq);
-    T.finvminsepsq = (float)(1. / T.minsepsq);
-    T.finvbinsize = (float)(1. / T.binsize);
-    T.flogminsep = (float)T.logminsep;
+    trav_setup(c, T, f1->coords, metric, quick, nq);
+    T.autoc = f2 ? 0 : 1;
     tc_field* g = f2 ? f2 : f1;
     T.c1 = f1->tcells; T.c2 = g->tcells;
     T.x1 = f1->cells.x; T.y1 = f1->cells.y; T.z1 = f1->cells.z;
@@ -482,63 +614,12 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
     TC_CU(cudaEventCreate(&e0));
     TC_CU(cudaEventCreate(&e1));
     TC_CU(cudaEventRecord(e0, st));
-    // The schedule lives on the device: batches of (schedule, expand) launches run without
-    // host round trips; the host only adds level buffers when the expansion gets deeper.
-    // Chunk size: up to 4M items per launch, less for small catalogs (level buffers hold
-    // 4 chunks each).
-    long long CH = 1LL << 16;
-    while (CH < (1LL << 22) && CH < 2 * (f1->n + (f2 ? f2->n : 0))) CH <<= 1;
-    if (!c->sched) TC_TRY(dalloc(&c->sched, 1));
-    ExpandSched hs;
-    std::memset(&hs, 0, sizeof(hs));
-    hs.cnt[0] = T.ngen;
-    hs.cap = 4 * CH;
-    hs.chunk_max = CH;
-    hs.out_level = -1;
-    int nlev = 32;
-    for (int l = 1; l < nlev; ++l) {
-        TC_TRY(level_reserve(c, l, 0, hs.cap, st));
-        hs.lev[l] = c->lev[l];
-    }
-    hs.nlev = nlev;
-    TC_CU(cudaMemcpyAsync(c->sched, &hs, sizeof(hs), cudaMemcpyHostToDevice, st));
     int derr = 0;
     long long launches = 0;
-    for (int batch = 0;; ++batch) {
-        TC_TRY(launch_expand_batch(T, blocks, c->sched, 64, st));
-        int flags[3];
-        TC_CU(cudaMemcpyAsync(flags, &c->sched->done, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
-        TC_CU(cudaMemcpyAsync(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
-        TC_CU(cudaStreamSynchronize(st));
-        if (derr) break;
-        if (flags[1]) {   // need_levels: the expansion reached the last allocated level
-            if (nlev >= EXP_MAXLEV) {
-                set_last_error("the dual-tree expansion is deeper than 512 levels");
-                cudaEventDestroy(e0); cudaEventDestroy(e1);
-                return TC_ERR_DEVICE;
-            }
-            int nl2 = std::min(EXP_MAXLEV, 2 * nlev);
-            for (int l = nlev; l < nl2; ++l) {
-                TC_TRY(level_reserve(c, l, 0, hs.cap, st));
-                hs.lev[l] = c->lev[l];
-            }
-            TC_CU(cudaMemcpyAsync(&c->sched->lev[nlev], &hs.lev[nlev],
-                                  sizeof(int2*) * (nl2 - nlev), cudaMemcpyHostToDevice, st));
-            const int zero = 0;
-            TC_CU(cudaMemcpyAsync(&c->sched->nlev, &nl2, sizeof(int), cudaMemcpyHostToDevice, st));
-            TC_CU(cudaMemcpyAsync(&c->sched->need_levels, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
-            nlev = nl2;
-            continue;
-        }
-        if (flags[0]) break;
-        if (batch > 1000000) {
-            set_last_error("traversal did not finish within 10^6 batches");
-            cudaEventDestroy(e0); cudaEventDestroy(e1);
-            return TC_ERR_DEVICE;
-        }
+    {
+        const int rc = expand_run(c, T, blocks, f1->n + (f2 ? f2->n : 0), st, &derr, &launches);
+        if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
     }
-    TC_CU(cudaMemcpyAsync(&launches, &c->sched->launches, sizeof(long long), cudaMemcpyDeviceToHost, st));
-    TC_CU(cudaStreamSynchronize(st));
     const long long launches_done = launches;
     if (derr) {
         set_last_error(std::string("device error: ") + dev_err_msg(derr));
@@ -937,6 +1018,278 @@ void tc_corr2_free(tc_corr2* c)
     dfree(c->sched);
     dfree(c->mlp); dfree(c->samples);
     delete c;
+}
+
+// ---- GenerateXYZ (src/KMeans.cpp:1013-1050) ------------------------------------------
+namespace {
+__global__ void k_generate_xyz(double* x, double* y, double* z, const double* ra,
+                               const double* dec, const double* r, long long n)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double sr, cr, sd, cd;
+    sincos(ra[i], &sr, &cr);
+    sincos(dec[i], &sd, &cd);
+    double xi = cd * cr, yi = cd * sr, zi = sd;
+    if (r) { const double ri = r[i]; xi *= ri; yi *= ri; zi *= ri; }
+    x[i] = xi; y[i] = yi; z[i] = zi;
+}
+}  // namespace
+
+int tc_generate_xyz_device(double* x, double* y, double* z, const double* ra, const double* dec,
+                           const double* r, int64_t n)
+{
+    if (n < 0 || (n > 0 && (!x || !y || !z || !ra || !dec))) { set_last_error("NULL argument"); return TC_ERR_ARG; }
+    if (n == 0) return TC_OK;
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    count_launch();
+    k_generate_xyz<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(x, y, z, ra, dec, r, n);
+    TC_CU(cudaGetLastError());
+    TC_CU(cudaStreamSynchronize(st));
+    return TC_OK;
+}
+
+int tc_generate_xyz(double* x, double* y, double* z, const double* ra, const double* dec,
+                    const double* r, int64_t n)
+{
+    if (n < 0 || (n > 0 && (!x || !y || !z || !ra || !dec))) { set_last_error("NULL argument"); return TC_ERR_ARG; }
+    if (n == 0) return TC_OK;
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    double* d = nullptr;
+    const int nin = r ? 3 : 2;
+    TC_TRY(dalloc(&d, (size_t)n * (3 + nin)));
+    double *dx = d, *dy = d + n, *dz = d + 2 * n, *dra = d + 3 * n, *ddec = d + 4 * n;
+    double* dr = r ? d + 5 * n : nullptr;
+    int rc = TC_OK;
+    if (cudaMemcpyAsync(dra, ra, sizeof(double) * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(ddec, dec, sizeof(double) * n, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        (r && cudaMemcpyAsync(dr, r, sizeof(double) * n, cudaMemcpyHostToDevice, st) != cudaSuccess)) {
+        set_last_error("host to device copy failed"); rc = TC_ERR_CUDA;
+    }
+    if (rc == TC_OK) rc = tc_generate_xyz_device(dx, dy, dz, dra, ddec, dr, n);
+    if (rc == TC_OK &&
+        (cudaMemcpyAsync(x, dx, sizeof(double) * n, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+         cudaMemcpyAsync(y, dy, sizeof(double) * n, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+         cudaMemcpyAsync(z, dz, sizeof(double) * n, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+         cudaStreamSynchronize(st) != cudaSuccess)) {
+        set_last_error("device to host copy failed"); rc = TC_ERR_CUDA;
+    }
+    dfree(d);
+    return rc;
+}
+
+// ---- Patches ----------------------------------------------------------------------------
+// All patch-pair correlations of one set of patch fields in one expansion (the per-pair
+// loop of corr2base.py:929-950 / _process_all_auto): pairs (i, j), i <= j, whose fields
+// can overlap; each gets its own arrays.
+int tc_corr2_process_patches(tc_corr2* c, tc_field* const* fields, int npatch, int metric,
+                             int quick, int max_pairs, int32_t* pair_i, int32_t* pair_j,
+                             double* results, int* npairs_out)
+{
+    if (!c || !fields || npatch < 1 || !pair_i || !pair_j || !results || !npairs_out) {
+        set_last_error("NULL argument"); return TC_ERR_ARG;
+    }
+    *npairs_out = 0;
+    c->stats = tc_stats();
+    const int coords = fields[0]->coords;
+    for (int i = 0; i < npatch; ++i) {
+        if (!fields[i] || fields[i]->dkind != c->d1 || fields[i]->coords != coords) {
+            set_last_error("patch fields must exist and match the corr's data kind and coords");
+            return TC_ERR_ARG;
+        }
+    }
+    TC_TRY(check_metric(coords, metric));
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    long long npoints = 0;
+    for (int i = 0; i < npatch; ++i) {
+        if (fields[i]->n == 0) continue;
+        TC_TRY(field_build(fields[i]));
+        npoints += fields[i]->n;
+        c->stats.build_ms += fields[i]->build_ms;
+    }
+    // The pairs, as the reference chooses them (triviallyZero, src/Corr2.cpp:1107-1128).
+    const double minsepsq = c->minsep * c->minsep, maxsepsq = c->maxsep * c->maxsep;
+    std::vector<int> P1, P2;
+    std::vector<int> pidx((size_t)npatch * npatch, -1);
+    for (int i = 0; i < npatch; ++i) {
+        if (fields[i]->n == 0) continue;
+        for (int j = i; j < npatch; ++j) {
+            if (fields[j]->n == 0) continue;
+            if (i != j) {
+                const double rsq = host_dist_sq(coords, metric, fields[i]->center, fields[j]->center);
+                const double s = std::sqrt(fields[i]->center[3]) + std::sqrt(fields[j]->center[3]);
+                if ((rsq < minsepsq && s < c->minsep && rsq < sqr(c->minsep - s)) ||
+                    (rsq >= maxsepsq && rsq >= sqr(c->maxsep + s)))
+                    continue;
+            }
+            pidx[(size_t)i * npatch + j] = pidx[(size_t)j * npatch + i] = (int)P1.size();
+            P1.push_back(i); P2.push_back(j);
+        }
+    }
+    const int npair = (int)P1.size();
+    if (npair > max_pairs) { set_last_error("more patch pairs than max_pairs"); return TC_ERR_ARG; }
+    const int nb = c->nbins;
+    const int nq = c->d1 == TC_GDATA ? 7 : (c->d1 == TC_KDATA ? 4 : 3);
+    for (int p = 0; p < npair; ++p) { pair_i[p] = P1[p]; pair_j[p] = P2[p]; }
+    std::fill(results, results + (size_t)npair * 8 * nb, 0.);
+    *npairs_out = npair;
+    if (npair == 0) return TC_OK;
+    // Combined cells and roots.
+    std::vector<long long> base(npatch, 0);
+    long long ncells = 0;
+    for (int i = 0; i < npatch; ++i) { base[i] = ncells; if (fields[i]->n) ncells += 2 * fields[i]->n - 1; }
+    TCell* tc = nullptr;
+    double* xyz = nullptr;
+    int2* roots = nullptr;
+    int* d_pidx = nullptr;
+    double* pacc = nullptr;
+    unsigned long long* pnp = nullptr;
+    int rc = TC_OK;
+    std::vector<int2> hroots;
+    for (int p = 0; p < npair; ++p) {
+        const int i = P1[p], j = P2[p];
+        const auto& ti = fields[i]->tops;
+        const auto& tj = fields[j]->tops;
+        if (i == j) {
+            for (size_t a = 0; a < ti.size(); ++a) {
+                hroots.push_back(make_int2((int)(ti[a] + base[i]), -1));
+                for (size_t b = a + 1; b < ti.size(); ++b)
+                    hroots.push_back(make_int2((int)(ti[a] + base[i]), (int)(ti[b] + base[i])));
+            }
+        } else {
+            for (int a : ti)
+                for (int b : tj) hroots.push_back(make_int2((int)(a + base[i]), (int)(b + base[j])));
+        }
+    }
+    do {
+        if (ncells > 2147483647LL) { set_last_error("too many cells for one patch expansion"); rc = TC_ERR_ARG; break; }
+        if ((rc = dalloc(&tc, (size_t)ncells))) break;
+        if ((rc = dalloc(&xyz, (size_t)ncells * 3))) break;
+        if ((rc = dalloc(&roots, hroots.size()))) break;
+        if ((rc = dalloc(&d_pidx, pidx.size()))) break;
+        if ((rc = dalloc(&pacc, (size_t)npair * nq * nb))) break;
+        if ((rc = dalloc(&pnp, (size_t)npair * nb))) break;
+        for (int i = 0; i < npatch && !rc; ++i) {
+            const long long n = fields[i]->n ? 2 * fields[i]->n - 1 : 0;
+            if (!n) continue;
+            if (cudaMemcpyAsync(tc + base[i], fields[i]->tcells, sizeof(TCell) * n, cudaMemcpyDeviceToDevice, st) ||
+                cudaMemcpyAsync(xyz + base[i], fields[i]->cells.x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st) ||
+                cudaMemcpyAsync(xyz + ncells + base[i], fields[i]->cells.y, sizeof(double) * n, cudaMemcpyDeviceToDevice, st) ||
+                cudaMemcpyAsync(xyz + 2 * ncells + base[i], fields[i]->cells.z, sizeof(double) * n, cudaMemcpyDeviceToDevice, st)) {
+                set_last_error("cell copy failed"); rc = TC_ERR_CUDA; break;
+            }
+            count_launch();
+            k_rebase_cells<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(tc + base[i], n, (int)base[i], i);
+        }
+        if (rc) break;
+        if (cudaMemcpyAsync(roots, hroots.data(), sizeof(int2) * hroots.size(), cudaMemcpyHostToDevice, st) ||
+            cudaMemcpyAsync(d_pidx, pidx.data(), sizeof(int) * pidx.size(), cudaMemcpyHostToDevice, st) ||
+            cudaMemsetAsync(pacc, 0, sizeof(double) * (size_t)npair * nq * nb, st) ||
+            cudaMemsetAsync(pnp, 0, sizeof(unsigned long long) * (size_t)npair * nb, st)) {
+            set_last_error("patch setup copy failed"); rc = TC_ERR_CUDA; break;
+        }
+        TravParams T;
+        trav_setup(c, T, coords, metric, quick, nq);
+        T.c1 = tc; T.c2 = tc;
+        T.x1 = xyz; T.y1 = xyz + ncells; T.z1 = xyz + 2 * ncells;
+        T.x2 = T.x1; T.y2 = T.y1; T.z2 = T.z1;
+        T.ngen = 0; T.in_tasks = roots; T.nin = (long long)hroots.size();
+        T.mode = 3; T.npatch = npatch; T.pair_index = d_pidx; T.pacc = pacc; T.pnp = pnp;
+        int blocks = 0, nwarps = 0;
+        if ((rc = expand_grid(nq, nb, &blocks, &nwarps, 3))) break;
+        if ((rc = expand_scratch(c, nwarps, nq))) break;
+        T.nwarps = nwarps; T.err = c->d_err; T.counters = c->ctl + 2;
+        cudaMemsetAsync(c->ctl, 0, 8 * sizeof(unsigned long long), st);
+        cudaMemsetAsync(c->d_err, 0, sizeof(int), st);
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0); cudaEventCreate(&e1);
+        cudaEventRecord(e0, st);
+        int derr = 0;
+        long long launches = 0;
+        rc = expand_run(c, T, blocks, npoints, st, &derr, &launches);
+        cudaEventRecord(e1, st);
+        if (!rc && derr) { set_last_error(std::string("device error: ") + dev_err_msg(derr)); rc = TC_ERR_DEVICE; }
+        std::vector<double> hacc;
+        std::vector<unsigned long long> hnp;
+        unsigned long long cntr[4] = {0, 0, 0, 0};
+        if (!rc) {
+            hacc.resize((size_t)npair * nq * nb);
+            hnp.resize((size_t)npair * nb);
+            if (cudaMemcpyAsync(hacc.data(), pacc, sizeof(double) * hacc.size(), cudaMemcpyDeviceToHost, st) ||
+                cudaMemcpyAsync(hnp.data(), pnp, sizeof(unsigned long long) * hnp.size(), cudaMemcpyDeviceToHost, st) ||
+                cudaMemcpyAsync(cntr, c->ctl + 2, sizeof(cntr), cudaMemcpyDeviceToHost, st) ||
+                cudaStreamSynchronize(st)) { set_last_error("result copy failed"); rc = TC_ERR_CUDA; }
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0); cudaEventDestroy(e1);
+        if (rc) break;
+        // results[p] = weight, meanr, meanlogr, xi0..xi3, npairs (each nb doubles).
+        for (int p = 0; p < npair; ++p) {
+            double* r = results + (size_t)p * 8 * nb;
+            const double* a = hacc.data() + (size_t)p * nq * nb;
+            for (int k = 0; k < nb; ++k) {
+                r[k] = a[k];
+                if (!quick) { r[nb + k] = a[nb + k]; r[2 * nb + k] = a[2 * nb + k]; }
+                for (int q = 3; q < nq; ++q) r[q * nb + k] = a[q * nb + k];
+                if (!quick) r[7 * nb + k] = (double)hnp[(size_t)p * nb + k];
+            }
+        }
+        c->stats.cell_pairs = (int64_t)cntr[0];
+        c->stats.accepted = (int64_t)cntr[1];
+        c->stats.escalated = (int64_t)cntr[2];
+        c->stats.launches = launches;
+        c->stats.traverse_ms = ms;
+    } while (0);
+    dfree(tc); dfree(xyz); dfree(roots); dfree(d_pidx); dfree(pacc); dfree(pnp);
+    return rc;
+}
+
+// Jackknife data vectors and covariance on the device (see k_jackknife_rows).
+int tc_jackknife_cov(const double* results, const int32_t* pair_i, const int32_t* pair_j,
+                     int npair, int npatch, int nbins, int dkind, int cross_patch_weight,
+                     double* v_out, double* cov_out)
+{
+    if (!results || !pair_i || !pair_j || !v_out || !cov_out || npair < 1 || npatch < 2 || nbins < 1) {
+        set_last_error("bad argument"); return TC_ERR_ARG;
+    }
+    if (dkind != TC_GDATA && dkind != TC_KDATA) { set_last_error("jackknife rows for GG and KK only"); return TC_ERR_UNSUPPORTED; }
+    if (cross_patch_weight < 0 || cross_patch_weight > 2) { set_last_error("cross_patch_weight: 0 simple, 1 mean, 2 match"); return TC_ERR_ARG; }
+    const int nstat = dkind == TC_GDATA ? 2 : 1;
+    const int nv = nstat * nbins;
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    double *dres = nullptr, *dv = nullptr, *dw = nullptr, *dc = nullptr;
+    int* dpi = nullptr;
+    int rc = TC_OK;
+    do {
+        if ((rc = dalloc(&dres, (size_t)npair * 8 * nbins))) break;
+        if ((rc = dalloc(&dpi, (size_t)2 * npair))) break;
+        if ((rc = dalloc(&dv, (size_t)npatch * nv))) break;
+        if ((rc = dalloc(&dw, (size_t)npatch))) break;
+        if ((rc = dalloc(&dc, (size_t)nv * nv))) break;
+        if (cudaMemcpyAsync(dres, results, sizeof(double) * npair * 8 * nbins, cudaMemcpyHostToDevice, st) ||
+            cudaMemcpyAsync(dpi, pair_i, sizeof(int) * npair, cudaMemcpyHostToDevice, st) ||
+            cudaMemcpyAsync(dpi + npair, pair_j, sizeof(int) * npair, cudaMemcpyHostToDevice, st)) {
+            set_last_error("copy failed"); rc = TC_ERR_CUDA; break;
+        }
+        // 'match' weight, Mohammad and Percival (2022) eq. 27 as in corr2base.py:1812.
+        const double wmatch = 1. - (double)npatch / (2. + std::sqrt(2.) * (npatch - 1));
+        count_launch();
+        k_jackknife_rows<<<npatch, 128, 0, st>>>(dres, dpi, dpi + npair, npair, nbins,
+                                                 cross_patch_weight, wmatch, nstat, 0, 2, dv, dw);
+        count_launch();
+        k_jackknife_cov<<<dim3(nv, (nv + 127) / 128), 128, 0, st>>>(dv, npatch, nv, dc);
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaMemcpyAsync(v_out, dv, sizeof(double) * npatch * nv, cudaMemcpyDeviceToHost, st) ||
+            cudaMemcpyAsync(cov_out, dc, sizeof(double) * nv * nv, cudaMemcpyDeviceToHost, st) ||
+            cudaStreamSynchronize(st)) { set_last_error("jackknife kernels failed"); rc = TC_ERR_CUDA; }
+    } while (0);
+    dfree(dres); dfree(dpi); dfree(dv); dfree(dw); dfree(dc);
+    return rc;
 }
 
 int tc_mlp_nparam(void) { return MLP_NPARAM; }

@@ -731,6 +731,40 @@ __global__ void __launch_bounds__(TB) k_traverse(TravParams T)
 // appended to out.  The grid is fixed; warps stride over the input, so all lanes stay busy
 // and the launch is balanced.  Bins live in shared memory for the whole launch and are added
 // to the warp's global FP64 slot at the end (the slots persist across launches).
+// Patches: the warp's bins (all of one patch pair) go to that pair's FP64 sums.
+__device__ __forceinline__ void patch_flush(const TravParams& T, int pair, int nq, int nb,
+                                            float* fb, double* fd, unsigned long long* np,
+                                            int lane)
+{
+    __syncwarp();
+    flush_bins(nq * nb, fb, fd, lane);
+    __syncwarp();
+    if (pair >= 0) {
+        double* pa = T.pacc + (size_t)pair * nq * nb;
+        for (int q = lane; q < nq * nb; q += 32)
+            if (fd[q] != 0.) atomicAdd(&pa[q], fd[q]);
+        unsigned long long* pn = T.pnp + (size_t)pair * nb;
+        for (int q = lane; q < nb; q += 32) {
+            const unsigned long long v = (np[q] + np[nb + q]) + (np[2 * nb + q] + np[3 * nb + q]);
+            if (v) atomicAdd(&pn[q], v);
+        }
+    }
+    __syncwarp();
+    for (int q = lane; q < nq * nb; q += 32) fd[q] = 0.;
+    for (int q = lane; q < 4 * nb; q += 32) np[q] = 0ull;
+    for (int q = lane; q < 4 * nq * nb; q += 32) fb[q] = 0.f;
+    __syncwarp();
+}
+
+// Patches: a lane whose pair is not the warp's current one adds directly.
+__device__ __forceinline__ void patch_add(const TravParams& T, int pair, int k, int nq, int nb,
+                                          const float (&v)[7], unsigned long long nn)
+{
+    double* pa = T.pacc + (size_t)pair * nq * nb;
+    for (int q = 0; q < nq; ++q) atomicAdd(&pa[q * nb + k], (double)v[q]);
+    atomicAdd(&T.pnp[(size_t)pair * nb + k], nn);
+}
+
 __device__ void sched_step(ExpandSched* S);
 
 // The last warp of a scheduled launch to finish runs the schedule step for the next one.
@@ -749,8 +783,11 @@ __device__ __forceinline__ void expand_warp_done(const ExpandSched* S, int lane)
     }
 }
 
+#ifndef EXPAND_MINB
+#define EXPAND_MINB 6   // resident blocks per SM the register budget is sized for
+#endif
 template <int MODE>
-__global__ void __launch_bounds__(TB, 5) k_expand(TravParams T, const int2* in, long long n_in,
+__global__ void __launch_bounds__(TB, EXPAND_MINB) k_expand(TravParams T, const int2* in, long long n_in,
                                                long long gen0, int2* out,
                                                unsigned long long* nout, long long out_cap,
                                                const ExpandSched* S)
@@ -788,6 +825,7 @@ __global__ void __launch_bounds__(TB, 5) k_expand(TravParams T, const int2* in, 
     }
     __syncwarp();
     long long n_eval = 0, n_acc = 0, n_esc = 0, n_learn = 0;
+    int cur_pair = -1;   // mode 3: the patch pair the warp's bins hold
     const long long stride = (long long)gridDim.x * TB;
     int iter = 0;
     for (long long base = (long long)gw * 32; base < n_in; base += stride) {
@@ -815,6 +853,31 @@ __global__ void __launch_bounds__(TB, 5) k_expand(TravParams T, const int2* in, 
                 if (cand) {
                     if (y <= T.mlp_thr) { nch = 0; ++n_acc; ++n_learn; }
                     else acc_k = -1;
+                }
+            }
+        }
+        if constexpr (MODE == 3) {
+            // The warp's bins hold one patch pair.  When every accepted lane is of another
+            // pair, the bins move to it; lanes of a pair other than the current one (mixed
+            // iterations) add directly.
+            int pr = -1;
+            if (acc_k >= 0) {
+                const int p1 = __float_as_int(T.c1[task.x].d.y), p2 = __float_as_int(T.c2[task.y].d.y);
+                pr = T.pair_index[p1 * T.npatch + p2];
+            }
+            const unsigned am = __ballot_sync(0xffffffffu, acc_k >= 0);
+            if (am) {
+                const int p0 = __shfl_sync(0xffffffffu, pr, __ffs(am) - 1);
+                const bool same = __all_sync(0xffffffffu, acc_k < 0 || pr == p0);
+                if (cur_pair < 0) cur_pair = p0;
+                if (same && p0 != cur_pair) {
+                    patch_flush(T, cur_pair, nq, nb, fb, fd, np, lane);
+                    cur_pair = p0;
+                    iter = 0;
+                }
+                if (acc_k >= 0 && pr != cur_pair) {
+                    if (pr >= 0) patch_add(T, pr, acc_k, nq, nb, av, acc_nn);
+                    acc_k = -1;
                 }
             }
         }
@@ -852,6 +915,16 @@ __global__ void __launch_bounds__(TB, 5) k_expand(TravParams T, const int2* in, 
     }
     if (n_acc == 0) {   // nothing accumulated by this warp in this launch
         if (lane == 0 && n_eval) atomicAdd(&T.counters[0], (unsigned long long)n_eval);
+        expand_warp_done(S, lane);
+        return;
+    }
+    if constexpr (MODE == 3) {
+        patch_flush(T, cur_pair, nq, nb, fb, fd, np, lane);
+        if (lane == 0) {
+            atomicAdd(&T.counters[0], (unsigned long long)n_eval);
+            atomicAdd(&T.counters[1], (unsigned long long)n_acc);
+            atomicAdd(&T.counters[2], (unsigned long long)n_esc);
+        }
         expand_warp_done(S, lane);
         return;
     }
@@ -976,7 +1049,8 @@ int launch_expand_batch(const TravParams& T, int blocks, ExpandSched* dS, int it
     k_expand_sched<<<1, 1, 0, st>>>(dS);
     for (int it = 0; it < iters; ++it) {
         count_launch();
-        if (T.mode == 2) k_expand<2><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
+        if (T.mode == 3) k_expand<3><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
+        else if (T.mode == 2) k_expand<2><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
         else if (T.mode == 1) k_expand<1><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
         else k_expand<0><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
     }
@@ -990,7 +1064,10 @@ int expand_grid(int nq, int nb, int* blocks, int* nwarps, int mode)
     TC_CU(cudaGetDevice(&dev));
     TC_CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     const size_t sm = expand_smem_bytes(nq, nb, mode);
-    if (mode == 2) {
+    if (mode == 3) {
+        TC_TRY(set_expand_attr<3>(sm));
+        TC_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_expand<3>, TB, sm));
+    } else if (mode == 2) {
         TC_TRY(set_expand_attr<2>(sm));
         TC_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_expand<2>, TB, sm));
     } else if (mode == 1) {

@@ -51,6 +51,13 @@ struct TravParams {
     unsigned long long* nsamples;
     long long sample_cap;
     unsigned sample_mod;
+    // Patches (mode 3): one expansion over the cells of all patch fields, whose records
+    // carry their patch in d.y; an accepted pair adds into the FP64 sums of its patch pair
+    // (pacc: [pair][nqf][nbins], pnp: [pair][nbins]).
+    int npatch;
+    const int* pair_index;          // [npatch][npatch] -> pair id
+    double* pacc;
+    unsigned long long* pnp;
 };
 
 // Fixed traversal scratch of the allocation-free entry point (traverse2pt.cu).
