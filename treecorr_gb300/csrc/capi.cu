@@ -1143,32 +1143,38 @@ int tc_corr2_process_patches(tc_corr2* c, tc_field* const* fields, int npatch, i
     for (int i = 0; i < npatch; ++i) { base[i] = ncells; if (fields[i]->n) ncells += 2 * fields[i]->n - 1; }
     TCell* tc = nullptr;
     double* xyz = nullptr;
-    int2* roots = nullptr;
     int* d_pidx = nullptr;
     double* pacc = nullptr;
     unsigned long long* pnp = nullptr;
+    long long* d_roff = nullptr;
+    int2* d_pairs = nullptr;
+    int* d_top = nullptr;
+    int* d_topoff = nullptr;
     int rc = TC_OK;
-    std::vector<int2> hroots;
+    // Root tables: the top-level items are generated on the device from them.
+    std::vector<int> htop, htopoff(npatch + 1, 0);
+    for (int i = 0; i < npatch; ++i) {
+        htopoff[i] = (int)htop.size();
+        if (fields[i]->n)
+            for (int t : fields[i]->tops) htop.push_back((int)(t + base[i]));
+    }
+    htopoff[npatch] = (int)htop.size();
+    std::vector<long long> hroff(npair + 1, 0);
+    std::vector<int2> hpairs(npair);
     for (int p = 0; p < npair; ++p) {
-        const int i = P1[p], j = P2[p];
-        const auto& ti = fields[i]->tops;
-        const auto& tj = fields[j]->tops;
-        if (i == j) {
-            for (size_t a = 0; a < ti.size(); ++a) {
-                hroots.push_back(make_int2((int)(ti[a] + base[i]), -1));
-                for (size_t b = a + 1; b < ti.size(); ++b)
-                    hroots.push_back(make_int2((int)(ti[a] + base[i]), (int)(ti[b] + base[i])));
-            }
-        } else {
-            for (int a : ti)
-                for (int b : tj) hroots.push_back(make_int2((int)(a + base[i]), (int)(b + base[j])));
-        }
+        const long long ni = htopoff[P1[p] + 1] - htopoff[P1[p]];
+        const long long nj = htopoff[P2[p] + 1] - htopoff[P2[p]];
+        hroff[p + 1] = hroff[p] + (P1[p] == P2[p] ? ni * (ni + 1) / 2 : ni * nj);
+        hpairs[p] = make_int2(P1[p], P2[p]);
     }
     do {
         if (ncells > 2147483647LL) { set_last_error("too many cells for one patch expansion"); rc = TC_ERR_ARG; break; }
         if ((rc = dalloc(&tc, (size_t)ncells))) break;
         if ((rc = dalloc(&xyz, (size_t)ncells * 3))) break;
-        if ((rc = dalloc(&roots, hroots.size()))) break;
+        if ((rc = dalloc(&d_roff, hroff.size()))) break;
+        if ((rc = dalloc(&d_pairs, hpairs.size()))) break;
+        if ((rc = dalloc(&d_top, std::max<size_t>(htop.size(), 1)))) break;
+        if ((rc = dalloc(&d_topoff, htopoff.size()))) break;
         if ((rc = dalloc(&d_pidx, pidx.size()))) break;
         if ((rc = dalloc(&pacc, (size_t)npair * nq * nb))) break;
         if ((rc = dalloc(&pnp, (size_t)npair * nb))) break;
@@ -1185,7 +1191,10 @@ int tc_corr2_process_patches(tc_corr2* c, tc_field* const* fields, int npatch, i
             k_rebase_cells<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(tc + base[i], n, (int)base[i], i);
         }
         if (rc) break;
-        if (cudaMemcpyAsync(roots, hroots.data(), sizeof(int2) * hroots.size(), cudaMemcpyHostToDevice, st) ||
+        if (cudaMemcpyAsync(d_roff, hroff.data(), sizeof(long long) * hroff.size(), cudaMemcpyHostToDevice, st) ||
+            cudaMemcpyAsync(d_pairs, hpairs.data(), sizeof(int2) * hpairs.size(), cudaMemcpyHostToDevice, st) ||
+            cudaMemcpyAsync(d_top, htop.data(), sizeof(int) * htop.size(), cudaMemcpyHostToDevice, st) ||
+            cudaMemcpyAsync(d_topoff, htopoff.data(), sizeof(int) * htopoff.size(), cudaMemcpyHostToDevice, st) ||
             cudaMemcpyAsync(d_pidx, pidx.data(), sizeof(int) * pidx.size(), cudaMemcpyHostToDevice, st) ||
             cudaMemsetAsync(pacc, 0, sizeof(double) * (size_t)npair * nq * nb, st) ||
             cudaMemsetAsync(pnp, 0, sizeof(unsigned long long) * (size_t)npair * nb, st)) {
@@ -1196,8 +1205,10 @@ int tc_corr2_process_patches(tc_corr2* c, tc_field* const* fields, int npatch, i
         T.c1 = tc; T.c2 = tc;
         T.x1 = xyz; T.y1 = xyz + ncells; T.z1 = xyz + 2 * ncells;
         T.x2 = T.x1; T.y2 = T.y1; T.z2 = T.z1;
-        T.ngen = 0; T.in_tasks = roots; T.nin = (long long)hroots.size();
+        T.ngen = hroff[npair]; T.in_tasks = nullptr; T.nin = 0;
         T.mode = 3; T.npatch = npatch; T.pair_index = d_pidx; T.pacc = pacc; T.pnp = pnp;
+        T.npair = npair; T.proot_off = d_roff; T.ppairs = d_pairs; T.ptop = d_top;
+        T.ptop_off = d_topoff;
         int blocks = 0, nwarps = 0;
         if ((rc = expand_grid(nq, nb, &blocks, &nwarps, 3))) break;
         if ((rc = expand_scratch(c, nwarps, nq))) break;
@@ -1244,7 +1255,8 @@ int tc_corr2_process_patches(tc_corr2* c, tc_field* const* fields, int npatch, i
         c->stats.launches = launches;
         c->stats.traverse_ms = ms;
     } while (0);
-    dfree(tc); dfree(xyz); dfree(roots); dfree(d_pidx); dfree(pacc); dfree(pnp);
+    dfree(tc); dfree(xyz); dfree(d_pidx); dfree(pacc); dfree(pnp);
+    dfree(d_roff); dfree(d_pairs); dfree(d_top); dfree(d_topoff);
     return rc;
 }
 

@@ -311,8 +311,46 @@ __device__ void project3d64(const TravParams& T, int i, int j, float& g1r, float
 // ---------------------------------------------------------------------------------------
 // Root generation.
 
+// Row i of the upper triangle (self + pairs j > i) of n top cells starts at
+// i*n - i*(i-1)/2; item g of that enumeration.
+__device__ __forceinline__ void tri_index(long long n, long long g, long long& i, long long& j)
+{
+    double b = 2.0 * n + 1.0;
+    i = (long long)((b - sqrt(b * b - 8.0 * (double)g)) * 0.5);
+    if (i < 0) i = 0;
+    if (i > n - 1) i = n - 1;
+    while (i > 0 && i * n - i * (i - 1) / 2 > g) --i;
+    while (i + 1 < n && (i + 1) * n - (i + 1) * i / 2 <= g) ++i;
+    j = g - (i * n - i * (i - 1) / 2) + i;
+}
+
+// Patches: root g of all patch pairs (auto enumeration within a patch, all top pairs
+// across two patches).
+__device__ __forceinline__ int2 make_patch_root(const TravParams& T, long long g)
+{
+    int lo = 0, hi = T.npair;          // proot_off[lo] <= g < proot_off[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (T.proot_off[mid] <= g) lo = mid; else hi = mid;
+    }
+    const int2 pr = T.ppairs[lo];
+    const long long r = g - T.proot_off[lo];
+    const int* ti = T.ptop + T.ptop_off[pr.x];
+    if (pr.x == pr.y) {
+        const long long n = T.ptop_off[pr.x + 1] - T.ptop_off[pr.x];
+        long long i, j;
+        tri_index(n, r, i, j);
+        return j == i ? make_int2(ti[i], -1) : make_int2(ti[i], ti[j]);
+    }
+    const int* tj = T.ptop + T.ptop_off[pr.y];
+    const long long nj = T.ptop_off[pr.y + 1] - T.ptop_off[pr.y];
+    return make_int2(ti[r / nj], tj[r % nj]);
+}
+
+template <int MODE = 0>
 __device__ __forceinline__ int2 make_root(const TravParams& T, long long g)
 {
+    if constexpr (MODE == 3) return make_patch_root(T, g);
     if (g >= T.ngen) return T.in_tasks[g - T.ngen];
     if (T.autoc) {
         // Row i of the upper triangle (self + pairs j>i) starts at i*n - i*(i-1)/2.
@@ -832,7 +870,7 @@ __global__ void __launch_bounds__(TB, EXPAND_MINB) k_expand(TravParams T, const 
         const long long idx = base + lane;
         const bool has = idx < n_in;
         int2 task = make_int2(0, 0);
-        if (has) task = in ? in[idx] : make_root(T, gen0 + idx);
+        if (has) task = in ? in[idx] : make_root<MODE>(T, gen0 + idx);
         int nch = 0;
         int2 ch[4];
         int acc_k = -1;

@@ -58,6 +58,13 @@ struct TravParams {
     const int* pair_index;          // [npatch][npatch] -> pair id
     double* pacc;
     unsigned long long* pnp;
+    // Mode 3 roots, generated on the device: pair p's top-level items are roots
+    // proot_off[p] .. proot_off[p+1]-1; ptop[ptop_off[i] ..] are patch i's top cells.
+    int npair;
+    const long long* proot_off;
+    const int2* ppairs;
+    const int* ptop;
+    const int* ptop_off;
 };
 
 // Fixed traversal scratch of the allocation-free entry point (traverse2pt.cu).
