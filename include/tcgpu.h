@@ -236,6 +236,11 @@ int tc_generate_xyz(double* x, double* y, double* z, const double* ra, const dou
 int tc_generate_xyz_device(double* x, double* y, double* z, const double* ra,
                            const double* dec, const double* r, int64_t n);
 
+/* Self-check of the tcgen05 tensor-core path (no reference counterpart): one CTA computes
+ * c[128 x n] = a[128 x k] * b[n x k]^T in TF32 through TMEM (k in 8..64, multiple of 8;
+ * n in 16..64, multiple of 16).  Host arrays, row-major. */
+int tc_tcgen05_selftest(const float* a, const float* b, float* c, int n, int k);
+
 /* ---- Learned opening criterion (no reference counterpart) ----------------------------
  * A 5-64-64-1 ReLU network (FP32 master parameters, tc_mlp_nparam() floats: W1[64][5],
  * b1[64], W2[64][64], b2[64], w3[64], b3) revisits the cell pairs the bin_slop rule

@@ -93,6 +93,8 @@ def lib():
         L.tc_jackknife_cov.restype = ctypes.c_int
         L.tc_jackknife_cov.argtypes = [dp, i32p, i32p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_int, dp, dp]
+        L.tc_tcgen05_selftest.restype = ctypes.c_int
+        L.tc_tcgen05_selftest.argtypes = [ctypes.POINTER(ctypes.c_float)] * 3 + [ctypes.c_int] * 2
         L.tc_generate_xyz.restype = ctypes.c_int
         L.tc_generate_xyz.argtypes = [dp, dp, dp, dp, dp, dp, i64]
         L.tc_generate_xyz_device.restype = ctypes.c_int
@@ -393,6 +395,15 @@ def GenerateXYZ(x, y, z, ra, dec, r):
 
 def _fptr(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+def tcgen05_selftest(a, b):
+    """c = a @ b.T through the tcgen05 tensor cores (TF32, TMEM); a: 128 x k, b: n x k."""
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    b = np.ascontiguousarray(b, dtype=np.float32)
+    c = np.zeros((a.shape[0], b.shape[0]), dtype=np.float32)
+    _check(lib().tc_tcgen05_selftest(_fptr(a), _fptr(b), _fptr(c), b.shape[0], a.shape[1]))
+    return c
 
 
 def mlp_nparam():

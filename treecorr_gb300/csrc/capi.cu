@@ -1304,6 +1304,15 @@ int tc_jackknife_cov(const double* results, const int32_t* pair_i, const int32_t
     return rc;
 }
 
+int tc_tcgen05_selftest(const float* a, const float* b, float* c, int n, int k)
+{
+    if (!a || !b || !c) { set_last_error("NULL argument"); return TC_ERR_ARG; }
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    const int rc = tcgen05_selftest(a, b, c, n, k, st);
+    return rc == 0 ? TC_OK : (rc == 1 ? TC_ERR_ARG : (rc == 4 ? TC_ERR_DEVICE : TC_ERR_CUDA));
+}
+
 int tc_mlp_nparam(void) { return MLP_NPARAM; }
 
 int tc_corr2_set_learned(tc_corr2* c, const float* params, double threshold, double cand_factor)

@@ -66,6 +66,7 @@ void launch_prepare(int n, int coords, int dkind, const double* x, const double*
                     const double* z, const double* d1, const double* d2, const double* w,
                     const double* wpos, Points P, cudaStream_t st);
 int scratch_ensure_level(BuildScratch& S, int nt, int nc);
+int tcgen05_selftest(const float* A, const float* B, float* C, int N, int K, cudaStream_t st);
 void launch_validate_tree(int ncap, const Cells& C, const int* tops, int ntop, int* err,
                           cudaStream_t st);
 
