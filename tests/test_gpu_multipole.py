@@ -69,3 +69,20 @@ def test_multipole_record_waves(gpu_lib, monkeypatch):
     err = max_rel_err(small, {k: g["ref_" + k] for k in MP_OUT})
     for k, v in err.items():
         assert v <= TOL, f"{k}: {v:.3e}"
+
+
+@pytest.mark.parametrize("tensor", ["1", "0"])
+def test_multipole_contraction_paths(gpu_lib, monkeypatch, tensor):
+    """The tcgen05 contraction (3xTF32, TMEM accumulators) and the FP32 CUDA-core one both
+    reproduce the reference."""
+    from cases3 import spec3
+    monkeypatch.setenv("TCGPU_MP_TENSOR", tensor)
+    for name in ("ggg_flat_mp", "ggg_flat_mp_n20", "ggg_sphere_mp"):
+        s = spec3(name)
+        g = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+        cat = {k[3:]: g[k] for k in g.files if k.startswith("c1_")}
+        out = gpu_multipole(gpu_lib, s, cat, float(g["min_size"]), float(g["max_size"]))
+        assert np.array_equal(out["ntri"], g["ref_ntri"]), name
+        err = max_rel_err(out, {k: g["ref_" + k] for k in MP_OUT})
+        for k, v in err.items():
+            assert v <= TOL, f"{name} {k} tensor={tensor}: {v:.3e}"

@@ -35,6 +35,7 @@
 #include "tc_internal.cuh"
 #include "tc_host.hpp"
 #include "multipole.hpp"
+#include "tc_mma.cuh"
 
 namespace tc {
 
@@ -1339,6 +1340,178 @@ __global__ void __launch_bounds__(ZB) k_mp_zeta(ZParams Q)
     }
 }
 
+// Tensor-core contraction (tcgen05, nbins <= 32).  Same sums as k_mp_zeta, as two real
+// GEMMs per n over the vertex records (the K dimension):
+//   region 0: rows [Re A0, Im A0, Re A3, Im A3] x cols [Re B0, Im B0, Re B2, Im B2]
+//   region 1: rows [Re A1, Im A1, Re AW, Im AW] x cols [Re B1, Im B1, Re BW, Im BW]
+// (each 4 nbins long, rows padded to M = 128, cols to NC = a multiple of 16), whose blocks
+// combine into the complex gam0, gam3, gam2 (region 0) and gam1, weight (region 1).  The
+// row-range mask min(a, b) in [ks, mk) is {a, b >= ks} minus {a, b >= mk}: every record
+// enters as two K entries, the second with negated A and both masked at mk.  Operands are
+// split into TF32 hi + lo parts and multiplied as hi*hi + hi*lo + lo*hi (FP32-level
+// products); the FP32 accumulators in TMEM are drained to FP64 every TC_DRAIN chunks.
+static constexpr int TCB = 128;        // threads (4 warps = the 128 TMEM lanes)
+static constexpr int TC_REC = 16;      // records per chunk = 32 K entries = 4 K steps
+static constexpr int TC_DRAIN = 64;    // chunks between FP64 drains
+
+__device__ __forceinline__ void tf32_split(float x, float& hi, float& lo)
+{
+    hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+    lo = x - hi;
+}
+
+__global__ void __launch_bounds__(TCB) k_mp_zeta_tc(ZParams Q, int* status)
+{
+    extern __shared__ __align__(1024) unsigned char zts[];
+    __shared__ uint64_t mbar;
+    __shared__ uint32_t taddr_sh;
+    const int nb = Q.nbins, M = Q.maxn, nn = 2 * M + 1, gst = 2 * M + 3;
+    const int n = (int)blockIdx.x - M;
+    const int g = blockIdx.y;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int NC = (4 * nb + 15) & ~15;
+    const int aBytes = 4 * 4096, bBytes = 4 * NC * 32, rgBytes = aBytes + bBytes;
+    // Operand tiles: [region][hi, lo][A (4 K steps of 128 rows) | B (4 K steps of NC rows)].
+    auto tileA = [&](int r, int h, int st) { return zts + (r * 2 + h) * rgBytes + st * 4096; };
+    auto tileB = [&](int r, int h, int st) { return zts + (r * 2 + h) * rgBytes + aBytes + st * NC * 32; };
+    for (int q = tid; q < 4 * rgBytes / 16; q += TCB)
+        reinterpret_cast<float4*>(zts)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (tid == 0) mbar_init(&mbar, 1);
+    __syncthreads();
+    if (wid == 0) tmem_alloc(&taddr_sh, 256);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tm = taddr_sh;
+    const uint32_t idesc = umma_idesc_tf32(128, NC);
+    const int nw = n >= 0 ? n : -n;
+    const long long r0 = Q.nrec * g / Q.ngroups, r1 = Q.nrec * (g + 1) / Q.ngroups;
+    uint32_t phase = 0;
+    int nchunk = 0;
+    bool fresh = true;     // the next MMA overwrites the accumulators
+    bool failed = false;
+    float* S = reinterpret_cast<float*>(zts);   // drain buffer [128][2 NC], over the tiles
+    const size_t Zs = (size_t)Q.Z;
+    auto drain = [&]() {
+        __syncthreads();
+        for (int r = 0; r < 2; ++r)
+            for (int c0 = 0; c0 < NC; c0 += 8) {
+                float v[8];
+                tmem_ld8(tm + ((uint32_t)(32 * wid) << 16) + (uint32_t)(r * 128 + c0), v);
+#pragma unroll
+                for (int q = 0; q < 8; ++q) S[(32 * wid + lane) * (2 * NC) + r * NC + c0 + q] = v[q];
+            }
+        tc_fence_before();
+        __syncthreads();
+        double* part = Q.part + (size_t)g * 10 * Zs;
+        for (int e = tid; e < nb * nb; e += TCB) {
+            const int a = e / nb, b = e % nb;
+            auto C0 = [&](int row, int col) { return S[row * (2 * NC) + col]; };
+            auto C1 = [&](int row, int col) { return S[row * (2 * NC) + NC + col]; };
+            // (Re X + i Im X)(Re Y + i Im Y) from the four real blocks.
+            const float g0r = C0(a, b) - C0(nb + a, nb + b), g0i = C0(a, nb + b) + C0(nb + a, b);
+            const float g2r = C0(a, 2 * nb + b) - C0(nb + a, 3 * nb + b);
+            const float g2i = C0(a, 3 * nb + b) + C0(nb + a, 2 * nb + b);
+            const float g3r = C0(2 * nb + a, b) - C0(3 * nb + a, nb + b);
+            const float g3i = C0(2 * nb + a, nb + b) + C0(3 * nb + a, b);
+            const float g1r = C1(a, b) - C1(nb + a, nb + b), g1i = C1(a, nb + b) + C1(nb + a, b);
+            const float wr = C1(2 * nb + a, 2 * nb + b) - C1(3 * nb + a, 3 * nb + b);
+            const float wi = a == b ? 0.f : C1(2 * nb + a, 3 * nb + b) + C1(3 * nb + a, 2 * nb + b);
+            const size_t i = (size_t)(a * nb + b) * nn + M + n;
+            part[0 * Zs + i] += g0r; part[1 * Zs + i] += g0i;
+            part[2 * Zs + i] += g1r; part[3 * Zs + i] += g1i;
+            part[4 * Zs + i] += g2r; part[5 * Zs + i] += g2i;
+            part[6 * Zs + i] += g3r; part[7 * Zs + i] += g3i;
+            part[8 * Zs + i] += wr;  part[9 * Zs + i] += wi;
+        }
+        __syncthreads();
+        // The tile area was overwritten: restore the zero padding before the next fill.
+        for (int q = tid; q < 4 * rgBytes / 16; q += TCB)
+            reinterpret_cast<float4*>(zts)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        __syncthreads();
+        fresh = true;
+        nchunk = 0;
+    };
+    for (long long c0 = r0; c0 < r1 && !failed; c0 += TC_REC) {
+        const int nv = (int)min((long long)TC_REC, r1 - c0);
+        // Fill the K entries 2v (rows >= ks) and 2v+1 (rows >= mk, A negated) of the chunk.
+        for (int idx = tid; idx < TC_REC * nb; idx += TCB) {
+            const int v = idx / nb, a = idx % nb;
+            float A0r = 0.f, A0i = 0.f, A1r = 0.f, A1i = 0.f, A3r = 0.f, A3i = 0.f, AWr = 0.f, AWi = 0.f;
+            float B0r = 0.f, B0i = 0.f, B1r = 0.f, B1i = 0.f, B2r = 0.f, B2i = 0.f, BWr = 0.f, BWi = 0.f;
+            int ks = nb, mk = nb;
+            if (v < nv) {
+                const float* R = Q.rec + (size_t)(c0 + v) * Q.rec_floats;
+                const float2* RG = reinterpret_cast<const float2*>(R + 8);
+                const float2* RW = RG + (size_t)gst * nb;
+                const float w1 = R[3], wr = R[4], wi = R[5];
+                ks = __float_as_int(R[1]); mk = __float_as_int(R[2]);
+                const float2 gm1 = RG[(n + M) * nb + a], gmm1 = RG[(M - n) * nb + a];
+                const float2 gp1 = RG[(n + M + 2) * nb + a], gmp1 = RG[(M + 2 - n) * nb + a];
+                float2 w = RW[nw * nb + a];
+                if (n < 0) w.y = -w.y;
+                A0r = wr * gm1.x - wi * gm1.y;   A0i = wr * gm1.y + wi * gm1.x;
+                A1r = wr * gp1.x + wi * gp1.y;   A1i = wr * gp1.y - wi * gp1.x;
+                A3r = wr * gmp1.x + wi * gmp1.y; A3i = wi * gmp1.x - wr * gmp1.y;
+                AWr = w1 * w.x;                  AWi = w1 * w.y;
+                B0r = gmm1.x; B0i = gmm1.y; B1r = gmp1.x; B1i = gmp1.y;
+                B2r = gp1.x;  B2i = -gp1.y; BWr = w.x;    BWi = -w.y;
+            }
+#pragma unroll
+            for (int t = 0; t < 2; ++t) {
+                const int e = 2 * v + t, st = e >> 3, kk = e & 7;
+                const bool on = a >= (t == 0 ? ks : mk);
+                const float sg = on ? (t == 0 ? 1.f : -1.f) : 0.f, sb = on ? 1.f : 0.f;
+                const float av[2][4] = {{A0r, A0i, A3r, A3i}, {A1r, A1i, AWr, AWi}};
+                const float bv[2][4] = {{B0r, B0i, B2r, B2i}, {B1r, B1i, BWr, BWi}};
+#pragma unroll
+                for (int r = 0; r < 2; ++r)
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const int row = q * nb + a;
+                        float hi, lo;
+                        tf32_split(sg * av[r][q], hi, lo);
+                        *reinterpret_cast<float*>(tileA(r, 0, st) + umma_tile_off(row, kk)) = hi;
+                        *reinterpret_cast<float*>(tileA(r, 1, st) + umma_tile_off(row, kk)) = lo;
+                        tf32_split(sb * bv[r][q], hi, lo);
+                        *reinterpret_cast<float*>(tileB(r, 0, st) + umma_tile_off(row, kk)) = hi;
+                        *reinterpret_cast<float*>(tileB(r, 1, st) + umma_tile_off(row, kk)) = lo;
+                    }
+            }
+        }
+        fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            for (int r = 0; r < 2; ++r) {
+                const uint32_t d = tm + (uint32_t)(r * 128);
+                for (int st = 0; st < 4; ++st) {
+                    const uint64_t ah = umma_desc(smem_u32(tileA(r, 0, st)), 128, 256);
+                    const uint64_t al = umma_desc(smem_u32(tileA(r, 1, st)), 128, 256);
+                    const uint64_t bh = umma_desc(smem_u32(tileB(r, 0, st)), 128, 256);
+                    const uint64_t bl = umma_desc(smem_u32(tileB(r, 1, st)), 128, 256);
+                    umma_tf32(d, ah, bh, idesc, (fresh && st == 0) ? 0u : 1u);
+                    umma_tf32(d, ah, bl, idesc, 1u);
+                    umma_tf32(d, al, bh, idesc, 1u);
+                }
+            }
+            umma_commit(&mbar);
+        }
+        const bool ok = mbar_wait(&mbar, phase, 1 << 24);
+        phase ^= 1u;
+        tc_fence_after();
+        failed = __syncthreads_or(!ok) != 0;
+        fresh = false;
+        if (failed) break;
+        if (++nchunk == TC_DRAIN) drain();
+    }
+    if (!failed && !fresh) drain();
+    if (failed && tid == 0) atomicExch(status, 1);
+    tc_fence_before();
+    __syncthreads();
+    if (wid == 0) tmem_dealloc(tm, 256);
+}
+
 // The n = 0 scalar outputs of calculateZeta over vertex records (ntri, meand2/3,
 // meanlogd2/3): for every entry (a, b) whose min(a, b) lies in the record's rows,
 //   a != b: ntri += n1 np_a np_b, meand2 += w1 sumw_b sumwr_a, meand3 += w1 sumw_a sumwr_b
@@ -1495,6 +1668,14 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
     const size_t zsh = (size_t)chunk * nb * 64;
     TC_CU(cudaFuncSetAttribute(k_mp_zeta, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zsh));
     const int etiles = (nb * nb + ZE * ZB - 1) / (ZE * ZB);
+    // The tensor-core contraction (tcgen05) for nbins <= 32, unless TCGPU_MP_TENSOR=0.  Its
+    // shared memory keeps at most two blocks on an SM (each holds 256 TMEM columns).
+    bool use_tc = 4 * nb <= 128;
+    if (const char* ev = std::getenv("TCGPU_MP_TENSOR")) use_tc = use_tc && std::atoi(ev) != 0;
+    const int NCt = (4 * nb + 15) & ~15;
+    const size_t tcsm = std::max<size_t>((size_t)4 * (16384 + 128 * NCt), 100 * 1024);
+    if (use_tc)
+        TC_CU(cudaFuncSetAttribute(k_mp_zeta_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tcsm));
     const int ngroups = std::max(1, (4 * nsm + nn * etiles - 1) / (nn * etiles));
     // Scalar outputs: records per chunk and record groups.
     const int chunk2 = (int)std::max<long long>(1, std::min<long long>(64, (48 * 1024) / (32LL * nb)));
@@ -1580,6 +1761,7 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
             X.ngroups = ngroups; X.part_stride = 10 * Z;
         }
         if (!X.ctl) TC_TRY(dalloc(&X.ctl, 4));
+        if (!X.tcstatus) TC_TRY(dalloc(&X.tcstatus, 1));
         if (!X.err) TC_TRY(dalloc(&X.err, 2));
         if (!X.dbg) TC_TRY(dalloc(&X.dbg, 32));
         X.nblk = std::max(X.nblk, nblk);
@@ -1602,6 +1784,7 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
         P.err = X.err;
         P.dbg = X.dbg;
         TC_CU(cudaMemsetAsync(X.ctl, 0, 4 * sizeof(unsigned long long), st));
+        TC_CU(cudaMemsetAsync(X.tcstatus, 0, sizeof(int), st));
         X.overflow = 0; X.records = 0; X.waves = 0;
         TC_CU(cudaMemsetAsync(X.err, 0, 2 * sizeof(int), st));
         TC_CU(cudaMemsetAsync(X.out, 0, sizeof(double) * (size_t)P.out_stride * nblk, st));
@@ -1636,7 +1819,8 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
             Q.ngroups = ngroups; Q.part = X.part; Q.Z = Z;
             if (Q.nrec > 0) {
                 count_launch();
-                k_mp_zeta<<<dim3(nn, ngroups, etiles), ZB, zsh, st>>>(Q);
+                if (use_tc) k_mp_zeta_tc<<<dim3(nn, ngroups), TCB, tcsm, st>>>(Q, X.tcstatus);
+                else k_mp_zeta<<<dim3(nn, ngroups, etiles), ZB, zsh, st>>>(Q);
                 TC_CU(cudaGetLastError());
                 if (!P.quick) {
                     ZParams Q2 = Q;
@@ -1678,6 +1862,15 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
             set_last_error("multipole: device stack overflow (tree too deep)");
             return 4;
         }
+        {
+            int tcs = 0;
+            TC_CU(cudaMemcpyAsync(&tcs, X.tcstatus, sizeof(int), cudaMemcpyDeviceToHost, st));
+            TC_CU(cudaStreamSynchronize(st));
+            if (tcs) {
+                set_last_error("multipole: a tensor-core contraction did not complete in time");
+                return 4;
+            }
+        }
         count_launch();
         k_mp_reduce<<<(unsigned)((P.out_stride + 255) / 256), 256, 0, st>>>(
             nblk, P.out_stride, Z, nb, nn, X.out, X.diag, 9LL * nb, ngroups, X.part,
@@ -1697,7 +1890,7 @@ void free_mp_scratch(MPScratch& X)
     dfree(X.arena1); dfree(X.jobs); dfree(X.arena2); dfree(X.acc); dfree(X.perm);
     dfree(X.slots); dfree(X.out); dfree(X.diag); dfree(X.total); dfree(X.zrec); dfree(X.part);
     dfree(X.spart); dfree(X.ntp);
-    dfree(X.ctl); dfree(X.err); dfree(X.dbg);
+    dfree(X.ctl); dfree(X.err); dfree(X.dbg); dfree(X.tcstatus);
     X = MPScratch();
 }
 

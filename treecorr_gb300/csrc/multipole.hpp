@@ -105,6 +105,7 @@ struct MPScratch {
     unsigned long long* ctl = nullptr;
     int* err = nullptr;
     double* dbg = nullptr;
+    int* tcstatus = nullptr;    // set when a tensor-core contraction timed out
     // Requested minimum capacities, raised after an overflow.
     long long want_a1 = 0, want_jobs = 0, want_a2 = 0;
     int want_slots = 0;
