@@ -1432,23 +1432,55 @@ __global__ void __launch_bounds__(TCB) k_mp_zeta_tc(ZParams Q, int* status)
         fresh = true;
         nchunk = 0;
     };
+    // The chunk's record data is loaded into registers one chunk ahead, so the loads of
+    // chunk i+1 overlap the MMAs of chunk i.  A thread holds up to TC_IT fill items.
+    const int nab = (nb + 7) >> 3;
+    constexpr int TC_IT = 4;                 // nab * 8 * TC_REC / TCB <= 4 for nbins <= 32
+    float2 ig[TC_IT][5];
+    float4 ih[TC_IT];                        // w1, Re wg1, Im wg1, (ks, mk) packed
+    auto load_items = [&](long long cb) {
+        const int nvb = (int)min((long long)TC_REC, r1 - cb);
+#pragma unroll
+        for (int j = 0; j < TC_IT; ++j) {
+            const int idx = tid + j * TCB;
+            const int w = idx >> 5, l = idx & 31;
+            const int a = (w % nab) * 8 + (l & 7);
+            const int v = (w / nab) * 4 + (l >> 3);
+            ih[j] = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+            if (idx >= nab * 8 * TC_REC || a >= nb || v >= nvb) continue;
+            const float* R = Q.rec + (size_t)(cb + v) * Q.rec_floats;
+            const float2* RG = reinterpret_cast<const float2*>(R + 8);
+            const float2* RW = RG + (size_t)gst * nb;
+            ig[j][0] = RG[(n + M) * nb + a];       // G[n-1]
+            ig[j][1] = RG[(M - n) * nb + a];       // G[-n-1]
+            ig[j][2] = RG[(n + M + 2) * nb + a];   // G[n+1]
+            ig[j][3] = RG[(M + 2 - n) * nb + a];   // G[-n+1]
+            ig[j][4] = RW[nw * nb + a];            // W[|n|]
+            const int ks = __float_as_int(R[1]), mk = __float_as_int(R[2]);
+            ih[j] = make_float4(R[3], R[4], R[5], __int_as_float((ks << 8) | mk));
+        }
+    };
+    if (r0 < r1) load_items(r0);
     for (long long c0 = r0; c0 < r1 && !failed; c0 += TC_REC) {
-        const int nv = (int)min((long long)TC_REC, r1 - c0);
-        // Fill the K entries 2v (rows >= ks) and 2v+1 (rows >= mk, A negated) of the chunk.
-        for (int idx = tid; idx < TC_REC * nb; idx += TCB) {
-            const int v = idx / nb, a = idx % nb;
+        // Fill the K entries v (rows >= ks) and TC_REC + v (rows >= mk, A negated) of the
+        // chunk.  A warp covers 8 consecutive bins x 4 consecutive records: its stores hit
+        // the 8 rows x 4 k of core matrices, all 32 banks once.
+#pragma unroll
+        for (int j = 0; j < TC_IT; ++j) {
+            const int idx = tid + j * TCB;
+            const int w = idx >> 5, l = idx & 31;
+            const int a = (w % nab) * 8 + (l & 7);
+            const int v = (w / nab) * 4 + (l >> 3);
+            if (idx >= nab * 8 * TC_REC || a >= nb) continue;
             float A0r = 0.f, A0i = 0.f, A1r = 0.f, A1i = 0.f, A3r = 0.f, A3i = 0.f, AWr = 0.f, AWi = 0.f;
             float B0r = 0.f, B0i = 0.f, B1r = 0.f, B1i = 0.f, B2r = 0.f, B2i = 0.f, BWr = 0.f, BWi = 0.f;
             int ks = nb, mk = nb;
-            if (v < nv) {
-                const float* R = Q.rec + (size_t)(c0 + v) * Q.rec_floats;
-                const float2* RG = reinterpret_cast<const float2*>(R + 8);
-                const float2* RW = RG + (size_t)gst * nb;
-                const float w1 = R[3], wr = R[4], wi = R[5];
-                ks = __float_as_int(R[1]); mk = __float_as_int(R[2]);
-                const float2 gm1 = RG[(n + M) * nb + a], gmm1 = RG[(M - n) * nb + a];
-                const float2 gp1 = RG[(n + M + 2) * nb + a], gmp1 = RG[(M + 2 - n) * nb + a];
-                float2 w = RW[nw * nb + a];
+            const int km = __float_as_int(ih[j].w);
+            if (km >= 0) {
+                const float w1 = ih[j].x, wr = ih[j].y, wi = ih[j].z;
+                ks = km >> 8; mk = km & 255;
+                const float2 gm1 = ig[j][0], gmm1 = ig[j][1], gp1 = ig[j][2], gmp1 = ig[j][3];
+                float2 w = ig[j][4];
                 if (n < 0) w.y = -w.y;
                 A0r = wr * gm1.x - wi * gm1.y;   A0i = wr * gm1.y + wi * gm1.x;
                 A1r = wr * gp1.x + wi * gp1.y;   A1i = wr * gp1.y - wi * gp1.x;
@@ -1459,7 +1491,7 @@ __global__ void __launch_bounds__(TCB) k_mp_zeta_tc(ZParams Q, int* status)
             }
 #pragma unroll
             for (int t = 0; t < 2; ++t) {
-                const int e = 2 * v + t, st = e >> 3, kk = e & 7;
+                const int e = t * TC_REC + v, st = e >> 3, kk = e & 7;
                 const bool on = a >= (t == 0 ? ks : mk);
                 const float sg = on ? (t == 0 ? 1.f : -1.f) : 0.f, sb = on ? 1.f : 0.f;
                 const float av[2][4] = {{A0r, A0i, A3r, A3i}, {A1r, A1i, AWr, AWi}};
@@ -1497,6 +1529,7 @@ __global__ void __launch_bounds__(TCB) k_mp_zeta_tc(ZParams Q, int* status)
             }
             umma_commit(&mbar);
         }
+        if (c0 + TC_REC < r1) load_items(c0 + TC_REC);   // overlaps the MMAs
         const bool ok = mbar_wait(&mbar, phase, 1 << 24);
         phase ^= 1u;
         tc_fence_after();
