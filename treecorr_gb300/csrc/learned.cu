@@ -217,7 +217,7 @@ __global__ void k_learn_label(LabelParams L, const int2* pairs, long long npairs
     const float dz = flat ? 0.f : (A.a.z - B.a.z) + (A.b.z - B.b.z);
     const float dsq = dx * dx + dy * dy + dz * dz;
     float rsq = dsq;
-    if (arc) { const float th = 2.f * asinf(0.5f * sqrtf(dsq)); rsq = th * th; }
+    if (arc) { const float th = arc_from_chord_sq(dsq); rsq = th * th; }
     const float lr = 0.5f * logf(rsq * L.finvminsepsq);
     const int kc = (int)(lr * L.finvbinsize);
     const int n1 = __float_as_int(A.c.z), n2 = __float_as_int(B.c.z);

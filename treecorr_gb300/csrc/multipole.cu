@@ -979,7 +979,7 @@ __global__ void __launch_bounds__(MB, 2) k_mp_finish(MPParams P)
                         }
                         float rsqf = dsq;
                         if (P.metric == ARC) {
-                            const float th = 2.f * asinf(0.5f * sqrtf(dsq));
+                            const float th = arc_from_chord_sq(dsq);
                             rsqf = th * th;
                         }
                         int k32 = -1;

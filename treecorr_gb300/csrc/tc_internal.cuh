@@ -119,4 +119,18 @@ struct BuildScratch {
     int cap_tasks = 0, cap_chunks = 0;
 };
 
+
+// Great-circle angle from the squared chord of two unit vectors, theta = 2 asin(c/2), in
+// FP32.  For c < 0.25 the Maclaurin series of arcsin to x^7 (x = c/2 <= 0.125; the first
+// omitted term, 35 x^9 / 1152, is below 2e-9 of x) replaces the library call.
+__device__ __forceinline__ float arc_from_chord_sq(float dsq)
+{
+    const float c = sqrtf(dsq);
+    if (c < 0.25f) {
+        const float x = 0.5f * c, x2 = x * x;
+        return 2.f * x * (1.f + x2 * (1.f / 6.f + x2 * (3.f / 40.f + x2 * (5.f / 112.f))));
+    }
+    return 2.f * asinf(0.5f * c);
+}
+
 }  // namespace tc

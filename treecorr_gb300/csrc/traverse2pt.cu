@@ -533,7 +533,7 @@ __device__ __forceinline__ void eval_task(const TravParams& T, bool has, int2 ta
                 const float dsq = dx * dx + dy * dy + dz * dz;
                 float rsq = dsq, theta = 0.f;
                 if (arc) {
-                    theta = 2.f * asinf(0.5f * sqrtf(dsq));
+                    theta = arc_from_chord_sq(dsq);
                     rsq = theta * theta;
                 }
                 const float s1 = A.a.w, s2 = B.a.w;
