@@ -581,6 +581,87 @@ def run_patches(args, rank, world):
                        "jackknife_max_rel_diff": float(np.abs(cov - c0).max() / np.abs(c0).max())}}
 
 
+def run_kmeans(args, rank, world):
+    """k-means patches of the curved-sky catalog (150 patches, the jackknife configuration):
+    the N field k-means builds (min_size 0, max_size inf, min_top 4, max_top 7 =
+    bit_length(150) - 1), KMeansInitTree, KMeansRun for a fixed number of iterations
+    (tol 0, so both sides iterate alike) and KMeansAssign.  Metric: point-iterations of
+    KMeansRun per second."""
+    import torch
+    from treecorr_gb300 import _treecorr as T
+    dev = torch.device("cuda", rank % max(torch.cuda.device_count(), 1))
+    torch.cuda.set_device(dev)
+    cat = curved_sky_catalog(args.n, seed=args.seed + rank)
+    npatch, iters = 150, 20
+    e = np.array([])
+    f = T.NFieldSphere(cat["x"], cat["y"], cat["z"], cat["w"], e, 0.0, np.inf, T.Mean, 0, False,
+                       4, 7)
+    t0 = time.perf_counter()
+    f.getNTopLevel()
+    build_s = time.perf_counter() - t0
+    c0 = np.zeros((npatch, 3))
+    t0 = time.perf_counter()
+    f.KMeansInitTree(c0, npatch, 1234)
+    init_s = time.perf_counter() - t0
+    c = c0.copy()
+    f.KMeansRun(c, npatch, 2, 0.0, False)          # warm-up
+    launches0 = T.launch_count()
+    ts = []
+    with ClockSampler(dev.index) as clk:
+        for _ in range(args.steps):
+            c = c0.copy()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            f.KMeansRun(c, npatch, iters, 0.0, False)
+            ts.append(time.perf_counter() - t0)
+    launches = T.launch_count() - launches0
+    pat = np.zeros(args.n, dtype=np.int64)
+    t0 = time.perf_counter()
+    f.KMeansAssign(c, npatch, pat)
+    assign_s = time.perf_counter() - t0
+    q = np.zeros(args.n, dtype=np.int64)
+    t0 = time.perf_counter()
+    T.QuickAssign(c, npatch, cat["x"], cat["y"], cat["z"], q)
+    quick_s = time.perf_counter() - t0
+    t_run = float(np.median(ts))
+    value = world * args.n * iters / t_run
+    unit = "point-iterations/s"
+    line = {"metric": "k-means KMeansRun point-iterations/s at N=10M, 150 patches (curved sky)",
+            "value": value, "unit": unit, "n_gpus": world, "steps": args.steps, "warmup": 1,
+            "ms_per_step": 1e3 * t_run, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded curved-sky catalog)",
+            "config": {"workload": f"k-means, {args.n}-point 1000 deg^2 cap, {npatch} patches, "
+                                   f"{iters} iterations (tol 0), init tree",
+                       "field": "NFieldSphere min_size 0, max_size inf, min_top 4, max_top 7"},
+            "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 24 * npatch,
+                    "d2h_bytes_per_step": 24 * npatch},
+            "gpu_launches": launches // max(args.steps, 1), "clocks": clk.summary(),
+            "detail": {"build_s": build_s, "init_tree_s": init_s, "assign_s": assign_s,
+                       "quick_assign_s": quick_s, "assign_equals_quick": bool(np.array_equal(pat, q)),
+                       "patch_counts_min_max": [int(np.bincount(pat, minlength=npatch).min()),
+                                                int(np.bincount(pat, minlength=npatch).max())]}}
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import oracle as O
+        of = O.OracleField("N", "spherical", cat["x"], cat["y"], cat["z"], w=cat["w"],
+                           min_size=0.0, max_size=np.inf, split_method="mean", min_top=4,
+                           max_top=7)
+        t0 = time.perf_counter()
+        of.ntop()
+        ob = time.perf_counter() - t0
+        it_cpu = 2
+        t0 = time.perf_counter()
+        oc, _ = of.kmeans_run(c0, it_cpu, 0.0, False)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": args.n * it_cpu / dt, "unit": unit, "cores": 1,
+                                "kind": "port",
+                                "sample": f"{it_cpu} iterations of the same run ({dt:.1f} s; "
+                                          f"tree build {ob:.1f} s excluded)"}
+        c2 = c0.copy()
+        f.KMeansRun(c2, npatch, it_cpu, 0.0, False)
+        line["detail"]["max_center_diff_vs_port_2it"] = float(np.abs(c2 - oc).max())
+    return line
+
+
 def cpu_sample(cat, bins, args, budget_s=15.0):
     """The oracle port of the reference algorithm on the host cores, over top-level rows of
     the auto loop until about budget_s seconds of traversal have been timed."""
@@ -690,10 +771,12 @@ def main():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    p.add_argument("--workload", default="gg", choices=["gg", "ggg", "learned", "patches"],
+    p.add_argument("--workload", default="gg",
+                   choices=["gg", "ggg", "learned", "patches", "kmeans"],
                    help="gg: the 2-point headline; ggg: the multipole 3-point configuration; "
                         "learned: the learned opening criterion against the plain rule; "
-                        "patches: 150 patches, all pairs in one expansion + jackknife")
+                        "patches: 150 patches, all pairs in one expansion + jackknife; "
+                        "kmeans: k-means patches of the curved-sky catalog")
     p.add_argument("--learned-threshold", type=float, default=-3.0)
     p.add_argument("--n", type=int, default=10_000_000)
     p.add_argument("--bin-slop", type=float, default=0.1)
@@ -712,6 +795,8 @@ def main():
         line = run_learned(args, rank, world)
     elif args.workload == "patches":
         line = run_patches(args, rank, world)
+    elif args.workload == "kmeans":
+        line = run_kmeans(args, rank, world)
     else:
         line = run_gpu(args, rank, world)
     if rank == 0 and line is not None:

@@ -125,6 +125,37 @@ int tc_field_center(const tc_field* f, double* xyz3);
 int64_t tc_field_dump(tc_field* f, double* xyz, float* size_w_d, int64_t* n_start,
                       int32_t* depth, int64_t cap);
 
+/* k-means patches on the field's tree: the BaseField methods bound at
+ * src/Field.cpp:630-634 (implemented in src/KMeans.cpp:743-849).  centers holds npatch
+ * rows of 2 (Flat) or 3 (ThreeD, Sphere; unit vectors) doubles in host memory.  The
+ * initialisations draw from the C library's rand() stream like the reference's urand()
+ * (a non-zero seed reseeds it).  npatch is limited to 5000 on the GPU path. */
+int tc_kmeans_init_tree(tc_field* f, double* centers, int npatch, int64_t seed);   /* KMeansInitTree */
+int tc_kmeans_init_rand(tc_field* f, double* centers, int npatch, int64_t seed);   /* KMeansInitRand */
+int tc_kmeans_init_kmpp(tc_field* f, double* centers, int npatch, int64_t seed);   /* KMeansInitKMPP */
+/* KMeansRun (src/KMeans.cpp:773-833): refines centers in place. */
+int tc_kmeans_run(tc_field* f, double* centers, int npatch, int max_iter, double tol, int alt);
+/* KMeansAssign (src/KMeans.cpp:835-849): patches[i] for every point i of the field
+ * (n must equal tc_field_nobj). */
+int tc_kmeans_assign(tc_field* f, const double* centers, int npatch, int64_t* patches,
+                     int64_t n);
+/* Iterations run by the last tc_kmeans_run on this field (no reference counterpart). */
+int tc_kmeans_iterations(const tc_field* f);
+
+/* QuickAssign (src/KMeans.cpp:890-942, bound at src/Field.cpp:700): the nearest centre of
+ * every point; z == NULL selects the 2-d form (centers npatch x 2). */
+int tc_quick_assign(const double* centers, int npatch, const double* x, const double* y,
+                    const double* z, int64_t n, int64_t* patches);
+/* SelectPatch (src/KMeans.cpp:944-1011, bound at src/Field.cpp:701): use[i] = 1 when patch
+ * is the nearest centre of point i (no other centre strictly closer), else 0. */
+int tc_select_patch(int patch, const double* centers, int npatch, const double* x,
+                    const double* y, const double* z, int64_t n, int64_t* use);
+/* The same two with device pointers for x, y, z and the output (no host copies). */
+int tc_quick_assign_device(const double* centers, int npatch, const double* x,
+                           const double* y, const double* z, int64_t n, int64_t* patches);
+int tc_select_patch_device(int patch, const double* centers, int npatch, const double* x,
+                           const double* y, const double* z, int64_t n, int64_t* use);
+
 /* Corr construction: replaces BuildCorr2 (src/Corr2.cpp:842-864) for the NN, KK and GG
  * classes (pybind11 at src/Corr2.cpp:1177-1199).  d1, d2: TC_NDATA/TC_KDATA/TC_GDATA with
  * d1 == d2.  xi0..xi3 may be NULL when unused (NN: all; KK: xi1..xi3).  Only

@@ -70,6 +70,18 @@ def lib():
         L.orc_last_accepted.restype = ctypes.c_longlong
         L.orc_last_accepted.argtypes = []
         L.orc_max_threads.restype = ctypes.c_int
+        lp = ctypes.POINTER(ctypes.c_long)
+        for nm in ("orc_kmeans_init_tree", "orc_kmeans_init_rand", "orc_kmeans_init_kmpp"):
+            getattr(L, nm).restype = ctypes.c_int
+            getattr(L, nm).argtypes = [ctypes.c_void_p, dp, ctypes.c_int, ctypes.c_longlong]
+        L.orc_kmeans_run.restype = ctypes.c_int
+        L.orc_kmeans_run.argtypes = [ctypes.c_void_p, dp, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_double, ctypes.c_int]
+        L.orc_kmeans_assign.restype = ctypes.c_int
+        L.orc_kmeans_assign.argtypes = [ctypes.c_void_p, dp, ctypes.c_int, lp]
+        L.orc_quick_assign.argtypes = [dp, ctypes.c_int, dp, dp, dp, ctypes.c_long, lp]
+        L.orc_select_patch.argtypes = [ctypes.c_int, dp, ctypes.c_int, dp, dp, dp,
+                                       ctypes.c_long, lp]
         _lib = L
     return _lib
 
@@ -124,6 +136,31 @@ class OracleField:
         return dict(x=xyz[:cnt, 0], y=xyz[:cnt, 1], z=xyz[:cnt, 2], size=swd[:cnt, 0],
                     w=swd[:cnt, 1], d1=swd[:cnt, 2], d2=swd[:cnt, 3], n=ns[:cnt, 0],
                     start=ns[:cnt, 1], depth=depth[:cnt])
+
+    # k-means (src/KMeans.cpp) on the oracle's tree; centers: (npatch, 2 or 3) float64.
+    def kmeans_init(self, npatch, init="tree", seed=1):
+        dim = 2 if self.coords == "flat" else 3
+        cen = np.zeros((npatch, dim))
+        fn = {"tree": "orc_kmeans_init_tree", "random": "orc_kmeans_init_rand",
+              "kmeans++": "orc_kmeans_init_kmpp"}[init]
+        rc = getattr(lib(), fn)(self.h, _p(cen), int(npatch), int(seed))
+        if rc:
+            raise RuntimeError("oracle k-means init failed")
+        return cen
+
+    def kmeans_run(self, centers, max_iter=200, tol=1e-5, alt=False):
+        """Refines a copy of centers; returns (centers, iterations)."""
+        cen = np.ascontiguousarray(centers, dtype=float).copy()
+        it = lib().orc_kmeans_run(self.h, _p(cen), cen.shape[0], int(max_iter), float(tol),
+                                  int(bool(alt)))
+        return cen, it
+
+    def kmeans_assign(self, centers):
+        cen = np.ascontiguousarray(centers, dtype=float)
+        out = np.empty(self.n, dtype=np.int64)
+        lib().orc_kmeans_assign(self.h, _p(cen), cen.shape[0],
+                                out.ctypes.data_as(ctypes.POINTER(ctypes.c_long)))
+        return out
 
     def order(self):
         out = np.zeros(self.n, dtype=np.int64)
@@ -190,4 +227,28 @@ def multipole(metric, bins, max_n, f, quick=False, nthreads=0):
                                         *[_p(out[k]) for k in MP_KEYS[8:]])
     if rc:
         raise ValueError("multipole needs a G field")
+    return out
+
+
+def quick_assign(centers, x, y, z=None):
+    """QuickAssign (src/KMeans.cpp:890-942) restated; z None selects the 2-d form."""
+    cen = np.ascontiguousarray(centers, dtype=float)
+    x = np.ascontiguousarray(x, dtype=float)
+    y = np.ascontiguousarray(y, dtype=float)
+    z = None if z is None else np.ascontiguousarray(z, dtype=float)
+    out = np.empty(len(x), dtype=np.int64)
+    lib().orc_quick_assign(_p(cen), cen.shape[0], _p(x), _p(y), _p(z), len(x),
+                           out.ctypes.data_as(ctypes.POINTER(ctypes.c_long)))
+    return out
+
+
+def select_patch(patch, centers, x, y, z=None):
+    """SelectPatch (src/KMeans.cpp:944-1011) restated."""
+    cen = np.ascontiguousarray(centers, dtype=float)
+    x = np.ascontiguousarray(x, dtype=float)
+    y = np.ascontiguousarray(y, dtype=float)
+    z = None if z is None else np.ascontiguousarray(z, dtype=float)
+    out = np.empty(len(x), dtype=np.int64)
+    lib().orc_select_patch(int(patch), _p(cen), cen.shape[0], _p(x), _p(y), _p(z), len(x),
+                           out.ctypes.data_as(ctypes.POINTER(ctypes.c_long)))
     return out

@@ -22,8 +22,11 @@
 #include <cmath>
 #include <complex>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
+#include <ctime>
 #include <limits>
+#include <set>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -825,6 +828,227 @@ void multipole_split1(const Params& P, const Field& f, int i1, const std::vector
 
 long long g_last_accepted = 0;   // directProcess11 calls of the last process call
 
+// ---------------------------------------------------------------------------------------
+// k-means patches (src/KMeans.cpp), on this oracle's tree.  Positions are 3-vectors with
+// z = 0 for Flat; Position<C>::normSq of a difference is ((dx dx + dy dy) + dz dz).
+
+struct P3 { double x = 0., y = 0., z = 0.; };
+
+inline double p3_dsq(const P3& a, const P3& b)
+{
+    const double dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+    return (dx * dx + dy * dy) + dz * dz;
+}
+inline bool p3_eq(const P3& a, const P3& b) { return a.x == b.x && a.y == b.y && a.z == b.z; }
+inline P3 node_pos(const Node& nd) { return P3{nd.x, nd.y, nd.z}; }
+
+// urand, src/Cell.cpp:59-80 (the C library's rand(); a non-zero seed reseeds and draws).
+bool g_first_urand = true;
+double urand(long long seed = 0)
+{
+    if (seed != 0) { srand((unsigned)seed); g_first_urand = false; }
+    else if (g_first_urand) { srand((unsigned)time(nullptr)); g_first_urand = false; }
+    double r = rand();
+    return r / RAND_MAX;
+}
+
+// SelectRandomFrom, src/Corr2.cpp:622-661.
+std::vector<long> select_random(long m, long n)
+{
+    std::vector<long> sel(n);
+    if (m > 3 * n) {
+        std::set<long> got;
+        while ((long)got.size() < n) {
+            long j = long(urand() * m);
+            if (j == m) j = m - 1;
+            if (got.insert(j).second) sel[got.size() - 1] = j;
+        }
+    } else {
+        std::vector<long> all(m);
+        for (long i = 0; i < m; ++i) all[i] = i;
+        for (long i = 0; i < n; ++i) {
+            long j = long(urand() * (m - i)) + i;
+            if (j == m) j = m - 1;
+            std::swap(all[i], all[j]);
+        }
+        std::copy(all.begin(), all.begin() + n, sel.begin());
+    }
+    return sel;
+}
+
+// InitializeCentersTree, recursive part, src/KMeans.cpp:28-59.
+void km_init_tree_cell(const Field& f, int id, long first, int nc, std::vector<P3>& cen)
+{
+    const Node& nd = f.nodes[id];
+    if (nc == 1) {
+        cen[first] = node_pos(nd);
+    } else if (nd.left >= 0) {
+        int m1 = nc / 2, m2 = nc - m1;
+        if (urand() < 0.5) std::swap(m1, m2);
+        km_init_tree_cell(f, nd.left, first, m1, cen);
+        km_init_tree_cell(f, nd.right, first + m1, m2, cen);
+    } else {
+        for (int i = 0; i < nc; ++i) {
+            const double a = 1. + urand() * 1.e-8;
+            P3 v{nd.x * a, nd.y * a, nd.z * a};
+            if (f.coords == SPHERE) normalize3(v.x, v.y, v.z);
+            cen[first + i] = v;
+        }
+    }
+}
+
+// getLeafNumber, src/Cell.cpp:675-685.
+int leaf_number(const Field& f, int id, long m)
+{
+    while (f.nodes[id].left >= 0) {
+        const Node& l = f.nodes[f.nodes[id].left];
+        if (m < l.n) id = f.nodes[id].left;
+        else { m -= l.n; id = f.nodes[id].right; }
+    }
+    return id;
+}
+
+// InitializeCentersKMPP, recursive part, src/KMeans.cpp:159-218; returns false for the
+// reference's LeafAlreadyUsed exception.
+bool km_kmpp_cell(const Field& f, int id, const std::vector<P3>& cen, long ncen, P3& out)
+{
+    const Node& nd = f.nodes[id];
+    if (nd.size == 0.f) {
+        for (long j = 0; j < ncen; ++j)
+            if (p3_eq(node_pos(nd), cen[j])) return false;
+        out = node_pos(nd);
+        return true;
+    }
+    const P3 lp = node_pos(f.nodes[nd.left]), rp = node_pos(f.nodes[nd.right]);
+    double d1 = p3_dsq(lp, cen[0]), d2 = p3_dsq(rp, cen[0]);
+    for (long j = 1; j < ncen; ++j) {
+        const double a = p3_dsq(lp, cen[j]), b = p3_dsq(rp, cen[j]);
+        if (a < d1) d1 = a;
+        if (b < d2) d2 = b;
+    }
+    if (d1 + d2 == 0.) return false;
+    const double u = urand() * (d1 + d2);
+    if (u < d1) {
+        if (km_kmpp_cell(f, nd.left, cen, ncen, out)) return true;
+        return km_kmpp_cell(f, nd.right, cen, ncen, out);
+    }
+    if (km_kmpp_cell(f, nd.right, cen, ncen, out)) return true;
+    return km_kmpp_cell(f, nd.left, cen, ncen, out);
+}
+
+// The per-cell actions of FindCellsInPatches (src/KMeans.cpp:318-541).
+struct KMAction {
+    int mode;                    // 0 update centres, 1 inertia, 2 assign
+    const Field* f;
+    const std::vector<P3>* cen;
+    std::vector<P3> sum;         // UpdateCenters
+    std::vector<double> w;
+    std::vector<double> inertia; // CalculateInertia
+    double sumw = 0.;
+    long* patches = nullptr;     // AssignPatches
+
+    void run(int p, int id)
+    {
+        const Node& nd = f->nodes[id];
+        if (mode == 0) {
+            const double ww = nd.w;
+            sum[p].x += nd.x * ww; sum[p].y += nd.y * ww; sum[p].z += nd.z * ww;
+            w[p] += ww;
+        } else if (mode == 1) {
+            const double ssq = double(nd.size) * double(nd.size);
+            const double ww = nd.w;
+            inertia[p] += p3_dsq(node_pos(nd), (*cen)[p]) * ww;
+            if (ssq > 0.) inertia[p] += 0.75 * ssq * ww;
+            sumw += ww;
+        } else {
+            for (long k = nd.start; k < nd.end; ++k) patches[f->pts[k].index] = p;
+        }
+    }
+};
+
+// FindCellsInPatches, src/KMeans.cpp:543-645 (candidate swaps included).
+void km_find(const Field& f, const std::vector<P3>& cen, int id, std::vector<long>& pat,
+             long ncand, std::vector<double>& saved, KMAction& act, const std::vector<double>* I)
+{
+    const Node& nd = f.nodes[id];
+    const P3 c = node_pos(nd);
+    const double s = nd.size;
+    long closest = pat[0];
+    double mind = p3_dsq(c, cen[closest]);
+    saved[0] = mind;
+    if (I) mind += (*I)[closest];
+    for (long j = 1; j < ncand; ++j) {
+        const long i = pat[j];
+        double d = p3_dsq(c, cen[i]);
+        saved[j] = d;
+        if (I) d += (*I)[i];
+        if (d < mind) {
+            std::swap(saved[0], saved[j]);
+            std::swap(pat[0], pat[j]);
+            closest = i;
+            mind = d;
+        }
+    }
+    const double min_d = std::sqrt(saved[0]);
+    const double thresh = I ? sqr(min_d + s) + (*I)[closest] : sqr(min_d + 2 * s);
+    for (long j = ncand - 1; j > 0; --j) {
+        double d = saved[j];
+        if (I) {
+            const double dd = std::sqrt(d);
+            d = (s > dd) ? 0. : sqr(dd - s) + (*I)[pat[j]];
+        }
+        if (d > thresh) {
+            --ncand;
+            if (j != ncand) std::swap(pat[j], pat[ncand]);
+        }
+    }
+    if (ncand == 1 || s == 0. || nd.left < 0) {
+        act.run((int)closest, id);
+    } else {
+        km_find(f, cen, nd.left, pat, ncand, saved, act, I);
+        km_find(f, cen, nd.right, pat, ncand, saved, act, I);
+    }
+}
+
+void km_find_all(const Field& f, const std::vector<P3>& cen, KMAction& act,
+                 const std::vector<double>* I)
+{
+    const long np = (long)cen.size();
+    std::vector<long> pat(np);
+    std::vector<double> saved(np);
+    for (long i = 0; i < np; ++i) pat[i] = i;
+    for (int t : f.tops) km_find(f, cen, t, pat, np, saved, act, I);
+}
+
+std::vector<P3> read_centers(const double* c, int npatch, int coords)
+{
+    const int dim = coords == FLAT ? 2 : 3;
+    std::vector<P3> v(npatch);
+    for (int p = 0; p < npatch; ++p) {
+        v[p] = P3{c[dim * p], c[dim * p + 1], dim == 3 ? c[dim * p + 2] : 0.};
+        if (coords == SPHERE) normalize3(v[p].x, v[p].y, v[p].z);
+    }
+    return v;
+}
+
+void write_centers(const std::vector<P3>& v, double* c, int coords)
+{
+    const int dim = coords == FLAT ? 2 : 3;
+    for (size_t p = 0; p < v.size(); ++p) {
+        c[dim * p] = v[p].x; c[dim * p + 1] = v[p].y;
+        if (dim == 3) c[dim * p + 2] = v[p].z;
+    }
+}
+
+// QuickAssign / SelectPatch distance, src/KMeans.cpp:911-935 and 970-1006.
+inline double qdist(const double* c, int dim, int k, double x, double y, double z)
+{
+    const double dx = x - c[dim * k], dy = y - c[dim * k + 1];
+    double r = dx * dx + dy * dy;
+    if (dim == 3) { const double dz = z - c[dim * k + 2]; r += dz * dz; }
+    return r;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1067,6 +1291,191 @@ int orc_max_threads(void)
 #else
     return 1;
 #endif
+}
+
+// KMeansInitTree1 / InitializeCentersTree, src/KMeans.cpp:61-109, 743-751.
+int orc_kmeans_init_tree(void* h, double* centers, int npatch, long long seed)
+{
+    Field& f = *static_cast<Field*>(h);
+    build_cells(f);
+    std::vector<P3> cen(npatch);
+    const long ncells = (long)f.tops.size();
+    urand(seed);
+    if (ncells > npatch) {
+        const std::vector<long> sel = select_random(ncells, npatch);
+        for (int i = 0; i < npatch; ++i) cen[i] = node_pos(f.nodes[f.tops[sel[i]]]);
+    } else {
+        const long n1 = npatch / ncells, k2 = npatch % ncells, k1 = ncells - k2;
+        std::vector<long> nv(ncells);
+        for (long k = 0; k < ncells; ++k) nv[k] = k < k1 ? n1 : n1 + 1;
+        for (long k = ncells; k > 1; --k) {
+            long j = int(urand() * k);
+            if (j > k - 1) j = k - 1;
+            if (j != k - 1) std::swap(nv[j], nv[k - 1]);
+        }
+        long first = 0;
+        for (long k = 0; k < ncells; ++k) {
+            km_init_tree_cell(f, f.tops[k], first, (int)nv[k], cen);
+            first += nv[k];
+        }
+    }
+    write_centers(cen, centers, f.coords);
+    return 0;
+}
+
+// KMeansInitRand1 / InitializeCentersRand, src/KMeans.cpp:111-157, 753-761.
+int orc_kmeans_init_rand(void* h, double* centers, int npatch, long long seed)
+{
+    Field& f = *static_cast<Field*>(h);
+    build_cells(f);
+    long ntot = 0;
+    for (int t : f.tops) ntot += f.nodes[t].n;
+    urand(seed);
+    const std::vector<long> index = select_random(ntot, npatch);
+    std::vector<P3> cen(npatch);
+    for (int i = 0; i < npatch; ++i) {
+        long m = index[i];
+        for (int t : f.tops) {
+            if (m < f.nodes[t].n) { cen[i] = node_pos(f.nodes[leaf_number(f, t, m)]); break; }
+            m -= f.nodes[t].n;
+        }
+        for (int i1 = 0; i1 < i; ++i1) {
+            if (p3_eq(cen[i1], cen[i])) {
+                const double a = 1. + urand() * 1.e-8;
+                cen[i].x *= a; cen[i].y *= a; cen[i].z *= a;
+            }
+        }
+    }
+    write_centers(cen, centers, f.coords);
+    return 0;
+}
+
+// KMeansInitKMPP1 / InitializeCentersKMPP, src/KMeans.cpp:220-315, 763-771.
+int orc_kmeans_init_kmpp(void* h, double* centers, int npatch, long long seed)
+{
+    Field& f = *static_cast<Field*>(h);
+    build_cells(f);
+    const long ncells = (long)f.tops.size();
+    urand(seed);
+    long ntot = 0;
+    for (int t : f.tops) ntot += f.nodes[t].n;
+    std::vector<long> per(ncells, 0);
+    std::vector<P3> cen(npatch);
+    long m = long(urand() * ntot);
+    for (long k = 0; k < ncells; ++k) {
+        const Node& t = f.nodes[f.tops[k]];
+        if (m < t.n) { cen[0] = node_pos(f.nodes[leaf_number(f, f.tops[k], m)]); per[k] += 1; break; }
+        m -= t.n;
+    }
+    const double coef = f.coords == THREED ? 0.6 : 0.5;
+    std::vector<double> p(ncells);
+    for (int i = 1; i < npatch; ++i) {
+        double sump = 0.;
+        for (long k = 0; k < ncells; ++k) {
+            const Node& t = f.nodes[f.tops[k]];
+            double d1 = p3_dsq(cen[0], node_pos(t));
+            for (int i1 = 1; i1 < i; ++i1) {
+                const double d2 = p3_dsq(cen[i1], node_pos(t));
+                if (d2 < d1) d1 = d2;
+            }
+            p[k] = (t.n - per[k]) * (d1 + coef * sqr(double(t.size)));
+            sump += p[k];
+        }
+        double u = urand();
+        for (long k = 0; k < ncells; ++k) {
+            p[k] /= sump;
+            if (u < p[k]) {
+                if (!km_kmpp_cell(f, f.tops[k], cen, i, cen[i])) return 1;
+                per[k] += 1;
+                break;
+            }
+            u -= p[k];
+        }
+    }
+    write_centers(cen, centers, f.coords);
+    return 0;
+}
+
+// KMeansRun1, src/KMeans.cpp:773-833.  Returns the iterations run.
+int orc_kmeans_run(void* h, double* centers, int npatch, int max_iter, double tol, int alt)
+{
+    Field& f = *static_cast<Field*>(h);
+    build_cells(f);
+    std::vector<P3> cen = read_centers(centers, npatch, f.coords);
+    const double tolsq = sqr(tol * std::sqrt(f.sizesq)) * npatch;
+    std::vector<double> inertia;
+    int it = 0;
+    for (; it < max_iter; ++it) {
+        if (alt) {
+            KMAction ci{1, &f, &cen};
+            ci.inertia.assign(npatch, 0.);
+            km_find_all(f, cen, ci, nullptr);
+            const double meanw = ci.sumw / npatch / 3.;
+            inertia = ci.inertia;
+            for (int i = 0; i < npatch; ++i) inertia[i] /= meanw;
+        }
+        KMAction up{0, &f, &cen};
+        up.sum.assign(npatch, P3{});
+        up.w.assign(npatch, 0.);
+        km_find_all(f, cen, up, alt ? &inertia : nullptr);
+        for (int i = 0; i < npatch; ++i) {
+            if (up.w[i] > 0.) {
+                up.sum[i].x /= up.w[i]; up.sum[i].y /= up.w[i]; up.sum[i].z /= up.w[i];
+                if (f.coords == SPHERE) normalize3(up.sum[i].x, up.sum[i].y, up.sum[i].z);
+            }
+        }
+        double shiftsq = 0.;
+        for (int i = 0; i < npatch; ++i) shiftsq += p3_dsq(cen[i], up.sum[i]);
+        cen = up.sum;
+        if (shiftsq < tolsq) { ++it; break; }
+    }
+    write_centers(cen, centers, f.coords);
+    return it;
+}
+
+// KMeansAssign1, src/KMeans.cpp:835-849.
+int orc_kmeans_assign(void* h, const double* centers, int npatch, long* patches)
+{
+    Field& f = *static_cast<Field*>(h);
+    build_cells(f);
+    std::vector<P3> cen = read_centers(centers, npatch, f.coords);
+    KMAction as{2, &f, &cen};
+    as.patches = patches;
+    km_find_all(f, cen, as, nullptr);
+    return 0;
+}
+
+// QuickAssign, src/KMeans.cpp:890-942 (z == NULL: the 2-d form).
+void orc_quick_assign(const double* centers, int npatch, const double* x, const double* y,
+                      const double* z, long n, long* out)
+{
+    const int dim = z ? 3 : 2;
+    for (long i = 0; i < n; ++i) {
+        const double zi = z ? z[i] : 0.;
+        int kmin = 0;
+        double mn = qdist(centers, dim, 0, x[i], y[i], zi);
+        for (int k = 1; k < npatch; ++k) {
+            const double r = qdist(centers, dim, k, x[i], y[i], zi);
+            if (r < mn) { kmin = k; mn = r; }
+        }
+        out[i] = kmin;
+    }
+}
+
+// SelectPatch, src/KMeans.cpp:944-1011.
+void orc_select_patch(int patch, const double* centers, int npatch, const double* x,
+                      const double* y, const double* z, long n, long* use)
+{
+    const int dim = z ? 3 : 2;
+    for (long i = 0; i < n; ++i) {
+        const double zi = z ? z[i] : 0.;
+        const double pd = qdist(centers, dim, patch, x[i], y[i], zi);
+        use[i] = 1;
+        for (int q = 0; q < npatch; ++q) {
+            if (q == patch) continue;
+            if (qdist(centers, dim, q, x[i], y[i], zi) < pd) { use[i] = 0; break; }
+        }
+    }
 }
 
 }  // extern "C"

@@ -95,7 +95,7 @@ def run_case(name):
     return out
 
 
-if __name__ == "__main__" and "--mp" not in sys.argv and "--xyz" not in sys.argv:
+if __name__ == "__main__" and not {"--mp", "--xyz", "--kmeans"} & set(sys.argv):
     _treecorr.SetOMPThreads(1)
     names = sys.argv[1:] or list(CASES)
     for name in names:
@@ -159,3 +159,49 @@ if __name__ == "__main__" and "--xyz" in sys.argv:
         out["x" + tag], out["y" + tag], out["z" + tag] = x, y, z
     np.savez(os.path.join(HERE, "generate_xyz.npz"), **out)
     print("generate_xyz.npz")
+
+
+# k-means (src/KMeans.cpp): the three initialisations, KMeansRun after 1 and 3 iterations and
+# to convergence (plain and alternate), KMeansAssign, QuickAssign and SelectPatch.
+if __name__ == "__main__" and "--kmeans" in sys.argv:
+    _treecorr.SetOMPThreads(1)
+    from cases_km import KM_CASES, KM_MAX_ITER, KM_SEED, KM_TOL, km_inputs, km_spec
+    for name in KM_CASES:
+        s = km_spec(name)
+        cat = km_inputs(name)
+        empty = np.array([])
+        z = cat["z"] if cat["z"] is not None else empty
+        cls = getattr(_treecorr, "NField" + COORDS[s["coords"]])
+        fld = cls(cat["x"], cat["y"], z, cat["w"], empty, 0., np.inf, _treecorr.Mean, 0, False,
+                  s["min_top"], s["max_top"])
+        npatch = s["npatch"]
+        dim = 2 if s["coords"] == "flat" else 3
+        out = {"x": cat["x"], "y": cat["y"], "w": cat["w"], "ntop": fld.getNTopLevel()}
+        if cat["z"] is not None:
+            out["z"] = cat["z"]
+        for tag, meth in (("tree", fld.KMeansInitTree), ("rand", fld.KMeansInitRand),
+                          ("kmpp", fld.KMeansInitKMPP)):
+            c = np.zeros((npatch, dim))
+            meth(c, npatch, KM_SEED)
+            out["init_" + tag] = c
+        for tag, iters, alt in (("it1", 1, False), ("it3", 3, False), ("run", KM_MAX_ITER, False),
+                                ("alt_it1", 1, True), ("alt_it3", 3, True),
+                                ("alt_run", KM_MAX_ITER, True)):
+            c = out["init_tree"].copy()
+            fld.KMeansRun(c, npatch, iters, KM_TOL, alt)
+            out[tag] = c
+        pat = np.zeros(s["n"], dtype=int)
+        fld.KMeansAssign(out["run"], npatch, pat)
+        out["assign"] = pat
+        pat = np.zeros(s["n"], dtype=int)
+        fld.KMeansAssign(out["alt_run"], npatch, pat)
+        out["alt_assign"] = pat
+        q = np.zeros(s["n"], dtype=int)
+        _treecorr.QuickAssign(out["run"], npatch, cat["x"], cat["y"], z, q)
+        out["quick"] = q
+        for pp in (0, npatch - 1):
+            use = np.zeros(s["n"], dtype=int)
+            _treecorr.SelectPatch(pp, out["run"], npatch, cat["x"], cat["y"], z, use)
+            out["select_%d" % pp] = use
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print(f"{name:16s} ntop={out['ntop']} patches used={len(np.unique(out['assign']))}")

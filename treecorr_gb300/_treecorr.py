@@ -133,6 +133,25 @@ def lib():
         L.tc_corr3_last_ms.argtypes = [vp]
         L.tc_corr3_stats.restype = ctypes.c_int
         L.tc_corr3_stats.argtypes = [vp, ctypes.POINTER(i64)]
+        lp64 = ctypes.POINTER(ctypes.c_int64)
+        for nm in ("tc_kmeans_init_tree", "tc_kmeans_init_rand", "tc_kmeans_init_kmpp"):
+            getattr(L, nm).restype = ctypes.c_int
+            getattr(L, nm).argtypes = [vp, dp, ctypes.c_int, i64]
+        L.tc_kmeans_run.restype = ctypes.c_int
+        L.tc_kmeans_run.argtypes = [vp, dp, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                    ctypes.c_int]
+        L.tc_kmeans_assign.restype = ctypes.c_int
+        L.tc_kmeans_assign.argtypes = [vp, dp, ctypes.c_int, lp64, i64]
+        L.tc_kmeans_iterations.restype = ctypes.c_int
+        L.tc_kmeans_iterations.argtypes = [vp]
+        L.tc_quick_assign.restype = ctypes.c_int
+        L.tc_quick_assign.argtypes = [dp, ctypes.c_int, dp, dp, dp, i64, lp64]
+        L.tc_select_patch.restype = ctypes.c_int
+        L.tc_select_patch.argtypes = [ctypes.c_int, dp, ctypes.c_int, dp, dp, dp, i64, lp64]
+        L.tc_quick_assign_device.restype = ctypes.c_int
+        L.tc_quick_assign_device.argtypes = [dp, ctypes.c_int, vp, vp, vp, i64, vp]
+        L.tc_select_patch_device.restype = ctypes.c_int
+        L.tc_select_patch_device.argtypes = [ctypes.c_int, dp, ctypes.c_int, vp, vp, vp, i64, vp]
         L.tc_launch_count.restype = ctypes.c_longlong
         L.tc_launch_count.argtypes = []
         L.tc_stream.restype = ctypes.c_void_p
@@ -273,10 +292,38 @@ class _FieldBase:
     def getNear(self, *args):
         raise NotImplementedError("getNear is not on the GPU path")
 
-    def KMeansInitTree(self, *args):
-        raise NotImplementedError("k-means patches are not on the GPU path")
+    # k-means (src/Field.cpp:630-634 -> src/KMeans.cpp:851-888).  cenp is the caller's
+    # (npatch, 2 or 3) float64 array, filled or refined in place like the reference's
+    # py::array_t; pp receives the patch of every point.
+    def _centers(self, cenp, npatch):
+        dim = 2 if self._coords == Coord.Flat else 3
+        if (not isinstance(cenp, np.ndarray) or cenp.dtype != np.float64 or
+                not cenp.flags.c_contiguous or cenp.size != npatch * dim):
+            raise ValueError(f"centers must be a contiguous float64 array of {npatch} x {dim}")
+        return _ptr(cenp)
 
-    KMeansInitRand = KMeansInitKMPP = KMeansRun = KMeansAssign = KMeansInitTree
+    def KMeansInitTree(self, cenp, npatch, seed):
+        _check(lib().tc_kmeans_init_tree(self._h, self._centers(cenp, npatch), int(npatch), int(seed)))
+
+    def KMeansInitRand(self, cenp, npatch, seed):
+        _check(lib().tc_kmeans_init_rand(self._h, self._centers(cenp, npatch), int(npatch), int(seed)))
+
+    def KMeansInitKMPP(self, cenp, npatch, seed):
+        _check(lib().tc_kmeans_init_kmpp(self._h, self._centers(cenp, npatch), int(npatch), int(seed)))
+
+    def KMeansRun(self, cenp, npatch, max_iter, tol, alt):
+        _check(lib().tc_kmeans_run(self._h, self._centers(cenp, npatch), int(npatch),
+                                   int(max_iter), float(tol), int(bool(alt))))
+
+    def KMeansAssign(self, cenp, npatch, pp):
+        if pp.dtype != np.int64 or not pp.flags.c_contiguous:
+            raise ValueError("patches must be a contiguous int64 array")
+        _check(lib().tc_kmeans_assign(self._h, self._centers(cenp, npatch), int(npatch),
+                                      pp.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), pp.size))
+
+    def kmeans_iterations(self):
+        """Iterations run by the last KMeansRun (no reference counterpart)."""
+        return int(lib().tc_kmeans_iterations(self._h))
 
     def _dump(self):
         """Canonical depth-first dump of the tree (tests only)."""
@@ -638,6 +685,36 @@ def _not_on_path(name):
 for _n in ("NKCorr", "NZCorr", "KZCorr", "ZZCorr", "NVCorr", "KVCorr", "VVCorr", "NGCorr",
            "KGCorr", "NTCorr", "KTCorr", "TTCorr", "NQCorr", "KQCorr", "QQCorr"):
     globals()[_n] = _not_on_path(_n)
-QuickAssign = _not_on_path("QuickAssign")
-SelectPatch = _not_on_path("SelectPatch")
 del _n
+
+
+def _assign_args(cenp, npatch, xp, yp, zp, out):
+    n = len(xp)
+    x = np.ascontiguousarray(xp, dtype=np.float64)
+    y = np.ascontiguousarray(yp, dtype=np.float64)
+    z = np.ascontiguousarray(zp, dtype=np.float64) if len(zp) else None
+    dim = 3 if z is not None else 2
+    if len(y) != n or (z is not None and len(z) != n) or len(out) != n:
+        raise ValueError("x, y, z and the output must have the same length")
+    cen = np.ascontiguousarray(cenp, dtype=np.float64)
+    if cen.size != npatch * dim:
+        raise ValueError(f"centers must have {npatch} x {dim} entries")
+    if out.dtype != np.int64 or not out.flags.c_contiguous:
+        raise ValueError("the output must be a contiguous int64 array")
+    return cen, x, y, z, n
+
+
+def QuickAssign(cenp, npatch, xp, yp, zp, pp):
+    """QuickAssign (src/KMeans.cpp:890-942): pp[i] = the nearest centre of point i; an empty
+    zp selects the 2-d form.  Computed on the GPU."""
+    cen, x, y, z, n = _assign_args(cenp, npatch, xp, yp, zp, pp)
+    _check(lib().tc_quick_assign(_ptr(cen), int(npatch), _ptr(x), _ptr(y), _ptr(z), n,
+                                 pp.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))
+
+
+def SelectPatch(patch, cenp, npatch, xp, yp, zp, usep):
+    """SelectPatch (src/KMeans.cpp:944-1011): usep[i] = 1 when patch is the nearest centre
+    of point i, else 0.  Computed on the GPU."""
+    cen, x, y, z, n = _assign_args(cenp, npatch, xp, yp, zp, usep)
+    _check(lib().tc_select_patch(int(patch), _ptr(cen), int(npatch), _ptr(x), _ptr(y), _ptr(z),
+                                 n, usep.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))))

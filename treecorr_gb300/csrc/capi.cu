@@ -19,6 +19,7 @@
 #include "traverse2pt.hpp"
 #include "multipole.hpp"
 #include "learned.hpp"
+#include "kmeans.hpp"
 
 namespace tc {
 
@@ -72,6 +73,7 @@ struct tc_field {
     float build_ms = 0.f;
     double* leafsums = nullptr;  // 4 per cell, built on first multipole use
     float4* leafsums_f = nullptr;  // the same as floats
+    int km_iters = 0;            // iterations of the last k-means run
 };
 
 struct tc_corr3 {
@@ -968,6 +970,123 @@ int64_t tc_field_dump(tc_field* f, double* xyz, float* size_w_d, int64_t* n_star
 {
     if (!f) { set_last_error("NULL field"); return -TC_ERR_ARG; }
     return field_dump(f, xyz, size_w_d, n_start, depth, cap);
+}
+
+}  // extern "C"
+
+namespace {
+
+// The built field as the k-means code sees it.
+int km_view(tc_field* f, KMField& F)
+{
+    if (!f) { set_last_error("NULL field"); return TC_ERR_ARG; }
+    TC_TRY(field_build(f));
+    F.coords = f->coords;
+    F.n = f->n;
+    F.ncap = f->n > 0 ? (int)(2 * f->n - 1) : 0;
+    F.cells = f->cells;
+    F.d_tops = f->d_tops;
+    F.ntop = (int)f->tops.size();
+    F.idx = f->buf[0].idx;
+    F.size = std::sqrt(f->center[3]);
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tc_kmeans_init_tree(tc_field* f, double* centers, int npatch, int64_t seed)
+{
+    KMField F;
+    TC_TRY(km_view(f, F));
+    if (!centers) { set_last_error("centers is NULL"); return TC_ERR_ARG; }
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    return kmeans_init_tree(F, centers, npatch, (long long)seed, st);
+}
+
+int tc_kmeans_init_rand(tc_field* f, double* centers, int npatch, int64_t seed)
+{
+    KMField F;
+    TC_TRY(km_view(f, F));
+    if (!centers) { set_last_error("centers is NULL"); return TC_ERR_ARG; }
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    return kmeans_init_rand(F, centers, npatch, (long long)seed, st);
+}
+
+int tc_kmeans_init_kmpp(tc_field* f, double* centers, int npatch, int64_t seed)
+{
+    KMField F;
+    TC_TRY(km_view(f, F));
+    if (!centers) { set_last_error("centers is NULL"); return TC_ERR_ARG; }
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    return kmeans_init_kmpp(F, centers, npatch, (long long)seed, st);
+}
+
+int tc_kmeans_run(tc_field* f, double* centers, int npatch, int max_iter, double tol, int alt)
+{
+    KMField F;
+    TC_TRY(km_view(f, F));
+    if (!centers) { set_last_error("centers is NULL"); return TC_ERR_ARG; }
+    if (max_iter < 0) { set_last_error("max_iter must be >= 0"); return TC_ERR_ARG; }
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    int iters = 0;
+    const int rc = kmeans_run(F, centers, npatch, max_iter, tol, alt != 0, st, &iters);
+    f->km_iters = iters;
+    return rc;
+}
+
+int tc_kmeans_assign(tc_field* f, const double* centers, int npatch, int64_t* patches, int64_t n)
+{
+    KMField F;
+    TC_TRY(km_view(f, F));
+    if (!centers || !patches) { set_last_error("NULL argument"); return TC_ERR_ARG; }
+    if (n != f->n) { set_last_error("patches must have one entry per point of the field"); return TC_ERR_ARG; }
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    return kmeans_assign(F, centers, npatch, patches, st);
+}
+
+int tc_kmeans_iterations(const tc_field* f) { return f ? f->km_iters : 0; }
+
+int tc_quick_assign(const double* centers, int npatch, const double* x, const double* y,
+                    const double* z, int64_t n, int64_t* patches)
+{
+    if (!centers || (n > 0 && (!x || !y || !patches))) { set_last_error("NULL argument"); return TC_ERR_ARG; }
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    return quick_assign(centers, npatch, x, y, z, n, patches, false, st);
+}
+
+int tc_select_patch(int patch, const double* centers, int npatch, const double* x,
+                    const double* y, const double* z, int64_t n, int64_t* use)
+{
+    if (!centers || (n > 0 && (!x || !y || !use))) { set_last_error("NULL argument"); return TC_ERR_ARG; }
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    return select_patch(patch, centers, npatch, x, y, z, n, use, false, st);
+}
+
+int tc_quick_assign_device(const double* centers, int npatch, const double* x, const double* y,
+                           const double* z, int64_t n, int64_t* patches)
+{
+    if (!centers || (n > 0 && (!x || !y || !patches))) { set_last_error("NULL argument"); return TC_ERR_ARG; }
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    return quick_assign(centers, npatch, x, y, z, n, patches, true, st);
+}
+
+int tc_select_patch_device(int patch, const double* centers, int npatch, const double* x,
+                           const double* y, const double* z, int64_t n, int64_t* use)
+{
+    if (!centers || (n > 0 && (!x || !y || !use))) { set_last_error("NULL argument"); return TC_ERR_ARG; }
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    return select_patch(patch, centers, npatch, x, y, z, n, use, true, st);
 }
 
 int tc_corr2_create(int d1, int d2, int bin_type, double minsep, double maxsep, int nbins,
