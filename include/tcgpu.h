@@ -61,10 +61,16 @@ extern "C" {
 #define TC_LOGRUV       3
 #define TC_LOGSAS       4
 #define TC_LOGMULTIPOLE 5
-/* Data kinds of a field (NData, KData, GData in include/Cell.h:37). */
-#define TC_NDATA 0
-#define TC_KDATA 1
-#define TC_GDATA 2
+/* Data kinds of a field (DataType, include/Cell.h:37; this ABI numbers them N, K, G, Z,
+ * V, T, Q = 0..6, the reference N, K, Z, V, G, T, Q = 0..6 -- Python passes classes, not
+ * numbers, so only the names must agree). */
+#define TC_NDATA 0   /* counts */
+#define TC_KDATA 1   /* scalar */
+#define TC_GDATA 2   /* spin-2 complex (shear) */
+#define TC_ZDATA 3   /* spin-0 complex */
+#define TC_VDATA 4   /* spin-1 complex (vector) */
+#define TC_TDATA 5   /* spin-3 complex */
+#define TC_QDATA 6   /* spin-4 complex */
 
 typedef struct tc_field tc_field;
 typedef struct tc_corr2 tc_corr2;
@@ -81,10 +87,12 @@ typedef struct tc_stats {
     int64_t learned;         /* cell pairs accepted by the learned criterion (of accepted) */
 } tc_stats;
 
-/* Field construction: replaces BuildNField / BuildKField / BuildGField for
- * C = Flat, Sphere, ThreeD (src/Field.cpp:430-546, pybind11 constructors at 686-691),
- * i.e. Field<D,C>::Field (src/Field.cpp:163-204).  Host arrays of length n:
- *   x, y: positions; z: NULL for Flat; d1 = k (KData) or g1 (GData), d2 = g2 (GData);
+/* Field construction: replaces BuildNField / BuildKField / BuildZField / BuildVField /
+ * BuildGField / BuildTField / BuildQField for C = Flat, Sphere, ThreeD (src/Field.cpp:430-560,
+ * pybind11 constructors at 683-689), i.e. Field<D,C>::Field (src/Field.cpp:163-204).
+ * Host arrays of length n:
+ *   x, y: positions; z: NULL for Flat; d1 = k (K) or the real part (Z, V, G, T, Q),
+ *   d2 = the imaginary part;
  *   w: weights; wpos: NULL means "use w" (src/Field.cpp:146-152).
  * The data are copied to the device here; the tree is built on the first call that needs
  * it (tc_field_ntop or a process call), like the reference's lazy BuildCells. */
@@ -156,9 +164,11 @@ int tc_quick_assign_device(const double* centers, int npatch, const double* x,
 int tc_select_patch_device(int patch, const double* centers, int npatch, const double* x,
                            const double* y, const double* z, int64_t n, int64_t* use);
 
-/* Corr construction: replaces BuildCorr2 (src/Corr2.cpp:842-864) for the NN, KK and GG
- * classes (pybind11 at src/Corr2.cpp:1177-1199).  d1, d2: TC_NDATA/TC_KDATA/TC_GDATA with
- * d1 == d2.  xi0..xi3 may be NULL when unused (NN: all; KK: xi1..xi3).  Only
+/* Corr construction: replaces BuildCorr2 (src/Corr2.cpp:842-864) for the 18 classes of
+ * src/Corr2.cpp:1204-1232: NN, NK, KK, and NX, KX, XX for X in Z, V, G, T, Q (d1 <= d2 as
+ * there).  xi arrays used: none (NN); xi0 (NK, KK); xi0, xi1 = real, imaginary (NX, KX;
+ * for NG and KG the tangential sign of DirectHelper<2>, src/Corr2.cpp:424-443); xi0..xi3 =
+ * xip, xip_im, xim, xim_im (XX); the others may be NULL.  Only
  * bin_type == TC_LOG is on the GPU path; minrpar/maxrpar/xp/yp/zp are accepted and
  * must be the defaults (no r_parallel cut, no period). */
 int tc_corr2_create(int d1, int d2, int bin_type, double minsep, double maxsep, int nbins,

@@ -17,7 +17,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _ROOT = os.path.dirname(_HERE)
 _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
 
-DTYPES = {"N": 0, "K": 1, "G": 2}
+DTYPES = {"N": 0, "K": 1, "G": 2, "Z": 3, "V": 4, "T": 5, "Q": 6}
 COORDS = {"flat": 1, "3d": 2, "spherical": 3}
 METRICS = {"Euclidean": 1, "Arc": 4}
 SPLITS = {"middle": 0, "median": 1, "mean": 2}
@@ -188,12 +188,18 @@ def minmax_size(metric, bins):
     return 0.0, 0.0
 
 
+def dpair(dtype):
+    """The correlation's two data kinds ("GG" or "G" for GG, "NG", ...) as d1 * 16 + d2."""
+    d1, d2 = (dtype[0], dtype[-1])
+    return DTYPES[d1] * 16 + DTYPES[d2]
+
+
 def process(dtype, metric, bins, f1, f2=None, quick=False, nthreads=0, rows=None):
     """Run the oracle's 2-point process; returns a dict of the 8 accumulated arrays."""
     nb = bins["nbins"]
     out = {k: np.zeros(nb) for k in ("xi0", "xi1", "xi2", "xi3", "meanr", "meanlogr",
                                       "weight", "npairs")}
-    args = [DTYPES[dtype], METRICS[metric], int(bool(quick)), bins["min_sep"], bins["max_sep"],
+    args = [dpair(dtype), METRICS[metric], int(bool(quick)), bins["min_sep"], bins["max_sep"],
             nb, bins["bin_size"], bins["b"], bins["a"]]
     ptrs = [_p(out[k]) for k in ("xi0", "xi1", "xi2", "xi3", "meanr", "meanlogr", "weight",
                                  "npairs")]

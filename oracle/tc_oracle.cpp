@@ -66,6 +66,7 @@ struct Node {
 
 struct Field {
     int dtype, coords;
+    int spin;        // complex data (Z, V, G, T, Q): 0, 1, 2, 3, 4
     double minsize, maxsize;
     int sm, brute, mintop, maxtop;
     std::vector<Pt> pts;
@@ -113,12 +114,32 @@ void build_cell_data(const Field& f, long start, long end, Node& nd)
     nd.n = end - start;
 }
 
-// calculate_expmsialpha<2>, include/ProjectHelper.h:45-47 (safe_norm 25-31).
-inline cd expmsialpha2(const cd& r)
+inline double safe_norm(const cd& z)
 {
-    double n = std::norm(r);
-    if (!(n > 0.)) n = 1.;
-    return std::conj(r * r) / n;
+    double n = std::norm(z);
+    return n > 0. ? n : 1.;
+}
+
+// calculate_expmsialpha<s>, include/ProjectHelper.h:33-60 (safe_norm 25-31): the spin-s
+// rotation exp(-i s alpha) of a direction r.
+inline cd expmsialpha(int s, const cd& r)
+{
+    switch (s) {
+      case 0: return cd(1., 0.);
+      case 1: return std::conj(r) / std::sqrt(safe_norm(r));
+      case 2: return std::conj(r * r) / safe_norm(r);
+      case 3: { cd r3 = r * r * r; return std::conj(r3) / std::sqrt(safe_norm(r3)); }
+      default: { cd r2 = r * r; return std::conj(r2 * r2) / safe_norm(r2); }
+    }
+}
+inline cd expmsialpha2(const cd& r) { return expmsialpha(2, r); }
+
+// The public data kinds (N, K, G, Z, V, T, Q = 0..6) as (payload kind, spin).
+inline int kind_of(int d) { return d <= 1 ? d : DG; }
+inline int spin_of(int d)
+{
+    static const int spin[7] = {0, 0, 2, 0, 1, 3, 4};
+    return (d >= 0 && d < 7) ? spin[d] : 0;
 }
 
 // finishAverages: SimpleSum (src/Cell.cpp:221-234) for Flat, ParallelTransportSum
@@ -154,7 +175,7 @@ void finish_averages(const Field& f, long start, long end, Node& nd)
                     double sinB = sinA;
                     double cosbeta = -cosA * cosB + sinA * sinB;
                     double sinbeta = sinA * cosB + cosA * sinB;
-                    sum += wz * expmsialpha2(cd(cosbeta, sinbeta));
+                    sum += wz * expmsialpha(f.spin, cd(cosbeta, sinbeta));
                 }
             }
         }
@@ -341,6 +362,7 @@ struct Accum {
 
 struct Params {
     int dtype, coords, metric, quick, nbins;
+    int k1, k2, s1, s2;   // payload kind (DN/DK/DG) and spin of the two fields
     double minsep, maxsep, binsize, b, a;
     double logminsep, halfminsep, minsepsq, maxsepsq, bsq, asq;
 };
@@ -370,7 +392,18 @@ inline cd calc_direction(double x1, double y1, double z1, double x2, double y2, 
     return cd(sinA, -cosA);
 }
 
-// Corr2::finishProcess + DirectHelper<0,1,3>, src/Corr2.cpp:394-566.
+// The direction term of a spin-s value at c2 (ProjectHelper<C>::Project, one value):
+// Flat: r = p2 - p1 (include/ProjectHelper.h:108-114); Sphere: the direction at p2
+// (370-376); ThreeD: the same on the normalised positions (561-569).
+inline cd project_one(const Params& P, int s, const Node& c1, const Node& c2)
+{
+    if (P.coords == FLAT) return expmsialpha(s, cd(c2.x - c1.x, c2.y - c1.y));
+    double x1 = c1.x, y1 = c1.y, z1 = c1.z, x2 = c2.x, y2 = c2.y, z2 = c2.z;
+    if (P.coords == THREED) { normalize3(x1, y1, z1); normalize3(x2, y2, z2); }
+    return expmsialpha(s, calc_direction(x1, y1, z1, x2, y2, z2));
+}
+
+// Corr2::finishProcess + DirectHelper<0..3>, src/Corr2.cpp:394-566.
 void finish_process(const Params& P, const Node& c1, const Node& c2, double r, double logr,
                     int k, Accum& A)
 {
@@ -381,22 +414,35 @@ void finish_process(const Params& P, const Node& c1, const Node& c2, double r, d
         A.meanr[k] += ww * r;
         A.meanlogr[k] += ww * logr;
     }
-    if (P.dtype == DK) {
-        A.xi0[k] += double(c1.d1) * double(c2.d1);
-    } else if (P.dtype == DG) {
+    // getWK: w for N, w k for K (include/ProjectHelper.h:73-79).
+    auto wk = [](const Node& c, int kind) { return kind == DN ? double(c.w) : double(c.d1); };
+    if (P.k1 == DN && P.k2 == DN) return;
+    if (P.k2 != DG) {
+        // DirectHelper<1>: NK, KK.
+        A.xi0[k] += wk(c1, P.k1) * wk(c2, P.k2);
+    } else if (P.k1 != DG) {
+        // DirectHelper<2>: the spin-s value at c2 projected to the line of the pair, times
+        // -wk1 for G (tangential shear) and wk1 otherwise.
+        cd g2(c2.d1, c2.d2);
+        g2 *= project_one(P, P.s2, c1, c2);
+        g2 *= (P.s2 == 2 ? -1. : 1.) * wk(c1, P.k1);
+        A.xi0[k] += g2.real();
+        A.xi1[k] += g2.imag();
+    } else {
+        // DirectHelper<3>: both values projected, then both_complex_prod(g2, g1).
         cd g1(c1.d1, c1.d2), g2(c2.d1, c2.d2);
         if (P.coords == FLAT) {
             // ProjectHelper<Flat>::Project, include/ProjectHelper.h:126-136.
-            cd r12(c2.x - c1.x, c2.y - c1.y);
-            cd e = expmsialpha2(r12);
+            cd e = expmsialpha(P.s1, cd(c2.x - c1.x, c2.y - c1.y));
             g1 *= e; g2 *= e;
         } else {
             // ProjectHelper<Sphere>::Project(c1,c2,z1,z2), include/ProjectHelper.h:370-388;
             // ThreeD first normalises both positions (include/ProjectHelper.h:570-584).
             double x1 = c1.x, y1 = c1.y, z1 = c1.z, x2 = c2.x, y2 = c2.y, z2 = c2.z;
             if (P.coords == THREED) { normalize3(x1, y1, z1); normalize3(x2, y2, z2); }
-            g2 *= expmsialpha2(calc_direction(x1, y1, z1, x2, y2, z2));
-            g1 *= expmsialpha2(calc_direction(x2, y2, z2, x1, y1, z1));
+            g2 *= expmsialpha(P.s2, calc_direction(x1, y1, z1, x2, y2, z2));
+            g1 *= expmsialpha(P.s1, calc_direction(x2, y2, z2, x1, y1, z1));
+            if (P.s1 == 1 || P.s1 == 3) g1 = -g1;
         }
         // both_complex_prod(g2, g1), include/ProjectHelper.h:84-101.
         double z1rz2r = g2.real() * g1.real();
@@ -521,11 +567,15 @@ void add_into(const Accum& A, double* xi0, double* xi1, double* xi2, double* xi3
     }
 }
 
-Params make_params(int dtype, int coords, int metric, int quick, double minsep, double maxsep,
+// dpair: the two public data kinds as d1 * 16 + d2.
+Params make_params(int dpair, int coords, int metric, int quick, double minsep, double maxsep,
                    int nbins, double binsize, double b, double a)
 {
     Params P;
-    P.dtype = dtype; P.coords = coords; P.metric = metric; P.quick = quick; P.nbins = nbins;
+    const int d1 = dpair >> 4, d2 = dpair & 15;
+    P.dtype = kind_of(d1);
+    P.k1 = kind_of(d1); P.k2 = kind_of(d2); P.s1 = spin_of(d1); P.s2 = spin_of(d2);
+    P.coords = coords; P.metric = metric; P.quick = quick; P.nbins = nbins;
     P.minsep = minsep; P.maxsep = maxsep; P.binsize = binsize; P.b = b; P.a = a;
     // BaseCorr2 constructor, src/Corr2.cpp:55-80.
     P.logminsep = std::log(minsep);
@@ -1062,6 +1112,8 @@ void* orc_field_build(int dtype, int coords, const double* x, const double* y, c
                       int maxtop)
 {
     Field* f = new Field();
+    f->spin = spin_of(dtype);
+    dtype = kind_of(dtype);
     f->dtype = dtype; f->coords = coords; f->minsize = minsize; f->maxsize = maxsize;
     f->sm = sm; f->brute = brute; f->mintop = mintop; f->maxtop = maxtop; f->built = false;
     f->pts.resize(n);
@@ -1253,8 +1305,8 @@ int orc_corr3_multipole_auto(int metric, int quick, double minsep, double maxsep
                              double* meanlogd3, double* weight, double* weight_im, double* ntri)
 {
     Field* f = static_cast<Field*>(h);
-    if (f->dtype != DG) return 1;
-    Params P = make_params(DG, f->coords, metric, quick, minsep, maxsep, nbins, binsize, b, a);
+    if (f->dtype != DG || f->spin != 2) return 1;
+    Params P = make_params(DG * 16 + DG, f->coords, metric, quick, minsep, maxsep, nbins, binsize, b, a);
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #else

@@ -85,7 +85,41 @@ CASES = {
     "kk_sphere_arc":    ("K", "spherical", "Arc", "sphere", 3000, 0, 2. * ARCMIN, 60. * ARCMIN, 10, 1.0, 1.0, "mean", False, 3, 10),
     "gg_3d":            ("G", "3d", "Euclidean", "threed", 3000, 0, 1., 30., 10, 1.0, 0.1, "mean", False, 3, 10),
     "nn_3d":            ("N", "3d", "Euclidean", "threed", 3000, 0, 1., 30., 10, 0.5, 0.1, "mean", False, 3, 10),
+    # The other 2-point classes (src/Corr2.cpp:1204-1232): a two-letter dtype is (d1, d2) of
+    # a cross correlation; Z, V, T, Q fields take the complex columns (g1, g2).
+    "nk_flat_cross":    ("NK", "flat", "Euclidean", "flat", 2000, 2500, 1., 20., 10, 1.0, 0.1, "mean", False, 3, 10),
+    "ng_flat_cross":    ("NG", "flat", "Euclidean", "flat", 2500, 3000, 1., 20., 10, 0.5, 0.1, "mean", False, 3, 10),
+    "kg_sphere_cross":  ("KG", "spherical", "Arc", "sphere", 2000, 2500, 2. * ARCMIN, 60. * ARCMIN, 10, 0.5, 0.1, "mean", False, 3, 10),
+    "ng_sphere_bs0":    ("NG", "spherical", "Arc", "sphere", 1200, 1500, 2. * ARCMIN, 60. * ARCMIN, 8, 0.0, 0.1, "mean", False, 3, 10),
+    "nz_flat_cross":    ("NZ", "flat", "Euclidean", "flat", 2000, 2500, 1., 20., 10, 1.0, 0.1, "mean", False, 3, 10),
+    "kv_sphere_cross":  ("KV", "spherical", "Arc", "sphere", 2000, 2500, 2. * ARCMIN, 60. * ARCMIN, 10, 0.5, 0.1, "mean", False, 3, 10),
+    "nt_3d_cross":      ("NT", "3d", "Euclidean", "threed", 2000, 2500, 1., 30., 10, 1.0, 0.1, "mean", False, 3, 10),
+    "kq_flat_cross":    ("KQ", "flat", "Euclidean", "flat", 2000, 2500, 1., 20., 10, 1.0, 0.1, "mean", False, 3, 10),
+    "zz_sphere":        ("Z", "spherical", "Arc", "sphere", 2500, 0, 2. * ARCMIN, 60. * ARCMIN, 10, 0.5, 0.1, "mean", False, 3, 10),
+    "vv_flat":          ("V", "flat", "Euclidean", "flat", 2500, 0, 1., 20., 10, 1.0, 0.1, "mean", False, 3, 10),
+    "vv_sphere":        ("V", "spherical", "Arc", "sphere", 2500, 0, 2. * ARCMIN, 60. * ARCMIN, 10, 0.5, 0.1, "mean", False, 3, 10),
+    "tt_sphere":        ("T", "spherical", "Arc", "sphere", 2500, 0, 2. * ARCMIN, 60. * ARCMIN, 10, 0.5, 0.1, "mean", False, 3, 10),
+    "qq_flat":          ("Q", "flat", "Euclidean", "flat", 2500, 0, 1., 20., 10, 1.0, 0.1, "mean", False, 3, 10),
+    "qq_3d":            ("Q", "3d", "Euclidean", "threed", 2500, 0, 1., 30., 10, 1.0, 0.1, "mean", False, 3, 10),
+    "tt_flat_cross":    ("T", "flat", "Euclidean", "flat", 2000, 2500, 1., 20., 10, 0.5, 0.1, "mean", False, 3, 10),
 }
+
+
+def kinds(dtype):
+    """(d1, d2) data kinds of a case's dtype ("G" -> ("G", "G"), "NG" -> ("N", "G"))."""
+    return dtype[0], dtype[-1]
+
+
+def xi_count(dtype):
+    """Number of xi arrays the reference's Corr2<D1,D2> fills (XiData, include/Corr2.h)."""
+    d1, d2 = kinds(dtype)
+    if d1 == "N" and d2 == "N":
+        return 0
+    if d2 in "NK":
+        return 1
+    if d1 in "NK":
+        return 2
+    return 4
 
 
 def make_inputs(name, seed=8675309):

@@ -19,7 +19,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, HERE)
-from cases import CASES, make_inputs, spec_dict  # noqa: E402
+from cases import CASES, kinds, make_inputs, spec_dict, xi_count  # noqa: E402
 
 so = glob.glob(os.path.join(ROOT, "oracle", "_ref", "_treecorr*.so"))
 if not so:
@@ -39,7 +39,7 @@ def build_field(dtype, coords, cat, min_size, max_size, split, brute, min_top, m
     args = [cat["x"], cat["y"], z]
     if dtype == "K":
         args += [cat["k"]]
-    elif dtype == "G":
+    elif dtype in "ZVGTQ":
         args += [cat["g1"], cat["g2"]]
     args += [cat["w"], empty, min_size, max_size, SPLIT[split], 0, brute, min_top, max_top]
     return cls(*args)
@@ -63,21 +63,19 @@ def run_case(name):
     out = {k: np.zeros(nb) for k in ("xi0", "xi1", "xi2", "xi3", "meanr", "meanlogr",
                                       "weight", "npairs")}
     e = np.array([])
-    xi = [out["xi0"], out["xi1"], out["xi2"], out["xi3"]]
-    if s["dtype"] == "N":
-        xi = [e, e, e, e]
-    elif s["dtype"] == "K":
-        xi = [out["xi0"], e, e, e]
-    corr = getattr(_treecorr, s["dtype"] * 2 + "Corr")(
+    d1, d2 = kinds(s["dtype"])
+    nxi = xi_count(s["dtype"])
+    xi = [out["xi%d" % i] if i < nxi else e for i in range(4)]
+    corr = getattr(_treecorr, d1 + d2 + "Corr")(
         _treecorr.Log, s["min_sep"], s["max_sep"], nb, bin_size, b, a,
         -sys.float_info.max, sys.float_info.max, 0., 0., 0.,
         xi[0], xi[1], xi[2], xi[3], out["meanr"], out["meanlogr"], out["weight"], out["npairs"])
-    f1 = build_field(s["dtype"], s["coords"], cat1, min_size, max_size, s["split"], s["brute"],
+    f1 = build_field(d1, s["coords"], cat1, min_size, max_size, s["split"], s["brute"],
                      s["min_top"], s["max_top"])
     if cat2 is None:
         corr.processAuto(f1, False, False, METRIC[s["metric"]])
     else:
-        f2 = build_field(s["dtype"], s["coords"], cat2, min_size, max_size, s["split"],
+        f2 = build_field(d2, s["coords"], cat2, min_size, max_size, s["split"],
                          s["brute"], s["min_top"], s["max_top"])
         corr.processCross(f1, f2, False, False, METRIC[s["metric"]])
     save = dict(min_size=min_size, max_size=max_size, bin_size=bin_size, b=b, a=a,

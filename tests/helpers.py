@@ -4,7 +4,7 @@ import sys
 
 import numpy as np
 
-from cases import CASES, spec_dict  # noqa: F401  (tests/golden on sys.path)
+from cases import CASES, kinds, spec_dict, xi_count  # noqa: F401  (tests/golden on sys.path)
 
 OUT_KEYS = ("xi0", "xi1", "xi2", "xi3", "meanr", "meanlogr", "weight", "npairs")
 COORD_NAME = {"flat": "Flat", "spherical": "Sphere", "3d": "ThreeD"}
@@ -24,7 +24,7 @@ def load_case(name):
 
 
 def field_args(dtype, cat):
-    if dtype == "G":
+    if dtype in "ZVGTQ":
         return [cat["g1"], cat["g2"]]
     if dtype == "K":
         return [cat["k"]]
@@ -42,15 +42,14 @@ def gpu_field(T, dtype, coords, cat, min_size, max_size, split="mean", brute=Fal
 
 
 def gpu_process(T, dtype, metric, bins, f1, f2=None, quick=False):
+    """dtype: "G" (GG) or a pair such as "NG"; the class is d1 + d2 + "Corr"."""
     nb = bins["nbins"]
     out = {k: np.zeros(nb) for k in OUT_KEYS}
     e = np.array([])
-    xi = [out["xi0"], out["xi1"], out["xi2"], out["xi3"]]
-    if dtype == "N":
-        xi = [e, e, e, e]
-    elif dtype == "K":
-        xi = [out["xi0"], e, e, e]
-    corr = getattr(T, dtype * 2 + "Corr")(T.Log, bins["min_sep"], bins["max_sep"], nb,
+    nxi = xi_count(dtype)
+    xi = [out["xi%d" % i] if i < nxi else e for i in range(4)]
+    d1, d2 = kinds(dtype)
+    corr = getattr(T, d1 + d2 + "Corr")(T.Log, bins["min_sep"], bins["max_sep"], nb,
                                           bins["bin_size"], bins["b"], bins["a"],
                                           -sys.float_info.max, sys.float_info.max, 0., 0., 0.,
                                           *xi, out["meanr"], out["meanlogr"], out["weight"],
@@ -82,11 +81,7 @@ def assert_outputs_close(got, ref, dtype, rtol=1e-5, exact_npairs=True, label=""
     if exact_npairs:
         assert np.array_equal(got["npairs"], ref["npairs"]), \
             f"{label} npairs differ: {got['npairs'] - ref['npairs']}"
-    keys = ["weight", "meanr", "meanlogr"]
-    if dtype == "K":
-        keys += ["xi0"]
-    if dtype == "G":
-        keys += ["xi0", "xi1", "xi2", "xi3"]
+    keys = ["weight", "meanr", "meanlogr"] + ["xi%d" % i for i in range(xi_count(dtype))]
     for k in keys:
         r = np.asarray(ref[k])
         g = np.asarray(got[k])
@@ -97,3 +92,16 @@ def assert_outputs_close(got, ref, dtype, rtol=1e-5, exact_npairs=True, label=""
             scale = max(scale, 1e-3 * np.abs(ref["weight"]).max())
         err = np.abs(g - r).max() / max(scale, 1e-300)
         assert err <= rtol, f"{label} {k}: max rel err {err:.3e} > {rtol:g}\n got {g}\n ref {r}"
+
+
+def case_fields(make, s, c1, c2, min_size, max_size):
+    """The case's two fields built by make(dtype, coords, cat, ...) (GPU or oracle); the
+    second is None for an auto correlation."""
+    d1, d2 = kinds(s["dtype"])
+    f1 = make(d1, s["coords"], c1, min_size, max_size, s["split"], s["brute"], s["min_top"],
+              s["max_top"])
+    f2 = None
+    if c2 is not None:
+        f2 = make(d2, s["coords"], c2, min_size, max_size, s["split"], s["brute"],
+                  s["min_top"], s["max_top"])
+    return f1, f2

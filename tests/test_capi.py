@@ -40,9 +40,13 @@ def test_python_mirror_matches_reference_names():
     """The mirror exports the reference module's names on this path, with its enum values
     (src/Corr2.cpp:1204-1234, include/Position.h:24, Metric.h:29, Cell.h:26, BinType.h:36)."""
     from treecorr_gb300 import _treecorr as T
-    for n in ("NFieldFlat", "NFieldSphere", "NFieldThreeD", "KFieldFlat", "KFieldSphere",
-              "KFieldThreeD", "GFieldFlat", "GFieldSphere", "GFieldThreeD", "NNCorr", "KKCorr",
-              "GGCorr", "BaseCorr2", "SetOMPThreads", "GetOMPThreads"):
+    for d in "NKZVGTQ":
+        for c in ("Flat", "Sphere", "ThreeD"):
+            assert hasattr(T, d + "Field" + c), d + "Field" + c
+    classes = ["NN", "NK", "KK"] + [a + x for x in "ZVGTQ" for a in ("N", "K", x)]
+    for n in [c + "Corr" for c in classes] + ["BaseCorr2", "GGGCorr", "SetOMPThreads",
+                                               "GetOMPThreads", "QuickAssign", "SelectPatch",
+                                               "GenerateXYZ"]:
         assert hasattr(T, n), n
     assert (int(T.Flat), int(T.ThreeD), int(T.Sphere)) == (1, 2, 3)
     assert (int(T.Euclidean), int(T.Rperp), int(T.Rlens), int(T.Arc), int(T.OldRperp),
@@ -51,4 +55,4 @@ def test_python_mirror_matches_reference_names():
     assert (int(T.Log), int(T.Linear), int(T.TwoD), int(T.LogRUV), int(T.LogSAS),
             int(T.LogMultipole)) == (0, 1, 2, 3, 4, 5)
     with pytest.raises(NotImplementedError):
-        T.NGCorr()
+        T.NNNCorr()

@@ -14,12 +14,7 @@ RTOL = 1e-5
 
 def _run_case(T, name):
     s, c1, c2, bins, min_size, max_size, ref = H.load_case(name)
-    f1 = H.gpu_field(T, s["dtype"], s["coords"], c1, min_size, max_size, s["split"], s["brute"],
-                     s["min_top"], s["max_top"])
-    f2 = None
-    if c2 is not None:
-        f2 = H.gpu_field(T, s["dtype"], s["coords"], c2, min_size, max_size, s["split"],
-                         s["brute"], s["min_top"], s["max_top"])
+    f1, f2 = H.case_fields(lambda *a: H.gpu_field(T, *a), s, c1, c2, min_size, max_size)
     got = H.gpu_process(T, s["dtype"], s["metric"], bins, f1, f2)
     return s, got, ref, f1
 
@@ -31,7 +26,8 @@ def test_golden(gpu_lib, name):
 
 
 @pytest.mark.parametrize("name", ["gg_flat_bs1", "gg_sphere_arc", "nn_3d", "gg_flat_middle",
-                                  "gg_flat_median", "gg_flat_clumped"])
+                                  "gg_flat_median", "gg_flat_clumped", "vv_sphere", "tt_sphere",
+                                  "qq_3d", "zz_sphere"])
 def test_tree_matches_oracle(gpu_lib, name):
     """Same cells (membership, centre, size, weight, payload) as the reference rules."""
     s, c1, c2, bins, min_size, max_size, ref = H.load_case(name)
@@ -106,6 +102,41 @@ def test_larger_sphere_arc_vs_oracle(gpu_lib):
     got = H.gpu_process(T, "G", "Arc", bins, H.gpu_field(T, "G", "spherical", cat, 0., 0.))
     ref = H.oracle_process("G", "Arc", bins, H.oracle_field("G", "spherical", cat, 0., 0.))
     H.assert_outputs_close(got, ref, "G", rtol=RTOL, label="sphere30k")
+
+
+@pytest.mark.parametrize("pair,geom", [("NG", "spherical"), ("KV", "flat"), ("TT", "3d"),
+                                       ("QQ", "spherical"), ("NK", "spherical"),
+                                       ("KZ", "3d")])
+def test_other_classes_vs_oracle(gpu_lib, pair, geom):
+    """The mixed and spin-s classes on 20-30K-point catalogs (cross for mixed kinds, auto for
+    XX): GPU vs oracle."""
+    from cases import threed_catalog
+    T = gpu_lib
+    rng = np.random.default_rng(sum(map(ord, pair + geom)))
+    if geom == "spherical":
+        mk = lambda n: sphere_catalog(rng, n, radius_deg=3.0)   # noqa: E731
+        lo, hi, metric = np.radians(1. / 60), np.radians(60. / 60), "Arc"
+    elif geom == "flat":
+        mk = lambda n: flat_catalog(rng, n, L=600.)   # noqa: E731
+        lo, hi, metric = 1., 60., "Euclidean"
+    else:
+        mk = lambda n: threed_catalog(rng, n, L=300.)   # noqa: E731
+        lo, hi, metric = 1., 60., "Euclidean"
+    nb = 12
+    bsz = np.log(hi / lo) / nb
+    bins = dict(min_sep=lo, max_sep=hi, nbins=nb, bin_size=bsz, b=0.2 * bsz, a=0.1)
+    mn, mx = (0., 0.) if metric == "Arc" else (lo * 0.02 / 2.06, hi * 0.02)
+    d1, d2 = pair[0], pair[1]
+    c1 = mk(20000)
+    c2 = mk(25000) if d1 != d2 else None
+    g1 = H.gpu_field(T, d1, geom, c1, mn, mx)
+    o1 = H.oracle_field(d1, geom, c1, mn, mx)
+    g2 = H.gpu_field(T, d2, geom, c2, mn, mx) if c2 is not None else None
+    o2 = H.oracle_field(d2, geom, c2, mn, mx) if c2 is not None else None
+    dt = pair if d1 != d2 else d1
+    got = H.gpu_process(T, dt, metric, bins, g1, g2)
+    ref = H.oracle_process(dt, metric, bins, o1, o2)
+    H.assert_outputs_close(got, ref, dt, rtol=RTOL, label=f"{pair} {geom}")
 
 
 def test_quick_mode(gpu_lib):

@@ -9,12 +9,7 @@ from cases import CASES
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_oracle_matches_reference(name):
     s, c1, c2, bins, min_size, max_size, ref = H.load_case(name)
-    f1 = H.oracle_field(s["dtype"], s["coords"], c1, min_size, max_size, s["split"], s["brute"],
-                        s["min_top"], s["max_top"])
-    f2 = None
-    if c2 is not None:
-        f2 = H.oracle_field(s["dtype"], s["coords"], c2, min_size, max_size, s["split"],
-                            s["brute"], s["min_top"], s["max_top"])
+    f1, f2 = H.case_fields(H.oracle_field, s, c1, c2, min_size, max_size)
     out = H.oracle_process(s["dtype"], s["metric"], bins, f1, f2, nthreads=1)
     assert np.array_equal(out["npairs"], ref["npairs"])
     for k in H.OUT_KEYS:

@@ -362,16 +362,12 @@ def _field_class(name, dkind, coords):
                                        "_coords": coords, "__module__": __name__})
 
 
-# BuildNField / BuildKField / BuildGField (src/Field.cpp:430-546)
-NFieldFlat = _field_class("NFieldFlat", 0, Coord.Flat)
-NFieldSphere = _field_class("NFieldSphere", 0, Coord.Sphere)
-NFieldThreeD = _field_class("NFieldThreeD", 0, Coord.ThreeD)
-KFieldFlat = _field_class("KFieldFlat", 1, Coord.Flat)
-KFieldSphere = _field_class("KFieldSphere", 1, Coord.Sphere)
-KFieldThreeD = _field_class("KFieldThreeD", 1, Coord.ThreeD)
-GFieldFlat = _field_class("GFieldFlat", 2, Coord.Flat)
-GFieldSphere = _field_class("GFieldSphere", 2, Coord.Sphere)
-GFieldThreeD = _field_class("GFieldThreeD", 2, Coord.ThreeD)
+# BuildNField / BuildKField / BuildZField / BuildVField / BuildGField / BuildTField /
+# BuildQField (src/Field.cpp:430-560): {N,K,Z,V,G,T,Q}Field{Flat,Sphere,ThreeD}.
+for _d, _k in (("N", 0), ("K", 1), ("G", 2), ("Z", 3), ("V", 4), ("T", 5), ("Q", 6)):
+    for _c in ("Flat", "Sphere", "ThreeD"):
+        globals()[_d + "Field" + _c] = _field_class(_d + "Field" + _c, _k, getattr(Coord, _c))
+del _d, _k, _c
 
 
 class DeviceField(_FieldBase):
@@ -499,6 +495,7 @@ def stream_handle():
 class BaseCorr2:
     """BaseCorr2 (src/Corr2.cpp:1168-1175): processAuto, processCross, triviallyZero."""
     _dkind = 0
+    _dkind2 = None      # the second field's kind when it differs (NK, NG, ...)
 
     def __init__(self, bin_type, minsep, maxsep, nbins, binsize, b, a, minrpar, maxrpar, xp,
                  yp, zp, xi0, xi1, xi2, xi3, meanr, meanlogr, weight, npairs):
@@ -519,7 +516,8 @@ class BaseCorr2:
         self._outs = outs
         self._nbins = int(nbins)
         h = ctypes.c_void_p()
-        _check(lib().tc_corr2_create(self._dkind, self._dkind, int(bin_type), float(minsep),
+        d2 = self._dkind if self._dkind2 is None else self._dkind2
+        _check(lib().tc_corr2_create(self._dkind, d2, int(bin_type), float(minsep),
                                      float(maxsep), int(nbins), float(binsize), float(b),
                                      float(a), float(minrpar), float(maxrpar), float(xp),
                                      float(yp), float(zp), *[_ptr(o) for o in outs],
@@ -600,16 +598,23 @@ class BaseCorr2:
         return {k: getattr(s, k) for k, _ in tc_stats._fields_}
 
 
-class NNCorr(BaseCorr2):
-    _dkind = 0
+# The 2-point classes of src/Corr2.cpp:1204-1232 (WrapCorr2<D1,D2>): NN, NK, KK and NX, KX,
+# XX for the complex kinds X = Z, V, G, T, Q (data kind numbers of include/tcgpu.h).
+_DKIND = {"N": 0, "K": 1, "G": 2, "Z": 3, "V": 4, "T": 5, "Q": 6}
 
 
-class KKCorr(BaseCorr2):
-    _dkind = 1
+def _corr2_class(d1, d2):
+    return type(d1 + d2 + "Corr", (BaseCorr2,),
+                {"_dkind": _DKIND[d1], "_dkind2": _DKIND[d2], "__module__": __name__})
 
 
-class GGCorr(BaseCorr2):
-    _dkind = 2
+NNCorr = _corr2_class("N", "N")
+NKCorr = _corr2_class("N", "K")
+KKCorr = _corr2_class("K", "K")
+for _x in "ZVGTQ":
+    for _a in ("N", "K", _x):
+        globals()[_a + _x + "Corr"] = _corr2_class(_a, _x)
+del _x, _a
 
 
 class BaseCorr3:
@@ -681,11 +686,13 @@ def _not_on_path(name):
     return f
 
 
-# Correlation classes of the reference that are outside this hot path.
-for _n in ("NKCorr", "NZCorr", "KZCorr", "ZZCorr", "NVCorr", "KVCorr", "VVCorr", "NGCorr",
-           "KGCorr", "NTCorr", "KTCorr", "TTCorr", "NQCorr", "KQCorr", "QQCorr"):
-    globals()[_n] = _not_on_path(_n)
+# The 3-point classes of src/Corr3.cpp (WrapCorr3) other than GGG with LogMultipole.
+for _n in ("NNN", "KKK", "NNK", "NKN", "KNN", "NKK", "KNK", "KKN", "NNG", "NGN", "GNN", "NGG",
+           "GNG", "GGN", "KKG", "KGK", "GKK", "KGG", "GKG", "GGK"):
+    globals()[_n + "Corr"] = _not_on_path(_n + "Corr")
 del _n
+
+
 
 
 def _assign_args(cenp, npatch, xp, yp, zp, out):

@@ -262,7 +262,8 @@ int field_build(tc_field* f)
     TC_CU(cudaEventCreate(&e1));
     TC_CU(cudaEventRecord(e0, st));
     BuildParams BP;
-    BP.coords = f->coords; BP.dkind = f->dkind; BP.split = f->split; BP.brute = f->brute;
+    BP.coords = f->coords; BP.dkind = kind_of(f->dkind); BP.spin = spin_of(f->dkind);
+    BP.split = f->split; BP.brute = f->brute;
     BP.minsizesq = f->minsize * f->minsize;
     BP.maxsizesq = f->maxsize * f->maxsize;
     BP.n = (int)n;
@@ -299,7 +300,7 @@ int field_create_impl(int dkind, int coords, const double* x, const double* y, c
         set_last_error("n out of range for the GPU path (0 <= n < 2^30)");
         return TC_ERR_ARG;
     }
-    if (dkind < TC_NDATA || dkind > TC_GDATA) { set_last_error("bad data kind"); return TC_ERR_ARG; }
+    if (dkind < TC_NDATA || dkind > TC_QDATA) { set_last_error("bad data kind"); return TC_ERR_ARG; }
     if (coords != TC_FLAT && coords != TC_THREED && coords != TC_SPHERE) {
         set_last_error("bad coords"); return TC_ERR_ARG;
     }
@@ -311,7 +312,7 @@ int field_create_impl(int dkind, int coords, const double* x, const double* y, c
         set_last_error("bad split_method"); return TC_ERR_ARG;
     }
     if (n > 0 && (!x || !y || !w || (coords != TC_FLAT && !z) || (dkind >= TC_KDATA && !d1) ||
-                  (dkind == TC_GDATA && !d2))) {
+                  (kind_of(dkind) == DG && !d2))) {
         set_last_error("missing input array"); return TC_ERR_ARG;
     }
     tc_field* f = new tc_field();
@@ -351,10 +352,11 @@ int field_create_impl(int dkind, int coords, const double* x, const double* y, c
         } else {
             for (int k = 0; k < 7; ++k) dsrc[k] = src[k];
         }
-        launch_prepare((int)n, coords, dkind, dsrc[0], dsrc[1], dsrc[2], dsrc[3], dsrc[4], dsrc[5],
-                       dsrc[6], f->buf[0], st);
+        launch_prepare((int)n, coords, kind_of(dkind), dsrc[0], dsrc[1], dsrc[2], dsrc[3], dsrc[4],
+                       dsrc[5], dsrc[6], f->buf[0], st);
         BuildParams BP;
-        BP.coords = coords; BP.dkind = dkind; BP.split = split_method; BP.brute = f->brute;
+        BP.coords = coords; BP.dkind = kind_of(dkind); BP.spin = spin_of(dkind);
+        BP.split = split_method; BP.brute = f->brute;
         BP.minsizesq = 0.; BP.maxsizesq = 0.; BP.n = (int)n;
         rc = field_center(BP, f->buf[0], f->S, st, f->center);
         if (staging) { cudaStreamSynchronize(st); dfree(staging); }
@@ -456,12 +458,32 @@ int check_metric(int coords, int metric)
     return TC_ERR_UNSUPPORTED;
 }
 
+// Number of xi arrays of Corr2<D1,D2> (XiData, include/Corr2.h:225-330): none for NN, one
+// for NK/KK, two (real, imaginary) for N or K with a complex kind, four for XX.
+int xi_count(int d1, int d2)
+{
+    if (d1 == TC_NDATA && d2 == TC_NDATA) return 0;
+    if (kind_of(d2) != DG) return 1;
+    if (kind_of(d1) != DG) return 2;
+    return 4;
+}
+
+// Adds bin k of the reduced xi sums (quantities 3.. of tot, nb bins each) into the outputs.
+void add_xi(tc_corr2* c, const double* tot, int nb, int k)
+{
+    double* xi[4] = {c->xi0, c->xi1, c->xi2, c->xi3};
+    const int nxi = xi_count(c->d1, c->d2);
+    for (int q = 0; q < nxi; ++q)
+        if (xi[q]) xi[q][k] += tot[(3 + q) * nb + k];
+}
+
 // The binning constants of a traversal (BaseCorr2 constructor, src/Corr2.cpp:55-80), in
 // FP64 and FP32.
 void trav_setup(const tc_corr2* c, TravParams& T, int coords, int metric, int quick, int nq)
 {
     std::memset(&T, 0, sizeof(T));
-    T.coords = coords; T.metric = metric; T.dkind = c->d1; T.quick = quick ? 1 : 0;
+    T.coords = coords; T.metric = metric; T.quick = quick ? 1 : 0;
+    T.k1 = kind_of(c->d1); T.k2 = kind_of(c->d2); T.s1 = spin_of(c->d1); T.s2 = spin_of(c->d2);
     T.nbins = c->nbins; T.nqf = nq;
     T.minsep = c->minsep; T.maxsep = c->maxsep; T.binsize = c->binsize; T.b = c->b; T.a = c->a;
     T.logminsep = std::log(c->minsep); T.halfminsep = 0.5 * c->minsep;
@@ -546,7 +568,7 @@ int expand_run(tc_corr2* c, const TravParams& T, int blocks, long long npoints, 
 int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
 {
     if (!c || !f1) { set_last_error("NULL argument"); return TC_ERR_ARG; }
-    if (c->d1 != f1->dkind || (f2 && c->d2 != f2->dkind)) {
+    if (c->d1 != f1->dkind || (f2 ? c->d2 != f2->dkind : c->d2 != f1->dkind)) {
         set_last_error("field data kind does not match the correlation"); return TC_ERR_ARG;
     }
     if (f2 && f2->coords != f1->coords) {
@@ -571,7 +593,7 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
     c->stats.build_ms = f1->build_ms + (f2 ? f2->build_ms : 0.f);
 
     const int nb = c->nbins;
-    const int nq = c->d1 == TC_GDATA ? 7 : (c->d1 == TC_KDATA ? 4 : 3);
+    const int nq = 3 + xi_count(c->d1, c->d2);
     TravParams T;
     trav_setup(c, T, f1->coords, metric, quick, nq);
     T.autoc = f2 ? 0 : 1;
@@ -654,14 +676,7 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
             c->meanlogr[k] += tot[2 * nb + k];
             c->npairs[k] += (double)totnp[k];
         }
-        if (c->d1 == TC_KDATA) {
-            if (c->xi0) c->xi0[k] += tot[3 * nb + k];
-        } else if (c->d1 == TC_GDATA) {
-            if (c->xi0) c->xi0[k] += tot[3 * nb + k];
-            if (c->xi1) c->xi1[k] += tot[4 * nb + k];
-            if (c->xi2) c->xi2[k] += tot[5 * nb + k];
-            if (c->xi3) c->xi3[k] += tot[6 * nb + k];
-        }
+        add_xi(c, tot.data(), nb, k);
     }
     return TC_OK;
 }
@@ -672,7 +687,7 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
 int corr_process_auto_noalloc(tc_corr2* c, tc_field* f, int quick, int metric)
 {
     if (!c || !f) { set_last_error("NULL argument"); return TC_ERR_ARG; }
-    if (c->d1 != f->dkind) {
+    if (c->d1 != f->dkind || c->d2 != f->dkind) {
         set_last_error("field data kind does not match the correlation"); return TC_ERR_ARG;
     }
     TC_TRY(check_metric(f->coords, metric));
@@ -694,10 +709,11 @@ int corr_process_auto_noalloc(tc_corr2* c, tc_field* f, int quick, int metric)
     unsigned char* B = static_cast<unsigned char*>(base);
 
     const int nb = c->nbins;
-    const int nq = c->d1 == TC_GDATA ? 7 : (c->d1 == TC_KDATA ? 4 : 3);
+    const int nq = 3 + xi_count(c->d1, c->d2);
     TravParams T;
     std::memset(&T, 0, sizeof(T));
-    T.coords = f->coords; T.metric = metric; T.dkind = c->d1; T.quick = quick ? 1 : 0;
+    T.coords = f->coords; T.metric = metric; T.quick = quick ? 1 : 0;
+    T.k1 = kind_of(c->d1); T.k2 = kind_of(c->d2); T.s1 = spin_of(c->d1); T.s2 = spin_of(c->d2);
     T.nbins = nb; T.autoc = 1; T.nqf = nq;
     T.minsep = c->minsep; T.maxsep = c->maxsep; T.binsize = c->binsize; T.b = c->b; T.a = c->a;
     T.logminsep = std::log(c->minsep); T.halfminsep = 0.5 * c->minsep;
@@ -795,14 +811,7 @@ int corr_process_auto_noalloc(tc_corr2* c, tc_field* f, int quick, int metric)
             c->meanlogr[k] += h_tot[2 * nb + k];
             c->npairs[k] += (double)h_np[k];
         }
-        if (c->d1 == TC_KDATA) {
-            if (c->xi0) c->xi0[k] += h_tot[3 * nb + k];
-        } else if (c->d1 == TC_GDATA) {
-            if (c->xi0) c->xi0[k] += h_tot[3 * nb + k];
-            if (c->xi1) c->xi1[k] += h_tot[4 * nb + k];
-            if (c->xi2) c->xi2[k] += h_tot[5 * nb + k];
-            if (c->xi3) c->xi3[k] += h_tot[6 * nb + k];
-        }
+        add_xi(c, h_tot, nb, k);
     }
     return TC_OK;
 }
@@ -1097,10 +1106,6 @@ int tc_corr2_create(int d1, int d2, int bin_type, double minsep, double maxsep, 
 {
     if (!out) { set_last_error("out is NULL"); return TC_ERR_ARG; }
     *out = nullptr;
-    if (d1 != d2 || d1 < TC_NDATA || d1 > TC_GDATA) {
-        set_last_error("only NN, KK and GG are on the GPU path");
-        return TC_ERR_UNSUPPORTED;
-    }
     if (bin_type != TC_LOG) {
         set_last_error("only Log binning is on the GPU path");
         return TC_ERR_UNSUPPORTED;
@@ -1114,8 +1119,16 @@ int tc_corr2_create(int d1, int d2, int bin_type, double minsep, double maxsep, 
         set_last_error("invalid binning");
         return TC_ERR_ARG;
     }
-    if (!meanr || !meanlogr || !weight || !npairs || (d1 == TC_KDATA && !xi0) ||
-        (d1 == TC_GDATA && (!xi0 || !xi1 || !xi2 || !xi3))) {
+    // The classes of src/Corr2.cpp:1204-1232: NN, NK, KK and, for every complex kind X,
+    // NX, KX and XX.
+    if (d1 < TC_NDATA || d1 > TC_QDATA || d2 < TC_NDATA || d2 > TC_QDATA ||
+        !(d1 == d2 || (d1 <= TC_KDATA && d2 > d1))) {
+        set_last_error("no correlation class for these data kinds");
+        return TC_ERR_ARG;
+    }
+    const int nxi = xi_count(d1, d2);
+    if (!meanr || !meanlogr || !weight || !npairs || (nxi >= 1 && !xi0) ||
+        (nxi >= 2 && !xi1) || (nxi >= 4 && (!xi2 || !xi3))) {
         set_last_error("missing output array");
         return TC_ERR_ARG;
     }
@@ -1214,7 +1227,8 @@ int tc_corr2_process_patches(tc_corr2* c, tc_field* const* fields, int npatch, i
     c->stats = tc_stats();
     const int coords = fields[0]->coords;
     for (int i = 0; i < npatch; ++i) {
-        if (!fields[i] || fields[i]->dkind != c->d1 || fields[i]->coords != coords) {
+        if (!fields[i] || fields[i]->dkind != c->d1 || c->d2 != c->d1 ||
+            fields[i]->coords != coords) {
             set_last_error("patch fields must exist and match the corr's data kind and coords");
             return TC_ERR_ARG;
         }
@@ -1251,7 +1265,7 @@ int tc_corr2_process_patches(tc_corr2* c, tc_field* const* fields, int npatch, i
     const int npair = (int)P1.size();
     if (npair > max_pairs) { set_last_error("more patch pairs than max_pairs"); return TC_ERR_ARG; }
     const int nb = c->nbins;
-    const int nq = c->d1 == TC_GDATA ? 7 : (c->d1 == TC_KDATA ? 4 : 3);
+    const int nq = 3 + xi_count(c->d1, c->d2);
     for (int p = 0; p < npair; ++p) { pair_i[p] = P1[p]; pair_j[p] = P2[p]; }
     std::fill(results, results + (size_t)npair * 8 * nb, 0.);
     *npairs_out = npair;

@@ -9,7 +9,15 @@ namespace tc {
 enum { FLAT = 1, THREED = 2, SPHERE = 3 };
 enum { EUCLIDEAN = 1, ARC = 4 };
 enum { MIDDLE = 0, MEDIAN = 1, MEAN = 2, RANDOM = 3 };
-enum { DN = 0, DK = 1, DG = 2 };
+enum { DN = 0, DK = 1, DG = 2 };   // payload: none, scalar, complex (Z, V, G, T, Q)
+
+// Public data kinds (TC_NDATA.. in include/tcgpu.h: N, K, G, Z, V, T, Q = 0..6) as the
+// payload kind and the spin of a complex value (include/ProjectHelper.h:63-71).
+__host__ __device__ inline int kind_of(int d) { return d <= 1 ? d : DG; }
+__host__ __device__ inline int spin_of(int d)
+{
+    return d == 2 ? 2 : d == 4 ? 1 : d == 5 ? 3 : d == 6 ? 4 : 0;
+}
 
 // Device status word: the first kernel error wins (atomicCAS from 0).
 enum DevErr : int {
@@ -70,6 +78,7 @@ struct BuildTask {
 
 struct BuildParams {
     int coords, dkind, split, brute;
+    int spin;          // complex payloads: the spin of the parallel transport
     double minsizesq, maxsizesq;
     int n;
 };

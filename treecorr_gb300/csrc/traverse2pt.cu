@@ -283,10 +283,42 @@ __device__ __forceinline__ void cmul(float ar, float ai, float br, float bi, flo
     ci = ar * bi + ai * br;
 }
 
-// GG projection for ThreeD coordinates in FP64 (positions normalised first,
-// include/ProjectHelper.h:570-584).
-__device__ void project3d64(const TravParams& T, int i, int j, float& g1r, float& g1i,
-                            float& g2r, float& g2i)
+// calculate_expmsialpha<s>(r) (include/ProjectHelper.h:33-60) in FP32: exp(-i s alpha) of
+// the direction r; 0 for r = 0 and s > 0 (safe_norm).
+__device__ __forceinline__ void expmsi(int s, float rx, float ry, float& er, float& ei)
+{
+    if (s == 2) { expm2i(rx, ry, er, ei); return; }
+    if (s == 0) { er = 1.f; ei = 0.f; return; }
+    const float n = rx * rx + ry * ry;
+    const float inv = n > 0.f ? rsqrtf(n) : 1.f;
+    const float ur = rx * inv, ui = -ry * inv;   // conj(r) / |r|
+    if (s == 1) { er = ur; ei = ui; return; }
+    const float u2r = ur * ur - ui * ui, u2i = 2.f * ur * ui;
+    if (s == 3) { cmul(u2r, u2i, ur, ui, er, ei); return; }
+    cmul(u2r, u2i, u2r, u2i, er, ei);
+}
+
+// The same in FP64 (ThreeD projections).
+__device__ void expmsi64(int s, double rx, double ry, double& er, double& ei)
+{
+    if (s == 0) { er = 1.; ei = 0.; return; }
+    double n = rx * rx + ry * ry;
+    if (!(n > 0.)) n = 1.;
+    if (s == 2) { er = (rx * rx - ry * ry) / n; ei = -2. * rx * ry / n; return; }
+    const double inv = 1. / sqrt(n);
+    const double ur = rx * inv, ui = -ry * inv;
+    if (s == 1) { er = ur; ei = ui; return; }
+    const double u2r = ur * ur - ui * ui, u2i = 2. * ur * ui;
+    if (s == 3) { er = u2r * ur - u2i * ui; ei = u2r * ui + u2i * ur; return; }
+    er = u2r * u2r - u2i * u2i; ei = 2. * u2r * u2i;
+}
+
+// Spin projections for ThreeD coordinates in FP64 (positions normalised first,
+// include/ProjectHelper.h:561-584): g2 by the direction at p2 with spin T.s2 and, when
+// both1, g1 by the direction at p1 with spin T.s1 (negated for odd spin,
+// include/ProjectHelper.h:386-387).
+__device__ void project3d64(const TravParams& T, int i, int j, bool both1, float& g1r,
+                            float& g1i, float& g2r, float& g2i)
 {
     double x1 = T.x1[i], y1 = T.y1[i], z1 = T.z1[i];
     double x2 = T.x2[j], y2 = T.y2[j], z2 = T.z2[j];
@@ -295,17 +327,17 @@ __device__ void project3d64(const TravParams& T, int i, int j, float& g1r, float
     if (n2 == 0.) { x2 = 1.; y2 = 0.; z2 = 0.; } else { x2 /= n2; y2 /= n2; z2 /= n2; }
     double dsq = (x1 - x2) * (x1 - x2) + (y1 - y2) * (y1 - y2) + (z1 - z2) * (z1 - z2);
     double ca = (z1 - z2) + 0.5 * z2 * dsq, sa = y1 * x2 - x1 * y2;   // direction at p2
-    double cb = (z2 - z1) + 0.5 * z1 * dsq, sb = y2 * x1 - x2 * y1;   // direction at p1
-    double ax = sa, ay = -ca, bx = sb, by = -cb;
-    double na = ax * ax + ay * ay, nb = bx * bx + by * by;
-    if (!(na > 0.)) na = 1.;
-    if (!(nb > 0.)) nb = 1.;
-    double e2r = (ax * ax - ay * ay) / na, e2i = -2. * ax * ay / na;
-    double e1r = (bx * bx - by * by) / nb, e1i = -2. * bx * by / nb;
+    double er, ei;
+    expmsi64(T.s2, sa, -ca, er, ei);
     double a = g2r, b = g2i;
-    g2r = float(a * e2r - b * e2i); g2i = float(a * e2i + b * e2r);
-    a = g1r; b = g1i;
-    g1r = float(a * e1r - b * e1i); g1i = float(a * e1i + b * e1r);
+    g2r = float(a * er - b * ei); g2i = float(a * ei + b * er);
+    if (both1) {
+        double cb = (z2 - z1) + 0.5 * z1 * dsq, sb = y2 * x1 - x2 * y1;   // direction at p1
+        expmsi64(T.s1, sb, -cb, er, ei);
+        if (T.s1 & 1) { er = -er; ei = -ei; }
+        a = g1r; b = g1i;
+        g1r = float(a * er - b * ei); g1i = float(a * ei + b * er);
+    }
 }
 
 // ---------------------------------------------------------------------------------------
@@ -457,39 +489,53 @@ __device__ __forceinline__ void accept_values(const TravParams& T, const TCell& 
     av[1] = ww * r;
     av[2] = ww * logr;
     acc_nn = (unsigned long long)__float_as_int(A.c.z) * (unsigned long long)__float_as_int(B.c.z);
-    if (T.dkind == DK) {
-        av[3] = A.c.x * B.c.x;
-    } else if (T.dkind == DG) {
-        float g1r = A.c.x, g1i = A.c.y, g2r = B.c.x, g2i = B.c.y;
-        if (flat) {
-            // ProjectHelper<Flat>::Project: r = p2 - p1 (ProjectHelper.h:126-136)
-            float er, ei;
-            expm2i(-dx, -dy, er, ei);
-            cmul(g1r, g1i, er, ei, g1r, g1i);
-            cmul(g2r, g2i, er, ei, g2r, g2i);
-        } else if (T.coords == SPHERE) {
-            // ProjectHelper<Sphere>::Project(c1,c2,z1,z2), ProjectHelper.h:370-388,
-            // with the direction terms written on accurate differences:
-            // y1*x2 - x1*y2 = x1*dy - y1*dx,  d = p1 - p2.
-            const float x1 = A.a.x, y1 = A.a.y, z1 = A.a.z, z2 = B.a.z;
-            const float sinA = x1 * dy - y1 * dx;
-            const float cosA = dz + 0.5f * z2 * dsq;
-            const float cosB = -dz + 0.5f * z1 * dsq;
-            float e2r, e2i, e1r, e1i;
-            expm2i(sinA, -cosA, e2r, e2i);
-            expm2i(-sinA, -cosB, e1r, e1i);
-            cmul(g2r, g2i, e2r, e2i, g2r, g2i);
-            cmul(g1r, g1i, e1r, e1i, g1r, g1i);
-        } else {
-            project3d64(T, i, j, g1r, g1i, g2r, g2i);
-        }
-        // both_complex_prod(g2, g1), ProjectHelper.h:84-101.
-        const float rr = g2r * g1r, ri = g2r * g1i, ir = g2i * g1r, ii = g2i * g1i;
-        av[3] = rr + ii;   // xip
-        av[4] = ri - ir;
-        av[5] = rr - ii;   // xim
-        av[6] = ri + ir;
+    // DirectHelper<0..3>, src/Corr2.cpp:394-474; getWK = w for N, w k for K.
+    if (T.k1 == DN && T.k2 == DN) return;
+    const float wk1 = T.k1 == DN ? A.b.w : A.c.x;
+    if (T.k2 != DG) {
+        av[3] = wk1 * (T.k2 == DN ? B.b.w : B.c.x);               // NK, KK
+        return;
     }
+    const bool both = (T.k1 == DG);
+    float g1r = A.c.x, g1i = A.c.y, g2r = B.c.x, g2i = B.c.y;
+    if (flat) {
+        // ProjectHelper<Flat>::Project: r = p2 - p1 (ProjectHelper.h:108-147).
+        float er, ei;
+        expmsi(T.s2, -dx, -dy, er, ei);
+        cmul(g2r, g2i, er, ei, g2r, g2i);
+        if (both) cmul(g1r, g1i, er, ei, g1r, g1i);
+    } else if (T.coords == SPHERE) {
+        // ProjectHelper<Sphere>::Project, ProjectHelper.h:362-388, with the direction terms
+        // written on accurate differences: y1*x2 - x1*y2 = x1*dy - y1*dx,  d = p1 - p2.
+        const float x1 = A.a.x, y1 = A.a.y, z1 = A.a.z, z2 = B.a.z;
+        const float sinA = x1 * dy - y1 * dx;
+        const float cosA = dz + 0.5f * z2 * dsq;
+        float e2r, e2i;
+        expmsi(T.s2, sinA, -cosA, e2r, e2i);
+        cmul(g2r, g2i, e2r, e2i, g2r, g2i);
+        if (both) {
+            const float cosB = -dz + 0.5f * z1 * dsq;
+            float e1r, e1i;
+            expmsi(T.s1, -sinA, -cosB, e1r, e1i);
+            if (T.s1 & 1) { e1r = -e1r; e1i = -e1i; }
+            cmul(g1r, g1i, e1r, e1i, g1r, g1i);
+        }
+    } else {
+        project3d64(T, i, j, both, g1r, g1i, g2r, g2i);
+    }
+    if (!both) {
+        // DirectHelper<2>: times -wk1 for G (the tangential shear), wk1 otherwise.
+        const float f = T.s2 == 2 ? -wk1 : wk1;
+        av[3] = g2r * f;
+        av[4] = g2i * f;
+        return;
+    }
+    // both_complex_prod(g2, g1), ProjectHelper.h:84-101.
+    const float rr = g2r * g1r, ri = g2r * g1i, ir = g2i * g1r, ii = g2i * g1i;
+    av[3] = rr + ii;   // xip
+    av[4] = ri - ir;
+    av[5] = rr - ii;   // xim
+    av[6] = ri + ir;
 }
 
 // One work item: process2 for a self item (task.y < 0), else process11 for a cell pair.

@@ -9,7 +9,8 @@
 namespace tc {
 
 struct TravParams {
-    int coords, metric, dkind, quick, nbins, autoc;
+    int coords, metric, quick, nbins, autoc;
+    int k1, k2, s1, s2;           // payload kind (DN/DK/DG) and spin of the two fields
     int nqf;                      // FP32 bin quantities: weight, meanr, meanlogr, xi...
     // FP64 constants (escalation path), BaseCorr2 constructor src/Corr2.cpp:55-80.
     double minsep, maxsep, binsize, b, a, logminsep, halfminsep, minsepsq, maxsepsq, bsq, asq;

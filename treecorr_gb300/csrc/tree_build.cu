@@ -52,12 +52,15 @@ __device__ __forceinline__ int split_axis(int coords, double xr, double yr, doub
     return yr > xr ? (zr > yr ? 2 : 1) : (zr > xr ? 2 : 0);
 }
 
-// One point's contribution to the parallel-transported shear sum, src/Cell.cpp:276-321.
-// (cx,cy,cz) is the centre as Position<Sphere> (normalised for ThreeD), cz_raw its raw z.
-__device__ __forceinline__ void transport_add(int coords, double cx, double cy, double cz,
-                                              double cz_raw, double px, double py, double pz,
-                                              double wr, double wi, double& sr, double& si)
+// One point's contribution to the parallel-transported sum of a spin-s value,
+// src/Cell.cpp:276-321.  (cx,cy,cz) is the centre as Position<Sphere> (normalised for
+// ThreeD), cz_raw its raw z.
+__device__ __forceinline__ void transport_add(int coords, int spin, double cx, double cy,
+                                              double cz, double cz_raw, double px, double py,
+                                              double pz, double wr, double wi, double& sr,
+                                              double& si)
 {
+    if (spin == 0) { sr += wr; si += wi; return; }   // calculate_expmsialpha<0> = 1
     if (coords == THREED) normalize3(px, py, pz);
     double dsq = (cx - px) * (cx - px) + (cy - py) * (cy - py) + (cz - pz) * (cz - pz);
     if (dsq < 1.e-12) { sr += wr; si += wi; return; }
@@ -68,11 +71,37 @@ __device__ __forceinline__ void transport_add(int coords, double cx, double cy, 
     double sinB = sinA;
     double cb = -cosA * cosB + sinA * sinB;
     double sb = sinA * cosB + cosA * sinB;
-    // calculate_expmsialpha<2>: conj(r^2)/|r|^2, include/ProjectHelper.h:45-47.
-    double nrm = cb * cb + sb * sb;
-    if (!(nrm > 0.)) nrm = 1.;
-    double er = (cb * cb - sb * sb) / nrm;
-    double ei = -(2. * cb * sb) / nrm;
+    // calculate_expmsialpha<s>(cb + i sb), include/ProjectHelper.h:33-60.
+    double er, ei;
+    if (spin == 2) {
+        double nrm = cb * cb + sb * sb;
+        if (!(nrm > 0.)) nrm = 1.;
+        er = (cb * cb - sb * sb) / nrm;
+        ei = -(2. * cb * sb) / nrm;
+    } else if (spin == 1) {
+        double nrm = cb * cb + sb * sb;
+        if (!(nrm > 0.)) nrm = 1.;
+        nrm = sqrt(nrm);
+        er = cb / nrm;
+        ei = -sb / nrm;
+    } else if (spin == 3) {
+        // r^3, then conj(r^3) / |r^3|.
+        const double r2r = cb * cb - sb * sb, r2i = 2. * cb * sb;
+        const double r3r = r2r * cb - r2i * sb, r3i = r2r * sb + r2i * cb;
+        double nrm = r3r * r3r + r3i * r3i;
+        if (!(nrm > 0.)) nrm = 1.;
+        nrm = sqrt(nrm);
+        er = r3r / nrm;
+        ei = -r3i / nrm;
+    } else {
+        // r^2 squared, then conj(r^4) / |r^2|^2.
+        const double r2r = cb * cb - sb * sb, r2i = 2. * cb * sb;
+        const double r4r = r2r * r2r - r2i * r2i, r4i = 2. * r2r * r2i;
+        double nrm = r2r * r2r + r2i * r2i;
+        if (!(nrm > 0.)) nrm = 1.;
+        er = r4r / nrm;
+        ei = -r4i / nrm;
+    }
     sr += wr * er - wi * ei;
     si += wr * ei + wi * er;
 }
@@ -293,7 +322,7 @@ __global__ void k_task_combine1(int ntask, const BuildTask* tasks, const int* ch
 
 __global__ void __launch_bounds__(CB) k_chunk_pass2(const Chunk* chunks, const BuildTask* tasks,
                                                      const TaskStats* st, Points P0, Points P1,
-                                                     int coords, int dkind, Part2* out)
+                                                     int coords, int dkind, int spin, Part2* out)
 {
     __shared__ double sh[CB / 32];
     __shared__ int shi[CB / 32];
@@ -316,7 +345,7 @@ __global__ void __launch_bounds__(CB) k_chunk_pass2(const Chunk* chunks, const B
             pr += P.d1[i];
         } else if (dkind == DG) {
             if (coords == FLAT) { pr += P.d1[i]; pi += P.d2[i]; }
-            else transport_add(coords, tcx, tcy, tcz, cz, px, py, pz, P.d1[i], P.d2[i], pr, pi);
+            else transport_add(coords, spin, tcx, tcy, tcz, cz, px, py, pz, P.d1[i], P.d2[i], pr, pi);
         }
     }
     Part2 r;
@@ -550,8 +579,8 @@ __global__ void k_small_subtree(int ntask, const BuildTask* tasks, Points P0, Po
             if (BP.dkind == DK) pr += A.d1[i];
             else if (BP.dkind == DG) {
                 if (BP.coords == FLAT) { pr += A.d1[i]; pi += A.d2[i]; }
-                else transport_add(BP.coords, tcx, tcy, tcz, cz, px, py, pz, A.d1[i], A.d2[i],
-                                   pr, pi);
+                else transport_add(BP.coords, BP.spin, tcx, tcy, tcz, cz, px, py, pz, A.d1[i],
+                                   A.d2[i], pr, pi);
             }
         }
         sizesq = warp_max(sizesq); pr = warp_sum(pr); pi = warp_sum(pi);
@@ -721,7 +750,7 @@ int build_tree(const BuildParams& BP, Points bufs[2], Cells C, int* d_tops, int*
         count_launch(); k_task_combine1<<<(nt * 32 + 255) / 256, 256, 0, st>>>(nt, S.tasks, S.chunk0, S.part1,
                                                                 bufs[0], bufs[1], BP, S.stats);
         count_launch(); k_chunk_pass2<<<nc, CB, 0, st>>>(S.chunks, S.tasks, S.stats, bufs[0], bufs[1], BP.coords,
-                                         BP.dkind, S.part2);
+                                         BP.dkind, BP.spin, S.part2);
         count_launch(); k_task_combine2<<<(nt + 127) / 128, 128, 0, st>>>(nt, S.tasks, S.chunk0, S.chunks, S.part2,
                                                           S.stats, BP, C, d_tops, d_ntop, S.big_next,
                                                           S.counters, S.small + 0, S.counters + 1,
@@ -792,7 +821,7 @@ int field_center(const BuildParams& BP, Points P, BuildScratch& S, cudaStream_t 
     B2.split = MEAN;
     count_launch(); k_chunk_pass1<<<nc, CB, 0, st>>>(S.chunks, S.tasks, Pn, Pn, BP.coords, S.part1);
     count_launch(); k_task_combine1<<<1, 32, 0, st>>>(1, S.tasks, S.chunk0, S.part1, Pn, Pn, B2, S.stats);
-    count_launch(); k_chunk_pass2<<<nc, CB, 0, st>>>(S.chunks, S.tasks, S.stats, Pn, Pn, BP.coords, DN, S.part2);
+    count_launch(); k_chunk_pass2<<<nc, CB, 0, st>>>(S.chunks, S.tasks, S.stats, Pn, Pn, BP.coords, DN, 0, S.part2);
     TC_CU(cudaGetLastError());
     std::vector<Part2> p2(nc);
     TaskStats ts;
