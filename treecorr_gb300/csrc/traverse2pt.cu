@@ -35,7 +35,7 @@ namespace tc {
 
 static constexpr int TB = 128;        // threads per traversal block
 static constexpr int WPB = TB / 32;   // warps per block
-static constexpr int FLUSH = 8;       // iterations between FP32 -> FP64 flushes
+static constexpr int FLUSH = 8;       // iterations between flushes of the FP32 bins
 
 // ---------------------------------------------------------------------------------------
 // Packing of the traversal records.
@@ -272,7 +272,7 @@ __device__ Decision decide64(const TravParams& T, double dsq, double s1, double 
 __device__ __forceinline__ void expm2i(float rx, float ry, float& er, float& ei)
 {
     float n = rx * rx + ry * ry;
-    float inv = n > 0.f ? 1.f / n : 1.f;
+    float inv = n > 0.f ? __fdividef(1.f, n) : 1.f;
     er = (rx * rx - ry * ry) * inv;
     ei = -2.f * rx * ry * inv;
 }
@@ -404,24 +404,43 @@ __device__ __forceinline__ int2 make_root(const TravParams& T, long long g)
 // ---------------------------------------------------------------------------------------
 // The traversal kernel.
 
-// FP32 bins (4 segment copies) -> the warp's FP64 bins, all in shared memory.
-__device__ __forceinline__ void flush_bins(int nqnb, float* fb, double* fd, int lane)
+// The warp's running totals are double-float pairs (hi, lo), about 48 bits: FP32 adds with
+// the rounding error kept (TwoSum, Knuth), instead of FP64 adds, whose rate on this GPU is
+// 1/64 of FP32.  They become FP64 once per launch.
+__device__ __forceinline__ void df_add(float2& a, float x)
+{
+    const float s = a.x + x;
+    const float bp = s - a.x;
+    a.y += (a.x - (s - bp)) + (x - bp);
+    a.x = s;
+}
+
+__device__ __forceinline__ double df_value(float2 a) { return (double)a.x + (double)a.y; }
+
+// FP32 bins (4 segment copies) -> the warp's double-float totals, all in shared memory.
+__device__ __forceinline__ void flush_bins(int nqnb, float* fb, float2* fd, int lane)
 {
     for (int q = lane; q < nqnb; q += 32) {
         float a = fb[q], b = fb[nqnb + q], c = fb[2 * nqnb + q], d = fb[3 * nqnb + q];
         if (a != 0.f || b != 0.f || c != 0.f || d != 0.f) {
-            fd[q] += ((double)a + (double)b) + ((double)c + (double)d);
+            float2 f = fd[q];
+            df_add(f, a); df_add(f, b); df_add(f, c); df_add(f, d);
+            const float t = f.x + f.y;          // renormalise (|lo| <= ulp(hi) / 2)
+            f.y -= t - f.x;
+            f.x = t;
+            fd[q] = f;
             fb[q] = 0.f; fb[nqnb + q] = 0.f; fb[2 * nqnb + q] = 0.f; fb[3 * nqnb + q] = 0.f;
         }
     }
 }
 
-// Adds the accepted pairs of this iteration to the warp's bins without atomics.  Each lane
-// stages (k, 7 values, npairs) in shared memory; then the warp works as 4 segments of 8
-// lanes: lane q of a segment owns quantity q (q = 7: npairs) and walks the segment's 8
-// staged entries in order, summing runs of equal bins in a register and adding each run
-// to its segment's copy of the bins.  The order is fixed, so the sums are deterministic.
-static constexpr int STG = 11;   // staged words per lane (odd stride: no bank conflicts)
+// Adds the accepted pairs of this iteration to the warp's bins.  Each lane stages (7 values,
+// k) in shared memory; then the warp works as 4 segments of 8 lanes: lane q < 7 of a segment
+// owns quantity q and adds the segment's 8 staged entries, in order, to its segment's copy
+// of the bins -- one read-modify-write per entry, the same instructions on every lane (an
+// entry without a pair adds 0 to bin 0), so the warp never diverges here.  The exact integer
+// npairs goes in with one 64-bit shared atomic per accepting lane (copy lane & 3).
+static constexpr int STG = 9;    // staged words per lane (odd stride: no bank conflicts)
 
 __host__ __device__ inline size_t traverse_warp_bytes(int nq, int nb)
 {
@@ -435,42 +454,21 @@ __device__ __forceinline__ void stage_accumulate(int k, const float (&v)[7],
                                                  float* stage, float* fb, unsigned long long* np,
                                                  int nb, int lane)
 {
+    if (!quick && k >= 0) atomicAdd(np + (lane & 3) * nb + k, nn);
     float* my = stage + lane * STG;
 #pragma unroll
     for (int q = 0; q < 7; ++q) my[q] = v[q];
     my[7] = __int_as_float(k);
-    my[8] = __uint_as_float((unsigned)(nn & 0xffffffffull));
-    my[9] = __uint_as_float((unsigned)(nn >> 32));
     __syncwarp();
     const int seg = lane >> 3, q = lane & 7;
-    const bool isn = (q == 7);
-    if (q < nq || (isn && !quick)) {
+    if (q < nq) {
         float* fbs = fb + seg * nq * nb + q * nb;
-        unsigned long long* nps = np + seg * nb;
-        int curk = -1;
-        float acc = 0.f;
-        unsigned long long acc64 = 0ull;
 #pragma unroll
         for (int t = 0; t < 8; ++t) {
             const float* e = stage + (seg * 8 + t) * STG;
             const int kj = __float_as_int(e[7]);
-            if (kj < 0) continue;
-            if (kj != curk) {
-                if (curk >= 0) {
-                    if (isn) nps[curk] += acc64;
-                    else fbs[curk] += acc;
-                }
-                curk = kj;
-                acc = 0.f;
-                acc64 = 0ull;
-            }
-            if (isn) acc64 += (unsigned long long)__float_as_uint(e[8]) |
-                              ((unsigned long long)__float_as_uint(e[9]) << 32);
-            else acc += e[q];
-        }
-        if (curk >= 0) {
-            if (isn) nps[curk] += acc64;
-            else fbs[curk] += acc;
+            const float x = kj >= 0 ? e[q] : 0.f;
+            fbs[kj >= 0 ? kj : 0] += x;
         }
     }
     __syncwarp();
@@ -659,11 +657,11 @@ __global__ void __launch_bounds__(TB) k_traverse(TravParams T)
     // Per-warp bins: nq*nb FP64 totals, 4 segment copies of the npairs (u64) and of the
     // nq*nb FP32 partials, and the 32-lane staging area.
     const size_t wbytes = traverse_warp_bytes(nq, nb);
-    double* fd = (double*)(smem + wib * wbytes);
+    float2* fd = (float2*)(smem + wib * wbytes);
     unsigned long long* np = (unsigned long long*)(fd + nq * nb);
     float* fb = (float*)(np + 4 * nb);
     float* stage = fb + 4 * nq * nb;
-    for (int q = lane; q < nq * nb; q += 32) fd[q] = 0.;
+    for (int q = lane; q < nq * nb; q += 32) fd[q] = make_float2(0.f, 0.f);
     for (int q = lane; q < 4 * nb; q += 32) np[q] = 0ull;
     for (int q = lane; q < 4 * nq * nb; q += 32) fb[q] = 0.f;
     __syncwarp();
@@ -792,7 +790,7 @@ __global__ void __launch_bounds__(TB) k_traverse(TravParams T)
     {
         // The warp's totals: added to its global slot (kept across relaunches).
         double* wa = T.wacc + (size_t)gw * nq * nb;
-        for (int q = lane; q < nq * nb; q += 32) wa[q] += fd[q];
+        for (int q = lane; q < nq * nb; q += 32) wa[q] += df_value(fd[q]);
         unsigned long long* wn = T.wnp + (size_t)gw * nb;
         for (int q = lane; q < nb; q += 32) wn[q] += (np[q] + np[nb + q]) + (np[2 * nb + q] + np[3 * nb + q]);
     }
@@ -817,7 +815,7 @@ __global__ void __launch_bounds__(TB) k_traverse(TravParams T)
 // to the warp's global FP64 slot at the end (the slots persist across launches).
 // Patches: the warp's bins (all of one patch pair) go to that pair's FP64 sums.
 __device__ __forceinline__ void patch_flush(const TravParams& T, int pair, int nq, int nb,
-                                            float* fb, double* fd, unsigned long long* np,
+                                            float* fb, float2* fd, unsigned long long* np,
                                             int lane)
 {
     __syncwarp();
@@ -825,8 +823,10 @@ __device__ __forceinline__ void patch_flush(const TravParams& T, int pair, int n
     __syncwarp();
     if (pair >= 0) {
         double* pa = T.pacc + (size_t)pair * nq * nb;
-        for (int q = lane; q < nq * nb; q += 32)
-            if (fd[q] != 0.) atomicAdd(&pa[q], fd[q]);
+        for (int q = lane; q < nq * nb; q += 32) {
+            const double v = df_value(fd[q]);
+            if (v != 0.) atomicAdd(&pa[q], v);
+        }
         unsigned long long* pn = T.pnp + (size_t)pair * nb;
         for (int q = lane; q < nb; q += 32) {
             const unsigned long long v = (np[q] + np[nb + q]) + (np[2 * nb + q] + np[3 * nb + q]);
@@ -834,7 +834,7 @@ __device__ __forceinline__ void patch_flush(const TravParams& T, int pair, int n
         }
     }
     __syncwarp();
-    for (int q = lane; q < nq * nb; q += 32) fd[q] = 0.;
+    for (int q = lane; q < nq * nb; q += 32) fd[q] = make_float2(0.f, 0.f);
     for (int q = lane; q < 4 * nb; q += 32) np[q] = 0ull;
     for (int q = lane; q < 4 * nq * nb; q += 32) fb[q] = 0.f;
     __syncwarp();
@@ -887,11 +887,11 @@ __global__ void __launch_bounds__(TB, EXPAND_MINB) k_expand(TravParams T, const 
     const int gw = blockIdx.x * WPB + wib;
     const int nq = T.nqf, nb = T.nbins;
     const size_t wbytes = traverse_warp_bytes(nq, nb);
-    double* fd = (double*)(smem + wib * wbytes);
+    float2* fd = (float2*)(smem + wib * wbytes);
     unsigned long long* np = (unsigned long long*)(fd + nq * nb);
     float* fb = (float*)(np + 4 * nb);
     float* stage = fb + 4 * nq * nb;
-    for (int q = lane; q < nq * nb; q += 32) fd[q] = 0.;
+    for (int q = lane; q < nq * nb; q += 32) fd[q] = make_float2(0.f, 0.f);
     for (int q = lane; q < 4 * nb; q += 32) np[q] = 0ull;
     for (int q = lane; q < 4 * nq * nb; q += 32) fb[q] = 0.f;
     // MODE 2: the network in shared memory after the bins, then per-warp staging.
@@ -1016,7 +1016,7 @@ __global__ void __launch_bounds__(TB, EXPAND_MINB) k_expand(TravParams T, const 
     flush_bins(nq * nb, fb, fd, lane);
     __syncwarp();
     double* wa = T.wacc + (size_t)gw * nq * nb;
-    for (int q = lane; q < nq * nb; q += 32) wa[q] += fd[q];
+    for (int q = lane; q < nq * nb; q += 32) wa[q] += df_value(fd[q]);
     unsigned long long* wn = T.wnp + (size_t)gw * nb;
     for (int q = lane; q < nb; q += 32) wn[q] += (np[q] + np[nb + q]) + (np[2 * nb + q] + np[3 * nb + q]);
     if (lane == 0) {
