@@ -506,10 +506,12 @@ int expand_run(tc_corr2* c, const TravParams& T, int blocks, long long npoints, 
 {
     // The schedule lives on the device: batches of (schedule, expand) launches run without
     // host round trips; the host only adds level buffers when the expansion gets deeper.
-    // Chunk size: up to 4M items per launch, less for small catalogs (level buffers hold
-    // 4 chunks each).
+    // Chunk size: up to 16M items per launch, less for small catalogs (level buffers hold
+    // 4 chunks each: 512 MB per level at the largest size).  Large launches amortise the
+    // per-launch work of every warp (bin set-up, the flush of its totals, the completion
+    // count); 4M-item chunks took 19% longer on a 10M-point catalog.
     long long CH = 1LL << 16;
-    while (CH < (1LL << 22) && CH < 2 * npoints) CH <<= 1;
+    while (CH < (1LL << 24) && CH < 2 * npoints) CH <<= 1;
     if (!c->sched) TC_TRY(dalloc(&c->sched, 1));
     ExpandSched hs;
     std::memset(&hs, 0, sizeof(hs));
