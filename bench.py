@@ -270,9 +270,9 @@ def run_gpu(args, rank, world):
     achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
     traffic = args.traffic
     if traffic is None and args.n == 10_000_000 and abs(args.bin_slop - 0.1) < 1e-12:
-        # DRAM bytes per launch: 24.4 bytes per evaluated cell pair measured with ncu over a
+        # DRAM bytes per launch: 25.3 bytes per evaluated cell pair measured with ncu over a
         # whole 1M-point traversal, times the cell pairs per launch of this workload.
-        traffic = round(24.4 * st["cell_pairs"] / max(st["launches"], 1))
+        traffic = round(25.3 * st["cell_pairs"] / max(st["launches"], 1))
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 4), "traffic": traffic,
                 "traffic_source": "ncu DRAM bytes per cell pair at 1M points, scaled"

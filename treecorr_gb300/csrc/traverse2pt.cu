@@ -868,7 +868,7 @@ __device__ __forceinline__ void expand_warp_done(const ExpandSched* S, int lane)
 }
 
 #ifndef EXPAND_MINB
-#define EXPAND_MINB 6   // resident blocks per SM the register budget is sized for
+#define EXPAND_MINB 7   // resident blocks per SM the register budget is sized for (72 registers)
 #endif
 template <int MODE>
 __global__ void __launch_bounds__(TB, EXPAND_MINB) k_expand(TravParams T, const int2* in, long long n_in,
