@@ -495,6 +495,118 @@ __device__ __forceinline__ int pack_meta(int side, int intop, int buf, int minto
     return side | (intop << 1) | (buf << 2) | (mintop << 8) | (maxtop << 20);
 }
 
+// Cells of at most THREAD_T points are finished by one thread: the steps of the warp loop
+// below (src/Cell.cpp:170-200, 520-615) with the sums taken in point order.  Small cells
+// are ~94% of a subtree's cells, and a warp spends the same reductions on a 2-point cell
+// as on a 2048-point one.
+constexpr int THREAD_T = 32;
+
+__device__ void subtree_by_thread(WTask root, Points P0, Points P1, const BuildParams& BP,
+                                  const Cells& C, int* tops, int* ntop, int* err)
+{
+    WTask stk[THREAD_T + 1];
+    int sp = 0;
+    stk[sp++] = root;
+    while (sp > 0) {
+        const WTask w = stk[--sp];
+        const int s = w.s, e = w.e, n = e - s;
+        const int side = w.meta & 1, buf = (w.meta >> 2) & 1;
+        int intop = (w.meta >> 1) & 1;
+        const int mintop = ((w.meta >> 8) & 0xfff) - 2048;
+        const int maxtop = ((w.meta >> 20) & 0xfff) - 2048;
+        const Points& A = buf ? P1 : P0;
+        const Points& B = buf ? P0 : P1;
+        if (n == 1) {
+            const int id = (BP.n - 1) + s;
+            write_cell(C, id, A.x[s], A.y[s], A.z[s], 0.f, A.w[s], A.d1[s], A.d2[s], 1, s,
+                       w.parent, side);
+            if (intop) add_top(tops, ntop, id, s);
+            if (buf) move_point(A, s, P0, s);
+            continue;
+        }
+        double sx = 0., sy = 0., sz = 0., swp = 0., sw = 0.;
+        double xmin = DBL_MAX, ymin = DBL_MAX, zmin = DBL_MAX;
+        double xmax = -DBL_MAX, ymax = -DBL_MAX, zmax = -DBL_MAX;
+        for (int i = s; i < e; ++i) {
+            const double px = A.x[i], py = A.y[i], pz = A.z[i], wp = A.wp[i];
+            sx += px * wp; sy += py * wp; sz += pz * wp; swp += wp; sw += A.w[i];
+            xmin = fmin(xmin, px); xmax = fmax(xmax, px);
+            ymin = fmin(ymin, py); ymax = fmax(ymax, py);
+            zmin = fmin(zmin, pz); zmax = fmax(zmax, pz);
+        }
+        double cx, cy, cz;
+        if (swp != 0.) {
+            cx = sx / swp; cy = sy / swp; cz = sz / swp;
+            if (BP.coords == SPHERE) normalize3(cx, cy, cz);
+        } else {
+            cx = A.x[s]; cy = A.y[s]; cz = A.z[s];
+        }
+        const int axis = split_axis(BP.coords, xmax - xmin, ymax - ymin, zmax - zmin);
+        double splitval;
+        if (BP.split == MIDDLE)
+            splitval = axis == 2 ? (zmax + zmin) / 2. : axis == 1 ? (ymax + ymin) / 2.
+                                                                   : (xmax + xmin) / 2.;
+        else
+            splitval = axis == 2 ? cz : axis == 1 ? cy : cx;
+        double tcx = cx, tcy = cy, tcz = cz;
+        if (BP.coords == THREED) normalize3(tcx, tcy, tcz);
+        double sizesq = 0., pr = 0., pi = 0.;
+        int nleft = 0;
+        for (int i = s; i < e; ++i) {
+            const double px = A.x[i], py = A.y[i], pz = A.z[i];
+            double d = (cx - px) * (cx - px) + (cy - py) * (cy - py);
+            if (BP.coords != FLAT) d += (cz - pz) * (cz - pz);
+            sizesq = fmax(sizesq, d);
+            const double c = axis == 2 ? pz : axis == 1 ? py : px;
+            nleft += (c < splitval) ? 1 : 0;
+            if (BP.dkind == DK) pr += A.d1[i];
+            else if (BP.dkind == DG) {
+                if (BP.coords == FLAT) { pr += A.d1[i]; pi += A.d2[i]; }
+                else transport_add(BP.coords, BP.spin, tcx, tcy, tcz, cz, px, py, pz, A.d1[i],
+                                   A.d2[i], pr, pi);
+            }
+        }
+        bool is_top;
+        const bool split = decide_split(BP, intop, mintop, maxtop, sizesq, is_top);
+        bool use_rank = (BP.split == MEDIAN);
+        int mid = s + nleft;
+        if (split && !use_rank && (nleft == 0 || nleft == n)) use_rank = true;
+        if (split && use_rank) mid = (s + e) / 2;   // SplitDataCore<Median>, src/Cell.cpp:464-479
+        float d1 = float(pr), d2 = float(pi);
+        if (BP.dkind == DN) { d1 = 0.f; d2 = 0.f; }
+        if (BP.dkind == DK) d2 = 0.f;
+        const int id = split ? mid - 1 : (BP.n - 1) + s;
+        write_cell(C, id, cx, cy, cz, split ? cell_size(BP, sizesq) : 0.f, float(sw), d1, d2, n,
+                   s, w.parent, side);
+        if (is_top) add_top(tops, ntop, id, s);
+        if (!split) {
+            if (buf) for (int i = s; i < e; ++i) move_point(A, i, P0, i);
+            continue;
+        }
+        // Stable partition into the other buffer.
+        int lo = s, hi = mid;
+        for (int i = s; i < e; ++i) {
+            const double c = axis == 2 ? A.z[i] : axis == 1 ? A.y[i] : A.x[i];
+            bool left;
+            if (!use_rank) {
+                left = c < splitval;
+            } else {
+                int rank = 0;
+                for (int j = s; j < e; ++j) {
+                    const double cj = axis == 2 ? A.z[j] : axis == 1 ? A.y[j] : A.x[j];
+                    rank += (cj < c || (cj == c && j < i)) ? 1 : 0;
+                }
+                left = rank < (mid - s);
+            }
+            move_point(A, i, B, left ? lo++ : hi++);
+        }
+        if (sp + 2 > THREAD_T + 1) { set_err(err, DEV_TASK_OVERFLOW); return; }
+        const int nb = buf ^ 1;
+        stk[sp++] = WTask{mid, e, id, pack_meta(1, intop, nb, mintop - 1, maxtop - 1)};
+        stk[sp++] = WTask{s, mid, id, pack_meta(0, intop, nb, mintop - 1, maxtop - 1)};
+    }
+}
+
 __global__ void k_small_subtree(int ntask, const BuildTask* tasks, Points P0, Points P1,
                                 BuildParams BP, Cells C, int* tops, int* ntop, WTask* wstack,
                                 int* err)
@@ -504,6 +616,10 @@ __global__ void k_small_subtree(int ntask, const BuildTask* tasks, Points P0, Po
     if (t >= ntask) return;
     const BuildTask root = tasks[t];
     WTask* stk = wstack + root.s;          // this task owns [root.s, root.e) of the stack
+    // Cells of at most THREAD_T points wait here until each lane can take one.
+    __shared__ WTask deferred[4][32];
+    WTask* dq = deferred[(threadIdx.x >> 5) & 3];
+    int ndq = 0;
     int sp = 0;
     if (lane == 0) {
         WTask w0 = {root.s, root.e, root.parent,
@@ -512,10 +628,22 @@ __global__ void k_small_subtree(int ntask, const BuildTask* tasks, Points P0, Po
     }
     sp = 1;
     __syncwarp();
-    while (sp > 0) {
+    while (sp > 0 || ndq > 0) {
+        if (sp == 0 || ndq == 32) {
+            __syncwarp();
+            if (lane < ndq) subtree_by_thread(dq[lane], P0, P1, BP, C, tops, ntop, err);
+            ndq = 0;
+            __syncwarp();
+            continue;
+        }
         --sp;
         WTask w = stk[sp];
         __syncwarp();
+        if (w.e - w.s <= THREAD_T) {
+            if (lane == 0) dq[ndq] = w;
+            ++ndq;
+            continue;
+        }
         const int s = w.s, e = w.e, n = e - s;
         const int side = w.meta & 1, buf = (w.meta >> 2) & 1;
         int intop = (w.meta >> 1) & 1;
