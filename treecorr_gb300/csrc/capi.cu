@@ -93,10 +93,7 @@ struct tc_corr2 {
     double *meanr = nullptr, *meanlogr = nullptr, *weight = nullptr, *npairs = nullptr;
     tc_stats stats = {};
     // Traversal scratch, grown on demand.
-    int2* stacks = nullptr;
-    int2* spill[2] = {nullptr, nullptr};
-    long long spill_cap = 0;
-    int stack_cap = 0, nwarps_alloc = 0, nq_alloc = 0;
+    int nwarps_alloc = 0, nq_alloc = 0;
     double* wacc = nullptr;
     unsigned long long* wnp = nullptr;
     double* tot = nullptr;
@@ -368,32 +365,6 @@ int field_create_impl(int dkind, int coords, const double* x, const double* y, c
     }
     *out = f;
     return TC_OK;
-}
-
-// Per-call traversal scratch.
-int corr_scratch(tc_corr2* c, int nwarps, int nq)
-{
-    const int stack_cap = c->stack_cap > 0 ? c->stack_cap : 8192;
-    if (nwarps > c->nwarps_alloc || stack_cap != c->stack_cap || nq > c->nq_alloc || !c->ctl) {
-        dfree(c->stacks); dfree(c->spill[0]); dfree(c->spill[1]); dfree(c->wacc); dfree(c->wnp);
-        dfree(c->tot); dfree(c->totnp); dfree(c->ctl); dfree(c->idle); dfree(c->d_err);
-        long long cap = (long long)nwarps * stack_cap;
-        if (c->spill_cap < cap) c->spill_cap = cap;
-        TC_TRY(dalloc(&c->stacks, (size_t)nwarps * stack_cap));
-        TC_TRY(dalloc(&c->spill[0], (size_t)c->spill_cap));
-        TC_TRY(dalloc(&c->spill[1], (size_t)c->spill_cap));
-        TC_TRY(dalloc(&c->wacc, (size_t)nwarps * nq * c->nbins));
-        TC_TRY(dalloc(&c->wnp, (size_t)nwarps * c->nbins));
-        TC_TRY(dalloc(&c->tot, (size_t)nq * c->nbins));
-        TC_TRY(dalloc(&c->totnp, (size_t)c->nbins));
-        TC_TRY(dalloc(&c->ctl, 8));
-        TC_TRY(dalloc(&c->idle, 1));
-        TC_TRY(dalloc(&c->d_err, 1));
-        c->nwarps_alloc = nwarps;
-        c->stack_cap = stack_cap;
-        c->nq_alloc = nq;
-    }
-    return 0;
 }
 
 double sqr(double x) { return x * x; }
@@ -1146,7 +1117,7 @@ int tc_corr2_create(int d1, int d2, int bin_type, double minsep, double maxsep, 
 void tc_corr2_free(tc_corr2* c)
 {
     if (!c) return;
-    dfree(c->stacks); dfree(c->spill[0]); dfree(c->spill[1]); dfree(c->wacc); dfree(c->wnp);
+    dfree(c->wacc); dfree(c->wnp);
     dfree(c->tot); dfree(c->totnp); dfree(c->ctl); dfree(c->idle); dfree(c->d_err);
     for (auto& p : c->lev) dfree(p);
     dfree(c->sched);
