@@ -230,3 +230,21 @@ def test_unsupported_raise(gpu_lib):
                  0., 0., 0., e, e, e, e, np.zeros(5), np.zeros(5), np.zeros(5), np.zeros(5))
     with pytest.raises(NotImplementedError):
         T.NFieldFlat(z, z, e, z + 1, e, 0., 0., T.Random, 0, False, 3, 10)
+
+
+def test_mixed_class_arguments(gpu_lib):
+    """The class fixes the two data kinds: an auto correlation of a mixed class, or fields of
+    other kinds, are refused (the reference's Python never builds them)."""
+    T = gpu_lib
+    s, c1, c2, bins, min_size, max_size, ref = H.load_case("ng_flat_cross")
+    fn = H.gpu_field(T, "N", "flat", c1, min_size, max_size)
+    fg = H.gpu_field(T, "G", "flat", c2, min_size, max_size)
+    fk = H.gpu_field(T, "K", "flat", c2, min_size, max_size)
+    with pytest.raises(ValueError):
+        H.gpu_process(T, "NG", "Euclidean", bins, fn)            # auto of a mixed class
+    with pytest.raises(ValueError):
+        H.gpu_process(T, "NG", "Euclidean", bins, fn, fk)        # K field as the G side
+    with pytest.raises(ValueError):
+        H.gpu_process(T, "NG", "Euclidean", bins, fg, fn)        # kinds swapped
+    got = H.gpu_process(T, "NG", "Euclidean", bins, fn, fg)
+    H.assert_outputs_close(got, ref, "NG", rtol=RTOL, label="ng after refusals")
