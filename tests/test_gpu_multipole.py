@@ -86,3 +86,35 @@ def test_multipole_contraction_paths(gpu_lib, monkeypatch, tensor):
         err = max_rel_err(out, {k: g["ref_" + k] for k in MP_OUT})
         for k, v in err.items():
             assert v <= TOL, f"{name} {k} tensor={tensor}: {v:.3e}"
+
+
+@pytest.mark.parametrize("name", ["nnn_flat_mp", "nnn_sphere_mp"])
+def test_multipole_nnn_golden(gpu_lib, name):
+    """NNN LogMultipole through NNNCorr on an N field against the reference's NNNCorr."""
+    from cases3 import spec3
+    T = gpu_lib
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    s = spec3(str(g["case"]))
+    cat = {k[3:]: g[k] for k in g.files if k.startswith("c1_")}
+    nb, mn = s["nbins"], s["max_n"]
+    shape = (nb, nb, 2 * mn + 1)
+    keys = ("meand1", "meanlogd1", "meand2", "meanlogd2", "meand3", "meanlogd3", "meanu",
+            "meanv", "weight", "weight_im", "ntri")
+    out = {k: np.zeros(shape) for k in keys}
+    e = np.array([])
+    corr = T.NNNCorr(T.LogMultipole, s["min_sep"], s["max_sep"], nb, s["bin_size"], s["b"],
+                     s["a"], 0., 0., mn, 0., 0., 0., 0., 0, 0., 0.,
+                     -sys.float_info.max, sys.float_info.max, 0., 0., 0.,
+                     e, e, e, e, e, e, e, e, *[out[k] for k in keys])
+    f = H.gpu_field(T, "N", s["coords"], cat, float(g["min_size"]), float(g["max_size"]))
+    m = T.Euclidean if s["metric"] == "Euclidean" else T.Arc
+    corr.processAuto(f, False, False, m)
+    assert np.array_equal(out["ntri"], g["ref_ntri"]), name
+    for k in ("weight", "weight_im", "meand2", "meanlogd2", "meand3", "meanlogd3"):
+        r = g["ref_" + k]
+        err = np.abs(out[k] - r).max() / max(np.abs(r).max(), 1e-300)
+        assert err <= TOL, f"{name} {k}: {err:.3e}"
+    # A G field is refused by NNN (and an N field by GGG).
+    fg = H.gpu_field(T, "G", s["coords"], cat, float(g["min_size"]), float(g["max_size"]))
+    with pytest.raises(ValueError):
+        corr.processAuto(fg, False, False, m)

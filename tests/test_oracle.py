@@ -67,3 +67,26 @@ def test_oracle_multipole_matches_reference(name):
     for k in O.MP_KEYS:
         r = g["ref_" + k]
         assert np.abs(out[k] - r).max() <= 1e-12 * max(np.abs(r).max(), 1e-300), k
+
+
+@pytest.mark.parametrize("name", ["nnn_flat_mp", "nnn_sphere_mp"])
+def test_oracle_multipole_nnn_matches_reference(name):
+    """NNN LogMultipole (the reference's NNNCorr): its weight, ntri and mean distances are
+    the multipole sums that do not depend on the payload, so the oracle's multipole on the
+    same points with zero shears reproduces them."""
+    import os
+    from cases3 import spec3
+    from oracle import oracle as O
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    s = spec3(str(g["case"]))
+    c = {k[3:]: g[k] for k in g.files if k.startswith("c1_")}
+    zero = np.zeros(len(c["x"]))
+    f = O.OracleField("G", s["coords"], c["x"], c["y"], c.get("z"), zero, zero, c["w"],
+                      None, float(g["min_size"]), float(g["max_size"]), "mean", False, 3, 10)
+    bins = dict(min_sep=s["min_sep"], max_sep=s["max_sep"], nbins=s["nbins"],
+                bin_size=s["bin_size"], b=s["b"], a=s["a"])
+    out = O.multipole(s["metric"], bins, s["max_n"], f, nthreads=1)
+    assert np.array_equal(out["ntri"], g["ref_ntri"])
+    for k in ("weight", "weight_im", "meand2", "meanlogd2", "meand3", "meanlogd3"):
+        r = g["ref_" + k]
+        assert np.abs(out[k] - r).max() <= 1e-12 * max(np.abs(r).max(), 1e-300), k

@@ -652,6 +652,7 @@ class BaseCorr3:
 
 class GGGCorr(BaseCorr3):
     """GGGCorr (BuildCorr3, src/Corr3.cpp:3599-3645): outputs aliased, accumulated."""
+    _dkind = 2
 
     def __init__(self, bin_type, minsep, maxsep, nbins, binsize, b, a, minu, maxu, nubins,
                  ubinsize, bu, minv, maxv, nvbins, vbinsize, bv, minrpar, maxrpar, xp, yp, zp,
@@ -668,7 +669,8 @@ class GGGCorr(BaseCorr3):
                                  "nbins*nbins*(2*max_n+1) entries")
         self._outs = arrs
         h = ctypes.c_void_p()
-        _check(lib().tc_corr3_create(2, 2, 2, int(bin_type), float(minsep), float(maxsep),
+        d = self._dkind
+        _check(lib().tc_corr3_create(d, d, d, int(bin_type), float(minsep), float(maxsep),
                                      int(nbins), float(binsize), float(b), float(a), float(minu),
                                      float(maxu), int(nubins), float(ubinsize), float(bu),
                                      float(minv), float(maxv), int(nvbins), float(vbinsize),
@@ -686,8 +688,14 @@ def _not_on_path(name):
     return f
 
 
-# The 3-point classes of src/Corr3.cpp (WrapCorr3) other than GGG with LogMultipole.
-for _n in ("NNN", "KKK", "NNK", "NKN", "KNN", "NKK", "KNK", "KKN", "NNG", "NGN", "GNN", "NGG",
+class NNNCorr(GGGCorr):
+    """NNNCorr (src/Corr3.cpp:4237) with LogMultipole binning: weight, weight_im, ntri and
+    the mean distances (the zeta arrays are empty for NNN)."""
+    _dkind = 0
+
+
+# The 3-point classes of src/Corr3.cpp (WrapCorr3) other than GGG / NNN with LogMultipole.
+for _n in ("KKK", "NNK", "NKN", "KNN", "NKK", "KNK", "KKN", "NNG", "NGN", "GNN", "NGG",
            "GNG", "GGN", "KKG", "KGK", "GKK", "KGG", "GKG", "GGK"):
     globals()[_n + "Corr"] = _not_on_path(_n + "Corr")
 del _n

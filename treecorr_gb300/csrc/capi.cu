@@ -77,6 +77,7 @@ struct tc_field {
 };
 
 struct tc_corr3 {
+    int dk = TC_GDATA;           // data kind of all three vertices (GGG or NNN)
     int bin_type = 0, nbins = 0, maxn = 0;
     double minsep = 0., maxsep = 0., binsize = 0., b = 0., a = 0.;
     double* zeta[8] = {nullptr};
@@ -793,7 +794,10 @@ int corr_process_auto_noalloc(tc_corr2* c, tc_field* f, int quick, int metric)
 int corr3_process_auto(tc_corr3* c, tc_field* f, int quick, int metric)
 {
     if (!c || !f) { set_last_error("NULL argument"); return TC_ERR_ARG; }
-    if (f->dkind != TC_GDATA) { set_last_error("GGG needs a G field"); return TC_ERR_ARG; }
+    if (f->dkind != c->dk) {
+        set_last_error(c->dk == TC_GDATA ? "GGG needs a G field" : "NNN needs an N field");
+        return TC_ERR_ARG;
+    }
     TC_TRY(check_metric(f->coords, metric));
     if (f->n == 0) return TC_OK;
     cudaStream_t st;
@@ -1581,8 +1585,10 @@ int tc_corr3_create(int d1, int d2, int d3, int bin_type, double minsep, double 
     (void)vbinsize; (void)bv; (void)meand1; (void)meanlogd1; (void)meanu; (void)meanv;
     if (!out) { set_last_error("out is NULL"); return TC_ERR_ARG; }
     *out = nullptr;
-    if (d1 != TC_GDATA || d2 != TC_GDATA || d3 != TC_GDATA) {
-        set_last_error("only GGG is on the GPU 3-point path");
+    // GGG, and NNN: its weight, ntri and mean distances are the multipole's own sums,
+    // which do not depend on the payload (an N field carries none).
+    if (d1 != d2 || d2 != d3 || (d1 != TC_GDATA && d1 != TC_NDATA)) {
+        set_last_error("only GGG and NNN are on the GPU 3-point path");
         return TC_ERR_UNSUPPORTED;
     }
     if (bin_type != TC_LOGMULTIPOLE) {
@@ -1598,16 +1604,18 @@ int tc_corr3_create(int d1, int d2, int d3, int bin_type, double minsep, double 
         set_last_error("invalid binning");
         return TC_ERR_ARG;
     }
-    if (!zeta0 || !zeta1 || !zeta2 || !zeta3 || !zeta4 || !zeta5 || !zeta6 || !zeta7 ||
+    const bool needz = (d1 == TC_GDATA);
+    if ((needz && (!zeta0 || !zeta1 || !zeta2 || !zeta3 || !zeta4 || !zeta5 || !zeta6 || !zeta7)) ||
         !meand2 || !meanlogd2 || !meand3 || !meanlogd3 || !weight || !weight_im || !ntri) {
         set_last_error("missing output array");
         return TC_ERR_ARG;
     }
     tc_corr3* c = new tc_corr3();
+    c->dk = d1;
     c->bin_type = bin_type; c->nbins = nbins; c->maxn = nubins;
     c->minsep = minsep; c->maxsep = maxsep; c->binsize = binsize; c->b = b; c->a = a;
     double* z[8] = {zeta0, zeta1, zeta2, zeta3, zeta4, zeta5, zeta6, zeta7};
-    for (int q = 0; q < 8; ++q) c->zeta[q] = z[q];
+    for (int q = 0; q < 8; ++q) c->zeta[q] = needz ? z[q] : nullptr;
     c->meand2 = meand2; c->meanlogd2 = meanlogd2; c->meand3 = meand3; c->meanlogd3 = meanlogd3;
     c->weight = weight; c->weight_im = weight_im; c->ntri = ntri;
     *out = c;
