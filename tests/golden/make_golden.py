@@ -93,7 +93,7 @@ def run_case(name):
     return out
 
 
-if __name__ == "__main__" and not {"--mp", "--mp-nnn", "--xyz", "--kmeans"} & set(sys.argv):
+if __name__ == "__main__" and not {"--mp", "--mp-nnn", "--mp-kkk", "--xyz", "--kmeans"} & set(sys.argv):
     _treecorr.SetOMPThreads(1)
     names = sys.argv[1:] or list(CASES)
     for name in names:
@@ -135,7 +135,7 @@ def run_case3(name):
     return out
 
 
-if __name__ == "__main__" and "--mp" in sys.argv and "--mp-nnn" not in sys.argv:
+if __name__ == "__main__" and "--mp" in sys.argv:
     _treecorr.SetOMPThreads(1)
     from cases3 import CASES3
     for name in CASES3:
@@ -239,3 +239,39 @@ if __name__ == "__main__" and "--mp-nnn" in sys.argv:
             save["ref_" + k] = v
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **save)
         print(f"{name:16s} ntri={out['ntri'].sum():.6g} weight={out['weight'].sum():.6g}")
+
+
+# KKK LogMultipole (the reference's KKKCorr, src/Corr3.cpp:4238): zeta (real, imaginary),
+# weight, ntri and the mean distances, on the catalogs of two GGG cases with their k column.
+if __name__ == "__main__" and "--mp-kkk" in sys.argv:
+    _treecorr.SetOMPThreads(1)
+    from cases3 import make_inputs3, spec3
+    for gname, name in (("ggg_flat_mp", "kkk_flat_mp"), ("ggg_sphere_mp", "kkk_sphere_mp")):
+        s = spec3(gname)
+        cat = make_inputs3(gname)
+        if s["metric"] == "Euclidean":
+            b1 = min(s["a"], s["b"])
+            min_size, max_size = 2 * s["min_sep"] * b1 / (2. + 3 * b1), s["max_sep"] * b1
+        else:
+            min_size, max_size = 0.0, 0.0
+        nb, mn = s["nbins"], s["max_n"]
+        shape = (nb, nb, 2 * mn + 1)
+        keys = ("zeta", "zeta_im", "meand1", "meanlogd1", "meand2", "meanlogd2", "meand3",
+                "meanlogd3", "meanu", "meanv", "weight", "weight_im", "ntri")
+        out = {k: np.zeros(shape) for k in keys}
+        e = np.array([])
+        corr = _treecorr.KKKCorr(
+            _treecorr.LogMultipole, s["min_sep"], s["max_sep"], nb, s["bin_size"], s["b"], s["a"],
+            0., 0., mn, 0., 0., 0., 0., 0, 0., 0.,
+            -sys.float_info.max, sys.float_info.max, 0., 0., 0.,
+            out["zeta"], out["zeta_im"], e, e, e, e, e, e, *[out[k] for k in keys[2:]])
+        f = build_field("K", s["coords"], cat, min_size, max_size, "mean", False, 3, 10)
+        corr.processAuto(f, False, False, METRIC[s["metric"]])
+        save = dict(min_size=min_size, max_size=max_size, case=gname)
+        for k, v in cat.items():
+            if v is not None:
+                save["c1_" + k] = v
+        for k, v in out.items():
+            save["ref_" + k] = v
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **save)
+        print(f"{name:16s} ntri={out['ntri'].sum():.6g} zeta={out['zeta'].sum():.6g}")

@@ -55,4 +55,4 @@ def test_python_mirror_matches_reference_names():
     assert (int(T.Log), int(T.Linear), int(T.TwoD), int(T.LogRUV), int(T.LogSAS),
             int(T.LogMultipole)) == (0, 1, 2, 3, 4, 5)
     with pytest.raises(NotImplementedError):
-        T.KKKCorr()
+        T.NNKCorr()

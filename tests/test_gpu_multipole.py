@@ -118,3 +118,32 @@ def test_multipole_nnn_golden(gpu_lib, name):
     fg = H.gpu_field(T, "G", s["coords"], cat, float(g["min_size"]), float(g["max_size"]))
     with pytest.raises(ValueError):
         corr.processAuto(fg, False, False, m)
+
+
+@pytest.mark.parametrize("name", ["kkk_flat_mp", "kkk_sphere_mp"])
+def test_multipole_kkk_golden(gpu_lib, name):
+    """KKK LogMultipole through KKKCorr on a K field against the reference's KKKCorr."""
+    from cases3 import spec3
+    T = gpu_lib
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    s = spec3(str(g["case"]))
+    cat = {k[3:]: g[k] for k in g.files if k.startswith("c1_")}
+    nb, mn = s["nbins"], s["max_n"]
+    shape = (nb, nb, 2 * mn + 1)
+    keys = ("zeta", "zeta_im", "meand1", "meanlogd1", "meand2", "meanlogd2", "meand3",
+            "meanlogd3", "meanu", "meanv", "weight", "weight_im", "ntri")
+    out = {k: np.zeros(shape) for k in keys}
+    e = np.array([])
+    corr = T.KKKCorr(T.LogMultipole, s["min_sep"], s["max_sep"], nb, s["bin_size"], s["b"],
+                     s["a"], 0., 0., mn, 0., 0., 0., 0., 0, 0., 0.,
+                     -sys.float_info.max, sys.float_info.max, 0., 0., 0.,
+                     out["zeta"], out["zeta_im"], e, e, e, e, e, e, *[out[k] for k in keys[2:]])
+    f = H.gpu_field(T, "K", s["coords"], cat, float(g["min_size"]), float(g["max_size"]))
+    m = T.Euclidean if s["metric"] == "Euclidean" else T.Arc
+    corr.processAuto(f, False, False, m)
+    assert np.array_equal(out["ntri"], g["ref_ntri"]), name
+    for k in ("zeta", "zeta_im", "weight", "weight_im", "meand2", "meanlogd2", "meand3",
+              "meanlogd3"):
+        r = g["ref_" + k]
+        err = np.abs(out[k] - r).max() / max(np.abs(r).max(), 1e-300)
+        assert err <= TOL, f"{name} {k}: {err:.3e}"

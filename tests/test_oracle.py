@@ -90,3 +90,34 @@ def test_oracle_multipole_nnn_matches_reference(name):
     for k in ("weight", "weight_im", "meand2", "meanlogd2", "meand3", "meanlogd3"):
         r = g["ref_" + k]
         assert np.abs(out[k] - r).max() <= 1e-12 * max(np.abs(r).max(), 1e-300), k
+
+
+@pytest.mark.parametrize("name", ["kkk_flat_mp", "kkk_sphere_mp"])
+def test_oracle_multipole_kkk_identity(name):
+    """KKK LogMultipole (the reference's KKKCorr): its zeta is the multipole weight
+    contraction with every weight w replaced by w k (src/Corr3.cpp:1912-1965 against
+    MultipoleHelper<1>, 2108-2150), so the oracle's multipole with weights w k, position
+    weights w and no shear reproduces it; weight and ntri come from the plain weights."""
+    import os
+    from cases3 import spec3
+    from oracle import oracle as O
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    s = spec3(str(g["case"]))
+    c = {k[3:]: g[k] for k in g.files if k.startswith("c1_")}
+    zero = np.zeros(len(c["x"]))
+    bins = dict(min_sep=s["min_sep"], max_sep=s["max_sep"], nbins=s["nbins"],
+                bin_size=s["bin_size"], b=s["b"], a=s["a"])
+    args = (float(g["min_size"]), float(g["max_size"]), "mean", False, 3, 10)
+    fk = O.OracleField("G", s["coords"], c["x"], c["y"], c.get("z"), zero, zero,
+                       c["w"] * c["k"], c["w"], *args)
+    zk = O.multipole(s["metric"], bins, s["max_n"], fk, nthreads=1)
+    for mine, ref in (("weight", "zeta"), ("weight_im", "zeta_im")):
+        r = g["ref_" + ref]
+        assert np.abs(zk[mine] - r).max() <= 1e-12 * max(np.abs(r).max(), 1e-300), ref
+    fw = O.OracleField("G", s["coords"], c["x"], c["y"], c.get("z"), zero, zero, c["w"], None,
+                       *args)
+    ww = O.multipole(s["metric"], bins, s["max_n"], fw, nthreads=1)
+    assert np.array_equal(ww["ntri"], g["ref_ntri"])
+    for k in ("weight", "weight_im", "meand2", "meanlogd2", "meand3", "meanlogd3"):
+        r = g["ref_" + k]
+        assert np.abs(ww[k] - r).max() <= 1e-12 * max(np.abs(r).max(), 1e-300), k

@@ -694,8 +694,15 @@ class NNNCorr(GGGCorr):
     _dkind = 0
 
 
-# The 3-point classes of src/Corr3.cpp (WrapCorr3) other than GGG / NNN with LogMultipole.
-for _n in ("KKK", "NNK", "NKN", "KNN", "NKK", "KNK", "KKN", "NNG", "NGN", "GNN", "NGG",
+class KKKCorr(GGGCorr):
+    """KKKCorr (src/Corr3.cpp:4238) with LogMultipole binning: zeta0, zeta1 = zeta (real,
+    imaginary), weight, weight_im, ntri and the mean distances."""
+    _dkind = 1
+
+
+# The 3-point classes of src/Corr3.cpp (WrapCorr3) other than GGG / NNN / KKK with
+# LogMultipole.
+for _n in ("NNK", "NKN", "KNN", "NKK", "KNK", "KKN", "NNG", "NGN", "GNN", "NGG",
            "GNG", "GGN", "KKG", "KGK", "GKK", "KGG", "GKG", "GGK"):
     globals()[_n + "Corr"] = _not_on_path(_n + "Corr")
 del _n

@@ -77,7 +77,7 @@ struct tc_field {
 };
 
 struct tc_corr3 {
-    int dk = TC_GDATA;           // data kind of all three vertices (GGG or NNN)
+    int dk = TC_GDATA;           // data kind of all three vertices (GGG, NNN or KKK)
     int bin_type = 0, nbins = 0, maxn = 0;
     double minsep = 0., maxsep = 0., binsize = 0., b = 0., a = 0.;
     double* zeta[8] = {nullptr};
@@ -795,7 +795,8 @@ int corr3_process_auto(tc_corr3* c, tc_field* f, int quick, int metric)
 {
     if (!c || !f) { set_last_error("NULL argument"); return TC_ERR_ARG; }
     if (f->dkind != c->dk) {
-        set_last_error(c->dk == TC_GDATA ? "GGG needs a G field" : "NNN needs an N field");
+        set_last_error(c->dk == TC_GDATA ? "GGG needs a G field"
+                       : c->dk == TC_NDATA ? "NNN needs an N field" : "KKK needs a K field");
         return TC_ERR_ARG;
     }
     TC_TRY(check_metric(f->coords, metric));
@@ -846,8 +847,40 @@ int corr3_process_auto(tc_corr3* c, tc_field* f, int quick, int metric)
     cudaEventDestroy(e0); cudaEventDestroy(e1);
     c->ms = ms;
     if (rc) return rc == 3 ? TC_ERR_UNSUPPORTED : (rc == 5 ? TC_ERR_NOMEM : TC_ERR_DEVICE);
+    if (c->dk == TC_KDATA) {
+        // KKK: the same multipole over the cells re-weighted by w k; its weight arrays are
+        // zeta (real, imaginary).
+        TCell* tc2 = nullptr;
+        double* ls2 = nullptr;
+        float4* lsf2 = nullptr;
+        float* zero = nullptr;
+        std::vector<double> h2(15 * Z);
+        int rc2 = 0;
+        do {
+            if ((rc2 = dalloc(&tc2, ncap)) || (rc2 = dalloc(&ls2, 4 * (size_t)ncap)) ||
+                (rc2 = dalloc(&lsf2, ncap)) || (rc2 = dalloc(&zero, ncap)))
+                break;
+            if (cudaMemsetAsync(zero, 0, sizeof(float) * (size_t)ncap, st) != cudaSuccess) {
+                set_last_error("memset failed"); rc2 = TC_ERR_CUDA; break;
+            }
+            if ((rc2 = launch_weight_swap((int)ncap, f->tcells, f->leafsums, tc2, ls2, lsf2, st)))
+                break;
+            MPParams P2 = P;
+            P2.w = f->cells.d1;
+            P2.d1 = zero; P2.d2 = zero;
+            P2.ls = ls2; P2.lsf = lsf2; P2.tc = tc2;
+            const int r = run_multipole(P2, c->X, P2.ntop, st, h2.data());
+            if (r) rc2 = r == 3 ? TC_ERR_UNSUPPORTED : (r == 5 ? TC_ERR_NOMEM : TC_ERR_DEVICE);
+        } while (0);
+        dfree(tc2); dfree(ls2); dfree(lsf2); dfree(zero);
+        if (rc2) return rc2;
+        for (size_t i = 0; i < Z; ++i) {
+            c->zeta[0][i] += h2[12 * Z + i];
+            c->zeta[1][i] += h2[13 * Z + i];
+        }
+    }
     // Corr3 adds into the caller's arrays (calculateZeta, src/Corr3.cpp:1861-1974).
-    for (int q = 0; q < 8; ++q)
+    for (int q = 0; q < 8 && c->dk == TC_GDATA; ++q)
         if (c->zeta[q]) for (size_t i = 0; i < Z; ++i) c->zeta[q][i] += h[q * Z + i];
     double* dst[7] = {c->meand2, c->meanlogd2, c->meand3, c->meanlogd3, c->weight, c->weight_im,
                       c->ntri};
@@ -1585,10 +1618,11 @@ int tc_corr3_create(int d1, int d2, int d3, int bin_type, double minsep, double 
     (void)vbinsize; (void)bv; (void)meand1; (void)meanlogd1; (void)meanu; (void)meanv;
     if (!out) { set_last_error("out is NULL"); return TC_ERR_ARG; }
     *out = nullptr;
-    // GGG, and NNN: its weight, ntri and mean distances are the multipole's own sums,
-    // which do not depend on the payload (an N field carries none).
-    if (d1 != d2 || d2 != d3 || (d1 != TC_GDATA && d1 != TC_NDATA)) {
-        set_last_error("only GGG and NNN are on the GPU 3-point path");
+    // GGG; NNN: its weight, ntri and mean distances are the multipole's own sums, which do
+    // not depend on the payload (an N field carries none); KKK: its zeta is the weight
+    // contraction over the weights w k (a second pass on the same tree).
+    if (d1 != d2 || d2 != d3 || (d1 != TC_GDATA && d1 != TC_NDATA && d1 != TC_KDATA)) {
+        set_last_error("only GGG, NNN and KKK are on the GPU 3-point path");
         return TC_ERR_UNSUPPORTED;
     }
     if (bin_type != TC_LOGMULTIPOLE) {
@@ -1606,6 +1640,7 @@ int tc_corr3_create(int d1, int d2, int d3, int bin_type, double minsep, double 
     }
     const bool needz = (d1 == TC_GDATA);
     if ((needz && (!zeta0 || !zeta1 || !zeta2 || !zeta3 || !zeta4 || !zeta5 || !zeta6 || !zeta7)) ||
+        (d1 == TC_KDATA && (!zeta0 || !zeta1)) ||
         !meand2 || !meanlogd2 || !meand3 || !meanlogd3 || !weight || !weight_im || !ntri) {
         set_last_error("missing output array");
         return TC_ERR_ARG;
@@ -1615,7 +1650,7 @@ int tc_corr3_create(int d1, int d2, int d3, int bin_type, double minsep, double 
     c->bin_type = bin_type; c->nbins = nbins; c->maxn = nubins;
     c->minsep = minsep; c->maxsep = maxsep; c->binsize = binsize; c->b = b; c->a = a;
     double* z[8] = {zeta0, zeta1, zeta2, zeta3, zeta4, zeta5, zeta6, zeta7};
-    for (int q = 0; q < 8; ++q) c->zeta[q] = needz ? z[q] : nullptr;
+    for (int q = 0; q < 8; ++q) c->zeta[q] = (needz || (d1 == TC_KDATA && q < 2)) ? z[q] : nullptr;
     c->meand2 = meand2; c->meanlogd2 = meanlogd2; c->meand3 = meand3; c->meanlogd3 = meanlogd3;
     c->weight = weight; c->weight_im = weight_im; c->ntri = ntri;
     *out = c;

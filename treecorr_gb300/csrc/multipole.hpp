@@ -112,6 +112,9 @@ struct MPScratch {
 };
 
 int launch_leaf_sums(int ncap, const Cells& C, double* ls, float4* lsf, cudaStream_t st);
+// K-field cells re-weighted by w k for the KKK zeta pass (records, leaf sums).
+int launch_weight_swap(int ncap, const TCell* tc, const double* ls, TCell* tc2, double* ls2,
+                       float4* lsf2, cudaStream_t st);
 // Runs both phases and the reduction; h_out receives 15 arrays of nbins*nbins*(2*maxn+1)
 // doubles: gam0r, gam0i, gam1r, gam1i, gam2r, gam2i, gam3r, gam3i, meand2, meanlogd2,
 // meand3, meanlogd3, weight, weight_im, ntri.
