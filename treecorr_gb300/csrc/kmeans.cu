@@ -528,37 +528,61 @@ __global__ void k_km_paint_big(Cells C, const int* assign, int tag, const int* i
 }
 
 // QuickAssign (mode 0, src/KMeans.cpp:890-942) and SelectPatch (mode 1, 944-1011).
-__global__ void k_quick_assign(const double* cen, int npatch, int dim, const double* x,
-                               const double* y, const double* z, int64_t n, int mode, int patch,
-                               int64_t* out, int cen_in_smem)
+// Distances are first taken in FP32 on coordinates shifted to an origin o (centre 0):
+// with R the largest |coordinate - o| of the point and the centres and u = 2^-24, the FP32
+// distance differs from the reference's FP64 one by at most 84 u R^2 (two roundings of each
+// shifted coordinate, the squares and the sum), so E = 6e-6 R^2 bounds it.  Only centres
+// within 4 E of the FP32 minimum can be the FP64 minimum or tie with it; those are compared
+// in FP64 with the reference's expression, in index order, so the result is the reference's.
+__global__ void k_quick_assign(const double* cen, const float4* cen32, float rc, int npatch,
+                               int dim, const double* x, const double* y, const double* z,
+                               int64_t n, int mode, int patch, int64_t* out, int cen_in_smem)
 {
-    extern __shared__ __align__(16) double qsm[];
-    const double* c = cen;
+    extern __shared__ __align__(16) float4 qsm[];
+    const float4* c32 = cen32;
     if (cen_in_smem) {
-        for (int q = threadIdx.x; q < npatch * dim; q += blockDim.x) qsm[q] = cen[q];
+        for (int q = threadIdx.x; q < npatch; q += blockDim.x) qsm[q] = cen32[q];
         __syncthreads();
-        c = qsm;
+        c32 = qsm;
     }
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double px = x[i], py = y[i], pz = z ? z[i] : 0.;
-    auto dist = [&](int k) {
-        return dsq3(px, py, pz, c[dim * k], c[dim * k + 1], dim == 3 ? c[dim * k + 2] : 0.);
+    const double ox = cen[0], oy = cen[1], oz = dim == 3 ? cen[2] : 0.;
+    const float qx = (float)(px - ox), qy = (float)(py - oy), qz = (float)(pz - oz);
+    const float r = fmaxf(rc, fmaxf(fabsf(qx), fmaxf(fabsf(qy), fabsf(qz))));
+    const float E = 6e-6f * r * r;
+    auto d32 = [&](int k) {
+        const float4 c = c32[k];
+        const float dx = qx - c.x, dy = qy - c.y, dz = qz - c.z;
+        return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+    };
+    auto d64 = [&](int k) {
+        return dsq3(px, py, pz, cen[dim * k], cen[dim * k + 1], dim == 3 ? cen[dim * k + 2] : 0.);
     };
     if (mode == 0) {
-        int kmin = 0;
-        double mn = dist(0);
-        for (int k = 1; k < npatch; ++k) {
-            const double d = dist(k);
-            if (d < mn) { kmin = k; mn = d; }
+        float mn = d32(0);
+        for (int k = 1; k < npatch; ++k) mn = fminf(mn, d32(k));
+        const float lim = mn + 4.f * E;
+        int kmin = -1;
+        double best = 0.;
+        for (int k = 0; k < npatch; ++k) {
+            if (d32(k) > lim) continue;
+            const double d = d64(k);
+            if (kmin < 0 || d < best) { kmin = k; best = d; }
         }
         out[i] = kmin;
     } else {
-        const double pd = dist(patch);
+        const float p32 = d32(patch);
+        double p64 = -1.;
         int64_t use = 1;
         for (int q = 0; q < npatch; ++q) {
             if (q == patch) continue;
-            if (dist(q) < pd) { use = 0; break; }
+            const float d = d32(q);
+            if (d > p32 + 2.f * E) continue;
+            if (d < p32 - 2.f * E) { use = 0; break; }
+            if (p64 < 0.) p64 = d64(patch);
+            if (d64(q) < p64) { use = 0; break; }
         }
         out[i] = use;
     }
@@ -1159,6 +1183,7 @@ int quick_common(int mode, int patch, const double* centers, int npatch, const d
     if (n <= 0) return 0;
     const int dim = z ? 3 : 2;
     double *dc = nullptr, *dx = nullptr, *dy = nullptr, *dz = nullptr;
+    float4* d32c = nullptr;
     int64_t* dout = nullptr;
     int rc = 0;
     do {
@@ -1177,11 +1202,25 @@ int quick_common(int mode, int patch, const double* centers, int npatch, const d
             if (z) cudaMemcpyAsync(dz, z, sizeof(double) * n, cudaMemcpyHostToDevice, st);
             px = dx; py = dy; pz = z ? dz : nullptr; po = dout;
         }
-        const size_t csm = sizeof(double) * npatch * dim;
+        // The centres shifted to centre 0, in FP32, and their largest |coordinate|.
+        std::vector<float4> h32(npatch);
+        float rmax = 0.f;
+        for (int k = 0; k < npatch; ++k) {
+            const float cx = (float)(centers[dim * k] - centers[0]);
+            const float cy = (float)(centers[dim * k + 1] - centers[1]);
+            const float cz = dim == 3 ? (float)(centers[dim * k + 2] - centers[2]) : 0.f;
+            h32[k] = make_float4(cx, cy, cz, 0.f);
+            rmax = std::max(rmax, std::max(std::fabs(cx), std::max(std::fabs(cy), std::fabs(cz))));
+        }
+        if ((rc = dalloc(&d32c, (size_t)npatch)) != 0) break;
+        if (cudaMemcpyAsync(d32c, h32.data(), sizeof(float4) * npatch, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+            set_last_error("centre copy failed"); rc = TC_ERR_CUDA; break;
+        }
+        const size_t csm = sizeof(float4) * npatch;
         const int in_smem = csm <= 48 * 1024 ? 1 : 0;
         count_launch();
         k_quick_assign<<<(unsigned)((n + 255) / 256), 256, in_smem ? csm : 0, st>>>(
-            dc, npatch, dim, px, py, pz, n, mode, patch, po, in_smem);
+            dc, d32c, rmax, npatch, dim, px, py, pz, n, mode, patch, po, in_smem);
         if (cudaGetLastError() != cudaSuccess) { set_last_error("assign launch failed"); rc = TC_ERR_CUDA; break; }
         if (!on_device &&
             cudaMemcpyAsync(out, dout, sizeof(int64_t) * n, cudaMemcpyDeviceToHost, st) != cudaSuccess) {
@@ -1189,7 +1228,7 @@ int quick_common(int mode, int patch, const double* centers, int npatch, const d
         }
         if (cudaStreamSynchronize(st) != cudaSuccess) { set_last_error("assign failed"); rc = TC_ERR_CUDA; break; }
     } while (0);
-    dfree(dc); dfree(dx); dfree(dy); dfree(dz); dfree(dout);
+    dfree(dc); dfree(d32c); dfree(dx); dfree(dy); dfree(dz); dfree(dout);
     return rc;
 }
 
