@@ -241,6 +241,14 @@ void tc_corr3_free(tc_corr3* c);
  * 1124-1175): the G_n / Gamma_n multipole accumulation over one G field. */
 int tc_corr3_process_auto(tc_corr3* c, tc_field* f, int dots, int quick, int metric);
 
+/* BaseCorr3.processCross12 -> ProcessCross12c -> BaseCorr3::multipole(field1, field2)
+ * (src/Corr3.cpp:4199, 3730-3768, 1177-1237): vertex 1 from f1, vertices 2 and 3 from f2,
+ * both fields of the class's data kind and coordinate system.  Only ordered = 1 is on the
+ * GPU path (what the Python layer passes for ordered=True, treecorr/corr3base.py:1968);
+ * ordered = 0 returns TC_ERR_UNSUPPORTED. */
+int tc_corr3_process_cross12(tc_corr3* c, tc_field* f1, tc_field* f2, int ordered, int dots,
+                             int quick, int metric);
+
 /* Device time of the last tc_corr3_process_auto call in ms (no reference counterpart). */
 double tc_corr3_last_ms(const tc_corr3* c);
 

@@ -830,14 +830,16 @@ double split_or_gn(const Params& P, const Field& f, const Node& c1,
     return maxrem;
 }
 
-// BaseCorr3::multipoleFinish, src/Corr3.cpp:1548-1613.
-void multipole_finish(const Params& P, const Field& f, int i1, const std::vector<int>& c2list,
-                      MPS& mp, int mink_zeta, double maxr, Out3& O)
+// BaseCorr3::multipoleFinish, src/Corr3.cpp:1548-1613.  c1 is a cell of f1, the list holds
+// cells of f2 (f2 = f1 for an auto-correlation).
+void multipole_finish(const Params& P, const Field& f1, const Field& f2, int i1,
+                      const std::vector<int>& c2list, MPS& mp, int mink_zeta, double maxr,
+                      Out3& O)
 {
-    const Node& c1 = f.nodes[i1];
+    const Node& c1 = f1.nodes[i1];
     bool anysplit1 = false;
     std::vector<int> newlist;
-    maxr = split_or_gn(P, f, c1, c2list, newlist, anysplit1, mp, maxr);
+    maxr = split_or_gn(P, f2, c1, c2list, newlist, anysplit1, mp, maxr);
     if (!newlist.empty()) {
         if (maxr < P.maxsep) {
             int k = maxr < P.minsep ? 0 : int((std::log(maxr) - P.logminsep) / P.binsize) + 1;
@@ -848,31 +850,31 @@ void multipole_finish(const Params& P, const Field& f, int i1, const std::vector
         }
         if (anysplit1) {
             MPS copy = mp;
-            multipole_finish(P, f, c1.left, newlist, mp, mink_zeta, maxr, O);
-            multipole_finish(P, f, c1.right, newlist, copy, mink_zeta, maxr, O);
+            multipole_finish(P, f1, f2, c1.left, newlist, mp, mink_zeta, maxr, O);
+            multipole_finish(P, f1, f2, c1.right, newlist, copy, mink_zeta, maxr, O);
         } else {
-            multipole_finish(P, f, i1, newlist, mp, mink_zeta, maxr, O);
+            multipole_finish(P, f1, f2, i1, newlist, mp, mink_zeta, maxr, O);
         }
     } else {
         calculate_zeta(P, c1, mp, 0, mink_zeta, O);
     }
 }
 
-// BaseCorr3::multipoleSplit1, src/Corr3.cpp:1374-1408.
-void multipole_split1(const Params& P, const Field& f, int i1, const std::vector<int>& c2list,
-                      MPS& mp, Out3& O)
+// BaseCorr3::multipoleSplit1, src/Corr3.cpp:1374-1408 (c1 in f1, the list in f2).
+void multipole_split1(const Params& P, const Field& f1, const Field& f2, int i1,
+                      const std::vector<int>& c2list, MPS& mp, Out3& O)
 {
-    const Node& c1 = f.nodes[i1];
+    const Node& c1 = f1.nodes[i1];
     double s1 = c1.size;
     std::vector<int> newlist;
-    split_c2_cells(P, f, c1, c2list, newlist);
+    split_c2_cells(P, f2, c1, c2list, newlist);
     double maxbsq_eff = P.maxsepsq * std::min(P.bsq, P.asq);
     if (double(s1) * double(s1) > maxbsq_eff) {
-        multipole_split1(P, f, c1.left, newlist, mp, O);
-        multipole_split1(P, f, c1.right, newlist, mp, O);
+        multipole_split1(P, f1, f2, c1.left, newlist, mp, O);
+        multipole_split1(P, f1, f2, c1.right, newlist, mp, O);
     } else {
         mp.clear();
-        multipole_finish(P, f, i1, newlist, mp, P.nbins, 0., O);
+        multipole_finish(P, f1, f2, i1, newlist, mp, P.nbins, 0., O);
     }
 }
 
@@ -1297,31 +1299,36 @@ int orc_corr2_process_rows(int dtype, int metric, int quick, double minsep, doub
 }
 
 
-// BaseCorr3::multipole (auto) for GGG with LogMultipole binning, src/Corr3.cpp:1124-1175.
+// BaseCorr3::multipole for GGG with LogMultipole binning: auto (h2 = h1, src/Corr3.cpp:
+// 1124-1175) or cross12 (vertex 1 from h1, vertices 2 and 3 from h2, 1177-1237).
 // Outputs have nbins*nbins*(2*maxn+1) entries, accumulated (+=) like the reference's.
-int orc_corr3_multipole_auto(int metric, int quick, double minsep, double maxsep, int nbins,
-                             double binsize, double b, double a, int maxn, void* h, int nthreads,
-                             double** gam8, double* meand2, double* meanlogd2, double* meand3,
-                             double* meanlogd3, double* weight, double* weight_im, double* ntri)
+static int multipole_run(int metric, int quick, double minsep, double maxsep, int nbins,
+                         double binsize, double b, double a, int maxn, void* h1, void* h2,
+                         int nthreads, double** gam8, double* meand2, double* meanlogd2,
+                         double* meand3, double* meanlogd3, double* weight, double* weight_im,
+                         double* ntri)
 {
-    Field* f = static_cast<Field*>(h);
-    if (f->dtype != DG || f->spin != 2) return 1;
-    Params P = make_params(DG * 16 + DG, f->coords, metric, quick, minsep, maxsep, nbins, binsize, b, a);
+    Field* f1 = static_cast<Field*>(h1);
+    Field* f2 = static_cast<Field*>(h2);
+    if (f1->dtype != DG || f1->spin != 2 || f2->dtype != DG || f2->spin != 2) return 1;
+    if (f1->coords != f2->coords) return 2;
+    Params P = make_params(DG * 16 + DG, f1->coords, metric, quick, minsep, maxsep, nbins, binsize, b, a);
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #else
     (void)nthreads;
 #endif
-    if (f->pts.empty()) return 0;
-    build_cells(*f);
-    const long n1 = (long)f->tops.size();
+    if (f1->pts.empty() || f2->pts.empty()) return 0;
+    build_cells(*f1);
+    if (f2 != f1) build_cells(*f2);
+    const long n1 = (long)f1->tops.size();
     Out3 total(nbins, maxn);
 #pragma omp parallel
     {
         Out3 O(nbins, maxn);
         MPS mp(nbins, maxn);
 #pragma omp for schedule(dynamic)
-        for (long i = 0; i < n1; ++i) multipole_split1(P, *f, f->tops[i], f->tops, mp, O);
+        for (long i = 0; i < n1; ++i) multipole_split1(P, *f1, *f2, f1->tops[i], f2->tops, mp, O);
 #pragma omp critical
         total.add(O);
     }
@@ -1334,6 +1341,27 @@ int orc_corr3_multipole_auto(int metric, int quick, double minsep, double maxsep
         ntri[i] += total.ntri[i];
     }
     return 0;
+}
+
+int orc_corr3_multipole_auto(int metric, int quick, double minsep, double maxsep, int nbins,
+                             double binsize, double b, double a, int maxn, void* h, int nthreads,
+                             double** gam8, double* meand2, double* meanlogd2, double* meand3,
+                             double* meanlogd3, double* weight, double* weight_im, double* ntri)
+{
+    return multipole_run(metric, quick, minsep, maxsep, nbins, binsize, b, a, maxn, h, h,
+                         nthreads, gam8, meand2, meanlogd2, meand3, meanlogd3, weight,
+                         weight_im, ntri);
+}
+
+int orc_corr3_multipole_cross12(int metric, int quick, double minsep, double maxsep, int nbins,
+                                double binsize, double b, double a, int maxn, void* h1,
+                                void* h2, int nthreads, double** gam8, double* meand2,
+                                double* meanlogd2, double* meand3, double* meanlogd3,
+                                double* weight, double* weight_im, double* ntri)
+{
+    return multipole_run(metric, quick, minsep, maxsep, nbins, binsize, b, a, maxn, h1, h2,
+                         nthreads, gam8, meand2, meanlogd2, meand3, meanlogd3, weight,
+                         weight_im, ntri);
 }
 
 int orc_max_threads(void)

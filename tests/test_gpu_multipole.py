@@ -147,3 +147,71 @@ def test_multipole_kkk_golden(gpu_lib, name):
         r = g["ref_" + k]
         err = np.abs(out[k] - r).max() / max(np.abs(r).max(), 1e-300)
         assert err <= TOL, f"{name} {k}: {err:.3e}"
+
+
+def _corr3(T, letter, s):
+    """A GGG / NNN / KKK LogMultipole object with its outputs (the reference's argument
+    order, src/Corr3.cpp:4207-4225)."""
+    nb, mn = s["nbins"], s["max_n"]
+    shape = (nb, nb, 2 * mn + 1)
+    common = ("meand1", "meanlogd1", "meand2", "meanlogd2", "meand3", "meanlogd3", "meanu",
+              "meanv", "weight", "weight_im", "ntri")
+    zk = {"G": MP_OUT[:8], "K": ("zeta", "zeta_im"), "N": ()}[letter]
+    out = {k: np.zeros(shape) for k in zk + common}
+    e = np.array([])
+    zeta = [out[k] for k in zk] + [e] * (8 - len(zk))
+    cls = getattr(T, letter * 3 + "Corr")
+    corr = cls(T.LogMultipole, s["min_sep"], s["max_sep"], nb, s["bin_size"], s["b"], s["a"],
+               0., 0., mn, 0., 0., 0., 0., 0, 0., 0., -sys.float_info.max, sys.float_info.max,
+               0., 0., 0., *zeta, *[out[k] for k in common])
+    return corr, out, zk
+
+
+@pytest.mark.parametrize("name", ["ggg_flat_mp_x12", "ggg_sphere_mp_x12", "nnn_flat_mp_x12",
+                                  "kkk_sphere_mp_x12"])
+def test_multipole_cross12_golden(gpu_lib, name):
+    """processCross12 (ordered = 1): vertex 1 from the first catalog, vertices 2 and 3 from
+    the second, against the reference's own processCross12."""
+    from cases3 import spec3
+    T = gpu_lib
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    s = spec3(str(g["case"]))
+    letter = str(g["letter"])
+    cats = [{k[3:]: g[k] for k in g.files if k.startswith(p)} for p in ("c1_", "c2_")]
+    f1, f2 = [H.gpu_field(T, letter, s["coords"], c, float(g["min_size"]), float(g["max_size"]))
+              for c in cats]
+    m = T.Euclidean if s["metric"] == "Euclidean" else T.Arc
+    corr, out, zk = _corr3(T, letter, s)
+    corr.processCross12(f1, f2, 1, False, False, m)
+    assert np.array_equal(out["ntri"], g["ref_ntri"]), name
+    for k in zk + ("weight", "weight_im", "meand2", "meanlogd2", "meand3", "meanlogd3"):
+        r = g["ref_" + k]
+        err = np.abs(out[k] - r).max() / max(np.abs(r).max(), 1e-300)
+        assert err <= TOL, f"{name} {k}: {err:.3e}"
+    # ordered = 0 needs the three-field cross multipole, which is not on the GPU path.
+    with pytest.raises(NotImplementedError):
+        corr.processCross12(f1, f2, 0, False, False, m)
+    # Fields of another data kind are refused.
+    other = "N" if letter != "N" else "G"
+    fo = H.gpu_field(T, other, s["coords"], cats[1], float(g["min_size"]), float(g["max_size"]))
+    with pytest.raises(ValueError):
+        corr.processCross12(f1, fo, 1, False, False, m)
+
+
+def test_multipole_cross12_self_equals_auto(gpu_lib):
+    """cross12 of a catalog with a second field built from the same catalog is its
+    auto-correlation: the same triangles (ntri exact) and the same sums up to their order."""
+    from cases3 import spec3
+    T = gpu_lib
+    name = "ggg_flat_mp"
+    s = spec3(name)
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    cat = {k[3:]: g[k] for k in g.files if k.startswith("c1_")}
+    f1 = H.gpu_field(T, "G", s["coords"], cat, float(g["min_size"]), float(g["max_size"]))
+    f2 = H.gpu_field(T, "G", s["coords"], cat, float(g["min_size"]), float(g["max_size"]))
+    corr, out, _ = _corr3(T, "G", s)
+    corr.processCross12(f1, f2, 1, False, False, T.Euclidean)
+    assert np.array_equal(out["ntri"], g["ref_ntri"])
+    err = max_rel_err(out, {k: g["ref_" + k] for k in MP_OUT})
+    for k, v in err.items():
+        assert v <= TOL, f"{k}: {v:.3e}"

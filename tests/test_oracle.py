@@ -121,3 +121,54 @@ def test_oracle_multipole_kkk_identity(name):
     for k in ("weight", "weight_im", "meand2", "meanlogd2", "meand3", "meanlogd3"):
         r = g["ref_" + k]
         assert np.abs(ww[k] - r).max() <= 1e-12 * max(np.abs(r).max(), 1e-300), k
+
+
+@pytest.mark.parametrize("name", ["ggg_flat_mp_x12", "ggg_sphere_mp_x12", "nnn_flat_mp_x12",
+                                  "kkk_sphere_mp_x12"])
+def test_oracle_multipole_cross12_matches_reference(name):
+    """processCross12 (ordered = 1) with LogMultipole: vertex 1 from the first catalog,
+    vertices 2 and 3 from the second (src/Corr3.cpp:1177-1237).  NNN and KKK go through the
+    same identities as their auto-correlations (zero shear; weights w k for KKK's zeta)."""
+    import os
+    from cases3 import spec3
+    from oracle import oracle as O
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    s = spec3(str(g["case"]))
+    letter = str(g["letter"])
+    bins = dict(min_sep=s["min_sep"], max_sep=s["max_sep"], nbins=s["nbins"],
+                bin_size=s["bin_size"], b=s["b"], a=s["a"])
+    args = (float(g["min_size"]), float(g["max_size"]), "mean", False, 3, 10)
+    cats = [{k[3:]: g[k] for k in g.files if k.startswith(p)} for p in ("c1_", "c2_")]
+
+    def fields(kind):
+        out = []
+        for c in cats:
+            zero = np.zeros(len(c["x"]))
+            if kind == "G":
+                out.append(O.OracleField("G", s["coords"], c["x"], c["y"], c.get("z"), c["g1"],
+                                         c["g2"], c["w"], None, *args))
+            elif kind == "wk":
+                out.append(O.OracleField("G", s["coords"], c["x"], c["y"], c.get("z"), zero,
+                                         zero, c["w"] * c["k"], c["w"], *args))
+            else:
+                out.append(O.OracleField("G", s["coords"], c["x"], c["y"], c.get("z"), zero,
+                                         zero, c["w"], None, *args))
+        return out
+
+    def close(a, r, what):
+        assert np.abs(a - r).max() <= 1e-12 * max(np.abs(r).max(), 1e-300), what
+
+    f1, f2 = fields("G" if letter == "G" else "w")
+    out = O.multipole(s["metric"], bins, s["max_n"], f1, nthreads=1, f2=f2)
+    assert np.array_equal(out["ntri"], g["ref_ntri"])
+    assert out["ntri"].sum() > 0
+    for k in ("weight", "weight_im", "meand2", "meanlogd2", "meand3", "meanlogd3"):
+        close(out[k], g["ref_" + k], k)
+    if letter == "G":
+        for k in O.MP_KEYS[:8]:
+            close(out[k], g["ref_" + k], k)
+    if letter == "K":
+        k1, k2 = fields("wk")
+        zk = O.multipole(s["metric"], bins, s["max_n"], k1, nthreads=1, f2=k2)
+        close(zk["weight"], g["ref_zeta"], "zeta")
+        close(zk["weight_im"], g["ref_zeta_im"], "zeta_im")

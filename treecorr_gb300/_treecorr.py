@@ -129,6 +129,8 @@ def lib():
         L.tc_corr3_free.argtypes = [vp]
         L.tc_corr3_process_auto.restype = ctypes.c_int
         L.tc_corr3_process_auto.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.tc_corr3_process_cross12.restype = ctypes.c_int
+        L.tc_corr3_process_cross12.argtypes = [vp, vp, vp] + [ctypes.c_int] * 4
         L.tc_corr3_last_ms.restype = ctypes.c_double
         L.tc_corr3_last_ms.argtypes = [vp]
         L.tc_corr3_stats.restype = ctypes.c_int
@@ -618,16 +620,26 @@ del _x, _a
 
 
 class BaseCorr3:
-    """BaseCorr3 (src/Corr3.cpp:4228-4235): processAuto for GGG with LogMultipole binning."""
+    """BaseCorr3 (src/Corr3.cpp:4187-4201): processAuto and processCross12 (ordered = 1)
+    with LogMultipole binning."""
 
     def processAuto(self, field, dots, quick, metric):
         _check(lib().tc_corr3_process_auto(self._h, field._h, int(bool(dots)), int(bool(quick)),
                                            int(metric)))
 
-    def processCross12(self, *args):
-        raise NotImplementedError("3-point cross correlations are not on the GPU path")
+    def processCross12(self, field1, field2, ordered, dots, quick, metric):
+        """One vertex from field1, two from field2 (ProcessCross12c, src/Corr3.cpp:3730-3768);
+        ordered = 0 (the three-field cross multipole) raises NotImplementedError."""
+        if int(ordered) != 1:
+            raise NotImplementedError("processCross12 with ordered = 0 needs the three-field "
+                                      "cross multipole, which is not on the GPU path")
+        _check(lib().tc_corr3_process_cross12(self._h, field1._h, field2._h, int(ordered),
+                                              int(bool(dots)), int(bool(quick)), int(metric)))
 
-    processCross21 = processCross = processCross12
+    def processCross21(self, *args):
+        raise NotImplementedError("processCross21 and processCross are not on the GPU path")
+
+    processCross = processCross21
 
     def triviallyZero(self, *args):
         raise NotImplementedError("triviallyZero for 3-point is not on the GPU path")

@@ -790,29 +790,110 @@ int corr_process_auto_noalloc(tc_corr2* c, tc_field* f, int quick, int metric)
     return TC_OK;
 }
 
-// BaseCorr3::multipole (auto) for GGG / LogMultipole, src/Corr3.cpp:1124-1175.
-int corr3_process_auto(tc_corr3* c, tc_field* f, int quick, int metric)
+// The cells of two fields in one id space: field 2's cells follow field 1's, with their
+// child ids shifted, so that the multipole kernels walk vertex 1 in field 1 and the pair
+// lists in field 2 without knowing there are two trees.
+struct JoinedCells {
+    Cells cells = {};
+    double* ls = nullptr;
+    float4* lsf = nullptr;
+    TCell* tc = nullptr;
+    int* tops2 = nullptr;
+    ~JoinedCells()
+    {
+        dfree(cells.x); dfree(cells.y); dfree(cells.z); dfree(cells.size); dfree(cells.w);
+        dfree(cells.d1); dfree(cells.d2); dfree(cells.n); dfree(cells.left);
+        dfree(cells.right); dfree(ls); dfree(lsf); dfree(tc); dfree(tops2);
+    }
+};
+
+__global__ void k_shift_ids(int* a, long long n, int base)
 {
-    if (!c || !f) { set_last_error("NULL argument"); return TC_ERR_ARG; }
-    if (f->dkind != c->dk) {
-        set_last_error(c->dk == TC_GDATA ? "GGG needs a G field"
-                       : c->dk == TC_NDATA ? "NNN needs an N field" : "KKK needs a K field");
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && a[i] >= 0) a[i] += base;
+}
+
+int join_cells(const tc_field* f1, const tc_field* f2, JoinedCells& J, cudaStream_t st)
+{
+    const size_t n1 = 2 * (size_t)f1->n - 1, n2 = 2 * (size_t)f2->n - 1, n = n1 + n2;
+    TC_TRY(dalloc(&J.cells.x, n)); TC_TRY(dalloc(&J.cells.y, n)); TC_TRY(dalloc(&J.cells.z, n));
+    TC_TRY(dalloc(&J.cells.size, n)); TC_TRY(dalloc(&J.cells.w, n));
+    TC_TRY(dalloc(&J.cells.d1, n)); TC_TRY(dalloc(&J.cells.d2, n));
+    TC_TRY(dalloc(&J.cells.n, n)); TC_TRY(dalloc(&J.cells.left, n));
+    TC_TRY(dalloc(&J.cells.right, n));
+    TC_TRY(dalloc(&J.ls, 4 * n)); TC_TRY(dalloc(&J.lsf, n)); TC_TRY(dalloc(&J.tc, n));
+    TC_TRY(dalloc(&J.tops2, f2->tops.size()));
+    auto cat = [&](auto* dst, const auto* a, const auto* b, size_t per) -> int {
+        const size_t e = sizeof(*dst) * per;
+        TC_CU(cudaMemcpyAsync(dst, a, e * n1, cudaMemcpyDeviceToDevice, st));
+        TC_CU(cudaMemcpyAsync(dst + per * n1, b, e * n2, cudaMemcpyDeviceToDevice, st));
+        return 0;
+    };
+    const Cells &A = f1->cells, &B = f2->cells;
+    TC_TRY(cat(J.cells.x, A.x, B.x, 1)); TC_TRY(cat(J.cells.y, A.y, B.y, 1));
+    TC_TRY(cat(J.cells.z, A.z, B.z, 1)); TC_TRY(cat(J.cells.size, A.size, B.size, 1));
+    TC_TRY(cat(J.cells.w, A.w, B.w, 1)); TC_TRY(cat(J.cells.d1, A.d1, B.d1, 1));
+    TC_TRY(cat(J.cells.d2, A.d2, B.d2, 1)); TC_TRY(cat(J.cells.n, A.n, B.n, 1));
+    TC_TRY(cat(J.cells.left, A.left, B.left, 1)); TC_TRY(cat(J.cells.right, A.right, B.right, 1));
+    TC_TRY(cat(J.ls, f1->leafsums, f2->leafsums, 4)); TC_TRY(cat(J.lsf, f1->leafsums_f, f2->leafsums_f, 1));
+    TC_TRY(cat(J.tc, f1->tcells, f2->tcells, 1));
+    TC_CU(cudaMemcpyAsync(J.tops2, f2->d_tops, sizeof(int) * f2->tops.size(),
+                          cudaMemcpyDeviceToDevice, st));
+    const unsigned g2 = (unsigned)((n2 + 255) / 256);
+    count_launch(); k_shift_ids<<<g2, 256, 0, st>>>(J.cells.left + n1, (long long)n2, (int)n1);
+    count_launch(); k_shift_ids<<<g2, 256, 0, st>>>(J.cells.right + n1, (long long)n2, (int)n1);
+    count_launch(); k_rebase_cells<<<g2, 256, 0, st>>>(J.tc + n1, (long long)n2, (int)n1, 0);
+    const unsigned gt = (unsigned)((f2->tops.size() + 255) / 256);
+    count_launch(); k_shift_ids<<<gt, 256, 0, st>>>(J.tops2, (long long)f2->tops.size(), (int)n1);
+    TC_CU(cudaGetLastError());
+    return 0;
+}
+
+int ensure_leaf_sums(tc_field* f, cudaStream_t st)
+{
+    if (f->leafsums) return 0;
+    const int64_t ncap = 2 * f->n - 1;
+    TC_TRY(dalloc(&f->leafsums, 4 * (size_t)ncap));
+    TC_TRY(dalloc(&f->leafsums_f, (size_t)ncap));
+    TC_TRY(launch_leaf_sums((int)ncap, f->cells, f->leafsums, f->leafsums_f, st));
+    return 0;
+}
+
+// BaseCorr3::multipole for GGG / NNN / KKK with LogMultipole binning: the auto-correlation
+// (f2 == f1, src/Corr3.cpp:1124-1175) or cross12, vertex 1 from f1 and vertices 2 and 3 from
+// f2 (src/Corr3.cpp:1177-1237, which ProcessCross12c runs for ordered = 1, 3730-3768).
+int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, int quick, int metric)
+{
+    if (!c || !f1 || !f2) { set_last_error("NULL argument"); return TC_ERR_ARG; }
+    const char* need = c->dk == TC_GDATA ? "GGG needs G fields"
+                       : c->dk == TC_NDATA ? "NNN needs N fields" : "KKK needs K fields";
+    if (f1->dkind != c->dk || f2->dkind != c->dk) { set_last_error(need); return TC_ERR_ARG; }
+    if (f1->coords != f2->coords) {
+        set_last_error("the fields have different coordinate systems");
         return TC_ERR_ARG;
     }
-    TC_TRY(check_metric(f->coords, metric));
-    if (f->n == 0) return TC_OK;
+    TC_TRY(check_metric(f1->coords, metric));
+    if (f1->n == 0 || f2->n == 0) return TC_OK;
     cudaStream_t st;
     TC_TRY(stream_get(&st));
-    TC_TRY(field_build(f));
-    const int64_t ncap = 2 * f->n - 1;
-    if (!f->leafsums) {
-        TC_TRY(dalloc(&f->leafsums, 4 * (size_t)ncap));
-        TC_TRY(dalloc(&f->leafsums_f, (size_t)ncap));
-        TC_TRY(launch_leaf_sums((int)ncap, f->cells, f->leafsums, f->leafsums_f, st));
+    TC_TRY(field_build(f1));
+    TC_TRY(ensure_leaf_sums(f1, st));
+    const bool cross = f2 != f1;
+    JoinedCells J;
+    if (cross) {
+        TC_TRY(field_build(f2));
+        TC_TRY(ensure_leaf_sums(f2, st));
+        TC_TRY(join_cells(f1, f2, J, st));
+    }
+    const int64_t ncap = cross ? (2 * f1->n - 1) + (2 * f2->n - 1) : 2 * f1->n - 1;
+    const Cells& CC = cross ? J.cells : f1->cells;
+    if (ncap >= (int64_t)INT32_MAX) {
+        set_last_error("too many cells for 32-bit cell ids");
+        return TC_ERR_UNSUPPORTED;
     }
     MPParams P;
     std::memset(&P, 0, sizeof(P));
-    P.coords = f->coords; P.metric = metric; P.quick = quick ? 1 : 0;
+    P.coords = f1->coords; P.metric = metric; P.quick = quick ? 1 : 0;
     P.nbins = c->nbins; P.maxn = c->maxn;
     P.minsep = c->minsep; P.maxsep = c->maxsep; P.binsize = c->binsize; P.b = c->b; P.a = c->a;
     // BaseCorr3 constructor, src/Corr3.cpp:107-115.
@@ -825,13 +906,14 @@ int corr3_process_auto(tc_corr3* c, tc_field* f, int quick, int metric)
     P.f_q25 = (float)(0.25 * (P.binsize + P.b) * (P.binsize + P.b));
     P.f_logminsep = (float)P.logminsep; P.f_binsize = (float)P.binsize; P.f_b = (float)P.b;
     P.f_minba = (float)std::min(P.bsq, P.asq);
-    P.x = f->cells.x; P.y = f->cells.y; P.z = f->cells.z;
-    P.size = f->cells.size; P.w = f->cells.w; P.d1 = f->cells.d1; P.d2 = f->cells.d2;
-    P.n = f->cells.n; P.left = f->cells.left; P.right = f->cells.right;
-    P.ls = f->leafsums;
-    P.lsf = f->leafsums_f;
-    P.tc = f->tcells;
-    P.tops = f->d_tops; P.ntop = (int)f->tops.size();
+    P.x = CC.x; P.y = CC.y; P.z = CC.z;
+    P.size = CC.size; P.w = CC.w; P.d1 = CC.d1; P.d2 = CC.d2;
+    P.n = CC.n; P.left = CC.left; P.right = CC.right;
+    P.ls = cross ? J.ls : f1->leafsums;
+    P.lsf = cross ? J.lsf : f1->leafsums_f;
+    P.tc = cross ? J.tc : f1->tcells;
+    P.tops = f1->d_tops; P.ntop = (int)f1->tops.size();
+    P.tops2 = cross ? J.tops2 : f1->d_tops; P.ntop2 = (int)f2->tops.size();
     P.ncells = (int)ncap;
     const size_t Z = (size_t)c->nbins * c->nbins * (2 * c->maxn + 1);
     std::vector<double> h(15 * Z);
@@ -863,10 +945,10 @@ int corr3_process_auto(tc_corr3* c, tc_field* f, int quick, int metric)
             if (cudaMemsetAsync(zero, 0, sizeof(float) * (size_t)ncap, st) != cudaSuccess) {
                 set_last_error("memset failed"); rc2 = TC_ERR_CUDA; break;
             }
-            if ((rc2 = launch_weight_swap((int)ncap, f->tcells, f->leafsums, tc2, ls2, lsf2, st)))
+            if ((rc2 = launch_weight_swap((int)ncap, P.tc, P.ls, tc2, ls2, lsf2, st)))
                 break;
             MPParams P2 = P;
-            P2.w = f->cells.d1;
+            P2.w = CC.d1;
             P2.d1 = zero; P2.d2 = zero;
             P2.ls = ls2; P2.lsf = lsf2; P2.tc = tc2;
             const int r = run_multipole(P2, c->X, P2.ntop, st, h2.data());
@@ -1667,7 +1749,19 @@ void tc_corr3_free(tc_corr3* c)
 int tc_corr3_process_auto(tc_corr3* c, tc_field* f, int dots, int quick, int metric)
 {
     (void)dots;
-    return corr3_process_auto(c, f, quick, metric);
+    return corr3_run(c, f, f, quick, metric);
+}
+
+int tc_corr3_process_cross12(tc_corr3* c, tc_field* f1, tc_field* f2, int ordered, int dots,
+                             int quick, int metric)
+{
+    (void)dots;
+    if (ordered != 1) {
+        set_last_error("processCross12 with ordered = 0 needs the three-field cross multipole, "
+                       "which is not on the GPU path");
+        return TC_ERR_UNSUPPORTED;
+    }
+    return corr3_run(c, f1, f2, quick, metric);
 }
 
 double tc_corr3_last_ms(const tc_corr3* c) { return c ? c->ms : 0.; }

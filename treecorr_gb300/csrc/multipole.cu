@@ -377,7 +377,9 @@ __device__ __forceinline__ bool mp_valid_cell(const MPParams& P, int c)
 { return c >= 0 && c < P.ncells && P.n[c] > 0; }
 
 // ---------------------------------------------------------------------------------------
-// Phase 1: multipoleSplit1 + splitC2Cells, one block per top-level cell.
+// Phase 1: multipoleSplit1 + splitC2Cells, one block per vertex-1 top-level cell; its pair
+// list starts as all top cells of the pair field (the same field for an auto-correlation,
+// src/Corr3.cpp:1124-1175; field 2 for cross12, 1177-1237).
 
 struct P1Entry { int c1, off, len, pad; };
 
@@ -389,11 +391,11 @@ __global__ void __launch_bounds__(MB) k_mp_split1(MPParams P)
     const int b = blockIdx.x;
     int* arena = P.arena1 + (size_t)b * P.arena1_cap;
     const int tid = threadIdx.x;
-    for (int j = tid; j < P.ntop; j += MB) arena[j] = P.tops[j];
+    for (int j = tid; j < P.ntop2; j += MB) arena[j] = P.tops2[j];
     if (tid == 0) {
         sp = 0;
-        top_rel = P.ntop;
-        stk[sp++] = {P.tops[b], 0, P.ntop, 0};
+        top_rel = P.ntop2;
+        stk[sp++] = {P.tops[b], 0, P.ntop2, 0};
     }
     __syncthreads();
     int guard = 0;
@@ -1747,7 +1749,7 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
     const int nsg = std::max(1, 2 * nsm / etiles);
     const int recf = mp_rec_floats(nb, M);
     const long long acc_cap = 4096;
-    X.want_a1 = std::max<long long>(X.want_a1, 4LL * ntop + (1 << 16));
+    X.want_a1 = std::max<long long>(X.want_a1, 4LL * std::max(ntop, P.ntop2) + (1 << 16));
     X.want_jobs = std::max<long long>(X.want_jobs, 1 << 18);
     X.want_a2 = std::max<long long>(X.want_a2, 1 << 20);
     X.want_slots = std::max(X.want_slots, 32);

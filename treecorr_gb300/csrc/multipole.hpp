@@ -35,8 +35,10 @@ struct MPParams {
     const double* ls;
     const float4* lsf;   // the leaf sums as floats
     const TCell* tc;     // packed cells (float hi/lo positions and payload)
-    const int* tops;
+    const int* tops;     // vertex-1 top cells (one phase-1 block each)
     int ntop;
+    const int* tops2;    // top cells that start every vertex's pair list
+    int ntop2;
     int ncells;          // cell ids are 0 .. ncells-1
     // Phase 1: per-block list arenas and the job list.
     int* arena1;
