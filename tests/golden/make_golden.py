@@ -280,18 +280,23 @@ if __name__ == "__main__" and "--mp-kkk" in sys.argv:
 
 # 3-point cross12 with LogMultipole (processCross12 with ordered = 1, src/Corr3.cpp:4199,
 # 3730-3768, 1177-1237): vertex 1 from the case's catalog, vertices 2 and 3 from a second
-# catalog of the same kind (seed + 1000), for GGG, NNN and KKK.
+# catalog (seed + 1000), for GGG, NNN, KKK, NKK and KNN.
 X12_CASES = {
-    "ggg_flat_mp_x12": ("G", "ggg_flat_mp"),
-    "ggg_sphere_mp_x12": ("G", "ggg_sphere_mp"),
-    "nnn_flat_mp_x12": ("N", "ggg_flat_mp"),
-    "kkk_sphere_mp_x12": ("K", "ggg_sphere_mp"),
+    "ggg_flat_mp_x12": ("GGG", "ggg_flat_mp"),
+    "ggg_sphere_mp_x12": ("GGG", "ggg_sphere_mp"),
+    "nnn_flat_mp_x12": ("NNN", "ggg_flat_mp"),
+    "kkk_sphere_mp_x12": ("KKK", "ggg_sphere_mp"),
+    "nkk_flat_mp_x12": ("NKK", "ggg_flat_mp"),
+    "knn_sphere_mp_x12": ("KNN", "ggg_sphere_mp"),
 }
 
 if __name__ == "__main__" and "--mp-x12" in sys.argv:
     _treecorr.SetOMPThreads(1)
     from cases3 import make_inputs3, spec3
-    for name, (letter, gname) in X12_CASES.items():
+    only = [a for a in sys.argv[1:] if not a.startswith("--")]
+    for name, (letters, gname) in X12_CASES.items():
+        if only and name not in only:
+            continue
         s = spec3(gname)
         cat1 = make_inputs3(gname)
         cat2 = make_inputs3(gname, seed=20240601 + 1000)
@@ -304,20 +309,20 @@ if __name__ == "__main__" and "--mp-x12" in sys.argv:
         shape = (nb, nb, 2 * mn + 1)
         common = ("meand1", "meanlogd1", "meand2", "meanlogd2", "meand3", "meanlogd3", "meanu",
                   "meanv", "weight", "weight_im", "ntri")
-        zk = {"G": ("gam0r", "gam0i", "gam1r", "gam1i", "gam2r", "gam2i", "gam3r", "gam3i"),
-              "K": ("zeta", "zeta_im"), "N": ()}[letter]
+        zk = (("gam0r", "gam0i", "gam1r", "gam1i", "gam2r", "gam2i", "gam3r", "gam3i")
+              if letters == "GGG" else ("zeta", "zeta_im") if "K" in letters else ())
         out = {k: np.zeros(shape) for k in zk + common}
         e = np.array([])
         zeta = [out[k] for k in zk] + [e] * (8 - len(zk))
-        cls = getattr(_treecorr, letter * 3 + "Corr")
+        cls = getattr(_treecorr, letters + "Corr")
         corr = cls(_treecorr.LogMultipole, s["min_sep"], s["max_sep"], nb, s["bin_size"], s["b"],
                    s["a"], 0., 0., mn, 0., 0., 0., 0., 0, 0., 0.,
                    -sys.float_info.max, sys.float_info.max, 0., 0., 0.,
                    *zeta, *[out[k] for k in common])
-        f1 = build_field(letter, s["coords"], cat1, min_size, max_size, "mean", False, 3, 10)
-        f2 = build_field(letter, s["coords"], cat2, min_size, max_size, "mean", False, 3, 10)
+        f1 = build_field(letters[0], s["coords"], cat1, min_size, max_size, "mean", False, 3, 10)
+        f2 = build_field(letters[1], s["coords"], cat2, min_size, max_size, "mean", False, 3, 10)
         corr.processCross12(f1, f2, 1, False, False, METRIC[s["metric"]])
-        save = dict(min_size=min_size, max_size=max_size, case=gname, letter=letter)
+        save = dict(min_size=min_size, max_size=max_size, case=gname, letters=letters)
         for tag, cat in (("c1_", cat1), ("c2_", cat2)):
             for k, v in cat.items():
                 if v is not None:

@@ -149,18 +149,18 @@ def test_multipole_kkk_golden(gpu_lib, name):
         assert err <= TOL, f"{name} {k}: {err:.3e}"
 
 
-def _corr3(T, letter, s):
+def _corr3(T, letters, s):
     """A GGG / NNN / KKK LogMultipole object with its outputs (the reference's argument
     order, src/Corr3.cpp:4207-4225)."""
     nb, mn = s["nbins"], s["max_n"]
     shape = (nb, nb, 2 * mn + 1)
     common = ("meand1", "meanlogd1", "meand2", "meanlogd2", "meand3", "meanlogd3", "meanu",
               "meanv", "weight", "weight_im", "ntri")
-    zk = {"G": MP_OUT[:8], "K": ("zeta", "zeta_im"), "N": ()}[letter]
+    zk = MP_OUT[:8] if letters == "GGG" else ("zeta", "zeta_im") if "K" in letters else ()
     out = {k: np.zeros(shape) for k in zk + common}
     e = np.array([])
     zeta = [out[k] for k in zk] + [e] * (8 - len(zk))
-    cls = getattr(T, letter * 3 + "Corr")
+    cls = getattr(T, letters + "Corr")
     corr = cls(T.LogMultipole, s["min_sep"], s["max_sep"], nb, s["bin_size"], s["b"], s["a"],
                0., 0., mn, 0., 0., 0., 0., 0, 0., 0., -sys.float_info.max, sys.float_info.max,
                0., 0., 0., *zeta, *[out[k] for k in common])
@@ -168,7 +168,7 @@ def _corr3(T, letter, s):
 
 
 @pytest.mark.parametrize("name", ["ggg_flat_mp_x12", "ggg_sphere_mp_x12", "nnn_flat_mp_x12",
-                                  "kkk_sphere_mp_x12"])
+                                  "kkk_sphere_mp_x12", "nkk_flat_mp_x12", "knn_sphere_mp_x12"])
 def test_multipole_cross12_golden(gpu_lib, name):
     """processCross12 (ordered = 1): vertex 1 from the first catalog, vertices 2 and 3 from
     the second, against the reference's own processCross12."""
@@ -176,12 +176,12 @@ def test_multipole_cross12_golden(gpu_lib, name):
     T = gpu_lib
     g = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
     s = spec3(str(g["case"]))
-    letter = str(g["letter"])
+    letters = str(g["letters"])
     cats = [{k[3:]: g[k] for k in g.files if k.startswith(p)} for p in ("c1_", "c2_")]
-    f1, f2 = [H.gpu_field(T, letter, s["coords"], c, float(g["min_size"]), float(g["max_size"]))
-              for c in cats]
+    f1, f2 = [H.gpu_field(T, L, s["coords"], c, float(g["min_size"]), float(g["max_size"]))
+              for L, c in zip(letters[:2], cats)]
     m = T.Euclidean if s["metric"] == "Euclidean" else T.Arc
-    corr, out, zk = _corr3(T, letter, s)
+    corr, out, zk = _corr3(T, letters, s)
     corr.processCross12(f1, f2, 1, False, False, m)
     assert np.array_equal(out["ntri"], g["ref_ntri"]), name
     for k in zk + ("weight", "weight_im", "meand2", "meanlogd2", "meand3", "meanlogd3"):
@@ -191,11 +191,17 @@ def test_multipole_cross12_golden(gpu_lib, name):
     # ordered = 0 needs the three-field cross multipole, which is not on the GPU path.
     with pytest.raises(NotImplementedError):
         corr.processCross12(f1, f2, 0, False, False, m)
-    # Fields of another data kind are refused.
-    other = "N" if letter != "N" else "G"
+    # Fields of another data kind are refused (vertex 1 and the pair field swapped, or a G
+    # field in place of an N one), and so is processAuto for a mixed class.
+    other = "N" if letters[1] != "N" else "G"
     fo = H.gpu_field(T, other, s["coords"], cats[1], float(g["min_size"]), float(g["max_size"]))
     with pytest.raises(ValueError):
         corr.processCross12(f1, fo, 1, False, False, m)
+    if letters[0] != letters[1]:
+        with pytest.raises(ValueError):
+            corr.processCross12(f2, f1, 1, False, False, m)
+        with pytest.raises(ValueError):
+            corr.processAuto(f1, False, False, m)
 
 
 def test_multipole_cross12_self_equals_auto(gpu_lib):
@@ -209,7 +215,7 @@ def test_multipole_cross12_self_equals_auto(gpu_lib):
     cat = {k[3:]: g[k] for k in g.files if k.startswith("c1_")}
     f1 = H.gpu_field(T, "G", s["coords"], cat, float(g["min_size"]), float(g["max_size"]))
     f2 = H.gpu_field(T, "G", s["coords"], cat, float(g["min_size"]), float(g["max_size"]))
-    corr, out, _ = _corr3(T, "G", s)
+    corr, out, _ = _corr3(T, "GGG", s)
     corr.processCross12(f1, f2, 1, False, False, T.Euclidean)
     assert np.array_equal(out["ntri"], g["ref_ntri"])
     err = max_rel_err(out, {k: g["ref_" + k] for k in MP_OUT})

@@ -124,51 +124,47 @@ def test_oracle_multipole_kkk_identity(name):
 
 
 @pytest.mark.parametrize("name", ["ggg_flat_mp_x12", "ggg_sphere_mp_x12", "nnn_flat_mp_x12",
-                                  "kkk_sphere_mp_x12"])
+                                  "kkk_sphere_mp_x12", "nkk_flat_mp_x12", "knn_sphere_mp_x12"])
 def test_oracle_multipole_cross12_matches_reference(name):
     """processCross12 (ordered = 1) with LogMultipole: vertex 1 from the first catalog,
-    vertices 2 and 3 from the second (src/Corr3.cpp:1177-1237).  NNN and KKK go through the
-    same identities as their auto-correlations (zero shear; weights w k for KKK's zeta)."""
+    vertices 2 and 3 from the second (src/Corr3.cpp:1177-1237).  The N and K classes go
+    through the identities of their auto-correlations: weight, ntri and the mean distances
+    do not depend on the payload, and zeta (MultipoleHelper<1>, 2108-2214) is the weight
+    contraction with every K point's weight w replaced by w k."""
     import os
     from cases3 import spec3
     from oracle import oracle as O
     g = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
     s = spec3(str(g["case"]))
-    letter = str(g["letter"])
+    letters = str(g["letters"])
     bins = dict(min_sep=s["min_sep"], max_sep=s["max_sep"], nbins=s["nbins"],
                 bin_size=s["bin_size"], b=s["b"], a=s["a"])
     args = (float(g["min_size"]), float(g["max_size"]), "mean", False, 3, 10)
     cats = [{k[3:]: g[k] for k in g.files if k.startswith(p)} for p in ("c1_", "c2_")]
 
-    def fields(kind):
-        out = []
-        for c in cats:
-            zero = np.zeros(len(c["x"]))
-            if kind == "G":
-                out.append(O.OracleField("G", s["coords"], c["x"], c["y"], c.get("z"), c["g1"],
-                                         c["g2"], c["w"], None, *args))
-            elif kind == "wk":
-                out.append(O.OracleField("G", s["coords"], c["x"], c["y"], c.get("z"), zero,
-                                         zero, c["w"] * c["k"], c["w"], *args))
-            else:
-                out.append(O.OracleField("G", s["coords"], c["x"], c["y"], c.get("z"), zero,
-                                         zero, c["w"], None, *args))
-        return out
+    def field(c, kind, wk):
+        zero = np.zeros(len(c["x"]))
+        if kind == "G":
+            return O.OracleField("G", s["coords"], c["x"], c["y"], c.get("z"), c["g1"], c["g2"],
+                                 c["w"], None, *args)
+        w, wpos = (c["w"] * c["k"], c["w"]) if (wk and kind == "K") else (c["w"], None)
+        return O.OracleField("G", s["coords"], c["x"], c["y"], c.get("z"), zero, zero, w, wpos,
+                             *args)
 
     def close(a, r, what):
         assert np.abs(a - r).max() <= 1e-12 * max(np.abs(r).max(), 1e-300), what
 
-    f1, f2 = fields("G" if letter == "G" else "w")
+    f1, f2 = field(cats[0], letters[0], False), field(cats[1], letters[1], False)
     out = O.multipole(s["metric"], bins, s["max_n"], f1, nthreads=1, f2=f2)
     assert np.array_equal(out["ntri"], g["ref_ntri"])
     assert out["ntri"].sum() > 0
     for k in ("weight", "weight_im", "meand2", "meanlogd2", "meand3", "meanlogd3"):
         close(out[k], g["ref_" + k], k)
-    if letter == "G":
+    if letters == "GGG":
         for k in O.MP_KEYS[:8]:
             close(out[k], g["ref_" + k], k)
-    if letter == "K":
-        k1, k2 = fields("wk")
+    if "K" in letters:
+        k1, k2 = field(cats[0], letters[0], True), field(cats[1], letters[1], True)
         zk = O.multipole(s["metric"], bins, s["max_n"], k1, nthreads=1, f2=k2)
         close(zk["weight"], g["ref_zeta"], "zeta")
         close(zk["weight_im"], g["ref_zeta_im"], "zeta_im")

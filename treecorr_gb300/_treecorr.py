@@ -681,8 +681,8 @@ class GGGCorr(BaseCorr3):
                                  "nbins*nbins*(2*max_n+1) entries")
         self._outs = arrs
         h = ctypes.c_void_p()
-        d = self._dkind
-        _check(lib().tc_corr3_create(d, d, d, int(bin_type), float(minsep), float(maxsep),
+        d1, d2 = self._dkind, getattr(self, "_dkind2", self._dkind)
+        _check(lib().tc_corr3_create(d1, d2, d2, int(bin_type), float(minsep), float(maxsep),
                                      int(nbins), float(binsize), float(b), float(a), float(minu),
                                      float(maxu), int(nubins), float(ubinsize), float(bu),
                                      float(minv), float(maxv), int(nvbins), float(vbinsize),
@@ -712,9 +712,24 @@ class KKKCorr(GGGCorr):
     _dkind = 1
 
 
-# The 3-point classes of src/Corr3.cpp (WrapCorr3) other than GGG / NNN / KKK with
-# LogMultipole.
-for _n in ("NNK", "NKN", "KNN", "NKK", "KNK", "KKN", "NNG", "NGN", "GNN", "NGG",
+class NKKCorr(GGGCorr):
+    """NKKCorr (src/Corr3.cpp:4245) with LogMultipole binning, processCross12 only (an N
+    vertex and two K vertices): zeta0, zeta1 = zeta (real, imaginary), weight, weight_im,
+    ntri and the mean distances."""
+    _dkind = 0
+    _dkind2 = 1
+
+
+class KNNCorr(GGGCorr):
+    """KNNCorr (src/Corr3.cpp:4243) with LogMultipole binning, processCross12 only (a K
+    vertex and two N vertices): zeta0, zeta1 = zeta (real, imaginary), weight, weight_im,
+    ntri and the mean distances."""
+    _dkind = 1
+    _dkind2 = 0
+
+
+# The 3-point classes of src/Corr3.cpp (WrapCorr3) that are not on the GPU path.
+for _n in ("NNK", "NKN", "KNK", "KKN", "NNG", "NGN", "GNN", "NGG",
            "GNG", "GGN", "KKG", "KGK", "GKK", "KGG", "GKG", "GGK"):
     globals()[_n + "Corr"] = _not_on_path(_n + "Corr")
 del _n

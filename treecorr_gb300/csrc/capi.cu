@@ -77,7 +77,8 @@ struct tc_field {
 };
 
 struct tc_corr3 {
-    int dk = TC_GDATA;           // data kind of all three vertices (GGG, NNN or KKK)
+    int dv = TC_GDATA;           // data kind of vertex 1
+    int dk = TC_GDATA;           // data kind of vertices 2 and 3 (GGG, NNN, KKK, NKK, KNN)
     int bin_type = 0, nbins = 0, maxn = 0;
     double minsep = 0., maxsep = 0., binsize = 0., b = 0., a = 0.;
     double* zeta[8] = {nullptr};
@@ -865,9 +866,13 @@ int ensure_leaf_sums(tc_field* f, cudaStream_t st)
 int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, int quick, int metric)
 {
     if (!c || !f1 || !f2) { set_last_error("NULL argument"); return TC_ERR_ARG; }
-    const char* need = c->dk == TC_GDATA ? "GGG needs G fields"
-                       : c->dk == TC_NDATA ? "NNN needs N fields" : "KKK needs K fields";
-    if (f1->dkind != c->dk || f2->dkind != c->dk) { set_last_error(need); return TC_ERR_ARG; }
+    if (f1->dkind != c->dv || f2->dkind != c->dk) {
+        static const char L[] = "NKGZVTQ";
+        const char cls[4] = {L[c->dv], L[c->dk], L[c->dk], 0};
+        set_last_error(std::string(cls) + ": the fields have the wrong data kind (vertex 1 " +
+                       L[c->dv] + ", vertices 2 and 3 " + L[c->dk] + ")");
+        return TC_ERR_ARG;
+    }
     if (f1->coords != f2->coords) {
         set_last_error("the fields have different coordinate systems");
         return TC_ERR_ARG;
@@ -929,32 +934,53 @@ int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, int quick, int metric)
     cudaEventDestroy(e0); cudaEventDestroy(e1);
     c->ms = ms;
     if (rc) return rc == 3 ? TC_ERR_UNSUPPORTED : (rc == 5 ? TC_ERR_NOMEM : TC_ERR_DEVICE);
-    if (c->dk == TC_KDATA) {
-        // KKK: the same multipole over the cells re-weighted by w k; its weight arrays are
-        // zeta (real, imaginary).
+    if (c->dv == TC_KDATA || c->dk == TC_KDATA) {
+        // KKK, NKK, KNN (MultipoleHelper<1>, src/Corr3.cpp:2108-2214): zeta is the weight
+        // contraction with the vertex weight w1 k1 (K) or w1 (N) and the pair weights
+        // w k (K) or w (N), so the multipole runs again over records whose weights are
+        // replaced by w k where the field is a K field; its weight arrays are zeta (real,
+        // imaginary).
         TCell* tc2 = nullptr;
         double* ls2 = nullptr;
         float4* lsf2 = nullptr;
+        float* w2 = nullptr;
         float* zero = nullptr;
         std::vector<double> h2(15 * Z);
         int rc2 = 0;
+        // Cell ranges of the two fields in the joined id space (one range for an auto).
+        const int64_t n1c = cross ? 2 * f1->n - 1 : ncap;
+        struct { int64_t lo, len; bool swap; } rng[2] = {
+            {0, n1c, c->dv == TC_KDATA}, {n1c, ncap - n1c, c->dk == TC_KDATA}};
         do {
             if ((rc2 = dalloc(&tc2, ncap)) || (rc2 = dalloc(&ls2, 4 * (size_t)ncap)) ||
-                (rc2 = dalloc(&lsf2, ncap)) || (rc2 = dalloc(&zero, ncap)))
+                (rc2 = dalloc(&lsf2, ncap)) || (rc2 = dalloc(&w2, ncap)) ||
+                (rc2 = dalloc(&zero, ncap)))
                 break;
-            if (cudaMemsetAsync(zero, 0, sizeof(float) * (size_t)ncap, st) != cudaSuccess) {
-                set_last_error("memset failed"); rc2 = TC_ERR_CUDA; break;
+            if (cudaMemsetAsync(zero, 0, sizeof(float) * (size_t)ncap, st) != cudaSuccess ||
+                cudaMemcpyAsync(tc2, P.tc, sizeof(TCell) * ncap, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+                cudaMemcpyAsync(ls2, P.ls, sizeof(double) * 4 * ncap, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+                cudaMemcpyAsync(lsf2, P.lsf, sizeof(float4) * ncap, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+                cudaMemcpyAsync(w2, CC.w, sizeof(float) * ncap, cudaMemcpyDeviceToDevice, st) != cudaSuccess) {
+                set_last_error("device copy failed"); rc2 = TC_ERR_CUDA; break;
             }
-            if ((rc2 = launch_weight_swap((int)ncap, P.tc, P.ls, tc2, ls2, lsf2, st)))
-                break;
+            for (const auto& r : rng) {
+                if (!r.swap || r.len <= 0 || rc2) continue;
+                if (cudaMemcpyAsync(w2 + r.lo, CC.d1 + r.lo, sizeof(float) * r.len,
+                                    cudaMemcpyDeviceToDevice, st) != cudaSuccess) {
+                    set_last_error("device copy failed"); rc2 = TC_ERR_CUDA; break;
+                }
+                rc2 = launch_weight_swap((int)r.len, P.tc + r.lo, P.ls + 4 * r.lo, tc2 + r.lo,
+                                         ls2 + 4 * r.lo, lsf2 + r.lo, st);
+            }
+            if (rc2) break;
             MPParams P2 = P;
-            P2.w = CC.d1;
+            P2.w = w2;
             P2.d1 = zero; P2.d2 = zero;
             P2.ls = ls2; P2.lsf = lsf2; P2.tc = tc2;
             const int r = run_multipole(P2, c->X, P2.ntop, st, h2.data());
             if (r) rc2 = r == 3 ? TC_ERR_UNSUPPORTED : (r == 5 ? TC_ERR_NOMEM : TC_ERR_DEVICE);
         } while (0);
-        dfree(tc2); dfree(ls2); dfree(lsf2); dfree(zero);
+        dfree(tc2); dfree(ls2); dfree(lsf2); dfree(w2); dfree(zero);
         if (rc2) return rc2;
         for (size_t i = 0; i < Z; ++i) {
             c->zeta[0][i] += h2[12 * Z + i];
@@ -1701,10 +1727,12 @@ int tc_corr3_create(int d1, int d2, int d3, int bin_type, double minsep, double 
     if (!out) { set_last_error("out is NULL"); return TC_ERR_ARG; }
     *out = nullptr;
     // GGG; NNN: its weight, ntri and mean distances are the multipole's own sums, which do
-    // not depend on the payload (an N field carries none); KKK: its zeta is the weight
-    // contraction over the weights w k (a second pass on the same tree).
-    if (d1 != d2 || d2 != d3 || (d1 != TC_GDATA && d1 != TC_NDATA && d1 != TC_KDATA)) {
-        set_last_error("only GGG, NNN and KKK are on the GPU 3-point path");
+    // not depend on the payload (an N field carries none); KKK, NKK, KNN: zeta is the weight
+    // contraction over the weights w k of the K vertices (a second pass on the same tree).
+    const bool same = d1 == d2 && (d1 == TC_GDATA || d1 == TC_NDATA || d1 == TC_KDATA);
+    const bool nk = (d1 == TC_NDATA && d2 == TC_KDATA) || (d1 == TC_KDATA && d2 == TC_NDATA);
+    if (d2 != d3 || !(same || nk)) {
+        set_last_error("only GGG, NNN, KKK, NKK and KNN are on the GPU 3-point path");
         return TC_ERR_UNSUPPORTED;
     }
     if (bin_type != TC_LOGMULTIPOLE) {
@@ -1722,17 +1750,19 @@ int tc_corr3_create(int d1, int d2, int d3, int bin_type, double minsep, double 
     }
     const bool needz = (d1 == TC_GDATA);
     if ((needz && (!zeta0 || !zeta1 || !zeta2 || !zeta3 || !zeta4 || !zeta5 || !zeta6 || !zeta7)) ||
-        (d1 == TC_KDATA && (!zeta0 || !zeta1)) ||
+        ((d1 == TC_KDATA || d2 == TC_KDATA) && (!zeta0 || !zeta1)) ||
         !meand2 || !meanlogd2 || !meand3 || !meanlogd3 || !weight || !weight_im || !ntri) {
         set_last_error("missing output array");
         return TC_ERR_ARG;
     }
     tc_corr3* c = new tc_corr3();
-    c->dk = d1;
+    c->dv = d1;
+    c->dk = d2;
     c->bin_type = bin_type; c->nbins = nbins; c->maxn = nubins;
     c->minsep = minsep; c->maxsep = maxsep; c->binsize = binsize; c->b = b; c->a = a;
     double* z[8] = {zeta0, zeta1, zeta2, zeta3, zeta4, zeta5, zeta6, zeta7};
-    for (int q = 0; q < 8; ++q) c->zeta[q] = (needz || (d1 == TC_KDATA && q < 2)) ? z[q] : nullptr;
+    const bool kz = d1 == TC_KDATA || d2 == TC_KDATA;
+    for (int q = 0; q < 8; ++q) c->zeta[q] = (needz || (kz && q < 2)) ? z[q] : nullptr;
     c->meand2 = meand2; c->meanlogd2 = meanlogd2; c->meand3 = meand3; c->meanlogd3 = meanlogd3;
     c->weight = weight; c->weight_im = weight_im; c->ntri = ntri;
     *out = c;
