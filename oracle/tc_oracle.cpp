@@ -365,6 +365,10 @@ struct Params {
     int k1, k2, s1, s2;   // payload kind (DN/DK/DG) and spin of the two fields
     double minsep, maxsep, binsize, b, a;
     double logminsep, halfminsep, minsepsq, maxsepsq, bsq, asq;
+    // 3-point: 1 when vertex 1 is an N or K field and the pairs G fields (NGG, KGG): G_n
+    // without the +-1 buffer, self-pair sums without z^2 (Corr3::getMP2 buffer 0,
+    // src/Corr3.cpp:1307-1313); its "shear" (d1, d2) then holds (w1 or w1 k1, 0).
+    int vreal = 0;
 };
 
 // MetricHelper<Euclidean>::DistSq (include/Metric.h:143-147, 202-207) and
@@ -678,7 +682,7 @@ void calculate_gn(const Params& P, const Node& c1, const Node& c2, double r, dou
     wg *= e;
     wgsq *= e * e;
     cd abswgsq = c2.sumabswzsq;
-    cd zsq = z * z;
+    cd zsq = P.vreal ? cd(1., 0.) : z * z;
     mp.gg0[k] += wgsq * std::conj(zsq);
     mp.gg1[k] += wgsq * zsq;
     mp.gg2[k] += abswgsq * std::conj(zsq);
@@ -742,13 +746,16 @@ void calculate_zeta(const Params& P, const Node& c1, const MPS& mp, int kstart, 
             }
         }
     }
-    // gam0..3 (Porth et al. eqs. 21, 23-25 with the projection already applied to G).
+    // gam0..3 (Porth et al. eqs. 21, 23-25 with the projection already applied to G).  For
+    // NGG / KGG (s = 0, wg1 = w1 or w1 k1) g0 and g2 are MultipoleHelper<2>'s gam0 and gam2
+    // (src/Corr3.cpp:2216-2317), its zeta0 and zeta1.
+    const int s = P.vreal ? 0 : 1;
     auto add_gam = [&](int a, int b, bool diag) {
         for (int n = -maxn; n <= maxn; ++n) {
-            cd g0 = wg1 * mp.G(a, n - 1) * mp.G(b, -n - 1);
-            cd g1 = std::conj(wg1) * mp.G(a, n + 1) * mp.G(b, -n + 1);
-            cd g2 = wg1 * mp.G(a, n - 1) * std::conj(mp.G(b, n + 1));
-            cd g3 = wg1 * std::conj(mp.G(a, -n + 1)) * mp.G(b, -n - 1);
+            cd g0 = wg1 * mp.G(a, n - s) * mp.G(b, -n - s);
+            cd g1 = std::conj(wg1) * mp.G(a, n + s) * mp.G(b, -n + s);
+            cd g2 = wg1 * mp.G(a, n - s) * std::conj(mp.G(b, n + s));
+            cd g3 = wg1 * std::conj(mp.G(a, -n + s)) * mp.G(b, -n - s);
             if (diag) {
                 g0 -= wg1 * mp.gg0[a];
                 g1 -= std::conj(wg1) * mp.gg1[a];
@@ -1304,15 +1311,19 @@ int orc_corr2_process_rows(int dtype, int metric, int quick, double minsep, doub
 // Outputs have nbins*nbins*(2*maxn+1) entries, accumulated (+=) like the reference's.
 static int multipole_run(int metric, int quick, double minsep, double maxsep, int nbins,
                          double binsize, double b, double a, int maxn, void* h1, void* h2,
-                         int nthreads, double** gam8, double* meand2, double* meanlogd2,
-                         double* meand3, double* meanlogd3, double* weight, double* weight_im,
-                         double* ntri)
+                         int vreal, int nthreads, double** gam8, double* meand2,
+                         double* meanlogd2, double* meand3, double* meanlogd3, double* weight,
+                         double* weight_im, double* ntri)
 {
     Field* f1 = static_cast<Field*>(h1);
     Field* f2 = static_cast<Field*>(h2);
-    if (f1->dtype != DG || f1->spin != 2 || f2->dtype != DG || f2->spin != 2) return 1;
+    // Vertex 1: a G field, or for NGG / KGG a K field whose k is 1 (N) or k (K), so that
+    // its cells' d1 is the real vertex weight (no parallel transport for spin 0).
+    const bool v_ok = vreal ? (f1->dtype == DK && f1->spin == 0) : (f1->dtype == DG && f1->spin == 2);
+    if (!v_ok || f2->dtype != DG || f2->spin != 2) return 1;
     if (f1->coords != f2->coords) return 2;
     Params P = make_params(DG * 16 + DG, f1->coords, metric, quick, minsep, maxsep, nbins, binsize, b, a);
+    P.vreal = vreal;
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #else
@@ -1348,19 +1359,19 @@ int orc_corr3_multipole_auto(int metric, int quick, double minsep, double maxsep
                              double** gam8, double* meand2, double* meanlogd2, double* meand3,
                              double* meanlogd3, double* weight, double* weight_im, double* ntri)
 {
-    return multipole_run(metric, quick, minsep, maxsep, nbins, binsize, b, a, maxn, h, h,
+    return multipole_run(metric, quick, minsep, maxsep, nbins, binsize, b, a, maxn, h, h, 0,
                          nthreads, gam8, meand2, meanlogd2, meand3, meanlogd3, weight,
                          weight_im, ntri);
 }
 
 int orc_corr3_multipole_cross12(int metric, int quick, double minsep, double maxsep, int nbins,
                                 double binsize, double b, double a, int maxn, void* h1,
-                                void* h2, int nthreads, double** gam8, double* meand2,
+                                void* h2, int vreal, int nthreads, double** gam8, double* meand2,
                                 double* meanlogd2, double* meand3, double* meanlogd3,
                                 double* weight, double* weight_im, double* ntri)
 {
     return multipole_run(metric, quick, minsep, maxsep, nbins, binsize, b, a, maxn, h1, h2,
-                         nthreads, gam8, meand2, meanlogd2, meand3, meanlogd3, weight,
+                         vreal, nthreads, gam8, meand2, meanlogd2, meand3, meanlogd3, weight,
                          weight_im, ntri);
 }
 

@@ -280,7 +280,7 @@ if __name__ == "__main__" and "--mp-kkk" in sys.argv:
 
 # 3-point cross12 with LogMultipole (processCross12 with ordered = 1, src/Corr3.cpp:4199,
 # 3730-3768, 1177-1237): vertex 1 from the case's catalog, vertices 2 and 3 from a second
-# catalog (seed + 1000), for GGG, NNN, KKK, NKK and KNN.
+# catalog (seed + 1000), for GGG, NNN, KKK, NKK, KNN, NGG and KGG.
 X12_CASES = {
     "ggg_flat_mp_x12": ("GGG", "ggg_flat_mp"),
     "ggg_sphere_mp_x12": ("GGG", "ggg_sphere_mp"),
@@ -288,6 +288,9 @@ X12_CASES = {
     "kkk_sphere_mp_x12": ("KKK", "ggg_sphere_mp"),
     "nkk_flat_mp_x12": ("NKK", "ggg_flat_mp"),
     "knn_sphere_mp_x12": ("KNN", "ggg_sphere_mp"),
+    "ngg_flat_mp_x12": ("NGG", "ggg_flat_mp"),
+    "ngg_sphere_mp_x12": ("NGG", "ggg_sphere_mp"),
+    "kgg_sphere_mp_x12": ("KGG", "ggg_sphere_mp"),
 }
 
 if __name__ == "__main__" and "--mp-x12" in sys.argv:
@@ -310,7 +313,8 @@ if __name__ == "__main__" and "--mp-x12" in sys.argv:
         common = ("meand1", "meanlogd1", "meand2", "meanlogd2", "meand3", "meanlogd3", "meanu",
                   "meanv", "weight", "weight_im", "ntri")
         zk = (("gam0r", "gam0i", "gam1r", "gam1i", "gam2r", "gam2i", "gam3r", "gam3i")
-              if letters == "GGG" else ("zeta", "zeta_im") if "K" in letters else ())
+              if letters == "GGG" else ("gam0r", "gam0i", "gam1r", "gam1i")
+              if letters[1:] == "GG" else ("zeta", "zeta_im") if "K" in letters else ())
         out = {k: np.zeros(shape) for k in zk + common}
         e = np.array([])
         zeta = [out[k] for k in zk] + [e] * (8 - len(zk))

@@ -156,7 +156,8 @@ def _corr3(T, letters, s):
     shape = (nb, nb, 2 * mn + 1)
     common = ("meand1", "meanlogd1", "meand2", "meanlogd2", "meand3", "meanlogd3", "meanu",
               "meanv", "weight", "weight_im", "ntri")
-    zk = MP_OUT[:8] if letters == "GGG" else ("zeta", "zeta_im") if "K" in letters else ()
+    zk = (MP_OUT[:8] if letters == "GGG" else MP_OUT[:4] if letters[1:] == "GG"
+          else ("zeta", "zeta_im") if "K" in letters else ())
     out = {k: np.zeros(shape) for k in zk + common}
     e = np.array([])
     zeta = [out[k] for k in zk] + [e] * (8 - len(zk))
@@ -168,7 +169,8 @@ def _corr3(T, letters, s):
 
 
 @pytest.mark.parametrize("name", ["ggg_flat_mp_x12", "ggg_sphere_mp_x12", "nnn_flat_mp_x12",
-                                  "kkk_sphere_mp_x12", "nkk_flat_mp_x12", "knn_sphere_mp_x12"])
+                                  "kkk_sphere_mp_x12", "nkk_flat_mp_x12", "knn_sphere_mp_x12",
+                                  "ngg_flat_mp_x12", "ngg_sphere_mp_x12", "kgg_sphere_mp_x12"])
 def test_multipole_cross12_golden(gpu_lib, name):
     """processCross12 (ordered = 1): vertex 1 from the first catalog, vertices 2 and 3 from
     the second, against the reference's own processCross12."""
@@ -221,3 +223,26 @@ def test_multipole_cross12_self_equals_auto(gpu_lib):
     err = max_rel_err(out, {k: g["ref_" + k] for k in MP_OUT})
     for k, v in err.items():
         assert v <= TOL, f"{k}: {v:.3e}"
+
+
+@pytest.mark.parametrize("name", ["ngg_flat_mp_x12", "kgg_sphere_mp_x12"])
+def test_multipole_cross12_cuda_core_contraction(gpu_lib, monkeypatch, name):
+    """NGG / KGG (G_n at n, no +-1 buffer) through the FP32 CUDA-core contraction as well as
+    the tensor-core one."""
+    from cases3 import spec3
+    T = gpu_lib
+    monkeypatch.setenv("TCGPU_MP_TENSOR", "0")
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    s = spec3(str(g["case"]))
+    letters = str(g["letters"])
+    cats = [{k[3:]: g[k] for k in g.files if k.startswith(p)} for p in ("c1_", "c2_")]
+    f1, f2 = [H.gpu_field(T, L, s["coords"], c, float(g["min_size"]), float(g["max_size"]))
+              for L, c in zip(letters[:2], cats)]
+    m = T.Euclidean if s["metric"] == "Euclidean" else T.Arc
+    corr, out, zk = _corr3(T, letters, s)
+    corr.processCross12(f1, f2, 1, False, False, m)
+    assert np.array_equal(out["ntri"], g["ref_ntri"]), name
+    for k in zk + ("weight", "weight_im"):
+        r = g["ref_" + k]
+        err = np.abs(out[k] - r).max() / max(np.abs(r).max(), 1e-300)
+        assert err <= TOL, f"{name} {k}: {err:.3e}"

@@ -123,8 +123,12 @@ def test_oracle_multipole_kkk_identity(name):
         assert np.abs(ww[k] - r).max() <= 1e-12 * max(np.abs(r).max(), 1e-300), k
 
 
-@pytest.mark.parametrize("name", ["ggg_flat_mp_x12", "ggg_sphere_mp_x12", "nnn_flat_mp_x12",
-                                  "kkk_sphere_mp_x12", "nkk_flat_mp_x12", "knn_sphere_mp_x12"])
+X12 = ["ggg_flat_mp_x12", "ggg_sphere_mp_x12", "nnn_flat_mp_x12", "kkk_sphere_mp_x12",
+       "nkk_flat_mp_x12", "knn_sphere_mp_x12", "ngg_flat_mp_x12", "ngg_sphere_mp_x12",
+       "kgg_sphere_mp_x12"]
+
+
+@pytest.mark.parametrize("name", X12)
 def test_oracle_multipole_cross12_matches_reference(name):
     """processCross12 (ordered = 1) with LogMultipole: vertex 1 from the first catalog,
     vertices 2 and 3 from the second (src/Corr3.cpp:1177-1237).  The N and K classes go
@@ -154,8 +158,17 @@ def test_oracle_multipole_cross12_matches_reference(name):
     def close(a, r, what):
         assert np.abs(a - r).max() <= 1e-12 * max(np.abs(r).max(), 1e-300), what
 
-    f1, f2 = field(cats[0], letters[0], False), field(cats[1], letters[1], False)
-    out = O.multipole(s["metric"], bins, s["max_n"], f1, nthreads=1, f2=f2)
+    vreal = letters[0] != "G" and letters[1] == "G"
+    if vreal:
+        # NGG / KGG: the vertex as a K field whose k is 1 (N) or k (K).
+        c = cats[0]
+        kv = c["k"] if letters[0] == "K" else np.ones(len(c["x"]))
+        f1 = O.OracleField("K", s["coords"], c["x"], c["y"], c.get("z"), kv, None, c["w"],
+                           None, *args)
+    else:
+        f1 = field(cats[0], letters[0], False)
+    f2 = field(cats[1], letters[1], False)
+    out = O.multipole(s["metric"], bins, s["max_n"], f1, nthreads=1, f2=f2, vreal=vreal)
     assert np.array_equal(out["ntri"], g["ref_ntri"])
     assert out["ntri"].sum() > 0
     for k in ("weight", "weight_im", "meand2", "meanlogd2", "meand3", "meanlogd3"):
@@ -163,7 +176,12 @@ def test_oracle_multipole_cross12_matches_reference(name):
     if letters == "GGG":
         for k in O.MP_KEYS[:8]:
             close(out[k], g["ref_" + k], k)
-    if "K" in letters:
+    if vreal:
+        # MultipoleHelper<2>'s zeta0 and zeta1 are the contraction's gam0 and gam2.
+        for mine, ref in (("gam0r", "gam0r"), ("gam0i", "gam0i"), ("gam2r", "gam1r"),
+                          ("gam2i", "gam1i")):
+            close(out[mine], g["ref_" + ref], ref)
+    elif "K" in letters:
         k1, k2 = field(cats[0], letters[0], True), field(cats[1], letters[1], True)
         zk = O.multipole(s["metric"], bins, s["max_n"], k1, nthreads=1, f2=k2)
         close(zk["weight"], g["ref_zeta"], "zeta")

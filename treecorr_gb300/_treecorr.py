@@ -728,9 +728,25 @@ class KNNCorr(GGGCorr):
     _dkind2 = 0
 
 
+class NGGCorr(GGGCorr):
+    """NGGCorr (src/Corr3.cpp:4253) with LogMultipole binning, processCross12 only (an N
+    vertex and two G vertices): zeta0..3 = gam0r, gam0i, gam1r, gam1i; weight, weight_im,
+    ntri and the mean distances."""
+    _dkind = 0
+    _dkind2 = 2
+
+
+class KGGCorr(GGGCorr):
+    """KGGCorr (src/Corr3.cpp:4261) with LogMultipole binning, processCross12 only (a K
+    vertex and two G vertices): zeta0..3 = gam0r, gam0i, gam1r, gam1i; weight, weight_im,
+    ntri and the mean distances."""
+    _dkind = 1
+    _dkind2 = 2
+
+
 # The 3-point classes of src/Corr3.cpp (WrapCorr3) that are not on the GPU path.
-for _n in ("NNK", "NKN", "KNK", "KKN", "NNG", "NGN", "GNN", "NGG",
-           "GNG", "GGN", "KKG", "KGK", "GKK", "KGG", "GKG", "GGK"):
+for _n in ("NNK", "NKN", "KNK", "KKN", "NNG", "NGN", "GNN",
+           "GNG", "GGN", "KKG", "KGK", "GKK", "GKG", "GGK"):
     globals()[_n + "Corr"] = _not_on_path(_n + "Corr")
 del _n
 

@@ -919,6 +919,18 @@ int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, int quick, int metric)
     P.tc = cross ? J.tc : f1->tcells;
     P.tops = f1->d_tops; P.ntop = (int)f1->tops.size();
     P.tops2 = cross ? J.tops2 : f1->d_tops; P.ntop2 = (int)f2->tops.size();
+    const bool xg = c->dk == TC_GDATA && c->dv != TC_GDATA;
+    if (xg) {
+        // NGG, KGG: vertex 1's payload becomes (w1 k1 or w1, 0), the real vertex weight of
+        // MultipoleHelper<2> (getWK, src/Corr3.cpp:2216-2405); field 1's cells are never
+        // pairs, so only the vertex sees it.
+        const size_t n1c = 2 * (size_t)f1->n - 1;
+        if (c->dv == TC_NDATA)
+            TC_CU(cudaMemcpyAsync(J.cells.d1, J.cells.w, sizeof(float) * n1c,
+                                  cudaMemcpyDeviceToDevice, st));
+        TC_CU(cudaMemsetAsync(J.cells.d2, 0, sizeof(float) * n1c, st));
+        P.vreal = 1;
+    }
     P.ncells = (int)ncap;
     const size_t Z = (size_t)c->nbins * c->nbins * (2 * c->maxn + 1);
     std::vector<double> h(15 * Z);
@@ -934,7 +946,7 @@ int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, int quick, int metric)
     cudaEventDestroy(e0); cudaEventDestroy(e1);
     c->ms = ms;
     if (rc) return rc == 3 ? TC_ERR_UNSUPPORTED : (rc == 5 ? TC_ERR_NOMEM : TC_ERR_DEVICE);
-    if (c->dv == TC_KDATA || c->dk == TC_KDATA) {
+    if ((c->dv == TC_KDATA || c->dk == TC_KDATA) && !xg) {
         // KKK, NKK, KNN (MultipoleHelper<1>, src/Corr3.cpp:2108-2214): zeta is the weight
         // contraction with the vertex weight w1 k1 (K) or w1 (N) and the pair weights
         // w k (K) or w (N), so the multipole runs again over records whose weights are
@@ -987,9 +999,13 @@ int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, int quick, int metric)
             c->zeta[1][i] += h2[13 * Z + i];
         }
     }
-    // Corr3 adds into the caller's arrays (calculateZeta, src/Corr3.cpp:1861-1974).
-    for (int q = 0; q < 8 && c->dk == TC_GDATA; ++q)
-        if (c->zeta[q]) for (size_t i = 0; i < Z; ++i) c->zeta[q][i] += h[q * Z + i];
+    // Corr3 adds into the caller's arrays (calculateZeta, src/Corr3.cpp:1861-1974).  NGG and
+    // KGG keep gam0 and gam2 of the contraction as their zeta0 (gam0) and zeta1 (gam1).
+    for (int q = 0; q < 8 && c->dk == TC_GDATA; ++q) {
+        const int src = xg ? (q < 2 ? q : q + 2) : q;
+        if (c->zeta[q] && (!xg || q < 4))
+            for (size_t i = 0; i < Z; ++i) c->zeta[q][i] += h[src * Z + i];
+    }
     double* dst[7] = {c->meand2, c->meanlogd2, c->meand3, c->meanlogd3, c->weight, c->weight_im,
                       c->ntri};
     for (int q = 0; q < 7; ++q) {
@@ -1729,10 +1745,12 @@ int tc_corr3_create(int d1, int d2, int d3, int bin_type, double minsep, double 
     // GGG; NNN: its weight, ntri and mean distances are the multipole's own sums, which do
     // not depend on the payload (an N field carries none); KKK, NKK, KNN: zeta is the weight
     // contraction over the weights w k of the K vertices (a second pass on the same tree).
+    // NGG, KGG: GGG's contraction with a real vertex weight and G_n taken at n (no +-1).
     const bool same = d1 == d2 && (d1 == TC_GDATA || d1 == TC_NDATA || d1 == TC_KDATA);
     const bool nk = (d1 == TC_NDATA && d2 == TC_KDATA) || (d1 == TC_KDATA && d2 == TC_NDATA);
-    if (d2 != d3 || !(same || nk)) {
-        set_last_error("only GGG, NNN, KKK, NKK and KNN are on the GPU 3-point path");
+    const bool xg = (d1 == TC_NDATA || d1 == TC_KDATA) && d2 == TC_GDATA;
+    if (d2 != d3 || !(same || nk || xg)) {
+        set_last_error("only GGG, NNN, KKK, NKK, KNN, NGG and KGG are on the GPU 3-point path");
         return TC_ERR_UNSUPPORTED;
     }
     if (bin_type != TC_LOGMULTIPOLE) {
@@ -1750,6 +1768,7 @@ int tc_corr3_create(int d1, int d2, int d3, int bin_type, double minsep, double 
     }
     const bool needz = (d1 == TC_GDATA);
     if ((needz && (!zeta0 || !zeta1 || !zeta2 || !zeta3 || !zeta4 || !zeta5 || !zeta6 || !zeta7)) ||
+        (xg && (!zeta0 || !zeta1 || !zeta2 || !zeta3)) ||
         ((d1 == TC_KDATA || d2 == TC_KDATA) && (!zeta0 || !zeta1)) ||
         !meand2 || !meanlogd2 || !meand3 || !meanlogd3 || !weight || !weight_im || !ntri) {
         set_last_error("missing output array");
@@ -1761,8 +1780,9 @@ int tc_corr3_create(int d1, int d2, int d3, int bin_type, double minsep, double 
     c->bin_type = bin_type; c->nbins = nbins; c->maxn = nubins;
     c->minsep = minsep; c->maxsep = maxsep; c->binsize = binsize; c->b = b; c->a = a;
     double* z[8] = {zeta0, zeta1, zeta2, zeta3, zeta4, zeta5, zeta6, zeta7};
-    const bool kz = d1 == TC_KDATA || d2 == TC_KDATA;
-    for (int q = 0; q < 8; ++q) c->zeta[q] = (needz || (kz && q < 2)) ? z[q] : nullptr;
+    const bool kz = (d1 == TC_KDATA || d2 == TC_KDATA) && !xg;
+    for (int q = 0; q < 8; ++q)
+        c->zeta[q] = (needz || (kz && q < 2) || (xg && q < 4)) ? z[q] : nullptr;
     c->meand2 = meand2; c->meanlogd2 = meanlogd2; c->meand3 = meand3; c->meanlogd3 = meanlogd3;
     c->weight = weight; c->weight_im = weight_im; c->ntri = ntri;
     *out = c;

@@ -1106,7 +1106,10 @@ __global__ void __launch_bounds__(MB, 2) k_mp_finish(MPParams P)
                             const float wgr = g1 * er - g2 * ei, wgi = g1 * ei + g2 * er;
                             const float e2r = er * er - ei * ei, e2i = 2.f * er * ei;
                             const float wsr = l1 * e2r - l2 * e2i, wsi = l1 * e2i + l2 * e2r;
-                            const float zsr = zr * zr - zi * zi, zsi = 2.f * zr * zi;
+                            // z^2 in the self-pair sums of a spin-2 vertex; 1 for an N or K
+                            // vertex (MultipoleScratch<GData>::calculateGn, buffer 0).
+                            const float zsr = P.vreal ? 1.f : zr * zr - zi * zi;
+                            const float zsi = P.vreal ? 0.f : 2.f * zr * zi;
                             const float a0r = wsr * zsr + wsi * zsi, a0i = wsi * zsr - wsr * zsi;
                             const float a1r = wsr * zsr - wsi * zsi, a1i = wsr * zsi + wsi * zsr;
                             float* R = acc + (size_t)(acc_n + apos) * MP_REC;
@@ -1127,7 +1130,7 @@ __global__ void __launch_bounds__(MB, 2) k_mp_finish(MPParams P)
                             const double* ls = P.ls + 4 * (size_t)ca;
                             const C2 wg = cmul({(double)P.d1[ca], (double)P.d2[ca]}, e);
                             const C2 wgsq = cmul({ls[1], ls[2]}, cmul(e, e));
-                            const C2 zsq = cmul(z, z);
+                            const C2 zsq = P.vreal ? C2{1., 0.} : cmul(z, z);
                             const C2 a0 = cmul(wgsq, conj2(zsq)), a1 = cmul(wgsq, zsq);
                             float* R = acc + (size_t)(acc_n + apos) * MP_REC;
                             *reinterpret_cast<float4*>(R) =
@@ -1258,11 +1261,15 @@ __global__ void __launch_bounds__(MB, 2) k_mp_finish(MPParams P)
 // over the records whose row range [ks, mk) holds min(a, b) -- a sum of outer products over
 // vertices.  Operands are staged in shared memory per chunk of records; products and chunk
 // sums are FP32, the running sums FP64; each group adds its sums to its own partial array.
+// These are GGG's sums (MultipoleHelper<5>).  With shift 0 the G indices are n and -n and
+// wg1 is the real w1 or w1 k1 of an N or K vertex, which makes gam0 and gam2 NGG's / KGG's
+// zeta0 and zeta1 (MultipoleHelper<2>, src/Corr3.cpp:2216-2405).
 
 struct ZParams {
     const float* rec;
     long long nrec;
     int rec_floats, nbins, maxn, chunk, ngroups;
+    int shift;             // 1: G_n at n -+ 1 (a spin-2 vertex); 0: at n (an N or K vertex)
     double* part;          // [group][10][Z]
     long long Z;
 };
@@ -1307,10 +1314,11 @@ __global__ void __launch_bounds__(ZB) k_mp_zeta(ZParams Q)
             const float2* RG = reinterpret_cast<const float2*>(R + 8);
             const float2* RW = RG + (size_t)gst * nb;
             const float w1 = R[3], wr = R[4], wi = R[5];
-            const float2 gm1 = RG[(n - 1 + M + 1) * nb + a];     // G[n-1]
-            const float2 gmm1 = RG[(-n - 1 + M + 1) * nb + a];   // G[-n-1]
-            const float2 gp1 = RG[(n + 1 + M + 1) * nb + a];     // G[n+1]
-            const float2 gmp1 = RG[(-n + 1 + M + 1) * nb + a];   // G[-n+1]
+            const int sh = Q.shift;
+            const float2 gm1 = RG[(n - sh + M + 1) * nb + a];     // G[n-1]
+            const float2 gmm1 = RG[(-n - sh + M + 1) * nb + a];   // G[-n-1]
+            const float2 gp1 = RG[(n + sh + M + 1) * nb + a];     // G[n+1]
+            const float2 gmp1 = RG[(-n + sh + M + 1) * nb + a];   // G[-n+1]
             float2 w = RW[nw * nb + a];
             if (n < 0) w.y = -w.y;
             float4 o0, o1, o2, o3;
@@ -1484,10 +1492,11 @@ __global__ void __launch_bounds__(TCB) k_mp_zeta_tc(ZParams Q, int* status)
             const float* R = Q.rec + (size_t)(cb + v) * Q.rec_floats;
             const float2* RG = reinterpret_cast<const float2*>(R + 8);
             const float2* RW = RG + (size_t)gst * nb;
-            ig[j][0] = RG[(n + M) * nb + a];       // G[n-1]
-            ig[j][1] = RG[(M - n) * nb + a];       // G[-n-1]
-            ig[j][2] = RG[(n + M + 2) * nb + a];   // G[n+1]
-            ig[j][3] = RG[(M + 2 - n) * nb + a];   // G[-n+1]
+            const int sh = Q.shift;
+            ig[j][0] = RG[(n - sh + M + 1) * nb + a];    // G[n-1]
+            ig[j][1] = RG[(-n - sh + M + 1) * nb + a];   // G[-n-1]
+            ig[j][2] = RG[(n + sh + M + 1) * nb + a];    // G[n+1]
+            ig[j][3] = RG[(-n + sh + M + 1) * nb + a];   // G[-n+1]
             ig[j][4] = RW[nw * nb + a];            // W[|n|]
             const int ks = __float_as_int(R[1]), mk = __float_as_int(R[2]);
             ih[j] = make_float4(R[3], R[4], R[5], __int_as_float((ks << 8) | mk));
@@ -1883,6 +1892,7 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
             Q.rec = X.zrec; Q.nrec = std::min<long long>((long long)c[2], X.zcap);
             Q.rec_floats = recf; Q.nbins = nb; Q.maxn = M; Q.chunk = chunk;
             Q.ngroups = ngroups; Q.part = X.part; Q.Z = Z;
+            Q.shift = P.vreal ? 0 : 1;
             if (Q.nrec > 0) {
                 count_launch();
                 if (use_tc) k_mp_zeta_tc<<<dim3(nn, ngroups), TCB, tcsm, st>>>(Q, X.tcstatus);

@@ -23,6 +23,9 @@ enum MPErr : int {
 
 struct MPParams {
     int coords, metric, quick, nbins, maxn;
+    // 0: a spin-2 vertex (GGG: G_n up to n = max_n + 1, self-pair sums with z^2); 1: an N or
+    // K vertex with G pairs (NGG, KGG: the record's vertex payload is (w1 or w1 k1, 0)).
+    int vreal;
     double minsep, maxsep, binsize, b, a, logminsep, minsepsq, maxsepsq, bsq, asq, maxbsq_eff;
     // FP32 copies for the FP32 decisions (the FP64 values decide whenever FP32 is too close).
     float f_minsepsq, f_minsep, f_maxsepsq, f_maxsep, f_asq, f_bsq, f_q25, f_logminsep, f_binsize, f_b,
