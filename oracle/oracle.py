@@ -226,12 +226,12 @@ MP_KEYS = ("gam0r", "gam0i", "gam1r", "gam1i", "gam2r", "gam2i", "gam3r", "gam3i
            "meand2", "meanlogd2", "meand3", "meanlogd3", "weight", "weight_im", "ntri")
 
 
-def multipole(metric, bins, max_n, f, quick=False, nthreads=0, f2=None, vreal=False):
+def multipole(metric, bins, max_n, f, quick=False, nthreads=0, f2=None, mode=0):
     """The oracle's GGG LogMultipole auto-correlation, or with f2 the cross12 one (vertex 1
     from f, vertices 2 and 3 from f2); dict of (nbins, nbins, 2*max_n+1) arrays (zeta0..7
-    as gam0r..gam3i, meand2/3, meanlogd2/3, weight, weight_im, ntri).  vreal selects the
-    NGG / KGG form (vertex 1's g1 holds 1 or k, its g2 zero): gam0 and gam2 are then their
-    zeta0 and zeta1."""
+    as gam0r..gam3i, meand2/3, meanlogd2/3, weight, weight_im, ntri).  mode 1 is the
+    NGG / KGG form (vertex 1 a K field whose k is 1 or k): gam0 and gam2 are then their
+    zeta0 and zeta1; mode 2 the GNN / GKK form (f2 such a K field): gam0 is their zeta."""
     nb = bins["nbins"]
     shape = (nb, nb, 2 * max_n + 1)
     out = {k: np.zeros(shape) for k in MP_KEYS}
@@ -242,8 +242,8 @@ def multipole(metric, bins, max_n, f, quick=False, nthreads=0, f2=None, vreal=Fa
     if f2 is None:
         rc = lib().orc_corr3_multipole_auto(*head, f.h, int(nthreads), gam, *tail)
     else:
-        rc = lib().orc_corr3_multipole_cross12(*head, f.h, f2.h, int(bool(vreal)),
-                                               int(nthreads), gam, *tail)
+        rc = lib().orc_corr3_multipole_cross12(*head, f.h, f2.h, int(mode), int(nthreads), gam,
+                                               *tail)
     if rc:
         raise ValueError("multipole needs G fields in one coordinate system")
     return out

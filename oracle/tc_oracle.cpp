@@ -369,6 +369,9 @@ struct Params {
     // without the +-1 buffer, self-pair sums without z^2 (Corr3::getMP2 buffer 0,
     // src/Corr3.cpp:1307-1313); its "shear" (d1, d2) then holds (w1 or w1 k1, 0).
     int vreal = 0;
+    // 3-point: 1 when vertex 1 is a G field and the pairs N or K fields (GNN, GKK): the pairs'
+    // payload (w or w k) is real and not rotated (MultipoleHelper<4>).
+    int pspin0 = 0;
 };
 
 // MetricHelper<Euclidean>::DistSq (include/Metric.h:143-147, 202-207) and
@@ -677,7 +680,7 @@ void calculate_gn(const Params& P, const Node& c1, const Node& c2, double r, dou
     mp.sumwwlogr[k] += wsq * logr;
     cd wg(c2.d1, c2.d2);
     cd z = exp_i_phi(P, c1, c2, r);
-    cd e = project2(P, c1, c2);
+    cd e = P.pspin0 ? cd(1., 0.) : project2(P, c1, c2);
     cd wgsq = c2.sumwzsq;
     wg *= e;
     wgsq *= e * e;
@@ -1311,7 +1314,7 @@ int orc_corr2_process_rows(int dtype, int metric, int quick, double minsep, doub
 // Outputs have nbins*nbins*(2*maxn+1) entries, accumulated (+=) like the reference's.
 static int multipole_run(int metric, int quick, double minsep, double maxsep, int nbins,
                          double binsize, double b, double a, int maxn, void* h1, void* h2,
-                         int vreal, int nthreads, double** gam8, double* meand2,
+                         int mode, int nthreads, double** gam8, double* meand2,
                          double* meanlogd2, double* meand3, double* meanlogd3, double* weight,
                          double* weight_im, double* ntri)
 {
@@ -1319,11 +1322,16 @@ static int multipole_run(int metric, int quick, double minsep, double maxsep, in
     Field* f2 = static_cast<Field*>(h2);
     // Vertex 1: a G field, or for NGG / KGG a K field whose k is 1 (N) or k (K), so that
     // its cells' d1 is the real vertex weight (no parallel transport for spin 0).
+    // mode 0: GGG; 1: NGG / KGG; 2: GNN / GKK, whose pairs come as a K field whose k is 1
+    // (N) or k (K).
+    const bool vreal = mode == 1, pspin0 = mode == 2;
     const bool v_ok = vreal ? (f1->dtype == DK && f1->spin == 0) : (f1->dtype == DG && f1->spin == 2);
-    if (!v_ok || f2->dtype != DG || f2->spin != 2) return 1;
+    const bool p_ok = pspin0 ? (f2->dtype == DK && f2->spin == 0) : (f2->dtype == DG && f2->spin == 2);
+    if (!v_ok || !p_ok) return 1;
     if (f1->coords != f2->coords) return 2;
     Params P = make_params(DG * 16 + DG, f1->coords, metric, quick, minsep, maxsep, nbins, binsize, b, a);
-    P.vreal = vreal;
+    P.vreal = vreal ? 1 : 0;
+    P.pspin0 = pspin0 ? 1 : 0;
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #else
@@ -1366,12 +1374,12 @@ int orc_corr3_multipole_auto(int metric, int quick, double minsep, double maxsep
 
 int orc_corr3_multipole_cross12(int metric, int quick, double minsep, double maxsep, int nbins,
                                 double binsize, double b, double a, int maxn, void* h1,
-                                void* h2, int vreal, int nthreads, double** gam8, double* meand2,
+                                void* h2, int mode, int nthreads, double** gam8, double* meand2,
                                 double* meanlogd2, double* meand3, double* meanlogd3,
                                 double* weight, double* weight_im, double* ntri)
 {
     return multipole_run(metric, quick, minsep, maxsep, nbins, binsize, b, a, maxn, h1, h2,
-                         vreal, nthreads, gam8, meand2, meanlogd2, meand3, meanlogd3, weight,
+                         mode, nthreads, gam8, meand2, meanlogd2, meand3, meanlogd3, weight,
                          weight_im, ntri);
 }
 

@@ -280,7 +280,7 @@ if __name__ == "__main__" and "--mp-kkk" in sys.argv:
 
 # 3-point cross12 with LogMultipole (processCross12 with ordered = 1, src/Corr3.cpp:4199,
 # 3730-3768, 1177-1237): vertex 1 from the case's catalog, vertices 2 and 3 from a second
-# catalog (seed + 1000), for GGG, NNN, KKK, NKK, KNN, NGG and KGG.
+# catalog (seed + 1000), for GGG, NNN, KKK, NKK, KNN, NGG, KGG, GNN and GKK.
 X12_CASES = {
     "ggg_flat_mp_x12": ("GGG", "ggg_flat_mp"),
     "ggg_sphere_mp_x12": ("GGG", "ggg_sphere_mp"),
@@ -291,6 +291,9 @@ X12_CASES = {
     "ngg_flat_mp_x12": ("NGG", "ggg_flat_mp"),
     "ngg_sphere_mp_x12": ("NGG", "ggg_sphere_mp"),
     "kgg_sphere_mp_x12": ("KGG", "ggg_sphere_mp"),
+    "gnn_flat_mp_x12": ("GNN", "ggg_flat_mp"),
+    "gnn_sphere_mp_x12": ("GNN", "ggg_sphere_mp"),
+    "gkk_sphere_mp_x12": ("GKK", "ggg_sphere_mp"),
 }
 
 if __name__ == "__main__" and "--mp-x12" in sys.argv:
@@ -314,7 +317,8 @@ if __name__ == "__main__" and "--mp-x12" in sys.argv:
                   "meanv", "weight", "weight_im", "ntri")
         zk = (("gam0r", "gam0i", "gam1r", "gam1i", "gam2r", "gam2i", "gam3r", "gam3i")
               if letters == "GGG" else ("gam0r", "gam0i", "gam1r", "gam1i")
-              if letters[1:] == "GG" else ("zeta", "zeta_im") if "K" in letters else ())
+              if letters[1:] == "GG" else ("zeta", "zeta_im")
+              if ("K" in letters or letters[0] == "G") else ())
         out = {k: np.zeros(shape) for k in zk + common}
         e = np.array([])
         zeta = [out[k] for k in zk] + [e] * (8 - len(zk))

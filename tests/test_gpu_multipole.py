@@ -157,7 +157,7 @@ def _corr3(T, letters, s):
     common = ("meand1", "meanlogd1", "meand2", "meanlogd2", "meand3", "meanlogd3", "meanu",
               "meanv", "weight", "weight_im", "ntri")
     zk = (MP_OUT[:8] if letters == "GGG" else MP_OUT[:4] if letters[1:] == "GG"
-          else ("zeta", "zeta_im") if "K" in letters else ())
+          else ("zeta", "zeta_im") if ("K" in letters or letters[0] == "G") else ())
     out = {k: np.zeros(shape) for k in zk + common}
     e = np.array([])
     zeta = [out[k] for k in zk] + [e] * (8 - len(zk))
@@ -170,7 +170,8 @@ def _corr3(T, letters, s):
 
 @pytest.mark.parametrize("name", ["ggg_flat_mp_x12", "ggg_sphere_mp_x12", "nnn_flat_mp_x12",
                                   "kkk_sphere_mp_x12", "nkk_flat_mp_x12", "knn_sphere_mp_x12",
-                                  "ngg_flat_mp_x12", "ngg_sphere_mp_x12", "kgg_sphere_mp_x12"])
+                                  "ngg_flat_mp_x12", "ngg_sphere_mp_x12", "kgg_sphere_mp_x12",
+                                  "gnn_flat_mp_x12", "gnn_sphere_mp_x12", "gkk_sphere_mp_x12"])
 def test_multipole_cross12_golden(gpu_lib, name):
     """processCross12 (ordered = 1): vertex 1 from the first catalog, vertices 2 and 3 from
     the second, against the reference's own processCross12."""
@@ -225,10 +226,10 @@ def test_multipole_cross12_self_equals_auto(gpu_lib):
         assert v <= TOL, f"{k}: {v:.3e}"
 
 
-@pytest.mark.parametrize("name", ["ngg_flat_mp_x12", "kgg_sphere_mp_x12"])
+@pytest.mark.parametrize("name", ["ngg_flat_mp_x12", "kgg_sphere_mp_x12", "gkk_sphere_mp_x12"])
 def test_multipole_cross12_cuda_core_contraction(gpu_lib, monkeypatch, name):
-    """NGG / KGG (G_n at n, no +-1 buffer) through the FP32 CUDA-core contraction as well as
-    the tensor-core one."""
+    """NGG / KGG (G_n at n, no +-1 buffer) and GKK (real pair payload) through the FP32
+    CUDA-core contraction as well as the tensor-core one."""
     from cases3 import spec3
     T = gpu_lib
     monkeypatch.setenv("TCGPU_MP_TENSOR", "0")

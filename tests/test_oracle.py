@@ -125,7 +125,7 @@ def test_oracle_multipole_kkk_identity(name):
 
 X12 = ["ggg_flat_mp_x12", "ggg_sphere_mp_x12", "nnn_flat_mp_x12", "kkk_sphere_mp_x12",
        "nkk_flat_mp_x12", "knn_sphere_mp_x12", "ngg_flat_mp_x12", "ngg_sphere_mp_x12",
-       "kgg_sphere_mp_x12"]
+       "kgg_sphere_mp_x12", "gnn_flat_mp_x12", "gnn_sphere_mp_x12", "gkk_sphere_mp_x12"]
 
 
 @pytest.mark.parametrize("name", X12)
@@ -159,16 +159,19 @@ def test_oracle_multipole_cross12_matches_reference(name):
         assert np.abs(a - r).max() <= 1e-12 * max(np.abs(r).max(), 1e-300), what
 
     vreal = letters[0] != "G" and letters[1] == "G"
-    if vreal:
-        # NGG / KGG: the vertex as a K field whose k is 1 (N) or k (K).
-        c = cats[0]
-        kv = c["k"] if letters[0] == "K" else np.ones(len(c["x"]))
-        f1 = O.OracleField("K", s["coords"], c["x"], c["y"], c.get("z"), kv, None, c["w"],
-                           None, *args)
-    else:
-        f1 = field(cats[0], letters[0], False)
-    f2 = field(cats[1], letters[1], False)
-    out = O.multipole(s["metric"], bins, s["max_n"], f1, nthreads=1, f2=f2, vreal=vreal)
+    pspin0 = letters[0] == "G" and letters[1] != "G"
+
+    def as_k(c, letter):
+        # An N or K catalog as a K field whose k is 1 (N) or k (K): its cells' d1 is the
+        # real payload w or w k, summed without parallel transport.
+        kv = c["k"] if letter == "K" else np.ones(len(c["x"]))
+        return O.OracleField("K", s["coords"], c["x"], c["y"], c.get("z"), kv, None, c["w"],
+                             None, *args)
+
+    f1 = as_k(cats[0], letters[0]) if vreal else field(cats[0], letters[0], False)
+    f2 = as_k(cats[1], letters[1]) if pspin0 else field(cats[1], letters[1], False)
+    mode = 1 if vreal else 2 if pspin0 else 0
+    out = O.multipole(s["metric"], bins, s["max_n"], f1, nthreads=1, f2=f2, mode=mode)
     assert np.array_equal(out["ntri"], g["ref_ntri"])
     assert out["ntri"].sum() > 0
     for k in ("weight", "weight_im", "meand2", "meanlogd2", "meand3", "meanlogd3"):
@@ -181,6 +184,10 @@ def test_oracle_multipole_cross12_matches_reference(name):
         for mine, ref in (("gam0r", "gam0r"), ("gam0i", "gam0i"), ("gam2r", "gam1r"),
                           ("gam2i", "gam1i")):
             close(out[mine], g["ref_" + ref], ref)
+    elif pspin0:
+        # MultipoleHelper<4>'s zeta is the contraction's gam0.
+        close(out["gam0r"], g["ref_zeta"], "zeta")
+        close(out["gam0i"], g["ref_zeta_im"], "zeta_im")
     elif "K" in letters:
         k1, k2 = field(cats[0], letters[0], True), field(cats[1], letters[1], True)
         zk = O.multipole(s["metric"], bins, s["max_n"], k1, nthreads=1, f2=k2)

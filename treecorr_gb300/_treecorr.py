@@ -744,9 +744,24 @@ class KGGCorr(GGGCorr):
     _dkind2 = 2
 
 
+class GNNCorr(GGGCorr):
+    """GNNCorr (src/Corr3.cpp:4251) with LogMultipole binning, processCross12 only (a G
+    vertex and two N vertices): zeta0, zeta1 = zeta (real, imaginary), weight, weight_im,
+    ntri and the mean distances."""
+    _dkind = 2
+    _dkind2 = 0
+
+
+class GKKCorr(GGGCorr):
+    """GKKCorr (src/Corr3.cpp:4259) with LogMultipole binning, processCross12 only (a G
+    vertex and two K vertices): zeta0, zeta1 = zeta (real, imaginary), weight, weight_im,
+    ntri and the mean distances."""
+    _dkind = 2
+    _dkind2 = 1
+
+
 # The 3-point classes of src/Corr3.cpp (WrapCorr3) that are not on the GPU path.
-for _n in ("NNK", "NKN", "KNK", "KKN", "NNG", "NGN", "GNN",
-           "GNG", "GGN", "KKG", "KGK", "GKK", "GKG", "GGK"):
+for _n in ("NNK", "NKN", "KNK", "KKN", "NNG", "NGN", "GNG", "GGN", "KKG", "KGK", "GKG", "GGK"):
     globals()[_n + "Corr"] = _not_on_path(_n + "Corr")
 del _n
 

@@ -931,6 +931,17 @@ int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, int quick, int metric)
         TC_CU(cudaMemsetAsync(J.cells.d2, 0, sizeof(float) * n1c, st));
         P.vreal = 1;
     }
+    const bool gx = c->dv == TC_GDATA && c->dk != TC_GDATA;
+    if (gx) {
+        // GNN, GKK (MultipoleHelper<4>, src/Corr3.cpp:2462-2580): zeta = wg1 G_a[n-1] G_b[-n-1]
+        // with G_n = sum w z^n (N) or sum w k z^n (K) and the self-pair sum w^2 or (w k)^2
+        // times conj(z^2): GGG's gam0 over field 2's cells with that real payload.
+        const size_t n1c = 2 * (size_t)f1->n - 1, n2c = (size_t)ncap - n1c;
+        TC_TRY(launch_scalar_pairs((int)n2c, c->dk == TC_NDATA ? 1 : 0, J.tc + n1c,
+                                   J.cells.d1 + n1c, J.cells.d2 + n1c, J.ls + 4 * n1c,
+                                   J.lsf + n1c, st));
+        P.pspin0 = 1;
+    }
     P.ncells = (int)ncap;
     const size_t Z = (size_t)c->nbins * c->nbins * (2 * c->maxn + 1);
     std::vector<double> h(15 * Z);
@@ -946,7 +957,7 @@ int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, int quick, int metric)
     cudaEventDestroy(e0); cudaEventDestroy(e1);
     c->ms = ms;
     if (rc) return rc == 3 ? TC_ERR_UNSUPPORTED : (rc == 5 ? TC_ERR_NOMEM : TC_ERR_DEVICE);
-    if ((c->dv == TC_KDATA || c->dk == TC_KDATA) && !xg) {
+    if ((c->dv == TC_KDATA || c->dk == TC_KDATA) && !xg && !gx) {
         // KKK, NKK, KNN (MultipoleHelper<1>, src/Corr3.cpp:2108-2214): zeta is the weight
         // contraction with the vertex weight w1 k1 (K) or w1 (N) and the pair weights
         // w k (K) or w (N), so the multipole runs again over records whose weights are
@@ -1000,10 +1011,11 @@ int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, int quick, int metric)
         }
     }
     // Corr3 adds into the caller's arrays (calculateZeta, src/Corr3.cpp:1861-1974).  NGG and
-    // KGG keep gam0 and gam2 of the contraction as their zeta0 (gam0) and zeta1 (gam1).
-    for (int q = 0; q < 8 && c->dk == TC_GDATA; ++q) {
+    // KGG keep gam0 and gam2 of the contraction as their zeta0 (gam0) and zeta1 (gam1); GNN
+    // and GKK keep gam0 as zeta (real, imaginary).
+    for (int q = 0; q < 8 && (c->dk == TC_GDATA || gx); ++q) {
         const int src = xg ? (q < 2 ? q : q + 2) : q;
-        if (c->zeta[q] && (!xg || q < 4))
+        if (c->zeta[q] && (!xg || q < 4) && (!gx || q < 2))
             for (size_t i = 0; i < Z; ++i) c->zeta[q][i] += h[src * Z + i];
     }
     double* dst[7] = {c->meand2, c->meanlogd2, c->meand3, c->meanlogd3, c->weight, c->weight_im,
@@ -1749,8 +1761,11 @@ int tc_corr3_create(int d1, int d2, int d3, int bin_type, double minsep, double 
     const bool same = d1 == d2 && (d1 == TC_GDATA || d1 == TC_NDATA || d1 == TC_KDATA);
     const bool nk = (d1 == TC_NDATA && d2 == TC_KDATA) || (d1 == TC_KDATA && d2 == TC_NDATA);
     const bool xg = (d1 == TC_NDATA || d1 == TC_KDATA) && d2 == TC_GDATA;
-    if (d2 != d3 || !(same || nk || xg)) {
-        set_last_error("only GGG, NNN, KKK, NKK, KNN, NGG and KGG are on the GPU 3-point path");
+    // GNN, GKK: GGG's gam0 with the pairs' real payload (w or w k) unrotated.
+    const bool gx = d1 == TC_GDATA && (d2 == TC_NDATA || d2 == TC_KDATA);
+    if (d2 != d3 || !(same || nk || xg || gx)) {
+        set_last_error("only GGG, NNN, KKK, NKK, KNN, NGG, KGG, GNN and GKK are on the GPU "
+                       "3-point path");
         return TC_ERR_UNSUPPORTED;
     }
     if (bin_type != TC_LOGMULTIPOLE) {
@@ -1766,10 +1781,10 @@ int tc_corr3_create(int d1, int d2, int d3, int bin_type, double minsep, double 
         set_last_error("invalid binning");
         return TC_ERR_ARG;
     }
-    const bool needz = (d1 == TC_GDATA);
+    const bool needz = (d1 == TC_GDATA && d2 == TC_GDATA);
     if ((needz && (!zeta0 || !zeta1 || !zeta2 || !zeta3 || !zeta4 || !zeta5 || !zeta6 || !zeta7)) ||
         (xg && (!zeta0 || !zeta1 || !zeta2 || !zeta3)) ||
-        ((d1 == TC_KDATA || d2 == TC_KDATA) && (!zeta0 || !zeta1)) ||
+        ((d1 == TC_KDATA || d2 == TC_KDATA || gx) && (!zeta0 || !zeta1)) ||
         !meand2 || !meanlogd2 || !meand3 || !meanlogd3 || !weight || !weight_im || !ntri) {
         set_last_error("missing output array");
         return TC_ERR_ARG;
@@ -1780,7 +1795,7 @@ int tc_corr3_create(int d1, int d2, int d3, int bin_type, double minsep, double 
     c->bin_type = bin_type; c->nbins = nbins; c->maxn = nubins;
     c->minsep = minsep; c->maxsep = maxsep; c->binsize = binsize; c->b = b; c->a = a;
     double* z[8] = {zeta0, zeta1, zeta2, zeta3, zeta4, zeta5, zeta6, zeta7};
-    const bool kz = (d1 == TC_KDATA || d2 == TC_KDATA) && !xg;
+    const bool kz = ((d1 == TC_KDATA || d2 == TC_KDATA) && !xg) || gx;
     for (int q = 0; q < 8; ++q)
         c->zeta[q] = (needz || (kz && q < 2) || (xg && q < 4)) ? z[q] : nullptr;
     c->meand2 = meand2; c->meanlogd2 = meanlogd2; c->meand3 = meand3; c->meanlogd3 = meanlogd3;

@@ -109,6 +109,36 @@ int launch_weight_swap(int ncap, const TCell* tc, const double* ls, TCell* tc2, 
     return 0;
 }
 
+// The cells of an N or K pair field as the real payload of GNN / GKK (MultipoleHelper<4>,
+// src/Corr3.cpp:2462-2580): (d1, d2) := (w, 0) for N (Sigma w z^n is its G_n), (w k, 0) for
+// K; the leaf sums (sum w^2 or sum (w k)^2, 0) stand where the squared shear was.
+__global__ void k_mp_scalar_pairs(int ncap, int is_n, TCell* tc, float* d1, float* d2,
+                                  double* ls, float4* lsf)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ncap) return;
+    TCell c = tc[i];
+    if (is_n) c.c.x = c.b.w;
+    c.c.y = 0.f;
+    tc[i] = c;
+    d1[i] = c.c.x;
+    d2[i] = 0.f;
+    double* l = ls + 4 * (size_t)i;
+    if (is_n) l[1] = l[0];
+    l[2] = 0.;
+    lsf[i] = make_float4((float)l[0], (float)l[1], 0.f, (float)l[3]);
+}
+
+int launch_scalar_pairs(int ncap, int is_n, TCell* tc, float* d1, float* d2, double* ls,
+                        float4* lsf, cudaStream_t st)
+{
+    if (ncap <= 0) return 0;
+    count_launch();
+    k_mp_scalar_pairs<<<(ncap + 255) / 256, 256, 0, st>>>(ncap, is_n, tc, d1, d2, ls, lsf);
+    TC_CU(cudaGetLastError());
+    return 0;
+}
+
 int launch_leaf_sums(int ncap, const Cells& C, double* ls, float4* lsf, cudaStream_t st)
 {
     TC_CU(cudaMemsetAsync(ls, 0, 4 * sizeof(double) * (size_t)ncap, st));
@@ -1098,7 +1128,9 @@ __global__ void __launch_bounds__(MB, 2) k_mp_finish(MPParams P)
                             const float zr = dxf / rr, zi = dyf / rr;
                             float nn2 = dxf * dxf + dyf * dyf;
                             if (!(nn2 > 0.f)) nn2 = 1.f;
-                            const float er = (dxf * dxf - dyf * dyf) / nn2, ei = -(2.f * dxf * dyf) / nn2;
+                            // (no rotation for the real payload of N / K pairs)
+                            const float er = P.pspin0 ? 1.f : (dxf * dxf - dyf * dyf) / nn2;
+                            const float ei = P.pspin0 ? 0.f : -(2.f * dxf * dyf) / nn2;
                             const float w2 = tb.w;
                             const float4 lf = __ldg(P.lsf + ca);
                             const float l0 = lf.x, l1 = lf.y, l2 = lf.z, l3 = lf.w;
@@ -1126,6 +1158,7 @@ __global__ void __launch_bounds__(MB, 2) k_mp_finish(MPParams P)
                             if (dec32) { racc = r32; lracc = lr32; }
                             C2 z, e;
                             phases(P, c1, ca, racc, z, e);
+                            if (P.pspin0) e = C2{1., 0.};
                             const double w2 = P.w[ca];
                             const double* ls = P.ls + 4 * (size_t)ca;
                             const C2 wg = cmul({(double)P.d1[ca], (double)P.d2[ca]}, e);

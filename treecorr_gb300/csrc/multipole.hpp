@@ -26,6 +26,8 @@ struct MPParams {
     // 0: a spin-2 vertex (GGG: G_n up to n = max_n + 1, self-pair sums with z^2); 1: an N or
     // K vertex with G pairs (NGG, KGG: the record's vertex payload is (w1 or w1 k1, 0)).
     int vreal;
+    // 1: the pairs are N or K cells whose payload is real (GNN, GKK): no spin-2 rotation.
+    int pspin0;
     double minsep, maxsep, binsize, b, a, logminsep, minsepsq, maxsepsq, bsq, asq, maxbsq_eff;
     // FP32 copies for the FP32 decisions (the FP64 values decide whenever FP32 is too close).
     float f_minsepsq, f_minsep, f_maxsepsq, f_maxsep, f_asq, f_bsq, f_q25, f_logminsep, f_binsize, f_b,
@@ -120,6 +122,9 @@ int launch_leaf_sums(int ncap, const Cells& C, double* ls, float4* lsf, cudaStre
 // K-field cells re-weighted by w k for the KKK zeta pass (records, leaf sums).
 int launch_weight_swap(int ncap, const TCell* tc, const double* ls, TCell* tc2, double* ls2,
                        float4* lsf2, cudaStream_t st);
+// N / K pair cells as the real payload (w or w k, 0) of GNN / GKK.
+int launch_scalar_pairs(int ncap, int is_n, TCell* tc, float* d1, float* d2, double* ls,
+                        float4* lsf, cudaStream_t st);
 // Runs both phases and the reduction; h_out receives 15 arrays of nbins*nbins*(2*maxn+1)
 // doubles: gam0r, gam0i, gam1r, gam1i, gam2r, gam2i, gam3r, gam3i, meand2, meanlogd2,
 // meand3, meanlogd3, weight, weight_im, ntri.
