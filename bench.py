@@ -662,6 +662,187 @@ def run_kmeans(args, rank, world):
     return line
 
 
+def run_classes(args, rank, world):
+    """The widened classes, one timed call each after a warm-up: 2-point NN and KK auto on
+    the curved-sky catalog, NG and KG cross (its first half as the N / K field, the second
+    half as the G field); 3-point LogMultipole cross12 GGG, NGG, GNN and NKK (1M vertex
+    points, 1M pair points, the multipole configuration's density and binning).  Each class
+    is reported with its GPU rate and the oracle port's rate on a bounded sample."""
+    import torch
+    from treecorr_gb300 import _treecorr as T
+    from oracle import oracle as O
+    dev = torch.device("cuda", rank % max(torch.cuda.device_count(), 1))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.ExternalStream(T.stream_handle(), device=dev)
+    nthreads = os.cpu_count() or 1
+    e = np.array([])
+    cat = curved_sky_catalog(args.n, seed=args.seed + rank)
+    cat["k"] = np.random.default_rng(args.seed + 7).normal(0, 0.02, args.n)
+    bins = binning(args.bin_slop)
+    nb = bins["nbins"]
+    half = args.n // 2
+
+    def sub(c, lo, hi):
+        return {k: np.ascontiguousarray(v[lo:hi]) for k, v in c.items()}
+
+    def field2(L, c):
+        cls = getattr(T, L + "FieldSphere")
+        pay = [] if L == "N" else [c["k"]] if L == "K" else [c["g1"], c["g2"]]
+        return cls(c["x"], c["y"], c["z"], *pay, c["w"], e, 0.0, 0.0, T.Mean, 0, False, 3, 10)
+
+    def timed(fn):
+        fn()                                  # warm-up
+        barrier(world)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        return allreduce_max(e0.elapsed_time(e1), world), r
+
+    res = {}
+    launches0 = T.launch_count()
+    with ClockSampler(dev.index) as clk:
+        for cls, (L1, L2) in (("NN", ("N", None)), ("KK", ("K", None)), ("NG", ("N", "G")),
+                              ("KG", ("K", "G"))):
+            def step():
+                out = {k: np.zeros(nb) for k in ("xi0", "xi1", "xi2", "xi3", "meanr",
+                                                 "meanlogr", "weight", "npairs")}
+                c = getattr(T, cls + "Corr")(
+                    T.Log, bins["min_sep"], bins["max_sep"], nb, bins["bin_size"], bins["b"],
+                    bins["a"], -sys.float_info.max, sys.float_info.max, 0., 0., 0.,
+                    *[out[k] for k in ("xi0", "xi1", "xi2", "xi3", "meanr", "meanlogr",
+                                       "weight", "npairs")])
+                if L2 is None:
+                    f = field2(L1, cat)
+                    c.processAuto(f, False, False, T.Arc)
+                else:
+                    f, g = field2(L1, sub(cat, 0, half)), field2(L2, sub(cat, half, args.n))
+                    c.processCross(f, g, False, False, T.Arc)
+                return c.stats()["accepted"]
+            ms, acc = timed(step)
+            res[cls] = {"gpu_ms": ms, "pair_evals": acc, "gpu_rate": world * acc / (ms / 1e3),
+                        "unit": UNIT, "n": args.n if L2 is None else [half, args.n - half]}
+        B = ggg_bins()
+        mb, mn = B["nbins"], B["max_n"]
+        shape = (mb, mb, 2 * mn + 1)
+        n3 = 1_000_000
+        side = 600.0 * np.sqrt(2 * n3 / 2e6)
+        cv = ggg_catalog(n3, args.seed + 11 + rank, side=side)
+        cp = ggg_catalog(n3, args.seed + 12 + rank, side=side)
+        for c3 in (cv, cp):
+            c3["k"] = np.random.default_rng(args.seed + 13).normal(0, 0.02, n3)
+        for cls in ("GGG", "NGG", "GNN", "NKK"):
+            zk = {"GGG": 8, "NGG": 4}.get(cls, 2)
+
+            def step3():
+                keys = [f"z{q}" for q in range(zk)] + [
+                    "meand1", "meanlogd1", "meand2", "meanlogd2", "meand3", "meanlogd3",
+                    "meanu", "meanv", "weight", "weight_im", "ntri"]
+                out = {k: np.zeros(shape) for k in keys}
+                zeta = [out[f"z{q}"] for q in range(zk)] + [e] * (8 - zk)
+                c = getattr(T, cls + "Corr")(
+                    T.LogMultipole, B["min_sep"], B["max_sep"], mb, B["bin_size"], B["b"],
+                    B["a"], 0., 0., mn, 0., 0., 0., 0., 0, 0., 0., -sys.float_info.max,
+                    sys.float_info.max, 0., 0., 0., *zeta, *[out[k] for k in keys[zk:]])
+
+                def fl(L, c3):
+                    pay = [] if L == "N" else [c3["k"]] if L == "K" else [c3["g1"], c3["g2"]]
+                    return getattr(T, L + "FieldFlat")(c3["x"], c3["y"], e, *pay, c3["w"], e,
+                                                       B["min_size"], B["max_size"], T.Mean,
+                                                       0, False, 3, 10)
+                c.processCross12(fl(cls[0], cv), fl(cls[1], cp), 1, False, False, T.Euclidean)
+                return float(out["ntri"].sum())
+            ms, ntri = timed(step3)
+            res[cls + "_x12"] = {"gpu_ms": ms, "triangles": ntri,
+                                 "gpu_rate": world * ntri / (ms / 1e3), "unit": "triangles/s",
+                                 "n": [n3, n3]}
+    launches = T.launch_count() - launches0
+    if rank == 0 and not args.no_cpu_baseline:
+        # 2-point: auto classes over top-level rows of the same catalog, cross classes on
+        # 1M + 1M points of it (the port's per-pair cost is what is compared).
+        for cls in ("NN", "KK", "NG", "KG"):
+            L1, L2 = cls[0], cls[1]
+            t_budget = max(2.0, args.cpu_budget / 4)
+            if cls in ("NN", "KK"):
+                pay = {"N": (None, None), "K": (cat["k"], None)}[L1]
+                f = O.OracleField(L1, "spherical", cat["x"], cat["y"], cat["z"], *pay, cat["w"],
+                                  None, 0.0, 0.0, "mean", False, 3, 10)
+                ntop = f.ntop()
+                acc, spent, row, chunk = 0, 0.0, 0, 1
+                while spent < t_budget and row < ntop:
+                    r1 = min(ntop, row + chunk)
+                    t0 = time.perf_counter()
+                    o = O.process(cls, "Arc", bins, f, rows=(row, r1), nthreads=nthreads)
+                    spent += time.perf_counter() - t0
+                    acc += o["_accepted"]
+                    row, chunk = r1, min(chunk * 2, 64)
+                sample = f"top-level rows 0..{row} of {ntop} ({spent:.1f} s)"
+            else:
+                m = min(1_000_000, half)
+                a, b = sub(cat, 0, m), sub(cat, half, half + m)
+                pay1 = {"N": (None, None), "K": (a["k"], None)}[L1]
+                f1 = O.OracleField(L1, "spherical", a["x"], a["y"], a["z"], *pay1, a["w"], None,
+                                   0.0, 0.0, "mean", False, 3, 10)
+                f2 = O.OracleField("G", "spherical", b["x"], b["y"], b["z"], b["g1"], b["g2"],
+                                   b["w"], None, 0.0, 0.0, "mean", False, 3, 10)
+                f1.ntop(); f2.ntop()
+                t0 = time.perf_counter()
+                o = O.process(cls, "Arc", bins, f1, f2, nthreads=nthreads)
+                spent = time.perf_counter() - t0
+                acc = o["_accepted"]
+                sample = f"{m} + {m} points of the same catalog ({spent:.1f} s)"
+            res[cls]["cpu_rate"] = acc / spent if spent > 0 else None
+            res[cls]["cpu_sample"] = sample
+        # 3-point: the oracle's cross12 on 50K + 50K points of the same density.
+        ms_ = 50_000
+        side_s = 600.0 * np.sqrt(2 * ms_ / 2e6)
+        sv = ggg_catalog(ms_, args.seed + 21, side=side_s)
+        sp = ggg_catalog(ms_, args.seed + 22, side=side_s)
+        for c3 in (sv, sp):
+            c3["k"] = np.random.default_rng(args.seed + 23).normal(0, 0.02, ms_)
+        B = ggg_bins()
+        for cls in ("GGG", "NGG", "GNN", "NKK"):
+            def of(L, c3, as_k):
+                if as_k:    # the oracle's real-payload fields (NGG vertex / GNN pairs)
+                    kv = c3["k"] if L == "K" else np.ones(len(c3["x"]))
+                    return O.OracleField("K", "flat", c3["x"], c3["y"], None, kv, None,
+                                         c3["w"], None, B["min_size"], B["max_size"], "mean",
+                                         False, 3, 10)
+                g1, g2 = (c3["g1"], c3["g2"]) if L == "G" else (0 * c3["w"], 0 * c3["w"])
+                return O.OracleField("G", "flat", c3["x"], c3["y"], None, g1, g2, c3["w"],
+                                     None, B["min_size"], B["max_size"], "mean", False, 3, 10)
+            mode = 1 if cls == "NGG" else 2 if cls == "GNN" else 0
+            f1 = of(cls[0], sv, mode == 1)
+            f2 = of(cls[1], sp, mode == 2)
+            f1.ntop(); f2.ntop()
+            t0 = time.perf_counter()
+            o = O.multipole("Euclidean", B, B["max_n"], f1, nthreads=nthreads, f2=f2, mode=mode)
+            spent = time.perf_counter() - t0
+            res[cls + "_x12"]["cpu_rate"] = float(o["ntri"].sum()) / spent
+            res[cls + "_x12"]["cpu_sample"] = f"{ms_} + {ms_} points, same density ({spent:.1f} s)"
+    ng = res["NG"]
+    line = {
+        "metric": "per-class throughput of the widened classes (value: NG cross pair-evals/s)",
+        "value": ng["gpu_rate"], "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 1,
+        "ms_per_step": ng["gpu_ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded curved-sky catalog; seeded flat catalogs)",
+        "config": {"workload": "classes: NN, KK auto and NG, KG cross on the 10M-point cap "
+                               "(Arc, 30 Log bins 1-300', bin_slop 0.1); GGG, NGG, GNN, NKK "
+                               "LogMultipole cross12, 1M + 1M flat points (20 bins 1-50', "
+                               "max_n 30)", "n": args.n, "parallelism": f"replicas{world}",
+                   "l2": "inputs larger than L2; no flush"},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "detail": {"classes": res, "cpu_cores": nthreads},
+    }
+    return line
+
+
 def cpu_sample(cat, bins, args, budget_s=15.0):
     """The oracle port of the reference algorithm on the host cores, over top-level rows of
     the auto loop until about budget_s seconds of traversal have been timed."""
@@ -772,11 +953,12 @@ def main():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     p.add_argument("--workload", default="gg",
-                   choices=["gg", "ggg", "learned", "patches", "kmeans"],
+                   choices=["gg", "ggg", "learned", "patches", "kmeans", "classes"],
                    help="gg: the 2-point headline; ggg: the multipole 3-point configuration; "
                         "learned: the learned opening criterion against the plain rule; "
                         "patches: 150 patches, all pairs in one expansion + jackknife; "
-                        "kmeans: k-means patches of the curved-sky catalog")
+                        "kmeans: k-means patches of the curved-sky catalog; "
+                        "classes: the other 2-point and 3-point classes, one call each")
     p.add_argument("--learned-threshold", type=float, default=-3.0)
     p.add_argument("--n", type=int, default=10_000_000)
     p.add_argument("--bin-slop", type=float, default=0.1)
@@ -797,6 +979,8 @@ def main():
         line = run_patches(args, rank, world)
     elif args.workload == "kmeans":
         line = run_kmeans(args, rank, world)
+    elif args.workload == "classes":
+        line = run_classes(args, rank, world)
     else:
         line = run_gpu(args, rank, world)
     if rank == 0 and line is not None:
