@@ -231,7 +231,8 @@ def multipole(metric, bins, max_n, f, quick=False, nthreads=0, f2=None, mode=0):
     from f, vertices 2 and 3 from f2); dict of (nbins, nbins, 2*max_n+1) arrays (zeta0..7
     as gam0r..gam3i, meand2/3, meanlogd2/3, weight, weight_im, ntri).  mode 1 is the
     NGG / KGG form (vertex 1 a K field whose k is 1 or k): gam0 and gam2 are then their
-    zeta0 and zeta1; mode 2 the GNN / GKK form (f2 such a K field): gam0 is their zeta."""
+    zeta0 and zeta1; mode 2 the GNN / GKK form (f2 such a K field): gam0 is their zeta;
+    mode 3 the KKK / NKK / KNN form (f and f2 such K fields): gam0 is their zeta."""
     nb = bins["nbins"]
     shape = (nb, nb, 2 * max_n + 1)
     out = {k: np.zeros(shape) for k in MP_KEYS}

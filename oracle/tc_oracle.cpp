@@ -1323,8 +1323,8 @@ static int multipole_run(int metric, int quick, double minsep, double maxsep, in
     // Vertex 1: a G field, or for NGG / KGG a K field whose k is 1 (N) or k (K), so that
     // its cells' d1 is the real vertex weight (no parallel transport for spin 0).
     // mode 0: GGG; 1: NGG / KGG; 2: GNN / GKK, whose pairs come as a K field whose k is 1
-    // (N) or k (K).
-    const bool vreal = mode == 1, pspin0 = mode == 2;
+    // (N) or k (K); 3: KKK / NKK / KNN, vertex and pairs such K fields.
+    const bool vreal = mode == 1 || mode == 3, pspin0 = mode == 2 || mode == 3;
     const bool v_ok = vreal ? (f1->dtype == DK && f1->spin == 0) : (f1->dtype == DG && f1->spin == 2);
     const bool p_ok = pspin0 ? (f2->dtype == DK && f2->spin == 0) : (f2->dtype == DG && f2->spin == 2);
     if (!v_ok || !p_ok) return 1;

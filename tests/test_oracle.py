@@ -158,8 +158,9 @@ def test_oracle_multipole_cross12_matches_reference(name):
     def close(a, r, what):
         assert np.abs(a - r).max() <= 1e-12 * max(np.abs(r).max(), 1e-300), what
 
-    vreal = letters[0] != "G" and letters[1] == "G"
-    pspin0 = letters[0] == "G" and letters[1] != "G"
+    real = "K" in letters and "G" not in letters     # KKK, NKK, KNN
+    vreal = (letters[0] != "G" and letters[1] == "G") or real
+    pspin0 = (letters[0] == "G" and letters[1] != "G") or real
 
     def as_k(c, letter):
         # An N or K catalog as a K field whose k is 1 (N) or k (K): its cells' d1 is the
@@ -170,7 +171,7 @@ def test_oracle_multipole_cross12_matches_reference(name):
 
     f1 = as_k(cats[0], letters[0]) if vreal else field(cats[0], letters[0], False)
     f2 = as_k(cats[1], letters[1]) if pspin0 else field(cats[1], letters[1], False)
-    mode = 1 if vreal else 2 if pspin0 else 0
+    mode = 3 if real else 1 if vreal else 2 if pspin0 else 0
     out = O.multipole(s["metric"], bins, s["max_n"], f1, nthreads=1, f2=f2, mode=mode)
     assert np.array_equal(out["ntri"], g["ref_ntri"])
     assert out["ntri"].sum() > 0
@@ -179,16 +180,18 @@ def test_oracle_multipole_cross12_matches_reference(name):
     if letters == "GGG":
         for k in O.MP_KEYS[:8]:
             close(out[k], g["ref_" + k], k)
-    if vreal:
+    if vreal and not real:
         # MultipoleHelper<2>'s zeta0 and zeta1 are the contraction's gam0 and gam2.
         for mine, ref in (("gam0r", "gam0r"), ("gam0i", "gam0i"), ("gam2r", "gam1r"),
                           ("gam2i", "gam1i")):
             close(out[mine], g["ref_" + ref], ref)
     elif pspin0:
-        # MultipoleHelper<4>'s zeta is the contraction's gam0.
+        # MultipoleHelper<4>'s and <1>'s zeta is the contraction's gam0.
         close(out["gam0r"], g["ref_zeta"], "zeta")
         close(out["gam0i"], g["ref_zeta_im"], "zeta_im")
-    elif "K" in letters:
+    if real:
+        # The same zeta as the weight contraction over the weights w k (the identity the
+        # KKK auto test checks).
         k1, k2 = field(cats[0], letters[0], True), field(cats[1], letters[1], True)
         zk = O.multipole(s["metric"], bins, s["max_n"], k1, nthreads=1, f2=k2)
         close(zk["weight"], g["ref_zeta"], "zeta")

@@ -919,29 +919,35 @@ int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, int quick, int metric)
     P.tc = cross ? J.tc : f1->tcells;
     P.tops = f1->d_tops; P.ntop = (int)f1->tops.size();
     P.tops2 = cross ? J.tops2 : f1->d_tops; P.ntop2 = (int)f2->tops.size();
+    // The classes other than GGG and NNN run GGG's contraction on real payloads:
+    //  * NGG, KGG (MultipoleHelper<2>, src/Corr3.cpp:2216-2405): an N or K vertex (vreal:
+    //    G_n at n, self-pair sums without z^2), zeta0 / zeta1 = gam0 / gam2;
+    //  * GNN, GKK (MultipoleHelper<4>, 2462-2580): N or K pairs with the real payload w or
+    //    w k, unrotated (pspin0), zeta = gam0;
+    //  * KKK, NKK, KNN (MultipoleHelper<1>, 2108-2214): both, so gam0 = wk1 K_a[n] conj(K_b[n])
+    //    minus wk1 sum (w k)^2 on the diagonal, with K_n = sum (w k or w) z^n: zeta = gam0.
+    // The vertex's payload is (w1 k1 or w1, 0) (getWK) and the pairs' (w k or w, 0); a K
+    // field carries exactly that, an N field's cells get it in the joined copy (a mixed class
+    // always has two fields).
+    const bool nnn = c->dv == TC_NDATA && c->dk == TC_NDATA;
+    const bool vreal = c->dv != TC_GDATA && !nnn;
+    const bool pspin0 = c->dk != TC_GDATA && !nnn;
     const bool xg = c->dk == TC_GDATA && c->dv != TC_GDATA;
-    if (xg) {
-        // NGG, KGG: vertex 1's payload becomes (w1 k1 or w1, 0), the real vertex weight of
-        // MultipoleHelper<2> (getWK, src/Corr3.cpp:2216-2405); field 1's cells are never
-        // pairs, so only the vertex sees it.
-        const size_t n1c = 2 * (size_t)f1->n - 1;
-        if (c->dv == TC_NDATA)
-            TC_CU(cudaMemcpyAsync(J.cells.d1, J.cells.w, sizeof(float) * n1c,
-                                  cudaMemcpyDeviceToDevice, st));
-        TC_CU(cudaMemsetAsync(J.cells.d2, 0, sizeof(float) * n1c, st));
-        P.vreal = 1;
-    }
-    const bool gx = c->dv == TC_GDATA && c->dk != TC_GDATA;
-    if (gx) {
-        // GNN, GKK (MultipoleHelper<4>, src/Corr3.cpp:2462-2580): zeta = wg1 G_a[n-1] G_b[-n-1]
-        // with G_n = sum w z^n (N) or sum w k z^n (K) and the self-pair sum w^2 or (w k)^2
-        // times conj(z^2): GGG's gam0 over field 2's cells with that real payload.
+    if (cross && (vreal || pspin0)) {
         const size_t n1c = 2 * (size_t)f1->n - 1, n2c = (size_t)ncap - n1c;
-        TC_TRY(launch_scalar_pairs((int)n2c, c->dk == TC_NDATA ? 1 : 0, J.tc + n1c,
-                                   J.cells.d1 + n1c, J.cells.d2 + n1c, J.ls + 4 * n1c,
-                                   J.lsf + n1c, st));
-        P.pspin0 = 1;
+        if (vreal) {
+            if (c->dv == TC_NDATA)
+                TC_CU(cudaMemcpyAsync(J.cells.d1, J.cells.w, sizeof(float) * n1c,
+                                      cudaMemcpyDeviceToDevice, st));
+            TC_CU(cudaMemsetAsync(J.cells.d2, 0, sizeof(float) * n1c, st));
+        }
+        if (pspin0)
+            TC_TRY(launch_scalar_pairs((int)n2c, c->dk == TC_NDATA ? 1 : 0, J.tc + n1c,
+                                       J.cells.d1 + n1c, J.cells.d2 + n1c, J.ls + 4 * n1c,
+                                       J.lsf + n1c, st));
     }
+    P.vreal = vreal ? 1 : 0;
+    P.pspin0 = pspin0 ? 1 : 0;
     P.ncells = (int)ncap;
     const size_t Z = (size_t)c->nbins * c->nbins * (2 * c->maxn + 1);
     std::vector<double> h(15 * Z);
@@ -957,66 +963,14 @@ int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, int quick, int metric)
     cudaEventDestroy(e0); cudaEventDestroy(e1);
     c->ms = ms;
     if (rc) return rc == 3 ? TC_ERR_UNSUPPORTED : (rc == 5 ? TC_ERR_NOMEM : TC_ERR_DEVICE);
-    if ((c->dv == TC_KDATA || c->dk == TC_KDATA) && !xg && !gx) {
-        // KKK, NKK, KNN (MultipoleHelper<1>, src/Corr3.cpp:2108-2214): zeta is the weight
-        // contraction with the vertex weight w1 k1 (K) or w1 (N) and the pair weights
-        // w k (K) or w (N), so the multipole runs again over records whose weights are
-        // replaced by w k where the field is a K field; its weight arrays are zeta (real,
-        // imaginary).
-        TCell* tc2 = nullptr;
-        double* ls2 = nullptr;
-        float4* lsf2 = nullptr;
-        float* w2 = nullptr;
-        float* zero = nullptr;
-        std::vector<double> h2(15 * Z);
-        int rc2 = 0;
-        // Cell ranges of the two fields in the joined id space (one range for an auto).
-        const int64_t n1c = cross ? 2 * f1->n - 1 : ncap;
-        struct { int64_t lo, len; bool swap; } rng[2] = {
-            {0, n1c, c->dv == TC_KDATA}, {n1c, ncap - n1c, c->dk == TC_KDATA}};
-        do {
-            if ((rc2 = dalloc(&tc2, ncap)) || (rc2 = dalloc(&ls2, 4 * (size_t)ncap)) ||
-                (rc2 = dalloc(&lsf2, ncap)) || (rc2 = dalloc(&w2, ncap)) ||
-                (rc2 = dalloc(&zero, ncap)))
-                break;
-            if (cudaMemsetAsync(zero, 0, sizeof(float) * (size_t)ncap, st) != cudaSuccess ||
-                cudaMemcpyAsync(tc2, P.tc, sizeof(TCell) * ncap, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
-                cudaMemcpyAsync(ls2, P.ls, sizeof(double) * 4 * ncap, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
-                cudaMemcpyAsync(lsf2, P.lsf, sizeof(float4) * ncap, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
-                cudaMemcpyAsync(w2, CC.w, sizeof(float) * ncap, cudaMemcpyDeviceToDevice, st) != cudaSuccess) {
-                set_last_error("device copy failed"); rc2 = TC_ERR_CUDA; break;
-            }
-            for (const auto& r : rng) {
-                if (!r.swap || r.len <= 0 || rc2) continue;
-                if (cudaMemcpyAsync(w2 + r.lo, CC.d1 + r.lo, sizeof(float) * r.len,
-                                    cudaMemcpyDeviceToDevice, st) != cudaSuccess) {
-                    set_last_error("device copy failed"); rc2 = TC_ERR_CUDA; break;
-                }
-                rc2 = launch_weight_swap((int)r.len, P.tc + r.lo, P.ls + 4 * r.lo, tc2 + r.lo,
-                                         ls2 + 4 * r.lo, lsf2 + r.lo, st);
-            }
-            if (rc2) break;
-            MPParams P2 = P;
-            P2.w = w2;
-            P2.d1 = zero; P2.d2 = zero;
-            P2.ls = ls2; P2.lsf = lsf2; P2.tc = tc2;
-            const int r = run_multipole(P2, c->X, P2.ntop, st, h2.data());
-            if (r) rc2 = r == 3 ? TC_ERR_UNSUPPORTED : (r == 5 ? TC_ERR_NOMEM : TC_ERR_DEVICE);
-        } while (0);
-        dfree(tc2); dfree(ls2); dfree(lsf2); dfree(w2); dfree(zero);
-        if (rc2) return rc2;
-        for (size_t i = 0; i < Z; ++i) {
-            c->zeta[0][i] += h2[12 * Z + i];
-            c->zeta[1][i] += h2[13 * Z + i];
-        }
-    }
-    // Corr3 adds into the caller's arrays (calculateZeta, src/Corr3.cpp:1861-1974).  NGG and
-    // KGG keep gam0 and gam2 of the contraction as their zeta0 (gam0) and zeta1 (gam1); GNN
-    // and GKK keep gam0 as zeta (real, imaginary).
-    for (int q = 0; q < 8 && (c->dk == TC_GDATA || gx); ++q) {
-        const int src = xg ? (q < 2 ? q : q + 2) : q;
-        if (c->zeta[q] && (!xg || q < 4) && (!gx || q < 2))
-            for (size_t i = 0; i < Z; ++i) c->zeta[q][i] += h[src * Z + i];
+    // Corr3 adds into the caller's arrays (calculateZeta, src/Corr3.cpp:1861-1974): GGG all
+    // of gam0..3; NGG / KGG gam0 and gam2 as their zeta0 (gam0) and zeta1 (gam1); the real
+    // classes gam0 as zeta (real, imaginary); NNN nothing.
+    const int zmap[8] = {0, 1, 2, 3, 4, 5, 6, 7}, xgmap[4] = {0, 1, 4, 5};
+    const int nz = (c->dv == TC_GDATA && c->dk == TC_GDATA) ? 8 : xg ? 4 : pspin0 ? 2 : 0;
+    for (int q = 0; q < nz; ++q) {
+        const int src = xg ? xgmap[q] : zmap[q];
+        if (c->zeta[q]) for (size_t i = 0; i < Z; ++i) c->zeta[q][i] += h[src * Z + i];
     }
     double* dst[7] = {c->meand2, c->meanlogd2, c->meand3, c->meanlogd3, c->weight, c->weight_im,
                       c->ntri};

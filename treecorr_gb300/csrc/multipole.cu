@@ -78,40 +78,10 @@ __global__ void k_leaf_sums_f(int ncap, const double* ls, float4* lsf)
     lsf[i] = make_float4((float)p[0], (float)p[1], (float)p[2], (float)p[3]);
 }
 
-// The cell arrays of a K field as a field whose weights are w k: packed records with
-// w := sum w k and no payload, leaf sums (sum (w k)^2, 0, 0, 0).  The multipole's weight
-// contraction over them is KKK's zeta (src/Corr3.cpp:1912-1965 with w -> w k, which is
-// MultipoleHelper<1>, 2108-2150).
-__global__ void k_mp_weight_swap(int ncap, const TCell* tc, const double* ls, TCell* tc2,
-                                 double* ls2, float4* lsf2)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ncap) return;
-    TCell c = tc[i];
-    c.b.w = c.c.x;
-    c.c.x = 0.f;
-    c.c.y = 0.f;
-    tc2[i] = c;
-    const double v = ls[4 * (size_t)i + 1];   // Re sum (w k)^2 of a K field: sum (w k)^2
-    ls2[4 * (size_t)i] = v;
-    ls2[4 * (size_t)i + 1] = 0.;
-    ls2[4 * (size_t)i + 2] = 0.;
-    ls2[4 * (size_t)i + 3] = 0.;
-    lsf2[i] = make_float4((float)v, 0.f, 0.f, 0.f);
-}
-
-int launch_weight_swap(int ncap, const TCell* tc, const double* ls, TCell* tc2, double* ls2,
-                       float4* lsf2, cudaStream_t st)
-{
-    count_launch();
-    k_mp_weight_swap<<<(ncap + 255) / 256, 256, 0, st>>>(ncap, tc, ls, tc2, ls2, lsf2);
-    TC_CU(cudaGetLastError());
-    return 0;
-}
-
-// The cells of an N or K pair field as the real payload of GNN / GKK (MultipoleHelper<4>,
-// src/Corr3.cpp:2462-2580): (d1, d2) := (w, 0) for N (Sigma w z^n is its G_n), (w k, 0) for
-// K; the leaf sums (sum w^2 or sum (w k)^2, 0) stand where the squared shear was.
+// The cells of an N or K pair field as a real payload (GNN, GKK, NKK, KNN, KKK;
+// MultipoleHelper<4> and <1>, src/Corr3.cpp:2462-2580, 2108-2214): (d1, d2) := (w, 0) for N
+// (Sigma w z^n is its G_n), (w k, 0) for K; the leaf sums (sum w^2 or sum (w k)^2, 0) stand
+// where the squared shear was.
 __global__ void k_mp_scalar_pairs(int ncap, int is_n, TCell* tc, float* d1, float* d2,
                                   double* ls, float4* lsf)
 {

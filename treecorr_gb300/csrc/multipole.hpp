@@ -119,10 +119,7 @@ struct MPScratch {
 };
 
 int launch_leaf_sums(int ncap, const Cells& C, double* ls, float4* lsf, cudaStream_t st);
-// K-field cells re-weighted by w k for the KKK zeta pass (records, leaf sums).
-int launch_weight_swap(int ncap, const TCell* tc, const double* ls, TCell* tc2, double* ls2,
-                       float4* lsf2, cudaStream_t st);
-// N / K pair cells as the real payload (w or w k, 0) of GNN / GKK.
+// N / K pair cells as the real payload (w or w k, 0) of GNN, GKK, NKK, KNN.
 int launch_scalar_pairs(int ncap, int is_n, TCell* tc, float* d1, float* d2, double* ls,
                         float4* lsf, cudaStream_t st);
 // Runs both phases and the reduction; h_out receives 15 arrays of nbins*nbins*(2*maxn+1)
