@@ -242,13 +242,23 @@ void tc_corr3_free(tc_corr3* c);
  * 1124-1175): the G_n / Gamma_n multipole accumulation over one G field. */
 int tc_corr3_process_auto(tc_corr3* c, tc_field* f, int dots, int quick, int metric);
 
-/* BaseCorr3.processCross12 -> ProcessCross12c -> BaseCorr3::multipole(field1, field2)
- * (src/Corr3.cpp:4199, 3730-3768, 1177-1237): vertex 1 from f1, vertices 2 and 3 from f2,
- * both fields of the class's data kind and coordinate system.  Only ordered = 1 is on the
- * GPU path (what the Python layer passes for ordered=True, treecorr/corr3base.py:1968);
- * ordered = 0 returns TC_ERR_UNSUPPORTED. */
+/* BaseCorr3.processCross12 -> ProcessCross12c (src/Corr3.cpp:4199, 3730-3768): one vertex
+ * from f1, two from f2.  ordered = 1 runs multipole(field1, field2) (1177-1237); ordered = 0
+ * adds the three-field multipole(field2, field1, field2, 1) first, as the reference does. */
 int tc_corr3_process_cross12(tc_corr3* c, tc_field* f1, tc_field* f2, int ordered, int dots,
                              int quick, int metric);
+
+/* BaseCorr3.processCross21 -> ProcessCross21c (src/Corr3.cpp:4200, 3831-3868): two vertices
+ * from f1, one from f2, through the three-field multipole (1239-1305): ordered = 3 runs
+ * multipole(f1, f1, f2, 4); ordered = 0 the three placements with ordered 1. */
+int tc_corr3_process_cross21(tc_corr3* c, tc_field* f1, tc_field* f2, int ordered, int dots,
+                             int quick, int metric);
+
+/* BaseCorr3.processCross -> ProcessCrossc (src/Corr3.cpp:4201, 3938-3976): one vertex from
+ * each field through the three-field multipole, with the reference's placements for
+ * ordered = 0 .. 4.  Vertex 2's and 3's fields must share a data kind (d2 = d3). */
+int tc_corr3_process_cross(tc_corr3* c, tc_field* f1, tc_field* f2, tc_field* f3,
+                           int ordered, int dots, int quick, int metric);
 
 /* Device time of the last tc_corr3_process_auto call in ms (no reference counterpart). */
 double tc_corr3_last_ms(const tc_corr3* c);

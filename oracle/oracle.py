@@ -73,6 +73,13 @@ def lib():
                                                   ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                                   ctypes.c_int, ctypes.POINTER(dp)] + [dp] * 7
+        L.orc_corr3_multipole_cross3.restype = ctypes.c_int
+        L.orc_corr3_multipole_cross3.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                                 ctypes.c_double, ctypes.c_int, ctypes.c_double,
+                                                 ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                                 ctypes.c_void_p, ctypes.c_void_p,
+                                                 ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.c_int, ctypes.POINTER(dp)] + [dp] * 7
         L.orc_last_accepted.restype = ctypes.c_longlong
         L.orc_last_accepted.argtypes = []
         L.orc_max_threads.restype = ctypes.c_int
@@ -247,6 +254,24 @@ def multipole(metric, bins, max_n, f, quick=False, nthreads=0, f2=None, mode=0):
                                                *tail)
     if rc:
         raise ValueError("multipole needs G fields in one coordinate system")
+    return out
+
+
+def multipole3(metric, bins, max_n, f1, f2, f3, ordered, quick=False, nthreads=0, mode=0,
+               out=None):
+    """The oracle's three-field LogMultipole (vertex 1 from f1, 2 from f2, 3 from f3,
+    ordered 1 or 4), accumulated into out (a dict as multipole returns) when given."""
+    nb = bins["nbins"]
+    shape = (nb, nb, 2 * max_n + 1)
+    if out is None:
+        out = {k: np.zeros(shape) for k in MP_KEYS}
+    gam = (ctypes.POINTER(ctypes.c_double) * 8)(*[_p(out[k]) for k in MP_KEYS[:8]])
+    rc = lib().orc_corr3_multipole_cross3(
+        METRICS[metric], int(bool(quick)), bins["min_sep"], bins["max_sep"], nb,
+        bins["bin_size"], bins["b"], bins["a"], int(max_n), f1.h, f2.h, f3.h, int(ordered),
+        int(mode), int(nthreads), gam, *[_p(out[k]) for k in MP_KEYS[8:]])
+    if rc:
+        raise ValueError("multipole3: fields, coordinates or ordered not supported")
     return out
 
 

@@ -888,6 +888,134 @@ void multipole_split1(const Params& P, const Field& f1, const Field& f2, int i1,
     }
 }
 
+// ---------------------------------------------------------------------------------------
+// The three-field multipole: vertex 1 from f1, vertex 2 from f2, vertex 3 from f3
+// (BaseCorr3::multipole(field1, field2, field3, ordered), src/Corr3.cpp:1239-1305).
+
+// Corr3::calculateZeta(c1, ordered, mp2, mp3, kstart, mink_zeta), src/Corr3.cpp:1976-2087,
+// with the multipole products of MultipoleHelper<5> written directly (its #if 0 form,
+// 2868-2890): entries (k2, k3) with min(k2, k3) in [kstart, mink_zeta); mp3 goes with k2
+// (it holds the d2 distances) and mp2 with k3; ordered = 1 adds the swapped products.
+void calculate_zeta3(const Params& P, const Node& c1, int ordered, const MPS& mp2,
+                     const MPS& mp3, int kstart, int mink_zeta, Out3& O)
+{
+    const int nb = mp2.nbins, maxn = mp2.maxn, nn = 2 * maxn + 1;
+    const double w1 = c1.w;
+    const cd wg1(c1.d1, c1.d2);
+    const int s = P.vreal ? 0 : 1;
+    const bool swap23 = ordered == 1;
+    // GNN / GKK's zeta (MultipoleHelper<4>, src/Corr3.cpp:2532-2572) is written for
+    // ordered = 4 only and has no swapped term; the weights and means still have it.
+    const bool swap_g = swap23 && !(P.pspin0 && !P.vreal);
+    auto idx = [&](int a, int b, int n) { return (a * nb + b) * nn + maxn + n; };
+    auto Wn = [&](const MPS& m, int k, int n) {
+        return n >= 0 ? m.Wn[m.widx(k) + n] : std::conj(m.Wn[m.widx(k) - n]);
+    };
+    for (int k2 = kstart; k2 < nb; ++k2) {
+        const int k3end = k2 < mink_zeta ? nb : mink_zeta;
+        for (int k3 = kstart; k3 < k3end; ++k3) {
+            if (!P.quick) {
+                const double n1 = double(c1.n);
+                const int i = idx(k2, k3, 0);
+                if (ordered == 4) {
+                    O.ntri[i] += n1 * mp3.npairs[k2] * mp2.npairs[k3];
+                    const double ww12 = w1 * mp3.sumw[k2], ww13 = w1 * mp2.sumw[k3];
+                    O.meand2[i] += ww13 * mp3.sumwr[k2];
+                    O.meanlogd2[i] += ww13 * mp3.sumwlogr[k2];
+                    O.meand3[i] += ww12 * mp2.sumwr[k3];
+                    O.meanlogd3[i] += ww12 * mp2.sumwlogr[k3];
+                } else {
+                    O.ntri[i] += n1 * (mp2.npairs[k2] * mp3.npairs[k3] +
+                                       mp3.npairs[k2] * mp2.npairs[k3]);
+                    O.meand2[i] += w1 * (mp2.sumw[k3] * mp3.sumwr[k2] + mp3.sumw[k3] * mp2.sumwr[k2]);
+                    O.meanlogd2[i] += w1 * (mp2.sumw[k3] * mp3.sumwlogr[k2] +
+                                            mp3.sumw[k3] * mp2.sumwlogr[k2]);
+                    O.meand3[i] += w1 * (mp2.sumw[k2] * mp3.sumwr[k3] + mp3.sumw[k2] * mp2.sumwr[k3]);
+                    // The reference's second term takes mp3.sumw at k3 (src/Corr3.cpp:2036).
+                    O.meanlogd3[i] += w1 * (mp2.sumw[k2] * mp3.sumwlogr[k3] +
+                                            mp3.sumw[k3] * mp2.sumwlogr[k3]);
+                }
+            }
+            for (int n = -maxn; n <= maxn; ++n) {
+                const int i = idx(k2, k3, n);
+                cd ww = w1 * Wn(mp3, k2, n) * std::conj(Wn(mp2, k3, n));
+                cd g0 = wg1 * mp3.G(k2, n - s) * mp2.G(k3, -n - s);
+                cd g1 = std::conj(wg1) * mp3.G(k2, n + s) * mp2.G(k3, -n + s);
+                cd g2 = wg1 * mp3.G(k2, n - s) * std::conj(mp2.G(k3, n + s));
+                cd g3 = wg1 * std::conj(mp3.G(k2, -n + s)) * mp2.G(k3, -n - s);
+                if (swap23) ww += w1 * Wn(mp2, k2, n) * std::conj(Wn(mp3, k3, n));
+                if (swap_g) {
+                    g0 += wg1 * mp2.G(k2, n - s) * mp3.G(k3, -n - s);
+                    g1 += std::conj(wg1) * mp2.G(k2, n + s) * mp3.G(k3, -n + s);
+                    g2 += wg1 * mp2.G(k2, n - s) * std::conj(mp3.G(k3, n + s));
+                    g3 += wg1 * std::conj(mp2.G(k2, -n + s)) * mp3.G(k3, -n - s);
+                }
+                O.weight[i] += ww.real(); O.weight_im[i] += ww.imag();
+                O.gam[0][i] += g0.real(); O.gam[1][i] += g0.imag();
+                O.gam[2][i] += g1.real(); O.gam[3][i] += g1.imag();
+                O.gam[4][i] += g2.real(); O.gam[5][i] += g2.imag();
+                O.gam[6][i] += g3.real(); O.gam[7][i] += g3.imag();
+            }
+        }
+    }
+}
+
+// BaseCorr3::multipoleFinish with two lists, src/Corr3.cpp:1615-1679.
+void multipole_finish3(const Params& P, const Field& f1, const Field& f2, const Field& f3,
+                       int i1, const std::vector<int>& l2, const std::vector<int>& l3,
+                       MPS& mp2, MPS& mp3, int ordered, int mink_zeta, double maxr2,
+                       double maxr3, Out3& O)
+{
+    const Node& c1 = f1.nodes[i1];
+    bool anysplit1 = false;
+    std::vector<int> n2, n3;
+    maxr2 = split_or_gn(P, f2, c1, l2, n2, anysplit1, mp2, maxr2);
+    maxr3 = split_or_gn(P, f3, c1, l3, n3, anysplit1, mp3, maxr3);
+    const double maxr = std::max(maxr2, maxr3);
+    if (!n2.empty() || !n3.empty()) {
+        if (maxr < P.maxsep) {
+            int k = maxr < P.minsep ? 0 : int((std::log(maxr) - P.logminsep) / P.binsize) + 1;
+            if (k < mink_zeta) {
+                calculate_zeta3(P, c1, ordered, mp2, mp3, k, mink_zeta, O);
+                mink_zeta = k;
+            }
+        }
+        if (anysplit1) {
+            MPS c2 = mp2, c3 = mp3;
+            multipole_finish3(P, f1, f2, f3, c1.left, n2, n3, mp2, mp3, ordered, mink_zeta,
+                              maxr2, maxr3, O);
+            multipole_finish3(P, f1, f2, f3, c1.right, n2, n3, c2, c3, ordered, mink_zeta,
+                              maxr2, maxr3, O);
+        } else {
+            multipole_finish3(P, f1, f2, f3, i1, n2, n3, mp2, mp3, ordered, mink_zeta, maxr2,
+                              maxr3, O);
+        }
+    } else {
+        calculate_zeta3(P, c1, ordered, mp2, mp3, 0, mink_zeta, O);
+    }
+}
+
+// BaseCorr3::multipoleSplit1 with two lists, src/Corr3.cpp:1410-1449.
+void multipole_split1_3(const Params& P, const Field& f1, const Field& f2, const Field& f3,
+                        int i1, const std::vector<int>& l2, const std::vector<int>& l3,
+                        MPS& mp2, MPS& mp3, int ordered, Out3& O)
+{
+    const Node& c1 = f1.nodes[i1];
+    const double s1 = c1.size;
+    std::vector<int> n2, n3;
+    split_c2_cells(P, f2, c1, l2, n2);
+    split_c2_cells(P, f3, c1, l3, n3);
+    const double maxbsq_eff = P.maxsepsq * std::min(P.bsq, P.asq);
+    if (s1 * s1 > maxbsq_eff) {
+        multipole_split1_3(P, f1, f2, f3, c1.left, n2, n3, mp2, mp3, ordered, O);
+        multipole_split1_3(P, f1, f2, f3, c1.right, n2, n3, mp2, mp3, ordered, O);
+    } else {
+        mp2.clear();
+        mp3.clear();
+        multipole_finish3(P, f1, f2, f3, i1, n2, n3, mp2, mp3, ordered, P.nbins, 0., 0., O);
+    }
+}
+
 long long g_last_accepted = 0;   // directProcess11 calls of the last process call
 
 // ---------------------------------------------------------------------------------------
@@ -1381,6 +1509,62 @@ int orc_corr3_multipole_cross12(int metric, int quick, double minsep, double max
     return multipole_run(metric, quick, minsep, maxsep, nbins, binsize, b, a, maxn, h1, h2,
                          mode, nthreads, gam8, meand2, meanlogd2, meand3, meanlogd3, weight,
                          weight_im, ntri);
+}
+
+// The three-field multipole (vertex 1 from h1, 2 from h2, 3 from h3; ordered 1 or 4); the
+// fields and modes as for orc_corr3_multipole_cross12 (h2 and h3 share a kind).
+int orc_corr3_multipole_cross3(int metric, int quick, double minsep, double maxsep, int nbins,
+                               double binsize, double b, double a, int maxn, void* h1,
+                               void* h2, void* h3, int ordered, int mode, int nthreads,
+                               double** gam8, double* meand2, double* meanlogd2,
+                               double* meand3, double* meanlogd3, double* weight,
+                               double* weight_im, double* ntri)
+{
+    Field* f1 = static_cast<Field*>(h1);
+    Field* f2 = static_cast<Field*>(h2);
+    Field* f3 = static_cast<Field*>(h3);
+    const bool vreal = mode == 1 || mode == 3, pspin0 = mode == 2 || mode == 3;
+    const bool v_ok = vreal ? (f1->dtype == DK && f1->spin == 0) : (f1->dtype == DG && f1->spin == 2);
+    auto p_ok = [&](const Field* f) {
+        return pspin0 ? (f->dtype == DK && f->spin == 0) : (f->dtype == DG && f->spin == 2);
+    };
+    if (!v_ok || !p_ok(f2) || !p_ok(f3)) return 1;
+    if (f1->coords != f2->coords || f1->coords != f3->coords) return 2;
+    if (ordered != 1 && ordered != 4) return 3;
+    Params P = make_params(DG * 16 + DG, f1->coords, metric, quick, minsep, maxsep, nbins, binsize, b, a);
+    P.vreal = vreal ? 1 : 0;
+    P.pspin0 = pspin0 ? 1 : 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+    if (f1->pts.empty() || f2->pts.empty() || f3->pts.empty()) return 0;
+    build_cells(*f1);
+    if (f2 != f1) build_cells(*f2);
+    if (f3 != f1 && f3 != f2) build_cells(*f3);
+    const long n1 = (long)f1->tops.size();
+    Out3 total(nbins, maxn);
+#pragma omp parallel
+    {
+        Out3 O(nbins, maxn);
+        MPS mp2(nbins, maxn), mp3(nbins, maxn);
+#pragma omp for schedule(dynamic)
+        for (long i = 0; i < n1; ++i)
+            multipole_split1_3(P, *f1, *f2, *f3, f1->tops[i], f2->tops, f3->tops, mp2, mp3,
+                               ordered, O);
+#pragma omp critical
+        total.add(O);
+    }
+    for (int q = 0; q < 8; ++q)
+        if (gam8[q]) for (int i = 0; i < total.size; ++i) gam8[q][i] += total.gam[q][i];
+    for (int i = 0; i < total.size; ++i) {
+        meand2[i] += total.meand2[i]; meanlogd2[i] += total.meanlogd2[i];
+        meand3[i] += total.meand3[i]; meanlogd3[i] += total.meanlogd3[i];
+        weight[i] += total.weight[i]; weight_im[i] += total.weight_im[i];
+        ntri[i] += total.ntri[i];
+    }
+    return 0;
 }
 
 int orc_max_threads(void)

@@ -93,8 +93,8 @@ def run_case(name):
     return out
 
 
-if __name__ == "__main__" and not {"--mp", "--mp-nnn", "--mp-kkk", "--mp-x12", "--xyz",
-                                   "--kmeans"} & set(sys.argv):
+if __name__ == "__main__" and not {"--mp", "--mp-nnn", "--mp-kkk", "--mp-x12", "--mp-x3",
+                                   "--xyz", "--kmeans"} & set(sys.argv):
     _treecorr.SetOMPThreads(1)
     names = sys.argv[1:] or list(CASES)
     for name in names:
@@ -339,3 +339,70 @@ if __name__ == "__main__" and "--mp-x12" in sys.argv:
             save["ref_" + k] = v
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **save)
         print(f"{name:20s} ntri={out['ntri'].sum():.6g} weight={out['weight'].sum():.6g}")
+
+
+# The three-field LogMultipole (src/Corr3.cpp:1239-1305) through the reference's
+# processCross (3938-3976), processCross21 (3831-3868) and processCross12 with ordered = 0
+# (3730-3768): name -> (class, catalogs' case, call, ordered).  Catalogs: the case's, seed +
+# 1000 and seed + 2000; a 21 / 12 call takes the first two.
+X3_CASES = {
+    "ggg_flat_mp_x3o4": ("GGG", "ggg_flat_mp", "cross", 4),
+    "ggg_sphere_mp_x3o1": ("GGG", "ggg_sphere_mp", "cross", 1),
+    "ggg_flat_mp_x21o3": ("GGG", "ggg_flat_mp", "cross21", 3),
+    "kkk_flat_mp_x3o0": ("KKK", "ggg_flat_mp", "cross", 0),
+    "nnn_sphere_mp_x12o0": ("NNN", "ggg_sphere_mp", "cross12", 0),
+    "ngg_flat_mp_x3o4": ("NGG", "ggg_flat_mp", "cross", 4),
+    "gkk_sphere_mp_x3o1": ("GKK", "ggg_sphere_mp", "cross", 1),
+}
+
+if __name__ == "__main__" and "--mp-x3" in sys.argv:
+    _treecorr.SetOMPThreads(1)
+    from cases3 import make_inputs3, spec3
+    only = [a for a in sys.argv[1:] if not a.startswith("--")]
+    for name, (letters, gname, call, ordered) in X3_CASES.items():
+        if only and name not in only:
+            continue
+        s = spec3(gname)
+        cats = [make_inputs3(gname, seed=20240601 + 1000 * i) for i in range(3)]
+        cats[0] = make_inputs3(gname)
+        if s["metric"] == "Euclidean":
+            b1 = min(s["a"], s["b"])
+            min_size, max_size = 2 * s["min_sep"] * b1 / (2. + 3 * b1), s["max_sep"] * b1
+        else:
+            min_size, max_size = 0.0, 0.0
+        nb, mn = s["nbins"], s["max_n"]
+        shape = (nb, nb, 2 * mn + 1)
+        common = ("meand1", "meanlogd1", "meand2", "meanlogd2", "meand3", "meanlogd3", "meanu",
+                  "meanv", "weight", "weight_im", "ntri")
+        zk = (("gam0r", "gam0i", "gam1r", "gam1i", "gam2r", "gam2i", "gam3r", "gam3i")
+              if letters == "GGG" else ("gam0r", "gam0i", "gam1r", "gam1i")
+              if letters[1:] == "GG" else ("zeta", "zeta_im")
+              if ("K" in letters or letters[0] == "G") else ())
+        out = {k: np.zeros(shape) for k in zk + common}
+        e = np.array([])
+        zeta = [out[k] for k in zk] + [e] * (8 - len(zk))
+        cls = getattr(_treecorr, letters + "Corr")
+        corr = cls(_treecorr.LogMultipole, s["min_sep"], s["max_sep"], nb, s["bin_size"], s["b"],
+                   s["a"], 0., 0., mn, 0., 0., 0., 0., 0, 0., 0.,
+                   -sys.float_info.max, sys.float_info.max, 0., 0., 0.,
+                   *zeta, *[out[k] for k in common])
+        kinds = {"cross": letters, "cross21": letters[0] + letters[2], "cross12": letters[:2]}[call]
+        fs = [build_field(L, s["coords"], c, min_size, max_size, "mean", False, 3, 10)
+              for L, c in zip(kinds, cats)]
+        m = METRIC[s["metric"]]
+        if call == "cross":
+            corr.processCross(fs[0], fs[1], fs[2], ordered, False, False, m)
+        elif call == "cross21":
+            corr.processCross21(fs[0], fs[1], ordered, False, False, m)
+        else:
+            corr.processCross12(fs[0], fs[1], ordered, False, False, m)
+        save = dict(min_size=min_size, max_size=max_size, case=gname, letters=letters,
+                    call=call, ordered=ordered)
+        for i in range(len(kinds)):
+            for k, v in cats[i].items():
+                if v is not None:
+                    save[f"c{i + 1}_" + k] = v
+        for k, v in out.items():
+            save["ref_" + k] = v
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **save)
+        print(f"{name:22s} ntri={out['ntri'].sum():.6g} weight={out['weight'].sum():.6g}")

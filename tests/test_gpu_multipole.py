@@ -191,9 +191,6 @@ def test_multipole_cross12_golden(gpu_lib, name):
         r = g["ref_" + k]
         err = np.abs(out[k] - r).max() / max(np.abs(r).max(), 1e-300)
         assert err <= TOL, f"{name} {k}: {err:.3e}"
-    # ordered = 0 needs the three-field cross multipole, which is not on the GPU path.
-    with pytest.raises(NotImplementedError):
-        corr.processCross12(f1, f2, 0, False, False, m)
     # Fields of another data kind are refused (vertex 1 and the pair field swapped, or a G
     # field in place of an N one), and so is processAuto for a mixed class.
     other = "N" if letters[1] != "N" else "G"
@@ -247,3 +244,58 @@ def test_multipole_cross12_cuda_core_contraction(gpu_lib, monkeypatch, name):
         r = g["ref_" + k]
         err = np.abs(out[k] - r).max() / max(np.abs(r).max(), 1e-300)
         assert err <= TOL, f"{name} {k}: {err:.3e}"
+
+
+def _x3_run(T, g, s):
+    """The fixture's processCross / processCross21 / processCross12(ordered = 0) call on the
+    GPU module."""
+    letters, call, ordered = str(g["letters"]), str(g["call"]), int(g["ordered"])
+    kinds = {"cross": letters, "cross21": letters[0] + letters[2], "cross12": letters[:2]}[call]
+    cats = [{k[3:]: g[k] for k in g.files if k.startswith(f"c{i + 1}_")} for i in range(len(kinds))]
+    fs = [H.gpu_field(T, L, s["coords"], c, float(g["min_size"]), float(g["max_size"]))
+          for L, c in zip(kinds, cats)]
+    m = T.Euclidean if s["metric"] == "Euclidean" else T.Arc
+    corr, out, zk = _corr3(T, letters, s)
+    if call == "cross":
+        corr.processCross(fs[0], fs[1], fs[2], ordered, False, False, m)
+    elif call == "cross21":
+        corr.processCross21(fs[0], fs[1], ordered, False, False, m)
+    else:
+        corr.processCross12(fs[0], fs[1], ordered, False, False, m)
+    return out, zk
+
+
+@pytest.mark.parametrize("name", ["ggg_flat_mp_x3o4", "ggg_sphere_mp_x3o1", "ggg_flat_mp_x21o3",
+                                  "kkk_flat_mp_x3o0", "nnn_sphere_mp_x12o0", "ngg_flat_mp_x3o4",
+                                  "gkk_sphere_mp_x3o1"])
+@pytest.mark.parametrize("tensor", ["1", "0"])
+def test_multipole_three_field_golden(gpu_lib, monkeypatch, name, tensor):
+    """The three-field multipole (vertex 2's pairs in bins [0, nb), vertex 3's in [nb, 2 nb)
+    of one scratch) through processCross / processCross21 / processCross12(ordered = 0),
+    against the reference's own calls, on the tensor-core and the CUDA-core contraction."""
+    from cases3 import spec3
+    monkeypatch.setenv("TCGPU_MP_TENSOR", tensor)
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    s = spec3(str(g["case"]))
+    out, zk = _x3_run(gpu_lib, g, s)
+    assert np.array_equal(out["ntri"], g["ref_ntri"]), name
+    for k in zk + ("weight", "weight_im", "meand2", "meanlogd2", "meand3", "meanlogd3"):
+        r = g["ref_" + k]
+        err = np.abs(out[k] - r).max() / max(np.abs(r).max(), 1e-300)
+        assert err <= TOL, f"{name} {k}: {err:.3e}"
+
+
+def test_multipole_three_field_inplace(gpu_lib, monkeypatch):
+    """A record buffer of a few vertices sends most vertex records of a three-field cross to
+    the in-place FP64 contraction; the result must not change."""
+    from cases3 import spec3
+    monkeypatch.setenv("TCGPU_MP_RECORD_BYTES", str(40 * 16 * 1024))
+    name = "ggg_sphere_mp_x3o1"
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    s = spec3(str(g["case"]))
+    out, zk = _x3_run(gpu_lib, g, s)
+    assert np.array_equal(out["ntri"], g["ref_ntri"])
+    for k in zk + ("weight", "weight_im", "meand2", "meanlogd2", "meand3", "meanlogd3"):
+        r = g["ref_" + k]
+        err = np.abs(out[k] - r).max() / max(np.abs(r).max(), 1e-300)
+        assert err <= TOL, f"{k}: {err:.3e}"

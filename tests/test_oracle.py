@@ -196,3 +196,118 @@ def test_oracle_multipole_cross12_matches_reference(name):
         zk = O.multipole(s["metric"], bins, s["max_n"], k1, nthreads=1, f2=k2)
         close(zk["weight"], g["ref_zeta"], "zeta")
         close(zk["weight_im"], g["ref_zeta_im"], "zeta_im")
+
+
+X3 = ["ggg_flat_mp_x3o4", "ggg_sphere_mp_x3o1", "ggg_flat_mp_x21o3", "kkk_flat_mp_x3o0",
+      "nnn_sphere_mp_x12o0", "ngg_flat_mp_x3o4", "gkk_sphere_mp_x3o1"]
+
+
+def x3_fields(O, g, s):
+    """The fixture's catalogs as oracle fields in the representation of the class (the
+    identities of the cross12 test) and the oracle mode."""
+    letters = str(g["letters"])
+    args = (float(g["min_size"]), float(g["max_size"]), "mean", False, 3, 10)
+    cats = []
+    for i in (1, 2, 3):
+        c = {k[3:]: g[k] for k in g.files if k.startswith(f"c{i}_")}
+        if c:
+            cats.append(c)
+
+    def mk(c, rep):
+        zero = np.zeros(len(c["x"]))
+        if rep == "G":
+            return O.OracleField("G", s["coords"], c["x"], c["y"], c.get("z"), c["g1"],
+                                 c["g2"], c["w"], None, *args)
+        if rep == "G0":
+            return O.OracleField("G", s["coords"], c["x"], c["y"], c.get("z"), zero, zero,
+                                 c["w"], None, *args)
+        kv = c["k"] if rep == "K" else np.ones(len(c["x"]))
+        return O.OracleField("K", s["coords"], c["x"], c["y"], c.get("z"), kv, None, c["w"],
+                             None, *args)
+
+    if letters == "GGG":
+        return [mk(c, "G") for c in cats], 0
+    if letters == "NNN":
+        return [mk(c, "G0") for c in cats], 0
+    if letters == "KKK":
+        return [mk(c, "K") for c in cats], 3
+    if letters == "NGG":
+        return [mk(cats[0], "K1")] + [mk(c, "G") for c in cats[1:]], 1
+    if letters == "GKK":
+        return [mk(cats[0], "G")] + [mk(c, "K") for c in cats[1:]], 2
+    raise AssertionError(letters)
+
+
+def x3_oracle(O, g, s):
+    """The reference's dispatch of processCross / processCross21 / processCross12
+    (src/Corr3.cpp:3938-3976, 3831-3868, 3730-3768) over the oracle's multipoles."""
+    fs, mode = x3_fields(O, g, s)
+    bins = dict(min_sep=s["min_sep"], max_sep=s["max_sep"], nbins=s["nbins"],
+                bin_size=s["bin_size"], b=s["b"], a=s["a"])
+    call, ordered = str(g["call"]), int(g["ordered"])
+    out = {k: np.zeros((s["nbins"], s["nbins"], 2 * s["max_n"] + 1)) for k in O.MP_KEYS}
+
+    def m3(a, b, c, o):
+        O.multipole3(s["metric"], bins, s["max_n"], a, b, c, o, nthreads=1, mode=mode, out=out)
+
+    if call == "cross":
+        f1, f2, f3 = fs
+        if ordered == 0:
+            m3(f2, f1, f3, 1); m3(f3, f1, f2, 1); m3(f1, f2, f3, 1)
+        elif ordered == 1:
+            m3(f1, f2, f3, 1)
+        elif ordered == 2:
+            m3(f1, f2, f3, 4); m3(f3, f2, f1, 4)
+        elif ordered == 3:
+            m3(f1, f2, f3, 4); m3(f2, f1, f3, 4)
+        else:
+            m3(f1, f2, f3, 4)
+    elif call == "cross21":
+        f1, f2 = fs
+        if ordered == 0:
+            m3(f2, f1, f1, 1); m3(f1, f2, f1, 1); m3(f1, f1, f2, 1)
+        else:
+            m3(f1, f1, f2, 4)
+    else:
+        f1, f2 = fs
+        if ordered == 0:
+            m3(f2, f1, f2, 1)
+        o2 = O.multipole(s["metric"], bins, s["max_n"], f1, nthreads=1, f2=f2, mode=mode)
+        for k in O.MP_KEYS:
+            out[k] += o2[k]
+    return out
+
+
+def x3_zeta_pairs(letters):
+    """(oracle output, reference output) pairs of the class's zeta arrays."""
+    if letters == "GGG":
+        return [(k, k) for k in ("gam0r", "gam0i", "gam1r", "gam1i", "gam2r", "gam2i", "gam3r",
+                                 "gam3i")]
+    if letters[1:] == "GG":
+        return [("gam0r", "gam0r"), ("gam0i", "gam0i"), ("gam2r", "gam1r"), ("gam2i", "gam1i")]
+    if "K" in letters or letters[0] == "G":
+        return [("gam0r", "zeta"), ("gam0i", "zeta_im")]
+    return []
+
+
+@pytest.mark.parametrize("name", X3)
+def test_oracle_multipole_three_field_matches_reference(name):
+    """The three-field multipole (src/Corr3.cpp:1239-1305, calculateZeta 1976-2087 with the
+    reference's ordered = 1 meanlogd3 term) through the reference's dispatch of
+    processCross / processCross21 / processCross12(ordered = 0)."""
+    import os
+    from cases3 import spec3
+    from oracle import oracle as O
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    s = spec3(str(g["case"]))
+    out = x3_oracle(O, g, s)
+    assert np.array_equal(out["ntri"], g["ref_ntri"])
+    assert out["ntri"].sum() > 0
+
+    def close(a, r, what):
+        assert np.abs(a - r).max() <= 1e-12 * max(np.abs(r).max(), 1e-300), what
+
+    for k in ("weight", "weight_im", "meand2", "meanlogd2", "meand3", "meanlogd3"):
+        close(out[k], g["ref_" + k], k)
+    for mine, ref in x3_zeta_pairs(str(g["letters"])):
+        close(out[mine], g["ref_" + ref], ref)

@@ -131,6 +131,10 @@ def lib():
         L.tc_corr3_process_auto.argtypes = [vp, vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         L.tc_corr3_process_cross12.restype = ctypes.c_int
         L.tc_corr3_process_cross12.argtypes = [vp, vp, vp] + [ctypes.c_int] * 4
+        L.tc_corr3_process_cross21.restype = ctypes.c_int
+        L.tc_corr3_process_cross21.argtypes = [vp, vp, vp] + [ctypes.c_int] * 4
+        L.tc_corr3_process_cross.restype = ctypes.c_int
+        L.tc_corr3_process_cross.argtypes = [vp, vp, vp, vp] + [ctypes.c_int] * 4
         L.tc_corr3_last_ms.restype = ctypes.c_double
         L.tc_corr3_last_ms.argtypes = [vp]
         L.tc_corr3_stats.restype = ctypes.c_int
@@ -620,26 +624,28 @@ del _x, _a
 
 
 class BaseCorr3:
-    """BaseCorr3 (src/Corr3.cpp:4187-4201): processAuto and processCross12 (ordered = 1)
-    with LogMultipole binning."""
+    """BaseCorr3 (src/Corr3.cpp:4187-4201): processAuto, processCross12, processCross21 and
+    processCross with LogMultipole binning."""
 
     def processAuto(self, field, dots, quick, metric):
         _check(lib().tc_corr3_process_auto(self._h, field._h, int(bool(dots)), int(bool(quick)),
                                            int(metric)))
 
     def processCross12(self, field1, field2, ordered, dots, quick, metric):
-        """One vertex from field1, two from field2 (ProcessCross12c, src/Corr3.cpp:3730-3768);
-        ordered = 0 (the three-field cross multipole) raises NotImplementedError."""
-        if int(ordered) != 1:
-            raise NotImplementedError("processCross12 with ordered = 0 needs the three-field "
-                                      "cross multipole, which is not on the GPU path")
+        """One vertex from field1, two from field2 (ProcessCross12c, src/Corr3.cpp:3730-3768)."""
         _check(lib().tc_corr3_process_cross12(self._h, field1._h, field2._h, int(ordered),
                                               int(bool(dots)), int(bool(quick)), int(metric)))
 
-    def processCross21(self, *args):
-        raise NotImplementedError("processCross21 and processCross are not on the GPU path")
+    def processCross21(self, field1, field2, ordered, dots, quick, metric):
+        """Two vertices from field1, one from field2 (ProcessCross21c, src/Corr3.cpp:3831-3868)."""
+        _check(lib().tc_corr3_process_cross21(self._h, field1._h, field2._h, int(ordered),
+                                              int(bool(dots)), int(bool(quick)), int(metric)))
 
-    processCross = processCross21
+    def processCross(self, field1, field2, field3, ordered, dots, quick, metric):
+        """One vertex from each field (ProcessCrossc, src/Corr3.cpp:3938-3976)."""
+        _check(lib().tc_corr3_process_cross(self._h, field1._h, field2._h, field3._h,
+                                            int(ordered), int(bool(dots)), int(bool(quick)),
+                                            int(metric)))
 
     def triviallyZero(self, *args):
         raise NotImplementedError("triviallyZero for 3-point is not on the GPU path")

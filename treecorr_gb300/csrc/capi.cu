@@ -814,38 +814,51 @@ __global__ void k_shift_ids(int* a, long long n, int base)
     if (i < n && a[i] >= 0) a[i] += base;
 }
 
-int join_cells(const tc_field* f1, const tc_field* f2, JoinedCells& J, cudaStream_t st)
+// nf fields (2 or 3) side by side; J.tops2 lists the top cells of fields 1..nf-1 (the pair
+// lists' starting cells), with their joined ids.
+int join_cells(tc_field* const* fs, int nf, JoinedCells& J, cudaStream_t st)
 {
-    const size_t n1 = 2 * (size_t)f1->n - 1, n2 = 2 * (size_t)f2->n - 1, n = n1 + n2;
+    size_t cnt[3], base[3], n = 0, ntops = 0;
+    for (int i = 0; i < nf; ++i) {
+        cnt[i] = 2 * (size_t)fs[i]->n - 1;
+        base[i] = n;
+        n += cnt[i];
+        if (i > 0) ntops += fs[i]->tops.size();
+    }
     TC_TRY(dalloc(&J.cells.x, n)); TC_TRY(dalloc(&J.cells.y, n)); TC_TRY(dalloc(&J.cells.z, n));
     TC_TRY(dalloc(&J.cells.size, n)); TC_TRY(dalloc(&J.cells.w, n));
     TC_TRY(dalloc(&J.cells.d1, n)); TC_TRY(dalloc(&J.cells.d2, n));
     TC_TRY(dalloc(&J.cells.n, n)); TC_TRY(dalloc(&J.cells.left, n));
     TC_TRY(dalloc(&J.cells.right, n));
     TC_TRY(dalloc(&J.ls, 4 * n)); TC_TRY(dalloc(&J.lsf, n)); TC_TRY(dalloc(&J.tc, n));
-    TC_TRY(dalloc(&J.tops2, f2->tops.size()));
-    auto cat = [&](auto* dst, const auto* a, const auto* b, size_t per) -> int {
-        const size_t e = sizeof(*dst) * per;
-        TC_CU(cudaMemcpyAsync(dst, a, e * n1, cudaMemcpyDeviceToDevice, st));
-        TC_CU(cudaMemcpyAsync(dst + per * n1, b, e * n2, cudaMemcpyDeviceToDevice, st));
+    TC_TRY(dalloc(&J.tops2, ntops));
+    auto cp = [&](auto* dst, const auto* src, size_t per, int i) -> int {
+        TC_CU(cudaMemcpyAsync(dst + per * base[i], src, sizeof(*dst) * per * cnt[i],
+                              cudaMemcpyDeviceToDevice, st));
         return 0;
     };
-    const Cells &A = f1->cells, &B = f2->cells;
-    TC_TRY(cat(J.cells.x, A.x, B.x, 1)); TC_TRY(cat(J.cells.y, A.y, B.y, 1));
-    TC_TRY(cat(J.cells.z, A.z, B.z, 1)); TC_TRY(cat(J.cells.size, A.size, B.size, 1));
-    TC_TRY(cat(J.cells.w, A.w, B.w, 1)); TC_TRY(cat(J.cells.d1, A.d1, B.d1, 1));
-    TC_TRY(cat(J.cells.d2, A.d2, B.d2, 1)); TC_TRY(cat(J.cells.n, A.n, B.n, 1));
-    TC_TRY(cat(J.cells.left, A.left, B.left, 1)); TC_TRY(cat(J.cells.right, A.right, B.right, 1));
-    TC_TRY(cat(J.ls, f1->leafsums, f2->leafsums, 4)); TC_TRY(cat(J.lsf, f1->leafsums_f, f2->leafsums_f, 1));
-    TC_TRY(cat(J.tc, f1->tcells, f2->tcells, 1));
-    TC_CU(cudaMemcpyAsync(J.tops2, f2->d_tops, sizeof(int) * f2->tops.size(),
-                          cudaMemcpyDeviceToDevice, st));
-    const unsigned g2 = (unsigned)((n2 + 255) / 256);
-    count_launch(); k_shift_ids<<<g2, 256, 0, st>>>(J.cells.left + n1, (long long)n2, (int)n1);
-    count_launch(); k_shift_ids<<<g2, 256, 0, st>>>(J.cells.right + n1, (long long)n2, (int)n1);
-    count_launch(); k_rebase_cells<<<g2, 256, 0, st>>>(J.tc + n1, (long long)n2, (int)n1, 0);
-    const unsigned gt = (unsigned)((f2->tops.size() + 255) / 256);
-    count_launch(); k_shift_ids<<<gt, 256, 0, st>>>(J.tops2, (long long)f2->tops.size(), (int)n1);
+    size_t toff = 0;
+    for (int i = 0; i < nf; ++i) {
+        const Cells& A = fs[i]->cells;
+        TC_TRY(cp(J.cells.x, A.x, 1, i)); TC_TRY(cp(J.cells.y, A.y, 1, i));
+        TC_TRY(cp(J.cells.z, A.z, 1, i)); TC_TRY(cp(J.cells.size, A.size, 1, i));
+        TC_TRY(cp(J.cells.w, A.w, 1, i)); TC_TRY(cp(J.cells.d1, A.d1, 1, i));
+        TC_TRY(cp(J.cells.d2, A.d2, 1, i)); TC_TRY(cp(J.cells.n, A.n, 1, i));
+        TC_TRY(cp(J.cells.left, A.left, 1, i)); TC_TRY(cp(J.cells.right, A.right, 1, i));
+        TC_TRY(cp(J.ls, fs[i]->leafsums, 4, i)); TC_TRY(cp(J.lsf, fs[i]->leafsums_f, 1, i));
+        TC_TRY(cp(J.tc, fs[i]->tcells, 1, i));
+        if (i == 0) continue;
+        const size_t nt = fs[i]->tops.size();
+        TC_CU(cudaMemcpyAsync(J.tops2 + toff, fs[i]->d_tops, sizeof(int) * nt,
+                              cudaMemcpyDeviceToDevice, st));
+        const unsigned g = (unsigned)((cnt[i] + 255) / 256), gt = (unsigned)((nt + 255) / 256);
+        const int bi = (int)base[i];
+        count_launch(); k_shift_ids<<<g, 256, 0, st>>>(J.cells.left + base[i], (long long)cnt[i], bi);
+        count_launch(); k_shift_ids<<<g, 256, 0, st>>>(J.cells.right + base[i], (long long)cnt[i], bi);
+        count_launch(); k_rebase_cells<<<g, 256, 0, st>>>(J.tc + base[i], (long long)cnt[i], bi, 0);
+        count_launch(); k_shift_ids<<<gt, 256, 0, st>>>(J.tops2 + toff, (long long)nt, bi);
+        toff += nt;
+    }
     TC_CU(cudaGetLastError());
     return 0;
 }
@@ -860,37 +873,45 @@ int ensure_leaf_sums(tc_field* f, cudaStream_t st)
     return 0;
 }
 
-// BaseCorr3::multipole for GGG / NNN / KKK with LogMultipole binning: the auto-correlation
-// (f2 == f1, src/Corr3.cpp:1124-1175) or cross12, vertex 1 from f1 and vertices 2 and 3 from
-// f2 (src/Corr3.cpp:1177-1237, which ProcessCross12c runs for ordered = 1, 3730-3768).
-int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, int quick, int metric)
+// BaseCorr3::multipole with LogMultipole binning: the auto-correlation (f2 == f1, f3 null,
+// src/Corr3.cpp:1124-1175), cross12 (vertex 1 from f1, vertices 2 and 3 from f2,
+// 1177-1237), or the three-field cross (vertex 1 from f1, vertex 2 from f2, vertex 3 from
+// f3, with ordered 1 or 4, 1239-1305).
+int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, tc_field* f3, int ordered, int quick,
+              int metric)
 {
     if (!c || !f1 || !f2) { set_last_error("NULL argument"); return TC_ERR_ARG; }
-    if (f1->dkind != c->dv || f2->dkind != c->dk) {
+    if (f1->dkind != c->dv || f2->dkind != c->dk || (f3 && f3->dkind != c->dk)) {
         static const char L[] = "NKGZVTQ";
         const char cls[4] = {L[c->dv], L[c->dk], L[c->dk], 0};
         set_last_error(std::string(cls) + ": the fields have the wrong data kind (vertex 1 " +
                        L[c->dv] + ", vertices 2 and 3 " + L[c->dk] + ")");
         return TC_ERR_ARG;
     }
-    if (f1->coords != f2->coords) {
+    if (f1->coords != f2->coords || (f3 && f3->coords != f1->coords)) {
         set_last_error("the fields have different coordinate systems");
         return TC_ERR_ARG;
     }
     TC_TRY(check_metric(f1->coords, metric));
-    if (f1->n == 0 || f2->n == 0) return TC_OK;
+    if (f1->n == 0 || f2->n == 0 || (f3 && f3->n == 0)) return TC_OK;
+    const bool three = f3 != nullptr;
+    if (three && 2 * c->nbins > MP_MAXNB) {
+        set_last_error("the three-field GPU multipole needs nbins <= 64");
+        return TC_ERR_UNSUPPORTED;
+    }
     cudaStream_t st;
     TC_TRY(stream_get(&st));
-    TC_TRY(field_build(f1));
-    TC_TRY(ensure_leaf_sums(f1, st));
-    const bool cross = f2 != f1;
-    JoinedCells J;
-    if (cross) {
-        TC_TRY(field_build(f2));
-        TC_TRY(ensure_leaf_sums(f2, st));
-        TC_TRY(join_cells(f1, f2, J, st));
+    tc_field* fs[3] = {f1, f2, f3};
+    const int nf = three ? 3 : 2;
+    for (int i = 0; i < nf; ++i) {
+        TC_TRY(field_build(fs[i]));
+        TC_TRY(ensure_leaf_sums(fs[i], st));
     }
-    const int64_t ncap = cross ? (2 * f1->n - 1) + (2 * f2->n - 1) : 2 * f1->n - 1;
+    const bool cross = three || f2 != f1;
+    JoinedCells J;
+    if (cross) TC_TRY(join_cells(fs, nf, J, st));
+    int64_t ncap = 0;
+    for (int i = 0; i < (cross ? nf : 1); ++i) ncap += 2 * fs[i]->n - 1;
     const Cells& CC = cross ? J.cells : f1->cells;
     if (ncap >= (int64_t)INT32_MAX) {
         set_last_error("too many cells for 32-bit cell ids");
@@ -918,7 +939,16 @@ int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, int quick, int metric)
     P.lsf = cross ? J.lsf : f1->leafsums_f;
     P.tc = cross ? J.tc : f1->tcells;
     P.tops = f1->d_tops; P.ntop = (int)f1->tops.size();
-    P.tops2 = cross ? J.tops2 : f1->d_tops; P.ntop2 = (int)f2->tops.size();
+    P.tops2 = cross ? J.tops2 : f1->d_tops;
+    P.ntop2 = (int)(f2->tops.size() + (three ? f3->tops.size() : 0));
+    // Distance bins; a three-field cross keeps vertex 3's pairs in bins [nb, 2 nb) of the
+    // scratch and the records.
+    const int nb = c->nbins, nbv = three ? 2 * nb : nb;
+    P.nbins = nbv;
+    P.nbd = nb;
+    P.three = three ? 1 : 0;
+    P.base3 = three ? (int)((2 * f1->n - 1) + (2 * f2->n - 1)) : 0;
+    P.typo32 = three && ordered == 1 ? 1 : 0;
     // The classes other than GGG and NNN run GGG's contraction on real payloads:
     //  * NGG, KGG (MultipoleHelper<2>, src/Corr3.cpp:2216-2405): an N or K vertex (vreal:
     //    G_n at n, self-pair sums without z^2), zeta0 / zeta1 = gam0 / gam2;
@@ -949,8 +979,9 @@ int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, int quick, int metric)
     P.vreal = vreal ? 1 : 0;
     P.pspin0 = pspin0 ? 1 : 0;
     P.ncells = (int)ncap;
-    const size_t Z = (size_t)c->nbins * c->nbins * (2 * c->maxn + 1);
-    std::vector<double> h(15 * Z);
+    const int nn = 2 * c->maxn + 1;
+    const size_t Z = (size_t)nb * nb * nn, Zv = (size_t)nbv * nbv * nn;
+    std::vector<double> h(15 * Zv);
     cudaEvent_t e0, e1;
     TC_CU(cudaEventCreate(&e0));
     TC_CU(cudaEventCreate(&e1));
@@ -963,6 +994,26 @@ int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, int quick, int metric)
     cudaEventDestroy(e0); cudaEventDestroy(e1);
     c->ms = ms;
     if (rc) return rc == 3 ? TC_ERR_UNSUPPORTED : (rc == 5 ? TC_ERR_NOMEM : TC_ERR_DEVICE);
+    if (three) {
+        // calculateZeta(c1, ordered, mp2, mp3, ...), src/Corr3.cpp:1976-2087: entry (k2, k3)
+        // is the vertex-3 x vertex-2 block (mp3 at k2, mp2 at k3); ordered = 1 adds the
+        // vertex-2 x vertex-3 block (cats 2 and 3 swapped).
+        // GNN / GKK's zeta (MultipoleHelper<4>, 2532-2572) is written for ordered = 4 only:
+        // it has no swapped term, while their weights and means do.
+        const bool gx = c->dv == TC_GDATA && c->dk != TC_GDATA;
+        std::vector<double> hz(15 * Z);
+        for (int q = 0; q < 15; ++q)
+            for (int k2 = 0; k2 < nb; ++k2)
+                for (int k3 = 0; k3 < nb; ++k3)
+                    for (int n = 0; n < nn; ++n) {
+                        const size_t i32 = ((size_t)(k2 + nb) * nbv + k3) * nn + n;
+                        const size_t i23 = ((size_t)k2 * nbv + k3 + nb) * nn + n;
+                        double v = h[q * Zv + i32];
+                        if (ordered == 1 && !(gx && q < 8)) v += h[q * Zv + i23];
+                        hz[q * Z + ((size_t)k2 * nb + k3) * nn + n] = v;
+                    }
+        h.swap(hz);
+    }
     // Corr3 adds into the caller's arrays (calculateZeta, src/Corr3.cpp:1861-1974): GGG all
     // of gam0..3; NGG / KGG gam0 and gam2 as their zeta0 (gam0) and zeta1 (gam1); the real
     // classes gam0 as zeta (real, imaginary); NNN nothing.
@@ -1768,19 +1819,55 @@ void tc_corr3_free(tc_corr3* c)
 int tc_corr3_process_auto(tc_corr3* c, tc_field* f, int dots, int quick, int metric)
 {
     (void)dots;
-    return corr3_run(c, f, f, quick, metric);
+    return corr3_run(c, f, f, nullptr, 1, quick, metric);
 }
 
 int tc_corr3_process_cross12(tc_corr3* c, tc_field* f1, tc_field* f2, int ordered, int dots,
                              int quick, int metric)
 {
     (void)dots;
-    if (ordered != 1) {
-        set_last_error("processCross12 with ordered = 0 needs the three-field cross multipole, "
-                       "which is not on the GPU path");
-        return TC_ERR_UNSUPPORTED;
+    // ProcessCross12c, src/Corr3.cpp:3730-3768.
+    if (ordered == 0) TC_TRY(corr3_run(c, f2, f1, f2, 1, quick, metric));
+    else if (ordered != 1) { set_last_error("ordered must be 0 or 1"); return TC_ERR_ARG; }
+    return corr3_run(c, f1, f2, nullptr, 1, quick, metric);
+}
+
+int tc_corr3_process_cross21(tc_corr3* c, tc_field* f1, tc_field* f2, int ordered, int dots,
+                             int quick, int metric)
+{
+    (void)dots;
+    // ProcessCross21c, src/Corr3.cpp:3831-3868.
+    if (ordered == 0) {
+        TC_TRY(corr3_run(c, f2, f1, f1, 1, quick, metric));
+        TC_TRY(corr3_run(c, f1, f2, f1, 1, quick, metric));
+        return corr3_run(c, f1, f1, f2, 1, quick, metric);
     }
-    return corr3_run(c, f1, f2, quick, metric);
+    if (ordered == 3) return corr3_run(c, f1, f1, f2, 4, quick, metric);
+    set_last_error("ordered must be 0 or 3");
+    return TC_ERR_ARG;
+}
+
+int tc_corr3_process_cross(tc_corr3* c, tc_field* f1, tc_field* f2, tc_field* f3, int ordered,
+                           int dots, int quick, int metric)
+{
+    (void)dots;
+    if (!f3) { set_last_error("NULL argument"); return TC_ERR_ARG; }
+    // ProcessCrossc, src/Corr3.cpp:3938-3976.
+    switch (ordered) {
+      case 0:
+        TC_TRY(corr3_run(c, f2, f1, f3, 1, quick, metric));
+        TC_TRY(corr3_run(c, f3, f1, f2, 1, quick, metric));
+        return corr3_run(c, f1, f2, f3, 1, quick, metric);
+      case 1: return corr3_run(c, f1, f2, f3, 1, quick, metric);
+      case 2:
+        TC_TRY(corr3_run(c, f1, f2, f3, 4, quick, metric));
+        return corr3_run(c, f3, f2, f1, 4, quick, metric);
+      case 3:
+        TC_TRY(corr3_run(c, f1, f2, f3, 4, quick, metric));
+        return corr3_run(c, f2, f1, f3, 4, quick, metric);
+      case 4: return corr3_run(c, f1, f2, f3, 4, quick, metric);
+      default: set_last_error("ordered must be 0 .. 4"); return TC_ERR_ARG;
+    }
 }
 
 double tc_corr3_last_ms(const tc_corr3* c) { return c ? c->ms : 0.; }

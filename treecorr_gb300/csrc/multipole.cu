@@ -272,7 +272,7 @@ __device__ __forceinline__ int mp_decide32(const MPParams& P, float rsq, float s
             const float frac = kk - (float)ik;
             if (frac < ML || frac > 1.f - ML) return -1;
         }
-        k = ik < P.nbins ? ik : P.nbins - 1;
+        k = ik < P.nbd ? ik : P.nbd - 1;
         logr = lr;
         return 1;
     }
@@ -466,7 +466,9 @@ __global__ void __launch_bounds__(MB) k_mp_split1(MPParams P)
 // ---------------------------------------------------------------------------------------
 // Phase 2: multipoleFinish per job.
 
-struct P2Entry { int c1, len, slot, mink; long long goff; double maxr; long long mark; };
+// maxr / maxr3: the previous pass's largest remaining r + s over the vertex-2 (or only)
+// list and the vertex-3 list (multipoleFinish keeps them apart, src/Corr3.cpp:1616-1679).
+struct P2Entry { int c1, len, slot, mink; long long goff; double maxr, maxr3; long long mark; };
 
 // Scratch slot layout (doubles): W_n [n = 0 .. M][bin] complex, G_n [n + M + 1 = 0 .. 2M+2]
 // [bin] complex, gg0/gg1/gg2 [bin] complex, then npairs, sumw, sumwr, sumwlogr, sumww,
@@ -818,6 +820,74 @@ __device__ void zeta_products(const MPParams& P, int c1, const double* S, int ks
     __syncthreads();
 }
 
+// The in-place path of a three-field cross (Corr3::calculateZeta with mp2, mp3,
+// src/Corr3.cpp:1976-2087): every entry (a, b) of the scratch's 2 nbd x 2 nbd bins whose
+// row and column belong to different vertices and whose min(a mod nbd, b mod nbd) is in
+// [ks, mk), with the auto-correlation's off-diagonal formulas; the caller keeps the
+// vertex-3 x vertex-2 block (and, for ordered = 1, adds the other).
+__device__ void zeta_inplace3(const MPParams& P, int c1, const double* S, int ks, int mk,
+                              double* out, double* shG, double* shW)
+{
+    const int nb = P.nbins, nbd = P.nbd, M = P.maxn, nn = 2 * M + 1;
+    const int gst = 2 * M + 3;
+    const size_t Z = (size_t)nb * nb * nn;
+    const double* W = S;
+    const double* G = S + 2 * (size_t)nb * (M + 1);
+    const double* SC = G + 2 * (size_t)nb * gst + 6 * (size_t)nb;
+    for (int q = threadIdx.x; q < 2 * nb * gst; q += MB) shG[q] = __ldcg(G + q);
+    for (int q = threadIdx.x; q < 2 * nb * (M + 1); q += MB) shW[q] = __ldcg(W + q);
+    __syncthreads();
+    const double w1 = P.w[c1];
+    const double n1 = P.n[c1];
+    const C2 wg1 = {(double)P.d1[c1], (double)P.d2[c1]};
+    const C2 wg1c = conj2(wg1);
+    const int sh = P.vreal ? 0 : 1;
+    auto Gv = [&](int k, int n) -> C2 {
+        const double* p = shG + sG(nb, M, n, k);
+        return {p[0], p[1]};
+    };
+    auto Wv = [&](int k, int n) -> C2 {
+        const double* p = shW + sW(nb, n >= 0 ? n : -n, k);
+        return n >= 0 ? C2{p[0], p[1]} : C2{p[0], -p[1]};
+    };
+    const long long cnt = (long long)nb * nb * nn;
+    for (long long t = threadIdx.x; t < cnt; t += MB) {
+        const int n = (int)(t % nn) - M;
+        const int b = (int)((t / nn) % nb), a = (int)(t / nn / nb);
+        if ((a >= nbd) == (b >= nbd)) continue;
+        const int m = min(a % nbd, b % nbd);
+        if (m < ks || m >= mk) continue;
+        const size_t i = (size_t)(a * nb + b) * nn + M + n;
+        const C2 p = cmul(Wv(a, n), conj2(Wv(b, n)));
+        out[12 * Z + i] += w1 * p.re;
+        out[13 * Z + i] += w1 * p.im;
+        const C2 g0 = cmul(cmul(wg1, Gv(a, n - sh)), Gv(b, -n - sh));
+        const C2 g1 = cmul(cmul(wg1c, Gv(a, n + sh)), Gv(b, -n + sh));
+        const C2 g2 = cmul(cmul(wg1, Gv(a, n - sh)), conj2(Gv(b, n + sh)));
+        const C2 g3 = cmul(cmul(wg1, conj2(Gv(a, -n + sh))), Gv(b, -n - sh));
+        out[0 * Z + i] += g0.re; out[1 * Z + i] += g0.im;
+        out[2 * Z + i] += g1.re; out[3 * Z + i] += g1.im;
+        out[4 * Z + i] += g2.re; out[5 * Z + i] += g2.im;
+        out[6 * Z + i] += g3.re; out[7 * Z + i] += g3.im;
+        if (n == 0 && !P.quick) {
+            const size_t i0 = (size_t)(a * nb + b) * nn + M;
+            const double npa = __ldcg(SC + a), npb = __ldcg(SC + b);
+            const double swa = __ldcg(SC + nb + a), swb = __ldcg(SC + nb + b);
+            const double sra = __ldcg(SC + 2 * nb + a), srb = __ldcg(SC + 2 * nb + b);
+            const double sla = __ldcg(SC + 3 * nb + a), slb = __ldcg(SC + 3 * nb + b);
+            // meanlogd3 of the vertex-3 x vertex-2 block for ordered = 1 as the reference
+            // writes it: mp3.sumw at the column's bin.
+            const double swl = (P.typo32 && a >= nbd) ? __ldcg(SC + nb + (b % nbd) + nbd) : swa;
+            out[14 * Z + i0] += n1 * npa * npb;
+            out[8 * Z + i0] += w1 * swb * sra;
+            out[9 * Z + i0] += w1 * swb * sla;
+            out[10 * Z + i0] += w1 * swa * srb;
+            out[11 * Z + i0] += w1 * swl * slb;
+        }
+    }
+    __syncthreads();
+}
+
 // calculateZeta for vertex c1, rows [ks, mk): the diagonal self-pair corrections now, the
 // rest as one vertex record for the batched contraction kernels (k_mp_zeta, k_mp_zscal).
 // Record (floats): header (c1, ks, mk, w1, Re/Im wg1, n1, pad), then G_n [n = -(M+1) ..
@@ -828,7 +898,8 @@ __device__ void zeta_emit(const MPParams& P, int c1, const double* S, int ks, in
                           unsigned long long* zidx_sh, int* emits_sh)
 {
     const int nb = P.nbins, M = P.maxn, gst = 2 * M + 3;
-    zeta_diag(P, c1, S, ks, mk, diag);
+    // (a three-field cross has no self-pair corrections: getMP2 / getMP3 without ww)
+    if (!P.three) zeta_diag(P, c1, S, ks, mk, diag);
     if (threadIdx.x == 0) {
         *zidx_sh = atomicAdd(P.zcount, 1ull);
         ++*emits_sh;
@@ -859,6 +930,8 @@ __device__ void zeta_emit(const MPParams& P, int c1, const double* S, int ks, in
             RS[4 * nb + q] = (float)__ldcg(SC + 5 * nb + q);            // sumwwr
             RS[5 * nb + q] = (float)__ldcg(SC + 6 * nb + q);            // sumwwlogr
         }
+    } else if (P.three) {
+        zeta_inplace3(P, c1, S, ks, mk, out, shG, shW);
     } else {
         if (!P.quick) zeta_scalars(P, c1, S, ks, mk, out);
         zeta_products(P, c1, S, ks, mk, out, shG, shW);
@@ -874,7 +947,7 @@ __global__ void __launch_bounds__(MB, 2) k_mp_finish(MPParams P)
     __shared__ P2Entry cur;
     __shared__ unsigned long long job_sh, zidx_sh;
     __shared__ int acc_n, new_n, anysplit, alloc_ok, have_sh, job_emits;
-    __shared__ double maxr_sh[MW];
+    __shared__ double maxr_sh[MW], maxr3_sh[MW];
     __shared__ long long arena_top;
     __shared__ int bh[MP_MAXNB];
     __shared__ int bw[MW][MP_MAXNB];
@@ -919,8 +992,8 @@ __global__ void __launch_bounds__(MB, 2) k_mp_finish(MPParams P)
             job_emits = 0;
             int s0 = free_list[--free_cnt];
             P2Entry e;
-            e.c1 = J.x; e.len = J.w; e.slot = s0; e.mink = nb;
-            e.goff = (long long)J.y * P.arena1_cap + J.z; e.maxr = 0.;
+            e.c1 = J.x; e.len = J.w; e.slot = s0; e.mink = P.nbd;
+            e.goff = (long long)J.y * P.arena1_cap + J.z; e.maxr = 0.; e.maxr3 = 0.;
             e.mark = 0;
             stk[sp++] = e;
         }
@@ -970,25 +1043,32 @@ __global__ void __launch_bounds__(MB, 2) k_mp_finish(MPParams P)
                 }
                 const int c1 = cur.c1;
                 const double s1 = P.size[c1];
-                const double thresh1 = (1. - P.binsize) * cur.maxr;   // oneBinLessThan
+                // oneBinLessThan of each list's previous maximum
+                const double thresh1_2 = (1. - P.binsize) * cur.maxr;
+                const double thresh1_3 = (1. - P.binsize) * cur.maxr3;
                 const int* list = (cur.goff >= 0) ? (arena1 + cur.goff) : nullptr;
                 const int* list2 = (cur.goff < 0) ? (arena + (-cur.goff - 1)) : nullptr;
                 const long long nbase = arena_top;
                 double* S = slot_ptr(P, blk, cur.slot);
                 if (tid == 0) { acc_n = 0; new_n = 0; anysplit = 0; }
-                double mymax = 0.;
-                float run32 = 0.f;
+                double mymax = 0., mymax3 = 0.;
+                float run32 = 0.f, run32_3 = 0.f;
                 int myany = 0;
                 const float4 c1a = __ldg(reinterpret_cast<const float4*>(P.tc + c1));
                 const float4 c1b = __ldg(reinterpret_cast<const float4*>(P.tc + c1) + 1);
                 const float s1f = c1a.w;
-                const float thresh1f = (float)thresh1;
+                const float thresh1f_2 = (float)thresh1_2, thresh1f_3 = (float)thresh1_3;
                 __syncthreads();
                 for (int j0 = 0; j0 < cur.len; j0 += MB) {
                     const int j = j0 + tid;
                     int cnt = 0, ca = -1, cb = -1, acc_ok = 0, kacc = -1;
                     double racc = 0., lracc = 0.;
                     const int c2 = j < cur.len ? __ldcg(list ? list + j : list2 + j) : 0;
+                    // A vertex-3 cell of a three-field cross: its own threshold, maximum and
+                    // bins [nbd, 2 nbd).
+                    const bool is3 = P.three && c2 >= P.base3;
+                    const double thresh1 = is3 ? thresh1_3 : thresh1_2;
+                    const float thresh1f = is3 ? thresh1f_3 : thresh1f_2;
                     bool dec32 = false;          // decided (and recorded) in FP32
                     float rs32 = 0.f;            // r + s of an FP32-decided unaccepted entry
                     float r32 = 0.f, lr32 = 0.f, dxf = 0.f, dyf = 0.f;
@@ -1044,12 +1124,13 @@ __global__ void __launch_bounds__(MB, 2) k_mp_finish(MPParams P)
                                         lr = log(r);
                                         k = int((lr - P.logminsep) / P.binsize);
                                     }
-                                    if (k >= nb) k = nb - 1;
+                                    if (k >= P.nbd) k = P.nbd - 1;
                                     acc_ok = 1; kacc = k; racc = r; lracc = lr;
                                     ca = c2;
                                 }
                             } else {
-                                mymax = fmax(mymax, r + s);
+                                if (is3) mymax3 = fmax(mymax3, r + s);
+                                else mymax = fmax(mymax, r + s);
                                 // CalcSplitSq (include/Split.h:82-101)
                                 double bsq_eff = rsq * fmin(P.bsq, P.asq);
                                 bool split1, split2;
@@ -1070,17 +1151,22 @@ __global__ void __launch_bounds__(MB, 2) k_mp_finish(MPParams P)
                     // the next pass's thresholds): the warp's FP32 maximum is compared with its
                     // running FP32 maximum, and the entries within the FP32 error of the larger
                     // one get their FP64 value; all other entries are below an evaluated one.
-                    {
-                        float wm = rs32;
+                    // (per list for a three-field cross)
+                    for (int li = 0; li < (P.three ? 2 : 1); ++li) {
+                        const float rsl = (li == 1) == is3 ? rs32 : 0.f;
+                        float& runl = li ? run32_3 : run32;
+                        float wm = rsl;
                         for (int o = 16; o > 0; o >>= 1) wm = fmaxf(wm, __shfl_xor_sync(0xffffffffu, wm, o));
-                        if (wm > run32 * (1.f - 8e-6f)) {
-                            if (rs32 > 0.f && rs32 > wm * (1.f - 8e-6f)) {
+                        if (wm > runl * (1.f - 8e-6f)) {
+                            if (rsl > 0.f && rsl > wm * (1.f - 8e-6f)) {
                                 const double rs64 = sqrt(mp_dist_sq(P, c1, c2)) + (s1 + (double)ta.w);
-                                mymax = fmax(mymax, rs64);
+                                if (li) mymax3 = fmax(mymax3, rs64);
+                                else mymax = fmax(mymax, rs64);
                             }
-                            run32 = fmaxf(run32, wm);
+                            runl = fmaxf(runl, wm);
                         }
                     }
+                    if (acc_ok && is3) kacc += P.nbd;
                     int tot_new, tot_acc;
                     int pos = block_excl_scan(cnt, scan_sh, tot_new);
                     int apos = block_excl_scan(acc_ok, scan_sh, tot_acc);
@@ -1169,12 +1255,20 @@ __global__ void __launch_bounds__(MB, 2) k_mp_finish(MPParams P)
                 // Block max of the remaining separations and OR of anysplit1.
                 for (int o = 16; o > 0; o >>= 1) {
                     mymax = fmax(mymax, __shfl_xor_sync(0xffffffffu, mymax, o));
+                    mymax3 = fmax(mymax3, __shfl_xor_sync(0xffffffffu, mymax3, o));
                     myany |= __shfl_xor_sync(0xffffffffu, myany, o);
                 }
-                if (lane == 0) { maxr_sh[wid] = mymax; if (myany) atomicOr(&anysplit, 1); }
+                if (lane == 0) {
+                    maxr_sh[wid] = mymax; maxr3_sh[wid] = mymax3;
+                    if (myany) atomicOr(&anysplit, 1);
+                }
                 __syncthreads();
-                double maxrem = 0.;
-                for (int k = 0; k < MW; ++k) maxrem = fmax(maxrem, maxr_sh[k]);
+                double maxrem2 = 0., maxrem3 = 0.;
+                for (int k = 0; k < MW; ++k) {
+                    maxrem2 = fmax(maxrem2, maxr_sh[k]);
+                    maxrem3 = fmax(maxrem3, maxr3_sh[k]);
+                }
+                const double maxrem = fmax(maxrem2, maxrem3);
                 const int n_new = new_n;
                 int mink = cur.mink;
                 if (n_new == 0) {
@@ -1203,7 +1297,8 @@ __global__ void __launch_bounds__(MB, 2) k_mp_finish(MPParams P)
                         } else {
                             P2Entry rgt;
                             rgt.c1 = P.right[c1]; rgt.len = n_new; rgt.slot = free_list[--free_cnt];
-                            rgt.mink = mink; rgt.goff = -nbase - 1; rgt.maxr = maxrem;
+                            rgt.mink = mink; rgt.goff = -nbase - 1;
+                            rgt.maxr = maxrem2; rgt.maxr3 = maxrem3;
                             rgt.mark = nbase + n_new;
                             stk[sp++] = rgt;
                         }
@@ -1241,7 +1336,8 @@ __global__ void __launch_bounds__(MB, 2) k_mp_finish(MPParams P)
                     cur.len = n_new;
                     cur.goff = -newoff - 1;
                     cur.mink = mink;
-                    cur.maxr = maxrem;
+                    cur.maxr = maxrem2;
+                    cur.maxr3 = maxrem3;
                     arena_top = newoff + n_new;
                 }
                 __syncthreads();
@@ -1273,6 +1369,8 @@ struct ZParams {
     long long nrec;
     int rec_floats, nbins, maxn, chunk, ngroups;
     int shift;             // 1: G_n at n -+ 1 (a spin-2 vertex); 0: at n (an N or K vertex)
+    int nbd;               // distance bins; a record's rows [ks, mk) hold min(a, b) mod nbd
+    int typo32;            // see MPParams::typo32
     double* part;          // [group][10][Z]
     long long Z;
 };
@@ -1345,7 +1443,7 @@ __global__ void __launch_bounds__(ZB) k_mp_zeta(ZParams Q)
             const int2 rw = rows_sh[v];
 #pragma unroll
             for (int j = 0; j < ZE; ++j) {
-                const int m = min(ea[j], eb[j]);
+                const int m = min(ea[j] % Q.nbd, eb[j] % Q.nbd);
                 if (!ev[j] || m < rw.x || m >= rw.y) continue;
                 const float4* pa = zsh + ((size_t)v * nb + ea[j]) * 4;
                 const float4* pb = zsh + ((size_t)v * nb + eb[j]) * 4;
@@ -1537,7 +1635,7 @@ __global__ void __launch_bounds__(TCB) k_mp_zeta_tc(ZParams Q, int* status)
 #pragma unroll
             for (int t = 0; t < 2; ++t) {
                 const int e = t * TC_REC + v, st = e >> 3, kk = e & 7;
-                const bool on = a >= (t == 0 ? ks : mk);
+                const bool on = a % Q.nbd >= (t == 0 ? ks : mk);
                 const float sg = on ? (t == 0 ? 1.f : -1.f) : 0.f, sb = on ? 1.f : 0.f;
                 const float av[2][4] = {{A0r, A0i, A3r, A3i}, {A1r, A1i, AWr, AWi}};
                 const float bv[2][4] = {{B0r, B0i, B2r, B2i}, {B1r, B1i, BWr, BWi}};
@@ -1644,7 +1742,7 @@ __global__ void __launch_bounds__(ZB) k_mp_zscal(ZParams Q, double* spart,
             const unsigned long long n1 = (unsigned long long)h.z;
 #pragma unroll
             for (int j = 0; j < ZE; ++j) {
-                const int m = min(ea[j], eb[j]);
+                const int m = min(ea[j] % Q.nbd, eb[j] % Q.nbd);
                 if (!ev[j] || m < h.x || m >= h.y) continue;
                 const float4 pa = zsh[((size_t)v * nb + ea[j]) * 2];
                 const unsigned long long npa = (unsigned)__float_as_int(pa.x);
@@ -1657,8 +1755,12 @@ __global__ void __launch_bounds__(ZB) k_mp_zscal(ZParams Q, double* spart,
                 } else {
                     const float4 pb = zsh[((size_t)v * nb + eb[j]) * 2];
                     C[j] += n1 * npa * (unsigned long long)(unsigned)__float_as_int(pb.x);
+                    // (ordered = 1's meanlogd3 in the vertex-3 x vertex-2 block takes
+                    // mp3.sumw at the column's bin, as the reference writes it)
+                    const float swl = (Q.typo32 && ea[j] >= Q.nbd)
+                        ? zsh[((size_t)v * nb + eb[j] % Q.nbd + Q.nbd) * 2].y : pa.y;
                     F[j][0] += w1 * pb.y * pa.z; F[j][1] += w1 * pb.y * pa.w;
-                    F[j][2] += w1 * pa.y * pb.z; F[j][3] += w1 * pa.y * pb.w;
+                    F[j][2] += w1 * pa.y * pb.z; F[j][3] += w1 * swl * pb.w;
                 }
             }
         }
@@ -1896,6 +1998,7 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
             Q.rec_floats = recf; Q.nbins = nb; Q.maxn = M; Q.chunk = chunk;
             Q.ngroups = ngroups; Q.part = X.part; Q.Z = Z;
             Q.shift = P.vreal ? 0 : 1;
+            Q.nbd = P.nbd; Q.typo32 = P.typo32;
             if (Q.nrec > 0) {
                 count_launch();
                 if (use_tc) k_mp_zeta_tc<<<dim3(nn, ngroups), TCB, tcsm, st>>>(Q, X.tcstatus);

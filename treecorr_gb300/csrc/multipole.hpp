@@ -28,6 +28,12 @@ struct MPParams {
     int vreal;
     // 1: the pairs are N or K cells whose payload is real (GNN, GKK): no spin-2 rotation.
     int pspin0;
+    // Three-field cross (vertex 1, vertex-2 cells, vertex-3 cells): nbd is the number of
+    // distance bins, nbins = 2 nbd the bins of the scratch and the records (vertex-3 pairs
+    // land in [nbd, 2 nbd)); cells with id >= base3 are vertex-3 cells.  typo32: ordered = 1's
+    // meanlogd3 second term as the reference writes it (mp3.sumw[k3], src/Corr3.cpp:2036).
+    // Without a three-field cross nbd = nbins and three = 0.
+    int three, nbd, base3, typo32;
     double minsep, maxsep, binsize, b, a, logminsep, minsepsq, maxsepsq, bsq, asq, maxbsq_eff;
     // FP32 copies for the FP32 decisions (the FP64 values decide whenever FP32 is too close).
     float f_minsepsq, f_minsep, f_maxsepsq, f_maxsep, f_asq, f_bsq, f_q25, f_logminsep, f_binsize, f_b,
