@@ -260,7 +260,9 @@ def multipole(metric, bins, max_n, f, quick=False, nthreads=0, f2=None, mode=0):
 def multipole3(metric, bins, max_n, f1, f2, f3, ordered, quick=False, nthreads=0, mode=0,
                out=None):
     """The oracle's three-field LogMultipole (vertex 1 from f1, 2 from f2, 3 from f3,
-    ordered 1 or 4), accumulated into out (a dict as multipole returns) when given."""
+    ordered 1 or 4), accumulated into out (a dict as multipole returns) when given.  mode
+    bits: 1 vertex 1, 2 vertex 2, 4 vertex 3 given as a K field whose k is 1 (N) or k (K)
+    (a real payload)."""
     nb = bins["nbins"]
     shape = (nb, nb, 2 * max_n + 1)
     if out is None:

@@ -369,9 +369,6 @@ struct Params {
     // without the +-1 buffer, self-pair sums without z^2 (Corr3::getMP2 buffer 0,
     // src/Corr3.cpp:1307-1313); its "shear" (d1, d2) then holds (w1 or w1 k1, 0).
     int vreal = 0;
-    // 3-point: 1 when vertex 1 is a G field and the pairs N or K fields (GNN, GKK): the pairs'
-    // payload (w or w k) is real and not rotated (MultipoleHelper<4>).
-    int pspin0 = 0;
 };
 
 // MetricHelper<Euclidean>::DistSq (include/Metric.h:143-147, 202-207) and
@@ -625,6 +622,7 @@ struct Out3 {
 // 296-383; Corr3::getMP2, src/Corr3.cpp:1307-1313).
 struct MPS {
     int nbins, maxn;
+    bool real = false;   // the list's cells carry a real payload (N: w, K: w k), not rotated
     std::vector<cd> Wn, Gn, gg0, gg1, gg2;
     std::vector<double> npairs, sumw, sumwr, sumwlogr, sumww, sumwwr, sumwwlogr;
     MPS(int nb, int mn) : nbins(nb), maxn(mn) { clear(); }
@@ -680,7 +678,7 @@ void calculate_gn(const Params& P, const Node& c1, const Node& c2, double r, dou
     mp.sumwwlogr[k] += wsq * logr;
     cd wg(c2.d1, c2.d2);
     cd z = exp_i_phi(P, c1, c2, r);
-    cd e = P.pspin0 ? cd(1., 0.) : project2(P, c1, c2);
+    cd e = mp.real ? cd(1., 0.) : project2(P, c1, c2);
     cd wgsq = c2.sumwzsq;
     wg *= e;
     wgsq *= e * e;
@@ -904,9 +902,11 @@ void calculate_zeta3(const Params& P, const Node& c1, int ordered, const MPS& mp
     const cd wg1(c1.d1, c1.d2);
     const int s = P.vreal ? 0 : 1;
     const bool swap23 = ordered == 1;
-    // GNN / GKK's zeta (MultipoleHelper<4>, src/Corr3.cpp:2532-2572) is written for
-    // ordered = 4 only and has no swapped term; the weights and means still have it.
-    const bool swap_g = swap23 && !(P.pspin0 && !P.vreal);
+    // The zeta of MultipoleHelper<3>, <4> and <6> (a real vertex with one real and one
+    // spin-2 list, a spin-2 vertex with real lists or with one of each; src/Corr3.cpp:
+    // 2418-2446, 2536-2572, 3029-3075) is written for ordered = 4 only and has no swapped
+    // term; the weights and means still have it.
+    const bool swap_g = swap23 && mp2.real == mp3.real && !(mp2.real && !P.vreal);
     auto idx = [&](int a, int b, int n) { return (a * nb + b) * nn + maxn + n; };
     auto Wn = [&](const MPS& m, int k, int n) {
         return n >= 0 ? m.Wn[m.widx(k) + n] : std::conj(m.Wn[m.widx(k) - n]);
@@ -1459,7 +1459,6 @@ static int multipole_run(int metric, int quick, double minsep, double maxsep, in
     if (f1->coords != f2->coords) return 2;
     Params P = make_params(DG * 16 + DG, f1->coords, metric, quick, minsep, maxsep, nbins, binsize, b, a);
     P.vreal = vreal ? 1 : 0;
-    P.pspin0 = pspin0 ? 1 : 0;
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #else
@@ -1474,6 +1473,7 @@ static int multipole_run(int metric, int quick, double minsep, double maxsep, in
     {
         Out3 O(nbins, maxn);
         MPS mp(nbins, maxn);
+        mp.real = pspin0;
 #pragma omp for schedule(dynamic)
         for (long i = 0; i < n1; ++i) multipole_split1(P, *f1, *f2, f1->tops[i], f2->tops, mp, O);
 #pragma omp critical
@@ -1523,17 +1523,18 @@ int orc_corr3_multipole_cross3(int metric, int quick, double minsep, double maxs
     Field* f1 = static_cast<Field*>(h1);
     Field* f2 = static_cast<Field*>(h2);
     Field* f3 = static_cast<Field*>(h3);
-    const bool vreal = mode == 1 || mode == 3, pspin0 = mode == 2 || mode == 3;
+    // mode bit 0: vertex 1 a K field whose k is 1 (N) or k (K); bit 1: the vertex-2 field
+    // such a K field; bit 2: the vertex-3 field.
+    const bool vreal = mode & 1, r2 = (mode >> 1) & 1, r3 = (mode >> 2) & 1;
     const bool v_ok = vreal ? (f1->dtype == DK && f1->spin == 0) : (f1->dtype == DG && f1->spin == 2);
-    auto p_ok = [&](const Field* f) {
-        return pspin0 ? (f->dtype == DK && f->spin == 0) : (f->dtype == DG && f->spin == 2);
+    auto p_ok = [&](const Field* f, bool real) {
+        return real ? (f->dtype == DK && f->spin == 0) : (f->dtype == DG && f->spin == 2);
     };
-    if (!v_ok || !p_ok(f2) || !p_ok(f3)) return 1;
+    if (!v_ok || !p_ok(f2, r2) || !p_ok(f3, r3)) return 1;
     if (f1->coords != f2->coords || f1->coords != f3->coords) return 2;
     if (ordered != 1 && ordered != 4) return 3;
     Params P = make_params(DG * 16 + DG, f1->coords, metric, quick, minsep, maxsep, nbins, binsize, b, a);
     P.vreal = vreal ? 1 : 0;
-    P.pspin0 = pspin0 ? 1 : 0;
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #else
@@ -1549,6 +1550,8 @@ int orc_corr3_multipole_cross3(int metric, int quick, double minsep, double maxs
     {
         Out3 O(nbins, maxn);
         MPS mp2(nbins, maxn), mp3(nbins, maxn);
+        mp2.real = r2;
+        mp3.real = r3;
 #pragma omp for schedule(dynamic)
         for (long i = 0; i < n1; ++i)
             multipole_split1_3(P, *f1, *f2, *f3, f1->tops[i], f2->tops, f3->tops, mp2, mp3,

@@ -345,6 +345,18 @@ if __name__ == "__main__" and "--mp-x12" in sys.argv:
 # processCross (3938-3976), processCross21 (3831-3868) and processCross12 with ordered = 0
 # (3730-3768): name -> (class, catalogs' case, call, ordered).  Catalogs: the case's, seed +
 # 1000 and seed + 2000; a 21 / 12 call takes the first two.
+def zeta_keys(letters):
+    """The zeta arrays of a 3-point class (ZetaData<0..4>, include/Corr3.h:581-720)."""
+    nG = letters.count("G")
+    if nG == 3:
+        return ("gam0r", "gam0i", "gam1r", "gam1i", "gam2r", "gam2i", "gam3r", "gam3i")
+    if letters == "NNN":
+        return ()
+    if nG == 2:
+        return ("gam0r", "gam0i", "gam1r", "gam1i")
+    return ("zeta", "zeta_im")
+
+
 X3_CASES = {
     "ggg_flat_mp_x3o4": ("GGG", "ggg_flat_mp", "cross", 4),
     "ggg_sphere_mp_x3o1": ("GGG", "ggg_sphere_mp", "cross", 1),
@@ -353,6 +365,18 @@ X3_CASES = {
     "nnn_sphere_mp_x12o0": ("NNN", "ggg_sphere_mp", "cross12", 0),
     "ngg_flat_mp_x3o4": ("NGG", "ggg_flat_mp", "cross", 4),
     "gkk_sphere_mp_x3o1": ("GKK", "ggg_sphere_mp", "cross", 1),
+    "nnk_flat_mp_x21o3": ("NNK", "ggg_flat_mp", "cross21", 3),
+    "nkn_sphere_mp_x3o4": ("NKN", "ggg_sphere_mp", "cross", 4),
+    "knk_flat_mp_x3o4": ("KNK", "ggg_flat_mp", "cross", 4),
+    "kkn_sphere_mp_x21o3": ("KKN", "ggg_sphere_mp", "cross21", 3),
+    "nng_flat_mp_x21o3": ("NNG", "ggg_flat_mp", "cross21", 3),
+    "ngn_sphere_mp_x3o4": ("NGN", "ggg_sphere_mp", "cross", 4),
+    "kkg_sphere_mp_x21o3": ("KKG", "ggg_sphere_mp", "cross21", 3),
+    "kgk_flat_mp_x3o4": ("KGK", "ggg_flat_mp", "cross", 4),
+    "gng_flat_mp_x3o4": ("GNG", "ggg_flat_mp", "cross", 4),
+    "ggn_sphere_mp_x21o3": ("GGN", "ggg_sphere_mp", "cross21", 3),
+    "gkg_sphere_mp_x3o4": ("GKG", "ggg_sphere_mp", "cross", 4),
+    "ggk_flat_mp_x21o3": ("GGK", "ggg_flat_mp", "cross21", 3),
 }
 
 if __name__ == "__main__" and "--mp-x3" in sys.argv:
@@ -374,10 +398,7 @@ if __name__ == "__main__" and "--mp-x3" in sys.argv:
         shape = (nb, nb, 2 * mn + 1)
         common = ("meand1", "meanlogd1", "meand2", "meanlogd2", "meand3", "meanlogd3", "meanu",
                   "meanv", "weight", "weight_im", "ntri")
-        zk = (("gam0r", "gam0i", "gam1r", "gam1i", "gam2r", "gam2i", "gam3r", "gam3i")
-              if letters == "GGG" else ("gam0r", "gam0i", "gam1r", "gam1i")
-              if letters[1:] == "GG" else ("zeta", "zeta_im")
-              if ("K" in letters or letters[0] == "G") else ())
+        zk = zeta_keys(letters)
         out = {k: np.zeros(shape) for k in zk + common}
         e = np.array([])
         zeta = [out[k] for k in zk] + [e] * (8 - len(zk))

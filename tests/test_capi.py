@@ -54,5 +54,7 @@ def test_python_mirror_matches_reference_names():
     assert (int(T.Middle), int(T.Median), int(T.Mean), int(T.Random)) == (0, 1, 2, 3)
     assert (int(T.Log), int(T.Linear), int(T.TwoD), int(T.LogRUV), int(T.LogSAS),
             int(T.LogMultipole)) == (0, 1, 2, 3, 4, 5)
-    with pytest.raises(NotImplementedError):
-        T.NNKCorr()
+    # All 21 3-point classes of the reference's module are there.
+    for n in ("NNN", "KKK", "GGG", "NNK", "NKN", "KNN", "NKK", "KNK", "KKN", "NNG", "NGN",
+              "GNN", "NGG", "GNG", "GGN", "KKG", "KGK", "GKK", "KGG", "GKG", "GGK"):
+        assert isinstance(getattr(T, n + "Corr"), type), n

@@ -156,8 +156,9 @@ def _corr3(T, letters, s):
     shape = (nb, nb, 2 * mn + 1)
     common = ("meand1", "meanlogd1", "meand2", "meanlogd2", "meand3", "meanlogd3", "meanu",
               "meanv", "weight", "weight_im", "ntri")
-    zk = (MP_OUT[:8] if letters == "GGG" else MP_OUT[:4] if letters[1:] == "GG"
-          else ("zeta", "zeta_im") if ("K" in letters or letters[0] == "G") else ())
+    nG = letters.count("G")
+    zk = (MP_OUT[:8] if nG == 3 else () if letters == "NNN" else MP_OUT[:4] if nG == 2
+          else ("zeta", "zeta_im"))
     out = {k: np.zeros(shape) for k in zk + common}
     e = np.array([])
     zeta = [out[k] for k in zk] + [e] * (8 - len(zk))
@@ -267,7 +268,11 @@ def _x3_run(T, g, s):
 
 @pytest.mark.parametrize("name", ["ggg_flat_mp_x3o4", "ggg_sphere_mp_x3o1", "ggg_flat_mp_x21o3",
                                   "kkk_flat_mp_x3o0", "nnn_sphere_mp_x12o0", "ngg_flat_mp_x3o4",
-                                  "gkk_sphere_mp_x3o1"])
+                                  "gkk_sphere_mp_x3o1", "nnk_flat_mp_x21o3", "nkn_sphere_mp_x3o4",
+                                  "knk_flat_mp_x3o4", "kkn_sphere_mp_x21o3", "nng_flat_mp_x21o3",
+                                  "ngn_sphere_mp_x3o4", "kkg_sphere_mp_x21o3", "kgk_flat_mp_x3o4",
+                                  "gng_flat_mp_x3o4", "ggn_sphere_mp_x21o3", "gkg_sphere_mp_x3o4",
+                                  "ggk_flat_mp_x21o3"])
 @pytest.mark.parametrize("tensor", ["1", "0"])
 def test_multipole_three_field_golden(gpu_lib, monkeypatch, name, tensor):
     """The three-field multipole (vertex 2's pairs in bins [0, nb), vertex 3's in [nb, 2 nb)

@@ -199,7 +199,10 @@ def test_oracle_multipole_cross12_matches_reference(name):
 
 
 X3 = ["ggg_flat_mp_x3o4", "ggg_sphere_mp_x3o1", "ggg_flat_mp_x21o3", "kkk_flat_mp_x3o0",
-      "nnn_sphere_mp_x12o0", "ngg_flat_mp_x3o4", "gkk_sphere_mp_x3o1"]
+      "nnn_sphere_mp_x12o0", "ngg_flat_mp_x3o4", "gkk_sphere_mp_x3o1", "nnk_flat_mp_x21o3",
+      "nkn_sphere_mp_x3o4", "knk_flat_mp_x3o4", "kkn_sphere_mp_x21o3", "nng_flat_mp_x21o3",
+      "ngn_sphere_mp_x3o4", "kkg_sphere_mp_x21o3", "kgk_flat_mp_x3o4", "gng_flat_mp_x3o4",
+      "ggn_sphere_mp_x21o3", "gkg_sphere_mp_x3o4", "ggk_flat_mp_x21o3"]
 
 
 def x3_fields(O, g, s):
@@ -229,13 +232,13 @@ def x3_fields(O, g, s):
         return [mk(c, "G") for c in cats], 0
     if letters == "NNN":
         return [mk(c, "G0") for c in cats], 0
-    if letters == "KKK":
-        return [mk(c, "K") for c in cats], 3
-    if letters == "NGG":
-        return [mk(cats[0], "K1")] + [mk(c, "G") for c in cats[1:]], 1
-    if letters == "GKK":
-        return [mk(cats[0], "G")] + [mk(c, "K") for c in cats[1:]], 2
-    raise AssertionError(letters)
+    # Every other class: each vertex's field as G (spin 2) or as a K field whose k is 1 (N)
+    # or k (K); mode bit i set where vertex i+1 is real.
+    kinds = {"cross": letters, "cross21": letters[0] + letters[2],
+             "cross12": letters[:2]}[str(g["call"])]
+    fs = [mk(c, "G" if L == "G" else "K" if L == "K" else "K1") for c, L in zip(cats, kinds)]
+    mode = sum(1 << i for i, L in enumerate(letters) if L != "G")
+    return fs, mode
 
 
 def x3_oracle(O, g, s):
@@ -279,15 +282,20 @@ def x3_oracle(O, g, s):
 
 
 def x3_zeta_pairs(letters):
-    """(oracle output, reference output) pairs of the class's zeta arrays."""
-    if letters == "GGG":
+    """(oracle output, reference output) pairs of the class's zeta arrays: GGG's gam0..3;
+    N/K-vertex with two G's (MultipoleHelper<2>): gam0, gam2; G-vertex with one G
+    (MultipoleHelper<6>): gam0, gam1; every class with one or no G: gam0 as zeta."""
+    nG = letters.count("G")
+    if nG == 3:
         return [(k, k) for k in ("gam0r", "gam0i", "gam1r", "gam1i", "gam2r", "gam2i", "gam3r",
                                  "gam3i")]
-    if letters[1:] == "GG":
+    if letters == "NNN":
+        return []
+    if nG == 2 and letters[0] != "G":
         return [("gam0r", "gam0r"), ("gam0i", "gam0i"), ("gam2r", "gam1r"), ("gam2i", "gam1i")]
-    if "K" in letters or letters[0] == "G":
-        return [("gam0r", "zeta"), ("gam0i", "zeta_im")]
-    return []
+    if nG == 2:
+        return [(k, k) for k in ("gam0r", "gam0i", "gam1r", "gam1i")]
+    return [("gam0r", "zeta"), ("gam0i", "zeta_im")]
 
 
 @pytest.mark.parametrize("name", X3)

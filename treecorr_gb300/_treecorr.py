@@ -688,7 +688,8 @@ class GGGCorr(BaseCorr3):
         self._outs = arrs
         h = ctypes.c_void_p()
         d1, d2 = self._dkind, getattr(self, "_dkind2", self._dkind)
-        _check(lib().tc_corr3_create(d1, d2, d2, int(bin_type), float(minsep), float(maxsep),
+        d3 = getattr(self, "_dkind3", d2)
+        _check(lib().tc_corr3_create(d1, d2, d3, int(bin_type), float(minsep), float(maxsep),
                                      int(nbins), float(binsize), float(b), float(a), float(minu),
                                      float(maxu), int(nubins), float(ubinsize), float(bu),
                                      float(minv), float(maxv), int(nvbins), float(vbinsize),
@@ -697,13 +698,6 @@ class GGGCorr(BaseCorr3):
                                      *[_ptr(a_ if a_ is not None and a_.size else None)
                                        for a_ in arrs], ctypes.byref(h)))
         self._h = h
-
-
-def _not_on_path(name):
-    def f(*args, **kwargs):
-        raise NotImplementedError(f"{name} is not on the GPU path")
-    f.__name__ = name
-    return f
 
 
 class NNNCorr(GGGCorr):
@@ -766,9 +760,17 @@ class GKKCorr(GGGCorr):
     _dkind2 = 1
 
 
-# The 3-point classes of src/Corr3.cpp (WrapCorr3) that are not on the GPU path.
+def _corr3_class(name):
+    """The mixed classes whose vertices 2 and 3 differ (WrapCorr3, src/Corr3.cpp:4240-4262):
+    processCross21 / processCross only."""
+    return type(name + "Corr", (GGGCorr,),
+                {"_dkind": _DKIND[name[0]], "_dkind2": _DKIND[name[1]],
+                 "_dkind3": _DKIND[name[2]], "__module__": __name__,
+                 "__doc__": f"{name}Corr (src/Corr3.cpp WrapCorr3) with LogMultipole binning."})
+
+
 for _n in ("NNK", "NKN", "KNK", "KKN", "NNG", "NGN", "GNG", "GGN", "KKG", "KGK", "GKG", "GGK"):
-    globals()[_n + "Corr"] = _not_on_path(_n + "Corr")
+    globals()[_n + "Corr"] = _corr3_class(_n)
 del _n
 
 

@@ -78,7 +78,8 @@ struct tc_field {
 
 struct tc_corr3 {
     int dv = TC_GDATA;           // data kind of vertex 1
-    int dk = TC_GDATA;           // data kind of vertices 2 and 3 (GGG, NNN, KKK, NKK, KNN)
+    int dk = TC_GDATA;           // data kind of vertex 2
+    int dk3 = TC_GDATA;          // data kind of vertex 3
     int bin_type = 0, nbins = 0, maxn = 0;
     double minsep = 0., maxsep = 0., binsize = 0., b = 0., a = 0.;
     double* zeta[8] = {nullptr};
@@ -873,6 +874,24 @@ int ensure_leaf_sums(tc_field* f, cudaStream_t st)
     return 0;
 }
 
+// TripleTraits<D1,D2,D3>::algo (src/Corr3.cpp:1835-1860) for N, K and G vertices.
+int c3_algo(const tc_corr3* c)
+{
+    const bool r2 = c->dk != TC_GDATA, r3 = c->dk3 != TC_GDATA;
+    if (c->dv != TC_GDATA) {
+        if (c->dv == TC_NDATA && c->dk == TC_NDATA && c->dk3 == TC_NDATA) return 0;
+        return r2 && r3 ? 1 : (!r2 && !r3 ? 2 : 3);
+    }
+    return r2 && r3 ? 4 : (!r2 && !r3 ? 5 : 6);
+}
+
+// Zeta arrays written per algorithm (ZetaData<0..4>, include/Corr3.h:581-720).
+int c3_nzeta(int algo)
+{
+    static const int nz[7] = {0, 2, 4, 2, 2, 8, 4};
+    return nz[algo];
+}
+
 // BaseCorr3::multipole with LogMultipole binning: the auto-correlation (f2 == f1, f3 null,
 // src/Corr3.cpp:1124-1175), cross12 (vertex 1 from f1, vertices 2 and 3 from f2,
 // 1177-1237), or the three-field cross (vertex 1 from f1, vertex 2 from f2, vertex 3 from
@@ -881,11 +900,12 @@ int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, tc_field* f3, int ordered
               int metric)
 {
     if (!c || !f1 || !f2) { set_last_error("NULL argument"); return TC_ERR_ARG; }
-    if (f1->dkind != c->dv || f2->dkind != c->dk || (f3 && f3->dkind != c->dk)) {
+    if (f1->dkind != c->dv || f2->dkind != c->dk || (f3 ? f3->dkind != c->dk3 : c->dk3 != c->dk)) {
         static const char L[] = "NKGZVTQ";
-        const char cls[4] = {L[c->dv], L[c->dk], L[c->dk], 0};
-        set_last_error(std::string(cls) + ": the fields have the wrong data kind (vertex 1 " +
-                       L[c->dv] + ", vertices 2 and 3 " + L[c->dk] + ")");
+        const char cls[4] = {L[c->dv], L[c->dk], L[c->dk3], 0};
+        set_last_error(std::string(cls) + ": the fields have the wrong data kind for the vertices" +
+                       (f3 || c->dk3 == c->dk ? "" : " (this class needs processCross21 or "
+                                                     "processCross)"));
         return TC_ERR_ARG;
     }
     if (f1->coords != f2->coords || (f3 && f3->coords != f1->coords)) {
@@ -949,35 +969,41 @@ int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, tc_field* f3, int ordered
     P.three = three ? 1 : 0;
     P.base3 = three ? (int)((2 * f1->n - 1) + (2 * f2->n - 1)) : 0;
     P.typo32 = three && ordered == 1 ? 1 : 0;
-    // The classes other than GGG and NNN run GGG's contraction on real payloads:
-    //  * NGG, KGG (MultipoleHelper<2>, src/Corr3.cpp:2216-2405): an N or K vertex (vreal:
-    //    G_n at n, self-pair sums without z^2), zeta0 / zeta1 = gam0 / gam2;
-    //  * GNN, GKK (MultipoleHelper<4>, 2462-2580): N or K pairs with the real payload w or
-    //    w k, unrotated (pspin0), zeta = gam0;
-    //  * KKK, NKK, KNN (MultipoleHelper<1>, 2108-2214): both, so gam0 = wk1 K_a[n] conj(K_b[n])
-    //    minus wk1 sum (w k)^2 on the diagonal, with K_n = sum (w k or w) z^n: zeta = gam0.
-    // The vertex's payload is (w1 k1 or w1, 0) (getWK) and the pairs' (w k or w, 0); a K
-    // field carries exactly that, an N field's cells get it in the joined copy (a mixed class
-    // always has two fields).
-    const bool nnn = c->dv == TC_NDATA && c->dk == TC_NDATA;
+    // Every class runs GGG's contraction (MultipoleHelper<5>) on the right payloads: a real
+    // vertex (N: w1, K: w1 k1, getWK) takes G_n at n instead of n -+ 1 and self-pair sums
+    // without z^2 (vreal; the scratch has no spin-2 buffer, src/Corr3.cpp:1307-1313); a real
+    // pair list (N: w, K: w k) is not rotated (a pspin0 bit).  Then, with the algorithm
+    // numbers of TripleTraits (1835-1860):
+    //   1 (KKK, NKK, NNK, ...; 2108-2214): gam0 = wk1 K_a[n] K_b[-n] is zeta;
+    //   2 (NGG, KGG; 2216-2405): gam0 and gam2 are zeta0 and zeta1;
+    //   3 (NNG, KGK, ...; 2408-2458): gam0 is zeta;  4 (GNN, GKK; 2462-2580): gam0 is zeta;
+    //   6 (GNG, GGK, ...; 3018-3082): gam0 and gam1 are zeta0 and zeta1.
+    // A K field carries its real payload already; an N field's cells get it in the joined
+    // copy (a class with an N and another kind always has several fields).
+    const bool nnn = c->dv == TC_NDATA && c->dk == TC_NDATA && c->dk3 == TC_NDATA;
     const bool vreal = c->dv != TC_GDATA && !nnn;
-    const bool pspin0 = c->dk != TC_GDATA && !nnn;
-    const bool xg = c->dk == TC_GDATA && c->dv != TC_GDATA;
-    if (cross && (vreal || pspin0)) {
-        const size_t n1c = 2 * (size_t)f1->n - 1, n2c = (size_t)ncap - n1c;
+    const bool l2r = c->dk != TC_GDATA && !nnn, l3r = c->dk3 != TC_GDATA && !nnn;
+    const int algo = c3_algo(c);
+    if (cross && (vreal || l2r || l3r)) {
+        const size_t n1c = 2 * (size_t)f1->n - 1;
+        const size_t n2c = three ? 2 * (size_t)f2->n - 1 : (size_t)ncap - n1c;
         if (vreal) {
             if (c->dv == TC_NDATA)
                 TC_CU(cudaMemcpyAsync(J.cells.d1, J.cells.w, sizeof(float) * n1c,
                                       cudaMemcpyDeviceToDevice, st));
             TC_CU(cudaMemsetAsync(J.cells.d2, 0, sizeof(float) * n1c, st));
         }
-        if (pspin0)
-            TC_TRY(launch_scalar_pairs((int)n2c, c->dk == TC_NDATA ? 1 : 0, J.tc + n1c,
-                                       J.cells.d1 + n1c, J.cells.d2 + n1c, J.ls + 4 * n1c,
-                                       J.lsf + n1c, st));
+        struct { bool real; int is_n; size_t lo, len; } lists[2] = {
+            {l2r, c->dk == TC_NDATA, n1c, n2c},
+            {three && l3r, c->dk3 == TC_NDATA, n1c + n2c, (size_t)ncap - n1c - n2c}};
+        for (const auto& L : lists)
+            if (L.real && L.len > 0)
+                TC_TRY(launch_scalar_pairs((int)L.len, L.is_n ? 1 : 0, J.tc + L.lo,
+                                           J.cells.d1 + L.lo, J.cells.d2 + L.lo,
+                                           J.ls + 4 * L.lo, J.lsf + L.lo, st));
     }
     P.vreal = vreal ? 1 : 0;
-    P.pspin0 = pspin0 ? 1 : 0;
+    P.pspin0 = (l2r ? 1 : 0) | (three && l3r ? 2 : 0);
     P.ncells = (int)ncap;
     const int nn = 2 * c->maxn + 1;
     const size_t Z = (size_t)nb * nb * nn, Zv = (size_t)nbv * nbv * nn;
@@ -998,9 +1024,9 @@ int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, tc_field* f3, int ordered
         // calculateZeta(c1, ordered, mp2, mp3, ...), src/Corr3.cpp:1976-2087: entry (k2, k3)
         // is the vertex-3 x vertex-2 block (mp3 at k2, mp2 at k3); ordered = 1 adds the
         // vertex-2 x vertex-3 block (cats 2 and 3 swapped).
-        // GNN / GKK's zeta (MultipoleHelper<4>, 2532-2572) is written for ordered = 4 only:
-        // it has no swapped term, while their weights and means do.
-        const bool gx = c->dv == TC_GDATA && c->dk != TC_GDATA;
+        // The zeta of algorithms 3, 4 and 6 (MultipoleHelper<3>, <4>, <6>) is written for
+        // ordered = 4 only: it has no swapped term, while their weights and means do.
+        const bool gx = algo == 3 || algo == 4 || algo == 6;
         std::vector<double> hz(15 * Z);
         for (int q = 0; q < 15; ++q)
             for (int k2 = 0; k2 < nb; ++k2)
@@ -1018,9 +1044,9 @@ int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, tc_field* f3, int ordered
     // of gam0..3; NGG / KGG gam0 and gam2 as their zeta0 (gam0) and zeta1 (gam1); the real
     // classes gam0 as zeta (real, imaginary); NNN nothing.
     const int zmap[8] = {0, 1, 2, 3, 4, 5, 6, 7}, xgmap[4] = {0, 1, 4, 5};
-    const int nz = (c->dv == TC_GDATA && c->dk == TC_GDATA) ? 8 : xg ? 4 : pspin0 ? 2 : 0;
+    const int nz = c3_nzeta(algo);
     for (int q = 0; q < nz; ++q) {
-        const int src = xg ? xgmap[q] : zmap[q];
+        const int src = algo == 2 ? xgmap[q] : zmap[q];
         if (c->zeta[q]) for (size_t i = 0; i < Z; ++i) c->zeta[q][i] += h[src * Z + i];
     }
     double* dst[7] = {c->meand2, c->meanlogd2, c->meand3, c->meanlogd3, c->weight, c->weight_im,
@@ -1759,18 +1785,12 @@ int tc_corr3_create(int d1, int d2, int d3, int bin_type, double minsep, double 
     (void)vbinsize; (void)bv; (void)meand1; (void)meanlogd1; (void)meanu; (void)meanv;
     if (!out) { set_last_error("out is NULL"); return TC_ERR_ARG; }
     *out = nullptr;
-    // GGG; NNN: its weight, ntri and mean distances are the multipole's own sums, which do
-    // not depend on the payload (an N field carries none); KKK, NKK, KNN: zeta is the weight
-    // contraction over the weights w k of the K vertices (a second pass on the same tree).
-    // NGG, KGG: GGG's contraction with a real vertex weight and G_n taken at n (no +-1).
-    const bool same = d1 == d2 && (d1 == TC_GDATA || d1 == TC_NDATA || d1 == TC_KDATA);
-    const bool nk = (d1 == TC_NDATA && d2 == TC_KDATA) || (d1 == TC_KDATA && d2 == TC_NDATA);
-    const bool xg = (d1 == TC_NDATA || d1 == TC_KDATA) && d2 == TC_GDATA;
-    // GNN, GKK: GGG's gam0 with the pairs' real payload (w or w k) unrotated.
-    const bool gx = d1 == TC_GDATA && (d2 == TC_NDATA || d2 == TC_KDATA);
-    if (d2 != d3 || !(same || nk || xg || gx)) {
-        set_last_error("only GGG, NNN, KKK, NKK, KNN, NGG, KGG, GNN and GKK are on the GPU "
-                       "3-point path");
+    // The 21 classes of WrapCorr3 (src/Corr3.cpp:4233-4262): N, K or G at each vertex, not
+    // all three different.
+    auto nkg = [](int d) { return d == TC_NDATA || d == TC_KDATA || d == TC_GDATA; };
+    if (!nkg(d1) || !nkg(d2) || !nkg(d3) || (d1 != d2 && d2 != d3 && d1 != d3)) {
+        set_last_error("the GPU 3-point path has the N, K and G classes of the reference "
+                       "(GGG, NNN, KKK, NKK, NNG, GKG, ...)");
         return TC_ERR_UNSUPPORTED;
     }
     if (bin_type != TC_LOGMULTIPOLE) {
@@ -1786,23 +1806,24 @@ int tc_corr3_create(int d1, int d2, int d3, int bin_type, double minsep, double 
         set_last_error("invalid binning");
         return TC_ERR_ARG;
     }
-    const bool needz = (d1 == TC_GDATA && d2 == TC_GDATA);
-    if ((needz && (!zeta0 || !zeta1 || !zeta2 || !zeta3 || !zeta4 || !zeta5 || !zeta6 || !zeta7)) ||
-        (xg && (!zeta0 || !zeta1 || !zeta2 || !zeta3)) ||
-        ((d1 == TC_KDATA || d2 == TC_KDATA || gx) && (!zeta0 || !zeta1)) ||
-        !meand2 || !meanlogd2 || !meand3 || !meanlogd3 || !weight || !weight_im || !ntri) {
+    tc_corr3 probe;
+    probe.dv = d1; probe.dk = d2; probe.dk3 = d3;
+    const int nz = c3_nzeta(c3_algo(&probe));
+    double* z[8] = {zeta0, zeta1, zeta2, zeta3, zeta4, zeta5, zeta6, zeta7};
+    bool have = true;
+    for (int q = 0; q < nz; ++q) have = have && z[q];
+    if (!have || !meand2 || !meanlogd2 || !meand3 || !meanlogd3 || !weight || !weight_im ||
+        !ntri) {
         set_last_error("missing output array");
         return TC_ERR_ARG;
     }
     tc_corr3* c = new tc_corr3();
     c->dv = d1;
     c->dk = d2;
+    c->dk3 = d3;
     c->bin_type = bin_type; c->nbins = nbins; c->maxn = nubins;
     c->minsep = minsep; c->maxsep = maxsep; c->binsize = binsize; c->b = b; c->a = a;
-    double* z[8] = {zeta0, zeta1, zeta2, zeta3, zeta4, zeta5, zeta6, zeta7};
-    const bool kz = ((d1 == TC_KDATA || d2 == TC_KDATA) && !xg) || gx;
-    for (int q = 0; q < 8; ++q)
-        c->zeta[q] = (needz || (kz && q < 2) || (xg && q < 4)) ? z[q] : nullptr;
+    for (int q = 0; q < 8; ++q) c->zeta[q] = q < nz ? z[q] : nullptr;
     c->meand2 = meand2; c->meanlogd2 = meanlogd2; c->meand3 = meand3; c->meanlogd3 = meanlogd3;
     c->weight = weight; c->weight_im = weight_im; c->ntri = ntri;
     *out = c;

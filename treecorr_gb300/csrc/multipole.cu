@@ -1185,8 +1185,9 @@ __global__ void __launch_bounds__(MB, 2) k_mp_finish(MPParams P)
                             float nn2 = dxf * dxf + dyf * dyf;
                             if (!(nn2 > 0.f)) nn2 = 1.f;
                             // (no rotation for the real payload of N / K pairs)
-                            const float er = P.pspin0 ? 1.f : (dxf * dxf - dyf * dyf) / nn2;
-                            const float ei = P.pspin0 ? 0.f : -(2.f * dxf * dyf) / nn2;
+                            const bool rl = (P.pspin0 >> (is3 ? 1 : 0)) & 1;
+                            const float er = rl ? 1.f : (dxf * dxf - dyf * dyf) / nn2;
+                            const float ei = rl ? 0.f : -(2.f * dxf * dyf) / nn2;
                             const float w2 = tb.w;
                             const float4 lf = __ldg(P.lsf + ca);
                             const float l0 = lf.x, l1 = lf.y, l2 = lf.z, l3 = lf.w;
@@ -1214,7 +1215,7 @@ __global__ void __launch_bounds__(MB, 2) k_mp_finish(MPParams P)
                             if (dec32) { racc = r32; lracc = lr32; }
                             C2 z, e;
                             phases(P, c1, ca, racc, z, e);
-                            if (P.pspin0) e = C2{1., 0.};
+                            if ((P.pspin0 >> (is3 ? 1 : 0)) & 1) e = C2{1., 0.};
                             const double w2 = P.w[ca];
                             const double* ls = P.ls + 4 * (size_t)ca;
                             const C2 wg = cmul({(double)P.d1[ca], (double)P.d2[ca]}, e);

@@ -26,7 +26,8 @@ struct MPParams {
     // 0: a spin-2 vertex (GGG: G_n up to n = max_n + 1, self-pair sums with z^2); 1: an N or
     // K vertex with G pairs (NGG, KGG: the record's vertex payload is (w1 or w1 k1, 0)).
     int vreal;
-    // 1: the pairs are N or K cells whose payload is real (GNN, GKK): no spin-2 rotation.
+    // Bit 0: the vertex-2 (or only) pair list holds N or K cells whose payload is real (w or
+    // w k): no spin-2 rotation; bit 1: the same for the vertex-3 list of a three-field cross.
     int pspin0;
     // Three-field cross (vertex 1, vertex-2 cells, vertex-3 cells): nbd is the number of
     // distance bins, nbins = 2 nbd the bins of the scratch and the records (vertex-3 pairs
