@@ -217,13 +217,14 @@ int tc_corr2_trivially_zero(tc_corr2* c, int metric, int coords,
 int tc_corr2_stats(const tc_corr2* c, tc_stats* out);
 
 /* 3-point correlation with LogMultipole binning: replaces BuildCorr3
- * (src/Corr3.cpp:3599-3645) for the GGG, NNN and KKK classes (d1 = d2 = d3) and the mixed
- * NKK, KNN, NGG, KGG, GNN, GKK (d2 = d3 != d1, cross12 only; pybind11 at
- * src/Corr3.cpp:4207-4261).  Arguments as the reference's (nubins = max_n; the u/v
+ * (src/Corr3.cpp:3599-3645) for the 21 classes of the reference's module: N, K or G
+ * (TC_NDATA, TC_KDATA, TC_GDATA) at each vertex, not all three different (pybind11 at
+ * src/Corr3.cpp:4207-4262).  Arguments as the reference's (nubins = max_n; the u/v
  * arguments are unused by LogMultipole).  Every output has nbins*nbins*(2*max_n+1)
- * entries; zeta0..zeta7 are gam0r, gam0i, gam1r, gam1i, gam2r, gam2i, gam3r, gam3i for GGG,
- * gam0r, gam0i, gam1r, gam1i in zeta0..3 for NGG / KGG, zeta (real, imaginary) in zeta0,
- * zeta1 for KKK, NKK, KNN, GNN, GKK, unused for NNN.  meand1, meanlogd1, meanu and meanv are accepted
+ * entries; the zeta arrays are those of the class's ZetaData (include/Corr3.h:581-720):
+ * gam0r..gam3i in zeta0..7 with three G's, gam0r, gam0i, gam1r, gam1i in zeta0..3 with two,
+ * zeta (real, imaginary) in zeta0, zeta1 with one or none, unused for NNN.  A class whose
+ * vertices 2 and 3 differ runs through tc_corr3_process_cross21 / _cross only. */  meand1, meanlogd1, meanu and meanv are accepted
  * and left untouched, as the reference's multipole code leaves them. */
 int tc_corr3_create(int d1, int d2, int d3, int bin_type, double minsep, double maxsep,
                     int nbins, double binsize, double b, double a, double minu, double maxu,
