@@ -666,7 +666,8 @@ def run_classes(args, rank, world):
     """The widened classes, one timed call each after a warm-up: 2-point NN and KK auto on
     the curved-sky catalog, NG and KG cross (its first half as the N / K field, the second
     half as the G field); 3-point LogMultipole cross12 GGG, NGG, GNN and NKK (1M vertex
-    points, 1M pair points, the multipole configuration's density and binning).  Each class
+    points, 1M pair points), NNG cross21 (ordered 3) and GGG three-field cross (ordered 4)
+    on 1M-point catalogs of the multipole configuration's density and binning.  Each class
     is reported with its GPU rate and the oracle port's rate on a bounded sample."""
     import torch
     from treecorr_gb300 import _treecorr as T
@@ -735,8 +736,9 @@ def run_classes(args, rank, world):
         cp = ggg_catalog(n3, args.seed + 12 + rank, side=side)
         for c3 in (cv, cp):
             c3["k"] = np.random.default_rng(args.seed + 13).normal(0, 0.02, n3)
-        for cls in ("GGG", "NGG", "GNN", "NKK"):
-            zk = {"GGG": 8, "NGG": 4}.get(cls, 2)
+        cw = ggg_catalog(n3, args.seed + 14 + rank, side=side)
+        for cls in ("GGG", "NGG", "GNN", "NKK", "NNG_x21", "GGG_x3"):
+            zk = {"GGG": 8, "NGG": 4, "GGG_x3": 8}.get(cls, 2)
 
             def step3():
                 keys = [f"z{q}" for q in range(zk)] + [
@@ -744,7 +746,7 @@ def run_classes(args, rank, world):
                     "meanu", "meanv", "weight", "weight_im", "ntri"]
                 out = {k: np.zeros(shape) for k in keys}
                 zeta = [out[f"z{q}"] for q in range(zk)] + [e] * (8 - zk)
-                c = getattr(T, cls + "Corr")(
+                c = getattr(T, cls[:3] + "Corr")(
                     T.LogMultipole, B["min_sep"], B["max_sep"], mb, B["bin_size"], B["b"],
                     B["a"], 0., 0., mn, 0., 0., 0., 0., 0, 0., 0., -sys.float_info.max,
                     sys.float_info.max, 0., 0., 0., *zeta, *[out[k] for k in keys[zk:]])
@@ -754,12 +756,19 @@ def run_classes(args, rank, world):
                     return getattr(T, L + "FieldFlat")(c3["x"], c3["y"], e, *pay, c3["w"], e,
                                                        B["min_size"], B["max_size"], T.Mean,
                                                        0, False, 3, 10)
-                c.processCross12(fl(cls[0], cv), fl(cls[1], cp), 1, False, False, T.Euclidean)
+                if cls == "NNG_x21":       # vertices 1 and 2 from the N catalog, 3 from G
+                    c.processCross21(fl("N", cv), fl("G", cp), 3, False, False, T.Euclidean)
+                elif cls == "GGG_x3":      # one vertex from each of three catalogs
+                    c.processCross(fl("G", cv), fl("G", cp), fl("G", cw), 4, False, False,
+                                   T.Euclidean)
+                else:
+                    c.processCross12(fl(cls[0], cv), fl(cls[1], cp), 1, False, False,
+                                     T.Euclidean)
                 return float(out["ntri"].sum())
             ms, ntri = timed(step3)
-            res[cls + "_x12"] = {"gpu_ms": ms, "triangles": ntri,
-                                 "gpu_rate": world * ntri / (ms / 1e3), "unit": "triangles/s",
-                                 "n": [n3, n3]}
+            key = cls if "_" in cls else cls + "_x12"
+            res[key] = {"gpu_ms": ms, "triangles": ntri, "gpu_rate": world * ntri / (ms / 1e3),
+                        "unit": "triangles/s", "n": [n3] * (3 if cls == "GGG_x3" else 2)}
     launches = T.launch_count() - launches0
     if rank == 0 and not args.no_cpu_baseline:
         # 2-point: auto classes over top-level rows of the same catalog, cross classes on
@@ -805,7 +814,8 @@ def run_classes(args, rank, world):
         for c3 in (sv, sp):
             c3["k"] = np.random.default_rng(args.seed + 23).normal(0, 0.02, ms_)
         B = ggg_bins()
-        for cls in ("GGG", "NGG", "GNN", "NKK"):
+        sw = ggg_catalog(ms_, args.seed + 24, side=side_s)
+        for cls in ("GGG", "NGG", "GNN", "NKK", "NNG_x21", "GGG_x3"):
             def of(L, c3, as_k):
                 if as_k:    # the oracle's real-payload fields (NGG vertex / GNN pairs)
                     kv = c3["k"] if L == "K" else np.ones(len(c3["x"]))
@@ -815,15 +825,29 @@ def run_classes(args, rank, world):
                 g1, g2 = (c3["g1"], c3["g2"]) if L == "G" else (0 * c3["w"], 0 * c3["w"])
                 return O.OracleField("G", "flat", c3["x"], c3["y"], None, g1, g2, c3["w"],
                                      None, B["min_size"], B["max_size"], "mean", False, 3, 10)
-            mode = 1 if cls == "NGG" else 2 if cls == "GNN" else 0
-            f1 = of(cls[0], sv, mode == 1)
-            f2 = of(cls[1], sp, mode == 2)
-            f1.ntop(); f2.ntop()
-            t0 = time.perf_counter()
-            o = O.multipole("Euclidean", B, B["max_n"], f1, nthreads=nthreads, f2=f2, mode=mode)
+            key = cls if "_" in cls else cls + "_x12"
+            if cls == "NNG_x21":
+                fn, fg = of("N", sv, True), of("G", sp, False)
+                fn.ntop(); fg.ntop()
+                t0 = time.perf_counter()
+                o = O.multipole3("Euclidean", B, B["max_n"], fn, fn, fg, 4, nthreads=nthreads,
+                                 mode=3)
+            elif cls == "GGG_x3":
+                fa, fb, fc = of("G", sv, False), of("G", sp, False), of("G", sw, False)
+                fa.ntop(); fb.ntop(); fc.ntop()
+                t0 = time.perf_counter()
+                o = O.multipole3("Euclidean", B, B["max_n"], fa, fb, fc, 4, nthreads=nthreads)
+            else:
+                mode = 1 if cls == "NGG" else 2 if cls == "GNN" else 0
+                f1 = of(cls[0], sv, mode == 1)
+                f2 = of(cls[1], sp, mode == 2)
+                f1.ntop(); f2.ntop()
+                t0 = time.perf_counter()
+                o = O.multipole("Euclidean", B, B["max_n"], f1, nthreads=nthreads, f2=f2,
+                                mode=mode)
             spent = time.perf_counter() - t0
-            res[cls + "_x12"]["cpu_rate"] = float(o["ntri"].sum()) / spent
-            res[cls + "_x12"]["cpu_sample"] = f"{ms_} + {ms_} points, same density ({spent:.1f} s)"
+            res[key]["cpu_rate"] = float(o["ntri"].sum()) / spent
+            res[key]["cpu_sample"] = f"{ms_}-point catalogs, same density ({spent:.1f} s)"
     ng = res["NG"]
     line = {
         "metric": "per-class throughput of the widened classes (value: NG cross pair-evals/s)",
@@ -833,8 +857,9 @@ def run_classes(args, rank, world):
         "data": "synthetic (seeded curved-sky catalog; seeded flat catalogs)",
         "config": {"workload": "classes: NN, KK auto and NG, KG cross on the 10M-point cap "
                                "(Arc, 30 Log bins 1-300', bin_slop 0.1); GGG, NGG, GNN, NKK "
-                               "LogMultipole cross12, 1M + 1M flat points (20 bins 1-50', "
-                               "max_n 30)", "n": args.n, "parallelism": f"replicas{world}",
+                               "LogMultipole cross12, NNG cross21 and GGG three-field cross, "
+                               "1M-point flat catalogs (20 bins 1-50', max_n 30)",
+                   "n": args.n, "parallelism": f"replicas{world}",
                    "l2": "inputs larger than L2; no flush"},
         "gpu_launches": launches,
         "clocks": clk.summary(),
