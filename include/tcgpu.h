@@ -224,8 +224,9 @@ int tc_corr2_stats(const tc_corr2* c, tc_stats* out);
  * entries; the zeta arrays are those of the class's ZetaData (include/Corr3.h:581-720):
  * gam0r..gam3i in zeta0..7 with three G's, gam0r, gam0i, gam1r, gam1i in zeta0..3 with two,
  * zeta (real, imaginary) in zeta0, zeta1 with one or none, unused for NNN.  A class whose
- * vertices 2 and 3 differ runs through tc_corr3_process_cross21 / _cross only. */  meand1, meanlogd1, meanu and meanv are accepted
- * and left untouched, as the reference's multipole code leaves them. */
+ * vertices 2 and 3 differ runs through tc_corr3_process_cross21 / _cross only.
+ * meand1, meanlogd1, meanu and meanv are accepted and left untouched, as the reference's
+ * multipole code leaves them. */
 int tc_corr3_create(int d1, int d2, int d3, int bin_type, double minsep, double maxsep,
                     int nbins, double binsize, double b, double a, double minu, double maxu,
                     int nubins, double ubinsize, double bu, double minv, double maxv,
