@@ -304,3 +304,37 @@ def test_multipole_three_field_inplace(gpu_lib, monkeypatch):
         r = g["ref_" + k]
         err = np.abs(out[k] - r).max() / max(np.abs(r).max(), 1e-300)
         assert err <= TOL, f"{k}: {err:.3e}"
+
+
+def test_multipole_three_field_many_bins(gpu_lib):
+    """NNG through processCross21 (ordered 3) with 20 bins (40 scratch bins: the CUDA-core
+    contraction and the larger shared-memory tiles) against the oracle on the same points."""
+    from oracle import oracle as O
+    T = gpu_lib
+    rng = np.random.default_rng(515)
+    n, side = 1500, 60.0
+    cn = {"x": rng.uniform(0, side, n), "y": rng.uniform(0, side, n), "w": rng.uniform(0.5, 1.5, n)}
+    cg = {"x": rng.uniform(0, side, n), "y": rng.uniform(0, side, n), "w": rng.uniform(0.5, 1.5, n),
+          "g1": rng.normal(0, 0.2, n), "g2": rng.normal(0, 0.2, n)}
+    lo, hi, nb, mn = 1.0, 20.0, 20, 8
+    bs = np.log(hi / lo) / nb
+    s = dict(coords="flat", metric="Euclidean", min_sep=lo, max_sep=hi, nbins=nb, max_n=mn,
+             bin_size=bs, b=min(bs, 0.1), a=np.pi / (2 * mn + 1))
+    b1 = min(s["a"], s["b"])
+    mins, maxs = 2 * lo * b1 / (2 + 3 * b1), hi * b1
+    corr, out, zk = _corr3(T, "NNG", s)
+    fN = H.gpu_field(T, "N", "flat", dict(cn, z=None), mins, maxs)
+    fG = H.gpu_field(T, "G", "flat", dict(cg, z=None), mins, maxs)
+    corr.processCross21(fN, fG, 3, False, False, T.Euclidean)
+    args = (mins, maxs, "mean", False, 3, 10)
+    on = O.OracleField("K", "flat", cn["x"], cn["y"], None, np.ones(n), None, cn["w"], None, *args)
+    og = O.OracleField("G", "flat", cg["x"], cg["y"], None, cg["g1"], cg["g2"], cg["w"], None,
+                       *args)
+    bins = dict(min_sep=lo, max_sep=hi, nbins=nb, bin_size=bs, b=s["b"], a=s["a"])
+    ref = O.multipole3("Euclidean", bins, mn, on, on, og, 4, nthreads=0, mode=3)
+    assert np.array_equal(out["ntri"], ref["ntri"])
+    assert out["ntri"].sum() > 0
+    for mine, r in (("zeta", "gam0r"), ("zeta_im", "gam0i"), ("weight", "weight"),
+                    ("meand2", "meand2"), ("meanlogd3", "meanlogd3")):
+        err = np.abs(out[mine] - ref[r]).max() / max(np.abs(ref[r]).max(), 1e-300)
+        assert err <= TOL, f"{mine}: {err:.3e}"

@@ -1861,6 +1861,8 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
     // Scalar outputs: records per chunk and record groups.
     const int chunk2 = (int)std::max<long long>(1, std::min<long long>(64, (48 * 1024) / (32LL * nb)));
     const size_t zsh2 = (size_t)chunk2 * nb * 32;
+    // (with its static header array this can pass the 48 KB that needs no opt-in)
+    TC_CU(cudaFuncSetAttribute(k_mp_zscal, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zsh2));
     const int nsg = std::max(1, 2 * nsm / etiles);
     const int recf = mp_rec_floats(nb, M);
     const long long acc_cap = 4096;
