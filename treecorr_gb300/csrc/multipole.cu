@@ -939,6 +939,9 @@ __device__ void zeta_emit(const MPParams& P, int c1, const double* S, int ks, in
     __syncthreads();
 }
 
+// THREE: a three-field cross (two pair lists); compiled apart so that the auto and cross12
+// paths carry none of its registers.
+template <bool THREE>
 __global__ void __launch_bounds__(MB, 2) k_mp_finish(MPParams P)
 {
     extern __shared__ __align__(16) double mp_sh[];
@@ -1066,7 +1069,7 @@ __global__ void __launch_bounds__(MB, 2) k_mp_finish(MPParams P)
                     const int c2 = j < cur.len ? __ldcg(list ? list + j : list2 + j) : 0;
                     // A vertex-3 cell of a three-field cross: its own threshold, maximum and
                     // bins [nbd, 2 nbd).
-                    const bool is3 = P.three && c2 >= P.base3;
+                    const bool is3 = THREE && c2 >= P.base3;
                     const double thresh1 = is3 ? thresh1_3 : thresh1_2;
                     const float thresh1f = is3 ? thresh1f_3 : thresh1f_2;
                     bool dec32 = false;          // decided (and recorded) in FP32
@@ -1152,7 +1155,7 @@ __global__ void __launch_bounds__(MB, 2) k_mp_finish(MPParams P)
                     // running FP32 maximum, and the entries within the FP32 error of the larger
                     // one get their FP64 value; all other entries are below an evaluated one.
                     // (per list for a three-field cross)
-                    for (int li = 0; li < (P.three ? 2 : 1); ++li) {
+                    for (int li = 0; li < (THREE ? 2 : 1); ++li) {
                         const float rsl = (li == 1) == is3 ? rs32 : 0.f;
                         float& runl = li ? run32_3 : run32;
                         float wm = rsl;
@@ -1387,7 +1390,7 @@ __global__ void __launch_bounds__(ZB) k_mp_zeta(ZParams Q)
     const int n = (int)blockIdx.x - M;
     const int g = blockIdx.y;
     const int tid = threadIdx.x;
-    int ea[ZE], eb[ZE];
+    int ea[ZE], eb[ZE], em[ZE];     // entry (a, b) and min(a, b) mod nbd (the row mask)
     bool ev[ZE];
 #pragma unroll
     for (int j = 0; j < ZE; ++j) {
@@ -1395,6 +1398,7 @@ __global__ void __launch_bounds__(ZB) k_mp_zeta(ZParams Q)
         ev[j] = e < nb * nb;
         ea[j] = ev[j] ? e / nb : 0;
         eb[j] = ev[j] ? e % nb : 0;
+        em[j] = min(ea[j] % Q.nbd, eb[j] % Q.nbd);
     }
     // Sums: FP32 per chunk (F), FP32 over up to 16 chunks (F2), then FP64 (D) -- FP64 work is
     // kept rare (GB300 runs FP64 at 1/64 of the FP32 rate).
@@ -1444,7 +1448,7 @@ __global__ void __launch_bounds__(ZB) k_mp_zeta(ZParams Q)
             const int2 rw = rows_sh[v];
 #pragma unroll
             for (int j = 0; j < ZE; ++j) {
-                const int m = min(ea[j] % Q.nbd, eb[j] % Q.nbd);
+                const int m = em[j];
                 if (!ev[j] || m < rw.x || m >= rw.y) continue;
                 const float4* pa = zsh + ((size_t)v * nb + ea[j]) * 4;
                 const float4* pb = zsh + ((size_t)v * nb + eb[j]) * 4;
@@ -1619,6 +1623,7 @@ __global__ void __launch_bounds__(TCB) k_mp_zeta_tc(ZParams Q, int* status)
             float A0r = 0.f, A0i = 0.f, A1r = 0.f, A1i = 0.f, A3r = 0.f, A3i = 0.f, AWr = 0.f, AWi = 0.f;
             float B0r = 0.f, B0i = 0.f, B1r = 0.f, B1i = 0.f, B2r = 0.f, B2i = 0.f, BWr = 0.f, BWi = 0.f;
             int ks = nb, mk = nb;
+            const int am = a % Q.nbd;    // the row mask's bin
             const int km = __float_as_int(ih[j].w);
             if (km >= 0) {
                 const float w1 = ih[j].x, wr = ih[j].y, wi = ih[j].z;
@@ -1636,7 +1641,7 @@ __global__ void __launch_bounds__(TCB) k_mp_zeta_tc(ZParams Q, int* status)
 #pragma unroll
             for (int t = 0; t < 2; ++t) {
                 const int e = t * TC_REC + v, st = e >> 3, kk = e & 7;
-                const bool on = a % Q.nbd >= (t == 0 ? ks : mk);
+                const bool on = am >= (t == 0 ? ks : mk);
                 const float sg = on ? (t == 0 ? 1.f : -1.f) : 0.f, sb = on ? 1.f : 0.f;
                 const float av[2][4] = {{A0r, A0i, A3r, A3i}, {A1r, A1i, AWr, AWi}};
                 const float bv[2][4] = {{B0r, B0i, B2r, B2i}, {B1r, B1i, BWr, BWi}};
@@ -1703,7 +1708,7 @@ __global__ void __launch_bounds__(ZB) k_mp_zscal(ZParams Q, double* spart,
     const int nb = Q.nbins, M = Q.maxn, gst = 2 * M + 3;
     const int nb2 = nb * nb;
     const int g = blockIdx.x, tid = threadIdx.x;
-    int ea[ZE], eb[ZE];
+    int ea[ZE], eb[ZE], em[ZE];     // entry (a, b) and min(a, b) mod nbd (the row mask)
     bool ev[ZE];
 #pragma unroll
     for (int j = 0; j < ZE; ++j) {
@@ -1711,6 +1716,7 @@ __global__ void __launch_bounds__(ZB) k_mp_zscal(ZParams Q, double* spart,
         ev[j] = e < nb2;
         ea[j] = ev[j] ? e / nb : 0;
         eb[j] = ev[j] ? e % nb : 0;
+        em[j] = min(ea[j] % Q.nbd, eb[j] % Q.nbd);
     }
     double D[ZE][4];
     unsigned long long C[ZE];
@@ -1743,7 +1749,7 @@ __global__ void __launch_bounds__(ZB) k_mp_zscal(ZParams Q, double* spart,
             const unsigned long long n1 = (unsigned long long)h.z;
 #pragma unroll
             for (int j = 0; j < ZE; ++j) {
-                const int m = min(ea[j] % Q.nbd, eb[j] % Q.nbd);
+                const int m = em[j];
                 if (!ev[j] || m < h.x || m >= h.y) continue;
                 const float4 pa = zsh[((size_t)v * nb + ea[j]) * 2];
                 const unsigned long long npa = (unsigned)__float_as_int(pa.x);
@@ -1837,9 +1843,10 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
                        "nbins * max_n within its shared-memory staging");
         return 3;
     }
-    TC_CU(cudaFuncSetAttribute(k_mp_finish, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shbytes));
+    auto* kfin = P.three ? k_mp_finish<true> : k_mp_finish<false>;
+    TC_CU(cudaFuncSetAttribute(kfin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shbytes));
     int per = 0;
-    TC_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_mp_finish, MB, shbytes));
+    TC_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kfin, MB, shbytes));
     if (per < 1) per = 1;
     const int nblk = nsm * std::min(per, 2);
     P.slot_doubles = (long long)mp_slot_doubles(nb, M);
@@ -1989,7 +1996,7 @@ int run_multipole(MPParams& P, MPScratch& X, int ntop, cudaStream_t st, double* 
         for (int wave = 0; e == 0; ++wave) {
             TC_CU(cudaMemsetAsync(X.ctl + 2, 0, sizeof(unsigned long long), st));
             count_launch();
-            k_mp_finish<<<nblk, MB, shbytes, st>>>(P);
+            kfin<<<nblk, MB, shbytes, st>>>(P);
             TC_CU(cudaGetLastError());
             unsigned long long c[4] = {0, 0, 0, 0};
             TC_CU(cudaMemcpyAsync(c, X.ctl, sizeof(c), cudaMemcpyDeviceToHost, st));
