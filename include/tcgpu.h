@@ -262,7 +262,8 @@ int tc_corr3_process_cross21(tc_corr3* c, tc_field* f1, tc_field* f2, int ordere
 int tc_corr3_process_cross(tc_corr3* c, tc_field* f1, tc_field* f2, tc_field* f3,
                            int ordered, int dots, int quick, int metric);
 
-/* Device time of the last tc_corr3_process_auto call in ms (no reference counterpart). */
+/* Device time of the last tc_corr3_process_* call in ms, summed over its multipoles (no
+ * reference counterpart). */
 double tc_corr3_last_ms(const tc_corr3* c);
 
 /* Counters of the last tc_corr3_process_auto call (no reference counterpart):

@@ -1018,7 +1018,7 @@ int corr3_run(tc_corr3* c, tc_field* f1, tc_field* f2, tc_field* f3, int ordered
     float ms = 0.f;
     cudaEventElapsedTime(&ms, e0, e1);
     cudaEventDestroy(e0); cudaEventDestroy(e1);
-    c->ms = ms;
+    c->ms += ms;   // summed over the multipoles of one process call (reset by the caller)
     if (rc) return rc == 3 ? TC_ERR_UNSUPPORTED : (rc == 5 ? TC_ERR_NOMEM : TC_ERR_DEVICE);
     if (three) {
         // calculateZeta(c1, ordered, mp2, mp3, ...), src/Corr3.cpp:1976-2087: entry (k2, k3)
@@ -1840,6 +1840,7 @@ void tc_corr3_free(tc_corr3* c)
 int tc_corr3_process_auto(tc_corr3* c, tc_field* f, int dots, int quick, int metric)
 {
     (void)dots;
+    if (c) c->ms = 0.;
     return corr3_run(c, f, f, nullptr, 1, quick, metric);
 }
 
@@ -1847,6 +1848,7 @@ int tc_corr3_process_cross12(tc_corr3* c, tc_field* f1, tc_field* f2, int ordere
                              int quick, int metric)
 {
     (void)dots;
+    if (c) c->ms = 0.;
     // ProcessCross12c, src/Corr3.cpp:3730-3768.
     if (ordered == 0) TC_TRY(corr3_run(c, f2, f1, f2, 1, quick, metric));
     else if (ordered != 1) { set_last_error("ordered must be 0 or 1"); return TC_ERR_ARG; }
@@ -1857,6 +1859,7 @@ int tc_corr3_process_cross21(tc_corr3* c, tc_field* f1, tc_field* f2, int ordere
                              int quick, int metric)
 {
     (void)dots;
+    if (c) c->ms = 0.;
     // ProcessCross21c, src/Corr3.cpp:3831-3868.
     if (ordered == 0) {
         TC_TRY(corr3_run(c, f2, f1, f1, 1, quick, metric));
@@ -1872,6 +1875,7 @@ int tc_corr3_process_cross(tc_corr3* c, tc_field* f1, tc_field* f2, tc_field* f3
                            int dots, int quick, int metric)
 {
     (void)dots;
+    if (c) c->ms = 0.;
     if (!f3) { set_last_error("NULL argument"); return TC_ERR_ARG; }
     // ProcessCrossc, src/Corr3.cpp:3938-3976.
     switch (ordered) {
