@@ -338,3 +338,35 @@ def test_multipole_three_field_many_bins(gpu_lib):
                     ("meand2", "meand2"), ("meanlogd3", "meanlogd3")):
         err = np.abs(out[mine] - ref[r]).max() / max(np.abs(ref[r]).max(), 1e-300)
         assert err <= TOL, f"{mine}: {err:.3e}"
+
+
+def test_multipole_three_field_edge_cases(gpu_lib):
+    """An empty field leaves the outputs untouched (the reference's loops do nothing); an
+    ordered value the reference's dispatch has no case for, or fields in different coordinate
+    systems, are refused."""
+    from cases3 import spec3
+    T = gpu_lib
+    name = "ggg_flat_mp_x3o4"
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    s = spec3(str(g["case"]))
+    cats = [{k[3:]: g[k] for k in g.files if k.startswith(f"c{i + 1}_")} for i in range(3)]
+    fs = [H.gpu_field(T, "G", "flat", c, float(g["min_size"]), float(g["max_size"])) for c in cats]
+    empty = {k: v[:0] for k, v in cats[2].items()}
+    fe = H.gpu_field(T, "G", "flat", empty, float(g["min_size"]), float(g["max_size"]))
+    corr, out, zk = _corr3(T, "GGG", s)
+    corr.processCross(fs[0], fs[1], fe, 4, False, False, T.Euclidean)
+    corr.processCross21(fe, fs[1], 3, False, False, T.Euclidean)
+    corr.processCross12(fs[0], fe, 0, False, False, T.Euclidean)
+    for k, v in out.items():
+        assert not np.any(v), k
+    with pytest.raises(ValueError):
+        corr.processCross21(fs[0], fs[1], 1, False, False, T.Euclidean)
+    with pytest.raises(ValueError):
+        corr.processCross(fs[0], fs[1], fs[2], 5, False, False, T.Euclidean)
+    with pytest.raises(ValueError):
+        corr.processCross12(fs[0], fs[1], 2, False, False, T.Euclidean)
+    sph = {"x": cats[2]["x"] * 0 + 1.0, "y": cats[2]["y"] * 0, "z": cats[2]["x"] * 0,
+           "g1": cats[2]["g1"], "g2": cats[2]["g2"], "w": cats[2]["w"]}
+    fsph = H.gpu_field(T, "G", "spherical", sph, 0.0, 0.0)
+    with pytest.raises(ValueError):
+        corr.processCross(fs[0], fs[1], fsph, 4, False, False, T.Euclidean)
