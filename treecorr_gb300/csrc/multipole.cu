@@ -1,11 +1,13 @@
-// multipole.cu -- GGG 3-point correlation with LogMultipole binning on sm_103a.
+// multipole.cu -- 3-point correlations with LogMultipole binning on sm_103a (all N / K / G
+// classes: GGG's contraction over the payloads each class needs, see MPParams).
 //
 // Semantics follow the reference's multipole algorithm (Porth et al.):
-//   BaseCorr3::multipole (src/Corr3.cpp:1124-1175), multipoleSplit1 (1374-1408),
-//   splitC2Cells (1323-1372), multipoleFinish (1548-1613), splitC2CellsOrCalculateGn
-//   (1452-1546), Corr3::calculateGn + MultipoleScratch<GData>::calculateGn (1681-1704,
-//   1767-1828), Corr3::calculateZeta (1861-1974) and MultipoleHelper<5>::CalculateZeta
-//   (2585-2843); scratch layout include/MultipoleScratch.h:36-125, 296-383.
+//   BaseCorr3::multipole (src/Corr3.cpp:1124-1175; cross12 1177-1237; three-field
+//   1239-1305), multipoleSplit1 (1374-1449), splitC2Cells (1323-1372), multipoleFinish
+//   (1548-1679), splitC2CellsOrCalculateGn (1452-1546), Corr3::calculateGn +
+//   MultipoleScratch<GData>::calculateGn (1681-1704, 1767-1828), Corr3::calculateZeta
+//   (1861-2087) and MultipoleHelper<1..6>::CalculateZeta (2108-3082); scratch layout
+//   include/MultipoleScratch.h:36-125, 296-383.
 //
 // GB300 design:
 //   * Phase 1: one block per top-level cell walks the c1 subtree of multipoleSplit1, refining
@@ -24,6 +26,8 @@
 //     batches (waves) between runs of the finish kernel, FP32 products with FP64 sums.
 //   * A last kernel sums the per-block outputs, the contraction partials and the diagonal
 //     self-pair corrections in a fixed order.
+//   * A three-field cross keeps vertex 3's pairs in scratch bins [nbd, 2 nbd), so the same
+//     kernels produce both cross blocks of a (2 nbd)^2 matrix (MPParams::three).
 // Geometry and the split/accept decisions are FP64 (the reference's arithmetic); the cell
 // payloads are the tree's float values.
 #include <cfloat>

@@ -1,4 +1,4 @@
-// multipole.hpp -- parameters and launchers of the GGG LogMultipole accumulation.
+// multipole.hpp -- parameters and launchers of the LogMultipole 3-point accumulation.
 #pragma once
 
 #include <cstdint>
