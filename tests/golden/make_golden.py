@@ -377,6 +377,9 @@ X3_CASES = {
     "ggn_sphere_mp_x21o3": ("GGN", "ggg_sphere_mp", "cross21", 3),
     "gkg_sphere_mp_x3o4": ("GKG", "ggg_sphere_mp", "cross", 4),
     "ggk_flat_mp_x21o3": ("GGK", "ggg_flat_mp", "cross21", 3),
+    "ggg_flat_mp_x3o2": ("GGG", "ggg_flat_mp", "cross", 2),
+    "nnn_flat_mp_x3o3": ("NNN", "ggg_flat_mp", "cross", 3),
+    "kkk_sphere_mp_x21o0": ("KKK", "ggg_sphere_mp", "cross21", 0),
 }
 
 if __name__ == "__main__" and "--mp-x3" in sys.argv:

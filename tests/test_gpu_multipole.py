@@ -272,7 +272,8 @@ def _x3_run(T, g, s):
                                   "knk_flat_mp_x3o4", "kkn_sphere_mp_x21o3", "nng_flat_mp_x21o3",
                                   "ngn_sphere_mp_x3o4", "kkg_sphere_mp_x21o3", "kgk_flat_mp_x3o4",
                                   "gng_flat_mp_x3o4", "ggn_sphere_mp_x21o3", "gkg_sphere_mp_x3o4",
-                                  "ggk_flat_mp_x21o3"])
+                                  "ggk_flat_mp_x21o3", "ggg_flat_mp_x3o2", "nnn_flat_mp_x3o3",
+                                  "kkk_sphere_mp_x21o0"])
 @pytest.mark.parametrize("tensor", ["1", "0"])
 def test_multipole_three_field_golden(gpu_lib, monkeypatch, name, tensor):
     """The three-field multipole (vertex 2's pairs in bins [0, nb), vertex 3's in [nb, 2 nb)

@@ -202,7 +202,8 @@ X3 = ["ggg_flat_mp_x3o4", "ggg_sphere_mp_x3o1", "ggg_flat_mp_x21o3", "kkk_flat_m
       "nnn_sphere_mp_x12o0", "ngg_flat_mp_x3o4", "gkk_sphere_mp_x3o1", "nnk_flat_mp_x21o3",
       "nkn_sphere_mp_x3o4", "knk_flat_mp_x3o4", "kkn_sphere_mp_x21o3", "nng_flat_mp_x21o3",
       "ngn_sphere_mp_x3o4", "kkg_sphere_mp_x21o3", "kgk_flat_mp_x3o4", "gng_flat_mp_x3o4",
-      "ggn_sphere_mp_x21o3", "gkg_sphere_mp_x3o4", "ggk_flat_mp_x21o3"]
+      "ggn_sphere_mp_x21o3", "gkg_sphere_mp_x3o4", "ggk_flat_mp_x21o3", "ggg_flat_mp_x3o2",
+      "nnn_flat_mp_x3o3", "kkk_sphere_mp_x21o0"]
 
 
 def x3_fields(O, g, s):
