@@ -85,6 +85,9 @@ typedef struct tc_stats {
     double  build_ms;        /* device time of the tree builds done by this call */
     double  traverse_ms;     /* device time of the traversal + reduction */
     int64_t learned;         /* cell pairs accepted by the learned criterion (of accepted) */
+    int64_t tiles;           /* leaf-pair tiles of the exact mode (angle_slop 0 or brute) */
+    int64_t tile_pairs;      /* leaf pairs evaluated in tiles (accepted ones are in accepted) */
+    int64_t tile_escalated;  /* tile leaf pairs decided again in FP64 near a bin edge */
 } tc_stats;
 
 /* Field construction: replaces BuildNField / BuildKField / BuildZField / BuildVField /
@@ -189,22 +192,27 @@ int tc_corr2_process_auto(tc_corr2* c, tc_field* f, int dots, int quick, int met
 int tc_corr2_process_cross(tc_corr2* c, tc_field* f1, tc_field* f2, int dots, int quick,
                            int metric);
 
-/* The auto-correlation of tc_corr2_process_auto, for callers that must not allocate GPU
- * memory during the call -- for instance code that runs while a CUDA stream is being
- * captured, where cudaMalloc is not allowed, or a process whose device memory is all handed
- * out by its own memory pool.  No reference counterpart: the reference runs on the CPU and
- * allocates per call.
+/* The auto-correlation of tc_corr2_process_auto, for callers that cannot let this library
+ * allocate GPU memory during the call: a process whose device memory is all handed out by
+ * its own memory pool (so a cudaMalloc here would fail or evict the pool's cache), or a
+ * latency-critical pipeline that must not take the device-wide synchronisation that
+ * cudaMalloc and cudaFree can cause.  No reference counterpart: the reference runs on the
+ * CPU and allocates per call.
  *
  * Nothing is allocated: the traversal's work lists and partial sums live in one fixed
  * device array of about 52 MiB that is part of this library (every GPU that loads the
  * library holds it until the process exits).  Limits: nbins <= 64, at most 1024 warps, and
  * work lists of the fixed size; a traversal that needs more space fails with
- * TC_ERR_DEVICE and a clear message (tc_corr2_process_auto has no such limit).
- * The field must already be built (call tc_field_ntop once beforehand: building the tree
- * allocates).  The first call on a device looks up the array's device address; make that
- * first call before any stream capture.  All calls share the array: calls that overlap on
- * the GPU (from several host threads or processes sharing a context) race and must be
- * serialised by the caller.  Results are added into the corr's output arrays as usual. */
+ * TC_ERR_DEVICE and a clear message (tc_corr2_process_auto has no such limit).  Only the
+ * bin_slop criterion runs: a corr with the learned criterion set (tc_corr2_set_learned) is
+ * refused with TC_ERR_ARG.  The field must already be built (call tc_field_ntop once
+ * beforehand: building the tree allocates).  The first call on a device looks up the
+ * array's device address (set-up, once per device, with that device current); make that
+ * first call before any stream capture.  All calls share the array, which keeps the last
+ * call's contents (each call clears what must start at zero): calls that overlap on the GPU
+ * (from several host threads, or processes sharing a context) race and must be serialised
+ * by the caller.  Results are added into the corr's output arrays as usual; in the stats,
+ * traverse_ms stays 0. */
 int tc_corr2_process_auto_noalloc(tc_corr2* c, tc_field* f, int quick, int metric);
 
 /* BaseCorr2.triviallyZero -> TriviallyZero (src/Corr2.cpp:1107-1128): 1 if no pair of

@@ -102,6 +102,16 @@ CASES = {
     "qq_flat":          ("Q", "flat", "Euclidean", "flat", 2500, 0, 1., 20., 10, 1.0, 0.1, "mean", False, 3, 10),
     "qq_3d":            ("Q", "3d", "Euclidean", "threed", 2500, 0, 1., 30., 10, 1.0, 0.1, "mean", False, 3, 10),
     "tt_flat_cross":    ("T", "flat", "Euclidean", "flat", 2000, 2500, 1., 20., 10, 0.5, 0.1, "mean", False, 3, 10),
+    # Exact mode (angle_slop 0, or brute fields): every accepted pair is a pair of leaves,
+    # which the GPU evaluates in leaf-pair tiles.
+    "gg_sphere_exact":  ("G", "spherical", "Arc", "sphere", 2500, 0, 2. * ARCMIN, 60. * ARCMIN, 10, 0.0, 0.0, "mean", False, 3, 10),
+    "nn_flat_exact_cross": ("N", "flat", "Euclidean", "flat", 2000, 2500, 1., 20., 10, 0.0, 0.0, "mean", False, 3, 10),
+    "kk_sphere_exact":  ("K", "spherical", "Arc", "sphere", 2500, 0, 2. * ARCMIN, 60. * ARCMIN, 10, 0.5, 0.0, "mean", False, 3, 10),
+    "ng_3d_exact_cross": ("NG", "3d", "Euclidean", "threed", 1500, 2000, 1., 30., 10, 0.0, 0.0, "mean", False, 3, 10),
+    "tt_sphere_exact_median": ("T", "spherical", "Arc", "sphere", 2000, 0, 2. * ARCMIN, 60. * ARCMIN, 10, 0.0, 0.0, "median", False, 3, 10),
+    "kg_flat_exact_clumped": ("KG", "flat", "Euclidean", "clumped", 2500, 2500, 0.5, 30., 15, 0.0, 0.0, "mean", False, 3, 10),
+    "qq_flat_brute":    ("Q", "flat", "Euclidean", "flat", 1200, 0, 1., 20., 10, 1.0, 0.1, "mean", True, 3, 10),
+    "zz_sphere_brute_euc": ("Z", "spherical", "Euclidean", "sphere", 1500, 0, 2. * ARCMIN, 60. * ARCMIN, 10, 0.5, 0.1, "mean", True, 3, 10),
 }
 
 

@@ -2,7 +2,7 @@
 
 Run in a container that has the reference sources (it does not run on the GPU machine):
 
-    make -f oracle/Makefile.ref -j8 REF=/root/reference   # builds oracle/_ref/_treecorr*.so
+    make -f oracle/Makefile.ref -j8 REF=$TREECORR_REFERENCE   # builds oracle/_ref/_treecorr*.so
     python tests/golden/make_golden.py
 
 For every case in tests/golden/cases.py it builds the reference's own native Field and
@@ -94,7 +94,7 @@ def run_case(name):
 
 
 if __name__ == "__main__" and not {"--mp", "--mp-nnn", "--mp-kkk", "--mp-x12", "--mp-x3",
-                                   "--xyz", "--kmeans"} & set(sys.argv):
+                                   "--xyz", "--kmeans", "--bench"} & set(sys.argv):
     _treecorr.SetOMPThreads(1)
     names = sys.argv[1:] or list(CASES)
     for name in names:
@@ -430,3 +430,75 @@ if __name__ == "__main__" and "--mp-x3" in sys.argv:
             save["ref_" + k] = v
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **save)
         print(f"{name:22s} ntri={out['ntri'].sum():.6g} weight={out['weight'].sum():.6g}")
+
+
+# The benchmark configurations' own shapes and binnings (tests/golden/cases_bench.py): the
+# catalogs are regenerated bit-identically from their seeds, so only the outputs and a hash
+# of the inputs are stored.
+def run_bench2(name):
+    from cases_bench import bench2_inputs, bench2_spec, catalog_hash
+    s = bench2_spec(name)
+    cat = bench2_inputs(name)
+    B = s["bins"]
+    nb = B["nbins"]
+    out = {k: np.zeros(nb) for k in ("xi0", "xi1", "xi2", "xi3", "meanr", "meanlogr",
+                                      "weight", "npairs")}
+    corr = _treecorr.GGCorr(
+        _treecorr.Log, B["min_sep"], B["max_sep"], nb, B["bin_size"], B["b"], B["a"],
+        -sys.float_info.max, sys.float_info.max, 0., 0., 0.,
+        out["xi0"], out["xi1"], out["xi2"], out["xi3"], out["meanr"], out["meanlogr"],
+        out["weight"], out["npairs"])
+    f = build_field("G", s["coords"], cat, s["min_size"], s["max_size"], s["split"],
+                    s["brute"], s["min_top"], s["max_top"])
+    corr.processAuto(f, False, False, METRIC[s["metric"]])
+    save = dict(min_size=s["min_size"], max_size=s["max_size"], ntop=f.getNTopLevel(),
+                input_sha256=catalog_hash(cat))
+    for k, v in out.items():
+        save["ref_" + k] = v
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **save)
+    return out
+
+
+def run_bench3(name):
+    from cases_bench import bench3_inputs, bench3_spec, catalog_hash
+    s = bench3_spec(name)
+    cat = bench3_inputs(name)
+    nb, mn = s["nbins"], s["max_n"]
+    shape = (nb, nb, 2 * mn + 1)
+    keys = ("gam0r", "gam0i", "gam1r", "gam1i", "gam2r", "gam2i", "gam3r", "gam3i",
+            "meand1", "meanlogd1", "meand2", "meanlogd2", "meand3", "meanlogd3", "meanu",
+            "meanv", "weight", "weight_im", "ntri")
+    out = {k: np.zeros(shape) for k in keys}
+    corr = _treecorr.GGGCorr(
+        _treecorr.LogMultipole, s["min_sep"], s["max_sep"], nb, s["bin_size"], s["b"], s["a"],
+        0., 0., mn, 0., 0., 0., 0., 0, 0., 0.,
+        -sys.float_info.max, sys.float_info.max, 0., 0., 0.,
+        *[out[k] for k in keys])
+    f = build_field("G", s["coords"], cat, s["min_size"], s["max_size"], "mean", False, 3, 10)
+    corr.processAuto(f, False, False, METRIC[s["metric"]])
+    save = dict(min_size=s["min_size"], max_size=s["max_size"], input_sha256=catalog_hash(cat))
+    for k, v in out.items():
+        save["ref_" + k] = v
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **save)
+    return out
+
+
+if __name__ == "__main__" and "--bench" in sys.argv:
+    import time
+    from cases_bench import BENCH2, BENCH3
+    _treecorr.SetOMPThreads(1)
+    only = [a for a in sys.argv[1:] if not a.startswith("--")]
+    for name in BENCH2:
+        if only and name not in only:
+            continue
+        t0 = time.time()
+        out = run_bench2(name)
+        print(f"{name:16s} npairs={out['npairs'].sum():.0f} weight={out['weight'].sum():.6g} "
+              f"({time.time() - t0:.1f} s)", flush=True)
+    for name in BENCH3:
+        if only and name not in only:
+            continue
+        t0 = time.time()
+        out = run_bench3(name)
+        print(f"{name:16s} ntri={out['ntri'].sum():.6g} weight={out['weight'].sum():.6g} "
+              f"({time.time() - t0:.1f} s)", flush=True)

@@ -1,10 +1,10 @@
 """GPU test of tc_corr2_process_auto_noalloc, the allocation-free auto-correlation.
 
-Some callers cannot allocate GPU memory while they run this code: a process that is
-capturing a CUDA stream into a graph (cudaMalloc is not allowed during capture), or one
-whose device memory is all handed out by its own memory pool.  For them the library offers
-one entry point that allocates nothing: it uses a fixed device array that is part of the
-library.  This test calls it through the C ABI, twice in a row, and checks each result
+Some callers cannot let this library allocate GPU memory while it runs: a process whose
+device memory is all handed out by its own memory pool, or a latency-critical pipeline that
+must not take the device-wide synchronisation cudaMalloc/cudaFree can cause.  For them the
+library offers one entry point that allocates nothing: it uses a fixed device array that is
+part of the library.  This test calls it through the C ABI, twice in a row, and checks each result
 against tc_corr2_process_auto on the same field, and that free device memory does not
 change across the calls.
 
@@ -88,3 +88,23 @@ def test_noalloc_rejects_what_it_cannot_hold(gpu_lib):
     rc = noalloc(corr_big._h, f._h, 0, int(T.Euclidean))
     assert rc == 1 and b"at most 64" in L.tc_last_error()
     assert not out["npairs"].any()
+
+
+def test_noalloc_refuses_the_learned_criterion(gpu_lib):
+    """The allocation-free call runs the bin_slop criterion only: a corr that has the learned
+    criterion set is refused with a clear message and its outputs stay untouched."""
+    T = gpu_lib
+    L, noalloc = _noalloc_fn(T)
+    s, c1, c2, bins, min_size, max_size, golden = H.load_case("gg_flat_bs1")
+    f = H.gpu_field(T, "G", "flat", c1, min_size, max_size)
+    f.getNTopLevel()
+    out = {k: np.zeros(bins["nbins"]) for k in H.OUT_KEYS}
+    corr = _corr(T, "G", bins, out)
+    corr.setLearned(np.zeros(T.mlp_nparam(), dtype=np.float32), threshold=-3.0)
+    rc = noalloc(corr._h, f._h, 0, int(T.Euclidean))
+    assert rc == 1 and b"bin_slop criterion only" in L.tc_last_error()
+    assert not out["weight"].any() and not out["npairs"].any()
+    corr.setLearned(None)   # back to the plain criterion: accepted again
+    rc = noalloc(corr._h, f._h, 0, int(T.Euclidean))
+    assert rc == 0, L.tc_last_error().decode()
+    H.assert_outputs_close(out, golden, "G", rtol=1e-5, label="after setLearned(None)")

@@ -31,7 +31,8 @@ class tc_stats(ctypes.Structure):
     _fields_ = [("cell_pairs", ctypes.c_int64), ("accepted", ctypes.c_int64),
                 ("escalated", ctypes.c_int64), ("launches", ctypes.c_int64),
                 ("build_ms", ctypes.c_double), ("traverse_ms", ctypes.c_double),
-                ("learned", ctypes.c_int64)]
+                ("learned", ctypes.c_int64), ("tiles", ctypes.c_int64),
+                ("tile_pairs", ctypes.c_int64), ("tile_escalated", ctypes.c_int64)]
 
 
 _lib = None

@@ -8,6 +8,7 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <string>
@@ -114,6 +115,11 @@ struct tc_corr2 {
     int2* samples = nullptr;
     long long sample_cap = 0;
     unsigned sample_mod = 1;
+    // Leaf-pair tiles of the exact mode: the tile list, its control words and the bin edges.
+    int2* tiles = nullptr;
+    long long tile_cap = 0;
+    unsigned long long* tctl = nullptr;
+    float* tedge = nullptr;              // [2][nbins+1]: 1/edge^2, log(edge)
 };
 
 namespace {
@@ -475,6 +481,15 @@ void trav_setup(const tc_corr2* c, TravParams& T, int coords, int metric, int qu
 
 // Runs the breadth-first expansion of T to completion (device-side schedule, batches of
 // launches, more level buffers on demand).  *derr: the device error word afterwards.
+// Items per expansion launch: up to 16M, less for small catalogs (level buffers hold 4
+// chunks each: 512 MB per level at the largest size).
+long long expand_chunk(long long npoints)
+{
+    long long CH = 1LL << 16;
+    while (CH < (1LL << 24) && CH < 2 * npoints) CH <<= 1;
+    return CH;
+}
+
 int expand_run(tc_corr2* c, const TravParams& T, int blocks, long long npoints, cudaStream_t st,
                int* derr_out, long long* launches_out)
 {
@@ -484,8 +499,7 @@ int expand_run(tc_corr2* c, const TravParams& T, int blocks, long long npoints, 
     // 4 chunks each: 512 MB per level at the largest size).  Large launches amortise the
     // per-launch work of every warp (bin set-up, the flush of its totals, the completion
     // count); 4M-item chunks took 19% longer on a 10M-point catalog.
-    long long CH = 1LL << 16;
-    while (CH < (1LL << 24) && CH < 2 * npoints) CH <<= 1;
+    const long long CH = expand_chunk(npoints);
     if (!c->sched) TC_TRY(dalloc(&c->sched, 1));
     ExpandSched hs;
     std::memset(&hs, 0, sizeof(hs));
@@ -596,7 +610,46 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
     T.samples = c->samples; T.sample_cap = c->sample_cap; T.sample_mod = c->sample_mod;
     int blocks = 0, nwarps = 0;
     TC_TRY(expand_grid(nq, nb, &blocks, &nwarps, c->mode));
-    TC_TRY(expand_scratch(c, nwarps, nq));
+    // Exact mode: every pair the reference accepts is a pair of leaves (angle_slop 0, or two
+    // brute fields), so the leaf pairs below small cell pairs go through k_tiles.
+    // TCGPU_TILES=0 turns the tiles off (the traversal then walks down to the leaves).
+    bool tiles = c->mode == 0 && (c->a == 0. || (f1->brute && g->brute));
+    if (const char* ev = std::getenv("TCGPU_TILES")) tiles = tiles && std::atoi(ev) != 0;
+    int tblocks = 0, twarps = 0;
+    if (tiles) {
+        T.tile_leaf = TILE_LEAF;      // tiles_grid picks the kernel from T's classes
+        TC_TRY(tiles_grid(T, &tblocks, &twarps));
+        const long long cap = expand_chunk(f1->n + (f2 ? f2->n : 0));
+        if (c->tile_cap < cap) {
+            dfree(c->tiles);
+            c->tiles = nullptr;
+            c->tile_cap = 0;
+            TC_TRY(dalloc(&c->tiles, (size_t)cap));
+            c->tile_cap = cap;
+        }
+        if (!c->tctl) TC_TRY(dalloc(&c->tctl, 8));
+        if (!c->tedge) TC_TRY(dalloc(&c->tedge, 2 * (size_t)(nb + 1)));
+        std::vector<float> te(2 * (size_t)(nb + 1));
+        for (int k = 0; k <= nb; ++k) {
+            const double le = std::log(c->minsep) + k * c->binsize;   // log of edge k
+            te[k] = (float)std::exp(-2. * le);
+            te[nb + 1 + k] = (float)le;
+        }
+        TC_CU(cudaMemcpyAsync(c->tedge, te.data(), te.size() * sizeof(float),
+                              cudaMemcpyHostToDevice, st));
+        TC_CU(cudaMemsetAsync(c->tctl, 0, 8 * sizeof(unsigned long long), st));
+        T.tile_leaf = TILE_LEAF;
+        T.leaf_base1 = (int)(f1->n - 1);
+        T.leaf_base2 = (int)(g->n - 1);
+        T.tiles = c->tiles;
+        T.tctl = c->tctl;
+        T.tile_cap = c->tile_cap;
+        T.tile_blocks = tblocks;
+        T.tile_wbase = nwarps;
+        T.tile_edge = c->tedge;
+        T.tile_ledge = c->tedge + nb + 1;
+    }
+    TC_TRY(expand_scratch(c, nwarps + twarps, nq));
     T.nsamples = c->ctl + 6;   // ctl exists from here on
     if ((c->mode == 1 && (!c->samples || c->sample_cap <= 0)) || (c->mode == 2 && !c->mlp)) {
         set_last_error("learned-criterion buffers missing");
@@ -606,8 +659,8 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
     T.wacc = c->wacc; T.wnp = c->wnp; T.err = c->d_err;
     T.counters = c->ctl + 2;
     T.in_tasks = nullptr; T.nin = 0;
-    TC_CU(cudaMemsetAsync(c->wacc, 0, sizeof(double) * (size_t)nwarps * nq * nb, st));
-    TC_CU(cudaMemsetAsync(c->wnp, 0, sizeof(unsigned long long) * (size_t)nwarps * nb, st));
+    TC_CU(cudaMemsetAsync(c->wacc, 0, sizeof(double) * (size_t)(nwarps + twarps) * nq * nb, st));
+    TC_CU(cudaMemsetAsync(c->wnp, 0, sizeof(unsigned long long) * (size_t)(nwarps + twarps) * nb, st));
     TC_CU(cudaMemsetAsync(c->ctl, 0, 8 * sizeof(unsigned long long), st));
     TC_CU(cudaMemsetAsync(c->d_err, 0, sizeof(int), st));
     cudaEvent_t e0, e1;
@@ -626,11 +679,15 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
         cudaEventDestroy(e0); cudaEventDestroy(e1);
         return TC_ERR_DEVICE;
     }
-    TC_TRY(launch_reduce(nwarps, nq, nb, c->wacc, c->wnp, c->tot, c->totnp, st));
+    TC_TRY(launch_reduce(nwarps + twarps, nq, nb, c->wacc, c->wnp, c->tot, c->totnp, st));
     TC_CU(cudaEventRecord(e1, st));
     std::vector<double> tot((size_t)nq * nb);
     std::vector<unsigned long long> totnp(nb);
     unsigned long long cntr[4];
+    unsigned long long tcnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (tiles)
+        TC_CU(cudaMemcpyAsync(tcnt, c->tctl, 8 * sizeof(unsigned long long),
+                              cudaMemcpyDeviceToHost, st));
     TC_CU(cudaMemcpyAsync(tot.data(), c->tot, tot.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
     TC_CU(cudaMemcpyAsync(totnp.data(), c->totnp, nb * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     TC_CU(cudaMemcpyAsync(cntr, c->ctl + 2, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
@@ -644,6 +701,9 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
     c->stats.learned = (int64_t)cntr[3];
     c->stats.launches = launches_done;
     c->stats.traverse_ms = ms;
+    c->stats.tiles = (int64_t)tcnt[2];
+    c->stats.tile_pairs = (int64_t)tcnt[3];
+    c->stats.tile_escalated = (int64_t)tcnt[4];
     // Corr2::finishProcess adds into the caller's arrays (src/Corr2.cpp:527-566).
     for (int k = 0; k < nb; ++k) {
         c->weight[k] += tot[k];
@@ -658,13 +718,22 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
 }
 
 // The auto-correlation of an already built field with the fixed traversal scratch: no
-// device or host allocation.  Same arithmetic as corr_process (the same kernels), with the
-// warp count capped at NOALLOC_MAXW and the bins at NOALLOC_MAXNB.
+// device or host allocation.  It runs the per-warp depth-first traversal kernel (k_traverse,
+// which no other path launches) with the same decision and accumulation code as k_expand,
+// the warp count capped at NOALLOC_MAXW and the bins at NOALLOC_MAXNB.  Only the exact
+// bin_slop criterion runs here: a corr set up for the learned criterion or for sampling its
+// training pairs is refused.
 int corr_process_auto_noalloc(tc_corr2* c, tc_field* f, int quick, int metric)
 {
     if (!c || !f) { set_last_error("NULL argument"); return TC_ERR_ARG; }
     if (c->d1 != f->dkind || c->d2 != f->dkind) {
         set_last_error("field data kind does not match the correlation"); return TC_ERR_ARG;
+    }
+    if (c->mode != 0) {
+        set_last_error("the allocation-free call runs the bin_slop criterion only; this corr "
+                       "has the learned criterion or pair sampling set (use "
+                       "tc_corr2_process_auto)");
+        return TC_ERR_ARG;
     }
     TC_TRY(check_metric(f->coords, metric));
     if (c->nbins > NOALLOC_MAXNB) {
@@ -687,22 +756,8 @@ int corr_process_auto_noalloc(tc_corr2* c, tc_field* f, int quick, int metric)
     const int nb = c->nbins;
     const int nq = 3 + xi_count(c->d1, c->d2);
     TravParams T;
-    std::memset(&T, 0, sizeof(T));
-    T.coords = f->coords; T.metric = metric; T.quick = quick ? 1 : 0;
-    T.k1 = kind_of(c->d1); T.k2 = kind_of(c->d2); T.s1 = spin_of(c->d1); T.s2 = spin_of(c->d2);
-    T.nbins = nb; T.autoc = 1; T.nqf = nq;
-    T.minsep = c->minsep; T.maxsep = c->maxsep; T.binsize = c->binsize; T.b = c->b; T.a = c->a;
-    T.logminsep = std::log(c->minsep); T.halfminsep = 0.5 * c->minsep;
-    T.minsepsq = c->minsep * c->minsep; T.maxsepsq = c->maxsep * c->maxsep;
-    T.bsq = c->b * c->b; T.asq = c->a * c->a;
-    T.fminsep = (float)T.minsep; T.fmaxsep = (float)T.maxsep; T.fbinsize = (float)T.binsize;
-    T.fb = (float)T.b; T.fminsepsq = (float)T.minsepsq; T.fmaxsepsq = (float)T.maxsepsq;
-    T.fbsq = (float)T.bsq; T.fasq = (float)std::min(T.asq, 1e30);
-    T.fbb = (float)(0.25 * sqr(T.binsize + T.b));
-    T.fmineff = (float)std::min(T.bsq, T.asq);
-    T.finvminsepsq = (float)(1. / T.minsepsq);
-    T.finvbinsize = (float)(1. / T.binsize);
-    T.flogminsep = (float)T.logminsep;
+    trav_setup(c, T, f->coords, metric, quick, nq);
+    T.autoc = 1;
     T.c1 = f->tcells; T.c2 = f->tcells;
     T.x1 = f->cells.x; T.y1 = f->cells.y; T.z1 = f->cells.z;
     T.x2 = f->cells.x; T.y2 = f->cells.y; T.z2 = f->cells.z;
@@ -780,6 +835,7 @@ int corr_process_auto_noalloc(tc_corr2* c, tc_field* f, int quick, int metric)
     c->stats.accepted = (int64_t)cnt[1];
     c->stats.escalated = (int64_t)cnt[2];
     c->stats.launches = launches;
+    c->stats.build_ms = f->build_ms;   // the field's earlier build; traverse_ms stays 0
     for (int k = 0; k < nb; ++k) {
         c->weight[k] += h_tot[k];
         if (!quick) {
@@ -1326,6 +1382,7 @@ void tc_corr2_free(tc_corr2* c)
     for (auto& p : c->lev) dfree(p);
     dfree(c->sched);
     dfree(c->mlp); dfree(c->samples);
+    dfree(c->tiles); dfree(c->tctl); dfree(c->tedge);
     delete c;
 }
 

@@ -28,8 +28,10 @@
 //     self-pair corrections in a fixed order.
 //   * A three-field cross keeps vertex 3's pairs in scratch bins [nbd, 2 nbd), so the same
 //     kernels produce both cross blocks of a (2 nbd)^2 matrix (MPParams::three).
-// Geometry and the split/accept decisions are FP64 (the reference's arithmetic); the cell
-// payloads are the tree's float values.
+// Geometry and the split/accept decisions are taken in FP32 with error margins
+// (mp_decide32); an entry inside a margin is decided again in FP64 with the reference's
+// arithmetic, so the decisions are the reference's.  The cell payloads are the tree's float
+// values.
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
@@ -1503,7 +1505,10 @@ __global__ void __launch_bounds__(ZB) k_mp_zeta(ZParams Q)
 // products); the FP32 accumulators in TMEM are drained to FP64 every TC_DRAIN chunks.
 static constexpr int TCB = 128;        // threads (4 warps = the 128 TMEM lanes)
 static constexpr int TC_REC = 16;      // records per chunk = 32 K entries = 4 K steps
-static constexpr int TC_DRAIN = 64;    // chunks between FP64 drains
+// Chunks between FP64 drains: the TMEM accumulators add 3 MMAs x 4 K steps x 2 entries per
+// record in FP32, and that error grows with the records per drain (at 20 bins / max_n 30,
+// 1024 records per drain gave 1.6e-5 of max|gam|; 128 records keep it near 2e-6).
+static constexpr int TC_DRAIN = 8;
 
 __device__ __forceinline__ void tf32_split(float x, float& hi, float& lo)
 {

@@ -1,0 +1,543 @@
+// tiles.cu -- leaf-pair tiles of the exact mode (angle_slop 0, or two brute fields).
+//
+// In that mode the reference accepts only pairs of leaves (src/Corr2.cpp:308-389:
+// BinTypeHelper<Log>::singleBin, include/BinType.h:93-151, needs s1 + s2 <= a r, which
+// a = 0 allows only for leaves, whose size is 0), so below a cell pair it visits every leaf
+// pair, keeps those in range (isRSqInRange, include/BinType.h:61-66) and adds each into the
+// bin of its own separation (directProcess11 and finishProcess with DirectHelper,
+// src/Corr2.cpp:394-566).  The traversal stops at cell pairs of at most TILE_LEAF points per
+// side and hands them here as tiles; k_tiles does the rest with one warp per tile and no tree
+// walk:
+//   * both sides' leaves are staged in shared memory as FP32 offsets from cell B's FP64 centre
+//     (hi + lo parts), so a separation is one FP32 difference of offsets whose error is a few
+//     ulps of the tile's extent;
+//   * the tile is classified once from the centres and the leaves' largest offsets: when every
+//     pair certainly lies inside the separation range and inside one bin (margins far above
+//     the FP32 errors), the per-pair range and bin work is skipped; otherwise each pair gets
+//     its range test and bin from log2 of its squared separation over the squared edge of the
+//     tile's lowest bin, with a band that covers every FP32 error -- a pair inside the band is
+//     decided again in FP64 from the FP64 positions with the reference's formulas;
+//   * lanes take the tile's leaf pairs in order (pair p: leaf p / nB of A, p % nB of B), and
+//     keep running sums for the tile's lowest two bins in registers; pairs in other bins (tiles
+//     that span three or more bins, at separations comparable with the cell sizes) go to the
+//     warp's shared-memory bins directly;
+//   * at the end of a tile the lanes' sums are combined by a reduce-scatter butterfly (one
+//     shuffle per value and step, halving the values each step) and added to the warp's FP32
+//     bins, which go into double-float totals every few tiles and into the warp's FP64 slot
+//     at the end, like the traversal's.
+// The kernel is compiled per geometry (flat, sphere with Arc, sphere or 3-d with Euclidean)
+// and per class family (NN; NK and KK; GG; the others through the generic projection code).
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+
+#include "tc_internal.cuh"
+#include "tc_host.hpp"
+#include "traverse2pt.hpp"
+#include "pair_math.cuh"
+
+namespace tc {
+
+namespace {
+
+constexpr int TPB = 128;          // threads per block
+constexpr int TWPB = TPB / 32;    // warps per block
+constexpr int TFLUSH = 8;         // tiles between flushes of the FP32 bins
+#ifndef TILES_MINB
+#define TILES_MINB 6
+#endif
+constexpr int TMINB = TILES_MINB; // resident blocks per SM the registers are sized for
+
+enum { TG_FLAT = 0, TG_ARC = 1, TG_SPHEUC = 2, TG_3D = 3 };   // geometry
+enum { TK_NN = 0, TK_SC = 1, TK_GEN = 2, TK_GG = 3 };           // class family
+
+// One side of a tile: its valid leaves (n > 0, w != 0) in point order.
+struct TileLeaves {
+    float4 P[32];   // (ox, oy, oz, z / 2): offset from B's centre, half the z coordinate
+    float4 Q[32];   // (x, y, w, n bits): position (FP32), weight, count
+    float4 V[32];   // (d1, d2, id bits, s): payload, leaf cell id, scalar payload (w or w k)
+};
+
+__host__ __device__ inline size_t bins_bytes(int nq, int nb)
+{
+    return ((size_t)nq * nb * 8 + (size_t)nb * 8 + (size_t)nq * nb * 4 + 15) & ~(size_t)15;
+}
+
+__host__ __device__ inline size_t warp_bytes(int nq, int nb)
+{
+    return bins_bytes(nq, nb) + 2 * sizeof(TileLeaves);
+}
+
+// Stages the valid leaves of cell c (points [start, start + n), leaf ids base + p) with their
+// offsets from the centre (ch + cl).  Returns the count; *single is false when a staged leaf
+// holds more than one point.
+__device__ __forceinline__ int stage(const TCell* cells, int base, float4 ca, float4 cb,
+                                     float4 cc, float4 cd, float chx, float chy, float chz,
+                                     float clx, float cly, float clz, int kind, TileLeaves& S,
+                                     int lane, float& on1, float& on2, bool& single)
+{
+    const int start = __float_as_int(cd.z), n = __float_as_int(cc.z);
+    bool v = false;
+    float4 P = make_float4(0.f, 0.f, 0.f, 0.f), Q = P, V = P;
+    int nn = 0;
+    if (lane < n) {
+        const int id = base + start + lane;
+        const float4 a = cells[id].a, b = cells[id].b, c = cells[id].c;
+        nn = __float_as_int(c.z);
+        v = nn > 0 && b.w != 0.f;
+        if (v) {
+            P = make_float4((a.x - chx) + (b.x - clx), (a.y - chy) + (b.y - cly),
+                            (a.z - chz) + (b.z - clz), 0.5f * a.z);
+            Q = make_float4(a.x, a.y, b.w, __int_as_float(nn));
+            V = make_float4(c.x, c.y, __int_as_float(id), kind == DN ? b.w : c.x);
+        }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, v);
+    single = __all_sync(0xffffffffu, !v || nn == 1);
+    if (v) {
+        const int p = __popc(m & ((1u << lane) - 1u));
+        S.P[p] = P; S.Q[p] = Q; S.V[p] = V;
+    }
+    on1 = fabsf(P.x) + fabsf(P.y) + fabsf(P.z);    // L1 norm of the offset
+    on2 = sqrtf(P.x * P.x + P.y * P.y + P.z * P.z); // its length
+    return __popc(m);
+}
+
+__device__ __forceinline__ float warp_max(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Sums v[0..7] over the warp: after the reduce-scatter each group of 4 lanes holds one value's
+// total; lane 4 q + 0 returns value q's total in *out (q = 0..7) and true.
+__device__ __forceinline__ bool warp_sum8(float (&v)[8], int lane, float& out)
+{
+    // xor 16: keep 4 of 8.
+    const bool h16 = lane & 16;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const float send = h16 ? v[q] : v[q + 4];
+        const float got = __shfl_xor_sync(0xffffffffu, send, 16);
+        v[q] = (h16 ? v[q + 4] : v[q]) + got;
+    }
+    // xor 8: keep 2 of 4.
+    const bool h8 = lane & 8;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+        const float send = h8 ? v[q] : v[q + 2];
+        const float got = __shfl_xor_sync(0xffffffffu, send, 8);
+        v[q] = (h8 ? v[q + 2] : v[q]) + got;
+    }
+    // xor 4: keep 1 of 2.
+    const bool h4 = lane & 4;
+    {
+        const float send = h4 ? v[0] : v[1];
+        const float got = __shfl_xor_sync(0xffffffffu, send, 4);
+        v[0] = (h4 ? v[1] : v[0]) + got;
+    }
+    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 2);
+    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+    out = v[0];
+    return (lane & 3) == 0;
+}
+
+// Which value a lane holds after warp_sum8: bit 4 picks the upper half, bit 3 the upper
+// quarter of that, bit 2 the upper one of the last two.
+__device__ __forceinline__ int warp_sum8_index(int lane)
+{
+    return ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
+}
+
+// A leaf pair decided in FP64 with the reference's formulas: decide64 (the reference's
+// process11 for s1 = s2 = 0) on the FP64 leaf positions.  Out of line: it runs for about one
+// pair in 10^5, and keeping it out of the loop keeps the loop's registers low.
+__device__ __noinline__ int leaf_pair64(const TravParams& T, int ida, int idb, bool self,
+                                        float* r, float* logr)
+{
+    const double* x2 = self ? T.x1 : T.x2;
+    const double* y2 = self ? T.y1 : T.y2;
+    const double* z2 = self ? T.z1 : T.z2;
+    const double dx = T.x1[ida] - x2[idb], dy = T.y1[ida] - y2[idb];
+    double dsq = dx * dx + dy * dy;
+    if (T.coords != FLAT) {
+        const double dz = T.z1[ida] - z2[idb];
+        dsq += dz * dz;
+    }
+    const Decision D = decide64(T, dsq, 0., 0.);
+    if (D.act != ACT_ACCEPT) return -1;
+    *r = D.r;
+    *logr = D.logr;
+    return D.k;
+}
+
+// The generic values of an accepted leaf pair (every class, with the projections of
+// accept_values).  Out of line for the same reason.
+__device__ __noinline__ void leaf_values_generic(const TravParams& T, float4 Pa, float4 Qa,
+                                                 float4 Va, float4 Pb, float4 Qb, float4 Vb,
+                                                 float dx, float dy, float dz, float dsq,
+                                                 float r, float logr, float* out)
+{
+    TCell A, B;
+    A.a = make_float4(Qa.x, Qa.y, 2.f * Pa.w, 0.f);
+    A.b = make_float4(0.f, 0.f, 0.f, Qa.z);
+    A.c = make_float4(Va.x, Va.y, Qa.w, 0.f);
+    A.d = make_float4(0.f, 0.f, 0.f, 0.f);
+    B.a = make_float4(Qb.x, Qb.y, 2.f * Pb.w, 0.f);
+    B.b = make_float4(0.f, 0.f, 0.f, Qb.z);
+    B.c = make_float4(Vb.x, Vb.y, Qb.w, 0.f);
+    B.d = A.d;
+    float av[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    unsigned long long nn = 0;
+    accept_values(T, A, B, __float_as_int(Va.z), __float_as_int(Vb.z), dx, dy, dz, dsq, r, logr,
+                  av, nn);
+#pragma unroll
+    for (int q = 3; q < 7; ++q) out[q - 3] = av[q];
+}
+
+// The correlation products of one leaf pair (quantities 3.. of the bins).
+template <int GEO, int KIND>
+__device__ __forceinline__ void pair_products(const TravParams& T, float4 Pa, float4 Qa,
+                                              float4 Va, float4 Pb, float4 Qb, float4 Vb,
+                                              float dx, float dy, float dz, float dsq, float r,
+                                              float logr, float (&x)[4])
+{
+    if constexpr (KIND == TK_SC) {
+        x[0] = Va.w * Vb.w;                                  // wk1 wk2 (DirectHelper<1>)
+    } else if constexpr (KIND == TK_GG && GEO == TG_FLAT) {
+        // ProjectHelper<Flat>: both shears rotated by exp(-2i alpha) of r = p2 - p1, so
+        // g1 conj(g2) is unchanged and g1 g2 turns by exp(-4i alpha) = conj(r)^4 / |r|^4.
+        const float g1r = Va.x, g1i = Va.y, g2r = Vb.x, g2i = Vb.y;
+        x[0] = g1r * g2r + g1i * g2i;                        // xi+ = g1 conj(g2)
+        x[1] = g1i * g2r - g1r * g2i;
+        const float dx2 = dx * dx, dy2 = dy * dy;
+        const float er = dx2 - dy2, ei = -2.f * dx * dy;     // conj(r)^2 (r = -d)
+        const float e2r = er * er - ei * ei, e2i = 2.f * er * ei;
+        const float inv = __fdividef(1.f, dsq * dsq);
+        const float pr = g1r * g2r - g1i * g2i, pi = g1r * g2i + g1i * g2r;   // g1 g2
+        x[2] = (pr * e2r - pi * e2i) * inv;                  // xi-
+        x[3] = (pr * e2i + pi * e2r) * inv;
+    } else if constexpr (KIND == TK_GG && (GEO == TG_ARC || GEO == TG_SPHEUC)) {
+        // ProjectHelper<Sphere>, include/ProjectHelper.h:272-388: directions at p2
+        // (sinA, -cosA) and at p1 (-sinA, -cosB) on accurate differences (d = p1 - p2):
+        // y1 x2 - x1 y2 = x1 dy - y1 dx.  Spin 2: exp(-2i a) = conj(u)^2 / |u|^2; one
+        // reciprocal serves both normalisations.
+        const float sinA = Qa.x * dy - Qa.y * dx;
+        const float cosA = dz + Pb.w * dsq;
+        const float cosB = -dz + Pa.w * dsq;
+        const float s2 = sinA * sinA;
+        const float n2 = fmaf(cosA, cosA, s2), n1 = fmaf(cosB, cosB, s2);
+        const float e2r = fmaf(-cosA, cosA, s2), e2i = 2.f * sinA * cosA;
+        const float e1r = fmaf(-cosB, cosB, s2), e1i = -2.f * sinA * cosB;
+        const float inv = __fdividef(1.f, n1 * n2);
+        const float a2r = Vb.x * e2r - Vb.y * e2i, a2i = Vb.x * e2i + Vb.y * e2r;   // g2 e2
+        const float a1r = Va.x * e1r - Va.y * e1i, a1i = Va.x * e1i + Va.y * e1r;   // g1 e1
+        const float rr = a2r * a1r, ri = a2r * a1i, ir = a2i * a1r, ii = a2i * a1i;
+        x[0] = (rr + ii) * inv;     // both_complex_prod(g2, g1), include/ProjectHelper.h:84-101
+        x[1] = (ri - ir) * inv;
+        x[2] = (rr - ii) * inv;
+        x[3] = (ri + ir) * inv;
+    } else if constexpr (KIND == TK_GG || KIND == TK_GEN) {
+        leaf_values_generic(T, Pa, Qa, Va, Pb, Qb, Vb, dx, dy, dz, dsq, r, logr, x);
+    }
+}
+
+// Adds a tile's register sums for bin kb (acc, count cn) into the warp's FP32 bins.
+__device__ __forceinline__ void tile_bin_out(float (&acc)[8], unsigned cn, int kb, int nq, int nb,
+                                             float* fb, unsigned long long* np, bool quick,
+                                             bool single, int lane)
+{
+    if (!__any_sync(0xffffffffu, cn != 0u) || kb >= nb) return;
+    float tot;
+    const bool holder = warp_sum8(acc, lane, tot);
+    const int q = warp_sum8_index(lane);
+    if (holder && q < nq) fb[q * nb + kb] += tot;
+    if (!quick) {
+        if (single) {
+            const unsigned ct = __reduce_add_sync(0xffffffffu, cn);
+            if (lane == 0) np[kb] += ct;
+        } else if (cn) {
+            atomicAdd(&np[kb], (unsigned long long)cn);
+        }
+    }
+    __syncwarp();
+}
+
+template <int GEO, int KIND>
+__global__ void __launch_bounds__(TPB, TMINB) k_tiles(const __grid_constant__ TravParams T)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int gw = blockIdx.x * TWPB + wib;
+    const int nq = T.nqf, nb = T.nbins;
+    constexpr int NX = KIND == TK_NN ? 0 : (KIND == TK_SC ? 1 : 4);   // products per pair
+    // Tiles waiting; an expansion launch that ran out of room counted past the capacity (and
+    // raised DEV_SPILL_OVERFLOW), so never read beyond it.
+    long long nt = (long long)*(volatile unsigned long long*)&T.tctl[0];
+    if (nt > T.tile_cap) nt = T.tile_cap;
+    unsigned char* wb = smem + (size_t)wib * warp_bytes(nq, nb);
+    float2* fd = reinterpret_cast<float2*>(wb);
+    unsigned long long* np = reinterpret_cast<unsigned long long*>(fd + nq * nb);
+    float* fb = reinterpret_cast<float*>(np + nb);
+    TileLeaves& SA = *reinterpret_cast<TileLeaves*>(wb + bins_bytes(nq, nb));
+    TileLeaves& SB = *(&SA + 1);
+    const long long nwt = (long long)gridDim.x * TWPB;
+    // Per-lane counters: at most ~10^8 pairs per lane in a launch, so 32 bits suffice.
+    unsigned n_acc = 0, n_pairs = 0, n_esc = 0, n_tiles = 0;
+    if ((long long)gw < nt) {
+        for (int q = lane; q < nq * nb; q += 32) { fd[q] = make_float2(0.f, 0.f); fb[q] = 0.f; }
+        for (int q = lane; q < nb; q += 32) np[q] = 0ull;
+        __syncwarp();
+        const float ln2h = 0.5f * 0.69314718f;          // log(r) per unit of log2(r^2)
+        const float ckk = ln2h * T.finvbinsize;          // bins per unit of log2(r^2)
+        const bool quick = T.quick != 0;
+        int since_flush = 0;
+        for (long long t = gw; t < nt; t += nwt) {
+            const int2 tile = T.tiles[t];
+            const bool self = tile.y < 0;
+            const int ia = tile.x, ib = self ? -2 - tile.y : tile.y;
+            const TCell* cB = self ? T.c1 : T.c2;
+            const int baseB = self ? T.leaf_base1 : T.leaf_base2;
+            const float4 Aa = T.c1[ia].a, Ab = T.c1[ia].b, Ac = T.c1[ia].c, Ad = T.c1[ia].d;
+            const float4 Ba = cB[ib].a, Bb = cB[ib].b, Bc = cB[ib].c, Bd = cB[ib].d;
+            ++n_tiles;
+            float eA, rA, eB, rB;
+            bool sA, sB;
+            const int nbl = stage(cB, baseB, Ba, Bb, Bc, Bd, Ba.x, Ba.y, Ba.z, Bb.x, Bb.y, Bb.z,
+                                  T.k2, SB, lane, eB, rB, sB);
+            int na = nbl;
+            // A's offsets are also taken from B's centre; D = centre A - centre B.
+            const float Dx = (Aa.x - Ba.x) + (Ab.x - Bb.x), Dy = (Aa.y - Ba.y) + (Ab.y - Bb.y);
+            const float Dz = GEO == TG_FLAT ? 0.f : (Aa.z - Ba.z) + (Ab.z - Bb.z);
+            if (!self) {
+                float on1, on2;
+                na = stage(T.c1, T.leaf_base1, Aa, Ab, Ac, Ad, Ba.x, Ba.y, Ba.z, Bb.x, Bb.y,
+                           Bb.z, T.k1, SA, lane, on1, on2, sA);
+                eA = on1;
+                // Distance of A's leaf from A's centre.
+                const float4 P = lane < na ? SA.P[lane] : make_float4(Dx, Dy, Dz, 0.f);
+                const float ux = P.x - Dx, uy = P.y - Dy, uz = P.z - Dz;
+                rA = lane < na ? sqrtf(ux * ux + uy * uy + uz * uz) : 0.f;
+            } else {
+                eA = eB; rA = rB; sA = sB;
+            }
+            __syncwarp();
+            if (na == 0 || nbl == 0) continue;
+            const TileLeaves& LA = self ? SB : SA;
+            // Tile bounds.  emax bounds |FP32 d - d| of every pair (each offset within 2 ulps
+            // of its L1 size, the difference one more; a 1.5x margin); the separation of any
+            // pair lies within |D| +- (rA + rB).
+            const float emax = 2.7e-7f * (warp_max(eA) + warp_max(eB)) + 1e-30f;
+            const float rAB = warp_max(rA) + warp_max(rB);
+            const float Dn = sqrtf(Dx * Dx + Dy * Dy + Dz * Dz);
+            const float slack = emax + 2e-6f * (Dn + rAB);
+            float lo = fmaxf(Dn - rAB - slack, 0.f), hi = Dn + rAB + slack;
+            if (GEO == TG_ARC) { lo = arc_from_chord_sq(lo * lo); hi = arc_from_chord_sq(hi * hi); }
+            lo *= 1.f - 1e-5f;
+            hi *= 1.f + 1e-5f;
+            if (lo >= T.fmaxsep || hi < T.fminsep) continue;   // no pair in range
+            const bool interior = lo >= T.fminsep && hi < T.fmaxsep;
+            int klo = (int)floorf(log2f(fmaxf(lo, T.fminsep) * fmaxf(lo, T.fminsep) *
+                                        T.finvminsepsq) * ckk);
+            int khi = (int)floorf(log2f(fminf(hi, T.fmaxsep) * fminf(hi, T.fmaxsep) *
+                                        T.finvminsepsq) * ckk);
+            klo = klo < 0 ? 0 : (klo > nb - 1 ? nb - 1 : klo);
+            khi = khi < 0 ? 0 : (khi > nb - 1 ? nb - 1 : khi);
+            const bool one_bin = interior && klo == khi;
+            const int kref = klo;
+            const float inv_edge = T.tile_edge[kref];     // 1 / (lower edge of kref)^2
+            const float ledge = T.tile_ledge[kref];       // log of that edge
+            // Band (in bins) outside which the FP32 bin is certain: r's relative error
+            // (emax / chord + 4e-7) and __log2f's (2^-22 absolute on [0.5, 2], else 2 ulps;
+            // |log2| <= lmax here), the roundings of its argument and of kk.
+            const float lmax = fmaxf(fabsf(log2f(hi * hi * inv_edge)), 1.f);
+            const float band_e = emax * T.finvbinsize;
+            const float band_0 = 4e-7f * T.finvbinsize + (5e-7f + 3e-7f * lmax) * ckk +
+                                 1.2e-7f * (lmax * ckk) + 1e-7f;
+            const int npt = na * nbl;
+            const int iters = (npt + 31) >> 5;
+            int ii = lane / nbl, jj = lane - (lane / nbl) * nbl;
+            const int di = 32 / nbl, dj = 32 - di * nbl;
+            float acc0[8], acc1[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) { acc0[q] = 0.f; acc1[q] = 0.f; }
+            unsigned c0 = 0u, c1 = 0u;
+            for (int it = 0; it < iters; ++it) {
+                const int i = ii, j = jj;
+                jj += dj; ii += di;
+                if (jj >= nbl) { jj -= nbl; ++ii; }
+                const bool use = (it * 32 + lane < npt) && (!self || j > i);
+                if (!use) continue;
+                ++n_pairs;
+                const float4 Pa = LA.P[i], Pb = SB.P[j];
+                const float4 Qa = LA.Q[i], Qb = SB.Q[j];
+                const float dx = Pa.x - Pb.x, dy = Pa.y - Pb.y;
+                const float dz = GEO == TG_FLAT ? 0.f : Pa.z - Pb.z;
+                const float dsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                const float invc = rsqrtf(dsq);
+                float r = dsq * invc;                       // chord (or flat) length
+                if (GEO == TG_ARC) r = arc_from_chord_sq(dsq);
+                const float rsq = r * r;
+                int k = kref;
+                float lr = __log2f(rsq * inv_edge);
+                float logr = fmaf(lr, ln2h, ledge);
+                if (!one_bin) {
+                    bool unsure = false;
+                    bool drop = false;
+                    if (!interior) {
+                        const float dr = emax + 4e-7f * r;
+                        if (r + dr < T.fminsep || r - dr >= T.fmaxsep) drop = true;
+                        else if (!(r - dr >= T.fminsep && r + dr < T.fmaxsep)) unsure = true;
+                    }
+                    if (drop) continue;
+                    if (!unsure) {
+                        const float kk = lr * ckk;
+                        const float fk = floorf(kk);
+                        const float fr = kk - fk;
+                        const float band = fmaf(band_e, invc, band_0);
+                        if (fr < band || fr > 1.f - band) unsure = true;
+                        k = kref + (int)fk;
+                        if (k >= nb) k = nb - 1;            // src/Corr2.cpp:514
+                        if (k < 0) unsure = true;
+                    }
+                    if (unsure) {
+                        ++n_esc;
+                        k = leaf_pair64(T, __float_as_int(LA.V[i].z), __float_as_int(SB.V[j].z),
+                                        self, &r, &logr);
+                        if (k < 0) continue;
+                    }
+                }
+                ++n_acc;
+                const float ww = Qa.z * Qb.z;
+                float v[8];
+                v[0] = ww; v[1] = ww * r; v[2] = ww * logr;
+                v[3] = v[4] = v[5] = v[6] = v[7] = 0.f;
+                if constexpr (NX > 0) {
+                    const float4 Va = LA.V[i], Vb = SB.V[j];
+                    float x[4] = {0.f, 0.f, 0.f, 0.f};
+                    pair_products<GEO, KIND>(T, Pa, Qa, Va, Pb, Qb, Vb, dx, dy, dz, dsq, r,
+                                             logr, x);
+#pragma unroll
+                    for (int q = 0; q < NX; ++q) v[3 + q] = x[q];
+                }
+                const unsigned nn = (unsigned)__float_as_int(Qa.w) * (unsigned)__float_as_int(Qb.w);
+                if (k == kref) {
+#pragma unroll
+                    for (int q = 0; q < 7; ++q) acc0[q] += v[q];
+                    c0 += nn;
+                } else if (k == kref + 1) {
+#pragma unroll
+                    for (int q = 0; q < 7; ++q) acc1[q] += v[q];
+                    c1 += nn;
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 7; ++q)
+                        if (q < nq) atomicAdd(&fb[q * nb + k], v[q]);
+                    if (!quick) atomicAdd(&np[k], (unsigned long long)nn);
+                }
+            }
+            // The tile's two register bins into the warp's FP32 bins.  With single-point
+            // leaves a lane counts at most 32 pairs, so the warp's u32 sum is exact; list
+            // leaves add their per-lane counts (n1 n2 each) one by one.
+            const bool single = sA && sB;
+            tile_bin_out(acc0, c0, kref, nq, nb, fb, np, quick, single, lane);
+            tile_bin_out(acc1, c1, kref + 1, nq, nb, fb, np, quick, single, lane);
+            if (++since_flush >= TFLUSH) {
+                since_flush = 0;
+                __syncwarp();
+                for (int q = lane; q < nq * nb; q += 32) {
+                    const float x = fb[q];
+                    if (x != 0.f) {
+                        float2 f = fd[q];
+                        df_add(f, x);
+                        fd[q] = f;
+                        fb[q] = 0.f;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+        __syncwarp();
+        for (int q = lane; q < nq * nb; q += 32) {
+            float2 f = fd[q];
+            df_add(f, fb[q]);
+            fd[q] = f;
+        }
+        __syncwarp();
+        double* wa = T.wacc + (size_t)(T.tile_wbase + gw) * nq * nb;
+        for (int q = lane; q < nq * nb; q += 32) wa[q] += df_value(fd[q]);
+        unsigned long long* wn = T.wnp + (size_t)(T.tile_wbase + gw) * nb;
+        for (int q = lane; q < nb; q += 32) wn[q] += np[q];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        n_acc += __shfl_xor_sync(0xffffffffu, n_acc, o);
+        n_pairs += __shfl_xor_sync(0xffffffffu, n_pairs, o);
+        n_esc += __shfl_xor_sync(0xffffffffu, n_esc, o);
+    }
+    if (lane == 0 && n_tiles) {
+        atomicAdd(&T.counters[1], (unsigned long long)n_acc);
+        atomicAdd(&T.tctl[2], (unsigned long long)n_tiles);
+        atomicAdd(&T.tctl[3], (unsigned long long)n_pairs);
+        atomicAdd(&T.tctl[4], (unsigned long long)n_esc);
+    }
+    // The last block to finish empties the tile list for the next expansion launch.
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned long long prev = atomicAdd(&T.tctl[1], 1ull);
+        if (prev == (unsigned long long)gridDim.x - 1) {
+            T.tctl[0] = 0ull;
+            T.tctl[1] = 0ull;
+            __threadfence();
+        }
+    }
+}
+
+using TileKernel = void (*)(TravParams);
+
+template <int GEO>
+TileKernel pick_kind(const TravParams& T)
+{
+    if (T.k1 == DN && T.k2 == DN) return k_tiles<GEO, TK_NN>;
+    if (T.k2 != DG) return k_tiles<GEO, TK_SC>;
+    if (T.k1 == DG && T.s1 == 2 && T.s2 == 2) return k_tiles<GEO, TK_GG>;
+    return k_tiles<GEO, TK_GEN>;
+}
+
+TileKernel pick(const TravParams& T)
+{
+    if (T.coords == FLAT) return pick_kind<TG_FLAT>(T);
+    if (T.coords == SPHERE) return T.metric == ARC ? pick_kind<TG_ARC>(T) : pick_kind<TG_SPHEUC>(T);
+    return pick_kind<TG_3D>(T);
+}
+
+}  // namespace
+
+int tiles_grid(const TravParams& T, int* blocks, int* nwarps)
+{
+    int dev = 0, nsm = 0, per = 0;
+    TC_CU(cudaGetDevice(&dev));
+    TC_CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const size_t sm = warp_bytes(T.nqf, T.nbins) * TWPB;
+    const TileKernel k = pick(T);
+    if (sm > 48 * 1024)
+        TC_CU(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    TC_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, TPB, sm));
+    if (per < 1) per = 1;
+    *blocks = nsm * per;
+    *nwarps = *blocks * TWPB;
+    return 0;
+}
+
+int launch_tiles(const TravParams& T, cudaStream_t st)
+{
+    const size_t sm = warp_bytes(T.nqf, T.nbins) * TWPB;
+    count_launch();
+    pick(T)<<<T.tile_blocks, TPB, sm, st>>>(T);
+    return 0;
+}
+
+}  // namespace tc

@@ -66,6 +66,20 @@ struct TravParams {
     const int2* ppairs;
     const int* ptop;
     const int* ptop_off;
+    // Leaf-pair tiles (exact mode: every accepted pair is a pair of leaves, which holds for
+    // angle_slop = 0 or two brute fields).  A cell pair that must be split while both cells
+    // hold at most tile_leaf points becomes a tile (c1, c2), and a self item on such a cell a
+    // self tile (c, -2 - c); k_tiles evaluates every leaf pair of a tile.  The leaf starting
+    // at point p of field 1 (2) has cell id leaf_base1 (leaf_base2) + p.
+    int tile_leaf;                  // 0: no tiles
+    int leaf_base1, leaf_base2;
+    int2* tiles;
+    unsigned long long* tctl;       // [0] tiles waiting, [1] blocks of k_tiles done,
+                                    // [2] tiles, [3] leaf pairs evaluated, [4] escalated
+    long long tile_cap;
+    int tile_blocks, tile_wbase;    // k_tiles grid; its warps' slots start at tile_wbase
+    const float* tile_edge;         // [nbins+1]: 1 / (min_sep^2 exp(2 k bin_size))
+    const float* tile_ledge;        // [nbins+1]: log(min_sep) + k bin_size
 };
 
 // Fixed traversal scratch of the allocation-free entry point (traverse2pt.cu).
@@ -116,6 +130,11 @@ int expand_grid(int nq, int nb, int* blocks, int* nwarps, int mode = 0);
 // Enqueues `iters` (schedule, expand) pairs on st without synchronising.
 int launch_expand_batch(const TravParams& T, int blocks, ExpandSched* dS, int iters,
                         cudaStream_t st);
+// Leaf-pair tiles (tiles.cu): the leaf size of a tile side, the k_tiles grid for a traversal
+// (its blocks fill every SM), and one k_tiles launch over the tiles waiting in T.tiles.
+static constexpr int TILE_LEAF = 32;
+int tiles_grid(const TravParams& T, int* blocks, int* nwarps);
+int launch_tiles(const TravParams& T, cudaStream_t st);
 int launch_reduce(int nwarps, int nq, int nb, const double* wacc, const unsigned long long* wnp,
                   double* out, unsigned long long* outnp, cudaStream_t st);
 
