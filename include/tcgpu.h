@@ -88,6 +88,8 @@ typedef struct tc_stats {
     int64_t tiles;           /* leaf-pair tiles of the exact mode (angle_slop 0 or brute) */
     int64_t tile_pairs;      /* leaf pairs evaluated in tiles (accepted ones are in accepted) */
     int64_t tile_escalated;  /* tile leaf pairs decided again in FP64 near a bin edge */
+    double  expand_ms;       /* device time of the expansion launches (k_expand) */
+    double  tiles_ms;        /* device time of the tile launches (k_tiles) */
 } tc_stats;
 
 /* Field construction: replaces BuildNField / BuildKField / BuildZField / BuildVField /

@@ -32,7 +32,8 @@ class tc_stats(ctypes.Structure):
                 ("escalated", ctypes.c_int64), ("launches", ctypes.c_int64),
                 ("build_ms", ctypes.c_double), ("traverse_ms", ctypes.c_double),
                 ("learned", ctypes.c_int64), ("tiles", ctypes.c_int64),
-                ("tile_pairs", ctypes.c_int64), ("tile_escalated", ctypes.c_int64)]
+                ("tile_pairs", ctypes.c_int64), ("tile_escalated", ctypes.c_int64),
+                ("expand_ms", ctypes.c_double), ("tiles_ms", ctypes.c_double)]
 
 
 _lib = None

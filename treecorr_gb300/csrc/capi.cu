@@ -120,6 +120,8 @@ struct tc_corr2 {
     long long tile_cap = 0;
     unsigned long long* tctl = nullptr;
     float* tedge = nullptr;              // [2][nbins+1]: 1/edge^2, log(edge)
+    std::vector<cudaEvent_t> kev;        // per-launch events of an expansion batch
+    ~tc_corr2() { for (auto e : kev) cudaEventDestroy(e); }
 };
 
 namespace {
@@ -516,12 +518,26 @@ int expand_run(tc_corr2* c, const TravParams& T, int blocks, long long npoints, 
     TC_CU(cudaMemcpyAsync(c->sched, &hs, sizeof(hs), cudaMemcpyHostToDevice, st));
     int derr = 0;
     long long launches = 0;
+    // Device time of the expansion and tile kernels, from events around every launch.
+    constexpr int BATCH = 64;
+    if (c->kev.empty()) {
+        c->kev.resize(3 * BATCH);
+        for (auto& e : c->kev) TC_CU(cudaEventCreate(&e));
+    }
+    double expand_ms = 0., tiles_ms = 0.;
     for (int batch = 0;; ++batch) {
-        TC_TRY(launch_expand_batch(T, blocks, c->sched, 64, st));
+        TC_TRY(launch_expand_batch(T, blocks, c->sched, BATCH, st, c->kev.data()));
         int flags[3];
         TC_CU(cudaMemcpyAsync(flags, &c->sched->done, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
         TC_CU(cudaMemcpyAsync(&derr, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
         TC_CU(cudaStreamSynchronize(st));
+        for (int it = 0; it < BATCH; ++it) {
+            float a = 0.f, b = 0.f;
+            TC_CU(cudaEventElapsedTime(&a, c->kev[3 * it], c->kev[3 * it + 1]));
+            TC_CU(cudaEventElapsedTime(&b, c->kev[3 * it + 1], c->kev[3 * it + 2]));
+            expand_ms += a;
+            tiles_ms += b;
+        }
         if (derr) break;
         if (flags[1]) {   // need_levels: the expansion reached the last allocated level
             if (nlev >= EXP_MAXLEV) {
@@ -551,6 +567,8 @@ int expand_run(tc_corr2* c, const TravParams& T, int blocks, long long npoints, 
     TC_CU(cudaStreamSynchronize(st));
     *derr_out = derr;
     *launches_out = launches;
+    c->stats.expand_ms = expand_ms;
+    c->stats.tiles_ms = tiles_ms;
     return TC_OK;
 }
 
@@ -701,7 +719,7 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
     c->stats.learned = (int64_t)cntr[3];
     c->stats.launches = launches_done;
     c->stats.traverse_ms = ms;
-    c->stats.tiles = (int64_t)tcnt[2];
+    c->stats.tiles = tiles ? (int64_t)tcnt[2] : 0;
     c->stats.tile_pairs = (int64_t)tcnt[3];
     c->stats.tile_escalated = (int64_t)tcnt[4];
     // Corr2::finishProcess adds into the caller's arrays (src/Corr2.cpp:527-566).

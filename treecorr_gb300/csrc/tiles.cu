@@ -51,11 +51,13 @@ constexpr int TMINB = TILES_MINB; // resident blocks per SM the registers are si
 enum { TG_FLAT = 0, TG_ARC = 1, TG_SPHEUC = 2, TG_3D = 3 };   // geometry
 enum { TK_NN = 0, TK_SC = 1, TK_GEN = 2, TK_GG = 3 };           // class family
 
-// One side of a tile: its valid leaves (n > 0, w != 0) in point order.
+// One side of a tile: its valid leaves (n > 0, w != 0) in point order.  Pair loops read P and
+// W of both sides (two 16-byte shared loads per side) and X only where it is needed.
 struct TileLeaves {
     float4 P[32];   // (ox, oy, oz, z / 2): offset from B's centre, half the z coordinate
-    float4 Q[32];   // (x, y, w, n bits): position (FP32), weight, count
-    float4 V[32];   // (d1, d2, id bits, s): payload, leaf cell id, scalar payload (w or w k)
+    float4 W[32];   // (w, p1, p2, n bits): weight, payload (p1 = w for N, w k for K, w g for
+                    // complex kinds), point count
+    float4 X[32];   // (x, y, id bits, 0): FP32 position (sphere projections), leaf cell id
 };
 
 __host__ __device__ inline size_t bins_bytes(int nq, int nb)
@@ -70,15 +72,15 @@ __host__ __device__ inline size_t warp_bytes(int nq, int nb)
 
 // Stages the valid leaves of cell c (points [start, start + n), leaf ids base + p) with their
 // offsets from the centre (ch + cl).  Returns the count; *single is false when a staged leaf
-// holds more than one point.
-__device__ __forceinline__ int stage(const TCell* cells, int base, float4 ca, float4 cb,
-                                     float4 cc, float4 cd, float chx, float chy, float chz,
-                                     float clx, float cly, float clz, int kind, TileLeaves& S,
-                                     int lane, float& on1, float& on2, bool& single)
+// holds more than one point.  on1 / on2: the L1 norm and the length of the lane's offset.
+__device__ __forceinline__ int stage(const TCell* cells, int base, float4 cc, float4 cd,
+                                     float chx, float chy, float chz, float clx, float cly,
+                                     float clz, int kind, TileLeaves& S, int lane, float& on1,
+                                     float& on2, bool& single)
 {
     const int start = __float_as_int(cd.z), n = __float_as_int(cc.z);
     bool v = false;
-    float4 P = make_float4(0.f, 0.f, 0.f, 0.f), Q = P, V = P;
+    float4 P = make_float4(0.f, 0.f, 0.f, 0.f), W = P, X = P;
     int nn = 0;
     if (lane < n) {
         const int id = base + start + lane;
@@ -88,18 +90,18 @@ __device__ __forceinline__ int stage(const TCell* cells, int base, float4 ca, fl
         if (v) {
             P = make_float4((a.x - chx) + (b.x - clx), (a.y - chy) + (b.y - cly),
                             (a.z - chz) + (b.z - clz), 0.5f * a.z);
-            Q = make_float4(a.x, a.y, b.w, __int_as_float(nn));
-            V = make_float4(c.x, c.y, __int_as_float(id), kind == DN ? b.w : c.x);
+            W = make_float4(b.w, kind == DN ? b.w : c.x, c.y, __int_as_float(nn));
+            X = make_float4(a.x, a.y, __int_as_float(id), 0.f);
         }
     }
     const unsigned m = __ballot_sync(0xffffffffu, v);
     single = __all_sync(0xffffffffu, !v || nn == 1);
     if (v) {
         const int p = __popc(m & ((1u << lane) - 1u));
-        S.P[p] = P; S.Q[p] = Q; S.V[p] = V;
+        S.P[p] = P; S.W[p] = W; S.X[p] = X;
     }
-    on1 = fabsf(P.x) + fabsf(P.y) + fabsf(P.z);    // L1 norm of the offset
-    on2 = sqrtf(P.x * P.x + P.y * P.y + P.z * P.z); // its length
+    on1 = fabsf(P.x) + fabsf(P.y) + fabsf(P.z);
+    on2 = sqrtf(P.x * P.x + P.y * P.y + P.z * P.z);
     return __popc(m);
 }
 
@@ -173,82 +175,95 @@ __device__ __noinline__ int leaf_pair64(const TravParams& T, int ida, int idb, b
 }
 
 // The generic values of an accepted leaf pair (every class, with the projections of
-// accept_values).  Out of line for the same reason.
-__device__ __noinline__ void leaf_values_generic(const TravParams& T, float4 Pa, float4 Qa,
-                                                 float4 Va, float4 Pb, float4 Qb, float4 Vb,
+// accept_values); x = the correlation products.  Out of line: it serves the rarer classes.
+__device__ __noinline__ void leaf_values_generic(const TravParams& T, float4 Pa, float4 Wa,
+                                                 float4 Xa, float4 Pb, float4 Wb, float4 Xb,
                                                  float dx, float dy, float dz, float dsq,
-                                                 float r, float logr, float* out)
+                                                 float r, float logr, float* x)
 {
     TCell A, B;
-    A.a = make_float4(Qa.x, Qa.y, 2.f * Pa.w, 0.f);
-    A.b = make_float4(0.f, 0.f, 0.f, Qa.z);
-    A.c = make_float4(Va.x, Va.y, Qa.w, 0.f);
+    A.a = make_float4(Xa.x, Xa.y, 2.f * Pa.w, 0.f);
+    A.b = make_float4(0.f, 0.f, 0.f, Wa.x);
+    A.c = make_float4(Wa.y, Wa.z, Wa.w, 0.f);
     A.d = make_float4(0.f, 0.f, 0.f, 0.f);
-    B.a = make_float4(Qb.x, Qb.y, 2.f * Pb.w, 0.f);
-    B.b = make_float4(0.f, 0.f, 0.f, Qb.z);
-    B.c = make_float4(Vb.x, Vb.y, Qb.w, 0.f);
+    B.a = make_float4(Xb.x, Xb.y, 2.f * Pb.w, 0.f);
+    B.b = make_float4(0.f, 0.f, 0.f, Wb.x);
+    B.c = make_float4(Wb.y, Wb.z, Wb.w, 0.f);
     B.d = A.d;
     float av[7] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     unsigned long long nn = 0;
-    accept_values(T, A, B, __float_as_int(Va.z), __float_as_int(Vb.z), dx, dy, dz, dsq, r, logr,
+    accept_values(T, A, B, __float_as_int(Xa.z), __float_as_int(Xb.z), dx, dy, dz, dsq, r, logr,
                   av, nn);
 #pragma unroll
-    for (int q = 3; q < 7; ++q) out[q - 3] = av[q];
+    for (int q = 3; q < 7; ++q) x[q - 3] = av[q];
 }
 
-// The correlation products of one leaf pair (quantities 3.. of the bins).
+// The correlation products of one leaf pair (quantities 3.. of the bins) as x * sc.
 template <int GEO, int KIND>
-__device__ __forceinline__ void pair_products(const TravParams& T, float4 Pa, float4 Qa,
-                                              float4 Va, float4 Pb, float4 Qb, float4 Vb,
-                                              float dx, float dy, float dz, float dsq, float r,
-                                              float logr, float (&x)[4])
+__device__ __forceinline__ void pair_products(const TravParams& T, const TileLeaves& LA,
+                                              const TileLeaves& SB, int i, int j, float4 Pa,
+                                              float4 Wa, float4 Pb, float4 Wb, float dx,
+                                              float dy, float dz, float dsq, float r, float logr,
+                                              float (&x)[4], float& sc)
 {
+    sc = 1.f;
     if constexpr (KIND == TK_SC) {
-        x[0] = Va.w * Vb.w;                                  // wk1 wk2 (DirectHelper<1>)
+        x[0] = Wa.y * Wb.y;                                  // wk1 wk2 (DirectHelper<1>)
     } else if constexpr (KIND == TK_GG && GEO == TG_FLAT) {
         // ProjectHelper<Flat>: both shears rotated by exp(-2i alpha) of r = p2 - p1, so
         // g1 conj(g2) is unchanged and g1 g2 turns by exp(-4i alpha) = conj(r)^4 / |r|^4.
-        const float g1r = Va.x, g1i = Va.y, g2r = Vb.x, g2i = Vb.y;
-        x[0] = g1r * g2r + g1i * g2i;                        // xi+ = g1 conj(g2)
-        x[1] = g1i * g2r - g1r * g2i;
-        const float dx2 = dx * dx, dy2 = dy * dy;
-        const float er = dx2 - dy2, ei = -2.f * dx * dy;     // conj(r)^2 (r = -d)
-        const float e2r = er * er - ei * ei, e2i = 2.f * er * ei;
+        const float g1r = Wa.y, g1i = Wa.z, g2r = Wb.y, g2i = Wb.z;
+        x[0] = fmaf(g1r, g2r, g1i * g2i);                    // xi+ = g1 conj(g2)
+        x[1] = fmaf(g1i, g2r, -g1r * g2i);
+        const float er = fmaf(dx, dx, -dy * dy), ei = -2.f * dx * dy;   // conj(r)^2, r = -d
+        const float e2r = fmaf(er, er, -ei * ei), e2i = 2.f * er * ei;
         const float inv = __fdividef(1.f, dsq * dsq);
-        const float pr = g1r * g2r - g1i * g2i, pi = g1r * g2i + g1i * g2r;   // g1 g2
-        x[2] = (pr * e2r - pi * e2i) * inv;                  // xi-
-        x[3] = (pr * e2i + pi * e2r) * inv;
+        const float pr = fmaf(g1r, g2r, -g1i * g2i), pi = fmaf(g1r, g2i, g1i * g2r);   // g1 g2
+        x[2] = fmaf(pr, e2r, -pi * e2i) * inv;               // xi-
+        x[3] = fmaf(pr, e2i, pi * e2r) * inv;
     } else if constexpr (KIND == TK_GG && (GEO == TG_ARC || GEO == TG_SPHEUC)) {
         // ProjectHelper<Sphere>, include/ProjectHelper.h:272-388: directions at p2
         // (sinA, -cosA) and at p1 (-sinA, -cosB) on accurate differences (d = p1 - p2):
-        // y1 x2 - x1 y2 = x1 dy - y1 dx.  Spin 2: exp(-2i a) = conj(u)^2 / |u|^2; one
-        // reciprocal serves both normalisations.
-        const float sinA = Qa.x * dy - Qa.y * dx;
-        const float cosA = dz + Pb.w * dsq;
-        const float cosB = -dz + Pa.w * dsq;
+        // y1 x2 - x1 y2 = x1 dy - y1 dx.  Spin 2: exp(-2i a) = conj(u)^2 / |u|^2; the two
+        // normalisations are one reciprocal, applied as the scale sc.
+        const float4 Xa = LA.X[i];
+        const float sinA = fmaf(Xa.x, dy, -Xa.y * dx);
+        const float cosA = fmaf(Pb.w, dsq, dz);
+        const float cosB = fmaf(Pa.w, dsq, -dz);
         const float s2 = sinA * sinA;
         const float n2 = fmaf(cosA, cosA, s2), n1 = fmaf(cosB, cosB, s2);
         const float e2r = fmaf(-cosA, cosA, s2), e2i = 2.f * sinA * cosA;
         const float e1r = fmaf(-cosB, cosB, s2), e1i = -2.f * sinA * cosB;
-        const float inv = __fdividef(1.f, n1 * n2);
-        const float a2r = Vb.x * e2r - Vb.y * e2i, a2i = Vb.x * e2i + Vb.y * e2r;   // g2 e2
-        const float a1r = Va.x * e1r - Va.y * e1i, a1i = Va.x * e1i + Va.y * e1r;   // g1 e1
-        const float rr = a2r * a1r, ri = a2r * a1i, ir = a2i * a1r, ii = a2i * a1i;
-        x[0] = (rr + ii) * inv;     // both_complex_prod(g2, g1), include/ProjectHelper.h:84-101
-        x[1] = (ri - ir) * inv;
-        x[2] = (rr - ii) * inv;
-        x[3] = (ri + ir) * inv;
+        sc = __fdividef(1.f, n1 * n2);
+        const float a2r = fmaf(Wb.y, e2r, -Wb.z * e2i), a2i = fmaf(Wb.y, e2i, Wb.z * e2r);
+        const float a1r = fmaf(Wa.y, e1r, -Wa.z * e1i), a1i = fmaf(Wa.y, e1i, Wa.z * e1r);
+        // both_complex_prod(g2, g1), include/ProjectHelper.h:84-101.
+        x[0] = fmaf(a2r, a1r, a2i * a1i);     // xi+
+        x[1] = fmaf(a2r, a1i, -a2i * a1r);
+        x[2] = fmaf(a2r, a1r, -a2i * a1i);    // xi-
+        x[3] = fmaf(a2r, a1i, a2i * a1r);
     } else if constexpr (KIND == TK_GG || KIND == TK_GEN) {
-        leaf_values_generic(T, Pa, Qa, Va, Pb, Qb, Vb, dx, dy, dz, dsq, r, logr, x);
+        leaf_values_generic(T, Pa, Wa, LA.X[i], Pb, Wb, SB.X[j], dx, dy, dz, dsq, r, logr, x);
     }
 }
 
-// Adds a tile's register sums for bin kb (acc, count cn) into the warp's FP32 bins.
+// The great-circle angle from a chord c < 0.25 (the tile checks it): the Maclaurin series
+// of 2 asin(c / 2) to x^7, x = c / 2 (the first omitted term is below 2e-9 of x).
+__device__ __forceinline__ float arc_series(float c)
+{
+    const float x = 0.5f * c, x2 = x * x;
+    return 2.f * x * fmaf(x2, fmaf(x2, fmaf(x2, 5.f / 112.f, 3.f / 40.f), 1.f / 6.f), 1.f);
+}
+
+// Adds a tile's per-lane sums of one bin into the warp's FP32 bins.  acc: weight, sum w w r,
+// sum w w lr (lr = log2(r^2 / edge^2) of the tile's reference edge), products; the bin's
+// meanlogr sum is (ln 2 / 2) sum w w lr + log(edge) sum w w.
 __device__ __forceinline__ void tile_bin_out(float (&acc)[8], unsigned cn, int kb, int nq, int nb,
-                                             float* fb, unsigned long long* np, bool quick,
-                                             bool single, int lane)
+                                             float ledge, float* fb, unsigned long long* np,
+                                             bool quick, bool single, int lane)
 {
     if (!__any_sync(0xffffffffu, cn != 0u) || kb >= nb) return;
+    acc[2] = fmaf(acc[2], 0.5f * 0.69314718f, acc[0] * ledge);
     float tot;
     const bool holder = warp_sum8(acc, lane, tot);
     const int q = warp_sum8_index(lane);
@@ -264,6 +279,133 @@ __device__ __forceinline__ void tile_bin_out(float (&acc)[8], unsigned cn, int k
     __syncwarp();
 }
 
+// Everything a tile's pair loop needs besides its leaves.
+struct TileCtx {
+    int na, nbl, kref;
+    float inv_edge, ledge, emax, band_e, band_0;
+    bool self, interior, small_chord;
+};
+
+// The leaf pairs of a tile whose pairs all lie in range and in bin kref (and, on the sphere,
+// whose chords are below 0.25): no range test, no bin, no FP64.
+template <int GEO, int KIND>
+__device__ __forceinline__ void tile_fast(const TravParams& T, const TileLeaves& LA,
+                                          const TileLeaves& SB, const TileCtx& C, int lane,
+                                          float (&acc)[8], unsigned& cnt)
+{
+    const int nbl = C.nbl, npt = C.na * nbl;
+    int ii = lane / nbl, jj = lane - ii * nbl;
+    const int di = 32 / nbl, dj = 32 - di * nbl;
+    for (int p = lane; p < npt; p += 32) {
+        const int i = ii, j = jj;
+        jj += dj; ii += di;
+        if (jj >= nbl) { jj -= nbl; ++ii; }
+        const float4 Pa = LA.P[i], Wa = LA.W[i], Pb = SB.P[j], Wb = SB.W[j];
+        const float dx = Pa.x - Pb.x, dy = Pa.y - Pb.y;
+        const float dz = GEO == TG_FLAT ? 0.f : Pa.z - Pb.z;
+        const float dsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const float c = dsq * rsqrtf(dsq);
+        const float r = GEO == TG_ARC ? arc_series(c) : c;
+        const float lr = __log2f(r * r * C.inv_edge);
+        const float ww = Wa.x * Wb.x;
+        acc[0] += ww;
+        acc[1] = fmaf(ww, r, acc[1]);
+        acc[2] = fmaf(ww, lr, acc[2]);
+        if constexpr (KIND != TK_NN) {
+            float x[4] = {0.f, 0.f, 0.f, 0.f}, sc;
+            pair_products<GEO, KIND>(T, LA, SB, i, j, Pa, Wa, Pb, Wb, dx, dy, dz, dsq, r,
+                                     fmaf(lr, 0.5f * 0.69314718f, C.ledge), x, sc);
+            constexpr int NX = KIND == TK_SC ? 1 : 4;
+#pragma unroll
+            for (int q = 0; q < NX; ++q) acc[3 + q] = fmaf(x[q], sc, acc[3 + q]);
+        }
+        cnt += (unsigned)__float_as_int(Wa.w) * (unsigned)__float_as_int(Wb.w);
+    }
+}
+
+// The general pair loop: range test near min_sep / max_sep, the bin of every pair with its
+// FP32 error band, FP64 re-decision inside the band, self tiles (j > i).  Bins kref and
+// kref + 1 are summed in registers, other bins and FP64-decided pairs go to the warp's
+// shared-memory bins directly.
+template <int GEO, int KIND>
+__device__ __forceinline__ void tile_general(const TravParams& T, const TileLeaves& LA,
+                                             const TileLeaves& SB, const TileCtx& C, int lane,
+                                             float (&acc0)[8], float (&acc1)[8], unsigned& c0,
+                                             unsigned& c1, float* fb, unsigned long long* np,
+                                             unsigned& n_acc, unsigned& n_pairs,
+                                             unsigned& n_esc)
+{
+    const int nbl = C.nbl, npt = C.na * nbl, nb = T.nbins, nq = T.nqf;
+    const float ln2h = 0.5f * 0.69314718f;
+    const float ckk = ln2h * T.finvbinsize;
+    int ii = lane / nbl, jj = lane - ii * nbl;
+    const int di = 32 / nbl, dj = 32 - di * nbl;
+    for (int p = lane; p < npt; p += 32) {
+        const int i = ii, j = jj;
+        jj += dj; ii += di;
+        if (jj >= nbl) { jj -= nbl; ++ii; }
+        if (C.self && j <= i) continue;
+        ++n_pairs;
+        const float4 Pa = LA.P[i], Wa = LA.W[i], Pb = SB.P[j], Wb = SB.W[j];
+        const float dx = Pa.x - Pb.x, dy = Pa.y - Pb.y;
+        const float dz = GEO == TG_FLAT ? 0.f : Pa.z - Pb.z;
+        const float dsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const float invc = rsqrtf(dsq);
+        float r = dsq * invc;
+        if (GEO == TG_ARC) r = C.small_chord ? arc_series(r) : arc_from_chord_sq(dsq);
+        float lr = __log2f(r * r * C.inv_edge);
+        bool unsure = false;
+        int k = C.kref;
+        if (!C.interior) {
+            const float dr = C.emax + 4e-7f * r;
+            if (r + dr < T.fminsep || r - dr >= T.fmaxsep) continue;
+            unsure = !(r - dr >= T.fminsep && r + dr < T.fmaxsep);
+        }
+        if (!unsure) {
+            const float kk = lr * ckk;
+            const float fk = floorf(kk);
+            const float fr = kk - fk;
+            const float band = fmaf(C.band_e, invc, C.band_0);
+            k = C.kref + (int)fk;
+            unsure = fr < band || fr > 1.f - band || k < 0;
+            if (k >= nb) k = nb - 1;                    // the clamp of src/Corr2.cpp:514
+        }
+        float logr = fmaf(lr, ln2h, C.ledge);
+        if (unsure) {
+            ++n_esc;
+            k = leaf_pair64(T, __float_as_int(LA.X[i].z), __float_as_int(SB.X[j].z), C.self, &r,
+                            &logr);
+            if (k < 0) continue;
+        }
+        ++n_acc;
+        const float ww = Wa.x * Wb.x;
+        float v[8] = {ww, ww * r, ww * lr, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if constexpr (KIND != TK_NN) {
+            float x[4] = {0.f, 0.f, 0.f, 0.f}, sc;
+            pair_products<GEO, KIND>(T, LA, SB, i, j, Pa, Wa, Pb, Wb, dx, dy, dz, dsq, r, logr,
+                                     x, sc);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) v[3 + q] = x[q] * sc;
+        }
+        const unsigned nn = (unsigned)__float_as_int(Wa.w) * (unsigned)__float_as_int(Wb.w);
+        if (!unsure && k == C.kref) {
+#pragma unroll
+            for (int q = 0; q < 7; ++q) acc0[q] += v[q];
+            c0 += nn;
+        } else if (!unsure && k == C.kref + 1) {
+#pragma unroll
+            for (int q = 0; q < 7; ++q) acc1[q] += v[q];
+            c1 += nn;
+        } else {
+            v[2] = ww * logr;   // the FP64 pair's own log r, or the tile edge's
+#pragma unroll
+            for (int q = 0; q < 7; ++q)
+                if (q < nq) atomicAdd(&fb[q * nb + k], v[q]);
+            if (!T.quick) atomicAdd(&np[k], (unsigned long long)nn);
+        }
+    }
+}
+
 template <int GEO, int KIND>
 __global__ void __launch_bounds__(TPB, TMINB) k_tiles(const __grid_constant__ TravParams T)
 {
@@ -272,7 +414,6 @@ __global__ void __launch_bounds__(TPB, TMINB) k_tiles(const __grid_constant__ Tr
     const int wib = threadIdx.x >> 5;
     const int gw = blockIdx.x * TWPB + wib;
     const int nq = T.nqf, nb = T.nbins;
-    constexpr int NX = KIND == TK_NN ? 0 : (KIND == TK_SC ? 1 : 4);   // products per pair
     // Tiles waiting; an expansion launch that ran out of room counted past the capacity (and
     // raised DEV_SPILL_OVERFLOW), so never read beyond it.
     long long nt = (long long)*(volatile unsigned long long*)&T.tctl[0];
@@ -290,160 +431,92 @@ __global__ void __launch_bounds__(TPB, TMINB) k_tiles(const __grid_constant__ Tr
         for (int q = lane; q < nq * nb; q += 32) { fd[q] = make_float2(0.f, 0.f); fb[q] = 0.f; }
         for (int q = lane; q < nb; q += 32) np[q] = 0ull;
         __syncwarp();
-        const float ln2h = 0.5f * 0.69314718f;          // log(r) per unit of log2(r^2)
-        const float ckk = ln2h * T.finvbinsize;          // bins per unit of log2(r^2)
+        const float ckk = 0.5f * 0.69314718f * T.finvbinsize;   // bins per unit of log2(r^2)
         const bool quick = T.quick != 0;
         int since_flush = 0;
         for (long long t = gw; t < nt; t += nwt) {
             const int2 tile = T.tiles[t];
-            const bool self = tile.y < 0;
-            const int ia = tile.x, ib = self ? -2 - tile.y : tile.y;
-            const TCell* cB = self ? T.c1 : T.c2;
-            const int baseB = self ? T.leaf_base1 : T.leaf_base2;
+            TileCtx C;
+            C.self = tile.y < 0;
+            const int ia = tile.x, ib = C.self ? -2 - tile.y : tile.y;
+            const TCell* cB = C.self ? T.c1 : T.c2;
+            const int baseB = C.self ? T.leaf_base1 : T.leaf_base2;
             const float4 Aa = T.c1[ia].a, Ab = T.c1[ia].b, Ac = T.c1[ia].c, Ad = T.c1[ia].d;
             const float4 Ba = cB[ib].a, Bb = cB[ib].b, Bc = cB[ib].c, Bd = cB[ib].d;
             ++n_tiles;
             float eA, rA, eB, rB;
             bool sA, sB;
-            const int nbl = stage(cB, baseB, Ba, Bb, Bc, Bd, Ba.x, Ba.y, Ba.z, Bb.x, Bb.y, Bb.z,
-                                  T.k2, SB, lane, eB, rB, sB);
-            int na = nbl;
+            C.nbl = stage(cB, baseB, Bc, Bd, Ba.x, Ba.y, Ba.z, Bb.x, Bb.y, Bb.z, T.k2, SB, lane,
+                          eB, rB, sB);
+            C.na = C.nbl;
             // A's offsets are also taken from B's centre; D = centre A - centre B.
             const float Dx = (Aa.x - Ba.x) + (Ab.x - Bb.x), Dy = (Aa.y - Ba.y) + (Ab.y - Bb.y);
             const float Dz = GEO == TG_FLAT ? 0.f : (Aa.z - Ba.z) + (Ab.z - Bb.z);
-            if (!self) {
-                float on1, on2;
-                na = stage(T.c1, T.leaf_base1, Aa, Ab, Ac, Ad, Ba.x, Ba.y, Ba.z, Bb.x, Bb.y,
-                           Bb.z, T.k1, SA, lane, on1, on2, sA);
-                eA = on1;
+            if (!C.self) {
+                float on2;
+                C.na = stage(T.c1, T.leaf_base1, Ac, Ad, Ba.x, Ba.y, Ba.z, Bb.x, Bb.y, Bb.z, T.k1,
+                             SA, lane, eA, on2, sA);
                 // Distance of A's leaf from A's centre.
-                const float4 P = lane < na ? SA.P[lane] : make_float4(Dx, Dy, Dz, 0.f);
+                __syncwarp();
+                const float4 P = lane < C.na ? SA.P[lane] : make_float4(Dx, Dy, Dz, 0.f);
                 const float ux = P.x - Dx, uy = P.y - Dy, uz = P.z - Dz;
-                rA = lane < na ? sqrtf(ux * ux + uy * uy + uz * uz) : 0.f;
+                rA = sqrtf(ux * ux + uy * uy + uz * uz);
             } else {
                 eA = eB; rA = rB; sA = sB;
             }
             __syncwarp();
-            if (na == 0 || nbl == 0) continue;
-            const TileLeaves& LA = self ? SB : SA;
+            if (C.na == 0 || C.nbl == 0) continue;
+            const TileLeaves& LA = C.self ? SB : SA;
             // Tile bounds.  emax bounds |FP32 d - d| of every pair (each offset within 2 ulps
             // of its L1 size, the difference one more; a 1.5x margin); the separation of any
             // pair lies within |D| +- (rA + rB).
-            const float emax = 2.7e-7f * (warp_max(eA) + warp_max(eB)) + 1e-30f;
+            C.emax = 2.7e-7f * (warp_max(eA) + warp_max(eB)) + 1e-30f;
             const float rAB = warp_max(rA) + warp_max(rB);
             const float Dn = sqrtf(Dx * Dx + Dy * Dy + Dz * Dz);
-            const float slack = emax + 2e-6f * (Dn + rAB);
+            const float slack = C.emax + 2e-6f * (Dn + rAB);
             float lo = fmaxf(Dn - rAB - slack, 0.f), hi = Dn + rAB + slack;
+            C.small_chord = hi < 0.25f;
             if (GEO == TG_ARC) { lo = arc_from_chord_sq(lo * lo); hi = arc_from_chord_sq(hi * hi); }
             lo *= 1.f - 1e-5f;
             hi *= 1.f + 1e-5f;
             if (lo >= T.fmaxsep || hi < T.fminsep) continue;   // no pair in range
-            const bool interior = lo >= T.fminsep && hi < T.fmaxsep;
-            int klo = (int)floorf(log2f(fmaxf(lo, T.fminsep) * fmaxf(lo, T.fminsep) *
-                                        T.finvminsepsq) * ckk);
-            int khi = (int)floorf(log2f(fminf(hi, T.fmaxsep) * fminf(hi, T.fmaxsep) *
-                                        T.finvminsepsq) * ckk);
+            C.interior = lo >= T.fminsep && hi < T.fmaxsep;
+            // Bins of the bounds: __log2f is within 2^-22 (or 2 ulps of a result <= 17) of
+            // log2, far inside the 1e-5 margins above.
+            const float lb = fmaxf(lo, T.fminsep), hb = fminf(hi, T.fmaxsep);
+            int klo = (int)floorf(__log2f(lb * lb * T.finvminsepsq) * ckk);
+            int khi = (int)floorf(__log2f(hb * hb * T.finvminsepsq) * ckk);
             klo = klo < 0 ? 0 : (klo > nb - 1 ? nb - 1 : klo);
             khi = khi < 0 ? 0 : (khi > nb - 1 ? nb - 1 : khi);
-            const bool one_bin = interior && klo == khi;
-            const int kref = klo;
-            const float inv_edge = T.tile_edge[kref];     // 1 / (lower edge of kref)^2
-            const float ledge = T.tile_ledge[kref];       // log of that edge
+            C.kref = klo;
+            C.inv_edge = T.tile_edge[klo];     // 1 / (lower edge of kref)^2
+            C.ledge = T.tile_ledge[klo];       // log of that edge
             // Band (in bins) outside which the FP32 bin is certain: r's relative error
             // (emax / chord + 4e-7) and __log2f's (2^-22 absolute on [0.5, 2], else 2 ulps;
             // |log2| <= lmax here), the roundings of its argument and of kk.
-            const float lmax = fmaxf(fabsf(log2f(hi * hi * inv_edge)), 1.f);
-            const float band_e = emax * T.finvbinsize;
-            const float band_0 = 4e-7f * T.finvbinsize + (5e-7f + 3e-7f * lmax) * ckk +
-                                 1.2e-7f * (lmax * ckk) + 1e-7f;
-            const int npt = na * nbl;
-            const int iters = (npt + 31) >> 5;
-            int ii = lane / nbl, jj = lane - (lane / nbl) * nbl;
-            const int di = 32 / nbl, dj = 32 - di * nbl;
+            const float lmax = fmaxf(fabsf(__log2f(hi * hi * C.inv_edge)), 1.f);
+            C.band_e = C.emax * T.finvbinsize;
+            C.band_0 = 4e-7f * T.finvbinsize + (5e-7f + 4.2e-7f * lmax) * ckk + 1e-7f;
             float acc0[8], acc1[8];
 #pragma unroll
             for (int q = 0; q < 8; ++q) { acc0[q] = 0.f; acc1[q] = 0.f; }
             unsigned c0 = 0u, c1 = 0u;
-            for (int it = 0; it < iters; ++it) {
-                const int i = ii, j = jj;
-                jj += dj; ii += di;
-                if (jj >= nbl) { jj -= nbl; ++ii; }
-                const bool use = (it * 32 + lane < npt) && (!self || j > i);
-                if (!use) continue;
-                ++n_pairs;
-                const float4 Pa = LA.P[i], Pb = SB.P[j];
-                const float4 Qa = LA.Q[i], Qb = SB.Q[j];
-                const float dx = Pa.x - Pb.x, dy = Pa.y - Pb.y;
-                const float dz = GEO == TG_FLAT ? 0.f : Pa.z - Pb.z;
-                const float dsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                const float invc = rsqrtf(dsq);
-                float r = dsq * invc;                       // chord (or flat) length
-                if (GEO == TG_ARC) r = arc_from_chord_sq(dsq);
-                const float rsq = r * r;
-                int k = kref;
-                float lr = __log2f(rsq * inv_edge);
-                float logr = fmaf(lr, ln2h, ledge);
-                if (!one_bin) {
-                    bool unsure = false;
-                    bool drop = false;
-                    if (!interior) {
-                        const float dr = emax + 4e-7f * r;
-                        if (r + dr < T.fminsep || r - dr >= T.fmaxsep) drop = true;
-                        else if (!(r - dr >= T.fminsep && r + dr < T.fmaxsep)) unsure = true;
-                    }
-                    if (drop) continue;
-                    if (!unsure) {
-                        const float kk = lr * ckk;
-                        const float fk = floorf(kk);
-                        const float fr = kk - fk;
-                        const float band = fmaf(band_e, invc, band_0);
-                        if (fr < band || fr > 1.f - band) unsure = true;
-                        k = kref + (int)fk;
-                        if (k >= nb) k = nb - 1;            // src/Corr2.cpp:514
-                        if (k < 0) unsure = true;
-                    }
-                    if (unsure) {
-                        ++n_esc;
-                        k = leaf_pair64(T, __float_as_int(LA.V[i].z), __float_as_int(SB.V[j].z),
-                                        self, &r, &logr);
-                        if (k < 0) continue;
-                    }
-                }
-                ++n_acc;
-                const float ww = Qa.z * Qb.z;
-                float v[8];
-                v[0] = ww; v[1] = ww * r; v[2] = ww * logr;
-                v[3] = v[4] = v[5] = v[6] = v[7] = 0.f;
-                if constexpr (NX > 0) {
-                    const float4 Va = LA.V[i], Vb = SB.V[j];
-                    float x[4] = {0.f, 0.f, 0.f, 0.f};
-                    pair_products<GEO, KIND>(T, Pa, Qa, Va, Pb, Qb, Vb, dx, dy, dz, dsq, r,
-                                             logr, x);
-#pragma unroll
-                    for (int q = 0; q < NX; ++q) v[3 + q] = x[q];
-                }
-                const unsigned nn = (unsigned)__float_as_int(Qa.w) * (unsigned)__float_as_int(Qb.w);
-                if (k == kref) {
-#pragma unroll
-                    for (int q = 0; q < 7; ++q) acc0[q] += v[q];
-                    c0 += nn;
-                } else if (k == kref + 1) {
-#pragma unroll
-                    for (int q = 0; q < 7; ++q) acc1[q] += v[q];
-                    c1 += nn;
-                } else {
-#pragma unroll
-                    for (int q = 0; q < 7; ++q)
-                        if (q < nq) atomicAdd(&fb[q * nb + k], v[q]);
-                    if (!quick) atomicAdd(&np[k], (unsigned long long)nn);
-                }
+            const bool fast = C.interior && klo == khi && !C.self &&
+                              (GEO != TG_ARC || C.small_chord);
+            if (fast) {
+                tile_fast<GEO, KIND>(T, LA, SB, C, lane, acc0, c0);
+                if (lane == 0) { n_pairs += C.na * C.nbl; n_acc += C.na * C.nbl; }
+            } else {
+                tile_general<GEO, KIND>(T, LA, SB, C, lane, acc0, acc1, c0, c1, fb, np, n_acc,
+                                        n_pairs, n_esc);
             }
-            // The tile's two register bins into the warp's FP32 bins.  With single-point
-            // leaves a lane counts at most 32 pairs, so the warp's u32 sum is exact; list
-            // leaves add their per-lane counts (n1 n2 each) one by one.
+            // The tile's register bins into the warp's FP32 bins.  With single-point leaves a
+            // lane counts at most 32 pairs, so the warp's u32 sum is exact; list leaves add
+            // their per-lane counts (n1 n2 each) one by one.
             const bool single = sA && sB;
-            tile_bin_out(acc0, c0, kref, nq, nb, fb, np, quick, single, lane);
-            tile_bin_out(acc1, c1, kref + 1, nq, nb, fb, np, quick, single, lane);
+            tile_bin_out(acc0, c0, C.kref, nq, nb, C.ledge, fb, np, quick, single, lane);
+            if (!fast)
+                tile_bin_out(acc1, c1, C.kref + 1, nq, nb, C.ledge, fb, np, quick, single, lane);
             if (++since_flush >= TFLUSH) {
                 since_flush = 0;
                 __syncwarp();
@@ -471,17 +544,18 @@ __global__ void __launch_bounds__(TPB, TMINB) k_tiles(const __grid_constant__ Tr
         unsigned long long* wn = T.wnp + (size_t)(T.tile_wbase + gw) * nb;
         for (int q = lane; q < nb; q += 32) wn[q] += np[q];
     }
+    unsigned long long a64 = n_acc, p64 = n_pairs, e64 = n_esc, t64 = n_tiles;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        n_acc += __shfl_xor_sync(0xffffffffu, n_acc, o);
-        n_pairs += __shfl_xor_sync(0xffffffffu, n_pairs, o);
-        n_esc += __shfl_xor_sync(0xffffffffu, n_esc, o);
+        a64 += __shfl_xor_sync(0xffffffffu, a64, o);
+        p64 += __shfl_xor_sync(0xffffffffu, p64, o);
+        e64 += __shfl_xor_sync(0xffffffffu, e64, o);
     }
-    if (lane == 0 && n_tiles) {
-        atomicAdd(&T.counters[1], (unsigned long long)n_acc);
-        atomicAdd(&T.tctl[2], (unsigned long long)n_tiles);
-        atomicAdd(&T.tctl[3], (unsigned long long)n_pairs);
-        atomicAdd(&T.tctl[4], (unsigned long long)n_esc);
+    if (lane == 0 && t64) {
+        atomicAdd(&T.counters[1], a64);
+        atomicAdd(&T.tctl[2], t64);
+        atomicAdd(&T.tctl[3], p64);
+        atomicAdd(&T.tctl[4], e64);
     }
     // The last block to finish empties the tile list for the next expansion launch.
     __syncthreads();

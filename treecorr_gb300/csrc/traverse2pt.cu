@@ -937,7 +937,7 @@ static int set_expand_attr(size_t sm)
 }
 
 int launch_expand_batch(const TravParams& T, int blocks, ExpandSched* dS, int iters,
-                        cudaStream_t st)
+                        cudaStream_t st, cudaEvent_t* ev)
 {
     const size_t sm = expand_smem_bytes(T.nqf, T.nbins, T.mode);
     // One schedule step starts the batch (the host may have changed the schedule); every
@@ -945,12 +945,15 @@ int launch_expand_batch(const TravParams& T, int blocks, ExpandSched* dS, int it
     count_launch();
     k_expand_sched<<<1, 1, 0, st>>>(dS);
     for (int it = 0; it < iters; ++it) {
+        if (ev) TC_CU(cudaEventRecord(ev[3 * it], st));
         count_launch();
         if (T.mode == 3) k_expand<3><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
         else if (T.mode == 2) k_expand<2><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
         else if (T.mode == 1) k_expand<1><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
         else k_expand<0><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
+        if (ev) TC_CU(cudaEventRecord(ev[3 * it + 1], st));
         if (T.mode == 0 && T.tile_leaf > 0) TC_TRY(launch_tiles(T, st));
+        if (ev) TC_CU(cudaEventRecord(ev[3 * it + 2], st));
     }
     TC_CU(cudaGetLastError());
     return 0;

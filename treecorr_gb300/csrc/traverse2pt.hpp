@@ -127,9 +127,11 @@ size_t traverse_smem_bytes(int nq, int nb);
 int traverse_grid(int nq, int nb, int* blocks, int* nwarps);
 int launch_traverse(const TravParams& T, int blocks, cudaStream_t st);
 int expand_grid(int nq, int nb, int* blocks, int* nwarps, int mode = 0);
-// Enqueues `iters` (schedule, expand) pairs on st without synchronising.
+// Enqueues `iters` (schedule, expand[, tiles]) launches on st without synchronising.  With
+// ev (3 * iters events) it records events around them: ev[3 it] before the expansion launch,
+// ev[3 it + 1] after it (= before the tiles), ev[3 it + 2] after the tiles.
 int launch_expand_batch(const TravParams& T, int blocks, ExpandSched* dS, int iters,
-                        cudaStream_t st);
+                        cudaStream_t st, cudaEvent_t* ev = nullptr);
 // Leaf-pair tiles (tiles.cu): the leaf size of a tile side, the k_tiles grid for a traversal
 // (its blocks fill every SM), and one k_tiles launch over the tiles waiting in T.tiles.
 static constexpr int TILE_LEAF = 32;
