@@ -2,7 +2,7 @@
 
 In that mode the reference accepts only pairs of leaves (src/Corr2.cpp:308-389 with
 include/BinType.h:93-151: s1 + s2 <= a r needs s1 + s2 = 0 when a = 0), so the GPU stops the
-tree walk at cell pairs of at most 32 points per side and evaluates every leaf pair of such a
+tree walk at cell pairs of at most 48 points per side and evaluates every leaf pair of such a
 tile in k_tiles.  The tests compare the tile path with the reference's outputs, with the
 traversal walked down to the leaves (TCGPU_TILES=0), and with the oracle on edge cases (list
 leaves of coincident points, zero weights, self tiles, cross fields).

@@ -48,6 +48,9 @@ static const char* dev_err_msg(int code)
                  "differ along the split axis (degenerate weights)";
       case DEV_BAD_CHILD: return "traversal asked to split a leaf cell (inconsistent tree)";
       case DEV_TASK_OVERFLOW: return "tree build task stack overflow";
+      case DEV_COPY_TIMEOUT:
+          return "an asynchronous copy of tile leaves into shared memory did not complete within "
+                 "its wait limit";
       default: return "unknown device error";
     }
 }

@@ -27,6 +27,7 @@ enum DevErr : int {
     DEV_DEGENERATE_SPLIT = 3,  // mean split failed on a large cell whose points differ
     DEV_BAD_CHILD = 4,         // traversal asked to split a leaf (inconsistent tree)
     DEV_TASK_OVERFLOW = 5,     // build task list overflow
+    DEV_COPY_TIMEOUT = 6,      // an asynchronous copy into shared memory did not complete
 };
 
 // Catalog points during the build (structure of arrays, one of two ping-pong buffers).

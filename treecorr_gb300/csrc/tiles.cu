@@ -27,6 +27,12 @@
 //     at the end, like the traversal's.
 // The kernel is compiled per geometry (flat, sphere with Arc, sphere or 3-d with Euclidean)
 // and per class family (NN; NK and KK; GG; the others through the generic projection code).
+// Measured on the 10M-point curved-sky catalog (bin_slop 0, angle_slop 0): the pair loops run
+// at ~3.6e11 pairs/s on one-bin tiles, and the per-tile work (staging, bounds, the final
+// butterfly) is the rest; tiles of up to 48 points per side (TILE_LEAF) balance the two (32:
+// 22.5 s, 48: 17.5 s).  A variant that staged the next tile's leaves with bulk copies
+// (cp.async.bulk + mbarrier) while the current one ran was 6% slower: the per-tile cost is
+// instruction issue, not load latency, with 24 warps per SM.
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
@@ -47,6 +53,10 @@ constexpr int TFLUSH = 8;         // tiles between flushes of the FP32 bins
 #define TILES_MINB 6
 #endif
 constexpr int TMINB = TILES_MINB; // resident blocks per SM the registers are sized for
+#ifndef TILE_CAP
+#define TILE_CAP 64
+#endif
+constexpr int TCAP = TILE_CAP;    // most leaves per tile side (>= the traversal's tile_leaf)
 
 enum { TG_FLAT = 0, TG_ARC = 1, TG_SPHEUC = 2, TG_3D = 3 };   // geometry
 enum { TK_NN = 0, TK_SC = 1, TK_GEN = 2, TK_GG = 3 };           // class family
@@ -54,15 +64,20 @@ enum { TK_NN = 0, TK_SC = 1, TK_GEN = 2, TK_GG = 3 };           // class family
 // One side of a tile: its valid leaves (n > 0, w != 0) in point order.  Pair loops read P and
 // W of both sides (two 16-byte shared loads per side) and X only where it is needed.
 struct TileLeaves {
-    float4 P[32];   // (ox, oy, oz, z / 2): offset from B's centre, half the z coordinate
-    float4 W[32];   // (w, p1, p2, n bits): weight, payload (p1 = w for N, w k for K, w g for
-                    // complex kinds), point count
-    float4 X[32];   // (x, y, id bits, 0): FP32 position (sphere projections), leaf cell id
+    float4 P[TCAP];   // (ox, oy, oz, z / 2): offset from B's centre, half the z coordinate
+    float4 W[TCAP];   // (w, p1, p2, n bits): weight, payload (p1 = w for N, w k for K, w g for
+                      // complex kinds), point count
+    float4 X[TCAP];   // (x, y, id bits, 0): FP32 position (sphere projections), leaf cell id
 };
 
 __host__ __device__ inline size_t bins_bytes(int nq, int nb)
 {
     return ((size_t)nq * nb * 8 + (size_t)nb * 8 + (size_t)nq * nb * 4 + 15) & ~(size_t)15;
+}
+
+__host__ __device__ inline size_t edges_bytes(int nb)
+{
+    return ((size_t)2 * (nb + 1) * 4 + 15) & ~(size_t)15;
 }
 
 __host__ __device__ inline size_t warp_bytes(int nq, int nb)
@@ -71,38 +86,51 @@ __host__ __device__ inline size_t warp_bytes(int nq, int nb)
 }
 
 // Stages the valid leaves of cell c (points [start, start + n), leaf ids base + p) with their
-// offsets from the centre (ch + cl).  Returns the count; *single is false when a staged leaf
-// holds more than one point.  on1 / on2: the L1 norm and the length of the lane's offset.
+// offsets from the centre (ch + cl), in point order.  Returns the count; *single is false when
+// a staged leaf holds more than one point.  on1 / on2: the largest L1 norm and length of the
+// lane's offsets (used only when the cells' sizes are not finite bounds, i.e. brute cells).
 __device__ __forceinline__ int stage(const TCell* cells, int base, float4 cc, float4 cd,
                                      float chx, float chy, float chz, float clx, float cly,
-                                     float clz, int kind, TileLeaves& S, int lane, float& on1,
-                                     float& on2, bool& single)
+                                     float clz, int kind, TileLeaves& S, int lane, bool norms,
+                                     float& on1, float& on2, bool& single)
 {
     const int start = __float_as_int(cd.z), n = __float_as_int(cc.z);
-    bool v = false;
-    float4 P = make_float4(0.f, 0.f, 0.f, 0.f), W = P, X = P;
-    int nn = 0;
-    if (lane < n) {
-        const int id = base + start + lane;
-        const float4 a = cells[id].a, b = cells[id].b, c = cells[id].c;
-        nn = __float_as_int(c.z);
-        v = nn > 0 && b.w != 0.f;
-        if (v) {
-            P = make_float4((a.x - chx) + (b.x - clx), (a.y - chy) + (b.y - cly),
-                            (a.z - chz) + (b.z - clz), 0.5f * a.z);
-            W = make_float4(b.w, kind == DN ? b.w : c.x, c.y, __int_as_float(nn));
-            X = make_float4(a.x, a.y, __int_as_float(id), 0.f);
+    int cnt = 0;
+    bool all1 = true;
+    on1 = 0.f; on2 = 0.f;
+#pragma unroll
+    for (int h = 0; h < TCAP / 32; ++h) {
+        const int p0 = lane + 32 * h;
+        bool v = false;
+        float4 P = make_float4(0.f, 0.f, 0.f, 0.f), W = P, X = P;
+        int nn = 0;
+        if (p0 < n) {
+            const int id = base + start + p0;
+            const float4 a = cells[id].a, b = cells[id].b, c = cells[id].c;
+            nn = __float_as_int(c.z);
+            v = nn > 0 && b.w != 0.f;
+            if (v) {
+                P = make_float4((a.x - chx) + (b.x - clx), (a.y - chy) + (b.y - cly),
+                                (a.z - chz) + (b.z - clz), 0.5f * a.z);
+                W = make_float4(b.w, kind == DN ? b.w : c.x, c.y, __int_as_float(nn));
+                X = make_float4(a.x, a.y, __int_as_float(id), 0.f);
+            }
         }
+        const unsigned m = __ballot_sync(0xffffffffu, v);
+        all1 = all1 && __all_sync(0xffffffffu, !v || nn == 1);
+        if (v) {
+            const int p = cnt + __popc(m & ((1u << lane) - 1u));
+            S.P[p] = P; S.W[p] = W; S.X[p] = X;
+        }
+        cnt += __popc(m);
+        if (norms) {
+            on1 = fmaxf(on1, fabsf(P.x) + fabsf(P.y) + fabsf(P.z));
+            on2 = fmaxf(on2, sqrtf(P.x * P.x + P.y * P.y + P.z * P.z));
+        }
+        if (32 * (h + 1) >= n) break;
     }
-    const unsigned m = __ballot_sync(0xffffffffu, v);
-    single = __all_sync(0xffffffffu, !v || nn == 1);
-    if (v) {
-        const int p = __popc(m & ((1u << lane) - 1u));
-        S.P[p] = P; S.W[p] = W; S.X[p] = X;
-    }
-    on1 = fabsf(P.x) + fabsf(P.y) + fabsf(P.z);
-    on2 = sqrtf(P.x * P.x + P.y * P.y + P.z * P.z);
-    return __popc(m);
+    single = all1;
+    return cnt;
 }
 
 __device__ __forceinline__ float warp_max(float v)
@@ -418,7 +446,13 @@ __global__ void __launch_bounds__(TPB, TMINB) k_tiles(const __grid_constant__ Tr
     // raised DEV_SPILL_OVERFLOW), so never read beyond it.
     long long nt = (long long)*(volatile unsigned long long*)&T.tctl[0];
     if (nt > T.tile_cap) nt = T.tile_cap;
-    unsigned char* wb = smem + (size_t)wib * warp_bytes(nq, nb);
+    // The bin edges (1 / edge^2 and log edge, nb + 1 each) for the whole block, then the
+    // warps' areas.
+    float* edge_sh = reinterpret_cast<float*>(smem);
+    for (int q = threadIdx.x; q < 2 * (nb + 1); q += TPB)
+        edge_sh[q] = q <= nb ? T.tile_edge[q] : T.tile_ledge[q - nb - 1];
+    __syncthreads();
+    unsigned char* wb = smem + edges_bytes(nb) + (size_t)wib * warp_bytes(nq, nb);
     float2* fd = reinterpret_cast<float2*>(wb);
     unsigned long long* np = reinterpret_cast<unsigned long long*>(fd + nq * nb);
     float* fb = reinterpret_cast<float*>(np + nb);
@@ -444,10 +478,14 @@ __global__ void __launch_bounds__(TPB, TMINB) k_tiles(const __grid_constant__ Tr
             const float4 Aa = T.c1[ia].a, Ab = T.c1[ia].b, Ac = T.c1[ia].c, Ad = T.c1[ia].d;
             const float4 Ba = cB[ib].a, Bb = cB[ib].b, Bc = cB[ib].c, Bd = cB[ib].d;
             ++n_tiles;
-            float eA, rA, eB, rB;
+            // Bounds of the tile's separations from the two cells' sizes (each point lies
+            // within size of its cell's FP64 centre; 1e-6 covers the size's FP32 rounding).
+            // Brute cells have infinite sizes: then the staged leaves give the bounds.
+            const bool sized = Aa.w < 1e30f && Ba.w < 1e30f;
+            float eA = 0.f, rA = 0.f, eB = 0.f, rB = 0.f;
             bool sA, sB;
             C.nbl = stage(cB, baseB, Bc, Bd, Ba.x, Ba.y, Ba.z, Bb.x, Bb.y, Bb.z, T.k2, SB, lane,
-                          eB, rB, sB);
+                          !sized, eB, rB, sB);
             C.na = C.nbl;
             // A's offsets are also taken from B's centre; D = centre A - centre B.
             const float Dx = (Aa.x - Ba.x) + (Ab.x - Bb.x), Dy = (Aa.y - Ba.y) + (Ab.y - Bb.y);
@@ -455,28 +493,42 @@ __global__ void __launch_bounds__(TPB, TMINB) k_tiles(const __grid_constant__ Tr
             if (!C.self) {
                 float on2;
                 C.na = stage(T.c1, T.leaf_base1, Ac, Ad, Ba.x, Ba.y, Ba.z, Bb.x, Bb.y, Bb.z, T.k1,
-                             SA, lane, eA, on2, sA);
-                // Distance of A's leaf from A's centre.
-                __syncwarp();
-                const float4 P = lane < C.na ? SA.P[lane] : make_float4(Dx, Dy, Dz, 0.f);
-                const float ux = P.x - Dx, uy = P.y - Dy, uz = P.z - Dz;
-                rA = sqrtf(ux * ux + uy * uy + uz * uz);
+                             SA, lane, !sized, eA, on2, sA);
+                if (!sized) {
+                    // Distance of A's leaves from A's centre.
+                    __syncwarp();
+                    for (int p = lane; p < C.na; p += 32) {
+                        const float4 P = SA.P[p];
+                        const float ux = P.x - Dx, uy = P.y - Dy, uz = P.z - Dz;
+                        rA = fmaxf(rA, sqrtf(ux * ux + uy * uy + uz * uz));
+                    }
+                }
             } else {
                 eA = eB; rA = rB; sA = sB;
             }
             __syncwarp();
             if (C.na == 0 || C.nbl == 0) continue;
             const TileLeaves& LA = C.self ? SB : SA;
-            // Tile bounds.  emax bounds |FP32 d - d| of every pair (each offset within 2 ulps
-            // of its L1 size, the difference one more; a 1.5x margin); the separation of any
-            // pair lies within |D| +- (rA + rB).
-            C.emax = 2.7e-7f * (warp_max(eA) + warp_max(eB)) + 1e-30f;
-            const float rAB = warp_max(rA) + warp_max(rB);
-            const float Dn = sqrtf(Dx * Dx + Dy * Dy + Dz * Dz);
+            const float Dsq = Dx * Dx + Dy * Dy + Dz * Dz;
+            const float Dn = Dsq > 0.f ? Dsq * rsqrtf(Dsq) : 0.f;    // |D| within 2 ulps
+            float rAB;
+            if (sized) {
+                // emax bounds |FP32 d - d| of every pair: each offset within 2 ulps of its L1
+                // size, the difference one more (a 1.5x margin), and L1 <= sqrt(3) L2.
+                rAB = (Aa.w + Ba.w) * (1.f + 1e-6f) + 1e-30f;
+                C.emax = 4.7e-7f * (Dn + rAB) + 1e-30f;
+            } else {
+                C.emax = 2.7e-7f * (warp_max(eA) + warp_max(eB)) + 1e-30f;
+                rAB = warp_max(rA) + warp_max(rB);
+            }
+            // Every pair's separation lies within |D| +- rAB, up to the FP32 errors (slack).
             const float slack = C.emax + 2e-6f * (Dn + rAB);
             float lo = fmaxf(Dn - rAB - slack, 0.f), hi = Dn + rAB + slack;
             C.small_chord = hi < 0.25f;
-            if (GEO == TG_ARC) { lo = arc_from_chord_sq(lo * lo); hi = arc_from_chord_sq(hi * hi); }
+            if (GEO == TG_ARC) {
+                if (C.small_chord) { lo = arc_series(lo); hi = arc_series(hi); }
+                else { lo = arc_from_chord_sq(lo * lo); hi = arc_from_chord_sq(hi * hi); }
+            }
             lo *= 1.f - 1e-5f;
             hi *= 1.f + 1e-5f;
             if (lo >= T.fmaxsep || hi < T.fminsep) continue;   // no pair in range
@@ -489,8 +541,8 @@ __global__ void __launch_bounds__(TPB, TMINB) k_tiles(const __grid_constant__ Tr
             klo = klo < 0 ? 0 : (klo > nb - 1 ? nb - 1 : klo);
             khi = khi < 0 ? 0 : (khi > nb - 1 ? nb - 1 : khi);
             C.kref = klo;
-            C.inv_edge = T.tile_edge[klo];     // 1 / (lower edge of kref)^2
-            C.ledge = T.tile_ledge[klo];       // log of that edge
+            C.inv_edge = edge_sh[klo];         // 1 / (lower edge of kref)^2
+            C.ledge = edge_sh[nb + 1 + klo];   // log of that edge
             // Band (in bins) outside which the FP32 bin is certain: r's relative error
             // (emax / chord + 4e-7) and __log2f's (2^-22 absolute on [0.5, 2], else 2 ulps;
             // |log2| <= lmax here), the roundings of its argument and of kk.
@@ -592,10 +644,14 @@ TileKernel pick(const TravParams& T)
 
 int tiles_grid(const TravParams& T, int* blocks, int* nwarps)
 {
+    if (T.tile_leaf > TCAP) {
+        set_last_error("tile leaf size above the tile kernel's staging capacity");
+        return 1;
+    }
     int dev = 0, nsm = 0, per = 0;
     TC_CU(cudaGetDevice(&dev));
     TC_CU(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    const size_t sm = warp_bytes(T.nqf, T.nbins) * TWPB;
+    const size_t sm = edges_bytes(T.nbins) + warp_bytes(T.nqf, T.nbins) * TWPB;
     const TileKernel k = pick(T);
     if (sm > 48 * 1024)
         TC_CU(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -608,7 +664,7 @@ int tiles_grid(const TravParams& T, int* blocks, int* nwarps)
 
 int launch_tiles(const TravParams& T, cudaStream_t st)
 {
-    const size_t sm = warp_bytes(T.nqf, T.nbins) * TWPB;
+    const size_t sm = edges_bytes(T.nbins) + warp_bytes(T.nqf, T.nbins) * TWPB;
     count_launch();
     pick(T)<<<T.tile_blocks, TPB, sm, st>>>(T);
     return 0;

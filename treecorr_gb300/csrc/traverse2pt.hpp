@@ -134,7 +134,7 @@ int launch_expand_batch(const TravParams& T, int blocks, ExpandSched* dS, int it
                         cudaStream_t st, cudaEvent_t* ev = nullptr);
 // Leaf-pair tiles (tiles.cu): the leaf size of a tile side, the k_tiles grid for a traversal
 // (its blocks fill every SM), and one k_tiles launch over the tiles waiting in T.tiles.
-static constexpr int TILE_LEAF = 32;
+static constexpr int TILE_LEAF = 48;
 int tiles_grid(const TravParams& T, int* blocks, int* nwarps);
 int launch_tiles(const TravParams& T, cudaStream_t st);
 int launch_reduce(int nwarps, int nq, int nb, const double* wacc, const unsigned long long* wnp,
