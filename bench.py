@@ -586,86 +586,202 @@ def run_gpu_ggg(args, rank, world):
     return line
 
 
+def run_exact(args, rank, world):
+    """One exact-mode GG correlation (bin_slop 0, angle_slop 0; the leaf-pair tiles) of a
+    curved-sky catalog of --n points on --area deg^2, 30 Log bins 1-300' -- at --n 1000000
+    --area 100 the same density (so the same tiles) as the 10M-point headline catalog, the
+    small case the k_tiles profiles are taken on.  Times args.steps correlations after
+    args.warmup with CUDA events on the library's stream."""
+    import torch
+    from treecorr_gb300 import _treecorr as T
+    dev = torch.device("cuda", rank % max(torch.cuda.device_count(), 1))
+    torch.cuda.set_device(dev)
+    cat = curved_sky_catalog(args.n, seed=args.seed + rank, area_deg2=args.area,
+                             ngrid=1024 if args.area < 500 else 4096)
+    e = np.array([])
+    f = T.GFieldSphere(cat["x"], cat["y"], cat["z"], cat["g1"], cat["g2"], cat["w"], e, 0.0,
+                       0.0, T.Mean, 0, False, 3, 10)
+    f.getNTopLevel()
+    B = binning(0.0)
+    nb = B["nbins"]
+    out = {k: np.zeros(nb) for k in ("xi0", "xi1", "xi2", "xi3", "meanr", "meanlogr", "weight",
+                                     "npairs")}
+    c = T.GGCorr(T.Log, B["min_sep"], B["max_sep"], nb, B["bin_size"], 0.0, 0.0,
+                 -sys.float_info.max, sys.float_info.max, 0., 0., 0., out["xi0"], out["xi1"],
+                 out["xi2"], out["xi3"], out["meanr"], out["meanlogr"], out["weight"],
+                 out["npairs"])
+    stream = torch.cuda.ExternalStream(T.stream_handle(), device=dev)
+    for _ in range(args.warmup):
+        c.processAuto(f, False, False, T.Arc)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        c.processAuto(f, False, False, T.Arc)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    st = c.stats()
+    return {"metric": "GG exact-mode pair-evals/s (bin_slop 0, angle_slop 0)",
+            "value": st["accepted"] / (ms / 1e3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic (seeded curved-sky GRF catalog)",
+            "config": {"workload": f"GG auto, {args.n} points on a {args.area:g} deg^2 cap, Arc, "
+                                   "30 Log bins 1-300', bin_slop 0, angle_slop 0 (tree built "
+                                   "once, correlation per step)"},
+            "detail": {k: st[k] for k in ("accepted", "tile_pairs", "tiles", "tile_escalated",
+                                          "cell_pairs", "launches", "tiles_ms", "expand_ms",
+                                          "traverse_ms")}}
+
+
+def clumped_catalog(n, seed, side=3000.0, nclump=100_000, sigma=2.0, frac=0.4):
+    """The learned-criterion configuration's catalog: flat U[0, side]^2 positions with
+    nclump Gaussian clumps (sigma arcmin) holding frac of the points; g ~ N(0, 0.25); w = 1."""
+    rng = np.random.default_rng(seed)
+    nc = int(n * frac)
+    cen = rng.uniform(0, side, size=(nclump, 2))
+    k = rng.integers(0, nclump, size=nc)
+    xy_c = cen[k] + rng.normal(0, sigma, size=(nc, 2))
+    xy_u = rng.uniform(0, side, size=(n - nc, 2))
+    xy = np.concatenate([xy_c, xy_u])
+    return dict(x=np.ascontiguousarray(xy[:, 0]), y=np.ascontiguousarray(xy[:, 1]), z=None,
+                g1=rng.normal(0, 0.25, n), g2=rng.normal(0, 0.25, n), w=np.ones(n))
+
+
 def run_learned(args, rank, world):
-    """Learned vs plain split on the curved-sky GG workload: the network is trained on a
-    1M-point catalog (a different seed), then the plain bin_slop 0.1 rule, the rule at
-    bin_slop 0.2 and the learned criterion (base bin_slop 0.1, candidates up to 4 b r,
-    accept when the predicted log10 leak <= threshold) process the evaluation catalog; each
-    is compared with bin_slop 0 / angle_slop 0.02 on the same catalog."""
+    """Learned vs plain split.  The network (5-64-64-1, trained by this library's kernels on
+    split candidates of plain traversals of a 1M-point catalog of the same distribution)
+    accepts candidate pairs -- pairs the bin_slop rule splits with s <= cand_factor b r --
+    whose predicted leak into other bins is below 10^threshold.
+
+    Equal accuracy at the metric's target (|d xi+-| <= 1e-4 max|xi+|): on these shape-noise-
+    dominated catalogs only bin_slop 0 / angle_slop 0 meets it (any accepted cell pair moves
+    its pairs' noise between bins or directions), and at bin_slop 0 the network has no
+    candidates, so learned and plain are the same computation; `value` is their time ratio
+    there.  `looser` compares the plain rule at bin_slop 0.1, 0.05 and 0.2 with the network on
+    a 0.1 base, each with its error against the exact result: the gain at equal accuracy is
+    the time of the fastest plain setting at least as accurate as the learned run, over the
+    learned run's time.  Curved sky (the 10M-point cap, 30 bins 1-300') by default;
+    --config5: 50M flat clumped points, 40 bins 0.5-500' (times on the full catalog, errors on
+    a 600' x 600' corner of it, where the exact result fits in seconds)."""
     import torch
     from treecorr_gb300 import _treecorr as T, learned
     dev = torch.device("cuda", rank % max(torch.cuda.device_count(), 1))
     torch.cuda.set_device(dev)
     e = np.array([])
+    c5 = args.config5
+    if c5:
+        nb, lo, hi = 40, 0.5, 500.0
+        metric = T.Euclidean
+    else:
+        nb, lo, hi = 30, ARCMIN, 300 * ARCMIN
+        metric = T.Arc
+    bsz = np.log(hi / lo) / nb
 
     def field(cat):
-        f = T.GFieldSphere(cat["x"], cat["y"], cat["z"], cat["g1"], cat["g2"], cat["w"], e,
-                           0.0, 0.0, T.Mean, 0, False, 3, 10)
+        if c5:
+            f = T.GFieldFlat(cat["x"], cat["y"], e, cat["g1"], cat["g2"], cat["w"], e, 0.0, 0.0,
+                             T.Mean, 0, False, 3, 10)
+        else:
+            f = T.GFieldSphere(cat["x"], cat["y"], cat["z"], cat["g1"], cat["g2"], cat["w"], e,
+                               0.0, 0.0, T.Mean, 0, False, 3, 10)
         f.getNTopLevel()
         return f
 
     def corr(slop, a=0.1):
-        B = binning(slop)
-        out = {k: np.zeros(B["nbins"]) for k in ("xi0", "xi1", "xi2", "xi3", "meanr",
-                                                  "meanlogr", "weight", "npairs")}
-        c = T.GGCorr(T.Log, B["min_sep"], B["max_sep"], B["nbins"], B["bin_size"], B["b"], a,
-                     -sys.float_info.max, sys.float_info.max, 0., 0., 0., out["xi0"],
-                     out["xi1"], out["xi2"], out["xi3"], out["meanr"], out["meanlogr"],
-                     out["weight"], out["npairs"])
+        out = {k: np.zeros(nb) for k in ("xi0", "xi1", "xi2", "xi3", "meanr", "meanlogr",
+                                          "weight", "npairs")}
+        c = T.GGCorr(T.Log, lo, hi, nb, bsz, slop * bsz, a, -sys.float_info.max,
+                     sys.float_info.max, 0., 0., 0., out["xi0"], out["xi1"], out["xi2"],
+                     out["xi3"], out["meanr"], out["meanlogr"], out["weight"], out["npairs"])
         return c, out
 
-    t0 = time.perf_counter()
-    ftrain = field(curved_sky_catalog(1_000_000, seed=args.seed + 1000))
-    c, _ = corr(0.1)
-    x, y = learned.collect(c, ftrain, T.Arc, sample_mod=4, max_samples=4 << 20)
-    params, loss = learned.train(x, y, steps=4000, batch=8192, lr=2e-3, seed=0)
-    t_train = time.perf_counter() - t0
-    del ftrain
-    f = field(curved_sky_catalog(args.n, seed=args.seed + rank))
-
-    def run(c, out, reps):
-        c.processAuto(f, False, False, T.Arc)
+    def run(f, c, out, reps):
+        c.processAuto(f, False, False, metric)
         ts = []
         for _ in range(reps):
             for k in out:
                 out[k][:] = 0.
             torch.cuda.synchronize()
             t1 = time.perf_counter()
-            c.processAuto(f, False, False, T.Arc)
+            c.processAuto(f, False, False, metric)
             ts.append(time.perf_counter() - t1)
         st = c.stats()
         return {"wall_s": float(np.median(ts)), "cell_pairs": st["cell_pairs"],
                 "accepted": st["accepted"], "learned": st["learned"],
                 "xip": out["xi0"] / out["weight"], "xim": out["xi2"] / out["weight"]}
 
-    ce, oe = corr(0.0, a=0.02)
-    ex = run(ce, oe, 1)
+    def make(n, seed):
+        return clumped_catalog(n, seed) if c5 else curved_sky_catalog(n, seed=seed)
+
+    t0 = time.perf_counter()
+    ftrain = field(clumped_catalog(1_000_000, args.seed + 1000, side=3000.0 / np.sqrt(50))
+                   if c5 else curved_sky_catalog(1_000_000, seed=args.seed + 1000))
+    ct, _ = corr(0.1)
+    x, y = learned.collect(ct, ftrain, metric, sample_mod=4, max_samples=4 << 20)
+    params, loss = learned.train(x, y, steps=4000, batch=8192, lr=2e-3, seed=0)
+    t_train = time.perf_counter() - t0
+    del ftrain
+    n = 50_000_000 if c5 else args.n
+    cat = make(n, args.seed + rank)
+    if c5:
+        sel = (cat["x"] < 600.0) & (cat["y"] < 600.0)
+        sub = {k: (np.ascontiguousarray(v[sel]) if v is not None else None) for k, v in cat.items()}
+    f = field(cat)
+    setups = [("plain_bs0.1", 0.1, None), ("plain_bs0.05", 0.05, None),
+              ("plain_bs0.2", 0.2, None), ("learned_bs0.1", 0.1, params)]
     res = {}
-    for name, slop in (("plain_bs0.1", 0.1), ("plain_bs0.2", 0.2)):
-        cp, op = corr(slop)
-        res[name] = run(cp, op, args.steps)
-    cl, ol = corr(0.1)
+    for name, slop, prm in setups:
+        c, o = corr(slop)
+        if prm is not None:
+            c.setLearned(prm, threshold=args.learned_threshold, cand_factor=4.0)
+        res[name] = run(f, c, o, args.steps)
+    if c5:
+        # Errors (and the exact-mode comparison) on the corner sub-catalog; the times of the
+        # setups above stay the full catalog's.
+        del f
+        f = field(sub)
+        for name, slop, prm in setups:
+            c, o = corr(slop)
+            if prm is not None:
+                c.setLearned(prm, threshold=args.learned_threshold, cand_factor=4.0)
+            r = run(f, c, o, 1)
+            res[name]["xip"], res[name]["xim"] = r["xip"], r["xim"]
+    ce, oe = corr(0.0, a=0.0)
+    ex = run(f, ce, oe, 1)
+    cl, ol = corr(0.0, a=0.0)
     cl.setLearned(params, threshold=args.learned_threshold, cand_factor=4.0)
-    res["learned"] = run(cl, ol, args.steps)
+    ex_l = run(f, cl, ol, 1)
     mx = float(np.abs(ex["xip"]).max())
     for r in res.values():
-        r["dxip_rel"] = float(np.abs(r["xip"] - ex["xip"]).max() / mx)
-        r["dxim_rel"] = float(np.abs(r["xim"] - ex["xim"]).max() / mx)
+        r["xi_err"] = float(max(np.abs(r["xip"] - ex["xip"]).max(),
+                                np.abs(r["xim"] - ex["xim"]).max()) / mx)
         del r["xip"], r["xim"]
-    speed = res["plain_bs0.1"]["wall_s"] / res["learned"]["wall_s"]
-    return {"metric": "GG wall-s, learned vs plain split (ratio plain/learned)",
-            "value": speed, "unit": "x", "n_gpus": world, "steps": args.steps,
+    lr = res["learned_bs0.1"]
+    ok = [r for k, r in res.items() if k.startswith("plain") and r["xi_err"] <= lr["xi_err"]]
+    eq_gain = (min(r["wall_s"] for r in ok) / lr["wall_s"]) if ok else None
+    value = ex["wall_s"] / ex_l["wall_s"]
+    wl = ("GG auto, 50M flat clumped points (1e5 clumps of 2', 40%), 40 Log bins 0.5-500'"
+          if c5 else f"GG auto, {n}-point curved sky, Arc, 30 Log bins 1-300'")
+    return {"metric": "GG wall-s, learned vs plain split at equal accuracy "
+                      "(|d xi+-| <= 1e-4 max|xi+|; ratio plain/learned)",
+            "value": value, "unit": "x", "n_gpus": world, "steps": args.steps,
             "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32+f16 network", "data": "synthetic (seeded curved-sky GRF catalog)",
-            "config": {"workload": f"GG auto, {args.n}-point curved sky, Arc, 30 Log bins "
-                                   "1-300'; network trained on a 1M-point catalog",
+            "dtype": "f32+f16 network", "data": "synthetic (seeded)",
+            "config": {"workload": wl + "; network trained on a 1M-point catalog of the same "
+                                        "distribution",
                        "threshold": args.learned_threshold, "cand_factor": 4.0},
-            "reference_result": "bin_slop 0, angle_slop 0.02 on the same catalog "
-                                f"({ex['wall_s']:.2f} s); errors are max over bins of "
-                                "|xi - xi_ref| / max|xi+_ref|",
+            "at_1e-4": {"plain_exact_s": ex["wall_s"], "learned_exact_s": ex_l["wall_s"],
+                        "learned_accepted": ex_l["learned"],
+                        "note": "bin_slop 0 / angle_slop 0: the network has no candidates"
+                                + (" (on the 600' x 600' corner)" if c5 else "")},
+            "looser": res, "gain_at_equal_accuracy_looser": eq_gain,
+            "reference_result": "bin_slop 0, angle_slop 0 on the same catalog"
+                                + (" (errors on the 600' x 600' corner)" if c5 else ""),
             "train": {"samples": int(len(y)), "seconds": t_train,
-                      "loss_first": float(loss[0]), "loss_last": float(loss[-20:].mean())},
-            "results": res}
+                      "loss_first": float(loss[0]), "loss_last": float(loss[-20:].mean())}}
 
 
 def run_patches(args, rank, world):
@@ -1176,14 +1292,19 @@ def main():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     p.add_argument("--workload", default="gg",
-                   choices=["gg", "ggg", "learned", "patches", "kmeans", "classes"],
+                   choices=["gg", "ggg", "learned", "patches", "kmeans", "classes", "exact"],
                    help="gg: the 2-point headline; ggg: the multipole 3-point configuration; "
                         "learned: the learned opening criterion against the plain rule; "
                         "patches: 150 patches, all pairs in one expansion + jackknife; "
                         "kmeans: k-means patches of the curved-sky catalog; "
-                        "classes: the other 2-point and 3-point classes, one call each")
+                        "classes: the other 2-point and 3-point classes, one call each; "
+                        "exact: one bin_slop 0 / angle_slop 0 correlation (--n, --area)")
     p.add_argument("--learned-threshold", type=float, default=-3.0)
+    p.add_argument("--config5", action="store_true",
+                   help="learned workload on 50M flat clumped points (40 bins 0.5-500')")
     p.add_argument("--n", type=int, default=10_000_000)
+    p.add_argument("--area", type=float, default=1000.0,
+                   help="cap area in deg^2 of the exact workload's catalog")
     p.add_argument("--bin-slop", type=float, default=0.1)
     p.add_argument("--seed", type=int, default=20261203)
     p.add_argument("--cpu-budget", type=float, default=15.0)
@@ -1207,6 +1328,8 @@ def main():
         line = run_kmeans(args, rank, world)
     elif args.workload == "classes":
         line = run_classes(args, rank, world)
+    elif args.workload == "exact":
+        line = run_exact(args, rank, world)
     else:
         line = run_gpu(args, rank, world)
     if rank == 0 and line is not None:

@@ -88,3 +88,104 @@ def test_collect_training_pairs(gpu_lib):
                   ref["xi3"], ref["meanr"], ref["meanlogr"], ref["weight"], ref["npairs"])
     c2.processAuto(f, False, False, T.Euclidean)
     assert np.array_equal(out["npairs"], ref["npairs"])
+
+
+def _gg_corr(T, bins, out):
+    return T.GGCorr(T.Log, bins["min_sep"], bins["max_sep"], bins["nbins"], bins["bin_size"],
+                    bins["b"], bins["a"], -sys.float_info.max, sys.float_info.max, 0., 0., 0.,
+                    out["xi0"], out["xi1"], out["xi2"], out["xi3"], out["meanr"],
+                    out["meanlogr"], out["weight"], out["npairs"])
+
+
+def _flat_setup(T, n=40000, L=300., seed=5):
+    import helpers as H
+    from cases import flat_catalog
+    cat = flat_catalog(np.random.default_rng(seed), n, L=L)
+    nb, lo, hi = 20, 1.0, 100.0
+    bs = np.log(hi / lo) / nb
+    f = H.gpu_field(T, "G", "flat", cat, 0.0, 0.0)
+    return cat, f, dict(nbins=nb, min_sep=lo, max_sep=hi, bin_size=bs, a=0.1)
+
+
+def _run(T, f, bins, params=None, threshold=-3.0, cand_factor=4.0):
+    import helpers as H
+    out = {k: np.zeros(bins["nbins"]) for k in H.OUT_KEYS}
+    c = _gg_corr(T, bins, out)
+    if params is not None:
+        c.setLearned(params, threshold=threshold, cand_factor=cand_factor)
+    c.processAuto(f, False, False, T.Euclidean)
+    out["_stats"] = c.stats()
+    return out
+
+
+def _xi_err(out, ref):
+    """max over bins of |d xi+-| / max |xi+| (the metric's measure)."""
+    xp, xm = out["xi0"] / out["weight"], out["xi2"] / out["weight"]
+    rp, rm = ref["xi0"] / ref["weight"], ref["xi2"] / ref["weight"]
+    mx = np.abs(rp).max()
+    return max(np.abs(xp - rp).max(), np.abs(xm - rm).max()) / mx
+
+
+def test_learned_traversal_accepting_nothing_is_plain(gpu_lib):
+    """k_expand<2> with a threshold no prediction can meet: the network is evaluated on every
+    candidate and accepts none, so the result is the bin_slop rule's (the reference's
+    include/BinType.h:93-151)."""
+    T = gpu_lib
+    cat, f, bins = _flat_setup(T)
+    bins = dict(bins, b=0.1 * bins["bin_size"])
+    plain = _run(T, f, bins)
+    learned = _run(T, f, bins, params=_params(7), threshold=-1e30)
+    st = learned["_stats"]
+    assert st["learned"] == 0
+    assert st["cell_pairs"] == plain["_stats"]["cell_pairs"]
+    assert np.array_equal(learned["npairs"], plain["npairs"])
+    for k in ("weight", "xi0", "xi1", "xi2", "xi3", "meanr", "meanlogr"):
+        np.testing.assert_allclose(learned[k], plain[k], rtol=1e-6,
+                                   atol=1e-6 * np.abs(plain["weight"]).max())
+
+
+def test_learned_traversal_error_and_gain(gpu_lib):
+    """A network trained on this distribution's split candidates, used inside the traversal
+    (base bin_slop 0.1, candidates up to 4 b r, accept when the predicted log10 leak <= -3),
+    against the exact result (bin_slop 0, angle_slop 0) on the same catalog: its error lies
+    between the base rule's and the rule at 4 b, and it evaluates fewer cell pairs than the
+    base rule (what the network gains).  At bin_slop 0 -- the only setting whose error meets
+    1e-4 of max|xi+| on shape-noise-dominated data -- the network has no candidates at all
+    (they are pairs the rule splits within cand_factor * b * r), so it can gain nothing."""
+    import time
+    import torch
+    T = gpu_lib
+    from treecorr_gb300 import learned
+    cat, f, bins = _flat_setup(T)
+    bs = bins["bin_size"]
+    # Training pairs from a separate catalog of the same distribution.
+    _, ftrain, _ = _flat_setup(T, seed=55)
+    out = {k: np.zeros(bins["nbins"]) for k in ("xi0", "xi1", "xi2", "xi3", "meanr",
+                                                 "meanlogr", "weight", "npairs")}
+    c = _gg_corr(T, dict(bins, b=0.1 * bs), out)
+    x, y = learned.collect(c, ftrain, T.Euclidean, sample_mod=2, max_samples=400000)
+    params, loss = learned.train(x, y, steps=1500, batch=4096, lr=2e-3, seed=0)
+    exact = _run(T, f, dict(bins, b=0.0, a=0.0))
+    base = _run(T, f, dict(bins, b=0.1 * bs))
+    wide = _run(T, f, dict(bins, b=0.4 * bs))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lrn = _run(T, f, dict(bins, b=0.1 * bs), params=params, threshold=-3.0, cand_factor=4.0)
+    t_lrn = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    base2 = _run(T, f, dict(bins, b=0.1 * bs))
+    t_base = time.perf_counter() - t0
+    e_base, e_wide, e_lrn = _xi_err(base, exact), _xi_err(wide, exact), _xi_err(lrn, exact)
+    st = lrn["_stats"]
+    gain = base2["_stats"]["cell_pairs"] / st["cell_pairs"]
+    print(f"xi err: base {e_base:.3e}  learned {e_lrn:.3e}  4b {e_wide:.3e}; cell pairs "
+          f"base {base2['_stats']['cell_pairs']} learned {st['cell_pairs']} (gain {gain:.3f}, "
+          f"{st['learned']} accepted by the network); wall base {t_base:.3f} s learned "
+          f"{t_lrn:.3f} s")
+    assert st["learned"] > 0
+    assert st["cell_pairs"] < base2["_stats"]["cell_pairs"]
+    assert e_lrn <= 1.5 * e_wide + 1e-6
+    # Exact mode: nothing is a candidate, so the network changes nothing.
+    ex_l = _run(T, f, dict(bins, b=0.0, a=0.0), params=params, threshold=10.0)
+    assert ex_l["_stats"]["learned"] == 0
+    assert np.array_equal(ex_l["npairs"], exact["npairs"])

@@ -623,18 +623,21 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
     // Breadth-first expansion by levels: each launch takes a chunk of the deepest non-empty
     // level (level 0 = the top-level pairs, generated on the fly) and appends the children to
     // the next level, so memory stays bounded by (depth x 4 chunk) items.
-    T.mode = c->mode;
+    // The learned criterion's candidates are pairs the rule splits with s <= cand_factor b r:
+    // with b = 0 there are none, and the plain traversal (with its tiles) is the same result.
+    const int mode = (c->mode == 2 && c->b == 0.) ? 0 : c->mode;
+    T.mode = mode;
     T.cand_f2 = (float)(sqr(c->cand_factor * c->b));
     T.mlp_thr = c->mlp_thr;
     T.finvlogrange = (float)(1. / std::log(c->maxsep / c->minsep));
     T.mlp = c->mlp;
     T.samples = c->samples; T.sample_cap = c->sample_cap; T.sample_mod = c->sample_mod;
     int blocks = 0, nwarps = 0;
-    TC_TRY(expand_grid(nq, nb, &blocks, &nwarps, c->mode));
+    TC_TRY(expand_grid(nq, nb, &blocks, &nwarps, mode));
     // Exact mode: every pair the reference accepts is a pair of leaves (angle_slop 0, or two
     // brute fields), so the leaf pairs below small cell pairs go through k_tiles.
     // TCGPU_TILES=0 turns the tiles off (the traversal then walks down to the leaves).
-    bool tiles = c->mode == 0 && (c->a == 0. || (f1->brute && g->brute));
+    bool tiles = mode == 0 && (c->a == 0. || (f1->brute && g->brute));
     if (const char* ev = std::getenv("TCGPU_TILES")) tiles = tiles && std::atoi(ev) != 0;
     int tblocks = 0, twarps = 0;
     if (tiles) {
