@@ -100,7 +100,9 @@ typedef struct tc_stats {
  *   d2 = the imaginary part;
  *   w: weights; wpos: NULL means "use w" (src/Field.cpp:146-152).
  * The data are copied to the device here; the tree is built on the first call that needs
- * it (tc_field_ntop or a process call), like the reference's lazy BuildCells. */
+ * it (tc_field_ntop or a process call), like the reference's lazy BuildCells.  A non-zero
+ * seed reseeds the random stream of the k-means initialisations, as BaseField's constructor
+ * does (src/Field.cpp:160). */
 int tc_field_create(int dkind, int coords,
                     const double* x, const double* y, const double* z,
                     const double* d1, const double* d2,

@@ -1189,7 +1189,7 @@ int tc_field_create(int dkind, int coords, const double* x, const double* y, con
                     int64_t n, double min_size, double max_size, int split_method, int64_t seed,
                     int brute, int min_top, int max_top, tc_field** out)
 {
-    (void)seed;
+    km_seed(seed);   // BaseField seeds the random stream (src/Field.cpp:160)
     return field_create_impl(dkind, coords, x, y, z, d1, d2, w, wpos, n, min_size, max_size,
                              split_method, brute, min_top, max_top, false, out);
 }
@@ -1200,7 +1200,7 @@ int tc_field_create_device(int dkind, int coords, const double* x, const double*
                            int split_method, int64_t seed, int brute, int min_top, int max_top,
                            tc_field** out)
 {
-    (void)seed;
+    km_seed(seed);
     return field_create_impl(dkind, coords, x, y, z, d1, d2, w, wpos, n, min_size, max_size,
                              split_method, brute, min_top, max_top, true, out);
 }

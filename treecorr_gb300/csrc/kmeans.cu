@@ -668,6 +668,17 @@ double urand(long long seed = 0)
     return r;
 }
 
+}  // namespace
+
+// The field constructor's seed (BaseField, src/Field.cpp:160): a non-zero seed reseeds the
+// urand stream that the k-means initialisations draw from afterwards.
+void km_seed(long long seed)
+{
+    if (seed != 0) urand(seed);
+}
+
+namespace {
+
 // SelectRandomFrom (src/Corr2.cpp:622-661): n distinct values of [0, m) -- Floyd's
 // algorithm with a set when m > 3 n, else a partial Fisher-Yates shuffle.
 std::vector<long> select_random_from(long m, long n)

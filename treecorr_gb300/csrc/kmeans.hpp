@@ -23,6 +23,9 @@ struct KMField {
 };
 
 // centers: npatch rows of 2 (Flat) or 3 (ThreeD, Sphere) doubles, host memory.
+// Reseeds the k-means initialisations' urand stream for a non-zero seed (the field
+// constructor's seed, src/Field.cpp:160).
+void km_seed(long long seed);
 int kmeans_init_tree(const KMField& F, double* centers, int npatch, long long seed,
                      cudaStream_t st);
 int kmeans_init_rand(const KMField& F, double* centers, int npatch, long long seed,
