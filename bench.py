@@ -211,12 +211,27 @@ def run_gpu(args, rank, world):
                         0., out["xi0"], out["xi1"], out["xi2"], out["xi3"], out["meanr"],
                         out["meanlogr"], out["weight"], out["npairs"])
 
+    def device_field():
+        return T.DeviceField(2, T.Sphere, args.n, dcols["x"].data_ptr(), dcols["y"].data_ptr(),
+                             dcols["z"].data_ptr(), dcols["g1"].data_ptr(),
+                             dcols["g2"].data_ptr(), dcols["w"].data_ptr(), 0, 0.0, 0.0, T.Mean,
+                             0, False, 3, 10)
+
+    # The autotuner picks the tile leaf size and expansion chunk on a sample of the top-level
+    # pairs, once, outside the timed region; every step then uses its choice.
+    t0 = time.perf_counter()
+    f, c = device_field(), corr_for(outputs())
+    tune = c.autotune(f, metric=T.Arc, frac=args.tune_frac) if args.tune_frac > 0 else \
+        {"tile_leaf": 0, "chunk": 0, "ms": 0.}
+    tune["tune_s"] = round(time.perf_counter() - t0, 2)
+    tune["frac"] = args.tune_frac
+    del f, c
+
     def step_device():
         out = outputs()
-        f = T.DeviceField(2, T.Sphere, args.n, dcols["x"].data_ptr(), dcols["y"].data_ptr(),
-                          dcols["z"].data_ptr(), dcols["g1"].data_ptr(), dcols["g2"].data_ptr(),
-                          dcols["w"].data_ptr(), 0, 0.0, 0.0, T.Mean, 0, False, 3, 10)
+        f = device_field()
         c = corr_for(out)
+        c.setTuning(tune["tile_leaf"], tune["chunk"])
         c.processAuto(f, False, False, T.Arc)
         st = c.stats()
         del f, c
@@ -229,6 +244,7 @@ def run_gpu(args, rank, world):
                            hcols["g1"].numpy(), hcols["g2"].numpy(), hcols["w"].numpy(), e,
                            0.0, 0.0, T.Mean, 0, False, 3, 10)
         c = corr_for(out)
+        c.setTuning(tune["tile_leaf"], tune["chunk"])
         c.processAuto(f, False, False, T.Arc)
         st = c.stats()
         del f, c
@@ -329,6 +345,7 @@ def run_gpu(args, rank, world):
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e / args.steps},
         "gpu_launches": launches,
+        "tuning": tune,
         "roofline": roofline,
         "clocks": clocks,
         "detail": {"accepted_per_step": acc_per_step, "cell_pairs_per_step": st["cell_pairs"],
@@ -371,12 +388,27 @@ def exact_entry(args, T, dcols, hcols, timed, world):
         return {k: np.zeros(nb) for k in ("xi0", "xi1", "xi2", "xi3", "meanr", "meanlogr",
                                           "weight", "npairs")}
 
+    def device_field():
+        return T.DeviceField(2, T.Sphere, args.n, dcols["x"].data_ptr(), dcols["y"].data_ptr(),
+                             dcols["z"].data_ptr(), dcols["g1"].data_ptr(),
+                             dcols["g2"].data_ptr(), dcols["w"].data_ptr(), 0, 0.0, 0.0, T.Mean,
+                             0, False, 3, 10)
+
+    # The autotuner picks the tile leaf size and expansion chunk on a sample of the top-level
+    # pairs, once, outside the timed region; every step then uses its choice.
+    t0 = time.perf_counter()
+    f, c = device_field(), corr_for(outputs())
+    tune = c.autotune(f, metric=T.Arc, frac=args.tune_frac) if args.tune_frac > 0 else \
+        {"tile_leaf": 0, "chunk": 0, "ms": 0.}
+    tune["tune_s"] = round(time.perf_counter() - t0, 2)
+    tune["frac"] = args.tune_frac
+    del f, c
+
     def step_device():
         out = outputs()
-        f = T.DeviceField(2, T.Sphere, args.n, dcols["x"].data_ptr(), dcols["y"].data_ptr(),
-                          dcols["z"].data_ptr(), dcols["g1"].data_ptr(), dcols["g2"].data_ptr(),
-                          dcols["w"].data_ptr(), 0, 0.0, 0.0, T.Mean, 0, False, 3, 10)
+        f = device_field()
         c = corr_for(out)
+        c.setTuning(tune["tile_leaf"], tune["chunk"])
         c.processAuto(f, False, False, T.Arc)
         st = c.stats()
         del f, c
@@ -389,6 +421,7 @@ def exact_entry(args, T, dcols, hcols, timed, world):
                            hcols["g1"].numpy(), hcols["g2"].numpy(), hcols["w"].numpy(), e,
                            0.0, 0.0, T.Mean, 0, False, 3, 10)
         c = corr_for(out)
+        c.setTuning(tune["tile_leaf"], tune["chunk"])
         c.processAuto(f, False, False, T.Arc)
         st = c.stats()
         del f, c
@@ -423,6 +456,7 @@ def exact_entry(args, T, dcols, hcols, timed, world):
                      "peak_source": "SMs x 128 FP32 lanes x 2 flop x the median SM clock "
                                     "sampled under load (MEASURED_PEAKS.json has no FP32 "
                                     "figure)"},
+        "tuning": tune,
         "detail": {"accepted_per_step": st["accepted"], "tile_pairs": st["tile_pairs"],
                    "tiles": st["tiles"], "tile_escalated": st["tile_escalated"],
                    "cell_pairs": st["cell_pairs"], "build_ms": st["build_ms"],
@@ -1312,6 +1346,9 @@ def main():
     p.add_argument("--no-exact", action="store_true",
                    help="skip the accurate (bin_slop 0, angle_slop 0) entry")
     p.add_argument("--exact-steps", type=int, default=2)
+    p.add_argument("--tune-frac", type=float, default=0.02,
+                   help="fraction of top-level pairs the autotuner times per trial in the "
+                        "accurate entry (0: library defaults, no tuning)")
     p.add_argument("--traffic", type=float, default=None,
                    help="DRAM bytes per traversal launch from an ncu capture, if known")
     args = p.parse_args()

@@ -219,6 +219,24 @@ int tc_corr2_process_cross(tc_corr2* c, tc_field* f1, tc_field* f2, int dots, in
  * traverse_ms stays 0. */
 int tc_corr2_process_auto_noalloc(tc_corr2* c, tc_field* f, int quick, int metric);
 
+/* Tuning of the 2-point path (no reference counterpart: the reference's OpenMP loop has no
+ * such knobs).  tile_leaf: the most points per side of a leaf-pair tile of the exact mode
+ * (8..64; 0 = the default 48); chunk: work items per expansion launch, the depth of the
+ * breadth-first queue (2^16..2^25; 0 = the default, 2^24 or twice the points if fewer).
+ * Neither changes a result. */
+int tc_corr2_set_tuning(tc_corr2* c, int tile_leaf, int64_t chunk);
+
+/* The autotuner: times this correlation of f1 (and f2, NULL for an auto-correlation) on its
+ * first frac of top-level cell pairs for tile leaf sizes 24..64 (exact mode only), then for
+ * expansion chunks down to 1/8 of the default, keeps the fastest in c (as
+ * tc_corr2_set_tuning) and in a per-process cache keyed by the classes, coordinates, metric,
+ * binning, slops, brute flags and catalog sizes (to a factor of 2), so a later call with the
+ * same key returns at once.  The corr's output arrays are not touched.  Outputs: the chosen
+ * values (0 = default) and the best sample's device time in ms (0 from the cache).  No
+ * reference counterpart. */
+int tc_corr2_autotune(tc_corr2* c, tc_field* f1, tc_field* f2, int metric, double frac,
+                      int* tile_leaf, int64_t* chunk, double* ms);
+
 /* BaseCorr2.triviallyZero -> TriviallyZero (src/Corr2.cpp:1107-1128): 1 if no pair of
  * the two patches (centre + size) can fall in range.  Result in *out. */
 int tc_corr2_trivially_zero(tc_corr2* c, int metric, int coords,

@@ -104,6 +104,12 @@ def lib():
         fp = ctypes.POINTER(ctypes.c_float)
         L.tc_mlp_nparam.restype = ctypes.c_int
         L.tc_mlp_nparam.argtypes = []
+        L.tc_corr2_set_tuning.restype = ctypes.c_int
+        L.tc_corr2_set_tuning.argtypes = [vp, ctypes.c_int, i64]
+        L.tc_corr2_autotune.restype = ctypes.c_int
+        L.tc_corr2_autotune.argtypes = [vp, vp, vp, ctypes.c_int, ctypes.c_double,
+                                        ctypes.POINTER(ctypes.c_int), ctypes.POINTER(i64),
+                                        ctypes.POINTER(ctypes.c_double)]
         L.tc_corr2_set_learned.restype = ctypes.c_int
         L.tc_corr2_set_learned.argtypes = [vp, fp, ctypes.c_double, ctypes.c_double]
         L.tc_learn_collect.restype = ctypes.c_int
@@ -575,6 +581,23 @@ class BaseCorr2:
             pj.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _ptr(res), ctypes.byref(npair)))
         k = npair.value
         return list(zip(pi[:k].tolist(), pj[:k].tolist())), res[:k].copy()
+
+    def setTuning(self, tile_leaf=0, chunk=0):
+        """Tile leaf size and expansion chunk of the following process calls (0 = defaults).
+        No reference counterpart."""
+        _check(lib().tc_corr2_set_tuning(self._h, int(tile_leaf), int(chunk)))
+
+    def autotune(self, field1, field2=None, metric=None, frac=0.05):
+        """Times this correlation on a frac of its top-level pairs for several tile leaf sizes
+        and expansion chunks and keeps the fastest (cached per configuration for the process;
+        the output arrays are not touched).  Returns {tile_leaf, chunk, ms}.  No reference
+        counterpart."""
+        leaf, ch, ms = ctypes.c_int(0), ctypes.c_int64(0), ctypes.c_double(0.)
+        m = int(metric if metric is not None else Metric.Euclidean)
+        _check(lib().tc_corr2_autotune(self._h, field1._h, field2._h if field2 is not None else None,
+                                       m, float(frac), ctypes.byref(leaf), ctypes.byref(ch),
+                                       ctypes.byref(ms)))
+        return {"tile_leaf": leaf.value, "chunk": ch.value, "ms": ms.value}
 
     def setLearned(self, params=None, threshold=-2.0, cand_factor=4.0):
         """Use the learned opening criterion (params: tc_mlp_nparam() floats) in the following

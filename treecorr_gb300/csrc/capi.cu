@@ -11,6 +11,9 @@
 #include <cstdlib>
 #include <cstring>
 #include <limits>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -124,6 +127,13 @@ struct tc_corr2 {
     unsigned long long* tctl = nullptr;
     float* tedge = nullptr;              // [2][nbins+1]: 1/edge^2, log(edge)
     std::vector<cudaEvent_t> kev;        // per-launch events of an expansion batch
+    // Tuning (tc_corr2_set_tuning / tc_corr2_autotune): tile leaf size and items per
+    // expansion launch, 0 = the defaults.  root_limit / no_output: the autotuner's sample
+    // runs (only the first root_limit top-level pairs, results not added to the outputs).
+    int tile_leaf = 0;
+    long long chunk = 0;
+    long long root_limit = 0;
+    bool no_output = false;
     ~tc_corr2() { for (auto e : kev) cudaEventDestroy(e); }
 };
 
@@ -504,7 +514,7 @@ int expand_run(tc_corr2* c, const TravParams& T, int blocks, long long npoints, 
     // 4 chunks each: 512 MB per level at the largest size).  Large launches amortise the
     // per-launch work of every warp (bin set-up, the flush of its totals, the completion
     // count); 4M-item chunks took 19% longer on a 10M-point catalog.
-    const long long CH = expand_chunk(npoints);
+    const long long CH = c->chunk > 0 ? c->chunk : expand_chunk(npoints);
     if (!c->sched) TC_TRY(dalloc(&c->sched, 1));
     ExpandSched hs;
     std::memset(&hs, 0, sizeof(hs));
@@ -615,6 +625,7 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
     T.tops1 = f1->d_tops; T.tops2 = g->d_tops;
     T.ntop1 = (long long)f1->tops.size(); T.ntop2 = (long long)g->tops.size();
     T.ngen = f2 ? T.ntop1 * T.ntop2 : T.ntop1 * (T.ntop1 + 1) / 2;
+    if (c->root_limit > 0 && c->root_limit < T.ngen) T.ngen = c->root_limit;
     if (T.minsep <= 0. || T.binsize <= 0. || nb <= 0) {
         set_last_error("Log binning needs min_sep > 0, bin_size > 0, nbins > 0");
         return TC_ERR_ARG;
@@ -641,9 +652,10 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
     if (const char* ev = std::getenv("TCGPU_TILES")) tiles = tiles && std::atoi(ev) != 0;
     int tblocks = 0, twarps = 0;
     if (tiles) {
-        T.tile_leaf = TILE_LEAF;      // tiles_grid picks the kernel from T's classes
+        T.tile_leaf = c->tile_leaf > 0 ? c->tile_leaf : TILE_LEAF;   // (tiles_grid picks the
+                                                                     // kernel from T's classes)
         TC_TRY(tiles_grid(T, &tblocks, &twarps));
-        const long long cap = expand_chunk(f1->n + (f2 ? f2->n : 0));
+        const long long cap = c->chunk > 0 ? c->chunk : expand_chunk(f1->n + (f2 ? f2->n : 0));
         if (c->tile_cap < cap) {
             dfree(c->tiles);
             c->tiles = nullptr;
@@ -662,7 +674,7 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
         TC_CU(cudaMemcpyAsync(c->tedge, te.data(), te.size() * sizeof(float),
                               cudaMemcpyHostToDevice, st));
         TC_CU(cudaMemsetAsync(c->tctl, 0, 8 * sizeof(unsigned long long), st));
-        T.tile_leaf = TILE_LEAF;
+        T.tile_leaf = c->tile_leaf > 0 ? c->tile_leaf : TILE_LEAF;
         T.leaf_base1 = (int)(f1->n - 1);
         T.leaf_base2 = (int)(g->n - 1);
         T.tiles = c->tiles;
@@ -729,7 +741,7 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
     c->stats.tile_pairs = (int64_t)tcnt[3];
     c->stats.tile_escalated = (int64_t)tcnt[4];
     // Corr2::finishProcess adds into the caller's arrays (src/Corr2.cpp:527-566).
-    for (int k = 0; k < nb; ++k) {
+    for (int k = 0; k < nb && !c->no_output; ++k) {
         c->weight[k] += tot[k];
         if (!quick) {
             c->meanr[k] += tot[nb + k];
@@ -1799,6 +1811,112 @@ int tc_mlp_train(float* params, const float* x, const float* y, int64_t n, int s
     cudaStream_t st;
     TC_TRY(stream_get(&st));
     return mlp_train_host(params, x, y, n, steps, batch, lr, seed, loss_out, st) ? TC_ERR_CUDA : TC_OK;
+}
+
+int tc_corr2_set_tuning(tc_corr2* c, int tile_leaf, int64_t chunk)
+{
+    if (!c) { set_last_error("NULL corr"); return TC_ERR_ARG; }
+    if (tile_leaf != 0 && (tile_leaf < 8 || tile_leaf > 64)) {
+        set_last_error("tile_leaf must be 0 (default) or 8..64"); return TC_ERR_ARG;
+    }
+    if (chunk != 0 && (chunk < (1 << 16) || chunk > (1LL << 25))) {
+        set_last_error("chunk must be 0 (default) or 2^16..2^25 work items"); return TC_ERR_ARG;
+    }
+    c->tile_leaf = tile_leaf;
+    c->chunk = chunk;
+    return TC_OK;
+}
+
+namespace {
+// The autotuner's choices per configuration (classes, coordinates, metric, binning, slops,
+// brute fields and catalog sizes to a factor of 2), for the life of the process.
+struct TuneKey {
+    int d1, d2, coords, metric, nbins, brute, lg1, lg2;
+    double minsep, maxsep, b, a;
+    bool operator<(const TuneKey& o) const
+    {
+        return std::tie(d1, d2, coords, metric, nbins, brute, lg1, lg2, minsep, maxsep, b, a) <
+               std::tie(o.d1, o.d2, o.coords, o.metric, o.nbins, o.brute, o.lg1, o.lg2,
+                        o.minsep, o.maxsep, o.b, o.a);
+    }
+};
+std::map<TuneKey, std::pair<int, long long>> g_tuned;
+std::mutex g_tune_mu;
+int ilog2(long long n) { int l = 0; while (n > 1) { n >>= 1; ++l; } return l; }
+}  // namespace
+
+// Times the correlation of f1 (and f2) on its first `frac` of top-level pairs for tile leaf
+// sizes 24..64 (exact mode) and then for expansion chunks 2^21..2^24 items (a coordinate
+// search, event-timed device time), keeps the fastest in c and in a per-process cache, and
+// restores the caller's outputs untouched.
+int tc_corr2_autotune(tc_corr2* c, tc_field* f1, tc_field* f2, int metric, double frac,
+                      int* tile_leaf_out, int64_t* chunk_out, double* ms_out)
+{
+    if (!c || !f1) { set_last_error("NULL argument"); return TC_ERR_ARG; }
+    if (!(frac > 0. && frac <= 1.)) { set_last_error("frac must be in (0, 1]"); return TC_ERR_ARG; }
+    if (c->mode != 0) { set_last_error("autotune runs the bin_slop criterion only"); return TC_ERR_ARG; }
+    TuneKey key{c->d1, c->d2, f1->coords, metric, c->nbins, f1->brute + 2 * (f2 ? f2->brute : 0),
+                ilog2(f1->n + 1), f2 ? ilog2(f2->n + 1) : -1, c->minsep, c->maxsep, c->b, c->a};
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tuned.find(key);
+        if (it != g_tuned.end()) {
+            c->tile_leaf = it->second.first;
+            c->chunk = it->second.second;
+            if (tile_leaf_out) *tile_leaf_out = c->tile_leaf;
+            if (chunk_out) *chunk_out = c->chunk;
+            if (ms_out) *ms_out = 0.;
+            return TC_OK;
+        }
+    }
+    TC_TRY(field_build(f1));
+    if (f2) TC_TRY(field_build(f2));
+    const long long ntop1 = (long long)f1->tops.size();
+    const long long ngen = f2 ? ntop1 * (long long)f2->tops.size() : ntop1 * (ntop1 + 1) / 2;
+    const bool exact = c->a == 0. || (f1->brute && (f2 ? f2->brute : f1->brute));
+    const long long npoints = f1->n + (f2 ? f2->n : 0);
+    const long long ch0 = expand_chunk(npoints);
+    c->root_limit = std::max<long long>(1, (long long)(frac * (double)ngen));
+    c->no_output = true;
+    auto trial = [&](int leaf, long long ch, double* ms) {
+        c->tile_leaf = leaf;
+        c->chunk = ch;
+        const int rc = corr_process(c, f1, f2, 0, metric);
+        *ms = c->stats.traverse_ms;
+        return rc;
+    };
+    int best_leaf = 0;
+    long long best_ch = 0;
+    double best = 0., ms = 0.;
+    int rc = trial(exact ? TILE_LEAF : 0, ch0, &ms);   // allocations, first launches
+    if (!rc) rc = trial(exact ? TILE_LEAF : 0, ch0, &best);
+    best_leaf = exact ? TILE_LEAF : 0;
+    best_ch = ch0;
+    if (!rc && exact) {
+        for (int leaf = 24; leaf <= 64 && !rc; leaf += 8) {
+            if (leaf == TILE_LEAF) continue;
+            rc = trial(leaf, ch0, &ms);
+            if (!rc && ms < best) { best = ms; best_leaf = leaf; }
+        }
+    }
+    for (long long ch = ch0 >> 1; ch >= std::max<long long>(1LL << 21, ch0 >> 3) && !rc; ch >>= 1) {
+        rc = trial(best_leaf, ch, &ms);
+        if (!rc && ms < best) { best = ms; best_ch = ch; }
+    }
+    c->root_limit = 0;
+    c->no_output = false;
+    c->stats = tc_stats();
+    if (rc) { c->tile_leaf = 0; c->chunk = 0; return rc; }
+    c->tile_leaf = best_leaf;
+    c->chunk = best_ch == ch0 ? 0 : best_ch;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tuned[key] = {c->tile_leaf, c->chunk};
+    }
+    if (tile_leaf_out) *tile_leaf_out = c->tile_leaf;
+    if (chunk_out) *chunk_out = c->chunk;
+    if (ms_out) *ms_out = best;
+    return TC_OK;
 }
 
 int tc_corr2_process_auto(tc_corr2* c, tc_field* f, int dots, int quick, int metric)
