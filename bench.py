@@ -192,6 +192,7 @@ def run_gpu(args, rank, world):
     from treecorr_gb300 import _treecorr as T
     dev = torch.device("cuda", rank % max(torch.cuda.device_count(), 1))
     torch.cuda.set_device(dev)
+    T.SetDeterministic(bool(args.fixed_order))
     cat = curved_sky_catalog(args.n, seed=args.seed + rank)
     bins = binning(args.bin_slop)
     nb = bins["nbins"]
@@ -341,6 +342,7 @@ def run_gpu(args, rank, world):
                                f"bin_slop {args.bin_slop}, angle_slop 0.1",
                    "n": args.n, "nbins": nb, "bin_slop": args.bin_slop,
                    "parallelism": f"replicas{world}",
+                   "fixed_order": bool(args.fixed_order),
                    "l2": "inputs larger than L2 (480 MB columns + 1.3 GB tree); no flush"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e / args.steps},
@@ -1346,6 +1348,9 @@ def main():
     p.add_argument("--no-exact", action="store_true",
                    help="skip the accurate (bin_slop 0, angle_slop 0) entry")
     p.add_argument("--exact-steps", type=int, default=2)
+    p.add_argument("--fixed-order", type=int, default=1, choices=(0, 1),
+                   help="1: fixed-order expansion (bit-identical repeats, the library's "
+                        "default); 0: children appended in arrival order")
     p.add_argument("--tune-frac", type=float, default=0.02,
                    help="fraction of top-level pairs the autotuner times per trial in the "
                         "accurate entry (0: library defaults, no tuning)")

@@ -378,6 +378,17 @@ int tc_mlp_train(float* params, const float* x, const float* y, int64_t n, int s
 int tc_set_omp_threads(int num_threads);
 int tc_get_omp_threads(void);
 
+/* Fixed-order 2-point expansion (no reference counterpart; the reference's results repeat
+ * bit for bit with num_threads = 1, tests/test_gg.py:573-574).  On (the default): the
+ * children and tiles of every expansion launch are joined in warp order, so every warp
+ * takes the same items in every run and all floating-point sums of a process call repeat
+ * bit for bit.  Off: they are appended in the order warps finish (slightly faster; sums
+ * then vary in the last bits from run to run).  Applies to the bin_slop and learned
+ * criteria of process/processAuto/processCross (not to the patch batch or the
+ * allocation-free call).  Returns the previous setting. */
+int tc_set_deterministic(int on);
+int tc_get_deterministic(void);
+
 /* Message of the last failure on the calling thread ("" if none). */
 const char* tc_last_error(void);
 

@@ -126,6 +126,10 @@ def lib():
         L.tc_set_omp_threads.argtypes = [ctypes.c_int]
         L.tc_get_omp_threads.restype = ctypes.c_int
         L.tc_get_omp_threads.argtypes = []
+        L.tc_set_deterministic.restype = ctypes.c_int
+        L.tc_set_deterministic.argtypes = [ctypes.c_int]
+        L.tc_get_deterministic.restype = ctypes.c_int
+        L.tc_get_deterministic.argtypes = []
         L.tc_last_error.restype = ctypes.c_char_p
         L.tc_last_error.argtypes = []
         L.tc_corr3_create.restype = ctypes.c_int
@@ -234,6 +238,17 @@ def SetOMPThreads(num_threads):
 def GetOMPThreads():
     """GetOMPThreads (src/Corr2.cpp:1005-1011); returns 1."""
     return lib().tc_get_omp_threads()
+
+
+def SetDeterministic(on=True):
+    """Fixed-order 2-point expansion (default on): repeated process calls give bit-identical
+    sums.  Returns the previous setting.  No reference counterpart."""
+    return bool(lib().tc_set_deterministic(1 if on else 0))
+
+
+def GetDeterministic():
+    """Whether the fixed-order 2-point expansion is on.  No reference counterpart."""
+    return bool(lib().tc_get_deterministic())
 
 
 def _arr(a, n=None, name="array"):

@@ -31,6 +31,8 @@ static thread_local std::string g_last_error;
 void set_last_error(const std::string& msg) { g_last_error = msg; }
 
 static std::atomic<long long> g_launches{0};
+// Fixed-order 2-point expansion (bitwise repeatable sums); tc_set_deterministic.
+static std::atomic<int> g_deterministic{1};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 static cudaStream_t g_stream = nullptr;
@@ -134,6 +136,13 @@ struct tc_corr2 {
     long long chunk = 0;
     long long root_limit = 0;
     bool no_output = false;
+    // Fixed-order expansion regions (tc_set_deterministic): per warp, 4 children and 1 tile
+    // per item it takes at most; counts [2][nwarps].
+    int2* det_out = nullptr;
+    int2* det_tout = nullptr;
+    int* det_cnt = nullptr;
+    long long det_out_cap = 0, det_tout_cap = 0;
+    int det_cnt_cap = 0;
     ~tc_corr2() { for (auto e : kev) cudaEventDestroy(e); }
 };
 
@@ -684,6 +693,35 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
         T.tile_wbase = nwarps;
         T.tile_edge = c->tedge;
         T.tile_ledge = c->tedge + nb + 1;
+    }
+    if (g_deterministic.load() && (mode == 0 || mode == 2)) {
+        // Fixed-order expansion: every warp's children and tiles go to regions of its own,
+        // joined in warp order after each launch (k_compact).
+        const long long CH = c->chunk > 0 ? c->chunk : expand_chunk(f1->n + (f2 ? f2->n : 0));
+        const long long ipw = det_items_per_warp(CH, nwarps);
+        const long long need_out = 4 * ipw * nwarps, need_t = tiles ? ipw * nwarps : 0;
+        if (c->det_out_cap < need_out) {
+            dfree(c->det_out); c->det_out = nullptr; c->det_out_cap = 0;
+            TC_TRY(dalloc(&c->det_out, (size_t)need_out));
+            c->det_out_cap = need_out;
+        }
+        if (c->det_tout_cap < need_t) {
+            dfree(c->det_tout); c->det_tout = nullptr; c->det_tout_cap = 0;
+            TC_TRY(dalloc(&c->det_tout, (size_t)need_t));
+            c->det_tout_cap = need_t;
+        }
+        if (c->det_cnt_cap < 2 * nwarps) {
+            dfree(c->det_cnt); c->det_cnt = nullptr; c->det_cnt_cap = 0;
+            TC_TRY(dalloc(&c->det_cnt, (size_t)2 * nwarps));
+            c->det_cnt_cap = 2 * nwarps;
+        }
+        T.det = 1;
+        T.det_nw = nwarps;
+        T.det_out = c->det_out;
+        T.det_tout = c->det_tout;
+        T.det_cnt = c->det_cnt;
+        T.det_ccap = 4 * ipw;
+        T.det_tcap = ipw;
     }
     TC_TRY(expand_scratch(c, nwarps + twarps, nq));
     T.nsamples = c->ctl + 6;   // ctl exists from here on
@@ -1419,6 +1457,7 @@ void tc_corr2_free(tc_corr2* c)
     dfree(c->sched);
     dfree(c->mlp); dfree(c->samples);
     dfree(c->tiles); dfree(c->tctl); dfree(c->tedge);
+    dfree(c->det_out); dfree(c->det_tout); dfree(c->det_cnt);
     delete c;
 }
 
@@ -2107,6 +2146,14 @@ int tc_corr3_stats(const tc_corr3* c, int64_t out[3])
 
 int tc_set_omp_threads(int num_threads) { (void)num_threads; return 1; }
 int tc_get_omp_threads(void) { return 1; }
+
+int tc_set_deterministic(int on)
+{
+    const int prev = g_deterministic.load();
+    g_deterministic.store(on ? 1 : 0);
+    return prev;
+}
+int tc_get_deterministic(void) { return g_deterministic.load(); }
 
 const char* tc_last_error(void) { return g_last_error.c_str(); }
 

@@ -353,8 +353,9 @@ __device__ __forceinline__ void tile_fast(const TravParams& T, const TileLeaves&
 
 // The general pair loop: range test near min_sep / max_sep, the bin of every pair with its
 // FP32 error band, FP64 re-decision inside the band, self tiles (j > i).  Bins kref and
-// kref + 1 are summed in registers, other bins and FP64-decided pairs go to the warp's
-// shared-memory bins directly.
+// kref + 1 are summed in registers; other bins and FP64-decided pairs go to the warp's
+// shared-memory bins, added lane by lane in ascending lane order (broadcast by shuffles), so
+// that the sums do not depend on the order in which conflicting shared atomics would land.
 template <int GEO, int KIND>
 __device__ __forceinline__ void tile_general(const TravParams& T, const TileLeaves& LA,
                                              const TileLeaves& SB, const TileCtx& C, int lane,
@@ -368,70 +369,88 @@ __device__ __forceinline__ void tile_general(const TravParams& T, const TileLeav
     const float ckk = ln2h * T.finvbinsize;
     int ii = lane / nbl, jj = lane - ii * nbl;
     const int di = 32 / nbl, dj = 32 - di * nbl;
-    for (int p = lane; p < npt; p += 32) {
+    for (int p0 = 0; p0 < npt; p0 += 32) {
         const int i = ii, j = jj;
         jj += dj; ii += di;
         if (jj >= nbl) { jj -= nbl; ++ii; }
-        if (C.self && j <= i) continue;
-        ++n_pairs;
-        const float4 Pa = LA.P[i], Wa = LA.W[i], Pb = SB.P[j], Wb = SB.W[j];
-        const float dx = Pa.x - Pb.x, dy = Pa.y - Pb.y;
-        const float dz = GEO == TG_FLAT ? 0.f : Pa.z - Pb.z;
-        const float dsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const float invc = rsqrtf(dsq);
-        float r = dsq * invc;
-        if (GEO == TG_ARC) r = C.small_chord ? arc_series(r) : arc_from_chord_sq(dsq);
-        float lr = __log2f(r * r * C.inv_edge);
-        bool unsure = false;
-        int k = C.kref;
-        if (!C.interior) {
-            const float dr = C.emax + 4e-7f * r;
-            if (r + dr < T.fminsep || r - dr >= T.fmaxsep) continue;
-            unsure = !(r - dr >= T.fminsep && r + dr < T.fmaxsep);
-        }
-        if (!unsure) {
-            const float kk = lr * ckk;
-            const float fk = floorf(kk);
-            const float fr = kk - fk;
-            const float band = fmaf(C.band_e, invc, C.band_0);
-            k = C.kref + (int)fk;
-            unsure = fr < band || fr > 1.f - band || k < 0;
-            if (k >= nb) k = nb - 1;                    // the clamp of src/Corr2.cpp:514
-        }
-        float logr = fmaf(lr, ln2h, C.ledge);
-        if (unsure) {
-            ++n_esc;
-            k = leaf_pair64(T, __float_as_int(LA.X[i].z), __float_as_int(SB.X[j].z), C.self, &r,
-                            &logr);
-            if (k < 0) continue;
-        }
-        ++n_acc;
-        const float ww = Wa.x * Wb.x;
-        float v[8] = {ww, ww * r, ww * lr, 0.f, 0.f, 0.f, 0.f, 0.f};
-        if constexpr (KIND != TK_NN) {
-            float x[4] = {0.f, 0.f, 0.f, 0.f}, sc;
-            pair_products<GEO, KIND>(T, LA, SB, i, j, Pa, Wa, Pb, Wb, dx, dy, dz, dsq, r, logr,
-                                     x, sc);
+        int kx = -1;             // the shared-memory bin of this lane's pair, if it has one
+        float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        do {                     // (break: no pair to add)
+            if (p0 + lane >= npt || (C.self && j <= i)) break;
+            ++n_pairs;
+            const float4 Pa = LA.P[i], Wa = LA.W[i], Pb = SB.P[j], Wb = SB.W[j];
+            const float dx = Pa.x - Pb.x, dy = Pa.y - Pb.y;
+            const float dz = GEO == TG_FLAT ? 0.f : Pa.z - Pb.z;
+            const float dsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const float invc = rsqrtf(dsq);
+            float r = dsq * invc;
+            if (GEO == TG_ARC) r = C.small_chord ? arc_series(r) : arc_from_chord_sq(dsq);
+            float lr = __log2f(r * r * C.inv_edge);
+            bool unsure = false;
+            int k = C.kref;
+            if (!C.interior) {
+                const float dr = C.emax + 4e-7f * r;
+                if (r + dr < T.fminsep || r - dr >= T.fmaxsep) break;
+                unsure = !(r - dr >= T.fminsep && r + dr < T.fmaxsep);
+            }
+            if (!unsure) {
+                const float kk = lr * ckk;
+                const float fk = floorf(kk);
+                const float fr = kk - fk;
+                const float band = fmaf(C.band_e, invc, C.band_0);
+                k = C.kref + (int)fk;
+                unsure = fr < band || fr > 1.f - band || k < 0;
+                if (k >= nb) k = nb - 1;                    // the clamp of src/Corr2.cpp:514
+            }
+            float logr = fmaf(lr, ln2h, C.ledge);
+            if (unsure) {
+                ++n_esc;
+                k = leaf_pair64(T, __float_as_int(LA.X[i].z), __float_as_int(SB.X[j].z), C.self,
+                                &r, &logr);
+                if (k < 0) break;
+            }
+            ++n_acc;
+            const float ww = Wa.x * Wb.x;
+            v[0] = ww; v[1] = ww * r; v[2] = ww * lr;
+            if constexpr (KIND != TK_NN) {
+                float x[4] = {0.f, 0.f, 0.f, 0.f}, sc;
+                pair_products<GEO, KIND>(T, LA, SB, i, j, Pa, Wa, Pb, Wb, dx, dy, dz, dsq, r,
+                                         logr, x, sc);
 #pragma unroll
-            for (int q = 0; q < 4; ++q) v[3 + q] = x[q] * sc;
-        }
-        const unsigned nn = (unsigned)__float_as_int(Wa.w) * (unsigned)__float_as_int(Wb.w);
-        if (!unsure && k == C.kref) {
+                for (int q = 0; q < 4; ++q) v[3 + q] = x[q] * sc;
+            }
+            const unsigned nn = (unsigned)__float_as_int(Wa.w) * (unsigned)__float_as_int(Wb.w);
+            if (!unsure && k == C.kref) {
 #pragma unroll
-            for (int q = 0; q < 7; ++q) acc0[q] += v[q];
-            c0 += nn;
-        } else if (!unsure && k == C.kref + 1) {
+                for (int q = 0; q < 7; ++q) acc0[q] += v[q];
+                c0 += nn;
+            } else if (!unsure && k == C.kref + 1) {
 #pragma unroll
-            for (int q = 0; q < 7; ++q) acc1[q] += v[q];
-            c1 += nn;
-        } else {
-            v[2] = ww * logr;   // the FP64 pair's own log r, or the tile edge's
+                for (int q = 0; q < 7; ++q) acc1[q] += v[q];
+                c1 += nn;
+            } else {
+                v[2] = ww * logr;   // the FP64 pair's own log r, or the tile edge's
+                kx = k;
+                if (!T.quick) atomicAdd(&np[k], (unsigned long long)nn);   // exact integer
+            }
+        } while (false);
+        // The pairs bound for the shared bins, in ascending lane order: lane q < nq adds
+        // quantity q of each.
+        unsigned m = __ballot_sync(0xffffffffu, kx >= 0);
+        while (m) {
+            const int t = __ffs(m) - 1;
+            m &= m - 1u;
+            const int kt = __shfl_sync(0xffffffffu, kx, t);
+            float x = 0.f;
 #pragma unroll
-            for (int q = 0; q < 7; ++q)
-                if (q < nq) atomicAdd(&fb[q * nb + k], v[q]);
-            if (!T.quick) atomicAdd(&np[k], (unsigned long long)nn);
+            for (int q = 0; q < 7; ++q) {
+                const float y = __shfl_sync(0xffffffffu, v[q], t);
+                x = lane == q ? y : x;
+            }
+            if (lane < nq) fb[lane * nb + kt] += x;
         }
     }
+    __syncwarp();
 }
 
 template <int GEO, int KIND>

@@ -664,6 +664,21 @@ __device__ __forceinline__ void expand_warp_done(const ExpandSched* S, int lane)
     }
 }
 
+// End of an expansion warp: the fixed-order mode records the warp's region counts (k_compact
+// commits them and takes the schedule step); otherwise the completion count above.
+__device__ __forceinline__ void expand_finish(const TravParams& T, const ExpandSched* S, int gw,
+                                              long long lo_ch, long long lo_tl, int lane)
+{
+    if (T.det) {
+        if (lane == 0) {
+            T.det_cnt[gw] = (int)(lo_ch < T.det_ccap ? lo_ch : T.det_ccap);
+            T.det_cnt[T.det_nw + gw] = (int)(lo_tl < T.det_tcap ? lo_tl : T.det_tcap);
+        }
+        return;
+    }
+    expand_warp_done(S, lane);
+}
+
 #ifndef EXPAND_MINB
 #define EXPAND_MINB 7   // resident blocks per SM the register budget is sized for (72 registers)
 #endif
@@ -706,6 +721,7 @@ __global__ void __launch_bounds__(TB, EXPAND_MINB) k_expand(TravParams T, const 
     }
     __syncwarp();
     long long n_eval = 0, n_acc = 0, n_esc = 0, n_learn = 0;
+    long long lo_ch = 0, lo_tl = 0;   // fixed-order mode: children and tiles in the regions
     int cur_pair = -1;   // mode 3: the patch pair the warp's bins hold
     const long long stride = (long long)gridDim.x * TB;
     int iter = 0;
@@ -774,7 +790,16 @@ __global__ void __launch_bounds__(TB, EXPAND_MINB) k_expand(TravParams T, const 
         }
         const int tot = __shfl_sync(0xffffffffu, off, 31);
         off -= nch;
-        if (tot > 0) {
+        if (tot > 0 && T.det) {
+            // Fixed order: the warp's own region, in iteration and lane order.
+            if (lo_ch + tot > T.det_ccap) {
+                if (lane == 0) atomicCAS(T.err, 0, DEV_SPILL_OVERFLOW);
+            } else {
+                int2* o = T.det_out + (size_t)gw * T.det_ccap + lo_ch + off;
+                for (int c = 0; c < nch; ++c) o[c] = ch[c];
+            }
+            lo_ch += tot;
+        } else if (tot > 0) {
             unsigned long long o0 = 0;
             if (lane == 0) o0 = atomicAdd(nout, (unsigned long long)tot);
             o0 = __shfl_sync(0xffffffffu, o0, 0);
@@ -787,14 +812,22 @@ __global__ void __launch_bounds__(TB, EXPAND_MINB) k_expand(TravParams T, const 
         if (MODE == 0 && T.tile_leaf > 0) {
             // Tiles go to the tile list that k_tiles, launched after this kernel, drains.
             const unsigned tm = __ballot_sync(0xffffffffu, tl.x >= 0);
-            if (tm) {
+            const int before = __popc(tm & ((1u << lane) - 1u));
+            if (tm && T.det) {
+                if (lo_tl + __popc(tm) > T.det_tcap) {
+                    if (lane == 0) atomicCAS(T.err, 0, DEV_SPILL_OVERFLOW);
+                } else if (tl.x >= 0) {
+                    T.det_tout[(size_t)gw * T.det_tcap + lo_tl + before] = tl;
+                }
+                lo_tl += __popc(tm);
+            } else if (tm) {
                 unsigned long long t0 = 0;
                 if (lane == 0) t0 = atomicAdd(&T.tctl[0], (unsigned long long)__popc(tm));
                 t0 = __shfl_sync(0xffffffffu, t0, 0);
                 if ((long long)(t0 + __popc(tm)) > T.tile_cap) {
                     if (lane == 0) atomicCAS(T.err, 0, DEV_SPILL_OVERFLOW);
                 } else if (tl.x >= 0) {
-                    T.tiles[t0 + __popc(tm & ((1u << lane) - 1u))] = tl;
+                    T.tiles[t0 + before] = tl;
                 }
             }
         }
@@ -812,7 +845,7 @@ __global__ void __launch_bounds__(TB, EXPAND_MINB) k_expand(TravParams T, const 
     }
     if (n_acc == 0) {   // nothing accumulated by this warp in this launch
         if (lane == 0 && n_eval) atomicAdd(&T.counters[0], (unsigned long long)n_eval);
-        expand_warp_done(S, lane);
+        expand_finish(T, S, gw, lo_ch, lo_tl, lane);
         return;
     }
     if constexpr (MODE == 3) {
@@ -838,7 +871,7 @@ __global__ void __launch_bounds__(TB, EXPAND_MINB) k_expand(TravParams T, const 
         atomicAdd(&T.counters[2], (unsigned long long)n_esc);
         if (MODE == 2 && n_learn) atomicAdd(&T.counters[3], (unsigned long long)n_learn);
     }
-    expand_warp_done(S, lane);
+    expand_finish(T, S, gw, lo_ch, lo_tl, lane);
 }
 
 // The schedule step: commits the previous launch's children and picks the next chunk.
@@ -874,6 +907,113 @@ __device__ void sched_step(ExpandSched* S)
 __global__ void k_expand_sched(ExpandSched* S)
 {
     if (!S->pending) sched_step(S);
+}
+
+// Fixed-order expansion: joins the child and tile regions of the expansion launch that just
+// ran, in warp order, into the level buffer (S->out) and the tile list; then the last block
+// commits the children and takes the schedule step, which the last warp of an expansion
+// launch does otherwise.  Block b copies the regions of warps CPB b .. CPB b + CPB - 1, one
+// per warp; every count is an integer, so the offsets do not depend on timing.
+static constexpr int CPB = 8;
+
+__device__ __forceinline__ long long warp_sum_ll(long long v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Copies n items from src to dst with 8 loads in flight per lane.
+__device__ __forceinline__ void copy_items(int2* dst, const int2* src, int n, int lane)
+{
+    for (int i0 = 0; i0 < n; i0 += 256) {
+        int2 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int i = i0 + 32 * u + lane;
+            if (i < n) v[u] = src[i];
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int i = i0 + 32 * u + lane;
+            if (i < n) dst[i] = v[u];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(CPB * 32) k_compact(const __grid_constant__ TravParams T,
+                                                      ExpandSched* S)
+{
+    if (S->n_in <= 0) return;   // the expansion launch had nothing to do
+    __shared__ long long red[2][CPB];
+    __shared__ int last;
+    const int nw = T.det_nw, tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    const int* cc = T.det_cnt;
+    const int* ct = T.det_cnt + nw;
+    const int r0 = blockIdx.x * CPB;
+    // Counts of the regions before this block's, four at a time (nw and r0 are multiples of
+    // 4, so both count arrays are 16-byte aligned).
+    long long pc = 0, pt = 0;
+    const int4* cc4 = reinterpret_cast<const int4*>(cc);
+    const int4* ct4 = reinterpret_cast<const int4*>(ct);
+    for (int q = tid; q < r0 / 4; q += CPB * 32) {
+        const int4 a = cc4[q], b = ct4[q];
+        pc += (long long)a.x + a.y + a.z + a.w;
+        pt += (long long)b.x + b.y + b.z + b.w;
+    }
+    pc = warp_sum_ll(pc);
+    pt = warp_sum_ll(pt);
+    if (lane == 0) { red[0][w] = pc; red[1][w] = pt; }
+    __syncthreads();
+    long long oc = 0, ot = 0;
+    for (int q = 0; q < CPB; ++q) { oc += red[0][q]; ot += red[1][q]; }
+    const int r = r0 + w;
+    if (r < nw) {
+        for (int q = r0; q < r; ++q) { oc += cc[q]; ot += ct[q]; }
+        const int n = cc[r], m = ct[r];
+        if (oc + n > S->out_cap) {
+            if (lane == 0) atomicCAS(T.err, 0, DEV_SPILL_OVERFLOW);
+        } else {
+            copy_items(S->out + oc, T.det_out + (size_t)r * T.det_ccap, n, lane);
+        }
+        if (m > 0 && ot + m > T.tile_cap) {
+            if (lane == 0) atomicCAS(T.err, 0, DEV_SPILL_OVERFLOW);
+        } else if (m > 0) {
+            copy_items(T.tiles + ot, T.det_tout + (size_t)r * T.det_tcap, m, lane);
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        __threadfence();
+        last = atomicAdd(&S->warps_done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    long long tc = 0, tt = 0;
+    for (int q = tid; q < nw / 4; q += CPB * 32) {
+        const int4 a = cc4[q], b = ct4[q];
+        tc += (long long)a.x + a.y + a.z + a.w;
+        tt += (long long)b.x + b.y + b.z + b.w;
+    }
+    tc = warp_sum_ll(tc);
+    tt = warp_sum_ll(tt);
+    if (lane == 0) { red[0][w] = tc; red[1][w] = tt; }
+    __syncthreads();
+    if (tid == 0) {
+        tc = 0; tt = 0;
+        for (int q = 0; q < CPB; ++q) { tc += red[0][q]; tt += red[1][q]; }
+        S->warps_done = 0;
+        S->nout = (unsigned long long)(tc < S->out_cap ? tc : S->out_cap);
+        if (T.tile_leaf > 0) T.tctl[0] = (unsigned long long)(tt < T.tile_cap ? tt : T.tile_cap);
+        sched_step(S);
+    }
+}
+
+long long det_items_per_warp(long long chunk, int nwarps)
+{
+    const long long per = 32LL * nwarps;
+    return 32LL * ((chunk + per - 1) / per);
 }
 
 // Sum of the per-warp totals in a fixed order: out[q*nb+k] (double), outnp[k] (u64).
@@ -951,6 +1091,10 @@ int launch_expand_batch(const TravParams& T, int blocks, ExpandSched* dS, int it
         else if (T.mode == 2) k_expand<2><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
         else if (T.mode == 1) k_expand<1><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
         else k_expand<0><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
+        if (T.det) {
+            count_launch();
+            k_compact<<<(T.det_nw + CPB - 1) / CPB, CPB * 32, 0, st>>>(T, dS);
+        }
         if (ev) TC_CU(cudaEventRecord(ev[3 * it + 1], st));
         if (T.mode == 0 && T.tile_leaf > 0) TC_TRY(launch_tiles(T, st));
         if (ev) TC_CU(cudaEventRecord(ev[3 * it + 2], st));

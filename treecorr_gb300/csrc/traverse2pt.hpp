@@ -80,6 +80,17 @@ struct TravParams {
     int tile_blocks, tile_wbase;    // k_tiles grid; its warps' slots start at tile_wbase
     const float* tile_edge;         // [nbins+1]: 1 / (min_sep^2 exp(2 k bin_size))
     const float* tile_ledge;        // [nbins+1]: log(min_sep) + k bin_size
+    // Fixed-order expansion (det != 0; modes 0 and 2): every warp of an expansion launch
+    // writes its children and tiles into regions of its own (det_out + gw det_ccap,
+    // det_tout + gw det_tcap) and their counts into det_cnt[gw] and det_cnt[det_nw + gw];
+    // k_compact then joins the regions in warp order.  The level buffers and the tile list,
+    // and with them the items every warp takes and the order of every floating-point sum,
+    // are then the same from run to run.
+    int det, det_nw;
+    int2* det_out;
+    int2* det_tout;
+    int* det_cnt;
+    long long det_ccap, det_tcap;
 };
 
 // Fixed traversal scratch of the allocation-free entry point (traverse2pt.cu).
@@ -132,6 +143,9 @@ int expand_grid(int nq, int nb, int* blocks, int* nwarps, int mode = 0);
 // ev[3 it + 1] after it (= before the tiles), ev[3 it + 2] after the tiles.
 int launch_expand_batch(const TravParams& T, int blocks, ExpandSched* dS, int iters,
                         cudaStream_t st, cudaEvent_t* ev = nullptr);
+// Items an expansion warp takes at most in one launch of `chunk` items (the size of its
+// fixed-order regions: 4 children and 1 tile per item at most).
+long long det_items_per_warp(long long chunk, int nwarps);
 // Leaf-pair tiles (tiles.cu): the leaf size of a tile side, the k_tiles grid for a traversal
 // (its blocks fill every SM), and one k_tiles launch over the tiles waiting in T.tiles.
 static constexpr int TILE_LEAF = 48;
