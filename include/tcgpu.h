@@ -331,6 +331,39 @@ int tc_generate_xyz(double* x, double* y, double* z, const double* ra, const dou
 int tc_generate_xyz_device(double* x, double* y, double* z, const double* ra,
                            const double* dec, const double* r, int64_t n);
 
+/* Catalog ingestion: the column work of Catalog._finish_input (treecorr/catalog.py:
+ * 1343-1487) on the GPU.  In order: flag -> weight (1393-1404: w = 0, and wpos = 0 when given,
+ * where (flag & ignore_flag) != 0; the Python layer's ignore_flag is ~ok_flag unless given);
+ * checkForNaN (1406-1425, 1684-1704) on the ncols columns in the given order, then on w,
+ * then on wpos (a NaN row gets w = 0 and the NaN becomes 0); wpos == 0 -> w = 0 (1433-1450);
+ * sumw (1452-1462); removal of the rows with wpos == 0 (w == 0 without wpos) unless
+ * keep_zero_weight, when the weights are non-trivial (1464-1468, Catalog.select).  The
+ * weights are non-trivial when w_given, flag != NULL, a NaN was found or some wpos is 0;
+ * otherwise w is filled with 1 and sumw = n.  The columns (positions: x, y, z or ra, dec,
+ * r; values: k, g1, g2, ...) are changed in place; removed rows are dropped keeping the
+ * order, info->nkeep rows remain.  w: length n (the caller's weights when w_given, else any
+ * buffer, filled here); wpos, flag: NULL when absent.  sumw == 0 with non-trivial weights
+ * is TC_ERR_ARG ("Catalog has invalid sumw == 0"), as the reference raises.  Positions from
+ * ra/dec then come from tc_generate_xyz(_device).  Host arrays for tc_catalog_finish
+ * (copied to the device and back), device arrays for tc_catalog_finish_device (cols is a
+ * host array of device pointers). */
+#define TC_CAT_MAXCOLS 24
+typedef struct {
+    int64_t nkeep;           /* rows left */
+    int64_t nobj;            /* rows with w != 0 (Catalog.nobj) */
+    double sumw;             /* Catalog.sumw */
+    int nontrivial_w;        /* Catalog.nontrivial_w */
+    int64_t wpos_zero;       /* rows with wpos == 0 */
+    int64_t wpos_conflicts;  /* of those, rows whose w was not 0 (the reference's logged error) */
+    int64_t nan_counts[TC_CAT_MAXCOLS + 2];   /* NaNs per column, then w, then wpos */
+} tc_catalog_info;
+int tc_catalog_finish(int64_t n, int ncols, double* const* cols, double* w, double* wpos,
+                      const int64_t* flag, int64_t ignore_flag, int w_given,
+                      int keep_zero_weight, tc_catalog_info* info);
+int tc_catalog_finish_device(int64_t n, int ncols, double* const* cols, double* w,
+                             double* wpos, const int64_t* flag, int64_t ignore_flag,
+                             int w_given, int keep_zero_weight, tc_catalog_info* info);
+
 /* Self-check of the tcgen05 tensor-core path (no reference counterpart): one CTA computes
  * c[128 x n] = a[128 x k] * b[n x k]^T in TF32 through TMEM (k in 8..64, multiple of 8;
  * n in 16..64, multiple of 16).  Host arrays, row-major. */

@@ -36,6 +36,16 @@ class tc_stats(ctypes.Structure):
                 ("expand_ms", ctypes.c_double), ("tiles_ms", ctypes.c_double)]
 
 
+CAT_MAXCOLS = 24
+
+
+class tc_catalog_info(ctypes.Structure):
+    _fields_ = [("nkeep", ctypes.c_int64), ("nobj", ctypes.c_int64), ("sumw", ctypes.c_double),
+                ("nontrivial_w", ctypes.c_int), ("wpos_zero", ctypes.c_int64),
+                ("wpos_conflicts", ctypes.c_int64),
+                ("nan_counts", ctypes.c_int64 * (CAT_MAXCOLS + 2))]
+
+
 _lib = None
 
 
@@ -101,6 +111,14 @@ def lib():
         L.tc_generate_xyz.argtypes = [dp, dp, dp, dp, dp, dp, i64]
         L.tc_generate_xyz_device.restype = ctypes.c_int
         L.tc_generate_xyz_device.argtypes = [vp, vp, vp, vp, vp, vp, i64]
+        L.tc_catalog_finish.restype = ctypes.c_int
+        L.tc_catalog_finish.argtypes = [i64, ctypes.c_int, ctypes.POINTER(dp), dp, dp,
+                                        ctypes.POINTER(ctypes.c_int64), i64, ctypes.c_int,
+                                        ctypes.c_int, ctypes.POINTER(tc_catalog_info)]
+        L.tc_catalog_finish_device.restype = ctypes.c_int
+        L.tc_catalog_finish_device.argtypes = [i64, ctypes.c_int, ctypes.POINTER(vp), vp, vp, vp,
+                                               i64, ctypes.c_int, ctypes.c_int,
+                                               ctypes.POINTER(tc_catalog_info)]
         fp = ctypes.POINTER(ctypes.c_float)
         L.tc_mlp_nparam.restype = ctypes.c_int
         L.tc_mlp_nparam.argtypes = []
@@ -460,6 +478,75 @@ def GenerateXYZ(x, y, z, ra, dec, r):
     rr = np.ascontiguousarray(r, dtype=float) if len(r) else None
     _check(lib().tc_generate_xyz(_ptr(x), _ptr(y), _ptr(z), _ptr(ra), _ptr(dec),
                                  _ptr(rr) if rr is not None else None, n))
+
+
+# ----------------------------------------------------------------------------------------
+# Catalog ingestion (treecorr/catalog.py:1343-1487; include/tcgpu.h tc_catalog_finish).
+
+# The order of the reference's checkForNaN calls (treecorr/catalog.py:1407-1425).
+CAT_COLUMNS = ("x", "y", "z", "ra", "dec", "r", "k", "z1", "z2", "v1", "v2", "g1", "g2",
+               "t1", "t2", "q1", "q2")
+
+
+def _cat_info(info, names, has_wpos):
+    counts = {nm: int(info.nan_counts[i]) for i, nm in enumerate(names)}
+    counts["w"] = int(info.nan_counts[len(names)])
+    if has_wpos:
+        counts["wpos"] = int(info.nan_counts[len(names) + 1])
+    return dict(nkeep=int(info.nkeep), nobj=int(info.nobj), sumw=float(info.sumw),
+                nontrivial_w=bool(info.nontrivial_w), wpos_zero=int(info.wpos_zero),
+                wpos_conflicts=int(info.wpos_conflicts), nan_counts=counts)
+
+
+def catalog_finish(cols, w=None, wpos=None, flag=None, ignore_flag=None, ok_flag=0,
+                   keep_zero_weight=False):
+    """Catalog._finish_input's column work on the GPU (flag -> w, NaN checks, wpos == 0,
+    sumw, removal of zero-weight rows; treecorr/catalog.py:1343-1487).  cols: name -> array
+    (names from CAT_COLUMNS).  Returns (cols, w, wpos, info) with the rows that remain; the
+    inputs are not changed.  No reference counterpart in the native module: the reference
+    does this in numpy inside Catalog."""
+    names = [k for k in CAT_COLUMNS if k in cols]
+    if len(names) != len(cols):
+        raise ValueError("unknown column names: %s" % sorted(set(cols) - set(CAT_COLUMNS)))
+    arrs = [np.array(cols[k], dtype=np.float64) for k in names]
+    n = len(arrs[0]) if arrs else (len(w) if w is not None else 0)
+    if any(len(a) != n for a in arrs):
+        raise ValueError("columns of different lengths")
+    w_given = w is not None
+    wa = np.array(w, dtype=np.float64) if w_given else np.ones(n)
+    wp = np.array(wpos, dtype=np.float64) if wpos is not None else None
+    fl = np.ascontiguousarray(flag, dtype=np.int64) if flag is not None else None
+    for a in ([wa] + ([wp] if wp is not None else []) + ([fl] if fl is not None else [])):
+        if len(a) != n:
+            raise ValueError("w, wpos and flag must have the columns' length")
+    ignore = int(ignore_flag) if ignore_flag is not None else ~int(ok_flag)
+    ptrs = (ctypes.POINTER(ctypes.c_double) * max(len(arrs), 1))(*[_ptr(a) for a in arrs])
+    info = tc_catalog_info()
+    _check(lib().tc_catalog_finish(
+        n, len(arrs), ptrs, _ptr(wa), _ptr(wp) if wp is not None else None,
+        fl.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)) if fl is not None else None,
+        ignore, 1 if w_given else 0, 1 if keep_zero_weight else 0, ctypes.byref(info)))
+    m = int(info.nkeep)
+    out = {k: a[:m] for k, a in zip(names, arrs)}
+    return out, wa[:m], (wp[:m] if wp is not None else None), _cat_info(info, names,
+                                                                          wp is not None)
+
+
+def catalog_finish_device(n, col_ptrs, w_ptr, wpos_ptr=0, flag_ptr=0, ignore_flag=None,
+                          ok_flag=0, w_given=True, keep_zero_weight=False, names=None):
+    """catalog_finish on device columns (integer device addresses of float64 arrays, in
+    CAT_COLUMNS order; flag: int64).  The columns are changed in place; info["nkeep"] rows
+    remain.  No reference counterpart."""
+    ptrs = (ctypes.c_void_p * max(len(col_ptrs), 1))(*[ctypes.c_void_p(int(p)) for p in col_ptrs])
+    ignore = int(ignore_flag) if ignore_flag is not None else ~int(ok_flag)
+    info = tc_catalog_info()
+    _check(lib().tc_catalog_finish_device(
+        int(n), len(col_ptrs), ptrs, ctypes.c_void_p(int(w_ptr)),
+        ctypes.c_void_p(int(wpos_ptr)) if wpos_ptr else None,
+        ctypes.c_void_p(int(flag_ptr)) if flag_ptr else None, ignore,
+        1 if w_given else 0, 1 if keep_zero_weight else 0, ctypes.byref(info)))
+    names = list(names) if names is not None else ["c%d" % i for i in range(len(col_ptrs))]
+    return _cat_info(info, names, bool(wpos_ptr))
 
 
 # ----------------------------------------------------------------------------------------

@@ -10,7 +10,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libtcgpu.so")
 SOURCES = ["tree_build.cu", "traverse2pt.cu", "tiles.cu", "multipole.cu", "learned.cu",
-           "tensorcore.cu", "kmeans.cu", "capi.cu"]
+           "tensorcore.cu", "kmeans.cu", "catalog.cu", "capi.cu"]
 NVCC = os.environ.get("NVCC", "nvcc")
 FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3", "-std=c++17",
          "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off",

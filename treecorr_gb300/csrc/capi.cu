@@ -24,6 +24,7 @@
 #include "multipole.hpp"
 #include "learned.hpp"
 #include "kmeans.hpp"
+#include "catalog.hpp"
 
 namespace tc {
 
@@ -1518,6 +1519,74 @@ int tc_generate_xyz(double* x, double* y, double* z, const double* ra, const dou
         set_last_error("device to host copy failed"); rc = TC_ERR_CUDA;
     }
     dfree(d);
+    return rc;
+}
+
+// ---- Catalog ingestion (treecorr/catalog.py:1343-1487; catalog.cu) -----------------------
+int tc_catalog_finish_device(int64_t n, int ncols, double* const* cols, double* w, double* wpos,
+                             const int64_t* flag, int64_t ignore_flag, int w_given,
+                             int keep_zero_weight, tc_catalog_info* info)
+{
+    if (!info) { set_last_error("NULL info"); return TC_ERR_ARG; }
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    return catalog_finish_device(n, ncols, cols, w, wpos, flag, ignore_flag, w_given,
+                                 keep_zero_weight, st, info);
+}
+
+int tc_catalog_finish(int64_t n, int ncols, double* const* cols, double* w, double* wpos,
+                      const int64_t* flag, int64_t ignore_flag, int w_given,
+                      int keep_zero_weight, tc_catalog_info* info)
+{
+    if (!info || n < 0 || ncols < 0 || ncols > TC_CAT_MAXCOLS || (ncols > 0 && !cols) ||
+        (n > 0 && !w)) {
+        set_last_error("catalog: bad arguments (n >= 0, 0 <= ncols <= TC_CAT_MAXCOLS, w needed)");
+        return TC_ERR_ARG;
+    }
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    const int nd = ncols + 1 + (wpos ? 1 : 0);
+    double* d = nullptr;
+    int64_t* dflag = nullptr;
+    TC_TRY(dalloc(&d, (size_t)std::max<int64_t>(n, 1) * nd));
+    if (flag) {
+        const int rc = dalloc(&dflag, (size_t)std::max<int64_t>(n, 1));
+        if (rc) { dfree(d); return rc; }
+    }
+    std::vector<double*> host(cols, cols + ncols), dev(nd);
+    host.push_back(w);
+    if (wpos) host.push_back(wpos);
+    for (int c = 0; c < nd; ++c) dev[c] = d + (size_t)c * std::max<int64_t>(n, 1);
+    int rc = TC_OK;
+    cudaError_t e = cudaSuccess;
+    for (int c = 0; c < nd && e == cudaSuccess && n > 0; ++c) {
+        if (c == ncols && !w_given) continue;   // filled on the device
+        if (!host[c]) { set_last_error("catalog: NULL column"); rc = TC_ERR_ARG; break; }
+        e = cudaMemcpyAsync(dev[c], host[c], sizeof(double) * n, cudaMemcpyHostToDevice, st);
+    }
+    if (rc == TC_OK && e == cudaSuccess && flag && n > 0)
+        e = cudaMemcpyAsync(dflag, flag, sizeof(int64_t) * n, cudaMemcpyHostToDevice, st);
+    if (rc == TC_OK && e != cudaSuccess) {
+        set_last_error(std::string("host to device copy: ") + cudaGetErrorString(e));
+        rc = TC_ERR_CUDA;
+    }
+    if (rc == TC_OK)
+        rc = catalog_finish_device(n, ncols, dev.data(), dev[ncols], wpos ? dev[ncols + 1] : nullptr,
+                                   flag ? dflag : nullptr, ignore_flag, w_given, keep_zero_weight,
+                                   st, info);
+    if (rc == TC_OK && n > 0) {
+        for (int c = 0; c < nd && e == cudaSuccess; ++c)
+            if (info->nkeep > 0)
+                e = cudaMemcpyAsync(host[c], dev[c], sizeof(double) * info->nkeep,
+                                    cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            set_last_error(std::string("device to host copy: ") + cudaGetErrorString(e));
+            rc = TC_ERR_CUDA;
+        }
+    }
+    dfree(d);
+    dfree(dflag);
     return rc;
 }
 
