@@ -351,13 +351,115 @@ __device__ __forceinline__ void tile_fast(const TravParams& T, const TileLeaves&
     }
 }
 
+// Adds the pairs that lanes hold for the shared bins (kx >= 0, values v) in ascending lane
+// order: lane q < nq adds quantity q of each, so the sums do not depend on the order in which
+// conflicting shared atomics would land.
+__device__ __forceinline__ void shared_bins_in_order(int kx, const float (&v)[8], float* fb,
+                                                     int nq, int nb, int lane)
+{
+    unsigned m = __ballot_sync(0xffffffffu, kx >= 0);
+    while (m) {
+        const int t = __ffs(m) - 1;
+        m &= m - 1u;
+        const int kt = __shfl_sync(0xffffffffu, kx, t);
+        float x = 0.f;
+#pragma unroll
+        for (int q = 0; q < 7; ++q) {
+            const float y = __shfl_sync(0xffffffffu, v[q], t);
+            x = lane == q ? y : x;
+        }
+        if (lane < nq) fb[lane * nb + kt] += x;
+    }
+}
+
+// Pairs inside the FP32 error band of a bin or range decision are decided in FP64 from the
+// FP64 positions (leaf_pair64).  The pair loops below run twice when a tile has such pairs:
+// the main pass (ESC = false) skips them and has no call in its loop, which keeps its
+// registers free of the call's saves; the escalation pass (ESC = true) takes only them.
+
+// The pair loop of a cross tile whose pairs all lie in range and in bins kref and kref + 1
+// (the common general case at large separations, where a tile straddles one bin edge): no
+// range test, one comparison with the middle edge (in units of bins, d = kk - 1, with the
+// same FP32 error band as the general loop), both bins summed branch-free in registers.
+template <int GEO, int KIND, bool ESC>
+__device__ __forceinline__ bool tile_two(const TravParams& T, const TileLeaves& LA,
+                                         const TileLeaves& SB, const TileCtx& C, int lane,
+                                         float (&acc0)[8], float (&acc1)[8], unsigned& c0,
+                                         unsigned& c1, float* fb, unsigned long long* np,
+                                         unsigned& n_drop, unsigned& n_esc)
+{
+    const int nbl = C.nbl, npt = C.na * nbl, nq = T.nqf, nb = T.nbins;
+    const float ln2h = 0.5f * 0.69314718f;
+    const float ckk = ln2h * T.finvbinsize;
+    int ii = lane / nbl, jj = lane - ii * nbl;
+    const int di = 32 / nbl, dj = 32 - di * nbl;
+    bool seen = false;   // main pass: a pair was left for the escalation pass
+    for (int p0 = 0; p0 < npt; p0 += 32) {
+        const int i = ii, j = jj;
+        jj += dj; ii += di;
+        if (jj >= nbl) { jj -= nbl; ++ii; }
+        int kx = -1;
+        float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        do {
+            if (p0 + lane >= npt) break;
+            const float4 Pa = LA.P[i], Pb = SB.P[j];
+            const float dx = Pa.x - Pb.x, dy = Pa.y - Pb.y;
+            const float dz = GEO == TG_FLAT ? 0.f : Pa.z - Pb.z;
+            const float dsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const float invc = rsqrtf(dsq);
+            float r = dsq * invc;
+            if (GEO == TG_ARC) r = arc_series(r);
+            const float lr = __log2f(r * r * C.inv_edge);
+            const float d = fmaf(lr, ckk, -1.f);
+            const bool unsure = fabsf(d) < fmaf(C.band_e, invc, C.band_0);
+            if (unsure != ESC) {
+                seen = seen || unsure;
+                break;
+            }
+            float logr = fmaf(lr, ln2h, C.ledge);
+            int k = C.kref + (d >= 0.f ? 1 : 0);
+            if constexpr (ESC) {
+                ++n_esc;
+                k = leaf_pair64(T, __float_as_int(LA.X[i].z), __float_as_int(SB.X[j].z), false,
+                                &r, &logr);
+                if (k < 0) { ++n_drop; break; }
+            }
+            const float4 Wa = LA.W[i], Wb = SB.W[j];
+            const float ww = Wa.x * Wb.x;
+            v[0] = ww; v[1] = ww * r; v[2] = ww * (ESC ? logr : lr);
+            if constexpr (KIND != TK_NN) {
+                float x[4] = {0.f, 0.f, 0.f, 0.f}, sc;
+                pair_products<GEO, KIND>(T, LA, SB, i, j, Pa, Wa, Pb, Wb, dx, dy, dz, dsq, r,
+                                         logr, x, sc);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) v[3 + q] = x[q] * sc;
+            }
+            const unsigned nn = (unsigned)__float_as_int(Wa.w) * (unsigned)__float_as_int(Wb.w);
+            if constexpr (ESC) {
+                kx = k;
+                if (!T.quick) atomicAdd(&np[k], (unsigned long long)nn);   // exact integer
+            } else {
+                const float m1 = d >= 0.f ? 1.f : 0.f, m0 = 1.f - m1;
+#pragma unroll
+                for (int q = 0; q < 7; ++q) {
+                    acc0[q] = fmaf(m0, v[q], acc0[q]);
+                    acc1[q] = fmaf(m1, v[q], acc1[q]);
+                }
+                if (d >= 0.f) c1 += nn; else c0 += nn;
+            }
+        } while (false);
+        if constexpr (ESC) shared_bins_in_order(kx, v, fb, nq, nb, lane);
+    }
+    __syncwarp();
+    return __any_sync(0xffffffffu, seen);
+}
+
 // The general pair loop: range test near min_sep / max_sep, the bin of every pair with its
-// FP32 error band, FP64 re-decision inside the band, self tiles (j > i).  Bins kref and
-// kref + 1 are summed in registers; other bins and FP64-decided pairs go to the warp's
-// shared-memory bins, added lane by lane in ascending lane order (broadcast by shuffles), so
-// that the sums do not depend on the order in which conflicting shared atomics would land.
-template <int GEO, int KIND>
-__device__ __forceinline__ void tile_general(const TravParams& T, const TileLeaves& LA,
+// FP32 error band, self tiles (j > i).  Bins kref and kref + 1 are summed in registers; other
+// bins go to the warp's shared-memory bins in lane order; pairs inside an error band are left
+// to the escalation pass (ESC = true), which decides them in FP64.
+template <int GEO, int KIND, bool ESC>
+__device__ __forceinline__ bool tile_general(const TravParams& T, const TileLeaves& LA,
                                              const TileLeaves& SB, const TileCtx& C, int lane,
                                              float (&acc0)[8], float (&acc1)[8], unsigned& c0,
                                              unsigned& c1, float* fb, unsigned long long* np,
@@ -369,6 +471,7 @@ __device__ __forceinline__ void tile_general(const TravParams& T, const TileLeav
     const float ckk = ln2h * T.finvbinsize;
     int ii = lane / nbl, jj = lane - ii * nbl;
     const int di = 32 / nbl, dj = 32 - di * nbl;
+    bool seen = false;
     for (int p0 = 0; p0 < npt; p0 += 32) {
         const int i = ii, j = jj;
         jj += dj; ii += di;
@@ -377,8 +480,8 @@ __device__ __forceinline__ void tile_general(const TravParams& T, const TileLeav
         float v[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         do {                     // (break: no pair to add)
             if (p0 + lane >= npt || (C.self && j <= i)) break;
-            ++n_pairs;
-            const float4 Pa = LA.P[i], Wa = LA.W[i], Pb = SB.P[j], Wb = SB.W[j];
+            if (!ESC) ++n_pairs;
+            const float4 Pa = LA.P[i], Pb = SB.P[j];
             const float dx = Pa.x - Pb.x, dy = Pa.y - Pb.y;
             const float dz = GEO == TG_FLAT ? 0.f : Pa.z - Pb.z;
             const float dsq = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
@@ -402,14 +505,19 @@ __device__ __forceinline__ void tile_general(const TravParams& T, const TileLeav
                 unsure = fr < band || fr > 1.f - band || k < 0;
                 if (k >= nb) k = nb - 1;                    // the clamp of src/Corr2.cpp:514
             }
+            if (unsure != ESC) {
+                seen = seen || unsure;
+                break;
+            }
             float logr = fmaf(lr, ln2h, C.ledge);
-            if (unsure) {
+            if constexpr (ESC) {
                 ++n_esc;
                 k = leaf_pair64(T, __float_as_int(LA.X[i].z), __float_as_int(SB.X[j].z), C.self,
                                 &r, &logr);
                 if (k < 0) break;
             }
             ++n_acc;
+            const float4 Wa = LA.W[i], Wb = SB.W[j];
             const float ww = Wa.x * Wb.x;
             v[0] = ww; v[1] = ww * r; v[2] = ww * lr;
             if constexpr (KIND != TK_NN) {
@@ -420,11 +528,11 @@ __device__ __forceinline__ void tile_general(const TravParams& T, const TileLeav
                 for (int q = 0; q < 4; ++q) v[3 + q] = x[q] * sc;
             }
             const unsigned nn = (unsigned)__float_as_int(Wa.w) * (unsigned)__float_as_int(Wb.w);
-            if (!unsure && k == C.kref) {
+            if (!ESC && k == C.kref) {
 #pragma unroll
                 for (int q = 0; q < 7; ++q) acc0[q] += v[q];
                 c0 += nn;
-            } else if (!unsure && k == C.kref + 1) {
+            } else if (!ESC && k == C.kref + 1) {
 #pragma unroll
                 for (int q = 0; q < 7; ++q) acc1[q] += v[q];
                 c1 += nn;
@@ -434,23 +542,10 @@ __device__ __forceinline__ void tile_general(const TravParams& T, const TileLeav
                 if (!T.quick) atomicAdd(&np[k], (unsigned long long)nn);   // exact integer
             }
         } while (false);
-        // The pairs bound for the shared bins, in ascending lane order: lane q < nq adds
-        // quantity q of each.
-        unsigned m = __ballot_sync(0xffffffffu, kx >= 0);
-        while (m) {
-            const int t = __ffs(m) - 1;
-            m &= m - 1u;
-            const int kt = __shfl_sync(0xffffffffu, kx, t);
-            float x = 0.f;
-#pragma unroll
-            for (int q = 0; q < 7; ++q) {
-                const float y = __shfl_sync(0xffffffffu, v[q], t);
-                x = lane == q ? y : x;
-            }
-            if (lane < nq) fb[lane * nb + kt] += x;
-        }
+        shared_bins_in_order(kx, v, fb, nq, nb, lane);
     }
     __syncwarp();
+    return __any_sync(0xffffffffu, seen);
 }
 
 template <int GEO, int KIND>
@@ -479,7 +574,7 @@ __global__ void __launch_bounds__(TPB, TMINB) k_tiles(const __grid_constant__ Tr
     TileLeaves& SB = *(&SA + 1);
     const long long nwt = (long long)gridDim.x * TWPB;
     // Per-lane counters: at most ~10^8 pairs per lane in a launch, so 32 bits suffice.
-    unsigned n_acc = 0, n_pairs = 0, n_esc = 0, n_tiles = 0;
+    unsigned n_acc = 0, n_pairs = 0, n_esc = 0, n_tiles = 0, n_drop = 0;
     if ((long long)gw < nt) {
         for (int q = lane; q < nq * nb; q += 32) { fd[q] = make_float2(0.f, 0.f); fb[q] = 0.f; }
         for (int q = lane; q < nb; q += 32) np[q] = 0ull;
@@ -574,12 +669,22 @@ __global__ void __launch_bounds__(TPB, TMINB) k_tiles(const __grid_constant__ Tr
             unsigned c0 = 0u, c1 = 0u;
             const bool fast = C.interior && klo == khi && !C.self &&
                               (GEO != TG_ARC || C.small_chord);
+            const bool two = C.interior && khi == klo + 1 && !C.self &&
+                             (GEO != TG_ARC || C.small_chord);
             if (fast) {
                 tile_fast<GEO, KIND>(T, LA, SB, C, lane, acc0, c0);
                 if (lane == 0) { n_pairs += C.na * C.nbl; n_acc += C.na * C.nbl; }
+            } else if (two) {
+                if (tile_two<GEO, KIND, false>(T, LA, SB, C, lane, acc0, acc1, c0, c1, fb, np,
+                                               n_drop, n_esc))
+                    tile_two<GEO, KIND, true>(T, LA, SB, C, lane, acc0, acc1, c0, c1, fb, np,
+                                              n_drop, n_esc);
+                if (lane == 0) { n_pairs += C.na * C.nbl; n_acc += C.na * C.nbl; }
             } else {
-                tile_general<GEO, KIND>(T, LA, SB, C, lane, acc0, acc1, c0, c1, fb, np, n_acc,
-                                        n_pairs, n_esc);
+                if (tile_general<GEO, KIND, false>(T, LA, SB, C, lane, acc0, acc1, c0, c1, fb, np,
+                                                   n_acc, n_pairs, n_esc))
+                    tile_general<GEO, KIND, true>(T, LA, SB, C, lane, acc0, acc1, c0, c1, fb, np,
+                                                  n_acc, n_pairs, n_esc);
             }
             // The tile's register bins into the warp's FP32 bins.  With single-point leaves a
             // lane counts at most 32 pairs, so the warp's u32 sum is exact; list leaves add
@@ -615,13 +720,15 @@ __global__ void __launch_bounds__(TPB, TMINB) k_tiles(const __grid_constant__ Tr
         unsigned long long* wn = T.wnp + (size_t)(T.tile_wbase + gw) * nb;
         for (int q = lane; q < nb; q += 32) wn[q] += np[q];
     }
-    unsigned long long a64 = n_acc, p64 = n_pairs, e64 = n_esc, t64 = n_tiles;
+    unsigned long long a64 = n_acc, p64 = n_pairs, e64 = n_esc, t64 = n_tiles, d64 = n_drop;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         a64 += __shfl_xor_sync(0xffffffffu, a64, o);
+        d64 += __shfl_xor_sync(0xffffffffu, d64, o);
         p64 += __shfl_xor_sync(0xffffffffu, p64, o);
         e64 += __shfl_xor_sync(0xffffffffu, e64, o);
     }
+    a64 -= d64;   // pairs of two-bin tiles that the FP64 decision put out of range
     if (lane == 0 && t64) {
         atomicAdd(&T.counters[1], a64);
         atomicAdd(&T.tctl[2], t64);
