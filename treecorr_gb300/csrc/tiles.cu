@@ -57,6 +57,7 @@ constexpr int TMINB = TILES_MINB; // resident blocks per SM the registers are si
 #define TILE_CAP 64
 #endif
 constexpr int TCAP = TILE_CAP;    // most leaves per tile side (>= the traversal's tile_leaf)
+static_assert(TCAP * 4 >= 32 * 8, "a tile side's X array doubles as the 32 x 8 staging area");
 
 enum { TG_FLAT = 0, TG_ARC = 1, TG_SPHEUC = 2, TG_3D = 3 };   // geometry
 enum { TK_NN = 0, TK_SC = 1, TK_GEN = 2, TK_GG = 3 };           // class family
@@ -372,6 +373,32 @@ __device__ __forceinline__ void shared_bins_in_order(int kx, const float (&v)[8]
     }
 }
 
+// The same through a staging area of 32 x 8 floats in shared memory (a part of the tile's
+// leaf arrays that the pass does not read): each lane writes its values and bin, then lane
+// q < nq adds quantity q of the staged pairs in ascending lane order -- a few instructions
+// per pair instead of a round of shuffles.
+__device__ __forceinline__ void shared_bins_staged(int kx, const float (&v)[8], float* stg,
+                                                   float* fb, int nq, int nb, int lane)
+{
+    unsigned m = __ballot_sync(0xffffffffu, kx >= 0);
+    if (!m) return;
+    if (kx >= 0) {
+        float4* my = reinterpret_cast<float4*>(stg + lane * 8);
+        my[0] = make_float4(v[0], v[1], v[2], v[3]);
+        my[1] = make_float4(v[4], v[5], v[6], __int_as_float(kx));
+    }
+    __syncwarp();
+    if (lane < nq) {
+        while (m) {
+            const int t = __ffs(m) - 1;
+            m &= m - 1u;
+            const float* e = stg + t * 8;
+            fb[lane * nb + __float_as_int(e[7])] += e[lane];
+        }
+    }
+    __syncwarp();
+}
+
 // Pairs inside the FP32 error band of a bin or range decision are decided in FP64 from the
 // FP64 positions (leaf_pair64).  The pair loops below run twice when a tile has such pairs:
 // the main pass (ESC = false) skips them and has no call in its loop, which keeps its
@@ -456,15 +483,16 @@ __device__ __forceinline__ bool tile_two(const TravParams& T, const TileLeaves& 
 
 // The general pair loop: range test near min_sep / max_sep, the bin of every pair with its
 // FP32 error band, self tiles (j > i).  Bins kref and kref + 1 are summed in registers; other
-// bins go to the warp's shared-memory bins in lane order; pairs inside an error band are left
-// to the escalation pass (ESC = true), which decides them in FP64.
+// bins go to the warp's shared-memory bins in lane order (through stg when it is given);
+// pairs inside an error band are left to the escalation pass (ESC = true), which decides
+// them in FP64.
 template <int GEO, int KIND, bool ESC>
 __device__ __forceinline__ bool tile_general(const TravParams& T, const TileLeaves& LA,
                                              const TileLeaves& SB, const TileCtx& C, int lane,
                                              float (&acc0)[8], float (&acc1)[8], unsigned& c0,
                                              unsigned& c1, float* fb, unsigned long long* np,
                                              unsigned& n_acc, unsigned& n_pairs,
-                                             unsigned& n_esc)
+                                             unsigned& n_esc, float* stg)
 {
     const int nbl = C.nbl, npt = C.na * nbl, nb = T.nbins, nq = T.nqf;
     const float ln2h = 0.5f * 0.69314718f;
@@ -542,7 +570,8 @@ __device__ __forceinline__ bool tile_general(const TravParams& T, const TileLeav
                 if (!T.quick) atomicAdd(&np[k], (unsigned long long)nn);   // exact integer
             }
         } while (false);
-        shared_bins_in_order(kx, v, fb, nq, nb, lane);
+        if (!ESC && stg) shared_bins_staged(kx, v, stg, fb, nq, nb, lane);
+        else shared_bins_in_order(kx, v, fb, nq, nb, lane);
     }
     __syncwarp();
     return __any_sync(0xffffffffu, seen);
@@ -681,10 +710,25 @@ __global__ void __launch_bounds__(TPB, TMINB) k_tiles(const __grid_constant__ Tr
                                               n_drop, n_esc);
                 if (lane == 0) { n_pairs += C.na * C.nbl; n_acc += C.na * C.nbl; }
             } else {
+                // Staging for the shared bins: the A side's arrays of a self tile (unused), or
+                // B's X array of a cross tile (read only by the escalation pass and the
+                // generic products): B's leaves are staged again before an escalation pass.
+                float* stg = C.self ? reinterpret_cast<float*>(SA.P)
+                                    : (KIND == TK_GEN ? nullptr : reinterpret_cast<float*>(SB.X));
                 if (tile_general<GEO, KIND, false>(T, LA, SB, C, lane, acc0, acc1, c0, c1, fb, np,
-                                                   n_acc, n_pairs, n_esc))
+                                                   n_acc, n_pairs, n_esc, stg)) {
+                    if (!C.self && stg) {
+                        const float4 Ba2 = cB[ib].a, Bb2 = cB[ib].b, Bc2 = cB[ib].c,
+                                     Bd2 = cB[ib].d;
+                        float u1, u2;
+                        bool u3;
+                        stage(cB, baseB, Bc2, Bd2, Ba2.x, Ba2.y, Ba2.z, Bb2.x, Bb2.y, Bb2.z,
+                              T.k2, SB, lane, false, u1, u2, u3);
+                        __syncwarp();
+                    }
                     tile_general<GEO, KIND, true>(T, LA, SB, C, lane, acc0, acc1, c0, c1, fb, np,
-                                                  n_acc, n_pairs, n_esc);
+                                                  n_acc, n_pairs, n_esc, nullptr);
+                }
             }
             // The tile's register bins into the warp's FP32 bins.  With single-point leaves a
             // lane counts at most 32 pairs, so the warp's u32 sum is exact; list leaves add
