@@ -211,8 +211,9 @@ int tc_corr2_process_cross(tc_corr2* c, tc_field* f1, tc_field* f2, int dots, in
  * bin_slop criterion runs: a corr with the learned criterion set (tc_corr2_set_learned) is
  * refused with TC_ERR_ARG.  The field must already be built (call tc_field_ntop once
  * beforehand: building the tree allocates).  The first call on a device looks up the
- * array's device address (set-up, once per device, with that device current); make that
- * first call before any stream capture.  All calls share the array, which keeps the last
+ * array's device address (set-up, once per device, with that device current).  The
+ * environment variable TCGPU_NOALLOC_SPILL_CAP (items) shortens the spill list, so that
+ * tests reach the overflow path on small catalogs.  All calls share the array, which keeps the last
  * call's contents (each call clears what must start at zero): calls that overlap on the GPU
  * (from several host threads, or processes sharing a context) race and must be serialised
  * by the caller.  Results are added into the corr's output arrays as usual; in the stats,

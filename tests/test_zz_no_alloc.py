@@ -108,3 +108,32 @@ def test_noalloc_refuses_the_learned_criterion(gpu_lib):
     rc = noalloc(corr._h, f._h, 0, int(T.Euclidean))
     assert rc == 0, L.tc_last_error().decode()
     H.assert_outputs_close(out, golden, "G", rtol=1e-5, label="after setLearned(None)")
+
+
+def test_noalloc_work_list_overflow_is_reported(gpu_lib, monkeypatch):
+    """When the traversal needs more spill-list space than the fixed array holds, the kernel
+    stops with a status (no write past the list), the call returns TC_ERR_DEVICE with the
+    documented message and adds nothing to the outputs.  The test shortens the list
+    (TCGPU_NOALLOC_SPILL_CAP) so that a 200,000-point catalog reaches that path."""
+    from cases_bench import bench2_inputs, bench2_spec
+    T = gpu_lib
+    L, noalloc = _noalloc_fn(T)
+    s = bench2_spec("gg_cfg1_bs1")
+    f = H.gpu_field(T, "G", s["coords"], bench2_inputs("gg_cfg1_bs1"), s["min_size"],
+                    s["max_size"])
+    f.getNTopLevel()
+    out = {k: np.zeros(s["bins"]["nbins"]) for k in H.OUT_KEYS}
+    c = _corr(T, "G", s["bins"], out)
+    monkeypatch.setenv("TCGPU_NOALLOC_SPILL_CAP", "0")
+    rc = noalloc(c._h, f._h, 0, int(T.Euclidean))
+    assert rc == 4    # TC_ERR_DEVICE
+    assert "work-list space" in L.tc_last_error().decode()
+    assert not any(out[k].any() for k in H.OUT_KEYS)
+    # The same call with the full list succeeds and matches the golden result.
+    monkeypatch.delenv("TCGPU_NOALLOC_SPILL_CAP")
+    assert noalloc(c._h, f._h, 0, int(T.Euclidean)) == 0
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                             "gg_cfg1_bs1.npz"))
+    H.assert_outputs_close(out, {k: g["ref_" + k] for k in H.OUT_KEYS}, "G", rtol=1e-5,
+                           label="noalloc after an overflow")

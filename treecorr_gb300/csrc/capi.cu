@@ -859,6 +859,12 @@ int corr_process_auto_noalloc(tc_corr2* c, tc_field* f, int quick, int metric)
     T.err = reinterpret_cast<int*>(B + NOALLOC_OFF_ERR);
     T.root_next = ctl; T.nout = ctl + 1; T.counters = ctl + 2;
     T.out_cap = NOALLOC_SPILL;
+    // Test hook: a shorter spill list (TCGPU_NOALLOC_SPILL_CAP items) makes the overflow path
+    // reachable on test-size catalogs.
+    if (const char* e = std::getenv("TCGPU_NOALLOC_SPILL_CAP")) {
+        const long long v = std::atoll(e);
+        if (v >= 0 && v < T.out_cap) T.out_cap = v;
+    }
     // The array keeps the previous call's contents: clear what must start at zero.
     TC_CU(cudaMemsetAsync(wacc, 0, sizeof(double) * (size_t)nwarps * nq * nb, st));
     TC_CU(cudaMemsetAsync(wnp, 0, sizeof(unsigned long long) * (size_t)nwarps * nb, st));

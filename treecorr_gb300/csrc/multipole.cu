@@ -1574,11 +1574,14 @@ __global__ void __launch_bounds__(TCB) k_mp_zeta_tc(ZParams Q, int* status)
             const float wr = C1(2 * nb + a, 2 * nb + b) - C1(3 * nb + a, 3 * nb + b);
             const float wi = a == b ? 0.f : C1(2 * nb + a, 3 * nb + b) + C1(3 * nb + a, 2 * nb + b);
             const size_t i = (size_t)(a * nb + b) * nn + M + n;
-            part[0 * Zs + i] += g0r; part[1 * Zs + i] += g0i;
-            part[2 * Zs + i] += g1r; part[3 * Zs + i] += g1i;
-            part[4 * Zs + i] += g2r; part[5 * Zs + i] += g2i;
-            part[6 * Zs + i] += g3r; part[7 * Zs + i] += g3i;
-            part[8 * Zs + i] += wr;  part[9 * Zs + i] += wi;
+            // All ten loads first, then the stores: one round trip per entry instead of ten
+            // (the compiler cannot reorder a load past a store to a possibly equal address).
+            const float add[10] = {g0r, g0i, g1r, g1i, g2r, g2i, g3r, g3i, wr, wi};
+            double o[10];
+#pragma unroll
+            for (int q = 0; q < 10; ++q) o[q] = part[q * Zs + i];
+#pragma unroll
+            for (int q = 0; q < 10; ++q) part[q * Zs + i] = o[q] + (double)add[q];
         }
         __syncthreads();
         // The tile area was overwritten: restore the zero padding before the next fill.
