@@ -144,6 +144,8 @@ struct tc_corr2 {
     int* det_cnt = nullptr;
     long long det_out_cap = 0, det_tout_cap = 0;
     int det_cnt_cap = 0;
+    unsigned long long* wctr = nullptr;  // per-warp counter slots [warps][8]
+    int wctr_cap = 0;
     ~tc_corr2() { for (auto e : kev) cudaEventDestroy(e); }
 };
 
@@ -734,6 +736,14 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
     T.wacc = c->wacc; T.wnp = c->wnp; T.err = c->d_err;
     T.counters = c->ctl + 2;
     T.in_tasks = nullptr; T.nin = 0;
+    if (!c->wctr || c->wctr_cap < nwarps + twarps) {
+        dfree(c->wctr);
+        c->wctr_cap = 0;
+        TC_TRY(dalloc(&c->wctr, (size_t)(nwarps + twarps) * 8));
+        c->wctr_cap = nwarps + twarps;
+    }
+    T.wctr = c->wctr;
+    TC_CU(cudaMemsetAsync(c->wctr, 0, sizeof(unsigned long long) * 8 * (size_t)(nwarps + twarps), st));
     TC_CU(cudaMemsetAsync(c->wacc, 0, sizeof(double) * (size_t)(nwarps + twarps) * nq * nb, st));
     TC_CU(cudaMemsetAsync(c->wnp, 0, sizeof(unsigned long long) * (size_t)(nwarps + twarps) * nb, st));
     TC_CU(cudaMemsetAsync(c->ctl, 0, 8 * sizeof(unsigned long long), st));
@@ -758,15 +768,18 @@ int corr_process(tc_corr2* c, tc_field* f1, tc_field* f2, int quick, int metric)
     TC_CU(cudaEventRecord(e1, st));
     std::vector<double> tot((size_t)nq * nb);
     std::vector<unsigned long long> totnp(nb);
-    unsigned long long cntr[4];
-    unsigned long long tcnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    if (tiles)
-        TC_CU(cudaMemcpyAsync(tcnt, c->tctl, 8 * sizeof(unsigned long long),
-                              cudaMemcpyDeviceToHost, st));
+    // The per-warp counter slots, summed in warp order.
+    std::vector<unsigned long long> wc((size_t)(nwarps + twarps) * 8);
+    TC_CU(cudaMemcpyAsync(wc.data(), c->wctr, wc.size() * sizeof(unsigned long long),
+                          cudaMemcpyDeviceToHost, st));
     TC_CU(cudaMemcpyAsync(tot.data(), c->tot, tot.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
     TC_CU(cudaMemcpyAsync(totnp.data(), c->totnp, nb * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-    TC_CU(cudaMemcpyAsync(cntr, c->ctl + 2, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     TC_CU(cudaStreamSynchronize(st));
+    unsigned long long cntr[4] = {0, 0, 0, 0}, tcnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (size_t w = 0; w < (size_t)(nwarps + twarps); ++w) {
+        for (int q = 0; q < 4; ++q) cntr[q] += wc[w * 8 + q];
+        for (int q = 4; q < 7; ++q) tcnt[q - 2] += wc[w * 8 + q];   // tiles, pairs, FP64
+    }
     float ms = 0.f;
     TC_CU(cudaEventElapsedTime(&ms, e0, e1));
     cudaEventDestroy(e0); cudaEventDestroy(e1);
@@ -1464,7 +1477,7 @@ void tc_corr2_free(tc_corr2* c)
     dfree(c->sched);
     dfree(c->mlp); dfree(c->samples);
     dfree(c->tiles); dfree(c->tctl); dfree(c->tedge);
-    dfree(c->det_out); dfree(c->det_tout); dfree(c->det_cnt);
+    dfree(c->det_out); dfree(c->det_tout); dfree(c->det_cnt); dfree(c->wctr);
     delete c;
 }
 

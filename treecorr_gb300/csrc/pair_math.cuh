@@ -162,6 +162,27 @@ __device__ __forceinline__ void df_add(float2& a, float x)
 
 __device__ __forceinline__ double df_value(float2 a) { return (double)a.x + (double)a.y; }
 
+// wa[q] += fd[q] (as FP64) for q < n, by the lanes of a warp, eight values per lane at a
+// time with all loads issued before the stores: a loop of plain += would wait for each
+// read-modify-write in turn (the compiler cannot move a load past a store to the same
+// array).
+__device__ __forceinline__ void warp_add_totals(double* wa, const float2* fd, int n, int lane)
+{
+    for (int q0 = 0; q0 < n; q0 += 256) {
+        double o[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int q = q0 + 32 * u + lane;
+            o[u] = q < n ? wa[q] : 0.;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int q = q0 + 32 * u + lane;
+            if (q < n) wa[q] = o[u] + df_value(fd[q]);
+        }
+    }
+}
+
 // The values an accepted pair adds (finishProcess and DirectHelper, src/Corr2.cpp:394-566):
 // w1 w2, w1 w2 r, w1 w2 logr, n1 n2 and the correlation products.
 __device__ __forceinline__ void accept_values(const TravParams& T, const TCell& A, const TCell& B,

@@ -760,7 +760,7 @@ __global__ void __launch_bounds__(TPB, TMINB) k_tiles(const __grid_constant__ Tr
         }
         __syncwarp();
         double* wa = T.wacc + (size_t)(T.tile_wbase + gw) * nq * nb;
-        for (int q = lane; q < nq * nb; q += 32) wa[q] += df_value(fd[q]);
+        warp_add_totals(wa, fd, nq * nb, lane);
         unsigned long long* wn = T.wnp + (size_t)(T.tile_wbase + gw) * nb;
         for (int q = lane; q < nb; q += 32) wn[q] += np[q];
     }
@@ -774,10 +774,19 @@ __global__ void __launch_bounds__(TPB, TMINB) k_tiles(const __grid_constant__ Tr
     }
     a64 -= d64;   // pairs of two-bin tiles that the FP64 decision put out of range
     if (lane == 0 && t64) {
-        atomicAdd(&T.counters[1], a64);
-        atomicAdd(&T.tctl[2], t64);
-        atomicAdd(&T.tctl[3], p64);
-        atomicAdd(&T.tctl[4], e64);
+        if (T.wctr) {
+            unsigned long long* w = T.wctr + (size_t)(T.tile_wbase + gw) * 8;
+            const unsigned long long o1 = w[1], o4 = w[4], o5 = w[5], o6 = w[6];
+            w[1] = o1 + a64;
+            w[4] = o4 + t64;
+            w[5] = o5 + p64;
+            w[6] = o6 + e64;
+        } else {
+            atomicAdd(&T.counters[1], a64);
+            atomicAdd(&T.tctl[2], t64);
+            atomicAdd(&T.tctl[3], p64);
+            atomicAdd(&T.tctl[4], e64);
+        }
     }
     // The last block to finish empties the tile list for the next expansion launch.
     __syncthreads();

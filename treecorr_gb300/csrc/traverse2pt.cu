@@ -587,7 +587,7 @@ __global__ void __launch_bounds__(TB) k_traverse(TravParams T)
     {
         // The warp's totals: added to its global slot (kept across relaunches).
         double* wa = T.wacc + (size_t)gw * nq * nb;
-        for (int q = lane; q < nq * nb; q += 32) wa[q] += df_value(fd[q]);
+        warp_add_totals(wa, fd, nq * nb, lane);
         unsigned long long* wn = T.wnp + (size_t)gw * nb;
         for (int q = lane; q < nb; q += 32) wn[q] += (np[q] + np[nb + q]) + (np[2 * nb + q] + np[3 * nb + q]);
     }
@@ -662,6 +662,25 @@ __device__ __forceinline__ void expand_warp_done(const ExpandSched* S, int lane)
             sched_step(W);
         }
     }
+}
+
+// A warp's counters: into its own slot when the launch has slots, else by atomics.
+__device__ __forceinline__ void add_counters(const TravParams& T, int gw, long long ev,
+                                             long long acc, long long esc, long long learn)
+{
+    if (T.wctr) {
+        unsigned long long* w = T.wctr + (size_t)gw * 8;
+        const unsigned long long o0 = w[0], o1 = w[1], o2 = w[2], o3 = w[3];
+        w[0] = o0 + (unsigned long long)ev;
+        w[1] = o1 + (unsigned long long)acc;
+        w[2] = o2 + (unsigned long long)esc;
+        w[3] = o3 + (unsigned long long)learn;
+        return;
+    }
+    if (ev) atomicAdd(&T.counters[0], (unsigned long long)ev);
+    if (acc) atomicAdd(&T.counters[1], (unsigned long long)acc);
+    if (esc) atomicAdd(&T.counters[2], (unsigned long long)esc);
+    if (learn) atomicAdd(&T.counters[3], (unsigned long long)learn);
 }
 
 // End of an expansion warp: the fixed-order mode records the warp's region counts (k_compact
@@ -844,7 +863,7 @@ __global__ void __launch_bounds__(TB, EXPAND_MINB) k_expand(TravParams T, const 
         if constexpr (MODE == 2) n_learn += __shfl_xor_sync(0xffffffffu, n_learn, o);
     }
     if (n_acc == 0) {   // nothing accumulated by this warp in this launch
-        if (lane == 0 && n_eval) atomicAdd(&T.counters[0], (unsigned long long)n_eval);
+        if (lane == 0 && n_eval) add_counters(T, gw, n_eval, 0, n_esc, 0);
         expand_finish(T, S, gw, lo_ch, lo_tl, lane);
         return;
     }
@@ -862,15 +881,10 @@ __global__ void __launch_bounds__(TB, EXPAND_MINB) k_expand(TravParams T, const 
     flush_bins(nq * nb, fb, fd, lane);
     __syncwarp();
     double* wa = T.wacc + (size_t)gw * nq * nb;
-    for (int q = lane; q < nq * nb; q += 32) wa[q] += df_value(fd[q]);
+    warp_add_totals(wa, fd, nq * nb, lane);
     unsigned long long* wn = T.wnp + (size_t)gw * nb;
     for (int q = lane; q < nb; q += 32) wn[q] += (np[q] + np[nb + q]) + (np[2 * nb + q] + np[3 * nb + q]);
-    if (lane == 0) {
-        atomicAdd(&T.counters[0], (unsigned long long)n_eval);
-        atomicAdd(&T.counters[1], (unsigned long long)n_acc);
-        atomicAdd(&T.counters[2], (unsigned long long)n_esc);
-        if (MODE == 2 && n_learn) atomicAdd(&T.counters[3], (unsigned long long)n_learn);
-    }
+    if (lane == 0) add_counters(T, gw, n_eval, n_acc, n_esc, MODE == 2 ? n_learn : 0);
     expand_finish(T, S, gw, lo_ch, lo_tl, lane);
 }
 

@@ -40,6 +40,10 @@ struct TravParams {
     unsigned long long* wnp;
     unsigned long long* counters;   // [0] evaluated, [1] accepted, [2] escalated,
                                     // [3] accepted by the learned criterion
+    // Per-warp counter slots (when set; the expansion's and the tiles' warps, [warp][8]):
+    // the counters above, then [4] tiles, [5] leaf pairs of tiles, [6] their FP64 decisions.
+    // A warp adds to its own slot, so launches end without contended atomics.
+    unsigned long long* wctr;
     int* err;
     // Learned opening criterion.  mode 0: the bin_slop rule; 1: the rule, and candidate pairs
     // are sampled into `samples`; 2: candidates go through the network.  A candidate is a
