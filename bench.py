@@ -347,6 +347,9 @@ def run_gpu(args, rank, world):
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e / args.steps},
         "gpu_launches": launches,
+        # The same step counted in point pairs in range (sum of npairs): independent of how
+        # an implementation groups them into cell pairs.
+        "point_pairs_per_s": world * float(out["npairs"].sum()) * args.steps / (ms / 1e3),
         "tuning": tune,
         "roofline": roofline,
         "clocks": clocks,

@@ -365,6 +365,16 @@ int tc_catalog_finish_device(int64_t n, int ncols, double* const* cols, double* 
                              double* wpos, const int64_t* flag, int64_t ignore_flag,
                              int w_given, int keep_zero_weight, tc_catalog_info* info);
 
+/* Catalog._get_center_size (treecorr/catalog.py:1330-1341; used by the triviallyZero tests
+ * of the patch loops, treecorr/corr2base.py:776-800): out = (mean x, mean y, mean z, size),
+ * the unweighted mean position and the largest distance of a point from it; z NULL for flat
+ * catalogs (mean z = 0).  Host arrays for tc_catalog_center_size, device arrays for
+ * tc_catalog_center_size_device.  n must be positive. */
+int tc_catalog_center_size(int64_t n, const double* x, const double* y, const double* z,
+                           double* out);
+int tc_catalog_center_size_device(int64_t n, const double* x, const double* y,
+                                  const double* z, double* out);
+
 /* Self-check of the tcgen05 tensor-core path (no reference counterpart): one CTA computes
  * c[128 x n] = a[128 x k] * b[n x k]^T in TF32 through TMEM (k in 8..64, multiple of 8;
  * n in 16..64, multiple of 16).  Host arrays, row-major. */

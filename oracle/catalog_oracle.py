@@ -82,3 +82,15 @@ def finish_input(cols, w=None, wpos=None, flag=None, ignore_flag=None, ok_flag=0
     info = dict(sumw=sumw, nobj=nobj, nontrivial_w=nontrivial, nan_counts=nan_counts,
                 wpos_zero=wpos_zero, wpos_conflicts=wpos_conflicts)
     return cols, w, wpos, info
+
+
+def center_size(x, y, z=None):
+    """Catalog._get_center_size (treecorr/catalog.py:1330-1341): the unweighted mean position
+    and the largest distance of a point from it."""
+    mx, my = np.mean(x), np.mean(y)
+    mz = 0
+    dsq = (x - mx) ** 2 + (y - my) ** 2
+    if z is not None:
+        mz = np.mean(z)
+        dsq += (z - mz) ** 2
+    return mx, my, mz, np.max(dsq) ** 0.5

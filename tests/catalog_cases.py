@@ -18,7 +18,7 @@ def load(name):
     inp = {k[3:]: g[k] for k in g.files if k.startswith("in_")}
     out = {k[4:]: g[k] for k in g.files if k.startswith("out_")}
     ref = dict(sumw=float(g["sumw"]), ntot=int(g["ntot"]), nobj=int(g["nobj"]),
-               nontrivial_w=bool(g["nontrivial_w"]))
+               nontrivial_w=bool(g["nontrivial_w"]), center_size=g["center_size"])
     return cfg, inp, out, ref
 
 

@@ -10,7 +10,8 @@ Run where the reference sources are (not on the GPU machine):
 It imports TreeCorr's Python package from the reference tree with the test-only `coord`
 stand-in (tests/golden/coord_shim) and the reference's compiled module (oracle/_ref), builds
 each catalog below from arrays, and stores the input columns, the configuration and the
-catalog's columns, sumw, ntot and nobj after construction in tests/golden/catalog_<name>.npz.
+catalog's columns, sumw, ntot, nobj and _get_center_size() (the centre and size that the
+patch loops' triviallyZero tests use) after construction in tests/golden/catalog_<name>.npz.
 """
 import json
 import os
@@ -94,6 +95,7 @@ def main():
         save["ntot"] = np.int64(cat.ntot)
         save["nobj"] = np.int64(cat.nobj)
         save["nontrivial_w"] = np.bool_(cat.nontrivial_w)
+        save["center_size"] = np.array(cat._get_center_size(), dtype=float)
         np.savez_compressed(os.path.join(HERE, "catalog_%s.npz" % name), **save)
         print(f"{name:16s} ntot {cat.ntot} nobj {cat.nobj} sumw {cat.sumw:.6f} "
               f"nontrivial {cat.nontrivial_w}")

@@ -30,3 +30,14 @@ def test_oracle_matches_reference_catalog(name):
         assert sum(info["nan_counts"].values()) > 0
     if name == "flat_wpos":
         assert info["wpos_zero"] > 0 and info["wpos_conflicts"] > 0
+
+
+@pytest.mark.parametrize("name", CC.NAMES)
+def test_center_size_matches_reference(name):
+    """Catalog._get_center_size of the finished catalog: the oracle's restatement equals the
+    reference's values."""
+    from oracle import catalog_oracle as O
+    _, _, out, ref = CC.load(name)
+    got = O.center_size(out["x"], out["y"], out.get("z"))
+    np.testing.assert_allclose(got, ref["center_size"], rtol=0,
+                               atol=1e-14 * max(1.0, np.abs(ref["center_size"]).max()))

@@ -92,3 +92,21 @@ def test_large_random_vs_oracle(gpu_lib):
     np.testing.assert_array_equal(a[2], b[2])
     np.testing.assert_allclose(a[3]["sumw"], b[3]["sumw"], rtol=1e-12)
     assert a[3]["nobj"] == b[3]["nobj"] and a[3]["nkeep"] == len(b[1])
+
+
+@pytest.mark.parametrize("name", CC.NAMES)
+def test_center_size_matches_reference(gpu_lib, name):
+    """The finished catalog's centre and size (what triviallyZero compares) on the GPU, host
+    and device entry points, against the reference's _get_center_size."""
+    import torch
+    T = gpu_lib
+    _, _, out, ref = CC.load(name)
+    z = out.get("z")
+    got = T.catalog_center_size(out["x"], out["y"], z)
+    tol = 1e-13 * max(1.0, np.abs(ref["center_size"]).max())
+    np.testing.assert_allclose(got, ref["center_size"], rtol=0, atol=tol)
+    d = [torch.from_numpy(np.array(a)).cuda() for a in (out["x"], out["y"])]
+    dz = torch.from_numpy(np.array(z)).cuda() if z is not None else None
+    got2 = T.catalog_center_size_device(len(out["x"]), d[0].data_ptr(), d[1].data_ptr(),
+                                        dz.data_ptr() if dz is not None else 0)
+    assert got2 == got

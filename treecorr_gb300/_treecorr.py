@@ -115,6 +115,10 @@ def lib():
         L.tc_catalog_finish.argtypes = [i64, ctypes.c_int, ctypes.POINTER(dp), dp, dp,
                                         ctypes.POINTER(ctypes.c_int64), i64, ctypes.c_int,
                                         ctypes.c_int, ctypes.POINTER(tc_catalog_info)]
+        L.tc_catalog_center_size.restype = ctypes.c_int
+        L.tc_catalog_center_size.argtypes = [i64, dp, dp, dp, dp]
+        L.tc_catalog_center_size_device.restype = ctypes.c_int
+        L.tc_catalog_center_size_device.argtypes = [i64, vp, vp, vp, dp]
         L.tc_catalog_finish_device.restype = ctypes.c_int
         L.tc_catalog_finish_device.argtypes = [i64, ctypes.c_int, ctypes.POINTER(vp), vp, vp, vp,
                                                i64, ctypes.c_int, ctypes.c_int,
@@ -530,6 +534,27 @@ def catalog_finish(cols, w=None, wpos=None, flag=None, ignore_flag=None, ok_flag
     out = {k: a[:m] for k, a in zip(names, arrs)}
     return out, wa[:m], (wp[:m] if wp is not None else None), _cat_info(info, names,
                                                                           wp is not None)
+
+
+def catalog_center_size(x, y, z=None):
+    """Catalog._get_center_size (treecorr/catalog.py:1330-1341) on the GPU: (mean x, mean y,
+    mean z, largest distance from the mean).  No reference counterpart in the native module."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    zz = np.ascontiguousarray(z, dtype=np.float64) if z is not None else None
+    out = np.zeros(4)
+    _check(lib().tc_catalog_center_size(len(x), _ptr(x), _ptr(y), _ptr(zz), _ptr(out)))
+    return tuple(float(v) for v in out)
+
+
+def catalog_center_size_device(n, x_ptr, y_ptr, z_ptr=0):
+    """catalog_center_size on device columns (integer addresses of float64 arrays)."""
+    out = np.zeros(4)
+    _check(lib().tc_catalog_center_size_device(int(n), ctypes.c_void_p(int(x_ptr)),
+                                               ctypes.c_void_p(int(y_ptr)),
+                                               ctypes.c_void_p(int(z_ptr)) if z_ptr else None,
+                                               _ptr(out)))
+    return tuple(float(v) for v in out)
 
 
 def catalog_finish_device(n, col_ptrs, w_ptr, wpos_ptr=0, flag_ptr=0, ignore_flag=None,

@@ -1609,6 +1609,39 @@ int tc_catalog_finish(int64_t n, int ncols, double* const* cols, double* w, doub
     return rc;
 }
 
+int tc_catalog_center_size_device(int64_t n, const double* x, const double* y, const double* z,
+                                  double* out)
+{
+    if (!out) { set_last_error("NULL out"); return TC_ERR_ARG; }
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    return catalog_center_size_device(n, x, y, z, st, out);
+}
+
+int tc_catalog_center_size(int64_t n, const double* x, const double* y, const double* z,
+                           double* out)
+{
+    if (!out || n <= 0 || !x || !y) { set_last_error("catalog centre: n > 0 and x, y needed"); return TC_ERR_ARG; }
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    const int nc = z ? 3 : 2;
+    double* d = nullptr;
+    TC_TRY(dalloc(&d, (size_t)n * nc));
+    const double* src[3] = {x, y, z};
+    cudaError_t e = cudaSuccess;
+    for (int c = 0; c < nc && e == cudaSuccess; ++c)
+        e = cudaMemcpyAsync(d + (size_t)c * n, src[c], sizeof(double) * n, cudaMemcpyHostToDevice, st);
+    int rc = TC_OK;
+    if (e != cudaSuccess) {
+        set_last_error(std::string("host to device copy: ") + cudaGetErrorString(e));
+        rc = TC_ERR_CUDA;
+    } else {
+        rc = catalog_center_size_device(n, d, d + n, z ? d + 2 * n : nullptr, st, out);
+    }
+    dfree(d);
+    return rc;
+}
+
 // ---- Patches ----------------------------------------------------------------------------
 // All patch-pair correlations of one set of patch fields in one expansion (the per-pair
 // loop of corr2base.py:929-950 / _process_all_auto): pairs (i, j), i <= j, whose fields

@@ -14,7 +14,9 @@
 //     error;
 //   * the removal of rows with wpos == 0 (or w == 0 without wpos) unless keep_zero_weight
 //     (1464-1468, Catalog.select): a stable compaction of every column in place.
-// GenerateXYZ (1609-1622) is the separate tc_generate_xyz_device.
+// GenerateXYZ (1609-1622) is the separate tc_generate_xyz_device; the catalog's centre and
+// size (_get_center_size, 1330-1341: the unweighted mean position and the largest distance
+// from it, which triviallyZero uses to skip far patch pairs) is catalog_center_size_device.
 //
 // k_cat_mark does the per-row rules, one thread per row, with integer atomic counts (rare:
 // NaNs and zero wpos) and per-block partial sums of w (a fixed shuffle tree), keep counts
@@ -23,7 +25,9 @@
 // their ranks (warp ballots), into a scratch column copied back.  Every sum is formed in a
 // fixed order, so the results repeat bit for bit; sumw differs from numpy's pairwise sum
 // only in rounding (~1e-16 relative).
+#include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <vector>
 
 #include "tc_host.hpp"
@@ -158,7 +162,110 @@ __global__ void __launch_bounds__(CAT_TPB) k_cat_scatter(int64_t n, const double
     if (kp) dst[boff[blockIdx.x] + before + __popc(m & ((1u << lane) - 1u))] = src[i];
 }
 
+// Catalog._get_center_size (treecorr/catalog.py:1330-1341): block sums of x, y, z for the
+// unweighted mean, then the largest squared distance from it.
+__global__ void __launch_bounds__(CAT_TPB) k_cat_sums(int64_t n, const double* x, const double* y,
+                                                      const double* z, double* bsum)
+{
+    __shared__ double ws[3][CAT_WPB];
+    const int64_t i = (int64_t)blockIdx.x * CAT_TPB + threadIdx.x;
+    double v[3] = {0., 0., 0.};
+    if (i < n) { v[0] = x[i]; v[1] = y[i]; v[2] = z ? z[i] : 0.; }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[c] += __shfl_xor_sync(0xffffffffu, v[c], o);
+        if ((threadIdx.x & 31) == 0) ws[c][threadIdx.x >> 5] = v[c];
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double t = 0.;
+        for (int q = 0; q < CAT_WPB; ++q) t += ws[threadIdx.x][q];
+        bsum[(size_t)blockIdx.x * 3 + threadIdx.x] = t;
+    }
+}
+
+// One block: the means from the block sums (fixed order), into cs[0..2].
+__global__ void __launch_bounds__(CAT_TOT) k_cat_mean(int nblk, int64_t n, const double* bsum,
+                                                      double* cs)
+{
+    __shared__ double ds[3][CAT_TOT];
+    const int t = threadIdx.x;
+    const int per = (nblk + CAT_TOT - 1) / CAT_TOT;
+    const int b0 = t * per, b1 = min(nblk, b0 + per);
+    double s0 = 0., s1 = 0., s2 = 0.;
+    for (int b = b0; b < b1; ++b) { s0 += bsum[3 * b]; s1 += bsum[3 * b + 1]; s2 += bsum[3 * b + 2]; }
+    ds[0][t] = s0; ds[1][t] = s1; ds[2][t] = s2;
+    __syncthreads();
+    if (t < 3) {
+        double S = 0.;
+        for (int q = 0; q < CAT_TOT; ++q) S += ds[t][q];
+        cs[t] = S / (double)n;
+    }
+}
+
+// The largest squared distance from the mean (an order-free maximum, as non-negative
+// doubles compared through their bit patterns).
+__global__ void __launch_bounds__(CAT_TPB) k_cat_maxd(int64_t n, const double* x, const double* y,
+                                                      const double* z, const double* cs,
+                                                      unsigned long long* dmax)
+{
+    const int64_t i = (int64_t)blockIdx.x * CAT_TPB + threadIdx.x;
+    double d = 0.;
+    if (i < n) {
+        const double dx = x[i] - cs[0], dy = y[i] - cs[1];
+        d = dx * dx + dy * dy;
+        if (z) { const double dz = z[i] - cs[2]; d += dz * dz; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) d = fmax(d, __shfl_xor_sync(0xffffffffu, d, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(dmax, (unsigned long long)__double_as_longlong(d));
+}
+
 }  // namespace
+
+int catalog_center_size_device(int64_t n, const double* x, const double* y, const double* z,
+                               cudaStream_t st, double out[4])
+{
+    out[0] = out[1] = out[2] = out[3] = 0.;
+    if (n <= 0 || !x || !y) { set_last_error("catalog centre: n > 0 and x, y needed"); return TC_ERR_ARG; }
+    const int64_t nblk64 = (n + CAT_TPB - 1) / CAT_TPB;
+    if (nblk64 > (int64_t)0x7fffffff) { set_last_error("catalog: too many rows"); return TC_ERR_ARG; }
+    const int nblk = (int)nblk64;
+    double* bsum = nullptr;
+    double* cs = nullptr;
+    unsigned long long* dmax = nullptr;
+    int rc = 0;
+    if ((rc = dalloc(&bsum, (size_t)nblk * 3)) || (rc = dalloc(&cs, 3)) || (rc = dalloc(&dmax, 1))) {
+        dfree(bsum); dfree(cs); dfree(dmax);
+        return rc;
+    }
+    double hc[3] = {0., 0., 0.};
+    unsigned long long hm = 0;
+    cudaError_t e = cudaMemsetAsync(dmax, 0, sizeof(unsigned long long), st);
+    if (e == cudaSuccess) {
+        count_launch();
+        k_cat_sums<<<nblk, CAT_TPB, 0, st>>>(n, x, y, z, bsum);
+        count_launch();
+        k_cat_mean<<<1, CAT_TOT, 0, st>>>(nblk, n, bsum, cs);
+        count_launch();
+        k_cat_maxd<<<nblk, CAT_TPB, 0, st>>>(n, x, y, z, cs, dmax);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hc, cs, 3 * sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hm, dmax, sizeof(hm), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    dfree(bsum); dfree(cs); dfree(dmax);
+    if (e != cudaSuccess) {
+        set_last_error(std::string("catalog centre: ") + cudaGetErrorString(e));
+        return TC_ERR_CUDA;
+    }
+    out[0] = hc[0]; out[1] = hc[1]; out[2] = z ? hc[2] : 0.;
+    double dm;
+    std::memcpy(&dm, &hm, sizeof(dm));
+    out[3] = std::sqrt(dm);
+    return TC_OK;
+}
 
 int catalog_finish_device(int64_t n, int ncols, double* const* cols, double* w, double* wpos,
                           const int64_t* flag, int64_t ignore_flag, int w_given,
