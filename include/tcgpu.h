@@ -223,7 +223,7 @@ int tc_corr2_process_auto_noalloc(tc_corr2* c, tc_field* f, int quick, int metri
 /* Tuning of the 2-point path (no reference counterpart: the reference's OpenMP loop has no
  * such knobs).  tile_leaf: the most points per side of a leaf-pair tile of the exact mode
  * (8..64; 0 = the default 48); chunk: work items per expansion launch, the depth of the
- * breadth-first queue (2^16..2^25; 0 = the default, 2^24 or twice the points if fewer).
+ * breadth-first queue (2^16..2^26; 0 = the default, 2^25 or twice the points if fewer).
  * Neither changes a result. */
 int tc_corr2_set_tuning(tc_corr2* c, int tile_leaf, int64_t chunk);
 

@@ -508,12 +508,12 @@ void trav_setup(const tc_corr2* c, TravParams& T, int coords, int metric, int qu
 
 // Runs the breadth-first expansion of T to completion (device-side schedule, batches of
 // launches, more level buffers on demand).  *derr: the device error word afterwards.
-// Items per expansion launch: up to 16M, less for small catalogs (level buffers hold 4
-// chunks each: 512 MB per level at the largest size).
+// Items per expansion launch: up to 32M, less for small catalogs (level buffers hold 4
+// chunks each: 1 GB per level at the largest size).
 long long expand_chunk(long long npoints)
 {
     long long CH = 1LL << 16;
-    while (CH < (1LL << 24) && CH < 2 * npoints) CH <<= 1;
+    while (CH < (1LL << 25) && CH < 2 * npoints) CH <<= 1;
     return CH;
 }
 
@@ -522,10 +522,11 @@ int expand_run(tc_corr2* c, const TravParams& T, int blocks, long long npoints, 
 {
     // The schedule lives on the device: batches of (schedule, expand) launches run without
     // host round trips; the host only adds level buffers when the expansion gets deeper.
-    // Chunk size: up to 16M items per launch, less for small catalogs (level buffers hold
-    // 4 chunks each: 512 MB per level at the largest size).  Large launches amortise the
-    // per-launch work of every warp (bin set-up, the flush of its totals, the completion
-    // count); 4M-item chunks took 19% longer on a 10M-point catalog.
+    // Chunk size: up to 32M items per launch, less for small catalogs (level buffers hold
+    // 4 chunks each: 1 GB per level at the largest size).  Large launches amortise the
+    // per-launch work of every warp (bin set-up, the flush of its totals, the fixed-order
+    // join, the launch tail): on a 10M-point catalog at bin_slop 0.1, 4M-item chunks took
+    // 19% longer than 16M, and 32M took 6% less (2197 launches instead of 4328).
     const long long CH = c->chunk > 0 ? c->chunk : expand_chunk(npoints);
     if (!c->sched) TC_TRY(dalloc(&c->sched, 1));
     ExpandSched hs;
@@ -1979,8 +1980,8 @@ int tc_corr2_set_tuning(tc_corr2* c, int tile_leaf, int64_t chunk)
     if (tile_leaf != 0 && (tile_leaf < 8 || tile_leaf > 64)) {
         set_last_error("tile_leaf must be 0 (default) or 8..64"); return TC_ERR_ARG;
     }
-    if (chunk != 0 && (chunk < (1 << 16) || chunk > (1LL << 25))) {
-        set_last_error("chunk must be 0 (default) or 2^16..2^25 work items"); return TC_ERR_ARG;
+    if (chunk != 0 && (chunk < (1 << 16) || chunk > (1LL << 26))) {
+        set_last_error("chunk must be 0 (default) or 2^16..2^26 work items"); return TC_ERR_ARG;
     }
     c->tile_leaf = tile_leaf;
     c->chunk = chunk;
@@ -2006,9 +2007,9 @@ int ilog2(long long n) { int l = 0; while (n > 1) { n >>= 1; ++l; } return l; }
 }  // namespace
 
 // Times the correlation of f1 (and f2) on its first `frac` of top-level pairs for tile leaf
-// sizes 24..64 (exact mode) and then for expansion chunks 2^21..2^24 items (a coordinate
-// search, event-timed device time), keeps the fastest in c and in a per-process cache, and
-// restores the caller's outputs untouched.
+// sizes 24..64 (exact mode) and then for expansion chunks of 1/2, 1/4 and 1/8 of the default
+// (down to 2^21 items): a coordinate search on event-timed device time.  Keeps the fastest
+// in c and in a per-process cache, and leaves the caller's outputs untouched.
 int tc_corr2_autotune(tc_corr2* c, tc_field* f1, tc_field* f2, int metric, double frac,
                       int* tile_leaf_out, int64_t* chunk_out, double* ms_out)
 {
