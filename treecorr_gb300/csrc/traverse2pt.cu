@@ -328,7 +328,10 @@ __device__ __forceinline__ void stage_accumulate(int k, const float (&v)[7],
 // Writes the children to ch (nch of them) and, for an accepted pair, its bin and values.
 // MODE 1 samples the candidate pairs of the learned criterion; MODE 2 marks them (cand),
 // returns their features and prepares both outcomes: the children and, in acc_k / av, the
-// values of accepting the pair into the bin of its separation.
+// values of accepting the pair into the bin of its separation.  MODE 4 is the bin_slop rule
+// of MODE 0 in exact mode: a pair it would split whose cells both hold at most tile_leaf
+// points becomes a leaf-pair tile (tl) instead (a separate instantiation, so that MODE 0
+// carries none of the tile code).
 template <int MODE>
 __device__ __forceinline__ void eval_task(const TravParams& T, bool has, int2 task,
                                           int2 (&ch)[4], int& nch, int2& tl, int& acc_k,
@@ -348,7 +351,7 @@ __device__ __forceinline__ void eval_task(const TravParams& T, bool has, int2 ta
             const float w = A.b.w, s = A.a.w;
             if (w != 0.f && !((double)s <= T.halfminsep)) {
                 int L = __float_as_int(A.c.w), R = __float_as_int(A.d.x);
-                if (MODE == 0 && T.tile_leaf > 0 && __float_as_int(A.c.z) <= T.tile_leaf) {
+                if (MODE == 4 && __float_as_int(A.c.z) <= T.tile_leaf) {
                     tl = make_int2(i, -2 - i);      // every leaf pair of this cell
                 } else if (L < 0 || R < 0) {
                     atomicCAS(T.err, 0, DEV_BAD_CHILD);
@@ -387,7 +390,7 @@ __device__ __forceinline__ void eval_task(const TravParams& T, bool has, int2 ta
                     ++n_acc;
                     acc_k = D.k;
                     accept_values(T, A, B, i, j, dx, dy, dz, dsq, D.r, D.logr, av, acc_nn);
-                } else if (MODE == 0 && D.act != ACT_DROP && T.tile_leaf > 0 &&
+                } else if (MODE == 4 && D.act != ACT_DROP &&
                            __float_as_int(A.c.z) <= T.tile_leaf &&
                            __float_as_int(B.c.z) <= T.tile_leaf) {
                     tl = make_int2(i, j);               // every leaf pair of the two cells
@@ -408,7 +411,7 @@ __device__ __forceinline__ void eval_task(const TravParams& T, bool has, int2 ta
                         if (L2 < 0) atomicCAS(T.err, 0, DEV_BAD_CHILD);
                         else { ch[0] = make_int2(i, L2); ch[1] = make_int2(i, R2); nch = 2; }
                     }
-                    if constexpr (MODE != 0) {
+                    if constexpr (MODE == 1 || MODE == 2) {
                         const float S = s1 + s2, S2 = S * S;
                         if (nch > 0 && rsq >= T.fminsepsq && rsq < T.fmaxsepsq &&
                             S2 <= T.fasq * rsq && S2 <= T.cand_f2 * rsq) {
@@ -685,10 +688,11 @@ __device__ __forceinline__ void add_counters(const TravParams& T, int gw, long l
 
 // End of an expansion warp: the fixed-order mode records the warp's region counts (k_compact
 // commits them and takes the schedule step); otherwise the completion count above.
+template <bool DET>
 __device__ __forceinline__ void expand_finish(const TravParams& T, const ExpandSched* S, int gw,
                                               long long lo_ch, long long lo_tl, int lane)
 {
-    if (T.det) {
+    if constexpr (DET) {
         if (lane == 0) {
             T.det_cnt[gw] = (int)(lo_ch < T.det_ccap ? lo_ch : T.det_ccap);
             T.det_cnt[T.det_nw + gw] = (int)(lo_tl < T.det_tcap ? lo_tl : T.det_tcap);
@@ -701,7 +705,7 @@ __device__ __forceinline__ void expand_finish(const TravParams& T, const ExpandS
 #ifndef EXPAND_MINB
 #define EXPAND_MINB 7   // resident blocks per SM the register budget is sized for (72 registers)
 #endif
-template <int MODE>
+template <int MODE, bool DET = false>
 __global__ void __launch_bounds__(TB, EXPAND_MINB) k_expand(TravParams T, const int2* in, long long n_in,
                                                long long gen0, int2* out,
                                                unsigned long long* nout, long long out_cap,
@@ -809,7 +813,7 @@ __global__ void __launch_bounds__(TB, EXPAND_MINB) k_expand(TravParams T, const 
         }
         const int tot = __shfl_sync(0xffffffffu, off, 31);
         off -= nch;
-        if (tot > 0 && T.det) {
+        if (DET && tot > 0) {
             // Fixed order: the warp's own region, in iteration and lane order.
             if (lo_ch + tot > T.det_ccap) {
                 if (lane == 0) atomicCAS(T.err, 0, DEV_SPILL_OVERFLOW);
@@ -828,11 +832,11 @@ __global__ void __launch_bounds__(TB, EXPAND_MINB) k_expand(TravParams T, const 
                 for (int c = 0; c < nch; ++c) out[o0 + off + c] = ch[c];
             }
         }
-        if (MODE == 0 && T.tile_leaf > 0) {
+        if constexpr (MODE == 4) {
             // Tiles go to the tile list that k_tiles, launched after this kernel, drains.
             const unsigned tm = __ballot_sync(0xffffffffu, tl.x >= 0);
             const int before = __popc(tm & ((1u << lane) - 1u));
-            if (tm && T.det) {
+            if (DET && tm) {
                 if (lo_tl + __popc(tm) > T.det_tcap) {
                     if (lane == 0) atomicCAS(T.err, 0, DEV_SPILL_OVERFLOW);
                 } else if (tl.x >= 0) {
@@ -864,7 +868,7 @@ __global__ void __launch_bounds__(TB, EXPAND_MINB) k_expand(TravParams T, const 
     }
     if (n_acc == 0) {   // nothing accumulated by this warp in this launch
         if (lane == 0 && n_eval) add_counters(T, gw, n_eval, 0, n_esc, 0);
-        expand_finish(T, S, gw, lo_ch, lo_tl, lane);
+        expand_finish<DET>(T, S, gw, lo_ch, lo_tl, lane);
         return;
     }
     if constexpr (MODE == 3) {
@@ -885,7 +889,7 @@ __global__ void __launch_bounds__(TB, EXPAND_MINB) k_expand(TravParams T, const 
     unsigned long long* wn = T.wnp + (size_t)gw * nb;
     for (int q = lane; q < nb; q += 32) wn[q] += (np[q] + np[nb + q]) + (np[2 * nb + q] + np[3 * nb + q]);
     if (lane == 0) add_counters(T, gw, n_eval, n_acc, n_esc, MODE == 2 ? n_learn : 0);
-    expand_finish(T, S, gw, lo_ch, lo_tl, lane);
+    expand_finish<DET>(T, S, gw, lo_ch, lo_tl, lane);
 }
 
 // The schedule step: commits the previous launch's children and picks the next chunk.
@@ -1082,11 +1086,11 @@ static size_t expand_smem_bytes(int nq, int nb, int mode)
     return sm;
 }
 
-template <int MODE>
+template <int MODE, bool DET = false>
 static int set_expand_attr(size_t sm)
 {
     if (sm > 48 * 1024)
-        TC_CU(cudaFuncSetAttribute(k_expand<MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        TC_CU(cudaFuncSetAttribute(k_expand<MODE, DET>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     return 0;
 }
 
@@ -1101,9 +1105,15 @@ int launch_expand_batch(const TravParams& T, int blocks, ExpandSched* dS, int it
     for (int it = 0; it < iters; ++it) {
         if (ev) TC_CU(cudaEventRecord(ev[3 * it], st));
         count_launch();
+        // The fixed-order mode (T.det: modes 0 and 2) and the tiles (mode 0 in exact mode,
+        // run as instantiation 4) are compiled in only where they are used.
         if (T.mode == 3) k_expand<3><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
+        else if (T.mode == 2 && T.det) k_expand<2, true><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
         else if (T.mode == 2) k_expand<2><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
         else if (T.mode == 1) k_expand<1><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
+        else if (T.tile_leaf > 0 && T.det) k_expand<4, true><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
+        else if (T.tile_leaf > 0) k_expand<4><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
+        else if (T.det) k_expand<0, true><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
         else k_expand<0><<<blocks, TB, sm, st>>>(T, nullptr, 0, 0, nullptr, nullptr, 0, dS);
         if (T.det) {
             count_launch();
@@ -1128,12 +1138,18 @@ int expand_grid(int nq, int nb, int* blocks, int* nwarps, int mode)
         TC_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_expand<3>, TB, sm));
     } else if (mode == 2) {
         TC_TRY(set_expand_attr<2>(sm));
+        TC_TRY((set_expand_attr<2, true>(sm)));
         TC_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_expand<2>, TB, sm));
     } else if (mode == 1) {
         TC_TRY(set_expand_attr<1>(sm));
         TC_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_expand<1>, TB, sm));
     } else {
+        // Mode 0 runs as k_expand<0>, or as k_expand<4> when it hands leaf-pair tiles to
+        // k_tiles; both have the same register bound and shared memory.
         TC_TRY(set_expand_attr<0>(sm));
+        TC_TRY((set_expand_attr<0, true>(sm)));
+        TC_TRY(set_expand_attr<4>(sm));
+        TC_TRY((set_expand_attr<4, true>(sm)));
         TC_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_expand<0>, TB, sm));
     }
     if (per < 1) per = 1;
