@@ -113,3 +113,43 @@ def test_exact_tiles_agree_with_traversal(gpu_lib, monkeypatch):
     b = H.gpu_process(T, "G", "Arc", bins, f)
     assert a["_stats"]["tiles"] > 0 and b["_stats"]["tiles"] == 0
     H.assert_outputs_close(a, b, "G", rtol=2e-6, label="tiles vs traversal")
+
+
+@pytest.mark.parametrize("dtype,coords,metric", [("G", "spherical", "Euclidean"),
+                                                 ("G", "3d", "Euclidean"),
+                                                 ("T", "spherical", "Arc")])
+def test_exact_other_geometries_vs_oracle(gpu_lib, dtype, coords, metric):
+    """The tile kernel's other geometry instantiations: sphere with the Euclidean (chord)
+    metric, 3-d GG (the generic projection), spin-3 on the sphere."""
+    T = gpu_lib
+    rng = np.random.default_rng(sum(map(ord, dtype + coords + metric)))
+    if coords == "spherical":
+        cat = sphere_catalog(rng, 25000, radius_deg=3.0)
+        lo, hi = np.radians(1. / 60), np.radians(90. / 60)
+    else:
+        cat, lo, hi = threed_catalog(rng, 20000, L=200.), 1., 40.
+    nb = 14
+    bins = dict(min_sep=lo, max_sep=hi, nbins=nb, bin_size=np.log(hi / lo) / nb, b=0.0, a=0.0)
+    got = _exact_vs_oracle(T, dtype, coords, metric, bins, cat,
+                           label=f"exact {dtype} {coords} {metric}")
+    assert got["_stats"]["tiles"] > 0
+
+
+def test_exact_negative_weights_and_quick(gpu_lib):
+    """Negative weights (cells whose sums stay non-zero) and corr_only (quick: no npairs,
+    meanr or meanlogr) through the tiles."""
+    T = gpu_lib
+    rng = np.random.default_rng(31)
+    cat = flat_catalog(rng, 30000, L=300.)
+    cat["w"] = cat["w"] * np.where(rng.uniform(size=len(cat["w"])) < 0.3, -1., 1.)
+    lo, hi, nb = 1., 50., 12
+    bins = dict(min_sep=lo, max_sep=hi, nbins=nb, bin_size=np.log(hi / lo) / nb, b=0.0, a=0.0)
+    _exact_vs_oracle(T, "G", "flat", "Euclidean", bins, cat, label="exact negative weights")
+    g = H.gpu_field(T, "G", "flat", cat, 0., 0.)
+    o = H.oracle_field("G", "flat", cat, 0., 0.)
+    got = H.gpu_process(T, "G", "Euclidean", bins, g, quick=True)
+    ref = H.oracle_process("G", "Euclidean", bins, o, quick=True)
+    assert not got["npairs"].any() and not got["meanr"].any()
+    for k in ("weight", "xi0", "xi1", "xi2", "xi3"):
+        scale = max(np.abs(ref[k]).max(), 1e-300)
+        assert np.abs(got[k] - ref[k]).max() <= RTOL * scale, k
