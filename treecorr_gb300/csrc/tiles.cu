@@ -711,10 +711,12 @@ __global__ void __launch_bounds__(TPB, TMINB) k_tiles(const __grid_constant__ Tr
                 if (lane == 0) { n_pairs += C.na * C.nbl; n_acc += C.na * C.nbl; }
             } else {
                 // Staging for the shared bins: the A side's arrays of a self tile (unused), or
-                // B's X array of a cross tile (read only by the escalation pass and the
-                // generic products): B's leaves are staged again before an escalation pass.
+                // B's X array of a cross tile when the pair products do not read it (only the
+                // generic projection does: the other class families, and GG in 3-d): B's
+                // leaves are staged again before an escalation pass, which reads their ids.
+                constexpr bool reads_xb = KIND == TK_GEN || (KIND == TK_GG && GEO == TG_3D);
                 float* stg = C.self ? reinterpret_cast<float*>(SA.P)
-                                    : (KIND == TK_GEN ? nullptr : reinterpret_cast<float*>(SB.X));
+                                    : (reads_xb ? nullptr : reinterpret_cast<float*>(SB.X));
                 if (tile_general<GEO, KIND, false>(T, LA, SB, C, lane, acc0, acc1, c0, c1, fb, np,
                                                    n_acc, n_pairs, n_esc, stg)) {
                     if (!C.self && stg) {
