@@ -11,28 +11,34 @@
 //   * both sides' leaves are staged in shared memory as FP32 offsets from cell B's FP64 centre
 //     (hi + lo parts), so a separation is one FP32 difference of offsets whose error is a few
 //     ulps of the tile's extent;
-//   * the tile is classified once from the centres and the leaves' largest offsets: when every
-//     pair certainly lies inside the separation range and inside one bin (margins far above
-//     the FP32 errors), the per-pair range and bin work is skipped; otherwise each pair gets
-//     its range test and bin from log2 of its squared separation over the squared edge of the
-//     tile's lowest bin, with a band that covers every FP32 error -- a pair inside the band is
-//     decided again in FP64 from the FP64 positions with the reference's formulas;
+//   * the tile is classified once from the centres and the cells' sizes: when every pair
+//     certainly lies inside the separation range and inside one bin (margins far above the
+//     FP32 errors), the per-pair range and bin work is skipped (tile_fast); when the pairs lie
+//     in range and on either side of one bin edge, one comparison with that edge decides the
+//     bin (tile_two); otherwise each pair gets its range test and its bin from log2 of its
+//     squared separation over the squared edge of the tile's lowest bin (tile_general).  Both
+//     decisions carry a band that covers every FP32 error; a pair inside the band is decided
+//     again in FP64 from the FP64 positions with the reference's formulas, in a second pass
+//     over the tile, so that the main pair loops have no call and keep their registers;
 //   * lanes take the tile's leaf pairs in order (pair p: leaf p / nB of A, p % nB of B), and
 //     keep running sums for the tile's lowest two bins in registers; pairs in other bins (tiles
-//     that span three or more bins, at separations comparable with the cell sizes) go to the
-//     warp's shared-memory bins directly;
+//     that span three or more bins, at separations comparable with the cell sizes) and the
+//     FP64-decided pairs go to the warp's shared-memory bins in ascending lane order (through
+//     a staging area in leaf arrays the pass does not read, or by shuffles), so every sum is
+//     formed in the same order in every run;
 //   * at the end of a tile the lanes' sums are combined by a reduce-scatter butterfly (one
 //     shuffle per value and step, halving the values each step) and added to the warp's FP32
 //     bins, which go into double-float totals every few tiles and into the warp's FP64 slot
 //     at the end, like the traversal's.
 // The kernel is compiled per geometry (flat, sphere with Arc, sphere or 3-d with Euclidean)
 // and per class family (NN; NK and KK; GG; the others through the generic projection code).
-// Measured on the 10M-point curved-sky catalog (bin_slop 0, angle_slop 0): the pair loops run
-// at ~3.6e11 pairs/s on one-bin tiles, and the per-tile work (staging, bounds, the final
-// butterfly) is the rest; tiles of up to 48 points per side (TILE_LEAF) balance the two (32:
-// 22.5 s, 48: 17.5 s).  A variant that staged the next tile's leaves with bulk copies
-// (cp.async.bulk + mbarrier) while the current one ran was 6% slower: the per-tile cost is
-// instruction issue, not load latency, with 24 warps per SM.
+// Measured on the 10M-point curved-sky catalog (bin_slop 0, angle_slop 0): the single-bin
+// loop runs at ~3.6e11 leaf pairs/s, the two-bin loop at ~2.4e11; tiles of up to 48 points
+// per side (TILE_LEAF; 64 with the autotuner on that catalog) balance the pair loops against
+// the per-tile work (staging, bounds, the final butterfly): 32-point tiles took 22.5 s, 48
+// 17.5 s before the two-pass loops, 15.3 s after.  A variant that staged the next tile's
+// leaves with bulk copies (cp.async.bulk + mbarrier) while the current one ran was 6% slower:
+// the per-tile cost is instruction issue, not load latency, with 24 warps per SM.
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
