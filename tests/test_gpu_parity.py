@@ -248,3 +248,20 @@ def test_mixed_class_arguments(gpu_lib):
         H.gpu_process(T, "NG", "Euclidean", bins, fg, fn)        # kinds swapped
     got = H.gpu_process(T, "NG", "Euclidean", bins, fn, fg)
     H.assert_outputs_close(got, ref, "NG", rtol=RTOL, label="ng after refusals")
+
+
+def test_pinned_host_columns_equal_pageable(gpu_lib):
+    """Page-locked host columns are read by the GPU in place, pageable ones through a staging
+    copy: the same field and the same correlation, bit for bit."""
+    import torch
+    T = gpu_lib
+    s, c1, c2, bins, min_size, max_size, ref = H.load_case("gg_sphere_arc")
+    pinned = {k: (torch.from_numpy(np.ascontiguousarray(v)).pin_memory().numpy()
+                  if v is not None else None) for k, v in c1.items()}
+    fa = H.gpu_field(T, "G", "spherical", c1, min_size, max_size)
+    fb = H.gpu_field(T, "G", "spherical", pinned, min_size, max_size)
+    a = H.gpu_process(T, "G", "Arc", bins, fa)
+    b = H.gpu_process(T, "G", "Arc", bins, fb)
+    for k in H.OUT_KEYS:
+        assert np.array_equal(a[k], b[k]), k
+    H.assert_outputs_close(b, ref, "G", rtol=RTOL, label="pinned columns")

@@ -366,12 +366,28 @@ int field_create_impl(int dkind, int coords, const double* x, const double* y, c
         const double* dsrc[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
         double* staging = nullptr;
         if (!on_device) {
+            // Page-locked host arrays (cudaHostAlloc / cudaHostRegister) are read by the
+            // preparation kernel in place, over the host link; the others are copied to a
+            // device staging buffer first.  Either way the catalog is copied before this call
+            // returns (field_center below waits for the stream), as the reference copies it.
+            bool pinned[7] = {false, false, false, false, false, false, false};
             int cnt = 0;
-            for (int k = 0; k < 7; ++k) if (src[k]) ++cnt;
-            if ((rc = dalloc(&staging, (size_t)cnt * n))) return fail(rc);
-            int slot = 0;
             for (int k = 0; k < 7; ++k) {
                 if (!src[k]) continue;
+                cudaPointerAttributes at;
+                if (cudaPointerGetAttributes(&at, src[k]) == cudaSuccess &&
+                    at.type == cudaMemoryTypeHost && at.devicePointer != nullptr) {
+                    pinned[k] = true;
+                    dsrc[k] = static_cast<const double*>(at.devicePointer);
+                } else {
+                    cudaGetLastError();
+                    ++cnt;
+                }
+            }
+            if (cnt > 0 && (rc = dalloc(&staging, (size_t)cnt * n))) return fail(rc);
+            int slot = 0;
+            for (int k = 0; k < 7; ++k) {
+                if (!src[k] || pinned[k]) continue;
                 double* dst = staging + (size_t)slot * n;
                 if (cudaMemcpyAsync(dst, src[k], n * sizeof(double), cudaMemcpyHostToDevice, st) !=
                     cudaSuccess) {
@@ -392,7 +408,8 @@ int field_create_impl(int dkind, int coords, const double* x, const double* y, c
         BP.split = split_method; BP.brute = f->brute;
         BP.minsizesq = 0.; BP.maxsizesq = 0.; BP.n = (int)n;
         rc = field_center(BP, f->buf[0], f->S, st, f->center);
-        if (staging) { cudaStreamSynchronize(st); dfree(staging); }
+        cudaStreamSynchronize(st);   // the caller's arrays are no longer read after this
+        dfree(staging);
         if (rc) return fail(rc);
         if (cudaGetLastError() != cudaSuccess) {
             set_last_error("field preparation kernel failed");
