@@ -433,6 +433,12 @@ int tc_get_omp_threads(void);
 int tc_set_deterministic(int on);
 int tc_get_deterministic(void);
 
+/* The 2-point expansion's level buffers (about 1 GB each at 10M points) come from the
+ * current device's stream-ordered memory pool, which keeps them after a corr is freed so
+ * that the next corr reuses them without driver calls.  tc_trim_memory returns the pool's
+ * unused memory to the driver (no reference counterpart). */
+int tc_trim_memory(void);
+
 /* Message of the last failure on the calling thread ("" if none). */
 const char* tc_last_error(void);
 

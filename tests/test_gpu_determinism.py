@@ -79,3 +79,20 @@ def test_learned_repeats_bit_identical(det_switch):
     assert a["_stats"]["learned"] > 0
     for k in H.OUT_KEYS:
         assert np.array_equal(a[k], b[k]), k
+
+
+def test_pooled_level_buffers_reused_and_trimmed(det_switch):
+    """Level buffers come from the stream-ordered pool: a second corr after the first is
+    freed gives the same result, and TrimMemory returns the pool's memory."""
+    import torch
+    T = det_switch
+    s, f, ref = _bench_case(T, "gg_cfg2_bs01")
+    a = H.gpu_process(T, "G", s["metric"], s["bins"], f)
+    b = H.gpu_process(T, "G", s["metric"], s["bins"], f)
+    for k in H.OUT_KEYS:
+        assert np.array_equal(a[k], b[k]), k
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    T.TrimMemory()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free1 >= free0

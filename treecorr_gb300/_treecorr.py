@@ -148,6 +148,8 @@ def lib():
         L.tc_set_omp_threads.argtypes = [ctypes.c_int]
         L.tc_get_omp_threads.restype = ctypes.c_int
         L.tc_get_omp_threads.argtypes = []
+        L.tc_trim_memory.restype = ctypes.c_int
+        L.tc_trim_memory.argtypes = []
         L.tc_set_deterministic.restype = ctypes.c_int
         L.tc_set_deterministic.argtypes = [ctypes.c_int]
         L.tc_get_deterministic.restype = ctypes.c_int
@@ -266,6 +268,12 @@ def SetDeterministic(on=True):
     """Fixed-order 2-point expansion (default on): repeated process calls give bit-identical
     sums.  Returns the previous setting.  No reference counterpart."""
     return bool(lib().tc_set_deterministic(1 if on else 0))
+
+
+def TrimMemory():
+    """Returns the cached expansion buffers of freed corrs to the driver.  No reference
+    counterpart."""
+    _check(lib().tc_trim_memory())
 
 
 def GetDeterministic():

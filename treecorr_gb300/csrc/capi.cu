@@ -440,6 +440,40 @@ int expand_scratch(tc_corr2* c, int nwarps, int nq)
     return 0;
 }
 
+// The expansion's level buffers (up to 1 GB each, ~31 of them at 10M points) come from the
+// device's stream-ordered memory pool, which keeps freed memory for the next corr instead of
+// returning it to the driver: a new corr per step then costs no cudaMalloc / cudaFree of
+// tens of GB (freeing them through the driver took 25 ms per 10M-point correlation).
+int pool_alloc_int2(int2** p, size_t count, cudaStream_t st)
+{
+    static bool configured[64] = {false};
+    int dev = 0;
+    TC_CU(cudaGetDevice(&dev));
+    if (dev >= 0 && dev < 64 && !configured[dev]) {
+        cudaMemPool_t pool;
+        TC_CU(cudaDeviceGetDefaultMemPool(&pool, dev));
+        unsigned long long thr = ~0ULL;   // keep freed blocks in the pool
+        TC_CU(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+        configured[dev] = true;
+    }
+    *p = nullptr;
+    const cudaError_t e = cudaMallocAsync((void**)p, std::max<size_t>(count, 1) * sizeof(int2), st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        set_last_error(std::string("cudaMallocAsync of ") + std::to_string(count * sizeof(int2)) +
+                       " bytes failed: " + cudaGetErrorString(e));
+        return TC_ERR_NOMEM;
+    }
+    return 0;
+}
+
+void pool_free(int2*& p, cudaStream_t st)
+{
+    if (p) cudaFreeAsync(p, st);
+    p = nullptr;
+}
+
 // Makes level L's item buffer hold at least `need` items, keeping its first `keep` items.
 int level_reserve(tc_corr2* c, int L, long long keep, long long need, cudaStream_t st)
 {
@@ -447,11 +481,11 @@ int level_reserve(tc_corr2* c, int L, long long keep, long long need, cudaStream
     if (c->levcap[L] >= need) return 0;
     long long cap = std::max(need, 2 * c->levcap[L]);
     int2* p = nullptr;
-    TC_TRY(dalloc(&p, (size_t)cap));
+    TC_TRY(pool_alloc_int2(&p, (size_t)cap, st));
     if (keep > 0)
         TC_CU(cudaMemcpyAsync(p, c->lev[L], sizeof(int2) * (size_t)keep, cudaMemcpyDeviceToDevice, st));
     TC_CU(cudaStreamSynchronize(st));
-    dfree(c->lev[L]);
+    pool_free(c->lev[L], st);
     c->lev[L] = p;
     c->levcap[L] = cap;
     return 0;
@@ -1491,7 +1525,11 @@ void tc_corr2_free(tc_corr2* c)
     if (!c) return;
     dfree(c->wacc); dfree(c->wnp);
     dfree(c->tot); dfree(c->totnp); dfree(c->ctl); dfree(c->idle); dfree(c->d_err);
-    for (auto& p : c->lev) dfree(p);
+    {
+        cudaStream_t st = nullptr;
+        if (stream_get(&st) == 0)
+            for (auto& p : c->lev) pool_free(p, st);
+    }
     dfree(c->sched);
     dfree(c->mlp); dfree(c->samples);
     dfree(c->tiles); dfree(c->tctl); dfree(c->tedge);
@@ -2285,6 +2323,19 @@ int tc_corr3_stats(const tc_corr3* c, int64_t out[3])
 
 int tc_set_omp_threads(int num_threads) { (void)num_threads; return 1; }
 int tc_get_omp_threads(void) { return 1; }
+
+int tc_trim_memory(void)
+{
+    int dev = 0;
+    TC_CU(cudaGetDevice(&dev));
+    cudaStream_t st;
+    TC_TRY(stream_get(&st));
+    TC_CU(cudaStreamSynchronize(st));
+    cudaMemPool_t pool;
+    TC_CU(cudaDeviceGetDefaultMemPool(&pool, dev));
+    TC_CU(cudaMemPoolTrimTo(pool, 0));
+    return TC_OK;
+}
 
 int tc_set_deterministic(int on)
 {
