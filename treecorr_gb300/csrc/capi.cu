@@ -578,7 +578,11 @@ int expand_run(tc_corr2* c, const TravParams& T, int blocks, long long npoints, 
     // per-launch work of every warp (bin set-up, the flush of its totals, the fixed-order
     // join, the launch tail): on a 10M-point catalog at bin_slop 0.1, 4M-item chunks took
     // 19% longer than 16M, and 32M took 6% less (2197 launches instead of 4328).
-    const long long CH = c->chunk > 0 ? c->chunk : expand_chunk(npoints);
+    // The patch batch (mode 3) keeps chunks of at most 16M items: its warps' bins follow the
+    // patch pair they work on, and a larger chunk mixes more pairs into one warp's items
+    // (2.14 s per 150-patch step at 32M, 1.87 s at 16M).
+    long long CH = c->chunk > 0 ? c->chunk : expand_chunk(npoints);
+    if (T.mode == 3 && c->chunk == 0 && CH > (1LL << 24)) CH = 1LL << 24;
     if (!c->sched) TC_TRY(dalloc(&c->sched, 1));
     ExpandSched hs;
     std::memset(&hs, 0, sizeof(hs));
