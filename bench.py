@@ -17,8 +17,14 @@ reference, src/Corr2.cpp:476-525) per second of the whole step.  The GPU path ta
 reference's accept/split decisions, so its count equals the reference's.
 
 value: inputs resident in HBM (device columns), timed with CUDA events on the library's
-stream.  e2e: the same step through the C ABI with host columns (pinned), host->device
-copies and the device->host read of the results inside the timed region.
+stream.  e2e: the same step through the C ABI with host columns (pinned: the preparation
+kernel reads them over the host link), the host->device transfer and the device->host read
+of the results inside the timed region.  point_pairs_per_s counts the same step in point
+pairs in range (sum of npairs), which does not depend on how pairs are grouped into cells.
+
+Before the timed steps each entry runs the library's autotuner (tile leaf size and
+expansion chunk, on 2% of the top-level pairs; reported in `tuning`).  The library's
+default fixed-order expansion is on (bit-identical repeats; --fixed-order 0 turns it off).
 
 The metric's accuracy clause (xi err <= 1e-4 vs FP64): bin_slop 0.1 redistributes the
 shape noise of the pairs it accepts whole, and its xi differs from the all-pairs result by
