@@ -41,3 +41,30 @@ def test_center_size_matches_reference(name):
     got = O.center_size(out["x"], out["y"], out.get("z"))
     np.testing.assert_allclose(got, ref["center_size"], rtol=0,
                                atol=1e-14 * max(1.0, np.abs(ref["center_size"]).max()))
+
+
+def test_wrapper_rejects_bad_columns():
+    """The module's catalog_finish checks its columns before any device work: unknown names
+    and columns of different lengths are ValueErrors."""
+    from treecorr_gb300 import _treecorr as T
+    x = np.arange(5.)
+    with pytest.raises(ValueError, match="unknown column"):
+        T.catalog_finish({"x": x, "y": x, "colour": x})
+    with pytest.raises(ValueError, match="lengths"):
+        T.catalog_finish({"x": x, "y": x[:4]})
+    with pytest.raises(ValueError, match="length"):
+        T.catalog_finish({"x": x, "y": x}, w=np.ones(4))
+
+
+def test_oracle_flag_and_nan_order():
+    """The reference's order of the steps: a NaN in w on a row that a NaN in x already zeroed
+    is not counted for w; a flagged row's NaN weight is not counted either."""
+    from oracle import catalog_oracle as O
+    x = np.array([0., np.nan, 2., 3.])
+    w = np.array([1., np.nan, np.nan, 1.])
+    flag = np.array([0, 0, 4, 0])
+    cols, gw, _, info = O.finish_input({"x": x, "y": np.zeros(4)}, w=w, flag=flag,
+                                       keep_zero_weight=True)
+    assert info["nan_counts"]["x"] == 1 and info["nan_counts"]["w"] == 0
+    np.testing.assert_array_equal(gw, [1., 0., 0., 1.])
+    assert info["sumw"] == 2.0 and info["nobj"] == 2
