@@ -348,8 +348,8 @@ def run_gpu(args, rank, world):
                                f"bin_slop {args.bin_slop}, angle_slop 0.1",
                    "n": args.n, "nbins": nb, "bin_slop": args.bin_slop,
                    "parallelism": f"replicas{world}",
-                   "fixed_order": bool(args.fixed_order),
                    "l2": "inputs larger than L2 (480 MB columns + 1.3 GB tree); no flush"},
+        "fixed_order": bool(args.fixed_order),
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": ms_e2e / args.steps},
         "gpu_launches": launches,
@@ -1290,9 +1290,13 @@ def run_reference(args, rank, world):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded curved-sky GRF catalog)", "impl": "reference",
+            # The same configuration object as the GPU arm's line (the same catalog and
+            # correlation; the l2 note describes the inputs' size).
             "config": {"workload": "GG auto, 10M-point 1000 deg^2 cap, Arc, 30 Log bins "
                                    f"1-300', bin_slop {args.bin_slop}, angle_slop 0.1",
-                       "n": args.n, "nbins": 30, "bin_slop": args.bin_slop},
+                       "n": args.n, "nbins": 30, "bin_slop": args.bin_slop,
+                       "parallelism": f"replicas{world}",
+                       "l2": "inputs larger than L2 (480 MB columns + 1.3 GB tree); no flush"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
                              "sample": f"top-level rows 0..{rows} of {ntop} per step "
                                        "(tree build excluded)"},
