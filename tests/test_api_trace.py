@@ -59,3 +59,27 @@ def test_jackknife_restatement_matches_reference_python():
     w = res[:, 0].sum(axis=0)
     np.testing.assert_allclose(A.finalize_xi(res[:, 3].sum(axis=0), w), tr.final["xip"],
                                rtol=1e-10, atol=1e-14)
+
+
+def _ggg_sas_inputs(tr):
+    call = [e for e in tr.events if e["op"] == "call" and e["method"] == "processAuto"][-1]
+    new = [e for e in tr.events if e["op"] == "new" and e["cls"] == "GGGCorr"][0]
+    nbins, min_sep, bin_size, max_n = new["args"][3], new["args"][1], new["args"][4], new["args"][9]
+    return call, nbins, max_n, min_sep, bin_size
+
+
+def test_tosas_restatement_matches_reference_python():
+    """The oracle's restatement of the multipole finalisation and toSAS
+    (treecorr/corr3base.py:2312-2396, 2489-2676), applied to the reference module's logged
+    GGG outputs, gives the LogSAS result TreeCorr's own Python computed."""
+    from oracle import tosas_oracle as O
+    tr = A.Trace("ggg_mp")
+    call, nbins, max_n, min_sep, bin_size = _ggg_sas_inputs(tr)
+    outs = [tr.arr(r) for r in call["outs"]]
+    w, gams = O.ggg_multipole_to_sas(outs, nbins, max_n, min_sep, bin_size,
+                                     tr.final["sas_phi"])
+    ref_w = tr.final["sas_weight"]
+    assert np.abs(w - ref_w).max() <= 1e-12 * np.abs(ref_w).max()
+    for k in range(4):
+        ref = tr.final["sas_gam%d" % k]
+        assert np.abs(gams[k] - ref).max() <= 1e-10 * np.abs(ref).max(), k
