@@ -223,8 +223,10 @@ int tc_corr2_process_auto_noalloc(tc_corr2* c, tc_field* f, int quick, int metri
 /* Tuning of the 2-point path (no reference counterpart: the reference's OpenMP loop has no
  * such knobs).  tile_leaf: the most points per side of a leaf-pair tile of the exact mode
  * (8..64; 0 = the default 48); chunk: work items per expansion launch, the depth of the
- * breadth-first queue (2^16..2^26; 0 = the default, 2^25 or twice the points if fewer).
- * Neither changes a result. */
+ * breadth-first queue (2^16..2^26; 0 = the default: the smallest power of two at least
+ * twice the points, between 2^16 and 2^25; 2^24 at most for the patch batch).  Neither
+ * changes which pairs land in which bins; the sums agree to FP32 rounding (bit for bit
+ * between runs with equal settings). */
 int tc_corr2_set_tuning(tc_corr2* c, int tile_leaf, int64_t chunk);
 
 /* The autotuner: times this correlation of f1 (and f2, NULL for an auto-correlation) on its
